@@ -1,0 +1,138 @@
+/*
+ * pdq.h -- C ABI of the GB300 probabilistic-IVP hot path.
+ *
+ * The reference (pnkraemer/probdiffeq) is pure JAX and has no FFI; its
+ * "operator API" is the set of Python constructors and the ivpsolve entry
+ * points.  Each function below replaces one of those entry points for a
+ * batch of independent IVP instances (the reference's jax.vmap over a solve):
+ *
+ *   pdq_solve_adaptive  <- ivpsolve.solve_adaptive_save_at / solve_adaptive_terminal_values
+ *                          (probdiffeq/_ivpsolve/solvers_via_adaptive_steps.py:16-148)
+ *                          with the solver, strategy, constraint, error estimator
+ *                          and controller chosen in pdq_config
+ *                          (probdiffeq/_probdiffeq/solvers.py:318-767, 850-996;
+ *                           probdiffeq/_ivpsolve/controllers.py:24-84)
+ *
+ * Conventions:
+ *   - every pointer in the argument structs is a DEVICE pointer unless
+ *     stated otherwise; the caller owns all buffers;
+ *   - float64 in and out; the arithmetic precision is pdq_config.precision;
+ *   - launches are asynchronous on the given stream; no allocation, no
+ *     synchronisation inside the calls;
+ *   - configuration errors return a non-zero pdq_status before any launch;
+ *     run-time failures are reported per instance in the status array
+ *     (never a trap).
+ */
+#ifndef PDQ_H_
+#define PDQ_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PDQ_ABI_VERSION 1u
+
+typedef enum pdq_status {
+  PDQ_SUCCESS = 0,
+  PDQ_ERROR_INVALID_VALUE = 1,
+  PDQ_ERROR_UNSUPPORTED = 2,
+  PDQ_ERROR_CUDA = 3,
+  PDQ_ERROR_WORKSPACE = 4,
+  PDQ_ERROR_ABI_VERSION = 5
+} pdq_status;
+
+/* State-space factorisation (probdiffeq/_probdiffeq/ssm_impl_*.py). */
+enum { PDQ_SSM_ISOTROPIC = 0, PDQ_SSM_BLOCKDIAG = 1, PDQ_SSM_DENSE = 2 };
+/* Linearisation: constraint_ode_ts0 / constraint_ode_ts1 (ssm_impl_api.py:520-558). */
+enum { PDQ_CONSTRAINT_TS0 = 0, PDQ_CONSTRAINT_TS1 = 1 };
+/* strategy_filter / strategy_smoother_fixedpoint (estimators_and_losses.py:347-591). */
+enum { PDQ_STRATEGY_FILTER = 0, PDQ_STRATEGY_FIXEDPOINT = 1 };
+/* solver / solver_mle / solver_dynamic (solvers.py:318-767). */
+enum { PDQ_SOLVER_PLAIN = 0, PDQ_SOLVER_MLE = 1, PDQ_SOLVER_DYNAMIC = 2 };
+/* error_residual_std (solvers.py:850-996). */
+enum { PDQ_ERROR_RESIDUAL_STD = 0 };
+/* control_integral / control_proportional_integral (controllers.py:24-84). */
+enum { PDQ_CONTROL_INTEGRAL = 0, PDQ_CONTROL_PROPORTIONAL_INTEGRAL = 1 };
+/* Bulk arithmetic precision; time, calibration and error-norm sums are float64 always. */
+enum { PDQ_PRECISION_F32 = 0, PDQ_PRECISION_F64 = 1 };
+/* Registered device vector fields (autonomous, first order). */
+enum {
+  PDQ_FIELD_LOTKA_VOLTERRA = 0, /* params (a, b, c, d), d = 2 */
+  PDQ_FIELD_VAN_DER_POL = 1,    /* params (mu), d = 2 */
+  PDQ_FIELD_FITZHUGH_NAGUMO = 2,/* params (a, b, c), d = 2 */
+  PDQ_FIELD_BURGERS = 3         /* params (nu), periodic grid, any d */
+};
+
+/* Per-instance run-time status. */
+enum {
+  PDQ_INSTANCE_OK = 0,
+  PDQ_INSTANCE_MAX_STEPS = 1,   /* attempt bound reached before the last checkpoint */
+  PDQ_INSTANCE_DT_UNDERFLOW = 2,/* step size collapsed below 1e-14 * max(1, |t|) */
+  PDQ_INSTANCE_NONFINITE = 3    /* NaN or Inf in the error norm or the state */
+};
+
+typedef struct pdq_config {
+  uint32_t abi_version;   /* must equal PDQ_ABI_VERSION */
+  int32_t ssm;            /* PDQ_SSM_* */
+  int32_t constraint;     /* PDQ_CONSTRAINT_* */
+  int32_t strategy;       /* PDQ_STRATEGY_* */
+  int32_t solver;         /* PDQ_SOLVER_* */
+  int32_t error;          /* PDQ_ERROR_* */
+  int32_t control;        /* PDQ_CONTROL_* */
+  int32_t precision;      /* PDQ_PRECISION_* */
+  int32_t field;          /* PDQ_FIELD_* */
+  int32_t num_derivatives;/* nu; the state holds nu + 1 Taylor coefficients */
+  int32_t ode_dim;        /* d */
+  int32_t clip_dt;        /* RejectionLoop clip_dt (solvers_via_adaptive_steps.py:300-301) */
+  int32_t correct_asymptotic_underconfidence; /* solver_mle (solvers.py:456-457) */
+  int32_t reserved0;
+  double safety, factor_min, factor_max;           /* controller (defaults 0.95, 0.2, 10) */
+  double exponent_integral, exponent_proportional; /* PI controller (0.3, 0.4) */
+  double atol, rtol, eps, damp;                    /* solve(...) arguments */
+  int64_t max_attempts;   /* bound on step attempts per instance (the reference has none) */
+} pdq_config;
+
+typedef struct pdq_adaptive_args {
+  int64_t num_instances;  /* B */
+  int32_t num_save_at;    /* S >= 2; save_at[b][0] = t0 */
+  int32_t terminal_only;  /* 1: write only the last checkpoint (solve_adaptive_terminal_values) */
+  const double* save_at;  /* (B, S) checkpoint times, strictly increasing per instance */
+  const double* params;   /* (B, P) vector-field parameters */
+  const double* y0;       /* (B, d) initial values; Taylor-mode derivatives are computed on device */
+  const double* dt0;      /* (B,) initial step */
+  /* outputs; S_out = terminal_only ? 1 : S */
+  double* u_mean;         /* isotropic (B, S_out, n, d); dense (B, S_out, n*d) */
+  double* u_chol;         /* isotropic (B, S_out, n, n); dense (B, S_out, n*d, n*d) */
+  double* output_scale;   /* (B, S_out) */
+  double* t;              /* (B, S_out) time of each output */
+  int32_t* num_steps;     /* (B, S_out) accepted steps up to each output */
+  int32_t* num_attempts;  /* (B,) total attempts (accepted + rejected) */
+  int32_t* status;        /* (B,) PDQ_INSTANCE_* */
+} pdq_adaptive_args;
+
+/* ABI version compiled into the library. */
+uint32_t pdq_abi_version(void);
+
+/* Human-readable name of a status code (static storage). */
+const char* pdq_status_string(pdq_status status);
+
+/* Fill a config with the reference's defaults for the given factorisation:
+ * filter strategy, solver_dynamic, error_residual_std, control_integral,
+ * TS0, float32 bulk, clip_dt 1, eps 1e-8, damp 0, atol = rtol = 1e-6. */
+pdq_status pdq_config_default(pdq_config* config, int32_t ssm, int32_t field, int32_t num_derivatives, int32_t ode_dim);
+
+/* Device scratch the solve needs, in bytes (0 for configurations without scratch). */
+pdq_status pdq_workspace_size(const pdq_config* config, int64_t num_instances, int32_t num_save_at, size_t* bytes);
+
+/* Adaptive solve of B independent instances; see the file header. */
+pdq_status pdq_solve_adaptive(const pdq_config* config, const pdq_adaptive_args* args, void* workspace,
+                              size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PDQ_H_ */

@@ -1,0 +1,199 @@
+"""ctypes binding of the C ABI in ``include/pdq.h``.
+
+This module is the only place that talks to ``libpdq_gb300.so``.  It fails
+loudly when the library is missing: there is no CPU fallback.
+"""
+
+import ctypes
+import os
+
+import torch
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libpdq_gb300.so")
+
+ABI_VERSION = 1
+
+# enums (include/pdq.h)
+SSM = {"isotropic": 0, "blockdiag": 1, "dense": 2}
+CONSTRAINT = {"ts0": 0, "ts1": 1}
+STRATEGY = {"filter": 0, "fixedpoint": 1}
+SOLVER = {"none": 0, "mle": 1, "dynamic": 2}
+ERROR = {"residual_std": 0}
+CONTROL = {"integral": 0, "proportional_integral": 1}
+PRECISION = {"float32": 0, "float64": 1}
+FIELD = {"lotka_volterra": 0, "van_der_pol": 1, "fitzhugh_nagumo": 2, "burgers": 3}
+INSTANCE_STATUS = {0: "ok", 1: "max_steps", 2: "dt_underflow", 3: "nonfinite"}
+
+
+class PdqConfig(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_uint32),
+        ("ssm", ctypes.c_int32),
+        ("constraint", ctypes.c_int32),
+        ("strategy", ctypes.c_int32),
+        ("solver", ctypes.c_int32),
+        ("error", ctypes.c_int32),
+        ("control", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("field", ctypes.c_int32),
+        ("num_derivatives", ctypes.c_int32),
+        ("ode_dim", ctypes.c_int32),
+        ("clip_dt", ctypes.c_int32),
+        ("correct_asymptotic_underconfidence", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
+        ("safety", ctypes.c_double),
+        ("factor_min", ctypes.c_double),
+        ("factor_max", ctypes.c_double),
+        ("exponent_integral", ctypes.c_double),
+        ("exponent_proportional", ctypes.c_double),
+        ("atol", ctypes.c_double),
+        ("rtol", ctypes.c_double),
+        ("eps", ctypes.c_double),
+        ("damp", ctypes.c_double),
+        ("max_attempts", ctypes.c_int64),
+    ]
+
+
+class PdqAdaptiveArgs(ctypes.Structure):
+    _fields_ = [
+        ("num_instances", ctypes.c_int64),
+        ("num_save_at", ctypes.c_int32),
+        ("terminal_only", ctypes.c_int32),
+        ("save_at", ctypes.c_void_p),
+        ("params", ctypes.c_void_p),
+        ("y0", ctypes.c_void_p),
+        ("dt0", ctypes.c_void_p),
+        ("u_mean", ctypes.c_void_p),
+        ("u_chol", ctypes.c_void_p),
+        ("output_scale", ctypes.c_void_p),
+        ("t", ctypes.c_void_p),
+        ("num_steps", ctypes.c_void_p),
+        ("num_attempts", ctypes.c_void_p),
+        ("status", ctypes.c_void_p),
+    ]
+
+
+# Every symbol include/pdq.h declares, with its ctypes signature.
+SIGNATURES = {
+    "pdq_abi_version": (ctypes.c_uint32, []),
+    "pdq_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "pdq_config_default": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32],
+    ),
+    "pdq_workspace_size": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "pdq_solve_adaptive": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqAdaptiveArgs), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "pdq_probe_fp32_fma": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
+    ),
+    "pdq_probe_sm_count": (ctypes.c_int, []),
+}
+
+_LIB = None
+
+
+class NativeError(RuntimeError):
+    """A non-zero pdq_status returned by the native library."""
+
+    def __init__(self, status, where):
+        self.status = status
+        super().__init__(f"{where}: {status_string(status)} (pdq_status {status})")
+
+
+def load():
+    """Load ``libpdq_gb300.so`` (raises if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"native library {LIB_PATH} is missing; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (no CPU fallback exists)"
+        )
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.pdq_abi_version() != ABI_VERSION:
+        raise RuntimeError("libpdq_gb300.so ABI version mismatch")
+    _LIB = lib
+    return lib
+
+
+def status_string(status):
+    return load().pdq_status_string(int(status)).decode()
+
+
+def check(status, where):
+    if status != 0:
+        raise NativeError(status, where)
+
+
+def config_default(ssm, field, num_derivatives, ode_dim):
+    cfg = PdqConfig()
+    check(load().pdq_config_default(ctypes.byref(cfg), SSM[ssm], FIELD[field], num_derivatives, ode_dim), "pdq_config_default")
+    return cfg
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream_handle(stream):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream=None):
+    """Call pdq_solve_adaptive on device tensors (all float64, contiguous).
+
+    ``outputs`` is a dict of preallocated device tensors (see ``alloc_outputs``).
+    """
+    B = y0.shape[0]
+    args = PdqAdaptiveArgs()
+    args.num_instances = B
+    args.num_save_at = save_at.shape[1]
+    args.terminal_only = 1 if terminal_only else 0
+    args.save_at = _ptr(save_at)
+    args.params = _ptr(params)
+    args.y0 = _ptr(y0)
+    args.dt0 = _ptr(dt0)
+    for k in ("u_mean", "u_chol", "output_scale", "t", "num_steps", "num_attempts", "status"):
+        setattr(args, k, _ptr(outputs[k]))
+    lib = load()
+    ws = ctypes.c_size_t(0)
+    check(lib.pdq_workspace_size(ctypes.byref(cfg), B, save_at.shape[1], ctypes.byref(ws)), "pdq_workspace_size")
+    check(lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), None, 0, _stream_handle(stream)), "pdq_solve_adaptive")
+    return outputs
+
+
+def alloc_outputs(cfg, B, S, terminal_only, device):
+    n = cfg.num_derivatives + 1
+    d = cfg.ode_dim
+    S_out = 1 if terminal_only else S
+    f64 = dict(dtype=torch.float64, device=device)
+    i32 = dict(dtype=torch.int32, device=device)
+    if cfg.ssm == SSM["dense"]:
+        N = n * d
+        mean_shape, chol_shape = (B, S_out, N), (B, S_out, N, N)
+    else:
+        mean_shape, chol_shape = (B, S_out, n, d), (B, S_out, n, n)
+    return {
+        "u_mean": torch.empty(mean_shape, **f64),
+        "u_chol": torch.empty(chol_shape, **f64),
+        "output_scale": torch.empty((B, S_out), **f64),
+        "t": torch.empty((B, S_out), **f64),
+        "num_steps": torch.empty((B, S_out), **i32),
+        "num_attempts": torch.empty((B,), **i32),
+        "status": torch.empty((B,), **i32),
+    }

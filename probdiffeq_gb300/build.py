@@ -1,0 +1,89 @@
+"""Build the native library ``libpdq_gb300.so`` in-tree for sm_103a.
+
+Each ``csrc/*.cu`` translation unit compiles in its own ``nvcc`` process (in
+parallel), then one shared object is linked with the CUDA runtime statically
+linked in.  Outputs: ``probdiffeq_gb300/libpdq_gb300.so`` (object files go to
+``_build/`` at the repository root).
+"""
+
+import concurrent.futures
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(ROOT, "_build")
+LIB = os.path.join(PKG, "libpdq_gb300.so")
+
+GENCODE = "arch=compute_103a,code=sm_103a"
+NVCC_FLAGS = [
+    "-gencode",
+    GENCODE,
+    "-O3",
+    "-lineinfo",
+    "-std=c++17",
+    "-Xcompiler",
+    "-fPIC",
+    "-I" + INCLUDE,
+    "-I" + CSRC,
+]
+
+
+def nvcc_path():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found; the native library cannot be built")
+
+
+def sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def _newest_input_mtime():
+    files = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    files.append(os.path.abspath(__file__))
+    return max(os.path.getmtime(f) for f in files)
+
+
+def is_stale():
+    return not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest_input_mtime()
+
+
+def build(force=False, verbose=False):
+    """Compile every translation unit and link the shared library."""
+    if not force and not is_stale():
+        return LIB
+    nvcc = nvcc_path()
+    os.makedirs(BUILD, exist_ok=True)
+
+    def compile_one(src):
+        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        cmd = [nvcc, *NVCC_FLAGS, "-c", src, "-o", obj]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
+        if verbose:
+            sys.stdout.write(res.stdout + res.stderr)
+        return obj
+
+    srcs = sources()
+    workers = min(len(srcs), max(1, os.cpu_count() or 1))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc, "-gencode", GENCODE, "-shared", "-o", tmp, *objs]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

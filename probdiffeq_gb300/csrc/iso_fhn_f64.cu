@@ -1,0 +1,4 @@
+// Isotropic adaptive kernels for the FitzHughNagumo field in double bulk precision.
+#include "iso_launch.cuh"
+
+PDQ_DEFINE_ISO_LAUNCH(pdq_launch_iso_fhn_f64, double, pdq::FitzHughNagumo)

@@ -1,0 +1,47 @@
+// Template dispatch of the isotropic kernel over (precision, nu, interpolation).
+#pragma once
+
+#include "iso_solver.cuh"
+
+namespace pdq {
+
+template <typename T, int NU, class F>
+cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
+  const unsigned grid = unsigned((a.B + block - 1) / block);
+  if (interp)
+    iso_adaptive_kernel<T, NU, F, true><<<grid, block, 0, stream>>>(a);
+  else
+    iso_adaptive_kernel<T, NU, F, false><<<grid, block, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, class F>
+cudaError_t launch_iso_precision(const IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block) {
+  switch (nu) {
+    case 1: return launch_iso_nu<T, 1, F>(a, interp, stream, block);
+    case 2: return launch_iso_nu<T, 2, F>(a, interp, stream, block);
+    case 3: return launch_iso_nu<T, 3, F>(a, interp, stream, block);
+    case 4: return launch_iso_nu<T, 4, F>(a, interp, stream, block);
+    case 5: return launch_iso_nu<T, 5, F>(a, interp, stream, block);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace pdq
+
+// Per-(field, precision) entry points, each defined in its own translation
+// unit so the instantiations compile in parallel.
+#define PDQ_DECLARE_ISO_LAUNCH(NAME) \
+  cudaError_t NAME(const pdq::IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block);
+
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_lv_f32)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_lv_f64)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_vdp_f32)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_vdp_f64)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fhn_f32)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fhn_f64)
+
+#define PDQ_DEFINE_ISO_LAUNCH(NAME, T, F)                                                       \
+  cudaError_t NAME(const pdq::IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block) { \
+    return pdq::launch_iso_precision<T, F>(a, nu, interp, stream, block);                       \
+  }

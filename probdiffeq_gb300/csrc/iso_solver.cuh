@@ -1,0 +1,449 @@
+// Isotropic TS0 adaptive solver: one thread per IVP instance.
+//
+// Follows, per attempt, the reference's isotropic path:
+//   IsotropicWienerIntegrated.transition   (_probdiffeq/ssm_impl_isotropic.py:367-378)
+//   IsotropicLatentCond.marginalise        (ssm_impl_isotropic.py:81-89)
+//   IsotropicOdeTs0.linearize              (ssm_impl_isotropic.py:304-317)
+//   IsotropicLatentCond.revert             (ssm_impl_isotropic.py:107-133)
+//   revert_conditional / sum_of_sqrtm      (util/cholesky_util.py:27-95)
+//   solver / solver_mle / solver_dynamic   (_probdiffeq/solvers.py:395-437, 549-599, 702-733)
+//   error_residual_std                     (solvers.py:925-996)
+//   control_integral / PI                  (_ivpsolve/controllers.py:24-84)
+//   RejectionLoop + save_at checkpoints    (_ivpsolve/solvers_via_adaptive_steps.py:46-375)
+// with the filter strategy (_probdiffeq/estimators_and_losses.py:347-421).
+//
+// Layout: the whole per-instance state (mean (n, d), lower Cholesky (n, n),
+// time, step, controller and calibration accumulators) lives in registers for
+// the entire solve; global memory is touched only to read the instance's
+// inputs once and to write one record per checkpoint.
+//
+// Precision: T (float or double) for the bulk arithmetic; time, step size,
+// the MLE sum of squares and the error-norm sum are always double.
+#pragma once
+
+#include "pdq_device.cuh"
+
+namespace pdq {
+
+constexpr int kMaxN = 8;
+
+struct IsoArgs {
+  int64_t B;
+  int32_t S, terminal_only, solver, control, clip_dt, correct;
+  double safety, factor_min, factor_max, exp_i, exp_p;
+  double atol, rtol, eps, damp;
+  int64_t max_attempts;
+  double q1[kMaxN][kMaxN];  // lower square root of flip(Hilbert) (utilities.py:57-71)
+  const double* save_at;
+  const double* params;
+  const double* y0;
+  const double* dt0;
+  double* u_mean;
+  double* u_chol;
+  double* output_scale;
+  double* t_out;
+  int32_t* num_steps;
+  int32_t* num_attempts;
+  int32_t* status;
+};
+
+// Preconditioner p_i = h^(NU-i)/(NU-i)!, p_inv_i = 1/p_i (utilities.py:74-84).
+template <typename T, int NU>
+PDQ_D void precon(T h, T (&p)[NU + 1], T (&pinv)[NU + 1]) {
+  const T hinv = T(1) / h;
+  p[NU] = T(1);
+  pinv[NU] = T(1);
+#pragma unroll
+  for (int i = NU - 1; i >= 0; --i) {
+    p[i] = p[i + 1] * h / T(NU - i);
+    pinv[i] = pinv[i + 1] * hinv * T(NU - i);
+  }
+}
+
+// IWP predict of the isotropic mean (marginalise, ssm_impl_isotropic.py:81-89):
+//   mp = p * A (pinv * m)
+template <typename T, int NU, int D>
+PDQ_D void iso_predict_mean(const T (&m)[NU + 1][D], const T (&p)[NU + 1], const T (&pinv)[NU + 1],
+                            T (&mp)[NU + 1][D]) {
+  constexpr int n = NU + 1;
+  T x[n][D];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) x[i][j] = pinv[i] * m[i][j];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = i; k < n; ++k) acc += T(iwp_a<NU>(i, k)) * x[k][j];
+      mp[i][j] = p[i] * acc;
+    }
+}
+
+// IWP predict of the isotropic Cholesky factor (marginalise, ssm_impl_isotropic.py:81-89):
+//   Lp = |p| * qr_r([ (A (pinv * L))^T ; (s sqrt|h| Q1)^T ])^T
+// The stacked matrix is 2n x n with an upper-triangular bottom block, so the
+// Householder reflector of column c only touches rows c..n-1 of the top block
+// and rows 0..c of the bottom block (n + 1 entries).
+template <typename T, int NU>
+PDQ_D void iso_predict_chol(const IsoArgs& a, const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
+                            const T (&pinv)[NU + 1], T scale_q, T (&Lp)[NU + 1][NU + 1]) {
+  constexpr int n = NU + 1;
+  // top block X = (A pinv L)^T: X[r][c] = sum_k A[c][k] pinv[k] L[k][r]
+  T X[n][n];
+  T U[n][n];  // bottom block (s sqrt|h| Q1)^T, upper triangular
+#pragma unroll
+  for (int c = 0; c < n; ++c)
+#pragma unroll
+    for (int r = 0; r < n; ++r) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = (c > r ? c : r); k < n; ++k) acc += T(iwp_a<NU>(c, k)) * pinv[k] * L[k][r];
+      X[r][c] = acc;
+      U[r][c] = (r <= c) ? scale_q * T(a.q1[c][r]) : T(0);
+    }
+  // structured Householder QR
+#pragma unroll
+  for (int c = 0; c < n; ++c) {
+    T nrm2 = T(0);
+#pragma unroll
+    for (int r = c; r < n; ++r) nrm2 += X[r][c] * X[r][c];
+#pragma unroll
+    for (int i = 0; i <= c; ++i) nrm2 += U[i][c] * U[i][c];
+    const T alpha = X[c][c];
+    if (nrm2 > T(0)) {
+      const T nrm = dev_sqrt(nrm2);
+      const T beta = alpha >= T(0) ? -nrm : nrm;
+      const T v0 = alpha - beta;
+      const T tau = (beta - alpha) / beta;
+      const T vinv = T(1) / v0;
+      // normalised reflector v = [1, X[c+1..][c]/v0, U[0..c][c]/v0]
+#pragma unroll
+      for (int r = c + 1; r < n; ++r) X[r][c] *= vinv;
+#pragma unroll
+      for (int i = 0; i <= c; ++i) U[i][c] *= vinv;
+#pragma unroll
+      for (int j = c + 1; j < n; ++j) {
+        T w = X[c][j];
+#pragma unroll
+        for (int r = c + 1; r < n; ++r) w += X[r][c] * X[r][j];
+#pragma unroll
+        for (int i = 0; i <= c; ++i) w += U[i][c] * U[i][j];
+        w *= tau;
+        X[c][j] -= w;
+#pragma unroll
+        for (int r = c + 1; r < n; ++r) X[r][j] -= w * X[r][c];
+#pragma unroll
+        for (int i = 0; i <= c; ++i) U[i][j] -= w * U[i][c];
+      }
+      X[c][c] = beta;
+    }
+  }
+  // Lp = |p| * R^T (lower triangular)
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) Lp[i][j] = (j <= i) ? dev_abs(p[i]) * X[j][i] : T(0);
+}
+
+template <typename T, int NU, int D>
+PDQ_D void iso_predict(const IsoArgs& a, const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1],
+                       const T (&p)[NU + 1], const T (&pinv)[NU + 1], T scale_q, T (&mp)[NU + 1][D],
+                       T (&Lp)[NU + 1][NU + 1]) {
+  iso_predict_mean<T, NU, D>(m, p, pinv, mp);
+  iso_predict_chol<T, NU>(a, L, p, pinv, scale_q, Lp);
+}
+
+template <typename T, int NU, int D>
+PDQ_D void write_record(const IsoArgs& a, int64_t b, int s_out, int S_out, const T (&m)[NU + 1][D],
+                        const T (&L)[NU + 1][NU + 1], double scale, double t, int steps) {
+  constexpr int n = NU + 1;
+  const int64_t rec = b * S_out + s_out;
+  double* um = a.u_mean + rec * (n * D);
+  double* uc = a.u_chol + rec * (n * n);
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) um[i * D + j] = double(m[i][j]);
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) uc[i * n + j] = double(L[i][j]);
+  a.output_scale[rec] = scale;
+  a.t_out[rec] = t;
+  a.num_steps[rec] = steps;
+}
+
+// One adaptive solve per thread.  INTERP: keep the interpolation state
+// (needed unless clip_dt makes every checkpoint an exact landing).
+template <typename T, int NU, class F, bool INTERP>
+__global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
+  constexpr int n = NU + 1;
+  constexpr int D = F::D;
+  constexpr int P = F::P;
+  constexpr int OUT = 1;  // ODE u' = f(u): observe coefficient 1 (problems.py:283-295)
+  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= a.B) return;
+
+  const int S = a.S;
+  const int S_out = a.terminal_only ? 1 : S;
+  const double* save_at = a.save_at + b * S;
+
+  // ---- inputs and Taylor-mode initial derivatives (float64) ----
+  double pd[P];
+#pragma unroll
+  for (int k = 0; k < P; ++k) pd[k] = a.params[b * P + k];
+  T pt[P];
+#pragma unroll
+  for (int k = 0; k < P; ++k) pt[k] = T(pd[k]);
+  double y0[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) y0[j] = a.y0[b * D + j];
+  double tc[n][D];
+  taylor_init<F, NU>(y0, pd, tc);
+
+  T m[n][D], L[n][n];
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) m[i][j] = T(tc[i][j]);
+#pragma unroll
+    for (int j = 0; j < n; ++j) L[i][j] = T(0);
+  }
+  // interpolation state (interp_from); dead code when INTERP is false
+  T mi[n][D], Li[n][n];
+  double ti = save_at[0];
+  if constexpr (INTERP) {
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
+#pragma unroll
+      for (int j = 0; j < n; ++j) Li[i][j] = T(0);
+    }
+  }
+
+  double t = save_at[0];
+  double dt = a.dt0[b];
+  double pi_prev = 1.0;  // PI controller state (controllers.py:41-43)
+  double mle_sumsq = 0.0;
+  int num_data = 0, num_steps = 0, attempts = 0, status = PDQ_INSTANCE_OK;
+  T sigma_sf = T(1);  // output scale of step_from (dynamic solver)
+  const T damp = T(a.damp);
+
+  // ||Q1 row OUT||^2 enters the observed std of the linearised residual
+  T q1_out2 = T(0);
+#pragma unroll
+  for (int j = 0; j < n; ++j) q1_out2 += T(a.q1[OUT][j]) * T(a.q1[OUT][j]);
+
+  if (!a.terminal_only) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, t, 0);
+
+  for (int s = 1; s < S && status == PDQ_INSTANCE_OK; ++s) {
+    const double t_next = save_at[s];
+    bool cont = true;
+    while (cont && status == PDQ_INSTANCE_OK) {
+      if (t + a.eps < t_next) {
+        // ---- rejection loop (solvers_via_adaptive_steps.py:249-328) ----
+        bool accepted = false;
+        while (!accepted) {
+          const double dt_use = a.clip_dt ? fmin(dt, t_next - t) : dt;
+          if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
+            status = PDQ_INSTANCE_DT_UNDERFLOW;
+            break;
+          }
+          if (attempts >= a.max_attempts) {
+            status = PDQ_INSTANCE_MAX_STEPS;
+            break;
+          }
+          ++attempts;
+          const T h = T(dt_use);
+          T p[n], pinv[n];
+          precon<T, NU>(h, p, pinv);
+
+          // extrapolated mean: the same for every calibration mode, and the
+          // error estimate's apply_flat(previous mean) (solvers.py:943-944)
+          T mp[n][D];
+          iso_predict_mean<T, NU, D>(m, p, pinv, mp);
+          // TS0 linearisation at the extrapolated mean (ssm_impl_isotropic.py:304-317)
+          T f[D];
+          F::eval(mp[0], pt, f);
+          T mobs[D];
+          T mobs2 = T(0);
+#pragma unroll
+          for (int j = 0; j < D; ++j) {
+            mobs[j] = mp[OUT][j] - f[j];
+            mobs2 += mobs[j] * mobs[j];
+          }
+          const T rms_mobs = dev_sqrt(mobs2 / T(D));
+          // fx.marginalise(apply_flat(m)) with unit scale: observed std
+          // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
+          // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
+          const T ell = dev_sqrt(p[OUT] * p[OUT] * dev_abs(h) * q1_out2 + damp * damp);
+          const T sigma_loc = rms_mobs / ell;
+
+          const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
+          T Lp[n][n];
+          iso_predict_chol<T, NU>(a, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
+
+          // ---- update: revert_conditional with H = e_OUT, a Givens chain
+          //      on [[damp, 0], [(H Lp)^T, Lp^T]] (util/cholesky_util.py:27-82) ----
+          T M[n + 1][n + 1];
+#pragma unroll
+          for (int c = 0; c <= n; ++c) M[0][c] = (c == 0) ? damp : T(0);
+#pragma unroll
+          for (int r = 1; r <= n; ++r) {
+            M[r][0] = Lp[OUT][r - 1];
+#pragma unroll
+            for (int c = 1; c <= n; ++c) M[r][c] = (c >= r) ? Lp[c - 1][r - 1] : T(0);
+          }
+#pragma unroll
+          for (int r = OUT + 1; r >= 1; --r) givens_rows<T, n + 1, n + 1>(M, r - 1, r, 0);
+#pragma unroll
+          for (int c = 1; c <= OUT; ++c) givens_rows<T, n + 1, n + 1>(M, c, c + 1, c);
+
+          const T R_Y = M[0][0];
+          const T ry_inv = T(1) / R_Y;
+          T mnew[n][D], Lnew[n][n];
+#pragma unroll
+          for (int i = 0; i < n; ++i) {
+            const T g = M[0][i + 1] * ry_inv;  // gain G = R12^T / R_Y
+#pragma unroll
+            for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - g * mobs[j];
+#pragma unroll
+            for (int j = 0; j < n; ++j) Lnew[i][j] = (j <= i) ? M[j + 1][i + 1] : T(0);
+          }
+
+          // ---- error estimate (error_residual_std, solvers.py:925-996) ----
+          const T err_abs = dev_abs(sigma_loc) * ell * h;  // std of rescaled observed * dt^1/1!
+          double sumsq = 0.0;
+#pragma unroll
+          for (int j = 0; j < D; ++j) {
+            const T ref = fmax(dev_abs(m[0][j]), dev_abs(mnew[0][j]));
+            const T ratio = err_abs / (T(a.atol) + T(a.rtol) * ref);
+            sumsq += double(ratio) * double(ratio);
+          }
+          const double norm2 = sumsq / D;
+          if (!(norm2 == norm2) || isinf(norm2)) {
+            status = PDQ_INSTANCE_NONFINITE;
+            break;
+          }
+          const T ep = dev_pow(T(norm2), T(-0.5) / T(n));  // error_norm^(-1/n)
+
+          // ---- controller (controllers.py:24-84) ----
+          double factor;
+          if (a.control == PDQ_CONTROL_INTEGRAL) {
+            factor = a.safety * double(ep);
+          } else {
+            const double gi = double(dev_pow(ep, T(a.exp_i)));
+            const double gp = double(dev_pow(T(double(ep) / pi_prev), T(a.exp_p)));
+            factor = a.safety * gi * gp;
+            if (double(ep) >= 1.0) pi_prev = double(ep);
+          }
+          factor = fmax(a.factor_min, fmin(factor, a.factor_max));
+          dt = factor * dt_use;
+          accepted = double(ep) >= 1.0;
+          if (accepted) {
+            if constexpr (INTERP) {
+              ti = t;
+#pragma unroll
+              for (int i = 0; i < n; ++i) {
+#pragma unroll
+                for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
+#pragma unroll
+                for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
+              }
+            }
+            t = t + dt_use;
+            ++num_steps;
+#pragma unroll
+            for (int i = 0; i < n; ++i) {
+#pragma unroll
+              for (int j = 0; j < D; ++j) m[i][j] = mnew[i][j];
+#pragma unroll
+              for (int j = 0; j < n; ++j) L[i][j] = Lnew[i][j];
+            }
+            if (a.solver == PDQ_SOLVER_MLE) {
+              // running scale via hypot recurrence == RMS of new terms (solvers.py:421-424)
+              const T new_term = rms_mobs / dev_abs(R_Y);
+              mle_sumsq += double(new_term) * double(new_term);
+              ++num_data;
+            }
+            sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
+          }
+        }
+      }
+      if (status != PDQ_INSTANCE_OK) break;
+      // ---- checkpoint branch (solvers_via_adaptive_steps.py:242-247) ----
+      const int s_out = a.terminal_only ? 0 : s;
+      const bool record = (!a.terminal_only) || (s == S - 1);
+      if (t + a.eps < t_next) {
+        // interp_skip: keep stepping towards the checkpoint
+      } else if (INTERP && t > t_next + a.eps) {
+        if constexpr (INTERP) {
+          // interp_beyond_t1: predict from interp_from to t_next
+          // (solvers.py:205-269, estimators_and_losses.py:403-414)
+          const T h = T(t_next - ti);
+          T p[n], pinv[n], mp[n][D], Lp[n][n];
+          precon<T, NU>(h, p, pinv);
+          iso_predict<T, NU, D>(a, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
+          if (record) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), t_next, num_steps);
+          ti = t_next;
+#pragma unroll
+          for (int i = 0; i < n; ++i) {
+#pragma unroll
+            for (int j = 0; j < D; ++j) mi[i][j] = mp[i][j];
+#pragma unroll
+            for (int j = 0; j < n; ++j) Li[i][j] = Lp[i][j];
+          }
+        }
+      } else {
+        // interp_at_t1: the state itself is the solution (estimators_and_losses.py:416-421)
+        if (record) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), t, num_steps);
+        if constexpr (INTERP) {
+          ti = t;
+#pragma unroll
+          for (int i = 0; i < n; ++i) {
+#pragma unroll
+            for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
+#pragma unroll
+            for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
+          }
+        }
+      }
+      cont = t + a.eps < t_next;
+    }
+  }
+
+  // ---- finalize: calibrated output scale (solvers.py:439-480, 601-633, 735-767) ----
+  if (status == PDQ_INSTANCE_OK) {
+    if (a.solver == PDQ_SOLVER_MLE) {
+      double scale = num_data > 0 ? sqrt(mle_sumsq / num_data) : 0.0;
+      if (a.correct) {
+        const int last = a.num_steps[b * S_out + (S_out - 1)];
+        scale = scale / sqrt(double(last));
+      }
+      for (int s = 0; s < S_out; ++s) {
+        const int64_t rec = b * S_out + s;
+        double* uc = a.u_chol + rec * (n * n);
+        for (int k = 0; k < n * n; ++k) uc[k] *= scale;
+        a.output_scale[rec] = scale;
+      }
+    }
+  } else {
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    for (int s = 0; s < S_out; ++s) {
+      const int64_t rec = b * S_out + s;
+      for (int k = 0; k < n * D; ++k) a.u_mean[rec * (n * D) + k] = nan;
+      for (int k = 0; k < n * n; ++k) a.u_chol[rec * (n * n) + k] = nan;
+      a.output_scale[rec] = nan;
+      a.t_out[rec] = nan;
+      a.num_steps[rec] = num_steps;
+    }
+  }
+  a.num_attempts[b] = attempts;
+  a.status[b] = status;
+}
+
+}  // namespace pdq

@@ -1,0 +1,191 @@
+// Host side of the C ABI declared in include/pdq.h: validation, constants of
+// the IWP prior, and dispatch to the solver kernels.
+#include <math.h>
+#include <string.h>
+
+#include "iso_launch.cuh"
+#include "pdq.h"
+
+namespace {
+
+// Lower square root (non-negative diagonal) of flip(Hilbert(n)):
+// (Q Q^T)[i][j] = 1 / (2 nu + 1 - i - j).  This is the Q_1d of
+// system_matrices_1d_iwp (_probdiffeq/utilities.py:57-71); the Cholesky
+// factor is unique, computed here in long double.
+void iwp_q1(int nu, double (&q)[pdq::kMaxN][pdq::kMaxN]) {
+  const int n = nu + 1;
+  long double c[pdq::kMaxN][pdq::kMaxN] = {};
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j <= i; ++j) {
+      long double s = 1.0L / (long double)(2 * nu + 1 - i - j);
+      for (int k = 0; k < j; ++k) s -= c[i][k] * c[j][k];
+      if (i == j)
+        c[i][j] = sqrtl(s > 0 ? s : 0);
+      else
+        c[i][j] = c[j][j] > 0 ? s / c[j][j] : 0;
+    }
+  }
+  for (int i = 0; i < pdq::kMaxN; ++i)
+    for (int j = 0; j < pdq::kMaxN; ++j) q[i][j] = (i < n && j <= i) ? (double)c[i][j] : 0.0;
+}
+
+int field_dim(int field) {
+  switch (field) {
+    case PDQ_FIELD_LOTKA_VOLTERRA:
+    case PDQ_FIELD_VAN_DER_POL:
+    case PDQ_FIELD_FITZHUGH_NAGUMO:
+      return 2;
+    case PDQ_FIELD_BURGERS:
+      return -1;  // any
+    default:
+      return 0;
+  }
+}
+
+pdq_status validate_common(const pdq_config* c) {
+  if (c == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  if (c->abi_version != PDQ_ABI_VERSION) return PDQ_ERROR_ABI_VERSION;
+  if (c->num_derivatives < 1 || c->num_derivatives > 5) return PDQ_ERROR_UNSUPPORTED;
+  const int d = field_dim(c->field);
+  if (d == 0) return PDQ_ERROR_INVALID_VALUE;
+  if (d > 0 && c->ode_dim != d) return PDQ_ERROR_INVALID_VALUE;
+  if (c->precision != PDQ_PRECISION_F32 && c->precision != PDQ_PRECISION_F64) return PDQ_ERROR_INVALID_VALUE;
+  if (c->solver < PDQ_SOLVER_PLAIN || c->solver > PDQ_SOLVER_DYNAMIC) return PDQ_ERROR_INVALID_VALUE;
+  if (c->control != PDQ_CONTROL_INTEGRAL && c->control != PDQ_CONTROL_PROPORTIONAL_INTEGRAL)
+    return PDQ_ERROR_INVALID_VALUE;
+  if (c->error != PDQ_ERROR_RESIDUAL_STD) return PDQ_ERROR_UNSUPPORTED;
+  if (!(c->atol >= 0) || !(c->rtol >= 0) || !(c->atol + c->rtol > 0)) return PDQ_ERROR_INVALID_VALUE;
+  if (!(c->eps >= 0) || !(c->damp >= 0)) return PDQ_ERROR_INVALID_VALUE;
+  if (!(c->factor_min > 0) || !(c->factor_max >= c->factor_min) || !(c->safety > 0)) return PDQ_ERROR_INVALID_VALUE;
+  if (c->max_attempts < 1) return PDQ_ERROR_INVALID_VALUE;
+  return PDQ_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t pdq_abi_version(void) { return PDQ_ABI_VERSION; }
+
+const char* pdq_status_string(pdq_status s) {
+  switch (s) {
+    case PDQ_SUCCESS: return "success";
+    case PDQ_ERROR_INVALID_VALUE: return "invalid value";
+    case PDQ_ERROR_UNSUPPORTED: return "unsupported configuration";
+    case PDQ_ERROR_CUDA: return "CUDA error";
+    case PDQ_ERROR_WORKSPACE: return "workspace too small";
+    case PDQ_ERROR_ABI_VERSION: return "ABI version mismatch";
+    default: return "unknown status";
+  }
+}
+
+pdq_status pdq_config_default(pdq_config* c, int32_t ssm, int32_t field, int32_t num_derivatives, int32_t ode_dim) {
+  if (c == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  memset(c, 0, sizeof(*c));
+  c->abi_version = PDQ_ABI_VERSION;
+  c->ssm = ssm;
+  c->constraint = PDQ_CONSTRAINT_TS0;
+  c->strategy = PDQ_STRATEGY_FILTER;
+  c->solver = PDQ_SOLVER_DYNAMIC;
+  c->error = PDQ_ERROR_RESIDUAL_STD;
+  c->control = PDQ_CONTROL_INTEGRAL;
+  c->precision = PDQ_PRECISION_F32;
+  c->field = field;
+  c->num_derivatives = num_derivatives;
+  c->ode_dim = ode_dim;
+  c->clip_dt = 1;
+  c->correct_asymptotic_underconfidence = 1;
+  c->safety = 0.95;
+  c->factor_min = 0.2;
+  c->factor_max = 10.0;
+  c->exponent_integral = 0.3;
+  c->exponent_proportional = 0.4;
+  c->atol = 1e-6;
+  c->rtol = 1e-6;
+  c->eps = 1e-8;
+  c->damp = 0.0;
+  c->max_attempts = 1 << 20;
+  return PDQ_SUCCESS;
+}
+
+pdq_status pdq_workspace_size(const pdq_config* c, int64_t num_instances, int32_t num_save_at, size_t* bytes) {
+  if (bytes == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  pdq_status st = validate_common(c);
+  if (st != PDQ_SUCCESS) return st;
+  if (num_instances < 0 || num_save_at < 2) return PDQ_ERROR_INVALID_VALUE;
+  *bytes = 0;
+  return PDQ_SUCCESS;
+}
+
+pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args, void* workspace,
+                              size_t workspace_bytes, void* stream_ptr) {
+  (void)workspace;
+  (void)workspace_bytes;
+  pdq_status st = validate_common(c);
+  if (st != PDQ_SUCCESS) return st;
+  if (args == nullptr || args->num_instances < 0 || args->num_save_at < 2) return PDQ_ERROR_INVALID_VALUE;
+  if (args->num_instances == 0) return PDQ_SUCCESS;
+  if (!args->save_at || !args->params || !args->y0 || !args->dt0 || !args->u_mean || !args->u_chol ||
+      !args->output_scale || !args->t || !args->num_steps || !args->num_attempts || !args->status)
+    return PDQ_ERROR_INVALID_VALUE;
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+
+  if (c->ssm == PDQ_SSM_ISOTROPIC) {
+    if (c->constraint != PDQ_CONSTRAINT_TS0 || c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
+    pdq::IsoArgs a;
+    memset(&a, 0, sizeof(a));
+    a.B = args->num_instances;
+    a.S = args->num_save_at;
+    a.terminal_only = args->terminal_only ? 1 : 0;
+    a.solver = c->solver;
+    a.control = c->control;
+    a.clip_dt = c->clip_dt ? 1 : 0;
+    a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
+    a.safety = c->safety;
+    a.factor_min = c->factor_min;
+    a.factor_max = c->factor_max;
+    a.exp_i = c->exponent_integral;
+    a.exp_p = c->exponent_proportional;
+    a.atol = c->atol;
+    a.rtol = c->rtol;
+    a.eps = c->eps;
+    a.damp = c->damp;
+    a.max_attempts = c->max_attempts;
+    iwp_q1(c->num_derivatives, a.q1);
+    a.save_at = args->save_at;
+    a.params = args->params;
+    a.y0 = args->y0;
+    a.dt0 = args->dt0;
+    a.u_mean = args->u_mean;
+    a.u_chol = args->u_chol;
+    a.output_scale = args->output_scale;
+    a.t_out = args->t;
+    a.num_steps = args->num_steps;
+    a.num_attempts = args->num_attempts;
+    a.status = args->status;
+    const bool interp = !c->clip_dt;
+    const int block = 64;
+    const bool f64 = c->precision == PDQ_PRECISION_F64;
+    cudaError_t err;
+    switch (c->field) {
+      case PDQ_FIELD_LOTKA_VOLTERRA:
+        err = f64 ? pdq_launch_iso_lv_f64(a, c->num_derivatives, interp, stream, block)
+                  : pdq_launch_iso_lv_f32(a, c->num_derivatives, interp, stream, block);
+        break;
+      case PDQ_FIELD_VAN_DER_POL:
+        err = f64 ? pdq_launch_iso_vdp_f64(a, c->num_derivatives, interp, stream, block)
+                  : pdq_launch_iso_vdp_f32(a, c->num_derivatives, interp, stream, block);
+        break;
+      case PDQ_FIELD_FITZHUGH_NAGUMO:
+        err = f64 ? pdq_launch_iso_fhn_f64(a, c->num_derivatives, interp, stream, block)
+                  : pdq_launch_iso_fhn_f32(a, c->num_derivatives, interp, stream, block);
+        break;
+      default:
+        return PDQ_ERROR_UNSUPPORTED;
+    }
+    return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+  }
+  return PDQ_ERROR_UNSUPPORTED;
+}
+
+}  // extern "C"

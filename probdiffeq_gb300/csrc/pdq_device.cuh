@@ -1,0 +1,226 @@
+// Device building blocks shared by the solver kernels.
+//
+// Everything here works on small fixed-size matrices held in registers (or in
+// per-thread local arrays the compiler keeps in registers when all indices are
+// compile-time constants).  Sizes are template parameters so every loop is
+// fully unrolled.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pdq.h"
+
+#define PDQ_HD __host__ __device__ __forceinline__
+#define PDQ_D __device__ __forceinline__
+
+namespace pdq {
+
+// ---------------------------------------------------------------------------
+// Scalar helpers
+// ---------------------------------------------------------------------------
+
+PDQ_D float dev_sqrt(float x) { return sqrtf(x); }
+PDQ_D double dev_sqrt(double x) { return sqrt(x); }
+PDQ_D float dev_rsqrt(float x) { return rsqrtf(x); }
+PDQ_D double dev_rsqrt(double x) { return rsqrt(x); }
+PDQ_D float dev_abs(float x) { return fabsf(x); }
+PDQ_D double dev_abs(double x) { return fabs(x); }
+PDQ_D float dev_pow(float x, float y) { return powf(x, y); }
+PDQ_D double dev_pow(double x, double y) { return pow(x, y); }
+
+template <int K>
+struct Factorial {
+  static constexpr double value = K * Factorial<K - 1>::value;
+};
+template <>
+struct Factorial<0> {
+  static constexpr double value = 1.0;
+};
+
+PDQ_HD constexpr double factorial(int k) { return k <= 1 ? 1.0 : k * factorial(k - 1); }
+
+PDQ_HD constexpr double binom(int n, int k) {
+  return (k < 0 || k > n) ? 0.0 : factorial(n) / (factorial(k) * factorial(n - k));
+}
+
+// IWP transition matrix in preconditioned coordinates (the reference's
+// flip(Pascal)): A[i][j] = binom(nu - i, nu - j) for j >= i, else 0.
+template <int NU>
+PDQ_HD constexpr double iwp_a(int i, int j) {
+  return j >= i ? binom(NU - i, NU - j) : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Truncated Taylor series ("jet") with normalised coefficients.
+// ---------------------------------------------------------------------------
+
+template <typename T, int K>
+struct Jet {
+  T c[K];
+  PDQ_HD Jet() {
+#pragma unroll
+    for (int k = 0; k < K; ++k) c[k] = T(0);
+  }
+  PDQ_HD Jet(T x) {
+    c[0] = x;
+#pragma unroll
+    for (int k = 1; k < K; ++k) c[k] = T(0);
+  }
+};
+
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator+(const Jet<T, K>& a, const Jet<T, K>& b) {
+  Jet<T, K> r;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.c[k] = a.c[k] + b.c[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator-(const Jet<T, K>& a, const Jet<T, K>& b) {
+  Jet<T, K> r;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.c[k] = a.c[k] - b.c[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator-(const Jet<T, K>& a) {
+  Jet<T, K> r;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.c[k] = -a.c[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator*(const Jet<T, K>& a, const Jet<T, K>& b) {
+  Jet<T, K> r;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    T acc = T(0);
+#pragma unroll
+    for (int j = 0; j <= k; ++j) acc += a.c[j] * b.c[k - j];
+    r.c[k] = acc;
+  }
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator*(T s, const Jet<T, K>& a) {
+  Jet<T, K> r;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.c[k] = s * a.c[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator*(const Jet<T, K>& a, T s) {
+  return s * a;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator+(T s, const Jet<T, K>& a) {
+  Jet<T, K> r = a;
+  r.c[0] += s;
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator+(const Jet<T, K>& a, T s) {
+  return s + a;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator-(T s, const Jet<T, K>& a) {
+  Jet<T, K> r = -a;
+  r.c[0] += s;
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Jet<T, K> operator-(const Jet<T, K>& a, T s) {
+  Jet<T, K> r = a;
+  r.c[0] -= s;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Vector-field registry.  Each field is written once, generic over the
+// scalar type S (float, double, Jet<...>, Dual<...>), so one definition gives
+// the value, the Taylor-mode initial derivatives and the Jacobian.
+//   eval(u, p, out): u[D] state, p[P] parameters (type T), out[D]
+// ---------------------------------------------------------------------------
+
+struct LotkaVolterra {
+  static constexpr int D = 2;
+  static constexpr int P = 4;
+  template <typename S, typename T>
+  PDQ_HD static void eval(const S* u, const T* p, S* out) {
+    S y01 = u[0] * u[1];
+    out[0] = p[0] * u[0] - p[1] * y01;
+    out[1] = p[3] * y01 - p[2] * u[1];
+  }
+};
+
+struct VanDerPol {
+  static constexpr int D = 2;
+  static constexpr int P = 1;
+  template <typename S, typename T>
+  PDQ_HD static void eval(const S* u, const T* p, S* out) {
+    out[0] = u[1];
+    out[1] = p[0] * ((T(1) - u[0] * u[0]) * u[1] - u[0]);
+  }
+};
+
+struct FitzHughNagumo {
+  static constexpr int D = 2;
+  static constexpr int P = 3;
+  template <typename S, typename T>
+  PDQ_HD static void eval(const S* u, const T* p, S* out) {
+    const T a = p[0], b = p[1], c = p[2];
+    out[0] = c * (u[0] - u[0] * u[0] * u[0] * (T(1) / T(3)) + u[1]);
+    out[1] = -(T(1) / c) * (u[0] - a - b * u[1]);
+  }
+};
+
+// Taylor-mode initial derivatives u(t0), u'(t0), ..., u^(NU)(t0) of an
+// autonomous ODE u' = f(u): with u(t) = sum a_k (t - t0)^k,
+// (k + 1) a_{k+1} = [f(u)]_k.  Returned as derivatives u^(k) = k! a_k.
+template <typename F, int NU, typename T>
+PDQ_HD void taylor_init(const T* y0, const T* p, T (&out)[NU + 1][F::D]) {
+  constexpr int K = NU + 1;
+  Jet<T, K> u[F::D];
+#pragma unroll
+  for (int j = 0; j < F::D; ++j) u[j] = Jet<T, K>(y0[j]);
+#pragma unroll
+  for (int k = 0; k < NU; ++k) {
+    Jet<T, K> f[F::D];
+    F::eval(u, p, f);
+#pragma unroll
+    for (int j = 0; j < F::D; ++j) u[j].c[k + 1] = f[j].c[k] / T(k + 1);
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+#pragma unroll
+    for (int j = 0; j < F::D; ++j) out[k][j] = u[j].c[k] * T(factorial(k));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Register-resident orthogonal triangularisation
+// ---------------------------------------------------------------------------
+
+// Rotate rows a and b of a register matrix (columns c0..NC-1) so that
+// M[b][c0] becomes zero; M[a][c0] becomes hypot(M[a][c0], M[b][c0]) >= 0.
+template <typename T, int NR, int NC>
+PDQ_D void givens_rows(T (&M)[NR][NC], int a, int b, int c0) {
+  const T x = M[a][c0], y = M[b][c0];
+  const T r2 = x * x + y * y;
+  if (r2 > T(0)) {
+    const T inv = dev_rsqrt(r2);
+    const T cs = x * inv, sn = y * inv;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+      if (j >= c0) {
+        const T ma = M[a][j], mb = M[b][j];
+        M[a][j] = cs * ma + sn * mb;
+        M[b][j] = cs * mb - sn * ma;
+      }
+    }
+    M[b][c0] = T(0);
+  }
+}
+
+}  // namespace pdq

@@ -1,0 +1,86 @@
+"""Batched solves of many independent IVP instances on one GPU.
+
+``solve_ensemble`` is the tensor-level entry point: one row of ``params`` and
+``y0`` per instance (the reference's ``jax.vmap`` over a solve).  Host
+tensors are copied to the device, the native solver runs on the current CUDA
+stream, and device tensors are returned.
+"""
+
+import torch
+
+from . import _native
+
+DEFAULT_MAX_ATTEMPTS = 1 << 20
+
+
+def make_config(
+    *,
+    field,
+    num_derivatives,
+    ode_dim,
+    ssm="isotropic",
+    constraint="ts0",
+    strategy="filter",
+    solver="dynamic",
+    control="integral",
+    precision="float32",
+    atol=1e-6,
+    rtol=1e-6,
+    clip_dt=True,
+    eps=1e-8,
+    damp=0.0,
+    correct_asymptotic_underconfidence=True,
+    safety=0.95,
+    factor_min=0.2,
+    factor_max=10.0,
+    exponent_integral=0.3,
+    exponent_proportional=0.4,
+    max_attempts=DEFAULT_MAX_ATTEMPTS,
+):
+    """Build a ``pdq_config`` (include/pdq.h) from keyword arguments."""
+    cfg = _native.config_default(ssm, field, num_derivatives, ode_dim)
+    cfg.constraint = _native.CONSTRAINT[constraint]
+    cfg.strategy = _native.STRATEGY[strategy]
+    cfg.solver = _native.SOLVER[solver]
+    cfg.control = _native.CONTROL[control]
+    cfg.precision = _native.PRECISION[precision]
+    cfg.atol, cfg.rtol, cfg.eps, cfg.damp = float(atol), float(rtol), float(eps), float(damp)
+    cfg.clip_dt = 1 if clip_dt else 0
+    cfg.correct_asymptotic_underconfidence = 1 if correct_asymptotic_underconfidence else 0
+    cfg.safety, cfg.factor_min, cfg.factor_max = float(safety), float(factor_min), float(factor_max)
+    cfg.exponent_integral, cfg.exponent_proportional = float(exponent_integral), float(exponent_proportional)
+    cfg.max_attempts = int(max_attempts)
+    return cfg
+
+
+def _dev(x, device, B=None, cols=None):
+    t = torch.as_tensor(x, dtype=torch.float64)
+    if B is not None and t.ndim == 1 and cols is not None and t.shape[0] == cols:
+        t = t.expand(B, cols)
+    return t.to(device, non_blocking=True).contiguous()
+
+
+def solve_ensemble(cfg, *, params, y0, save_at, dt0=0.1, terminal_only=True, device="cuda", stream=None, outputs=None):
+    """Solve B instances; returns the dict of output device tensors.
+
+    params (B, P), y0 (B, d), save_at (S,) shared or (B, S) per instance,
+    dt0 scalar or (B,).  Output layout as in include/pdq.h.
+    """
+    y0 = _dev(y0, device)
+    B = y0.shape[0]
+    params = _dev(params, device)
+    if params.ndim == 1:
+        params = params.expand(B, params.shape[0]).contiguous()
+    save_at = torch.as_tensor(save_at, dtype=torch.float64)
+    if save_at.ndim == 1:
+        save_at = save_at.expand(B, save_at.shape[0])
+    save_at = save_at.to(device, non_blocking=True).contiguous()
+    dt0 = torch.as_tensor(dt0, dtype=torch.float64)
+    if dt0.ndim == 0:
+        dt0 = dt0.expand(B)
+    dt0 = dt0.to(device, non_blocking=True).contiguous()
+    S = save_at.shape[1]
+    if outputs is None:
+        outputs = _native.alloc_outputs(cfg, B, S, terminal_only, device)
+    _native.solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream=stream)
+    return outputs

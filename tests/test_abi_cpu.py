@@ -1,0 +1,94 @@
+"""Host-side checks of the C ABI (no GPU needed; no compute calls).
+
+The library must load, export every function ``include/*.h`` declares, and
+reject malformed configurations before any launch.
+"""
+
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from probdiffeq_gb300 import _native
+    from probdiffeq_gb300 import build as native_build
+
+    native_build.build()
+    return _native.load()
+
+
+def declared_functions():
+    names = set()
+    for header in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(header).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(pdq_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert "pdq_solve_adaptive" in names
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_abi_version_and_status_strings(lib):
+    from probdiffeq_gb300 import _native
+
+    assert lib.pdq_abi_version() == _native.ABI_VERSION
+    assert _native.status_string(0) == "success"
+    assert _native.status_string(2) == "unsupported configuration"
+
+
+def test_config_default_matches_reference_defaults(lib):
+    from probdiffeq_gb300 import _native
+
+    cfg = _native.config_default("isotropic", "lotka_volterra", 4, 2)
+    # control_integral defaults (controllers.py:66-84), solve(...) defaults (solvers_via_adaptive_steps.py:35)
+    assert (cfg.safety, cfg.factor_min, cfg.factor_max) == (0.95, 0.2, 10.0)
+    assert (cfg.exponent_integral, cfg.exponent_proportional) == (0.3, 0.4)
+    assert cfg.eps == 1e-8 and cfg.damp == 0.0 and cfg.clip_dt == 1
+
+
+def test_malformed_configs_are_rejected_before_launch(lib):
+    from probdiffeq_gb300 import _native, ensemble
+
+    bad = []
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=3)  # LV has d = 2
+    bad.append(cfg)
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=9, ode_dim=2)
+    bad.append(cfg)
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2)
+    cfg.abi_version = 999
+    bad.append(cfg)
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2, atol=0.0, rtol=0.0)
+    bad.append(cfg)
+    for cfg in bad:
+        ws = ctypes.c_size_t(0)
+        st = lib.pdq_workspace_size(ctypes.byref(cfg), 4, 2, ctypes.byref(ws))
+        assert st != 0
+        args = _native.PdqAdaptiveArgs()
+        args.num_instances = 4
+        args.num_save_at = 2
+        st = lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), None, 0, None)
+        assert st != 0
+
+
+def test_missing_buffers_are_rejected(lib):
+    from probdiffeq_gb300 import _native, ensemble
+
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2)
+    args = _native.PdqAdaptiveArgs()
+    args.num_instances = 4
+    args.num_save_at = 2
+    assert lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), None, 0, None) == 1
+    args.num_save_at = 1
+    assert lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), None, 0, None) == 1

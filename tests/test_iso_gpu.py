@@ -1,0 +1,171 @@
+"""Parity of the isotropic TS0 CUDA solver against the oracle (GPU).
+
+The kernel runs through the C ABI (``pdq_solve_adaptive``) via
+``probdiffeq_gb300.ensemble``; the oracle is the float64 CPU restatement of
+the reference.  Tolerances (stated per test):
+  * float64 bulk: terminal means within 1e-9 relative, covariances within
+    1e-7 relative (of the largest entry), accepted steps within +-1;
+  * float32 bulk: terminal means within 1e-4 relative, covariances within
+    5e-3 relative, accepted steps within 2 % (+-1 minimum) -- single precision
+    can flip accept decisions near error_power = 1.
+"""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import problems, solvers, ssm
+
+pytestmark = pytest.mark.gpu
+
+NOMINAL = torch.tensor([0.5, 0.05, 0.5, 0.05], dtype=torch.float64)
+
+
+def lv_instances(B, seed=0):
+    g = torch.Generator().manual_seed(seed)
+    params = NOMINAL * torch.exp(0.2 * torch.randn((B, 4), generator=g, dtype=torch.float64))
+    y0 = 10.0 + 20.0 * torch.rand((B, 2), generator=g, dtype=torch.float64)
+    return params, y0
+
+
+_ORACLE = {}
+
+
+def oracle_solve(field, params, y0, nu, solver, save_at, atol, rtol, clip_dt, control="integral"):
+    key = (field, tuple(params.tolist()), tuple(y0.tolist()), nu, solver, tuple(save_at), atol, rtol, clip_dt, control)
+    if key in _ORACLE:
+        return _ORACLE[key]
+    fn = problems.FIELDS[field]
+    tc = problems.taylor_derivatives(fn, y0, params, nu)
+    S = ssm.IsoSSM()
+    prior = S.prior_wiener_integrated(tc)
+    c = S.constraint_ode_ts0(lambda u, t: fn(u[0], params))
+    cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE, "none": solvers.SolverPlain}[solver]
+    ctrl = solvers.ControlIntegral() if control == "integral" else solvers.ControlPI()
+    res = solvers.solve_adaptive_save_at(
+        cls(solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c), prior, list(save_at), atol, rtol,
+        control=ctrl, clip_dt=clip_dt, dt0=0.1,
+    )
+    _ORACLE[key] = res
+    return res
+
+
+def gpu_solve(field, params, y0, nu, solver, save_at, atol, rtol, clip_dt, precision, terminal_only, control="integral"):
+    from probdiffeq_gb300 import ensemble
+
+    cfg = ensemble.make_config(
+        field=field, num_derivatives=nu, ode_dim=2, solver=solver, precision=precision,
+        atol=atol, rtol=rtol, clip_dt=clip_dt, control=control,
+    )
+    out = ensemble.solve_ensemble(cfg, params=params, y0=y0, save_at=torch.tensor(save_at), dt0=0.1, terminal_only=terminal_only)
+    torch.cuda.synchronize()
+    return {k: v.cpu() for k, v in out.items()}
+
+
+def tolerances(precision):
+    if precision == "float64":
+        return dict(mean=1e-9, cov=1e-7, steps_rel=0.0)
+    return dict(mean=1e-4, cov=5e-3, steps_rel=0.02)
+
+
+def compare_record(gm, gc, om, oc, steps_g, steps_o, tol):
+    assert torch.allclose(gm, om, rtol=tol["mean"], atol=tol["mean"] * om.abs().max()), (gm, om)
+    cg, co = gc @ gc.T, oc @ oc.T
+    scale = co.abs().max().clamp_min(1e-300)
+    assert ((cg - co).abs().max() / scale) <= tol["cov"], ((cg - co).abs().max() / scale)
+    allowed = max(1, math.ceil(tol["steps_rel"] * steps_o))
+    assert abs(int(steps_g) - int(steps_o)) <= allowed, (steps_g, steps_o)
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+@pytest.mark.parametrize("solver", ["dynamic", "mle", "none"])
+def test_lv_terminal_values(solver, precision):
+    """solve_adaptive_terminal_values, filter, TS0, nu=4, rtol=atol=1e-6."""
+    params, y0 = lv_instances(5, seed=1)
+    save_at = [0.0, 10.0]
+    out = gpu_solve("lotka_volterra", params, y0, 4, solver, save_at, 1e-6, 1e-6, True, precision, True)
+    tol = tolerances(precision)
+    assert (out["status"] == 0).all()
+    for b in range(params.shape[0]):
+        res = oracle_solve("lotka_volterra", params[b], y0[b], 4, solver, save_at, 1e-6, 1e-6, True)
+        o = res.u[-1]
+        compare_record(out["u_mean"][b, 0], out["u_chol"][b, 0], o.mean, o.cholesky, out["num_steps"][b, 0], res.num_steps[-1], tol)
+        assert abs(float(out["t"][b, 0]) - 10.0) < 1e-8
+        scale_o = float(res.output_scale[-1])
+        assert abs(float(out["output_scale"][b, 0]) - scale_o) <= 10 * tol["mean"] * max(1.0, abs(scale_o)) + tol["cov"] * abs(scale_o)
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+def test_lv_save_at_with_interpolation(precision):
+    """solve_adaptive_save_at without clip_dt: checkpoints by interpolation (solvers.py:205-269)."""
+    params, y0 = lv_instances(3, seed=2)
+    save_at = [0.0, 0.7, 2.0, 3.3, 5.0]
+    out = gpu_solve("lotka_volterra", params, y0, 3, "dynamic", save_at, 1e-5, 1e-5, False, precision, False)
+    tol = tolerances(precision)
+    assert (out["status"] == 0).all()
+    for b in range(params.shape[0]):
+        res = oracle_solve("lotka_volterra", params[b], y0[b], 3, "dynamic", save_at, 1e-5, 1e-5, False)
+        for s in range(len(save_at)):
+            o = res.u[s]
+            steps_o = 0 if s == 0 else res.num_steps[s - 1]
+            compare_record(out["u_mean"][b, s], out["u_chol"][b, s], o.mean, o.cholesky, out["num_steps"][b, s], steps_o, tol)
+            assert abs(float(out["t"][b, s]) - save_at[s]) < 1e-7
+
+
+@pytest.mark.parametrize("field,params,y0", [
+    ("van_der_pol", [2.0], [2.0, 0.0]),
+    ("fitzhugh_nagumo", [0.2, 0.2, 3.0], [-1.0, 1.0]),
+])
+def test_other_fields_pi_controller(field, params, y0):
+    """Registered fields with the PI controller (controllers.py:24-63), float64."""
+    params = torch.tensor([params], dtype=torch.float64)
+    y0 = torch.tensor([y0], dtype=torch.float64)
+    save_at = [0.0, 3.0]
+    out = gpu_solve(field, params, y0, 3, "mle", save_at, 1e-5, 1e-5, True, "float64", True, control="proportional_integral")
+    res = oracle_solve(field, params[0], y0[0], 3, "mle", save_at, 1e-5, 1e-5, True, control="proportional_integral")
+    o = res.u[-1]
+    assert int(out["status"][0]) == 0
+    compare_record(out["u_mean"][0, 0], out["u_chol"][0, 0], o.mean, o.cholesky, out["num_steps"][0, 0], res.num_steps[-1], tolerances("float64"))
+
+
+@pytest.mark.parametrize("B", [1, 7, 33, 130])
+def test_ragged_batch_sizes_are_independent(B):
+    """Tail/warp edge cases: instance b's result does not depend on the batch it runs in."""
+    params, y0 = lv_instances(B, seed=3)
+    out = gpu_solve("lotka_volterra", params, y0, 2, "mle", [0.0, 2.0], 1e-4, 1e-4, True, "float32", True)
+    single = gpu_solve("lotka_volterra", params[B - 1 : B], y0[B - 1 : B], 2, "mle", [0.0, 2.0], 1e-4, 1e-4, True, "float32", True)
+    assert (out["status"] == 0).all()
+    assert torch.equal(out["u_mean"][B - 1], single["u_mean"][0])
+    assert torch.equal(out["num_steps"][B - 1], single["num_steps"][0])
+
+
+def test_empty_batch_is_a_noop():
+    from probdiffeq_gb300 import ensemble
+
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=2, ode_dim=2)
+    out = ensemble.solve_ensemble(cfg, params=torch.zeros((0, 4)), y0=torch.zeros((0, 2)), save_at=torch.tensor([0.0, 1.0]))
+    torch.cuda.synchronize()
+    assert out["u_mean"].shape[0] == 0
+
+
+def test_failure_statuses_are_reported_not_trapped():
+    """Run-time failures become per-instance status codes (never a trap or hang)."""
+    params, y0 = lv_instances(3, seed=4)
+    y0[1, 0] = float("nan")
+    out = gpu_solve("lotka_volterra", params, y0, 2, "mle", [0.0, 5.0], 1e-6, 1e-6, True, "float32", True)
+    assert out["status"].tolist()[1] == 3  # NONFINITE
+    assert out["status"].tolist()[0] == 0 and out["status"].tolist()[2] == 0
+    assert torch.isnan(out["u_mean"][1]).all()
+    # attempt bound
+    from probdiffeq_gb300 import ensemble
+
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=2, ode_dim=2, max_attempts=3)
+    out = ensemble.solve_ensemble(cfg, params=params[:1], y0=torch.tensor([[20.0, 20.0]]), save_at=torch.tensor([0.0, 50.0]))
+    torch.cuda.synchronize()
+    assert int(out["status"][0]) == 1 and int(out["num_attempts"][0]) == 3
+    # dt underflow
+    out = ensemble.solve_ensemble(cfg, params=params[:1], y0=torch.tensor([[20.0, 20.0]]), save_at=torch.tensor([0.0, 1.0]), dt0=0.0)
+    torch.cuda.synchronize()
+    assert int(out["status"][0]) == 2
