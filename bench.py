@@ -185,7 +185,8 @@ def run_ours(args):
     device = torch.device(f"cuda:{local}")
     torch.cuda.set_device(device)
 
-    B = WORKLOAD["instances"]
+    B = args.instances
+    WORKLOAD["instances"] = B
     params, y0 = lv_inputs(B, seed=rank)
     t0, t1 = WORKLOAD["t_span"]
     save_at = torch.tensor([t0, t1], dtype=torch.float64)
@@ -385,6 +386,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="ensemble size (16384 is the headline workload)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

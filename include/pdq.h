@@ -111,6 +111,14 @@ typedef struct pdq_adaptive_args {
   int32_t* num_steps;     /* (B, S_out) accepted steps up to each output */
   int32_t* num_attempts;  /* (B,) total attempts (accepted + rejected) */
   int32_t* status;        /* (B,) PDQ_INSTANCE_* */
+  /* optional outputs (NULL: not written); dense factorisation only, N = n*d */
+  double* cond_A;           /* (B, S-1, N, N) fixed-point smoother: backward conditional of each checkpoint */
+  double* cond_noise_mean;  /* (B, S-1, N) */
+  double* cond_noise_chol;  /* (B, S-1, N, N) */
+  double* cond_to_latent;   /* (B, S-1, N) */
+  double* cond_to_observed; /* (B, S-1, N) */
+  double* filter_mean;      /* (B, S, N) filtering marginals at the checkpoints */
+  double* filter_chol;      /* (B, S, N, N) */
 } pdq_adaptive_args;
 
 /* ABI version compiled into the library. */

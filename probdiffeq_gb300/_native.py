@@ -71,6 +71,13 @@ class PdqAdaptiveArgs(ctypes.Structure):
         ("num_steps", ctypes.c_void_p),
         ("num_attempts", ctypes.c_void_p),
         ("status", ctypes.c_void_p),
+        ("cond_A", ctypes.c_void_p),
+        ("cond_noise_mean", ctypes.c_void_p),
+        ("cond_noise_chol", ctypes.c_void_p),
+        ("cond_to_latent", ctypes.c_void_p),
+        ("cond_to_observed", ctypes.c_void_p),
+        ("filter_mean", ctypes.c_void_p),
+        ("filter_chol", ctypes.c_void_p),
     ]
 
 
@@ -154,7 +161,7 @@ def _stream_handle(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
-def solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream=None):
+def solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream=None, workspace=None):
     """Call pdq_solve_adaptive on device tensors (all float64, contiguous).
 
     ``outputs`` is a dict of preallocated device tensors (see ``alloc_outputs``).
@@ -170,28 +177,60 @@ def solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream
     args.dt0 = _ptr(dt0)
     for k in ("u_mean", "u_chol", "output_scale", "t", "num_steps", "num_attempts", "status"):
         setattr(args, k, _ptr(outputs[k]))
+    for k in OPTIONAL_OUTPUTS:
+        setattr(args, k, _ptr(outputs.get(k)))
     lib = load()
-    ws = ctypes.c_size_t(0)
-    check(lib.pdq_workspace_size(ctypes.byref(cfg), B, save_at.shape[1], ctypes.byref(ws)), "pdq_workspace_size")
-    check(lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), None, 0, _stream_handle(stream)), "pdq_solve_adaptive")
+    ws_bytes = workspace_size(cfg, B, save_at.shape[1])
+    ws = workspace if workspace is not None else None
+    if ws_bytes > 0 and (ws is None or ws.numel() * ws.element_size() < ws_bytes):
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=y0.device)
+    check(
+        lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), _ptr(ws), ctypes.c_size_t(ws_bytes), _stream_handle(stream)),
+        "pdq_solve_adaptive",
+    )
+    outputs["_workspace"] = ws
     return outputs
 
 
-def alloc_outputs(cfg, B, S, terminal_only, device):
+OPTIONAL_OUTPUTS = ("cond_A", "cond_noise_mean", "cond_noise_chol", "cond_to_latent", "cond_to_observed", "filter_mean", "filter_chol")
+
+
+def workspace_size(cfg, B, S):
+    ws = ctypes.c_size_t(0)
+    check(load().pdq_workspace_size(ctypes.byref(cfg), B, S, ctypes.byref(ws)), "pdq_workspace_size")
+    return int(ws.value)
+
+
+def alloc_outputs(cfg, B, S, terminal_only, device, posterior=False):
+    """Output tensors; ``posterior`` adds the dense smoother's conditionals and filtering marginals."""
     n = cfg.num_derivatives + 1
     d = cfg.ode_dim
     S_out = 1 if terminal_only else S
     f64 = dict(dtype=torch.float64, device=device)
     i32 = dict(dtype=torch.int32, device=device)
+    extra = {}
     if cfg.ssm == SSM["dense"]:
         N = n * d
         mean_shape, chol_shape = (B, S_out, N), (B, S_out, N, N)
+        if posterior:
+            extra = {
+                "cond_A": torch.empty((B, S - 1, N, N), **f64),
+                "cond_noise_mean": torch.empty((B, S - 1, N), **f64),
+                "cond_noise_chol": torch.empty((B, S - 1, N, N), **f64),
+                "cond_to_latent": torch.empty((B, S - 1, N), **f64),
+                "cond_to_observed": torch.empty((B, S - 1, N), **f64),
+                "filter_mean": torch.empty((B, S, N), **f64),
+                "filter_chol": torch.empty((B, S, N, N), **f64),
+            }
+    elif cfg.ssm == SSM["blockdiag"]:
+        mean_shape, chol_shape = (B, S_out, d, n), (B, S_out, d, n, n)
     else:
         mean_shape, chol_shape = (B, S_out, n, d), (B, S_out, n, n)
     return {
+        **extra,
         "u_mean": torch.empty(mean_shape, **f64),
         "u_chol": torch.empty(chol_shape, **f64),
-        "output_scale": torch.empty((B, S_out), **f64),
+        "output_scale": torch.empty((B, S_out, d) if cfg.ssm == SSM["blockdiag"] else (B, S_out), **f64),
         "t": torch.empty((B, S_out), **f64),
         "num_steps": torch.empty((B, S_out), **i32),
         "num_attempts": torch.empty((B,), **i32),

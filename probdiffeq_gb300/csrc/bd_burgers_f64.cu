@@ -1,0 +1,6 @@
+// Block-diagonal cluster kernels (Burgers stencil) in double bulk precision.
+#include "bd_launch.cuh"
+
+cudaError_t pdq_launch_bd_burgers_f64(const pdq::BdArgs& a, int nu, cudaStream_t stream) {
+  return pdq::launch_bd_precision<double>(a, nu, stream);
+}

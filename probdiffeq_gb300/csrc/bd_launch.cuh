@@ -1,0 +1,56 @@
+// Cluster launch of the block-diagonal kernel.
+#pragma once
+
+#include "bd_solver.cuh"
+
+namespace pdq {
+
+// Cluster size: aim at ~4 dimensions per thread, d divisible by the cluster.
+inline int bd_cluster_size(int d) {
+  int cl = 1;
+  while (cl < 8 && (d / cl) > kBdThreads * 4) cl *= 2;
+  while (cl > 1 && d % cl != 0) cl /= 2;
+  return cl;
+}
+
+template <typename T, int NU>
+cudaError_t launch_bd_nu(BdArgs a, cudaStream_t stream) {
+  cudaError_t e = ensure_stack<bd_adaptive_kernel<T, NU>>();
+  if (e != cudaSuccess) return e;
+  const int CL = a.cluster;
+  const size_t smem = size_t(a.d / CL) * sizeof(T);
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(bd_adaptive_kernel<T, NU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(a.B * CL), 1, 1);
+  cfg.blockDim = dim3(kBdThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, bd_adaptive_kernel<T, NU>, a);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_bd_precision(const BdArgs& a, int nu, cudaStream_t stream) {
+  switch (nu) {
+    case 2: return launch_bd_nu<T, 2>(a, stream);
+    case 3: return launch_bd_nu<T, 3>(a, stream);
+    case 4: return launch_bd_nu<T, 4>(a, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace pdq
+
+cudaError_t pdq_launch_bd_burgers_f32(const pdq::BdArgs& a, int nu, cudaStream_t stream);
+cudaError_t pdq_launch_bd_burgers_f64(const pdq::BdArgs& a, int nu, cudaStream_t stream);

@@ -1,0 +1,384 @@
+// Block-diagonal TS0 adaptive solver for high-dimensional ODEs (d up to a
+// few thousand per instance), one thread-block CLUSTER per instance.
+//
+// Follows the reference's block-diagonal path per dimension j:
+//   BlockDiagWienerIntegrated.transition  _probdiffeq/ssm_impl_blockdiag.py:406-432 (per-dim scale)
+//   BlockDiagLatentCond.apply_flat / marginalise / revert  ssm_impl_blockdiag.py:19-102
+//   BlockDiagOdeTs0.linearize             ssm_impl_blockdiag.py:129-144
+//   residual_whitened_rms_flat (per dim)  ssm_impl_blockdiag.py:285-292
+//   solver_dynamic / solver_mle / solver  _probdiffeq/solvers.py (per-dim output scale)
+//   error_residual_std (error (d,), rms over d)  solvers.py:925-996
+//   control, RejectionLoop with clip_dt   _ivpsolve/*.py
+// The vector field couples dimensions only through the stencil of f; the
+// error norm couples them through one sum over d.
+//
+// GB300 mapping: the instance's d dimensions are split contiguously over the
+// CL CTAs of a cluster.  Each attempt:
+//   1. every thread extrapolates its dimensions and writes u(t+h) of each to
+//      its CTA's shared memory;  cluster barrier;
+//   2. f at its dimensions reads the two stencil neighbours, from distributed
+//      shared memory of the neighbouring CTA at the CTA boundary; the
+//      per-dimension predict/update follows; the float64 error-norm partial
+//      is reduced in the CTA and published in shared memory;  cluster barrier;
+//   3. every CTA reads all CL partials over DSMEM and takes the same
+//      accept/step decision.
+// The per-dimension state (mean n, lower Cholesky n(n+1)/2) lives in two
+// scratch buffers in global memory (L2-resident: 64 x 4096 x 14 floats is
+// 15 MB per buffer); the proposal is written to the other buffer, so an
+// accept is a parity flip.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "iso_solver.cuh"
+
+namespace pdq {
+
+namespace cg = cooperative_groups;
+
+constexpr int kBdThreads = 256;
+constexpr int kBdMaxDimsPerThread = 8;
+
+struct BdArgs {
+  int64_t B;
+  int32_t S, terminal_only, solver, control, correct, d, cluster;
+  double safety, factor_min, factor_max, exp_i, exp_p;
+  double atol, rtol, eps, damp;
+  int64_t max_attempts;
+  double q1[kMaxN][kMaxN];
+  const double* save_at;
+  const double* params;  // (B, 1): viscosity
+  const double* y0;      // (B, d)
+  const double* dt0;
+  double* u_mean;        // (B, S_out, d, n)
+  double* u_chol;        // (B, S_out, d, n, n)
+  double* output_scale;  // (B, S_out, d)
+  double* t_out;
+  int32_t* num_steps;
+  int32_t* num_attempts;
+  int32_t* status;
+  void* workspace;       // 2 state buffers (B, ns, d) in T, then MLE sums (B, d) double
+};
+
+template <int NU>
+PDQ_HD constexpr int bd_state_rows() {
+  return (NU + 1) + (NU + 1) * (NU + 2) / 2;
+}
+
+// Viscous Burgers with periodic central differences (the flux-form stencil
+// of benchmarks/A5_work-precision-burgers-pde.py:124-134, periodic wrap).
+template <typename T>
+PDQ_D T burgers_f(T left, T mid, T right, T nu_visc, T inv_dx) {
+  const T flux = (right * right - left * left) * (T(0.25) * inv_dx);
+  const T lap = (right - T(2) * mid + left) * (inv_dx * inv_dx);
+  return -flux + nu_visc * lap;
+}
+
+template <typename T, int NU>
+__global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
+  constexpr int n = NU + 1;
+  constexpr int NS = bd_state_rows<NU>();
+  constexpr int OUT = 1;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CL = a.cluster;
+  const int rank = int(cluster.block_rank());
+  const int64_t inst = blockIdx.x / CL;
+  if (inst >= a.B) return;  // uniform per cluster
+  const int d = a.d;
+  const int dl = d / CL;
+  const int j0 = rank * dl;
+  const int tid = threadIdx.x;
+  const int dpt = (dl + kBdThreads - 1) / kBdThreads;  // <= kBdMaxDimsPerThread (host-checked)
+
+  extern __shared__ unsigned char smem_raw[];
+  T* ex = reinterpret_cast<T*>(smem_raw);                 // [dl] extrapolated u(t+h) of this CTA
+  __shared__ double partial[2];                           // CTA partial sums (error norm), parity
+  __shared__ double warp_sums[kBdThreads / 32];
+
+  T* const buf0 = reinterpret_cast<T*>(a.workspace);
+  T* const bufs[2] = {buf0 + inst * NS * int64_t(d), buf0 + (a.B + inst) * NS * int64_t(d)};
+  double* mle_sum = reinterpret_cast<double*>(buf0 + 2 * a.B * NS * int64_t(d)) + inst * int64_t(d);
+
+  const T nu_visc = T(a.params[inst]);
+  const T inv_dx = T(d);
+  const int S = a.S;
+  const int S_out = a.terminal_only ? 1 : S;
+  const double* save_at = a.save_at + inst * S;
+
+  // ---- Taylor-mode initial derivatives through the stencil (float64 jets) ----
+  // coefficient k of every dimension lives in row k of buffer 0 as a
+  // normalised Taylor coefficient during the recursion.
+  T* st = bufs[0];
+  for (int jl = tid; jl < dl; jl += kBdThreads) {
+    const int g = j0 + jl;
+    st[0 * d + g] = T(a.y0[inst * d + g]);
+  }
+  __threadfence();
+  cluster.sync();
+  for (int k = 0; k < NU; ++k) {
+    for (int jl = tid; jl < dl; jl += kBdThreads) {
+      const int g = j0 + jl;
+      const int gl = (g - 1 + d) % d, gr = (g + 1) % d;
+      // [f(u)]_k with quadratic flux: (u^2)_k = sum_l a_l a_{k-l}
+      double sq_l = 0.0, sq_r = 0.0;
+      for (int l = 0; l <= k; ++l) {
+        sq_l += double(st[l * d + gl]) * double(st[(k - l) * d + gl]);
+        sq_r += double(st[l * d + gr]) * double(st[(k - l) * d + gr]);
+      }
+      const double ul = st[k * d + gl], um = st[k * d + g], ur = st[k * d + gr];
+      const double idx = double(d);
+      const double fk = -(sq_r - sq_l) * 0.25 * idx + double(a.params[inst]) * (ur - 2.0 * um + ul) * idx * idx;
+      st[(k + 1) * d + g] = T(fk / (k + 1));
+    }
+    __threadfence();
+    cluster.sync();
+  }
+  // to derivatives; Cholesky rows zero (exact initial coefficients)
+  for (int jl = tid; jl < dl; jl += kBdThreads) {
+    const int g = j0 + jl;
+    for (int k = 0; k < n; ++k) st[k * d + g] = T(double(st[k * d + g]) * factorial(k));
+    for (int r = n; r < NS; ++r) st[r * d + g] = T(0);
+    mle_sum[g] = 0.0;
+  }
+  __threadfence();
+  cluster.sync();
+
+  double t = save_at[0], dt = a.dt0[inst], pi_prev = 1.0;
+  int cur = 0, num_steps = 0, attempts = 0, status = PDQ_INSTANCE_OK, num_data = 0, par = 0;
+  T sig[kBdMaxDimsPerThread];
+#pragma unroll
+  for (int k = 0; k < kBdMaxDimsPerThread; ++k) sig[k] = T(1);
+  const T damp = T(a.damp);
+  T q1_out2 = T(0);
+#pragma unroll
+  for (int j = 0; j < n; ++j) q1_out2 += T(a.q1[OUT][j]) * T(a.q1[OUT][j]);
+
+  auto write_checkpoint = [&](int s_out, double tt) {
+    const T* x = bufs[cur];
+    const int64_t rec = inst * S_out + s_out;
+    for (int jl = tid; jl < dl; jl += kBdThreads) {
+      const int g = j0 + jl;
+      double* um = a.u_mean + (rec * d + g) * n;
+      double* uc = a.u_chol + (rec * d + g) * n * n;
+      for (int i = 0; i < n; ++i) um[i] = double(x[i * d + g]);
+      int o = n;
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) uc[i * n + j] = (j <= i) ? double(x[(n + i * (i + 1) / 2 + j) * d + g]) : 0.0;
+      (void)o;
+    }
+    if (rank == 0 && tid == 0) {
+      a.t_out[rec] = tt;
+      a.num_steps[rec] = num_steps;
+    }
+  };
+  auto write_scale = [&](int s_out) {
+    const int64_t rec = inst * S_out + s_out;
+#pragma unroll
+    for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
+      const int jl = tid + k * kBdThreads;
+      if (k < dpt && jl < dl) a.output_scale[rec * d + j0 + jl] = double(sig[k]);
+    }
+  };
+
+  if (!a.terminal_only) {
+    write_checkpoint(0, t);
+#pragma unroll
+    for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
+      const int jl = tid + k * kBdThreads;
+      if (k < dpt && jl < dl) a.output_scale[(inst * S_out) * d + j0 + jl] = 1.0;
+    }
+  }
+
+  for (int s = 1; s < S && status == PDQ_INSTANCE_OK; ++s) {
+    const double t_next = save_at[s];
+    while (t + a.eps < t_next && status == PDQ_INSTANCE_OK) {
+      const double dt_use = fmin(dt, t_next - t);  // clip_dt
+      if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
+        status = PDQ_INSTANCE_DT_UNDERFLOW;
+        break;
+      }
+      if (attempts >= a.max_attempts) {
+        status = PDQ_INSTANCE_MAX_STEPS;
+        break;
+      }
+      ++attempts;
+      const T h = T(dt_use);
+      T p[n], pinv[n];
+      precon<T, NU>(h, p, pinv);
+      const T sq_h = dev_sqrt(dev_abs(h));
+      const T ell = dev_sqrt(p[OUT] * p[OUT] * dev_abs(h) * q1_out2 + damp * damp);
+      const T* x = bufs[cur];
+      T* y = bufs[cur ^ 1];
+
+      // ---- phase 1: extrapolated means; u(t+h) to shared memory ----
+      T mpk[kBdMaxDimsPerThread][n];
+#pragma unroll
+      for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
+        const int jl = tid + k * kBdThreads;
+        if (k < dpt && jl < dl) {
+          const int g = j0 + jl;
+          T m[n], mp[n];
+#pragma unroll
+          for (int i = 0; i < n; ++i) m[i] = x[i * d + g];
+#pragma unroll
+          for (int i = 0; i < n; ++i) {
+            T acc = T(0);
+#pragma unroll
+            for (int kk = i; kk < n; ++kk) acc += T(iwp_a<NU>(i, kk)) * pinv[kk] * m[kk];
+            mp[i] = p[i] * acc;
+            mpk[k][i] = mp[i];
+          }
+          ex[jl] = mp[0];
+        }
+      }
+      cluster.sync();
+
+      // ---- phase 2: stencil, calibration, predict, update, error partial ----
+      const T* ex_left = cluster.map_shared_rank(ex, (rank - 1 + CL) % CL);
+      const T* ex_right = cluster.map_shared_rank(ex, (rank + 1) % CL);
+      double local = 0.0;
+      T newt[kBdMaxDimsPerThread];
+      T sig_new[kBdMaxDimsPerThread];
+      T pinv_abs[n];
+#pragma unroll
+      for (int i = 0; i < n; ++i) pinv_abs[i] = dev_abs(pinv[i]);
+#pragma unroll
+      for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
+        newt[k] = T(0);
+        sig_new[k] = T(1);
+        const int jl = tid + k * kBdThreads;
+        if (k < dpt && jl < dl) {
+          const int g = j0 + jl;
+          const T left = jl > 0 ? ex[jl - 1] : ex_left[dl - 1];
+          const T right = jl < dl - 1 ? ex[jl + 1] : ex_right[0];
+          const T f = burgers_f(left, mpk[k][0], right, nu_visc, inv_dx);
+          const T mobs = mpk[k][OUT] - f;
+          // per-dimension residual_whitened_rms of fx.marginalise(apply_flat(m))
+          const T sigma = dev_div(dev_abs(mobs), ell);
+          const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma : T(1);
+          T L[n][n];
+#pragma unroll
+          for (int i = 0; i < n; ++i)
+#pragma unroll
+            for (int j = 0; j < n; ++j) L[i][j] = (j <= i) ? x[(n + i * (i + 1) / 2 + j) * d + g] : T(0);
+          // the block-diagonal marginalise scales the factor by |p_inv| (ssm_impl_blockdiag.py:32)
+          T Lp[n][n];
+          iso_predict_chol<T, NU>(a.q1, L, p, pinv_abs, s_pred * sq_h, Lp);
+          T gain[n], Lnew[n][n];
+          const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew);
+          T mnew[n];
+#pragma unroll
+          for (int i = 0; i < n; ++i) mnew[i] = mpk[k][i] - gain[i] * mobs;
+          // proposal -> the other buffer
+#pragma unroll
+          for (int i = 0; i < n; ++i) y[i * d + g] = mnew[i];
+#pragma unroll
+          for (int i = 0; i < n; ++i)
+#pragma unroll
+            for (int j = 0; j <= i; ++j) y[(n + i * (i + 1) / 2 + j) * d + g] = Lnew[i][j];
+          // error_residual_std: std = |sigma| l, error = std * h; reference max(|u0|, |u1|)
+          const T err_abs = dev_abs(sigma) * ell * h;
+          const T ref = fmax(dev_abs(x[g]), dev_abs(mnew[0]));
+          const T ratio = dev_div(err_abs, T(a.atol) + T(a.rtol) * ref);
+          local += double(ratio) * double(ratio);
+          newt[k] = dev_div(dev_abs(mobs), dev_abs(R_Y));
+          sig_new[k] = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma : T(1);
+        }
+      }
+      // CTA reduction of the float64 partial (warp shuffles, then warps)
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) local += __shfl_xor_sync(0xffffffffu, local, off);
+      if ((tid & 31) == 0) warp_sums[tid >> 5] = local;
+      __syncthreads();
+      if (tid == 0) {
+        double sum = 0.0;
+#pragma unroll
+        for (int w = 0; w < kBdThreads / 32; ++w) sum += warp_sums[w];
+        partial[par] = sum;
+      }
+      cluster.sync();
+
+      // ---- phase 3: identical decision in every CTA of the cluster ----
+      double total = 0.0;
+      for (int r = 0; r < CL; ++r) total += *cluster.map_shared_rank(&partial[par], r);
+      par ^= 1;
+      const double norm2 = total / double(d);
+      if (!(norm2 == norm2) || isinf(norm2)) {
+        status = PDQ_INSTANCE_NONFINITE;
+        break;
+      }
+      const T ep = dev_fpow(T(norm2), T(-0.5 / n));
+      double factor;
+      if (a.control == PDQ_CONTROL_INTEGRAL) {
+        factor = a.safety * double(ep);
+      } else {
+        factor = a.safety * double(dev_fpow(ep, T(a.exp_i))) * double(dev_fpow(dev_div(ep, T(pi_prev)), T(a.exp_p)));
+        if (norm2 <= 1.0) pi_prev = double(ep);
+      }
+      factor = fmax(a.factor_min, fmin(factor, a.factor_max));
+      dt = factor * dt_use;
+      if (norm2 <= 1.0) {
+        cur ^= 1;
+        t = t + dt_use;
+        ++num_steps;
+#pragma unroll
+        for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
+          const int jl = tid + k * kBdThreads;
+          if (k < dpt && jl < dl) {
+            sig[k] = sig_new[k];
+            if (a.solver == PDQ_SOLVER_MLE) mle_sum[j0 + jl] += double(newt[k]) * double(newt[k]);
+          }
+        }
+        if (a.solver == PDQ_SOLVER_MLE) ++num_data;
+      }
+    }
+    if (status != PDQ_INSTANCE_OK) break;
+    // clip_dt: every checkpoint is an exact landing (interp_at_t1)
+    if (!a.terminal_only || s == S - 1) {
+      const int s_out = a.terminal_only ? 0 : s;
+      write_checkpoint(s_out, t);
+      if (a.solver != PDQ_SOLVER_MLE) write_scale(s_out);
+    }
+  }
+
+  // ---- finalize ----
+  if (status == PDQ_INSTANCE_OK && a.solver == PDQ_SOLVER_MLE) {
+    // per-dimension calibrated scale, corrected by sqrt(num_steps) (solvers.py:449-465)
+    const int last = num_steps;
+    for (int s = 0; s < S_out; ++s) {
+      const int64_t rec = inst * S_out + s;
+      for (int jl = tid; jl < dl; jl += kBdThreads) {
+        const int g = j0 + jl;
+        double sc = num_data > 0 ? sqrt(mle_sum[g] / num_data) : 0.0;
+        if (a.correct) sc /= sqrt(double(last));
+        a.output_scale[rec * d + g] = sc;
+        double* uc = a.u_chol + (rec * d + g) * n * n;
+        for (int q = 0; q < n * n; ++q) uc[q] *= sc;
+      }
+    }
+  }
+  if (status != PDQ_INSTANCE_OK) {
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    for (int s = 0; s < S_out; ++s) {
+      const int64_t rec = inst * S_out + s;
+      for (int jl = tid; jl < dl; jl += kBdThreads) {
+        const int g = j0 + jl;
+        for (int q = 0; q < n; ++q) a.u_mean[(rec * d + g) * n + q] = nan;
+        for (int q = 0; q < n * n; ++q) a.u_chol[(rec * d + g) * n * n + q] = nan;
+        a.output_scale[rec * d + g] = nan;
+      }
+      if (rank == 0 && tid == 0) {
+        a.t_out[rec] = nan;
+        a.num_steps[rec] = num_steps;
+      }
+    }
+  }
+  if (rank == 0 && tid == 0) {
+    a.num_attempts[inst] = attempts;
+    a.status[inst] = status;
+  }
+  // keep every CTA's shared memory alive until the peers' last DSMEM reads
+  cluster.sync();
+}
+
+}  // namespace pdq

@@ -1,0 +1,4 @@
+// Dense-factorisation adaptive kernels for the FitzHughNagumo field in double bulk precision.
+#include "dense_launch.cuh"
+
+PDQ_DEFINE_DENSE_LAUNCH(pdq_launch_dense_fhn_f64, double, pdq::FitzHughNagumo)

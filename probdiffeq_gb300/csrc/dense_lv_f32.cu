@@ -1,0 +1,4 @@
+// Dense-factorisation adaptive kernels for the LotkaVolterra field in float bulk precision.
+#include "dense_launch.cuh"
+
+PDQ_DEFINE_DENSE_LAUNCH(pdq_launch_dense_lv_f32, float, pdq::LotkaVolterra)

@@ -7,11 +7,12 @@ namespace pdq {
 
 template <typename T, int NU, class F>
 cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
+  auto kernel = interp ? iso_adaptive_kernel<T, NU, F, true> : iso_adaptive_kernel<T, NU, F, false>;
+  cudaError_t e = interp ? ensure_stack<iso_adaptive_kernel<T, NU, F, true>>()
+                         : ensure_stack<iso_adaptive_kernel<T, NU, F, false>>();
+  if (e != cudaSuccess) return e;
   const unsigned grid = unsigned((a.B + block - 1) / block);
-  if (interp)
-    iso_adaptive_kernel<T, NU, F, true><<<grid, block, 0, stream>>>(a);
-  else
-    iso_adaptive_kernel<T, NU, F, false><<<grid, block, 0, stream>>>(a);
+  kernel<<<grid, block, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -50,12 +50,12 @@ struct IsoArgs {
 // Preconditioner p_i = h^(NU-i)/(NU-i)!, p_inv_i = 1/p_i (utilities.py:74-84).
 template <typename T, int NU>
 PDQ_D void precon(T h, T (&p)[NU + 1], T (&pinv)[NU + 1]) {
-  const T hinv = T(1) / h;
+  const T hinv = dev_rcp(h);
   p[NU] = T(1);
   pinv[NU] = T(1);
 #pragma unroll
   for (int i = NU - 1; i >= 0; --i) {
-    p[i] = p[i + 1] * h / T(NU - i);
+    p[i] = p[i + 1] * h * T(1.0 / (NU - i));
     pinv[i] = pinv[i + 1] * hinv * T(NU - i);
   }
 }
@@ -88,7 +88,7 @@ PDQ_D void iso_predict_mean(const T (&m)[NU + 1][D], const T (&p)[NU + 1], const
 // Householder reflector of column c only touches rows c..n-1 of the top block
 // and rows 0..c of the bottom block (n + 1 entries).
 template <typename T, int NU>
-PDQ_D void iso_predict_chol(const IsoArgs& a, const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
+PDQ_D void iso_predict_chol(const double (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
                             const T (&pinv)[NU + 1], T scale_q, T (&Lp)[NU + 1][NU + 1]) {
   constexpr int n = NU + 1;
   // top block X = (A pinv L)^T: X[r][c] = sum_k A[c][k] pinv[k] L[k][r]
@@ -102,7 +102,7 @@ PDQ_D void iso_predict_chol(const IsoArgs& a, const T (&L)[NU + 1][NU + 1], cons
 #pragma unroll
       for (int k = (c > r ? c : r); k < n; ++k) acc += T(iwp_a<NU>(c, k)) * pinv[k] * L[k][r];
       X[r][c] = acc;
-      U[r][c] = (r <= c) ? scale_q * T(a.q1[c][r]) : T(0);
+      U[r][c] = (r <= c) ? scale_q * T(q1[c][r]) : T(0);
     }
   // structured Householder QR
 #pragma unroll
@@ -117,8 +117,8 @@ PDQ_D void iso_predict_chol(const IsoArgs& a, const T (&L)[NU + 1][NU + 1], cons
       const T nrm = dev_sqrt(nrm2);
       const T beta = alpha >= T(0) ? -nrm : nrm;
       const T v0 = alpha - beta;
-      const T tau = (beta - alpha) / beta;
-      const T vinv = T(1) / v0;
+      const T tau = dev_div(beta - alpha, beta);
+      const T vinv = dev_rcp(v0);
       // normalised reflector v = [1, X[c+1..][c]/v0, U[0..c][c]/v0]
 #pragma unroll
       for (int r = c + 1; r < n; ++r) X[r][c] *= vinv;
@@ -149,11 +149,44 @@ PDQ_D void iso_predict_chol(const IsoArgs& a, const T (&L)[NU + 1][NU + 1], cons
 }
 
 template <typename T, int NU, int D>
-PDQ_D void iso_predict(const IsoArgs& a, const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1],
+PDQ_D void iso_predict(const double (&q1)[kMaxN][kMaxN], const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1],
                        const T (&p)[NU + 1], const T (&pinv)[NU + 1], T scale_q, T (&mp)[NU + 1][D],
                        T (&Lp)[NU + 1][NU + 1]) {
   iso_predict_mean<T, NU, D>(m, p, pinv, mp);
-  iso_predict_chol<T, NU>(a, L, p, pinv, scale_q, Lp);
+  iso_predict_chol<T, NU>(q1, L, p, pinv, scale_q, Lp);
+}
+
+// revert_conditional for a TS0 observation of coefficient OUT
+// (util/cholesky_util.py:27-82, H = e_OUT, noise chol damp): a Givens chain
+// on [[damp, 0], [(H Lp)^T, Lp^T]].  Column 0 has nonzeros in rows 0..OUT+1;
+// eliminating it bottom-up fills one subdiagonal entry per row, which one
+// rotation per column 1..OUT removes.  Returns R_Y; gain = R12^T / R_Y and
+// Lnew = R22^T.
+template <typename T, int NU, int OUT>
+PDQ_D T ts0_update(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (&Lnew)[NU + 1][NU + 1]) {
+  constexpr int n = NU + 1;
+  T M[n + 1][n + 1];
+#pragma unroll
+  for (int c = 0; c <= n; ++c) M[0][c] = (c == 0) ? damp : T(0);
+#pragma unroll
+  for (int r = 1; r <= n; ++r) {
+    M[r][0] = Lp[OUT][r - 1];
+#pragma unroll
+    for (int c = 1; c <= n; ++c) M[r][c] = (c >= r) ? Lp[c - 1][r - 1] : T(0);
+  }
+#pragma unroll
+  for (int r = OUT + 1; r >= 1; --r) givens_rows<T, n + 1, n + 1>(M, r - 1, r, 0);
+#pragma unroll
+  for (int c = 1; c <= OUT; ++c) givens_rows<T, n + 1, n + 1>(M, c, c + 1, c);
+  const T R_Y = M[0][0];
+  const T ry_inv = dev_rcp(R_Y);
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+    gain[i] = M[0][i + 1] * ry_inv;
+#pragma unroll
+    for (int j = 0; j < n; ++j) Lnew[i][j] = (j <= i) ? M[j + 1][i + 1] : T(0);
+  }
+  return R_Y;
 }
 
 template <typename T, int NU, int D>
@@ -276,44 +309,26 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             mobs[j] = mp[OUT][j] - f[j];
             mobs2 += mobs[j] * mobs[j];
           }
-          const T rms_mobs = dev_sqrt(mobs2 / T(D));
+          const T rms_mobs = dev_sqrt(mobs2 * T(1.0 / D));
           // fx.marginalise(apply_flat(m)) with unit scale: observed std
           // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
           // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
           const T ell = dev_sqrt(p[OUT] * p[OUT] * dev_abs(h) * q1_out2 + damp * damp);
-          const T sigma_loc = rms_mobs / ell;
+          const T sigma_loc = dev_div(rms_mobs, ell);
 
           const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
           T Lp[n][n];
-          iso_predict_chol<T, NU>(a, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
+          iso_predict_chol<T, NU>(a.q1, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
 
-          // ---- update: revert_conditional with H = e_OUT, a Givens chain
-          //      on [[damp, 0], [(H Lp)^T, Lp^T]] (util/cholesky_util.py:27-82) ----
-          T M[n + 1][n + 1];
+          // ---- update (revert_conditional, H = e_OUT) ----
+          T gain[n], Lnew[n][n];
+          const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew);
+          const T ry_inv = dev_rcp(R_Y);
+          T mnew[n][D];
 #pragma unroll
-          for (int c = 0; c <= n; ++c) M[0][c] = (c == 0) ? damp : T(0);
+          for (int i = 0; i < n; ++i)
 #pragma unroll
-          for (int r = 1; r <= n; ++r) {
-            M[r][0] = Lp[OUT][r - 1];
-#pragma unroll
-            for (int c = 1; c <= n; ++c) M[r][c] = (c >= r) ? Lp[c - 1][r - 1] : T(0);
-          }
-#pragma unroll
-          for (int r = OUT + 1; r >= 1; --r) givens_rows<T, n + 1, n + 1>(M, r - 1, r, 0);
-#pragma unroll
-          for (int c = 1; c <= OUT; ++c) givens_rows<T, n + 1, n + 1>(M, c, c + 1, c);
-
-          const T R_Y = M[0][0];
-          const T ry_inv = T(1) / R_Y;
-          T mnew[n][D], Lnew[n][n];
-#pragma unroll
-          for (int i = 0; i < n; ++i) {
-            const T g = M[0][i + 1] * ry_inv;  // gain G = R12^T / R_Y
-#pragma unroll
-            for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - g * mobs[j];
-#pragma unroll
-            for (int j = 0; j < n; ++j) Lnew[i][j] = (j <= i) ? M[j + 1][i + 1] : T(0);
-          }
+            for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - gain[i] * mobs[j];
 
           // ---- error estimate (error_residual_std, solvers.py:925-996) ----
           const T err_abs = dev_abs(sigma_loc) * ell * h;  // std of rescaled observed * dt^1/1!
@@ -321,29 +336,31 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
           for (int j = 0; j < D; ++j) {
             const T ref = fmax(dev_abs(m[0][j]), dev_abs(mnew[0][j]));
-            const T ratio = err_abs / (T(a.atol) + T(a.rtol) * ref);
+            const T ratio = dev_div(err_abs, T(a.atol) + T(a.rtol) * ref);
             sumsq += double(ratio) * double(ratio);
           }
-          const double norm2 = sumsq / D;
+          const double norm2 = sumsq * (1.0 / D);
           if (!(norm2 == norm2) || isinf(norm2)) {
             status = PDQ_INSTANCE_NONFINITE;
             break;
           }
-          const T ep = dev_pow(T(norm2), T(-0.5) / T(n));  // error_norm^(-1/n)
+          // error_power = error_norm^(-1/n); accepted iff error_power >= 1,
+          // i.e. iff error_norm^2 <= 1 (decided exactly on the float64 sum)
+          const T ep = dev_fpow(T(norm2), T(-0.5 / n));
 
           // ---- controller (controllers.py:24-84) ----
           double factor;
           if (a.control == PDQ_CONTROL_INTEGRAL) {
             factor = a.safety * double(ep);
           } else {
-            const double gi = double(dev_pow(ep, T(a.exp_i)));
-            const double gp = double(dev_pow(T(double(ep) / pi_prev), T(a.exp_p)));
+            const double gi = double(dev_fpow(ep, T(a.exp_i)));
+            const double gp = double(dev_fpow(dev_div(ep, T(pi_prev)), T(a.exp_p)));
             factor = a.safety * gi * gp;
-            if (double(ep) >= 1.0) pi_prev = double(ep);
+            if (norm2 <= 1.0) pi_prev = double(ep);
           }
           factor = fmax(a.factor_min, fmin(factor, a.factor_max));
           dt = factor * dt_use;
-          accepted = double(ep) >= 1.0;
+          accepted = norm2 <= 1.0;
           if (accepted) {
             if constexpr (INTERP) {
               ti = t;
@@ -366,7 +383,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             }
             if (a.solver == PDQ_SOLVER_MLE) {
               // running scale via hypot recurrence == RMS of new terms (solvers.py:421-424)
-              const T new_term = rms_mobs / dev_abs(R_Y);
+              const T new_term = rms_mobs * dev_abs(ry_inv);
               mle_sumsq += double(new_term) * double(new_term);
               ++num_data;
             }
@@ -387,7 +404,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           const T h = T(t_next - ti);
           T p[n], pinv[n], mp[n][D], Lp[n][n];
           precon<T, NU>(h, p, pinv);
-          iso_predict<T, NU, D>(a, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
+          iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
           if (record) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), t_next, num_steps);
           ti = t_next;
 #pragma unroll

@@ -3,6 +3,8 @@
 #include <math.h>
 #include <string.h>
 
+#include "bd_launch.cuh"
+#include "dense_launch.cuh"
 #include "iso_launch.cuh"
 #include "pdq.h"
 
@@ -114,6 +116,18 @@ pdq_status pdq_workspace_size(const pdq_config* c, int64_t num_instances, int32_
   if (st != PDQ_SUCCESS) return st;
   if (num_instances < 0 || num_save_at < 2) return PDQ_ERROR_INVALID_VALUE;
   *bytes = 0;
+  if (c->ssm == PDQ_SSM_BLOCKDIAG) {
+    const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
+    const int nu = c->num_derivatives;
+    const size_t rows = size_t(nu + 1) + size_t(nu + 1) * (nu + 2) / 2;
+    *bytes = 2 * size_t(num_instances) * rows * size_t(c->ode_dim) * elem + size_t(num_instances) * c->ode_dim * 8;
+  }
+  if (c->ssm == PDQ_SSM_DENSE && c->strategy == PDQ_STRATEGY_FIXEDPOINT) {
+    const int N = (c->num_derivatives + 1) * c->ode_dim;
+    const size_t floats = size_t(N) * N + N + size_t(N) * (N + 1) / 2 + 2 * N;
+    const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
+    *bytes = size_t(num_instances) * size_t(num_save_at - 1) * floats * elem;
+  }
   return PDQ_SUCCESS;
 }
 
@@ -179,6 +193,132 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
       case PDQ_FIELD_FITZHUGH_NAGUMO:
         err = f64 ? pdq_launch_iso_fhn_f64(a, c->num_derivatives, interp, stream, block)
                   : pdq_launch_iso_fhn_f32(a, c->num_derivatives, interp, stream, block);
+        break;
+      default:
+        return PDQ_ERROR_UNSUPPORTED;
+    }
+    return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+  }
+  if (c->ssm == PDQ_SSM_BLOCKDIAG) {
+    if (c->field != PDQ_FIELD_BURGERS) return PDQ_ERROR_UNSUPPORTED;
+    if (c->constraint != PDQ_CONSTRAINT_TS0 || c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
+    if (!c->clip_dt) return PDQ_ERROR_UNSUPPORTED;  // checkpoints by exact landing only
+    if (c->num_derivatives < 2 || c->num_derivatives > 4) return PDQ_ERROR_UNSUPPORTED;
+    const int d = c->ode_dim;
+    if (d < 3) return PDQ_ERROR_INVALID_VALUE;
+    const int CL = pdq::bd_cluster_size(d);
+    if (d % CL != 0 || d / CL > pdq::kBdThreads * pdq::kBdMaxDimsPerThread) return PDQ_ERROR_UNSUPPORTED;
+    size_t need = 0;
+    pdq_workspace_size(c, args->num_instances, args->num_save_at, &need);
+    if (workspace == nullptr || workspace_bytes < need) return PDQ_ERROR_WORKSPACE;
+    pdq::BdArgs a;
+    memset(&a, 0, sizeof(a));
+    a.B = args->num_instances;
+    a.S = args->num_save_at;
+    a.terminal_only = args->terminal_only ? 1 : 0;
+    a.solver = c->solver;
+    a.control = c->control;
+    a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
+    a.d = d;
+    a.cluster = CL;
+    a.safety = c->safety;
+    a.factor_min = c->factor_min;
+    a.factor_max = c->factor_max;
+    a.exp_i = c->exponent_integral;
+    a.exp_p = c->exponent_proportional;
+    a.atol = c->atol;
+    a.rtol = c->rtol;
+    a.eps = c->eps;
+    a.damp = c->damp;
+    a.max_attempts = c->max_attempts;
+    iwp_q1(c->num_derivatives, a.q1);
+    a.save_at = args->save_at;
+    a.params = args->params;
+    a.y0 = args->y0;
+    a.dt0 = args->dt0;
+    a.u_mean = args->u_mean;
+    a.u_chol = args->u_chol;
+    a.output_scale = args->output_scale;
+    a.t_out = args->t;
+    a.num_steps = args->num_steps;
+    a.num_attempts = args->num_attempts;
+    a.status = args->status;
+    a.workspace = workspace;
+    const cudaError_t err = c->precision == PDQ_PRECISION_F64
+                                ? pdq_launch_bd_burgers_f64(a, c->num_derivatives, stream)
+                                : pdq_launch_bd_burgers_f32(a, c->num_derivatives, stream);
+    return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+  }
+  if (c->ssm == PDQ_SSM_DENSE) {
+    if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
+    if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
+    if (c->strategy != PDQ_STRATEGY_FILTER && c->strategy != PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_INVALID_VALUE;
+    const bool fp = c->strategy == PDQ_STRATEGY_FIXEDPOINT;
+    size_t need = 0;
+    pdq_workspace_size(c, args->num_instances, args->num_save_at, &need);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need)) return PDQ_ERROR_WORKSPACE;
+    const bool any_cond = args->cond_A || args->cond_noise_mean || args->cond_noise_chol || args->cond_to_latent ||
+                          args->cond_to_observed;
+    const bool all_cond = args->cond_A && args->cond_noise_mean && args->cond_noise_chol && args->cond_to_latent &&
+                          args->cond_to_observed;
+    if (any_cond && (!all_cond || !fp || args->terminal_only)) return PDQ_ERROR_INVALID_VALUE;
+    if ((args->filter_mean == nullptr) != (args->filter_chol == nullptr)) return PDQ_ERROR_INVALID_VALUE;
+    pdq::DenseArgs a;
+    memset(&a, 0, sizeof(a));
+    a.B = args->num_instances;
+    a.S = args->num_save_at;
+    a.terminal_only = args->terminal_only ? 1 : 0;
+    a.solver = c->solver;
+    a.control = c->control;
+    a.clip_dt = c->clip_dt ? 1 : 0;
+    a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
+    a.fixedpoint = fp ? 1 : 0;
+    a.safety = c->safety;
+    a.factor_min = c->factor_min;
+    a.factor_max = c->factor_max;
+    a.exp_i = c->exponent_integral;
+    a.exp_p = c->exponent_proportional;
+    a.atol = c->atol;
+    a.rtol = c->rtol;
+    a.eps = c->eps;
+    a.damp = c->damp;
+    a.max_attempts = c->max_attempts;
+    iwp_q1(c->num_derivatives, a.q1);
+    a.save_at = args->save_at;
+    a.params = args->params;
+    a.y0 = args->y0;
+    a.dt0 = args->dt0;
+    a.u_mean = args->u_mean;
+    a.u_chol = args->u_chol;
+    a.output_scale = args->output_scale;
+    a.t_out = args->t;
+    a.num_steps = args->num_steps;
+    a.num_attempts = args->num_attempts;
+    a.status = args->status;
+    a.cond_A = args->cond_A;
+    a.cond_noise_mean = args->cond_noise_mean;
+    a.cond_noise_chol = args->cond_noise_chol;
+    a.cond_to_latent = args->cond_to_latent;
+    a.cond_to_observed = args->cond_to_observed;
+    a.filter_mean = args->filter_mean;
+    a.filter_chol = args->filter_chol;
+    a.workspace = workspace;
+    const bool ts1 = c->constraint == PDQ_CONSTRAINT_TS1;
+    const bool f64 = c->precision == PDQ_PRECISION_F64;
+    const int block = 32;
+    cudaError_t err;
+    switch (c->field) {
+      case PDQ_FIELD_LOTKA_VOLTERRA:
+        err = f64 ? pdq_launch_dense_lv_f64(a, c->num_derivatives, ts1, fp, stream, block)
+                  : pdq_launch_dense_lv_f32(a, c->num_derivatives, ts1, fp, stream, block);
+        break;
+      case PDQ_FIELD_VAN_DER_POL:
+        err = f64 ? pdq_launch_dense_vdp_f64(a, c->num_derivatives, ts1, fp, stream, block)
+                  : pdq_launch_dense_vdp_f32(a, c->num_derivatives, ts1, fp, stream, block);
+        break;
+      case PDQ_FIELD_FITZHUGH_NAGUMO:
+        err = f64 ? pdq_launch_dense_fhn_f64(a, c->num_derivatives, ts1, fp, stream, block)
+                  : pdq_launch_dense_fhn_f32(a, c->num_derivatives, ts1, fp, stream, block);
         break;
       default:
         return PDQ_ERROR_UNSUPPORTED;

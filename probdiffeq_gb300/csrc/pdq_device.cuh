@@ -16,6 +16,39 @@
 
 namespace pdq {
 
+// Raise this context's per-thread stack limit to what `kernel` needs (its
+// local frame plus headroom for calls) before its first launch.  Kernels
+// whose frame exceeds the default limit (1 KB) otherwise overrun the stack.
+// cudaDeviceSetLimit waits for the device, so it is only called when the
+// limit actually grows (once per process for each larger kernel).
+template <typename K>
+inline cudaError_t ensure_stack_for_uncached(K kernel) {
+  cudaFuncAttributes attr;
+  cudaError_t e = cudaFuncGetAttributes(&attr, kernel);
+  if (e != cudaSuccess) return e;
+  size_t cur = 0;
+  e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
+  if (e != cudaSuccess) return e;
+  const size_t need = attr.localSizeBytes + 1024;
+  if (need > cur) return cudaDeviceSetLimit(cudaLimitStackSize, need);
+  return cudaSuccess;
+}
+
+// Cached per kernel (template argument) and device (bit d of a 64-bit
+// mask), so steady-state launches do no attribute queries.
+template <auto KERNEL>
+inline cudaError_t ensure_stack() {
+  static unsigned long long ready = 0ull;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (__atomic_load_n(&ready, __ATOMIC_ACQUIRE) & bit)) return cudaSuccess;
+  e = ensure_stack_for_uncached(KERNEL);
+  if (e == cudaSuccess && bit) __atomic_fetch_or(&ready, bit, __ATOMIC_RELEASE);
+  return e;
+}
+
 // ---------------------------------------------------------------------------
 // Scalar helpers
 // ---------------------------------------------------------------------------
@@ -28,6 +61,13 @@ PDQ_D float dev_abs(float x) { return fabsf(x); }
 PDQ_D double dev_abs(double x) { return fabs(x); }
 PDQ_D float dev_pow(float x, float y) { return powf(x, y); }
 PDQ_D double dev_pow(double x, double y) { return pow(x, y); }
+// Fast variants for the float32 bulk path (a few ulp); exact in float64.
+PDQ_D float dev_div(float a, float b) { return __fdividef(a, b); }
+PDQ_D double dev_div(double a, double b) { return a / b; }
+PDQ_D float dev_rcp(float a) { return __frcp_rn(a); }
+PDQ_D double dev_rcp(double a) { return 1.0 / a; }
+PDQ_D float dev_fpow(float x, float y) { return __powf(x, y); }
+PDQ_D double dev_fpow(double x, double y) { return pow(x, y); }
 
 template <int K>
 struct Factorial {
@@ -137,6 +177,110 @@ PDQ_HD Jet<T, K> operator-(const Jet<T, K>& a, T s) {
 }
 
 // ---------------------------------------------------------------------------
+// Forward-mode dual numbers with K tangent directions (Jacobians of the
+// registered fields: jacobian_materialize, _probdiffeq/jacobians.py:78-113).
+// ---------------------------------------------------------------------------
+
+template <typename T, int K>
+struct Dual {
+  T v;
+  T g[K];
+  PDQ_HD Dual() : v(T(0)) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) g[k] = T(0);
+  }
+  PDQ_HD Dual(T x) : v(x) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) g[k] = T(0);
+  }
+};
+
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator+(const Dual<T, K>& a, const Dual<T, K>& b) {
+  Dual<T, K> r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = a.g[k] + b.g[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator-(const Dual<T, K>& a, const Dual<T, K>& b) {
+  Dual<T, K> r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = a.g[k] - b.g[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator-(const Dual<T, K>& a) {
+  Dual<T, K> r;
+  r.v = -a.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = -a.g[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator*(const Dual<T, K>& a, const Dual<T, K>& b) {
+  Dual<T, K> r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = a.g[k] * b.v + a.v * b.g[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator*(T s, const Dual<T, K>& a) {
+  Dual<T, K> r;
+  r.v = s * a.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = s * a.g[k];
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator*(const Dual<T, K>& a, T s) {
+  return s * a;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator+(T s, const Dual<T, K>& a) {
+  Dual<T, K> r = a;
+  r.v += s;
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator+(const Dual<T, K>& a, T s) {
+  return s + a;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator-(T s, const Dual<T, K>& a) {
+  Dual<T, K> r = -a;
+  r.v += s;
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator-(const Dual<T, K>& a, T s) {
+  Dual<T, K> r = a;
+  r.v -= s;
+  return r;
+}
+
+// f(u) and the Jacobian J[i][j] = df_i/du_j of a registered field.
+template <class F, typename T>
+PDQ_HD void eval_with_jacobian(const T* u, const T* p, T* f, T (&J)[F::D][F::D]) {
+  Dual<T, F::D> x[F::D], y[F::D];
+#pragma unroll
+  for (int j = 0; j < F::D; ++j) {
+    x[j] = Dual<T, F::D>(u[j]);
+    x[j].g[j] = T(1);
+  }
+  F::eval(x, p, y);
+#pragma unroll
+  for (int i = 0; i < F::D; ++i) {
+    f[i] = y[i].v;
+#pragma unroll
+    for (int j = 0; j < F::D; ++j) J[i][j] = y[i].g[j];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Vector-field registry.  Each field is written once, generic over the
 // scalar type S (float, double, Jet<...>, Dual<...>), so one definition gives
 // the value, the Taylor-mode initial derivatives and the Jacobian.
@@ -220,6 +364,41 @@ PDQ_D void givens_rows(T (&M)[NR][NC], int a, int b, int c0) {
       }
     }
     M[b][c0] = T(0);
+  }
+}
+
+// Householder R factor of a register matrix M (R x C, R >= C), in place:
+// afterwards M[0..C-1][*] holds R (upper triangle), rows below are zero.
+// Unstructured; used where the inputs carry no exploitable zero pattern.
+template <typename T, int NR, int NC>
+PDQ_D void householder_r(T (&M)[NR][NC]) {
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    T nrm2 = T(0);
+#pragma unroll
+    for (int r = c; r < NR; ++r) nrm2 += M[r][c] * M[r][c];
+    if (nrm2 > T(0)) {
+      const T alpha = M[c][c];
+      const T nrm = dev_sqrt(nrm2);
+      const T beta = alpha >= T(0) ? -nrm : nrm;
+      const T vinv = dev_rcp(alpha - beta);
+      const T tau = dev_div(beta - alpha, beta);
+#pragma unroll
+      for (int r = c + 1; r < NR; ++r) M[r][c] *= vinv;
+#pragma unroll
+      for (int j = c + 1; j < NC; ++j) {
+        T w = M[c][j];
+#pragma unroll
+        for (int r = c + 1; r < NR; ++r) w += M[r][c] * M[r][j];
+        w *= tau;
+        M[c][j] -= w;
+#pragma unroll
+        for (int r = c + 1; r < NR; ++r) M[r][j] -= w * M[r][c];
+      }
+      M[c][c] = beta;
+    }
+#pragma unroll
+    for (int r = c + 1; r < NR; ++r) M[r][c] = T(0);
   }
 }
 

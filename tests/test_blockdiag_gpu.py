@@ -1,0 +1,141 @@
+"""Parity of the block-diagonal cluster CUDA solver (viscous Burgers) (GPU).
+
+Configuration of the high-dimensional batch: periodic viscous Burgers with
+central differences, initial condition a sum of 8 random Fourier modes with
+amplitudes ~ N(0, 1/k^2), IWP with 3 derivatives, TS0 blockdiag filter,
+per-dimension dynamic calibration, error_residual_std, integral control,
+terminal values (clip_dt).
+
+Parity against the oracle runs at d = 64 (the oracle loops over dimensions
+in Python); the full size d = 4096 is checked against scipy's DOP853 on the
+same semi-discretisation (the reference's own accuracy tests compare against
+a classical solver) and float32 against float64.
+
+Tolerances: float64 -- solution 1e-8, rows 1e-5, covariances 1e-5,
+per-dimension output scales 1e-6, steps +-1; float32 -- solution 1e-3,
+other quantities within 4x the float32 oracle's deviation (floor 5e-2),
+steps within 2 % (+-1).
+"""
+
+import math
+
+import numpy as np
+import pytest
+import scipy.integrate
+import torch
+
+from oracle import problems, solvers, ssm
+
+pytestmark = pytest.mark.gpu
+
+NU_VISC = 0.01
+
+
+def burgers_ic(d, seed):
+    g = np.random.default_rng(seed)
+    x = np.arange(d) / d
+    k = np.arange(1, 9)
+    amp = g.normal(0.0, 1.0 / k)
+    phase = g.uniform(0.0, 2 * np.pi, size=8)
+    return (amp[:, None] * np.sin(2 * np.pi * k[:, None] * x[None, :] + phase[:, None])).sum(axis=0)
+
+
+def oracle_bd(u0, t1, solver="dynamic", atol=1e-4, rtol=1e-4, dtype=torch.float64):
+    p = torch.tensor([NU_VISC], dtype=torch.float64)
+    tc = problems.taylor_derivatives(problems.burgers, torch.tensor(u0), p, 3).to(dtype)
+    S = ssm.BdSSM()
+    prior = S.prior_wiener_integrated(tc)
+    pt = p.to(dtype)
+    c = S.constraint_ode_ts0(lambda u, t: problems.burgers(u[0], pt))
+    cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE, "none": solvers.SolverPlain}[solver]
+    return solvers.solve_adaptive_terminal_values(cls(solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c), prior, 0.0, t1, atol, rtol)
+
+
+def gpu_bd(u0s, t1, precision, solver="dynamic", atol=1e-4, rtol=1e-4):
+    from probdiffeq_gb300 import ensemble
+
+    u0s = torch.as_tensor(np.asarray(u0s), dtype=torch.float64)
+    B, d = u0s.shape
+    cfg = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=d, ssm="blockdiag", solver=solver,
+                               precision=precision, atol=atol, rtol=rtol, clip_dt=True)
+    out = ensemble.solve_ensemble(cfg, params=torch.full((B, 1), NU_VISC, dtype=torch.float64), y0=u0s,
+                                  save_at=torch.tensor([0.0, t1], dtype=torch.float64), dt0=0.1 * t1)
+    torch.cuda.synchronize()
+    return {k: v.cpu() for k, v in out.items() if k != "_workspace" and v is not None}
+
+
+def rel(a, b):
+    return float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+
+
+def compare(out, b, res, tol):
+    o = res.u[-1]  # BdNormal: mean (d, n), chol (d, n, n)
+    gm, gc = out["u_mean"][b, 0], out["u_chol"][b, 0]
+    err_u = rel(gm[:, 0], o.mean[:, 0])
+    err_rows = max(rel(gm[:, i], o.mean[:, i]) for i in range(o.mean.shape[1]))
+    cg = gc @ gc.transpose(-1, -2)
+    co = o.cholesky @ o.cholesky.transpose(-1, -2)
+    err_cov = max(rel(cg[j], co[j]) for j in range(co.shape[0]))
+    msg = f"u {err_u:.2e} rows {err_rows:.2e} cov {err_cov:.2e}"
+    assert err_u <= tol["u"], msg
+    assert err_rows <= tol["rows"], msg
+    assert err_cov <= tol["cov"], msg
+    allowed = max(1, math.ceil(tol["steps"] * res.num_steps[-1]))
+    assert abs(int(out["num_steps"][b, 0]) - res.num_steps[-1]) <= allowed
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+@pytest.mark.parametrize("solver", ["dynamic", "mle"])
+def test_burgers_small_vs_oracle(solver, precision):
+    d, t1 = 64, 0.05
+    u0s = [burgers_ic(d, s) for s in (1, 2)]
+    out = gpu_bd(u0s, t1, precision, solver=solver)
+    assert (out["status"] == 0).all()
+    for b, u0 in enumerate(u0s):
+        res = oracle_bd(u0, t1, solver=solver)
+        if precision == "float64":
+            tol = dict(u=1e-8, rows=1e-5, cov=1e-5, steps=0.0)
+        else:
+            r32 = oracle_bd(u0, t1, solver=solver, dtype=torch.float32)
+            o64, o32 = res.u[-1], r32.u[-1]
+            rows = max(rel(o32.mean[:, i].double(), o64.mean[:, i]) for i in range(4))
+            c32 = o32.cholesky.double()
+            cov = max(rel((c32 @ c32.transpose(-1, -2))[j], (o64.cholesky @ o64.cholesky.transpose(-1, -2))[j]) for j in range(d))
+            tol = dict(u=1e-3, rows=max(5e-2, 4 * rows), cov=max(5e-2, 4 * cov), steps=0.02)
+        compare(out, b, res, tol)
+        if precision == "float64":
+            assert rel(out["output_scale"][b, 0], torch.as_tensor(res.output_scale[-1]).reshape(-1)) < 1e-6
+
+
+def burgers_rhs(d):
+    dx = 1.0 / d
+
+    def f(t, u):
+        left, right = np.roll(u, 1), np.roll(u, -1)
+        return -(right**2 - left**2) / (4 * dx) + NU_VISC * (right - 2 * u + left) / dx**2
+
+    return f
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+def test_burgers_full_size_vs_classical_solver(precision):
+    """d = 4096, t in [0, 1], rtol = atol = 1e-4: terminal u against DOP853 (rtol 1e-10)."""
+    d = 4096
+    u0s = [burgers_ic(d, s) for s in (3, 4)]
+    out = gpu_bd(u0s, 1.0, precision)
+    assert (out["status"] == 0).all()
+    for b, u0 in enumerate(u0s):
+        ref = scipy.integrate.solve_ivp(burgers_rhs(d), (0.0, 1.0), u0, method="DOP853", rtol=1e-10, atol=1e-10).y[:, -1]
+        u = out["u_mean"][b, 0, :, 0].numpy()
+        err = np.abs(u - ref).max() / np.abs(ref).max()
+        assert err < 2e-3, err  # global error of an rtol = 1e-4 local-error controller
+
+
+def test_burgers_f32_matches_f64_full_size():
+    d = 4096
+    u0s = [burgers_ic(d, 5)]
+    o32 = gpu_bd(u0s, 0.5, "float32")
+    o64 = gpu_bd(u0s, 0.5, "float64")
+    err = rel(o32["u_mean"][0, 0, :, 0], o64["u_mean"][0, 0, :, 0])
+    assert err < 1e-3, err
+    assert abs(int(o32["num_steps"][0, 0]) - int(o64["num_steps"][0, 0])) <= max(1, math.ceil(0.02 * int(o64["num_steps"][0, 0])))

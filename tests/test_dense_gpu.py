@@ -1,0 +1,170 @@
+"""Parity of the dense-factorisation CUDA solver against the oracle (GPU).
+
+Configuration of the stiff dense batch: van der Pol (first order), IWP with 3
+derivatives, TS1 with the analytic Jacobian, fixed-point smoother with
+save_at checkpoints, dynamic calibration, error_residual_std, integral
+control.  The oracle's step count grows quickly with mu (48 / 3.5e3 / 1e5
+accepted steps for mu = 1 / 10 / 100), so parity runs at small mu.
+
+Tolerances (relative to the largest entry per Taylor-coefficient row and of
+L L^T): float64 -- solution 1e-8, rows 1e-5, covariance 1e-5, steps +-1;
+float32 -- solution 1e-3, rows/covariance within 4x the float32 oracle's own
+deviation (floor 5e-2), steps within 2 % (+-1).
+"""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import problems, solvers, ssm
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_vdp(mu, save_at, strategy="fixedpoint", constraint="ts1", solver="dynamic", atol=1e-5, rtol=1e-5, dtype=torch.float64):
+    p = torch.tensor([mu], dtype=torch.float64)
+    y0 = torch.tensor([2.0, 0.0], dtype=torch.float64)
+    tc = problems.taylor_derivatives(problems.van_der_pol, y0, p, 3).to(dtype)
+    pt = p.to(dtype)
+    D = ssm.DenseSSM()
+    prior = D.prior_wiener_integrated(tc)
+    vf = lambda u, t: problems.van_der_pol(u[0], pt)
+    jac = lambda u, t: problems.jacobian(problems.van_der_pol, u, pt)
+    c = D.constraint_ode_ts1(vf, jac, 2) if constraint == "ts1" else D.constraint_ode_ts0(vf, 2)
+    strat = solvers.StrategyFixedPoint() if strategy == "fixedpoint" else solvers.StrategyFilter()
+    cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE, "none": solvers.SolverPlain}[solver]
+    return solvers.solve_adaptive_save_at(cls(strat, c), solvers.ErrorResidualStd(c), prior, save_at, atol, rtol)
+
+
+def gpu_dense(field, params, y0, save_at, precision, strategy="fixedpoint", constraint="ts1", solver="dynamic",
+              atol=1e-5, rtol=1e-5, nu=3, posterior=True, clip_dt=False, terminal_only=False):
+    from probdiffeq_gb300 import _native, ensemble
+
+    cfg = ensemble.make_config(
+        field=field, num_derivatives=nu, ode_dim=2, ssm="dense", constraint=constraint, strategy=strategy,
+        solver=solver, precision=precision, atol=atol, rtol=rtol, clip_dt=clip_dt,
+    )
+    params = torch.as_tensor(params, dtype=torch.float64)
+    y0 = torch.as_tensor(y0, dtype=torch.float64)
+    save_at = torch.as_tensor(save_at, dtype=torch.float64)
+    B, S = y0.shape[0], save_at.shape[-1]
+    outs = _native.alloc_outputs(cfg, B, S, terminal_only, "cuda", posterior=posterior and strategy == "fixedpoint" and not terminal_only)
+    out = ensemble.solve_ensemble(cfg, params=params, y0=y0, save_at=save_at, dt0=0.1, terminal_only=terminal_only, outputs=outs)
+    torch.cuda.synchronize()
+    return {k: v.cpu() for k, v in out.items() if k != "_workspace" and v is not None}
+
+
+def rel(a, b):
+    return float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+
+
+def row_rel(g, o, d=2):
+    g, o = g.reshape(-1, d), o.reshape(-1, d)
+    return max(rel(g[i], o[i]) for i in range(o.shape[0]))
+
+
+def check(gm, gc, o, tol):
+    err_u = rel(gm[:2], o.mean[:2])
+    err_rows = row_rel(gm, o.mean)
+    co = o.cholesky @ o.cholesky.T
+    err_cov = rel(gc @ gc.T, co)
+    msg = f"u {err_u:.2e} rows {err_rows:.2e} cov {err_cov:.2e}"
+    assert err_u <= tol["u"], msg
+    assert err_rows <= tol["rows"], msg
+    assert err_cov <= tol["cov"], msg
+
+
+def f32_tol(o64, o32):
+    rows = row_rel(o32.mean.double(), o64.mean)
+    c32 = o32.cholesky.double()
+    cov = rel(c32 @ c32.T, o64.cholesky @ o64.cholesky.T)
+    return dict(u=1e-3, rows=max(5e-2, 4 * rows), cov=max(5e-2, 4 * cov))
+
+
+TOL64 = dict(u=1e-8, rows=1e-5, cov=1e-5)
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+@pytest.mark.parametrize("mu", [1.0, 3.0])
+def test_vdp_fixedpoint_ts1_save_at(mu, precision):
+    """Smoothed marginals at the checkpoints, the backward pass included."""
+    save_at = np.linspace(0.0, 2.0 * mu, 8)
+    res = oracle_vdp(mu, save_at)
+    out = gpu_dense("van_der_pol", [[mu]], [[2.0, 0.0]], save_at, precision)
+    assert int(out["status"][0]) == 0
+    if precision == "float32":
+        r32 = oracle_vdp(mu, save_at, dtype=torch.float32)
+    steps_o = [0] + list(res.num_steps)
+    for s in range(len(save_at)):
+        tol = TOL64 if precision == "float64" else f32_tol(res.u[s], r32.u[s])
+        check(out["u_mean"][0, s], out["u_chol"][0, s], res.u[s], tol)
+        allowed = 1 if precision == "float64" else max(1, math.ceil(0.02 * steps_o[s]))
+        assert abs(int(out["num_steps"][0, s]) - steps_o[s]) <= allowed
+    if precision == "float64":
+        # the backward conditionals of the smoother posterior
+        for k, c in enumerate(res.posterior["conditionals"]):
+            assert rel(out["cond_A"][0, k], c.A) < 1e-6
+            assert rel(out["cond_noise_mean"][0, k], c.noise.mean) < 1e-6
+            X = out["cond_noise_chol"][0, k]
+            assert rel(X @ X.T, c.noise.cholesky @ c.noise.cholesky.T) < 1e-5
+            assert rel(out["cond_to_latent"][0, k], c.to_latent) < 1e-6  # 1/p: ~h^-3, sensitive to t rounding
+            assert rel(out["cond_to_observed"][0, k], c.to_observed) < 1e-6
+        # filtering marginals at the checkpoints
+        for s, f in enumerate(res.posterior["filtering"]):
+            assert rel(out["filter_mean"][0, s], f.mean) < 1e-6
+
+
+def test_vdp_filter_ts0_and_mle():
+    """Dense TS0 with the filter and MLE calibration, float64."""
+    save_at = np.linspace(0.0, 2.0, 5)
+    res = oracle_vdp(1.0, save_at, strategy="filter", constraint="ts0", solver="mle")
+    out = gpu_dense("van_der_pol", [[1.0]], [[2.0, 0.0]], save_at, "float64", strategy="filter", constraint="ts0", solver="mle")
+    assert int(out["status"][0]) == 0
+    for s in range(len(save_at)):
+        check(out["u_mean"][0, s], out["u_chol"][0, s], res.u[s], TOL64)
+
+
+def test_dense_equals_isotropic_on_lotka_volterra():
+    """TS0 with kron-structured priors: dense and isotropic agree
+    (tests/test_probdiffeq/test_calibration/test_dynamic_across_factorisations.py:10-64)."""
+    from probdiffeq_gb300 import ensemble
+
+    params = torch.tensor([[0.5, 0.05, 0.5, 0.05]], dtype=torch.float64)
+    y0 = torch.tensor([[20.0, 20.0]], dtype=torch.float64)
+    save_at = torch.tensor([0.0, 5.0], dtype=torch.float64)
+    dn = gpu_dense("lotka_volterra", params, y0, save_at, "float64", strategy="filter", constraint="ts0",
+                   atol=1e-6, rtol=1e-6, nu=3, clip_dt=True, terminal_only=True)
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=3, ode_dim=2, solver="dynamic", precision="float64")
+    iso = ensemble.solve_ensemble(cfg, params=params, y0=y0, save_at=save_at)
+    torch.cuda.synchronize()
+    assert int(dn["num_steps"][0, 0]) == int(iso["num_steps"][0, 0].item())
+    assert rel(dn["u_mean"][0, 0], iso["u_mean"][0, 0].cpu().reshape(-1)) < 1e-9
+    Ld = dn["u_chol"][0, 0]
+    Li = iso["u_chol"][0, 0].cpu()
+    Ci = torch.kron(Li @ Li.T, torch.eye(2, dtype=torch.float64))
+    assert rel(Ld @ Ld.T, Ci) < 1e-7
+
+
+def test_dense_batch_and_workspace_errors():
+    """Several instances in one launch; too small a workspace is rejected before launch."""
+    import ctypes
+
+    from probdiffeq_gb300 import _native, ensemble
+
+    mus = [1.0, 1.5, 2.0]
+    save_at = np.linspace(0.0, 2.0, 4)
+    out = gpu_dense("van_der_pol", [[m] for m in mus], [[2.0, 0.0]] * 3, save_at, "float64", posterior=False)
+    for b, mu in enumerate(mus):
+        res = oracle_vdp(mu, np.linspace(0.0, 2.0, 4))
+        check(out["u_mean"][b, -1], out["u_chol"][b, -1], res.u[-1], TOL64)
+    cfg = ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense", constraint="ts1", strategy="fixedpoint")
+    assert _native.workspace_size(cfg, 3, 4) > 0
+    args = _native.PdqAdaptiveArgs()
+    args.num_instances, args.num_save_at = 3, 4
+    dummy = torch.zeros(64, dtype=torch.float64, device="cuda")
+    for k in ("save_at", "params", "y0", "dt0", "u_mean", "u_chol", "output_scale", "t", "num_steps", "num_attempts", "status"):
+        setattr(args, k, ctypes.c_void_p(dummy.data_ptr()))
+    st = _native.load().pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), ctypes.c_void_p(dummy.data_ptr()), 8, None)
+    assert st == 4  # PDQ_ERROR_WORKSPACE, nothing launched
