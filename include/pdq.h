@@ -121,6 +121,22 @@ typedef struct pdq_adaptive_args {
   double* filter_chol;      /* (B, S, N, N) */
 } pdq_adaptive_args;
 
+typedef struct pdq_lml_args {
+  int64_t num_instances;  /* B parameter samples */
+  int32_t num_steps;      /* fixed grid of num_steps steps of size dt from t0 */
+  int32_t save_every;     /* one observation every save_every steps (num_steps % save_every == 0) */
+  int32_t average_pdfs;   /* loss_lml_timeseries(average_pdfs=...) */
+  int32_t with_gradient;  /* 1: also write d lml / d params */
+  double t0, dt;
+  const double* params;   /* (B, P) vector-field parameters */
+  const double* y0;       /* (B, d) initial values */
+  const double* data;     /* (num_obs, d), num_obs = num_steps / save_every + 1, at t0 + k save_every dt */
+  const double* std;      /* (num_obs,) observation noise standard deviations */
+  double* lml;            /* (B,) log-marginal likelihood */
+  double* grad;           /* (B, P) gradient, written if with_gradient */
+  int32_t* status;        /* (B,) PDQ_INSTANCE_* */
+} pdq_lml_args;
+
 /* ABI version compiled into the library. */
 uint32_t pdq_abi_version(void);
 
@@ -138,6 +154,23 @@ pdq_status pdq_workspace_size(const pdq_config* config, int64_t num_instances, i
 /* Adaptive solve of B independent instances; see the file header. */
 pdq_status pdq_solve_adaptive(const pdq_config* config, const pdq_adaptive_args* args, void* workspace,
                               size_t workspace_bytes, void* stream);
+
+/* Device scratch of pdq_lml_fixed_grid in bytes. */
+pdq_status pdq_lml_workspace_size(const pdq_config* config, int64_t num_instances, int32_t num_steps, int32_t save_every,
+                                  size_t* bytes);
+
+/* Log-marginal likelihood of time-series data, and its gradient with respect
+ * to the vector-field parameters, for B parameter samples:
+ *   an isotropic TS0 solve with the uncalibrated solver and the fixed-point
+ *   smoother on a fixed grid whose every save_every-th point is an
+ *   observation (checkpoint reset, estimators_and_losses.py:534-547), then
+ *   loss_lml_timeseries on the resulting backward Markov sequence
+ *   (probdiffeq/_probdiffeq/estimators_and_losses.py:53-105, 180-218).
+ * The gradient follows the reference's differentiation rules (qr_r's custom
+ * JVP, probdiffeq/backend/linalg.py:13-37; no gradient through dt).
+ * config: ssm isotropic, constraint TS0, strategy fixedpoint, solver plain. */
+pdq_status pdq_lml_fixed_grid(const pdq_config* config, const pdq_lml_args* args, void* workspace, size_t workspace_bytes,
+                              void* stream);
 
 #ifdef __cplusplus
 }

@@ -81,6 +81,25 @@ class PdqAdaptiveArgs(ctypes.Structure):
     ]
 
 
+class PdqLmlArgs(ctypes.Structure):
+    _fields_ = [
+        ("num_instances", ctypes.c_int64),
+        ("num_steps", ctypes.c_int32),
+        ("save_every", ctypes.c_int32),
+        ("average_pdfs", ctypes.c_int32),
+        ("with_gradient", ctypes.c_int32),
+        ("t0", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("params", ctypes.c_void_p),
+        ("y0", ctypes.c_void_p),
+        ("data", ctypes.c_void_p),
+        ("std", ctypes.c_void_p),
+        ("lml", ctypes.c_void_p),
+        ("grad", ctypes.c_void_p),
+        ("status", ctypes.c_void_p),
+    ]
+
+
 # Every symbol include/pdq.h declares, with its ctypes signature.
 SIGNATURES = {
     "pdq_abi_version": (ctypes.c_uint32, []),
@@ -96,6 +115,14 @@ SIGNATURES = {
     "pdq_solve_adaptive": (
         ctypes.c_int,
         [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqAdaptiveArgs), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "pdq_lml_workspace_size": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "pdq_lml_fixed_grid": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlArgs), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
     ),
     "pdq_probe_fp32_fma": (
         ctypes.c_int,
@@ -236,3 +263,33 @@ def alloc_outputs(cfg, B, S, terminal_only, device, posterior=False):
         "num_attempts": torch.empty((B,), **i32),
         "status": torch.empty((B,), **i32),
     }
+
+
+def lml_fixed_grid(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every, average_pdfs=False, gradient=True,
+                   stream=None, workspace=None, outputs=None):
+    """Call pdq_lml_fixed_grid on device tensors (float64, contiguous); returns (lml, grad, status)."""
+    lib = load()
+    B = y0.shape[0]
+    P = params.shape[1]
+    dev = y0.device
+    if outputs is None:
+        outputs = {
+            "lml": torch.empty(B, dtype=torch.float64, device=dev),
+            "grad": torch.empty((B, P), dtype=torch.float64, device=dev) if gradient else None,
+            "status": torch.empty(B, dtype=torch.int32, device=dev),
+        }
+    nbytes = ctypes.c_size_t(0)
+    check(lib.pdq_lml_workspace_size(ctypes.byref(cfg), B, num_steps, save_every, ctypes.byref(nbytes)), "pdq_lml_workspace_size")
+    ws = workspace
+    if ws is None or ws.numel() * ws.element_size() < nbytes.value:
+        ws = torch.empty(max(1, nbytes.value), dtype=torch.uint8, device=dev)
+    a = PdqLmlArgs()
+    a.num_instances, a.num_steps, a.save_every = B, num_steps, save_every
+    a.average_pdfs, a.with_gradient = int(bool(average_pdfs)), int(bool(gradient))
+    a.t0, a.dt = float(t0), float(dt)
+    a.params, a.y0, a.data, a.std = _ptr(params), _ptr(y0), _ptr(data), _ptr(std)
+    a.lml, a.grad, a.status = _ptr(outputs["lml"]), _ptr(outputs.get("grad")), _ptr(outputs["status"])
+    check(lib.pdq_lml_fixed_grid(ctypes.byref(cfg), ctypes.byref(a), _ptr(ws), ctypes.c_size_t(nbytes.value), _stream_handle(stream)),
+          "pdq_lml_fixed_grid")
+    outputs["_workspace"] = ws
+    return outputs

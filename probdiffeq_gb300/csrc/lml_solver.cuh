@@ -1,0 +1,513 @@
+// Log-marginal likelihood of time-series data under the fixed-point-smoother
+// posterior of an isotropic TS0 solve on a fixed grid, and its gradient with
+// respect to the vector-field parameters.  One thread per parameter sample.
+//
+// Forward (value) path, following the reference:
+//   solver (uncalibrated) step              _probdiffeq/solvers.py:702-733
+//   strategy_smoother_fixedpoint.predict     _probdiffeq/estimators_and_losses.py:526-532
+//     IsotropicLatentCond.revert / merge     _probdiffeq/ssm_impl_isotropic.py:91-133
+//   checkpoint reset to the identity         estimators_and_losses.py:534-547
+//     (the save_at mechanics on a grid whose steps land on the observations)
+//   Smoother.finalize (rv at t1)             estimators_and_losses.py:437-470
+//   loss_lml_timeseries / evaluate_lml       estimators_and_losses.py:53-105, 180-218
+//     with to_derivative(0, std), bayes_rule_and_logpdf_tree and
+//     IsotropicNormal.logpdf_flat            ssm_impl_api.py:118-124, ssm_impl_isotropic.py:217-278
+//   Taylor-mode initial derivatives          _probdiffeq/jet_expansion_algorithms.py:49-103
+//
+// Derivative: every value carries P tangents (forward mode, one direction per
+// parameter).  The rules are the reference's: qr_r has the custom JVP
+// R_dot = Q^T M_dot with Q held constant (backend/linalg.py:13-37), so the
+// reflectors / rotations computed from the values are applied to the tangent
+// matrices and the tangent of a triangular factor is a full matrix;
+// triangular solves differentiate through the triangle only (back
+// substitution on dual numbers); the time step carries no tangent (the
+// reference stops gradients through dt).  For the 3 parameters of the
+// configurations this costs about what one reverse sweep costs and needs no
+// checkpoint storage.  The log-likelihood sum and its tangents are float64.
+#pragma once
+
+#include "iso_solver.cuh"
+
+namespace pdq {
+
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator/(const Dual<T, K>& a, const Dual<T, K>& b) {
+  Dual<T, K> r;
+  const T inv = T(1) / b.v;
+  r.v = a.v * inv;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = (a.g[k] - r.v * b.g[k]) * inv;
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator/(const Dual<T, K>& a, T b) {
+  Dual<T, K> r;
+  const T inv = T(1) / b;
+  r.v = a.v * inv;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = a.g[k] * inv;
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator/(T a, const Dual<T, K>& b) {
+  return Dual<T, K>(a) / b;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> dual_abs_scale(T s, const Dual<T, K>& a) {  // |s| * a for a constant s
+  return (s < T(0) ? -s : s) * a;
+}
+
+struct LmlArgs {
+  int64_t B;
+  int32_t num_steps, save_every, average_pdfs, with_gradient;
+  double t0, dt, damp;
+  double q1[kMaxN][kMaxN];
+  const double* params;  // (B, P)
+  const double* y0;      // (B, d)
+  const double* data;    // (num_obs, d)
+  const double* std;     // (num_obs,)
+  double* lml;           // (B,)
+  double* grad;          // (B, P) or nullptr
+  int32_t* status;       // (B,)
+  void* workspace;       // (B, num_obs - 1) conditionals with tangents, T
+};
+
+// Householder QR (R x C, R >= C) of a dual matrix with the Q-constant tangent
+// rule: reflectors from the values; the values become R (zeros below), the
+// tangents become the first rows of Q^T M_dot (full, not triangular).
+template <typename T, int P, int R, int C>
+PDQ_D void qr_qconst(Dual<T, P> (&M)[R][C]) {
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    T nrm2 = T(0);
+#pragma unroll
+    for (int r = c; r < R; ++r) nrm2 += M[r][c].v * M[r][c].v;
+    if (nrm2 > T(0)) {
+      const T alpha = M[c][c].v;
+      const T nrm = dev_sqrt(nrm2);
+      const T beta = alpha >= T(0) ? -nrm : nrm;
+      const T v0inv = T(1) / (alpha - beta);
+      const T tau = (beta - alpha) / beta;
+      T v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = (r < c) ? T(0) : (r == c ? T(1) : M[r][c].v * v0inv);
+      // values: columns > c
+#pragma unroll
+      for (int j = c + 1; j < C; ++j) {
+        T w = T(0);
+#pragma unroll
+        for (int r = c; r < R; ++r) w += v[r] * M[r][j].v;
+        w *= tau;
+#pragma unroll
+        for (int r = c; r < R; ++r) M[r][j].v -= w * v[r];
+      }
+      // tangents: every column
+#pragma unroll
+      for (int k = 0; k < P; ++k)
+#pragma unroll
+        for (int j = 0; j < C; ++j) {
+          T w = T(0);
+#pragma unroll
+          for (int r = c; r < R; ++r) w += v[r] * M[r][j].g[k];
+          w *= tau;
+#pragma unroll
+          for (int r = c; r < R; ++r) M[r][j].g[k] -= w * v[r];
+        }
+      M[c][c].v = beta;
+#pragma unroll
+      for (int r = c + 1; r < R; ++r) M[r][c].v = T(0);
+    }
+  }
+}
+
+// Givens rotation of rows a, b zeroing M[b][c0] in the values; the same
+// rotation is applied to all value columns and all tangents (Q constant).
+template <typename T, int P, int NR, int NC>
+PDQ_D void givens_qconst(Dual<T, P> (&M)[NR][NC], int a, int b, int c0) {
+  const T x = M[a][c0].v, y = M[b][c0].v;
+  const T r2 = x * x + y * y;
+  if (r2 > T(0)) {
+    const T inv = dev_rsqrt(r2);
+    const T cs = x * inv, sn = y * inv;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+      const Dual<T, P> ma = M[a][j], mb = M[b][j];
+      M[a][j] = cs * ma + sn * mb;
+      M[b][j] = cs * mb - sn * ma;
+    }
+    M[b][c0].v = T(0);
+  }
+}
+
+template <typename T, int P, int NU, int D>
+struct LmlCond {
+  Dual<T, P> A[NU + 1][NU + 1];
+  Dual<T, P> xi[NU + 1][D];
+  Dual<T, P> X[NU + 1][NU + 1];
+  T tl[NU + 1];
+  T to[NU + 1];
+};
+
+template <typename T, int P, int NU, int D>
+PDQ_D void lml_cond_identity(LmlCond<T, P, NU, D>& c) {
+  constexpr int n = NU + 1;
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+      c.A[i][j] = Dual<T, P>(i == j ? T(1) : T(0));
+      c.X[i][j] = Dual<T, P>(T(0));
+    }
+#pragma unroll
+    for (int j = 0; j < D; ++j) c.xi[i][j] = Dual<T, P>(T(0));
+    c.tl[i] = T(1);
+    c.to[i] = T(1);
+  }
+}
+
+// cond.marginalise(rv) (ssm_impl_isotropic.py:81-89)
+template <typename T, int P, int NU, int D>
+PDQ_D void lml_marginalise(const LmlCond<T, P, NU, D>& c, const Dual<T, P> (&m)[NU + 1][D],
+                           const Dual<T, P> (&L)[NU + 1][NU + 1], Dual<T, P> (&mo)[NU + 1][D],
+                           Dual<T, P> (&Lo)[NU + 1][NU + 1]) {
+  constexpr int n = NU + 1;
+  using DT = Dual<T, P>;
+  DT M[2 * n][n];
+#pragma unroll
+  for (int r = 0; r < n; ++r)
+#pragma unroll
+    for (int col = 0; col < n; ++col) {
+      DT acc(T(0));
+#pragma unroll
+      for (int k = 0; k < n; ++k) acc = acc + c.A[col][k] * (c.tl[k] * L[k][r]);
+      M[r][col] = acc;
+      M[n + r][col] = c.X[col][r];
+    }
+  qr_qconst<T, P, 2 * n, n>(M);
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      DT acc = c.xi[i][j];
+#pragma unroll
+      for (int k = 0; k < n; ++k) acc = acc + c.A[i][k] * (c.tl[k] * m[k][j]);
+      mo[i][j] = c.to[i] * acc;
+    }
+#pragma unroll
+    for (int j = 0; j < n; ++j) Lo[i][j] = dual_abs_scale(c.to[i], M[j][i]);
+  }
+}
+
+template <typename T, int NU, class F>
+__global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
+  constexpr int n = NU + 1;
+  constexpr int D = F::D;
+  constexpr int P = F::P;
+  constexpr int OUT = 1;
+  using DT = Dual<T, P>;
+  using DD = Dual<double, P>;
+  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= a.B) return;
+  const int num_obs = a.num_steps / a.save_every + 1;
+  constexpr int CF = 2 * n * n + n * D;  // duals per stored conditional (A, X, xi)
+  T* ws = reinterpret_cast<T*>(a.workspace) + b * int64_t(num_obs - 1) * (CF * (P + 1) + 2 * n);
+
+  // ---- parameters with unit tangents; Taylor-mode initial derivatives ----
+  DD pd[P];
+  DT pt[P];
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    pd[k] = DD(a.params[b * P + k]);
+    pd[k].g[k] = 1.0;
+    pt[k] = DT(T(pd[k].v));
+    pt[k].g[k] = T(1);
+  }
+  DD y0[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) y0[j] = DD(a.y0[b * D + j]);
+  DD tc[n][D];
+  taylor_init<F, NU>(y0, pd, tc);
+
+  DT m[n][D], L[n][n];
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      m[i][j].v = T(tc[i][j].v);
+#pragma unroll
+      for (int k = 0; k < P; ++k) m[i][j].g[k] = T(tc[i][j].g[k]);
+    }
+#pragma unroll
+    for (int j = 0; j < n; ++j) L[i][j] = DT(T(0));
+  }
+  LmlCond<T, P, NU, D> bw;
+  lml_cond_identity(bw);
+
+  // constants of the fixed step: p, p_inv, the noise factor sqrt(dt) Q1
+  const T h = T(a.dt);
+  T p[n], pinv[n];
+  precon<T, NU>(h, p, pinv);
+  const T sq = dev_sqrt(dev_abs(h));
+  const T damp = T(a.damp);
+
+  int status = PDQ_INSTANCE_OK;
+  for (int step = 1; step <= a.num_steps; ++step) {
+    // ---- fixed-point predict: transition.revert(marginal), merged into bw ----
+    DT M[2 * n][2 * n];
+#pragma unroll
+    for (int r = 0; r < n; ++r)
+#pragma unroll
+      for (int c = 0; c < n; ++c) {
+        M[r][c] = DT((r <= c) ? sq * T(a.q1[c][r]) : T(0));  // R_YX = (sqrt(dt) Q1)^T
+        M[r][n + c] = DT(T(0));
+        DT acc(T(0));
+#pragma unroll
+        for (int k = c; k < n; ++k) acc = acc + T(iwp_a<NU>(c, k)) * (dev_abs(pinv[k]) * L[k][r]);
+        M[n + r][c] = acc;                               // R_X_F = (A chol)^T
+        M[n + r][n + c] = dev_abs(pinv[c]) * L[c][r];   // R_X = chol^T
+      }
+    qr_qconst<T, P, 2 * n, 2 * n>(M);
+    // G^T = R_Y^{-1} R12 by back substitution through the triangle
+    DT Gt[n][n];
+#pragma unroll
+    for (int col = 0; col < n; ++col)
+#pragma unroll
+      for (int i = n - 1; i >= 0; --i) {
+        DT acc = M[i][n + col];
+#pragma unroll
+        for (int k = i + 1; k < n; ++k) acc = acc - M[i][k] * Gt[k][col];
+        Gt[i][col] = acc / M[i][i];
+      }
+    DT mean_l[n][D], mobs[n][D], mp[n][D], Lp[n][n];
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) mean_l[i][j] = pinv[i] * m[i][j];
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        DT acc(T(0));
+#pragma unroll
+        for (int k = i; k < n; ++k) acc = acc + T(iwp_a<NU>(i, k)) * mean_l[k][j];
+        mobs[i][j] = acc;
+        mp[i][j] = p[i] * acc;
+      }
+    LmlCond<T, P, NU, D> cn;  // the new backward conditional
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        DT acc = mean_l[i][j];
+#pragma unroll
+        for (int k = 0; k < n; ++k) acc = acc - Gt[k][i] * mobs[k][j];
+        cn.xi[i][j] = acc;
+      }
+#pragma unroll
+      for (int j = 0; j < n; ++j) {
+        cn.A[i][j] = Gt[j][i];
+        cn.X[i][j] = M[n + j][n + i];  // R_XY^T
+        Lp[i][j] = dual_abs_scale(p[i], M[j][i]);
+      }
+      cn.tl[i] = T(1) / p[i];
+      cn.to[i] = T(1) / pinv[i];
+    }
+    // merge: bw <- bw.merge(cn) (ssm_impl_isotropic.py:91-105)
+    {
+      T Tv[n];
+#pragma unroll
+      for (int i = 0; i < n; ++i) Tv[i] = bw.tl[i] * cn.to[i];
+      DT Mm[2 * n][n];
+      LmlCond<T, P, NU, D> out;
+#pragma unroll
+      for (int i = 0; i < n; ++i) {
+#pragma unroll
+        for (int j = 0; j < n; ++j) {
+          DT g(T(0)), r1(T(0));
+#pragma unroll
+          for (int k = 0; k < n; ++k) {
+            g = g + bw.A[i][k] * (Tv[k] * cn.A[k][j]);
+            r1 = r1 + bw.A[i][k] * (dev_abs(Tv[k]) * cn.X[k][j]);
+          }
+          out.A[i][j] = g;
+          Mm[j][i] = r1;
+          Mm[n + j][i] = bw.X[i][j];
+        }
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          DT x = bw.xi[i][j];
+#pragma unroll
+          for (int k = 0; k < n; ++k) x = x + bw.A[i][k] * (Tv[k] * cn.xi[k][j]);
+          out.xi[i][j] = x;
+        }
+      }
+      qr_qconst<T, P, 2 * n, n>(Mm);
+#pragma unroll
+      for (int i = 0; i < n; ++i) {
+#pragma unroll
+        for (int j = 0; j < n; ++j) out.X[i][j] = Mm[j][i];
+        out.tl[i] = cn.tl[i];
+        out.to[i] = bw.to[i];
+      }
+      bw = out;
+    }
+    // ---- TS0 linearisation at the predicted mean; update (Givens, H = e_1) ----
+    DT f[D];
+    F::eval(mp[0], pt, f);
+    DT Mu[n + 1][n + 1];
+#pragma unroll
+    for (int c = 0; c <= n; ++c) Mu[0][c] = DT(c == 0 ? damp : T(0));
+#pragma unroll
+    for (int r = 1; r <= n; ++r) {
+      Mu[r][0] = Lp[OUT][r - 1];
+#pragma unroll
+      for (int c = 1; c <= n; ++c) Mu[r][c] = Lp[c - 1][r - 1];
+    }
+#pragma unroll
+    for (int r = OUT + 1; r >= 1; --r) givens_qconst<T, P, n + 1, n + 1>(Mu, r - 1, r, 0);
+#pragma unroll
+    for (int c = 1; c <= OUT; ++c) givens_qconst<T, P, n + 1, n + 1>(Mu, c, c + 1, c);
+    DT res[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) res[j] = mp[OUT][j] - f[j];
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+      const DT g = Mu[0][i + 1] / Mu[0][0];
+#pragma unroll
+      for (int j = 0; j < D; ++j) m[i][j] = mp[i][j] - g * res[j];
+#pragma unroll
+      for (int j = 0; j < n; ++j) L[i][j] = Mu[j + 1][i + 1];
+    }
+    if (!(m[0][0].v == m[0][0].v)) {
+      status = PDQ_INSTANCE_NONFINITE;
+      break;
+    }
+    // ---- checkpoint at an observation: store the conditional, reset ----
+    if (step % a.save_every == 0) {
+      T* dst = ws + int64_t(step / a.save_every - 1) * (CF * (P + 1) + 2 * n);
+      int o = 0;
+#pragma unroll
+      for (int i = 0; i < n; ++i)
+#pragma unroll
+        for (int j = 0; j < n; ++j) {
+          dst[o++] = bw.A[i][j].v;
+#pragma unroll
+          for (int k = 0; k < P; ++k) dst[o++] = bw.A[i][j].g[k];
+          dst[o++] = bw.X[i][j].v;
+#pragma unroll
+          for (int k = 0; k < P; ++k) dst[o++] = bw.X[i][j].g[k];
+        }
+#pragma unroll
+      for (int i = 0; i < n; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          dst[o++] = bw.xi[i][j].v;
+#pragma unroll
+          for (int k = 0; k < P; ++k) dst[o++] = bw.xi[i][j].g[k];
+        }
+#pragma unroll
+      for (int i = 0; i < n; ++i) {
+        dst[o++] = bw.tl[i];
+        dst[o++] = bw.to[i];
+      }
+      lml_cond_identity(bw);
+    }
+  }
+
+  // ---- LML: reverse Kalman filter over the data (evaluate_lml) ----
+  DD pdf(0.0);
+  if (status == PDQ_INSTANCE_OK) {
+    // rv_at_t1 = posterior1.conditional.marginalise(marginal); the last step
+    // lands on the last observation, so that conditional is the identity
+    DT rm[n][D], rL[n][n];
+    lml_marginalise<T, P, NU, D>(bw, m, L, rm, rL);
+    const double LOG2PI = 1.8378770664093453;
+    int num = 0;
+    for (int k = num_obs - 1; k >= 0; --k) {
+      if (k < num_obs - 1) {
+        LmlCond<T, P, NU, D> c;
+        const T* src = ws + int64_t(k) * (CF * (P + 1) + 2 * n);
+        int o = 0;
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            c.A[i][j].v = src[o++];
+            for (int q = 0; q < P; ++q) c.A[i][j].g[q] = src[o++];
+            c.X[i][j].v = src[o++];
+            for (int q = 0; q < P; ++q) c.X[i][j].g[q] = src[o++];
+          }
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < D; ++j) {
+            c.xi[i][j].v = src[o++];
+            for (int q = 0; q < P; ++q) c.xi[i][j].g[q] = src[o++];
+          }
+        for (int i = 0; i < n; ++i) {
+          c.tl[i] = src[o++];
+          c.to[i] = src[o++];
+        }
+        DT pm[n][D], pL[n][n];
+        lml_marginalise<T, P, NU, D>(c, rm, rL, pm, pL);
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+#pragma unroll
+          for (int j = 0; j < D; ++j) rm[i][j] = pm[i][j];
+#pragma unroll
+          for (int j = 0; j < n; ++j) rL[i][j] = pL[i][j];
+        }
+      }
+      // model_k = to_derivative(0, std_k); bayes_rule_and_logpdf_tree
+      const T s = T(a.std[k]);
+      DT Mo[n + 1][n + 1];
+#pragma unroll
+      for (int c = 0; c <= n; ++c) Mo[0][c] = DT(c == 0 ? s : T(0));
+#pragma unroll
+      for (int r = 1; r <= n; ++r) {
+        Mo[r][0] = rL[0][r - 1];
+#pragma unroll
+        for (int c = 1; c <= n; ++c) Mo[r][c] = rL[c - 1][r - 1];
+      }
+      givens_qconst<T, P, n + 1, n + 1>(Mo, 0, 1, 0);
+      const DT ry = Mo[0][0];
+      // logpdf of the observed N(m[0], ry^2) at the data, summed over d
+      DD pdf_n(0.0);
+      DT ginv[n];
+#pragma unroll
+      for (int i = 0; i < n; ++i) ginv[i] = Mo[0][i + 1] / ry;
+      const T ryv = ry.v < T(0) ? -ry.v : ry.v;
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        const DT dx = DT(T(a.data[int64_t(k) * D + j])) - rm[0][j];
+        const DT w = dx / ry;
+        pdf_n.v += -0.5 * (2.0 * log(double(ryv)) + double(w.v) * double(w.v) + LOG2PI);
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+          pdf_n.g[q] += -0.5 * (2.0 * double(ry.g[q]) / double(ry.v) + 2.0 * double(w.v) * double(w.g[q]));
+#pragma unroll
+        for (int i = 0; i < n; ++i) rm[i][j] = rm[i][j] + ginv[i] * dx;
+      }
+#pragma unroll
+      for (int i = 0; i < n; ++i)
+#pragma unroll
+        for (int j = 0; j < n; ++j) rL[i][j] = Mo[j + 1][i + 1];
+      if (a.average_pdfs && num > 0) {
+        pdf.v = (pdf.v * num + pdf_n.v) / (num + 1);
+#pragma unroll
+        for (int q = 0; q < P; ++q) pdf.g[q] = (pdf.g[q] * num + pdf_n.g[q]) / (num + 1);
+      } else {
+        pdf.v += pdf_n.v;
+#pragma unroll
+        for (int q = 0; q < P; ++q) pdf.g[q] += pdf_n.g[q];
+      }
+      ++num;
+    }
+    if (!(pdf.v == pdf.v)) status = PDQ_INSTANCE_NONFINITE;
+  }
+  const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+  a.lml[b] = status == PDQ_INSTANCE_OK ? pdf.v : nan;
+  if (a.grad) {
+#pragma unroll
+    for (int q = 0; q < P; ++q) a.grad[b * P + q] = status == PDQ_INSTANCE_OK ? pdf.g[q] : nan;
+  }
+  a.status[b] = status;
+}
+
+}  // namespace pdq

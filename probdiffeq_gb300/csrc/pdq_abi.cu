@@ -5,6 +5,7 @@
 
 #include "bd_launch.cuh"
 #include "dense_launch.cuh"
+#include "lml_launch.cuh"
 #include "iso_launch.cuh"
 #include "pdq.h"
 
@@ -326,6 +327,75 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
   }
   return PDQ_ERROR_UNSUPPORTED;
+}
+
+static pdq_status lml_check(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every) {
+  pdq_status st = validate_common(c);
+  if (st != PDQ_SUCCESS) return st;
+  if (c->ssm != PDQ_SSM_ISOTROPIC || c->constraint != PDQ_CONSTRAINT_TS0 || c->strategy != PDQ_STRATEGY_FIXEDPOINT ||
+      c->solver != PDQ_SOLVER_PLAIN)
+    return PDQ_ERROR_UNSUPPORTED;
+  if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
+  if (c->field != PDQ_FIELD_FITZHUGH_NAGUMO && c->field != PDQ_FIELD_LOTKA_VOLTERRA) return PDQ_ERROR_UNSUPPORTED;
+  if (c->field == PDQ_FIELD_LOTKA_VOLTERRA && c->precision != PDQ_PRECISION_F64) return PDQ_ERROR_UNSUPPORTED;
+  if (B < 0 || num_steps < 1 || save_every < 1 || num_steps % save_every != 0) return PDQ_ERROR_INVALID_VALUE;
+  return PDQ_SUCCESS;
+}
+
+static size_t lml_bytes(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every) {
+  const int n = c->num_derivatives + 1, d = c->ode_dim;
+  const int P = c->field == PDQ_FIELD_FITZHUGH_NAGUMO ? 3 : 4;
+  const size_t per = size_t(2 * n * n + n * d) * (P + 1) + 2 * n;
+  const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
+  return size_t(B) * size_t(num_steps / save_every) * per * elem;
+}
+
+pdq_status pdq_lml_workspace_size(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every, size_t* bytes) {
+  if (bytes == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  pdq_status st = lml_check(c, B, num_steps, save_every);
+  if (st != PDQ_SUCCESS) return st;
+  *bytes = lml_bytes(c, B, num_steps, save_every);
+  return PDQ_SUCCESS;
+}
+
+pdq_status pdq_lml_fixed_grid(const pdq_config* c, const pdq_lml_args* args, void* workspace, size_t workspace_bytes,
+                              void* stream_ptr) {
+  if (args == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  pdq_status st = lml_check(c, args->num_instances, args->num_steps, args->save_every);
+  if (st != PDQ_SUCCESS) return st;
+  if (args->num_instances == 0) return PDQ_SUCCESS;
+  if (!args->params || !args->y0 || !args->data || !args->std || !args->lml || !args->status ||
+      (args->with_gradient && !args->grad) || !(args->dt > 0))
+    return PDQ_ERROR_INVALID_VALUE;
+  if (workspace == nullptr || workspace_bytes < lml_bytes(c, args->num_instances, args->num_steps, args->save_every))
+    return PDQ_ERROR_WORKSPACE;
+  pdq::LmlArgs a;
+  memset(&a, 0, sizeof(a));
+  a.B = args->num_instances;
+  a.num_steps = args->num_steps;
+  a.save_every = args->save_every;
+  a.average_pdfs = args->average_pdfs ? 1 : 0;
+  a.with_gradient = args->with_gradient ? 1 : 0;
+  a.t0 = args->t0;
+  a.dt = args->dt;
+  a.damp = c->damp;
+  iwp_q1(c->num_derivatives, a.q1);
+  a.params = args->params;
+  a.y0 = args->y0;
+  a.data = args->data;
+  a.std = args->std;
+  a.lml = args->lml;
+  a.grad = args->with_gradient ? args->grad : nullptr;
+  a.status = args->status;
+  a.workspace = workspace;
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+  cudaError_t err;
+  if (c->field == PDQ_FIELD_FITZHUGH_NAGUMO)
+    err = c->precision == PDQ_PRECISION_F64 ? pdq_launch_lml_fhn_f64(a, c->num_derivatives, stream)
+                                            : pdq_launch_lml_fhn_f32(a, c->num_derivatives, stream);
+  else
+    err = pdq_launch_lml_lv_f64(a, c->num_derivatives, stream);
+  return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
 }
 
 }  // extern "C"

@@ -193,6 +193,18 @@ struct Dual {
 #pragma unroll
     for (int k = 0; k < K; ++k) g[k] = T(0);
   }
+  PDQ_HD Dual& operator+=(const Dual& o) {
+    v += o.v;
+#pragma unroll
+    for (int k = 0; k < K; ++k) g[k] += o.g[k];
+    return *this;
+  }
+  PDQ_HD Dual& operator-=(const Dual& o) {
+    v -= o.v;
+#pragma unroll
+    for (int k = 0; k < K; ++k) g[k] -= o.g[k];
+    return *this;
+  }
 };
 
 template <typename T, int K>

@@ -48,7 +48,9 @@ def oracle_bd(u0, t1, solver="dynamic", atol=1e-4, rtol=1e-4, dtype=torch.float6
     pt = p.to(dtype)
     c = S.constraint_ode_ts0(lambda u, t: problems.burgers(u[0], pt))
     cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE, "none": solvers.SolverPlain}[solver]
-    return solvers.solve_adaptive_terminal_values(cls(solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c), prior, 0.0, t1, atol, rtol)
+    return solvers.solve_adaptive_terminal_values(
+        cls(solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c), prior, 0.0, t1, atol, rtol, dt0=0.1 * t1
+    )
 
 
 def gpu_bd(u0s, t1, precision, solver="dynamic", atol=1e-4, rtol=1e-4):
