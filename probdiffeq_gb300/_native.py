@@ -41,7 +41,7 @@ class PdqConfig(ctypes.Structure):
         ("ode_dim", ctypes.c_int32),
         ("clip_dt", ctypes.c_int32),
         ("correct_asymptotic_underconfidence", ctypes.c_int32),
-        ("reserved0", ctypes.c_int32),
+        ("kernel_variant", ctypes.c_int32),
         ("safety", ctypes.c_double),
         ("factor_min", ctypes.c_double),
         ("factor_max", ctypes.c_double),
@@ -215,7 +215,8 @@ def solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream
         lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), _ptr(ws), ctypes.c_size_t(ws_bytes), _stream_handle(stream)),
         "pdq_solve_adaptive",
     )
-    outputs["_workspace"] = ws
+    if ws is not None:
+        outputs["_workspace"] = ws
     return outputs
 
 

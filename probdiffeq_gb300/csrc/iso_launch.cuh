@@ -2,8 +2,32 @@
 #pragma once
 
 #include "iso_solver.cuh"
+#include "iso_warp.cuh"
 
 namespace pdq {
+
+// Lanes per instance of the warp-cooperative kernel.
+constexpr int kIsoLanes = 8;
+
+// minb: 2 lets the compiler use up to 128 registers per lane (no spills),
+// 3 caps it at 85 (more resident warps, a few spills to L1).
+template <typename T, int NU, class F>
+cudaError_t launch_iso_warp_nu(const IsoArgs& a, int minb, cudaStream_t stream) {
+  const int block = 256;
+  const int64_t threads = a.B * kIsoLanes;
+  const unsigned grid = unsigned((threads + block - 1) / block);
+  cudaError_t e;
+  if (minb == 3) {
+    e = ensure_stack<iso_warp_kernel<T, NU, F, kIsoLanes, 3>>();
+    if (e != cudaSuccess) return e;
+    iso_warp_kernel<T, NU, F, kIsoLanes, 3><<<grid, block, 0, stream>>>(a);
+  } else {
+    e = ensure_stack<iso_warp_kernel<T, NU, F, kIsoLanes, 2>>();
+    if (e != cudaSuccess) return e;
+    iso_warp_kernel<T, NU, F, kIsoLanes, 2><<<grid, block, 0, stream>>>(a);
+  }
+  return cudaGetLastError();
+}
 
 template <typename T, int NU, class F>
 cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
@@ -18,6 +42,17 @@ cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, in
 
 template <typename T, class F>
 cudaError_t launch_iso_precision(const IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block) {
+  if (block <= 0) {  // lane-cooperative variant (clip_dt only); -block = min blocks per SM
+    const int minb = -block;
+    switch (nu) {
+      case 1: return launch_iso_warp_nu<T, 1, F>(a, minb, stream);
+      case 2: return launch_iso_warp_nu<T, 2, F>(a, minb, stream);
+      case 3: return launch_iso_warp_nu<T, 3, F>(a, minb, stream);
+      case 4: return launch_iso_warp_nu<T, 4, F>(a, minb, stream);
+      case 5: return launch_iso_warp_nu<T, 5, F>(a, minb, stream);
+      default: return cudaErrorInvalidValue;
+    }
+  }
   switch (nu) {
     case 1: return launch_iso_nu<T, 1, F>(a, interp, stream, block);
     case 2: return launch_iso_nu<T, 2, F>(a, interp, stream, block);

@@ -179,7 +179,13 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.num_attempts = args->num_attempts;
     a.status = args->status;
     const bool interp = !c->clip_dt;
-    const int block = 64;
+    if (c->kernel_variant < 0 || c->kernel_variant > 3) return PDQ_ERROR_INVALID_VALUE;
+    // 0 selects the lane-cooperative kernel (8 lanes, <= 85 registers) where it
+    // applies (exact checkpoint landings); 1 one thread per instance; 2 / 3 the
+    // lane-cooperative kernel with <= 128 / <= 85 registers per lane
+    const bool warp = c->clip_dt && c->kernel_variant != 1;
+    if (c->kernel_variant >= 2 && !c->clip_dt) return PDQ_ERROR_UNSUPPORTED;
+    const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : 64;
     const bool f64 = c->precision == PDQ_PRECISION_F64;
     cudaError_t err;
     switch (c->field) {

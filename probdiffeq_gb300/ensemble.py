@@ -36,6 +36,7 @@ def make_config(
     exponent_integral=0.3,
     exponent_proportional=0.4,
     max_attempts=DEFAULT_MAX_ATTEMPTS,
+    kernel_variant=0,
 ):
     """Build a ``pdq_config`` (include/pdq.h) from keyword arguments."""
     cfg = _native.config_default(ssm, field, num_derivatives, ode_dim)
@@ -50,6 +51,7 @@ def make_config(
     cfg.safety, cfg.factor_min, cfg.factor_max = float(safety), float(factor_min), float(factor_max)
     cfg.exponent_integral, cfg.exponent_proportional = float(exponent_integral), float(exponent_proportional)
     cfg.max_attempts = int(max_attempts)
+    cfg.kernel_variant = {"auto": 0, "thread": 1, "lanes": 2, "lanes_compact": 3}.get(kernel_variant, kernel_variant)
     return cfg
 
 

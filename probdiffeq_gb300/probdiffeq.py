@@ -1,0 +1,290 @@
+"""Constructors of the probabilistic solver, mirroring ``probdiffeq.probdiffeq``.
+
+Same names and keyword signatures as the reference's public namespace
+(``probdiffeq/probdiffeq.py:6-17``): state-space-model factories, priors,
+constraints, strategies, solvers, error estimators, Taylor-mode
+initialisation and the LML loss.  The objects are descriptions; solving
+happens in one native call (``probdiffeq_gb300.ivpsolve``), so the shapes of
+a batch of instances (the reference's ``jax.vmap`` axis) are the leading axis
+of ``y0`` and of the vector-field parameters.
+
+Vector fields are registered device functors (``ode("lotka_volterra",
+params)``) rather than Python callables: the whole solve runs on the GPU.
+"""
+
+import dataclasses
+from typing import Any, Optional
+
+import torch
+
+from . import _native
+
+__all__ = [
+    "ode",
+    "Field",
+    "jetexpand_ode_padded_scan",
+    "jetexpand_ode_unroll",
+    "state_space_model_isotropic",
+    "state_space_model_blockdiag",
+    "state_space_model_dense",
+    "strategy_filter",
+    "strategy_smoother_fixedpoint",
+    "solver",
+    "solver_mle",
+    "solver_dynamic",
+    "error_residual_std",
+    "jacobian_materialize",
+    "loss_lml_timeseries",
+]
+
+_FIELD_DIMS = {"lotka_volterra": 2, "van_der_pol": 2, "fitzhugh_nagumo": 2, "burgers": None}
+_FIELD_PARAMS = {"lotka_volterra": 4, "van_der_pol": 1, "fitzhugh_nagumo": 3, "burgers": 1}
+
+
+@dataclasses.dataclass(frozen=True)
+class Field:
+    """A registered first-order autonomous vector field u' = f(u; params).
+
+    ``params`` has shape (P,) or (B, P) for a batch of instances.
+    Corresponds to ``probdiffeq.ode`` (``_probdiffeq/problems.py:283-295``):
+    one Taylor coefficient in, the output is coefficient 1.
+    """
+
+    name: str
+    params: Any
+    jacobian: Any = None
+    num_tcoeffs_in_args: int = 1
+    tcoeff_indices_output: tuple = (1,)
+
+
+def ode(name, params, *, jacobian=None):
+    """Describe u' = f(u) with a registered device field (problems.py:283-295)."""
+    if name not in _FIELD_DIMS:
+        raise ValueError(f"unknown vector field {name!r}; registered: {sorted(_FIELD_DIMS)}")
+    params = torch.as_tensor(params, dtype=torch.float64)
+    if params.shape[-1] != _FIELD_PARAMS[name]:
+        raise ValueError(f"{name} takes {_FIELD_PARAMS[name]} parameters, got shape {tuple(params.shape)}")
+    return Field(name, params, jacobian)
+
+
+class jacobian_materialize:
+    """Materialised Jacobians (jacobians.py:78-113); the device fields supply them exactly."""
+
+
+@dataclasses.dataclass(frozen=True)
+class TaylorCoefficients:
+    """Taylor-mode initial derivatives u(t0), ..., u^(num)(t0), computed on the device.
+
+    Holds the initial values and the order; the derivatives themselves are
+    produced inside the solver kernels (jet recursion on the registered field).
+    """
+
+    field: Field
+    y0: torch.Tensor  # (d,) or (B, d)
+    num: int
+
+    def __len__(self):
+        return self.num + 1
+
+
+class _JetExpand:
+    def __init__(self, num):
+        if num < 1:
+            raise ValueError("num must be positive")
+        self.num = num
+
+    def __call__(self, vf, inits, /, *, t=0.0):
+        """jetexpand_ode_*(num)(vf, (u0,), t=t0) -> (tcoeffs, info) (jet_expansion_algorithms.py:49-152)."""
+        if not isinstance(vf, Field):
+            raise TypeError("vf must come from probdiffeq_gb300.probdiffeq.ode(...)")
+        (u0,) = inits
+        return TaylorCoefficients(vf, torch.as_tensor(u0, dtype=torch.float64), self.num), {}
+
+
+def jetexpand_ode_padded_scan(*, num):
+    """Taylor-mode initialisation (jet_expansion_algorithms.py:49-103)."""
+    return _JetExpand(num)
+
+
+def jetexpand_ode_unroll(*, num):
+    """Taylor-mode initialisation (jet_expansion_algorithms.py:110-152)."""
+    return _JetExpand(num)
+
+
+@dataclasses.dataclass(frozen=True)
+class Prior:
+    """An integrated Wiener process prior (ssm_impl_*.py prior_wiener_integrated)."""
+
+    ssm: str
+    tcoeffs: TaylorCoefficients
+
+    @property
+    def num_derivatives(self):
+        return self.tcoeffs.num
+
+
+@dataclasses.dataclass(frozen=True)
+class Constraint:
+    ssm: str
+    kind: str  # "ts0" | "ts1"
+    field: Field
+    residual_order: int = 2
+
+
+class _StateSpaceModel:
+    name = ""
+
+    def prior_wiener_integrated(self, tcoeffs, /, *, is_exact=True, inexact_eps=1e-6, diffuse_derivatives=0,
+                                diffuse_eps=1.0, output_scale=None):
+        """IWP prior from exact Taylor coefficients (ssm_impl_isotropic.py:409-482)."""
+        if not isinstance(tcoeffs, TaylorCoefficients):
+            raise TypeError("tcoeffs must come from jetexpand_ode_padded_scan(...)(vf, (u0,))")
+        if is_exact is not True or diffuse_derivatives or output_scale is not None:
+            raise NotImplementedError("only exact initial coefficients with the default output scale are native")
+        return Prior(self.name, tcoeffs)
+
+    def constraint_ode_ts0(self, ode, /):
+        if not isinstance(ode, Field):
+            raise TypeError(ode)
+        return Constraint(self.name, "ts0", ode)
+
+    def constraint_ode_ts1(self, ode, /, taylor_point=None):
+        if not isinstance(ode, Field):
+            raise TypeError(ode)
+        if self.name != "dense":
+            raise NotImplementedError("TS1 is native for the dense factorisation")
+        if taylor_point is not None:
+            raise NotImplementedError("only the prior-mean Taylor point (taylor_point_prior) is native")
+        return Constraint(self.name, "ts1", ode)
+
+
+class state_space_model_isotropic(_StateSpaceModel):
+    """Isotropic factorisation (ssm_impl_isotropic.py:406-584)."""
+
+    name = "isotropic"
+
+
+class state_space_model_blockdiag(_StateSpaceModel):
+    """Block-diagonal factorisation (ssm_impl_blockdiag.py:460-654)."""
+
+    name = "blockdiag"
+
+
+class state_space_model_dense(_StateSpaceModel):
+    """Dense factorisation (ssm_impl_dense.py:455-732)."""
+
+    name = "dense"
+
+
+class strategy_filter:
+    """estimators_and_losses.py:347-421."""
+
+    name = "filter"
+    is_suitable_for_save_at = True
+    is_suitable_for_save_every_step = True
+
+
+class strategy_smoother_fixedpoint:
+    """estimators_and_losses.py:473-591."""
+
+    name = "fixedpoint"
+    is_suitable_for_save_at = True
+    is_suitable_for_save_every_step = False
+
+
+@dataclasses.dataclass(frozen=True)
+class _Solver:
+    strategy: Any
+    constraint: Constraint
+    kind: str
+    correct_asymptotic_underconfidence: bool = True
+
+    @property
+    def is_suitable_for_save_at(self):
+        return self.strategy.is_suitable_for_save_at
+
+    @property
+    def is_suitable_for_save_every_step(self):
+        return self.strategy.is_suitable_for_save_every_step
+
+
+def solver(*, strategy, constraint, constraint_init=None):
+    """Uncalibrated solver (solvers.py:636-767)."""
+    if constraint_init is not None:
+        raise NotImplementedError("constraint_init is not native")
+    return _Solver(strategy, constraint, "none")
+
+
+def solver_mle(*, strategy, constraint, constraint_init=None, correct_asymptotic_underconfidence=True):
+    """MLE calibration (solvers.py:318-480)."""
+    if constraint_init is not None:
+        raise NotImplementedError("constraint_init is not native")
+    return _Solver(strategy, constraint, "mle", correct_asymptotic_underconfidence)
+
+
+def solver_dynamic(*, strategy, constraint, constraint_init=None, re_linearize_after_calibration=False,
+                   stop_gradient_through_calibration=True):
+    """Dynamic calibration (solvers.py:483-633)."""
+    if constraint_init is not None or re_linearize_after_calibration:
+        raise NotImplementedError("constraint_init / re-linearisation are not native")
+    return _Solver(strategy, constraint, "dynamic")
+
+
+@dataclasses.dataclass(frozen=True)
+class error_residual_std:
+    """Residual-std error estimate (solvers.py:850-996), cached linearisation."""
+
+    constraint: Constraint
+    error_norm: Optional[Any] = None
+    re_linearize_before_error: bool = False
+    error_per_unit_step: bool = False
+
+    def __post_init__(self):
+        if self.error_norm is not None or self.re_linearize_before_error or self.error_per_unit_step:
+            raise NotImplementedError("only the default error_residual_std is native")
+
+
+@dataclasses.dataclass(frozen=True)
+class loss_lml_timeseries:
+    """LML of time-series data (estimators_and_losses.py:53-105).
+
+    Natively evaluated together with the solve by ``ivpsolve.lml_fixed_grid``.
+    """
+
+    average_pdfs: bool = True
+    tcoeff_index: int = 0
+
+    def __post_init__(self):
+        if self.tcoeff_index != 0:
+            raise NotImplementedError("observations of the solution (tcoeff_index=0) only")
+
+
+def _field_dim(field, y0):
+    d = _FIELD_DIMS[field.name]
+    return y0.shape[-1] if d is None else d
+
+
+def lower(solver_obj, error, control, *, num_derivatives, y0, precision, atol, rtol, clip_dt, eps, damp):
+    """Lower constructor objects to a pdq_config (include/pdq.h)."""
+    from . import ensemble
+    from .ivpsolve import control_integral, control_proportional_integral
+
+    c = solver_obj.constraint
+    if error is not None and error.constraint is not c:
+        raise ValueError("the error estimator must use the solver's constraint")
+    ctrl = control if control is not None else control_integral()
+    kw = dict(safety=ctrl.safety, factor_min=ctrl.factor_min, factor_max=ctrl.factor_max)
+    if isinstance(ctrl, control_proportional_integral):
+        kw.update(control="proportional_integral", exponent_integral=ctrl.exponent_integral,
+                  exponent_proportional=ctrl.exponent_proportional)
+    else:
+        kw.update(control="integral")
+    return ensemble.make_config(
+        field=c.field.name, num_derivatives=num_derivatives, ode_dim=_field_dim(c.field, y0), ssm=c.ssm,
+        constraint=c.kind, strategy=solver_obj.strategy.name, solver=solver_obj.kind, precision=precision,
+        atol=atol, rtol=rtol, clip_dt=clip_dt, eps=eps, damp=damp,
+        correct_asymptotic_underconfidence=solver_obj.correct_asymptotic_underconfidence, **kw,
+    )
+
+
+_native_status = _native.INSTANCE_STATUS
