@@ -113,11 +113,30 @@ PDQ_D void iso_predict_chol(const double (&q1)[kMaxN][kMaxN], const T (&L)[NU + 
 #pragma unroll
     for (int i = 0; i <= c; ++i) nrm2 += U[i][c] * U[i][c];
     const T alpha = X[c][c];
+    T nrm;
+    if (norm2_out_of_range(nrm2)) {
+      T sc = T(0);
+#pragma unroll
+      for (int r = c; r < n; ++r) sc = fmax(sc, dev_abs(X[r][c]));
+#pragma unroll
+      for (int i = 0; i <= c; ++i) sc = fmax(sc, dev_abs(U[i][c]));
+      T acc = T(0);
+      if (sc > T(0)) {
+        const T inv = T(1) / sc;
+#pragma unroll
+        for (int r = c; r < n; ++r) acc += (X[r][c] * inv) * (X[r][c] * inv);
+#pragma unroll
+        for (int i = 0; i <= c; ++i) acc += (U[i][c] * inv) * (U[i][c] * inv);
+      }
+      nrm = sc * dev_sqrt(acc);
+      nrm2 = nrm > T(0) ? T(1) : T(0);
+    } else {
+      nrm = dev_sqrt(nrm2);
+    }
     if (nrm2 > T(0)) {
-      const T nrm = dev_sqrt(nrm2);
       const T beta = alpha >= T(0) ? -nrm : nrm;
       const T v0 = alpha - beta;
-      const T tau = dev_div(beta - alpha, beta);
+      const T tau = (beta - alpha) / beta;
       const T vinv = dev_rcp(v0);
       // normalised reflector v = [1, X[c+1..][c]/v0, U[0..c][c]/v0]
 #pragma unroll

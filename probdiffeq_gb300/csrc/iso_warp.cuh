@@ -26,6 +26,23 @@ PDQ_D T shfl(unsigned mask, T v, int src, int width) {
   return __shfl_sync(mask, v, src, width);
 }
 
+// Rotation (cs, sn) taking (x, y) to (r, 0); identity for x = y = 0; the
+// squares are rescaled when they leave the normal range.
+template <typename T>
+PDQ_D void givens_params(T x, T y, T& cs, T& sn) {
+  T r2 = x * x + y * y;
+  if (norm2_out_of_range(r2)) {
+    const T sc = dev_fmax_abs(x, y);
+    if (!(sc > T(0))) return;
+    x = x / sc;
+    y = y / sc;
+    r2 = x * x + y * y;
+  }
+  const T inv = dev_rsqrt(r2);
+  cs = x * inv;
+  sn = y * inv;
+}
+
 template <typename T, int NU, class F, int LPI, int MINB>
 __global__ void __launch_bounds__(256, MINB) iso_warp_kernel(IsoArgs a) {
   constexpr int n = NU + 1;
@@ -148,12 +165,31 @@ __global__ void __launch_bounds__(256, MINB) iso_warp_kernel(IsoArgs a) {
           for (int r = c; r < n; ++r) nrm2 += cx[r] * cx[r];
 #pragma unroll
           for (int i = 0; i <= c; ++i) nrm2 += cu[i] * cu[i];
+          T nrm;
+          if (norm2_out_of_range(nrm2)) {
+            T sc = T(0);
+#pragma unroll
+            for (int r = c; r < n; ++r) sc = fmax(sc, dev_abs(cx[r]));
+#pragma unroll
+            for (int i = 0; i <= c; ++i) sc = fmax(sc, dev_abs(cu[i]));
+            T acc = T(0);
+            if (sc > T(0)) {
+              const T inv = T(1) / sc;
+#pragma unroll
+              for (int r = c; r < n; ++r) acc += (cx[r] * inv) * (cx[r] * inv);
+#pragma unroll
+              for (int i = 0; i <= c; ++i) acc += (cu[i] * inv) * (cu[i] * inv);
+            }
+            nrm = sc * dev_sqrt(acc);
+            nrm2 = nrm > T(0) ? T(1) : T(0);
+          } else {
+            nrm = dev_sqrt(nrm2);
+          }
           if (nrm2 > T(0)) {
             const T alpha = cx[c];
-            const T nrm = dev_sqrt(nrm2);
             beta = alpha >= T(0) ? -nrm : nrm;
             v0inv = dev_rcp(alpha - beta);
-            tau = dev_div(beta - alpha, beta);
+            tau = (beta - alpha) / beta;
             active = true;
           }
         }
@@ -205,13 +241,7 @@ __global__ void __launch_bounds__(256, MINB) iso_warp_kernel(IsoArgs a) {
       for (int r = OUT + 1; r >= 1; --r) {
         T cs = T(1), sn = T(0);
         if (l == n) {
-          const T x = mc[r - 1], y = mc[r];
-          const T r2 = x * x + y * y;
-          if (r2 > T(0)) {
-            const T inv = dev_rsqrt(r2);
-            cs = x * inv;
-            sn = y * inv;
-          }
+          givens_params(mc[r - 1], mc[r], cs, sn);
         }
         cs = shfl(mask, cs, n, LPI);
         sn = shfl(mask, sn, n, LPI);
@@ -224,13 +254,7 @@ __global__ void __launch_bounds__(256, MINB) iso_warp_kernel(IsoArgs a) {
       for (int c = 1; c <= OUT; ++c) {
         T cs = T(1), sn = T(0);
         if (l == c - 1) {
-          const T x = mc[c], y = mc[c + 1];
-          const T r2 = x * x + y * y;
-          if (r2 > T(0)) {
-            const T inv = dev_rsqrt(r2);
-            cs = x * inv;
-            sn = y * inv;
-          }
+          givens_params(mc[c], mc[c + 1], cs, sn);
         }
         cs = shfl(mask, cs, c - 1, LPI);
         sn = shfl(mask, sn, c - 1, LPI);

@@ -69,6 +69,17 @@ PDQ_D double dev_rcp(double a) { return 1.0 / a; }
 PDQ_D float dev_fpow(float x, float y) { return __powf(x, y); }
 PDQ_D double dev_fpow(double x, double y) { return pow(x, y); }
 
+// Sums of squares leave the normal range of T for entries beyond ~1e19
+// (float) or below ~1e-19; the QR and rotation kernels then recompute the
+// norm with scaling (as LAPACK's geqrf does).  The common case costs one test.
+PDQ_D bool norm2_out_of_range(float s) { return !(s < 1e36f) || s < 1e-30f; }
+PDQ_D bool norm2_out_of_range(double s) { return !(s < 1e300) || s < 1e-290; }
+
+template <typename T>
+PDQ_D T dev_fmax_abs(T a, T b) {
+  return fmax(dev_abs(a), dev_abs(b));
+}
+
 template <int K>
 struct Factorial {
   static constexpr double value = K * Factorial<K - 1>::value;
@@ -363,10 +374,22 @@ PDQ_HD void taylor_init(const T* y0, const T* p, T (&out)[NU + 1][F::D]) {
 template <typename T, int NR, int NC>
 PDQ_D void givens_rows(T (&M)[NR][NC], int a, int b, int c0) {
   const T x = M[a][c0], y = M[b][c0];
-  const T r2 = x * x + y * y;
-  if (r2 > T(0)) {
+  T r2 = x * x + y * y;
+  T cs, sn;
+  if (norm2_out_of_range(r2)) {
+    const T s = dev_fmax_abs(x, y);
+    if (!(s > T(0))) return;
+    const T xs = x / s, ys = y / s;
+    const T inv = dev_rsqrt(xs * xs + ys * ys);
+    cs = xs * inv;
+    sn = ys * inv;
+    r2 = T(1);
+  } else {
     const T inv = dev_rsqrt(r2);
-    const T cs = x * inv, sn = y * inv;
+    cs = x * inv;
+    sn = y * inv;
+  }
+  if (r2 > T(0)) {
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
       if (j >= c0) {
@@ -389,9 +412,24 @@ PDQ_D void householder_r(T (&M)[NR][NC]) {
     T nrm2 = T(0);
 #pragma unroll
     for (int r = c; r < NR; ++r) nrm2 += M[r][c] * M[r][c];
+    T nrm;
+    if (norm2_out_of_range(nrm2)) {
+      T sc = T(0);
+#pragma unroll
+      for (int r = c; r < NR; ++r) sc = fmax(sc, dev_abs(M[r][c]));
+      T acc = T(0);
+      if (sc > T(0)) {
+        const T inv = T(1) / sc;
+#pragma unroll
+        for (int r = c; r < NR; ++r) acc += (M[r][c] * inv) * (M[r][c] * inv);
+      }
+      nrm = sc * dev_sqrt(acc);
+      nrm2 = nrm > T(0) ? T(1) : T(0);
+    } else {
+      nrm = dev_sqrt(nrm2);
+    }
     if (nrm2 > T(0)) {
       const T alpha = M[c][c];
-      const T nrm = dev_sqrt(nrm2);
       const T beta = alpha >= T(0) ? -nrm : nrm;
       const T vinv = dev_rcp(alpha - beta);
       const T tau = dev_div(beta - alpha, beta);
