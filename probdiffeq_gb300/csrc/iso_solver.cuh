@@ -17,8 +17,9 @@
 // the entire solve; global memory is touched only to read the instance's
 // inputs once and to write one record per checkpoint.
 //
-// Precision: T (float or double) for the bulk arithmetic; time, step size,
-// the MLE sum of squares and the error-norm sum are always double.
+// Precision: T (float or double) for the bulk arithmetic and the step-size
+// controller; the time, the MLE sum of squares and the error-norm sum are
+// Wide<T> (double, or a float pair with a 48-bit significand for float).
 #pragma once
 
 #include "pdq_device.cuh"
@@ -34,6 +35,11 @@ struct IsoArgs {
   double atol, rtol, eps, damp;
   int64_t max_attempts;
   double q1[kMaxN][kMaxN];  // lower square root of flip(Hilbert) (utilities.py:57-71)
+  // float copies of the constants, so the float32 kernels read them without
+  // conversions on the FP64 pipe
+  float q1f[kMaxN][kMaxN];
+  float safety_f, factor_min_f, factor_max_f, exp_i_f, exp_p_f;
+  float atol_f, rtol_f, eps_f, damp_f;
   const double* save_at;
   const double* params;
   const double* y0;
@@ -47,10 +53,20 @@ struct IsoArgs {
   int32_t* status;
 };
 
+// A constant in the kernel's precision: the float copy for float, else the double.
+template <typename T>
+PDQ_D T cst(double d, float f) {
+  if constexpr (sizeof(T) == sizeof(float)) {
+    return f;
+  } else {
+    return d;
+  }
+}
+
 // Preconditioner p_i = h^(NU-i)/(NU-i)!, p_inv_i = 1/p_i (utilities.py:74-84).
 template <typename T, int NU>
 PDQ_D void precon(T h, T (&p)[NU + 1], T (&pinv)[NU + 1]) {
-  const T hinv = dev_rcp(h);
+  const T hinv = fast_rcp(h);
   p[NU] = T(1);
   pinv[NU] = T(1);
 #pragma unroll
@@ -87,77 +103,119 @@ PDQ_D void iso_predict_mean(const T (&m)[NU + 1][D], const T (&p)[NU + 1], const
 // The stacked matrix is 2n x n with an upper-triangular bottom block, so the
 // Householder reflector of column c only touches rows c..n-1 of the top block
 // and rows 0..c of the bottom block (n + 1 entries).
-template <typename T, int NU>
-PDQ_D void iso_predict_chol(const double (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
+//
+// Reflector of column c with alpha = X[c][c], nrm = ||column||:
+//   beta = -sign(alpha) nrm,  v = [alpha - beta, rest],  H = I - g v v^T,
+//   g = 2 / (v^T v) = 1 / (nrm (nrm + |alpha|)),
+// applied unnormalised so the dot products with the other columns start
+// before the square root is known; the dependency chain per column is one
+// sum of squares, one square root and one reciprocal.  Sums of squares
+// outside [1e-30, 1e36] (where g would leave the float range) take the
+// LAPACK-style scaled path with a normalised reflector instead.
+template <typename T, int NU, typename Q>
+PDQ_D void iso_predict_chol(const Q (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
                             const T (&pinv)[NU + 1], T scale_q, T (&Lp)[NU + 1][NU + 1]) {
   constexpr int n = NU + 1;
   // top block X = (A pinv L)^T: X[r][c] = sum_k A[c][k] pinv[k] L[k][r]
   T X[n][n];
   T U[n][n];  // bottom block (s sqrt|h| Q1)^T, upper triangular
+  T PL[n][n];
+#pragma unroll
+  for (int k = 0; k < n; ++k)
+#pragma unroll
+    for (int r = 0; r < n; ++r) PL[k][r] = pinv[k] * L[k][r];
 #pragma unroll
   for (int c = 0; c < n; ++c)
 #pragma unroll
     for (int r = 0; r < n; ++r) {
       T acc = T(0);
 #pragma unroll
-      for (int k = (c > r ? c : r); k < n; ++k) acc += T(iwp_a<NU>(c, k)) * pinv[k] * L[k][r];
+      for (int k = (c > r ? c : r); k < n; ++k) acc += T(iwp_a<NU>(c, k)) * PL[k][r];
       X[r][c] = acc;
       U[r][c] = (r <= c) ? scale_q * T(q1[c][r]) : T(0);
     }
   // structured Householder QR
 #pragma unroll
   for (int c = 0; c < n; ++c) {
-    T nrm2 = T(0);
+    // below-diagonal part of the column, two interleaved partial sums
+    T e0 = T(0), e1 = T(0);
 #pragma unroll
-    for (int r = c; r < n; ++r) nrm2 += X[r][c] * X[r][c];
-#pragma unroll
-    for (int i = 0; i <= c; ++i) nrm2 += U[i][c] * U[i][c];
-    const T alpha = X[c][c];
-    T nrm;
-    if (norm2_out_of_range(nrm2)) {
-      T sc = T(0);
-#pragma unroll
-      for (int r = c; r < n; ++r) sc = fmax(sc, dev_abs(X[r][c]));
-#pragma unroll
-      for (int i = 0; i <= c; ++i) sc = fmax(sc, dev_abs(U[i][c]));
-      T acc = T(0);
-      if (sc > T(0)) {
-        const T inv = T(1) / sc;
-#pragma unroll
-        for (int r = c; r < n; ++r) acc += (X[r][c] * inv) * (X[r][c] * inv);
-#pragma unroll
-        for (int i = 0; i <= c; ++i) acc += (U[i][c] * inv) * (U[i][c] * inv);
-      }
-      nrm = sc * dev_sqrt(acc);
-      nrm2 = nrm > T(0) ? T(1) : T(0);
-    } else {
-      nrm = dev_sqrt(nrm2);
+    for (int r = c + 1; r < n; ++r) {
+      if ((r & 1) == 0) e0 += X[r][c] * X[r][c];
+      else e1 += X[r][c] * X[r][c];
     }
-    if (nrm2 > T(0)) {
-      const T beta = alpha >= T(0) ? -nrm : nrm;
-      const T v0 = alpha - beta;
-      const T tau = (beta - alpha) / beta;
-      const T vinv = dev_rcp(v0);
-      // normalised reflector v = [1, X[c+1..][c]/v0, U[0..c][c]/v0]
 #pragma unroll
-      for (int r = c + 1; r < n; ++r) X[r][c] *= vinv;
-#pragma unroll
-      for (int i = 0; i <= c; ++i) U[i][c] *= vinv;
+    for (int i = 0; i <= c; ++i) {
+      if ((i & 1) == 0) e0 += U[i][c] * U[i][c];
+      else e1 += U[i][c] * U[i][c];
+    }
+    const T alpha = X[c][c];
+    const T nrm2 = alpha * alpha + (e0 + e1);
+    if (!norm2_out_of_range(nrm2)) {
+      const T nrm = fast_sqrt(nrm2);
+      const T s = dev_abs(alpha) + nrm;
+      const T v0 = alpha >= T(0) ? s : -s;
+      const T g = fast_rcp(nrm * s);
 #pragma unroll
       for (int j = c + 1; j < n; ++j) {
-        T w = X[c][j];
+        T d0 = T(0), d1 = T(0);
 #pragma unroll
-        for (int r = c + 1; r < n; ++r) w += X[r][c] * X[r][j];
+        for (int r = c + 1; r < n; ++r) {
+          if ((r & 1) == 0) d0 += X[r][c] * X[r][j];
+          else d1 += X[r][c] * X[r][j];
+        }
 #pragma unroll
-        for (int i = 0; i <= c; ++i) w += U[i][c] * U[i][j];
-        w *= tau;
-        X[c][j] -= w;
+        for (int i = 0; i <= c; ++i) {
+          if ((i & 1) == 0) d0 += U[i][c] * U[i][j];
+          else d1 += U[i][c] * U[i][j];
+        }
+        const T w = (v0 * X[c][j] + (d0 + d1)) * g;
+        X[c][j] -= w * v0;
 #pragma unroll
         for (int r = c + 1; r < n; ++r) X[r][j] -= w * X[r][c];
 #pragma unroll
         for (int i = 0; i <= c; ++i) U[i][j] -= w * U[i][c];
       }
-      X[c][c] = beta;
+      X[c][c] = alpha >= T(0) ? -nrm : nrm;
+    } else {
+      // scaled norm and normalised reflector v = [1, rest / v0], tau = (beta - alpha) / beta
+      T sc = dev_abs(alpha);
+#pragma unroll
+      for (int r = c + 1; r < n; ++r) sc = fmax(sc, dev_abs(X[r][c]));
+#pragma unroll
+      for (int i = 0; i <= c; ++i) sc = fmax(sc, dev_abs(U[i][c]));
+      if (sc > T(0)) {
+        const T inv = T(1) / sc;
+        T acc = T(0);
+#pragma unroll
+        for (int r = c; r < n; ++r) acc += (X[r][c] * inv) * (X[r][c] * inv);
+#pragma unroll
+        for (int i = 0; i <= c; ++i) acc += (U[i][c] * inv) * (U[i][c] * inv);
+        const T nrm = sc * dev_sqrt(acc);
+        const T beta = alpha >= T(0) ? -nrm : nrm;
+        const T v0 = alpha - beta;
+        const T tau = (beta - alpha) / beta;
+        const T vinv = T(1) / v0;
+#pragma unroll
+        for (int r = c + 1; r < n; ++r) X[r][c] *= vinv;
+#pragma unroll
+        for (int i = 0; i <= c; ++i) U[i][c] *= vinv;
+#pragma unroll
+        for (int j = c + 1; j < n; ++j) {
+          T w = X[c][j];
+#pragma unroll
+          for (int r = c + 1; r < n; ++r) w += X[r][c] * X[r][j];
+#pragma unroll
+          for (int i = 0; i <= c; ++i) w += U[i][c] * U[i][j];
+          w *= tau;
+          X[c][j] -= w;
+#pragma unroll
+          for (int r = c + 1; r < n; ++r) X[r][j] -= w * X[r][c];
+#pragma unroll
+          for (int i = 0; i <= c; ++i) U[i][j] -= w * U[i][c];
+        }
+        X[c][c] = beta;
+      }
     }
   }
   // Lp = |p| * R^T (lower triangular)
@@ -167,8 +225,8 @@ PDQ_D void iso_predict_chol(const double (&q1)[kMaxN][kMaxN], const T (&L)[NU + 
     for (int j = 0; j < n; ++j) Lp[i][j] = (j <= i) ? dev_abs(p[i]) * X[j][i] : T(0);
 }
 
-template <typename T, int NU, int D>
-PDQ_D void iso_predict(const double (&q1)[kMaxN][kMaxN], const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1],
+template <typename T, int NU, int D, typename Q>
+PDQ_D void iso_predict(const Q (&q1)[kMaxN][kMaxN], const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1],
                        const T (&p)[NU + 1], const T (&pinv)[NU + 1], T scale_q, T (&mp)[NU + 1][D],
                        T (&Lp)[NU + 1][NU + 1]) {
   iso_predict_mean<T, NU, D>(m, p, pinv, mp);
@@ -198,7 +256,7 @@ PDQ_D T ts0_update(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (
 #pragma unroll
   for (int c = 1; c <= OUT; ++c) givens_rows<T, n + 1, n + 1>(M, c, c + 1, c);
   const T R_Y = M[0][0];
-  const T ry_inv = dev_rcp(R_Y);
+  const T ry_inv = fast_rcp(R_Y);
 #pragma unroll
   for (int i = 0; i < n; ++i) {
     gain[i] = M[0][i + 1] * ry_inv;
@@ -266,7 +324,9 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   }
   // interpolation state (interp_from); dead code when INTERP is false
   T mi[n][D], Li[n][n];
-  double ti = save_at[0];
+  using W = Wide<T>;
+  constexpr bool kNarrow = sizeof(T) == sizeof(float);
+  W ti = wide_from(save_at[0], T(0));
   if constexpr (INTERP) {
 #pragma unroll
     for (int i = 0; i < n; ++i) {
@@ -277,31 +337,47 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
     }
   }
 
-  double t = save_at[0];
-  double dt = a.dt0[b];
-  double pi_prev = 1.0;  // PI controller state (controllers.py:41-43)
-  double mle_sumsq = 0.0;
+  W t = wide_from(save_at[0], T(0));
+  T dt = T(a.dt0[b]);
+  T pi_prev = T(1);  // PI controller state (controllers.py:41-43)
+  W mle_sumsq = wide_from(0.0, T(0));
   int num_data = 0, num_steps = 0, attempts = 0, status = PDQ_INSTANCE_OK;
   T sigma_sf = T(1);  // output scale of step_from (dynamic solver)
-  const T damp = T(a.damp);
+  const T damp = cst<T>(a.damp, a.damp_f);
+  const T eps = cst<T>(a.eps, a.eps_f);
+  const T atol = cst<T>(a.atol, a.atol_f), rtol = cst<T>(a.rtol, a.rtol_f);
+  const T safety = cst<T>(a.safety, a.safety_f);
+  const T factor_min = cst<T>(a.factor_min, a.factor_min_f), factor_max = cst<T>(a.factor_max, a.factor_max_f);
 
   // ||Q1 row OUT||^2 enters the observed std of the linearised residual
   T q1_out2 = T(0);
 #pragma unroll
-  for (int j = 0; j < n; ++j) q1_out2 += T(a.q1[OUT][j]) * T(a.q1[OUT][j]);
+  for (int j = 0; j < n; ++j) q1_out2 += cst<T>(a.q1[OUT][j], a.q1f[OUT][j]) * cst<T>(a.q1[OUT][j], a.q1f[OUT][j]);
 
-  if (!a.terminal_only) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, t, 0);
+  if (!a.terminal_only) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, wide_value(t), 0);
+
+  // t + eps < t_next (float64: exactly the reference's comparison; float
+  // pairs: the difference, rounded once, against eps)
+  auto before = [&](const W& x, const W& y) -> bool {
+    if constexpr (kNarrow) {
+      return wide_diff(y, x) > eps;
+    } else {
+      return x + a.eps < y;
+    }
+  };
 
   for (int s = 1; s < S && status == PDQ_INSTANCE_OK; ++s) {
-    const double t_next = save_at[s];
+    const W t_next = wide_from(save_at[s], T(0));
     bool cont = true;
     while (cont && status == PDQ_INSTANCE_OK) {
-      if (t + a.eps < t_next) {
+      if (before(t, t_next)) {
         // ---- rejection loop (solvers_via_adaptive_steps.py:249-328) ----
         bool accepted = false;
         while (!accepted) {
-          const double dt_use = a.clip_dt ? fmin(dt, t_next - t) : dt;
-          if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
+          const T remaining = wide_diff(t_next, t);
+          const bool clipped = a.clip_dt && !(dt < remaining);
+          const T dt_use = clipped ? remaining : dt;
+          if (!(dev_abs(dt_use) > T(1e-14) * fmax(T(1), dev_abs(T(wide_hi(t)))))) {
             status = PDQ_INSTANCE_DT_UNDERFLOW;
             break;
           }
@@ -310,7 +386,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             break;
           }
           ++attempts;
-          const T h = T(dt_use);
+          const T h = dt_use;
           T p[n], pinv[n];
           precon<T, NU>(h, p, pinv);
 
@@ -328,21 +404,25 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             mobs[j] = mp[OUT][j] - f[j];
             mobs2 += mobs[j] * mobs[j];
           }
-          const T rms_mobs = dev_sqrt(mobs2 * T(1.0 / D));
+          const T rms_mobs = fast_sqrt(mobs2 * T(1.0 / D));
           // fx.marginalise(apply_flat(m)) with unit scale: observed std
           // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
           // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
-          const T ell = dev_sqrt(p[OUT] * p[OUT] * dev_abs(h) * q1_out2 + damp * damp);
+          const T ell = fast_sqrt(p[OUT] * p[OUT] * dev_abs(h) * q1_out2 + damp * damp);
           const T sigma_loc = dev_div(rms_mobs, ell);
 
           const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
           T Lp[n][n];
-          iso_predict_chol<T, NU>(a.q1, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
+          if constexpr (kNarrow) {
+            iso_predict_chol<T, NU>(a.q1f, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp);
+          } else {
+            iso_predict_chol<T, NU>(a.q1, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
+          }
 
           // ---- update (revert_conditional, H = e_OUT) ----
           T gain[n], Lnew[n][n];
           const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew);
-          const T ry_inv = dev_rcp(R_Y);
+          const T ry_inv = fast_rcp(R_Y);
           T mnew[n][D];
 #pragma unroll
           for (int i = 0; i < n; ++i)
@@ -351,35 +431,35 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 
           // ---- error estimate (error_residual_std, solvers.py:925-996) ----
           const T err_abs = dev_abs(sigma_loc) * ell * h;  // std of rescaled observed * dt^1/1!
-          double sumsq = 0.0;
+          W sumsq = wide_from(0.0, T(0));
 #pragma unroll
           for (int j = 0; j < D; ++j) {
             const T ref = fmax(dev_abs(m[0][j]), dev_abs(mnew[0][j]));
-            const T ratio = dev_div(err_abs, T(a.atol) + T(a.rtol) * ref);
-            sumsq += double(ratio) * double(ratio);
+            const T ratio = dev_div(err_abs, atol + rtol * ref);
+            sumsq = wide_add_sq(sumsq, ratio);
           }
-          const double norm2 = sumsq * (1.0 / D);
+          // error_norm^2 = sumsq / D; accepted iff error_power = error_norm^(-1/n)
+          // >= 1, i.e. iff sumsq <= D (decided on the wide sum)
+          const T norm2 = T(wide_hi(sumsq)) * T(1.0 / D);
           if (!(norm2 == norm2) || isinf(norm2)) {
             status = PDQ_INSTANCE_NONFINITE;
             break;
           }
-          // error_power = error_norm^(-1/n); accepted iff error_power >= 1,
-          // i.e. iff error_norm^2 <= 1 (decided exactly on the float64 sum)
-          const T ep = dev_fpow(T(norm2), T(-0.5 / n));
+          const T ep = dev_fpow(norm2, T(-0.5 / n));
+          accepted = wide_le(sumsq, T(D));
 
           // ---- controller (controllers.py:24-84) ----
-          double factor;
+          T factor;
           if (a.control == PDQ_CONTROL_INTEGRAL) {
-            factor = a.safety * double(ep);
+            factor = safety * ep;
           } else {
-            const double gi = double(dev_fpow(ep, T(a.exp_i)));
-            const double gp = double(dev_fpow(dev_div(ep, T(pi_prev)), T(a.exp_p)));
-            factor = a.safety * gi * gp;
-            if (norm2 <= 1.0) pi_prev = double(ep);
+            const T gi = dev_fpow(ep, cst<T>(a.exp_i, a.exp_i_f));
+            const T gp = dev_fpow(dev_div(ep, pi_prev), cst<T>(a.exp_p, a.exp_p_f));
+            factor = safety * gi * gp;
+            if (accepted) pi_prev = ep;
           }
-          factor = fmax(a.factor_min, fmin(factor, a.factor_max));
+          factor = fmax(factor_min, fmin(factor, factor_max));
           dt = factor * dt_use;
-          accepted = norm2 <= 1.0;
           if (accepted) {
             if constexpr (INTERP) {
               ti = t;
@@ -391,7 +471,13 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
                 for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
               }
             }
-            t = t + dt_use;
+            // a step clipped to the checkpoint lands on it exactly in float
+            // pairs; float64 adds as the reference does
+            if constexpr (kNarrow) {
+              t = clipped ? t_next : wide_add(t, dt_use);
+            } else {
+              t = t + dt_use;
+            }
             ++num_steps;
 #pragma unroll
             for (int i = 0; i < n; ++i) {
@@ -403,7 +489,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             if (a.solver == PDQ_SOLVER_MLE) {
               // running scale via hypot recurrence == RMS of new terms (solvers.py:421-424)
               const T new_term = rms_mobs * dev_abs(ry_inv);
-              mle_sumsq += double(new_term) * double(new_term);
+              mle_sumsq = wide_add_sq(mle_sumsq, new_term);
               ++num_data;
             }
             sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
@@ -414,17 +500,21 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
       // ---- checkpoint branch (solvers_via_adaptive_steps.py:242-247) ----
       const int s_out = a.terminal_only ? 0 : s;
       const bool record = (!a.terminal_only) || (s == S - 1);
-      if (t + a.eps < t_next) {
+      if (before(t, t_next)) {
         // interp_skip: keep stepping towards the checkpoint
-      } else if (INTERP && t > t_next + a.eps) {
+      } else if (INTERP && before(t_next, t)) {
         if constexpr (INTERP) {
           // interp_beyond_t1: predict from interp_from to t_next
           // (solvers.py:205-269, estimators_and_losses.py:403-414)
-          const T h = T(t_next - ti);
+          const T h = T(wide_diff(t_next, ti));
           T p[n], pinv[n], mp[n][D], Lp[n][n];
           precon<T, NU>(h, p, pinv);
-          iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
-          if (record) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), t_next, num_steps);
+          if constexpr (kNarrow) {
+            iso_predict<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
+          } else {
+            iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
+          }
+          if (record) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), wide_value(t_next), num_steps);
           ti = t_next;
 #pragma unroll
           for (int i = 0; i < n; ++i) {
@@ -436,7 +526,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
         }
       } else {
         // interp_at_t1: the state itself is the solution (estimators_and_losses.py:416-421)
-        if (record) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), t, num_steps);
+        if (record) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), wide_value(t), num_steps);
         if constexpr (INTERP) {
           ti = t;
 #pragma unroll
@@ -448,14 +538,14 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           }
         }
       }
-      cont = t + a.eps < t_next;
+      cont = before(t, t_next);
     }
   }
 
   // ---- finalize: calibrated output scale (solvers.py:439-480, 601-633, 735-767) ----
   if (status == PDQ_INSTANCE_OK) {
     if (a.solver == PDQ_SOLVER_MLE) {
-      double scale = num_data > 0 ? sqrt(mle_sumsq / num_data) : 0.0;
+      double scale = num_data > 0 ? sqrt(wide_value(mle_sumsq) / num_data) : 0.0;
       if (a.correct) {
         const int last = a.num_steps[b * S_out + (S_out - 1)];
         scale = scale / sqrt(double(last));

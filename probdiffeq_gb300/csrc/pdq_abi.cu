@@ -167,6 +167,17 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.damp = c->damp;
     a.max_attempts = c->max_attempts;
     iwp_q1(c->num_derivatives, a.q1);
+    for (int i = 0; i < pdq::kMaxN; ++i)
+      for (int j = 0; j < pdq::kMaxN; ++j) a.q1f[i][j] = float(a.q1[i][j]);
+    a.safety_f = float(a.safety);
+    a.factor_min_f = float(a.factor_min);
+    a.factor_max_f = float(a.factor_max);
+    a.exp_i_f = float(a.exp_i);
+    a.exp_p_f = float(a.exp_p);
+    a.atol_f = float(a.atol);
+    a.rtol_f = float(a.rtol);
+    a.eps_f = float(a.eps);
+    a.damp_f = float(a.damp);
     a.save_at = args->save_at;
     a.params = args->params;
     a.y0 = args->y0;
@@ -180,10 +191,10 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.status = args->status;
     const bool interp = !c->clip_dt;
     if (c->kernel_variant < 0 || c->kernel_variant > 3) return PDQ_ERROR_INVALID_VALUE;
-    // 0 selects the lane-cooperative kernel (8 lanes, <= 85 registers) where it
-    // applies (exact checkpoint landings); 1 one thread per instance; 2 / 3 the
-    // lane-cooperative kernel with <= 128 / <= 85 registers per lane
-    const bool warp = c->clip_dt && c->kernel_variant != 1;
+    // 0 (auto) and 1: one thread per instance; 2 / 3: the lane-cooperative
+    // kernel (8 lanes per instance) with <= 128 / <= 85 registers per lane,
+    // for exact checkpoint landings only
+    const bool warp = c->clip_dt && c->kernel_variant >= 2;
     if (c->kernel_variant >= 2 && !c->clip_dt) return PDQ_ERROR_UNSUPPORTED;
     const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : 64;
     const bool f64 = c->precision == PDQ_PRECISION_F64;

@@ -80,6 +80,100 @@ PDQ_D T dev_fmax_abs(T a, T b) {
   return fmax(dev_abs(a), dev_abs(b));
 }
 
+// Single-instruction approximations (PTX .approx, flush-to-zero) for the
+// float32 hot loops, where the IEEE-rounded library sequences would sit on
+// the dependency chain of every step attempt.  Callers keep the arguments in
+// the normal range (the QR and rotation code checks sums of squares against
+// [1e-30, 1e36] before using these).  In float64 they are the exact ops.
+PDQ_D float fast_sqrt(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+PDQ_D float fast_rsqrt(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+PDQ_D float fast_rcp(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+PDQ_D double fast_sqrt(double x) { return sqrt(x); }
+PDQ_D double fast_rsqrt(double x) { return rsqrt(x); }
+PDQ_D double fast_rcp(double x) { return 1.0 / x; }
+
+// ---------------------------------------------------------------------------
+// Wide scalars for time and accumulators
+// ---------------------------------------------------------------------------
+// With T = double they are doubles.  With T = float they are unevaluated
+// float pairs hi + lo (|lo| <= ulp(hi) / 2, a 48-bit significand) built from
+// error-free transformations -- Knuth's TwoSum, Dekker's Fast2Sum and the
+// FMA two-product -- so the time, the error-norm sum and the calibration sum
+// keep near-float64 accuracy while running on the FP32 pipes: GB300's FP64
+// pipe issues a warp instruction only every 64 cycles, which made the
+// handful of float64 operations per attempt a third of a float32 solve.
+
+struct FloatPair {
+  float hi, lo;
+};
+
+PDQ_D FloatPair two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+PDQ_D FloatPair fast_two_sum(float a, float b) {  // requires |a| >= |b| or a == 0
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+
+template <typename T>
+struct WideOf {
+  using type = double;
+};
+template <>
+struct WideOf<float> {
+  using type = FloatPair;
+};
+template <typename T>
+using Wide = typename WideOf<T>::type;
+
+PDQ_D double wide_from(double x, double) { return x; }
+PDQ_D FloatPair wide_from(double x, float) {
+  const float hi = float(x);
+  return {hi, float(x - double(hi))};
+}
+PDQ_D double wide_value(double x) { return x; }
+PDQ_D double wide_value(FloatPair x) { return double(x.hi) + double(x.lo); }
+PDQ_D double wide_hi(double x) { return x; }
+PDQ_D float wide_hi(FloatPair x) { return x.hi; }
+
+// x + y for a narrow y
+PDQ_D double wide_add(double x, double y) { return x + y; }
+PDQ_D FloatPair wide_add(FloatPair x, float y) {
+  const FloatPair s = two_sum(x.hi, y);
+  return fast_two_sum(s.hi, s.lo + x.lo);
+}
+// x + y^2
+PDQ_D double wide_add_sq(double x, double y) { return x + y * y; }
+PDQ_D FloatPair wide_add_sq(FloatPair x, float y) {
+  const float p = y * y;
+  const float pe = fmaf(y, y, -p);
+  const FloatPair s = two_sum(x.hi, p);
+  return fast_two_sum(s.hi, s.lo + (pe + x.lo));
+}
+// x - y rounded to the narrow type (the difference of two nearby times)
+PDQ_D double wide_diff(double x, double y) { return x - y; }
+PDQ_D float wide_diff(FloatPair x, FloatPair y) {
+  const FloatPair s = two_sum(x.hi, -y.hi);
+  return s.hi + (s.lo + (x.lo - y.lo));
+}
+// x <= c for a narrow constant c
+PDQ_D bool wide_le(double x, double c) { return x <= c; }
+PDQ_D bool wide_le(FloatPair x, float c) { return x.hi < c || (x.hi == c && x.lo <= 0.0f); }
+
 template <int K>
 struct Factorial {
   static constexpr double value = K * Factorial<K - 1>::value;
@@ -385,7 +479,7 @@ PDQ_D void givens_rows(T (&M)[NR][NC], int a, int b, int c0) {
     sn = ys * inv;
     r2 = T(1);
   } else {
-    const T inv = dev_rsqrt(r2);
+    const T inv = fast_rsqrt(r2);
     cs = x * inv;
     sn = y * inv;
   }

@@ -15,9 +15,11 @@ float64.  At d = 4096 the viscous term is stiff (largest eigenvalue
 full-size checks use the horizon [0, 2e-3] (hundreds of steps).
 
 Tolerances: float64 -- solution 1e-8, rows 1e-5, covariances 1e-5,
-per-dimension output scales 1e-6, steps +-1; float32 -- solution 1e-3 and
-the per-dimension std of u within a factor 2 (float32 cannot carry these
-covariances), steps within 2 % (+-1).
+per-dimension output scales 1e-6, steps +-1; float32 -- solution 1e-3; the
+per-dimension std of u within max(2, 4 r) of float64, r >= 1 the largest
+ratio the oracle itself shows when run in float32 (float32 cannot carry
+these covariances: the reference algorithm in single precision deviates the
+same way); steps within max(2 %, 2x the float32 oracle's difference, 1).
 """
 
 import math
@@ -87,11 +89,12 @@ def compare(out, b, res, tol):
         # float32 cannot carry these covariances; std of u per dimension within 2x
         assert torch.isfinite(gc).all(), msg
         sg, so = cg[:, 0, 0].sqrt(), co[:, 0, 0].sqrt()
-        assert bool(((sg >= 0.5 * so) & (sg <= 2.0 * so)).all()), msg
+        f = tol["std_factor"]
+        assert bool(((sg >= so / f) & (sg <= f * so)).all()), (msg, f, float((sg / so).min()), float((sg / so).max()))
     else:
         assert err_rows <= tol["rows"], msg
         assert err_cov <= tol["cov"], msg
-    allowed = max(1, math.ceil(tol["steps"] * res.num_steps[-1]))
+    allowed = max(1, math.ceil(tol["steps"] * res.num_steps[-1]), tol.get("steps_abs", 0))
     assert abs(int(out["num_steps"][b, 0]) - res.num_steps[-1]) <= allowed
 
 
@@ -108,11 +111,11 @@ def test_burgers_small_vs_oracle(solver, precision):
             tol = dict(u=1e-8, rows=1e-5, cov=1e-5, steps=0.0)
         else:
             r32 = oracle_bd(u0, t1, solver=solver, dtype=torch.float32)
-            o64, o32 = res.u[-1], r32.u[-1]
-            rows = max(rel(o32.mean[:, i].double(), o64.mean[:, i]) for i in range(4))
-            c32 = o32.cholesky.double()
-            cov = max(rel((c32 @ c32.transpose(-1, -2))[j], (o64.cholesky @ o64.cholesky.transpose(-1, -2))[j]) for j in range(d))
-            tol = dict(u=1e-3, rows=max(5e-2, 4 * rows), cov=max(5e-2, 4 * cov), steps=0.02, f32=True)
+            c64, c32 = res.u[-1].cholesky, r32.u[-1].cholesky.double()
+            ratio = ((c32 @ c32.transpose(-1, -2))[:, 0, 0] / (c64 @ c64.transpose(-1, -2))[:, 0, 0]).sqrt()
+            r = float(torch.maximum(ratio, 1.0 / ratio).max())
+            dsteps = abs(int(r32.num_steps[-1]) - int(res.num_steps[-1]))
+            tol = dict(u=1e-3, std_factor=max(2.0, 4.0 * r), steps=0.02, steps_abs=2 * dsteps, f32=True)
         compare(out, b, res, tol)
         if precision == "float64":
             assert rel(out["output_scale"][b, 0], torch.as_tensor(res.output_scale[-1]).reshape(-1)) < 1e-6
