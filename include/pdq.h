@@ -41,7 +41,8 @@ typedef enum pdq_status {
   PDQ_ERROR_UNSUPPORTED = 2,
   PDQ_ERROR_CUDA = 3,
   PDQ_ERROR_WORKSPACE = 4,
-  PDQ_ERROR_ABI_VERSION = 5
+  PDQ_ERROR_ABI_VERSION = 5,
+  PDQ_ERROR_STATIC_SCRATCH = 6
 } pdq_status;
 
 /* State-space factorisation (probdiffeq/_probdiffeq/ssm_impl_*.py). */
@@ -172,6 +173,22 @@ pdq_status pdq_lml_workspace_size(const pdq_config* config, int64_t num_instance
  * config: ssm isotropic, constraint TS0, strategy fixedpoint, solver plain. */
 pdq_status pdq_lml_fixed_grid(const pdq_config* config, const pdq_lml_args* args, void* workspace, size_t workspace_bytes,
                               void* stream);
+
+/* Size of the scratch array inside the library used by pdq_lml_fixed_grid_static. */
+#define PDQ_LML_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/* pdq_lml_fixed_grid without any allocation, for callers that cannot call
+ * cudaMalloc (code running under stream capture, plugin hosts that pass only
+ * input and output buffers, allocation-free loops).  No counterpart in the
+ * reference: it is an addition of this library.  The scratch is a 32 MiB
+ * array inside the library (held on every GPU that loads it, until exit);
+ * problems whose scratch (pdq_lml_workspace_size) exceeds
+ * PDQ_LML_STATIC_SCRATCH_BYTES return PDQ_ERROR_STATIC_SCRATCH before any
+ * launch.  The first call on a device looks up the array's device address, so
+ * make it before any stream capture.  All calls share the array: calls whose
+ * launches overlap on the GPU race.  Allocates nothing (no cudaMalloc or
+ * cudaFree). */
+pdq_status pdq_lml_fixed_grid_static(const pdq_config* config, const pdq_lml_args* args, void* stream);
 
 #ifdef __cplusplus
 }

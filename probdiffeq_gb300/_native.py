@@ -124,6 +124,10 @@ SIGNATURES = {
         ctypes.c_int,
         [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlArgs), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
     ),
+    "pdq_lml_fixed_grid_static": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlArgs), ctypes.c_void_p],
+    ),
     "pdq_probe_fp32_fma": (
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],

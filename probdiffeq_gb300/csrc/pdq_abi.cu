@@ -78,6 +78,7 @@ const char* pdq_status_string(pdq_status s) {
     case PDQ_ERROR_CUDA: return "CUDA error";
     case PDQ_ERROR_WORKSPACE: return "workspace too small";
     case PDQ_ERROR_ABI_VERSION: return "ABI version mismatch";
+    case PDQ_ERROR_STATIC_SCRATCH: return "problem exceeds the library's static scratch array";
     default: return "unknown status";
   }
 }
