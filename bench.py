@@ -1,21 +1,31 @@
 """Benchmark: ensemble IVP solves/s on one GB300 (or N replicas).
 
-Workload (the configuration the headline metric is quoted on): 16384
+Headline workload (``--workload lv_ensemble``, the default): 16384
 Lotka--Volterra instances, each of (a, b, c, d) = nominal * exp(0.2 z),
 z ~ N(0, 1), y0 ~ U[10, 30]^2 (seed 0; rank r uses seed r), t in [0, 50],
 IWP prior with 4 derivatives (Taylor-mode initial derivatives on device),
 isotropic TS0, filter, MLE calibration, error_residual_std, integral
 control, terminal values with clip_dt, rtol = atol = 1e-6, dt0 = 0.1.
-Bulk arithmetic float32; time, calibration and error-norm sums float64.
+Bulk arithmetic float32; time, calibration and error-norm sums in float
+pairs (48-bit significand).
 
 A "step" is one full ensemble solve.  ``value`` times the native solve on
 device-resident inputs (CUDA events on the launching stream, an L2 flush
 between steps outside the events); ``e2e`` times the public API
 (``probdiffeq_gb300.ensemble.solve_ensemble``) from pinned host inputs to
-pinned host outputs, copies included.
+pinned host outputs, copies included.  The same line carries the float64
+batch, the single-instance latencies (the plain per-instance method) and the
+LML-gradient throughput under ``secondary``.
+
+Other workloads, one JSON line each (``--workload``):
+  lv_single          one LV instance, dynamic calibration, float64 and float32
+  fhn_lml            LML + gradient for 1024 FitzHugh--Nagumo parameter samples
+  vdp_dense          4096 stiff van der Pol instances, dense TS1, fixed-point
+                     smoother, 100 checkpoints (minutes per solve at mu <= 1000)
+  burgers_blockdiag  64 viscous Burgers instances, d = 4096, blockdiag TS0
 
 ``--impl reference`` times the CPU restatement of the reference's algorithm
-(the C port in ``oracle/port``, float64, all host cores) on the same
+(the C port in ``oracle/port``, float64, all host cores) on the headline
 workload; the reference itself is JAX code and JAX is not installed.
 """
 
@@ -52,6 +62,7 @@ WORKLOAD = {
     "output": "terminal values (clip_dt)",
     "l2": "flushed between timed steps (256 MiB write)",
 }
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "iso_adaptive_kernel_lv16384.md")
 
 
 def lv_inputs(B, seed):
@@ -75,8 +86,20 @@ def flops_per_attempt(n, d):
     return 2 * n**3 + (10.0 / 3.0) * n**3 + (4.0 / 3.0) * (n + 1) ** 3 + 4 * n * n * d + 15 * n * d
 
 
+def profiled_dram_bytes(path=PROFILE_SUMMARY):
+    """DRAM bytes per launch of the headline kernel from the committed ncu summary, or None."""
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1].strip().split()[0])
+    except OSError:
+        return None
+    return None
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled while the measurements run."""
 
     QUERY = (
         "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -129,7 +152,7 @@ class ClockSampler:
 
 
 def measured_fp32_peak(torch, _native, device):
-    """FP32 FMA throughput of this GPU from the probe kernel (TFLOP/s), best of 3."""
+    """FP32 FMA throughput of this GPU from the probe kernel (TFLOP/s), best of 4."""
     lib = _native.load()
     sms = lib.pdq_probe_sm_count()
     blocks, threads, iters = sms * 8, 256, 1 << 16
@@ -147,29 +170,127 @@ def measured_fp32_peak(torch, _native, device):
     return best, sms
 
 
-def cpu_baseline(seconds_budget=20.0, impl_steps=None):
-    """Time the C port of the oracle on host cores; returns a dict."""
+def cpu_baseline(seconds_budget=15.0):
+    """Time the C port of the oracle on all host cores over whole ensemble passes."""
     from oracle.port import port
 
     cores = os.cpu_count() or 1
     params, y0 = lv_inputs(WORKLOAD["instances"], 0)
-    # calibrate the sample size to the time budget
-    n = cores
-    t = port.time_lv_ensemble(params[:n], y0[:n], threads=cores)
-    per = t / n
-    sample = int(max(cores, min(WORKLOAD["instances"], seconds_budget / max(per, 1e-9))))
-    t = port.time_lv_ensemble(params[:sample], y0[:sample], threads=cores)
+    B = WORKLOAD["instances"]
+    passes, total = 0, 0.0
+    while passes == 0 or total < seconds_budget * 0.5:
+        total += port.time_lv_ensemble(params, y0, threads=cores)
+        passes += 1
+        if total * (passes + 1) / passes > seconds_budget:
+            break
     return {
-        "value": sample / t,
+        "value": passes * B / total,
         "unit": UNIT,
         "cores": cores,
         "kind": "port",
-        "sample": f"first {sample} of the {WORKLOAD['instances']} instances, float64 C port of the reference algorithm, {cores} threads",
-        "seconds": t,
+        "sample": f"{passes} pass(es) over all {B} instances, float64 C port of the reference algorithm, {cores} threads",
+        "seconds": total,
     }
 
 
-def run_ours(args):
+def timed_region(torch, stream, fn, K, W, flush=None, world=1, dist=None):
+    """W untimed calls, then K calls each bracketed by CUDA events; returns seconds."""
+    for _ in range(W):
+        fn()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    total = 0.0
+    for _ in range(K):
+        if flush is not None:
+            flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    return total / 1e3
+
+
+# ---------------------------------------------------------------------------
+# secondary measurements (single instance, LML gradients)
+# ---------------------------------------------------------------------------
+
+
+def single_instance(torch, _native, ensemble, device, reps=3):
+    """One LV instance (nominal parameters, y0 = (20, 20)), dynamic calibration,
+    terminal values on [0, 50], rtol = atol = 1e-6: latency per solve."""
+    out = {}
+    stream = torch.cuda.current_stream()
+    for prec in ("float64", "float32"):
+        cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2, solver="dynamic",
+                                   precision=prec, atol=1e-6, rtol=1e-6, clip_dt=True)
+        p = torch.tensor([[0.5, 0.05, 0.5, 0.05]], dtype=torch.float64, device=device)
+        y0 = torch.tensor([[20.0, 20.0]], dtype=torch.float64, device=device)
+        sa = torch.tensor([[0.0, 50.0]], dtype=torch.float64, device=device)
+        dt0 = torch.full((1,), 0.1, dtype=torch.float64, device=device)
+        outs = _native.alloc_outputs(cfg, 1, 2, True, device)
+        t = timed_region(torch, stream, lambda: _native.solve_adaptive(cfg, sa, p, y0, dt0, True, outs, stream=stream),
+                         reps, 3)
+        out[prec] = {
+            "ms_per_solve": 1e3 * t / reps,
+            "attempts": int(outs["num_attempts"][0]),
+            "accepted_steps": int(outs["num_steps"][0, 0]),
+            "status": int(outs["status"][0]),
+        }
+    return out
+
+
+LML_FLOPS_PER_GRADIENT = None  # set in lml_gradients from the workload sizes
+
+
+def lml_gradients(torch, _native, ensemble, device, precisions=("float32", "float64"), reps=3, B=1024):
+    """LML of 200 FitzHugh--Nagumo observations and its gradient w.r.t. (a, b, c)
+    for B parameter samples (fixed grid of 2000 steps on [0, 20], IWP nu = 3,
+    isotropic TS0, fixed-point smoother checkpoints at the observations)."""
+    import numpy as np
+
+    from tests import lml_problem
+
+    num_steps, data_np = lml_problem.observations()
+    thetas = torch.tensor(lml_problem.theta_samples(B), dtype=torch.float64, device=device)
+    y0 = torch.tensor(np.tile(lml_problem.U0, (B, 1)), dtype=torch.float64, device=device)
+    data = torch.tensor(data_np, dtype=torch.float64, device=device)
+    std = torch.full((data.shape[0],), lml_problem.STD, dtype=torch.float64, device=device)
+    stream = torch.cuda.current_stream()
+    res = {}
+    for prec in precisions:
+        cfg = ensemble.make_config(field="fitzhugh_nagumo", num_derivatives=3, ode_dim=2, strategy="fixedpoint",
+                                   solver="none", precision=prec)
+        holder = {}
+
+        def call():
+            holder.update(_native.lml_fixed_grid(cfg, thetas, y0, data, std, t0=0.0, dt=0.01, num_steps=num_steps,
+                                                 save_every=10, average_pdfs=False, gradient=True, stream=stream,
+                                                 workspace=holder.get("_workspace"), outputs=holder.get("out")))
+            holder["out"] = {k: holder[k] for k in ("lml", "grad", "status")}
+
+        t = timed_region(torch, stream, call, reps, 3)
+        res[prec] = {
+            "grads_per_s": B * reps / t,
+            "ms_per_batch": 1e3 * t / reps,
+            "all_status_ok": bool((holder["status"] == 0).all().item()),
+        }
+    res["config"] = {"samples": B, "num_steps": num_steps, "observations": int(data.shape[0]), "num_derivatives": 3}
+    return res
+
+
+# ---------------------------------------------------------------------------
+# the headline workload
+# ---------------------------------------------------------------------------
+
+
+def run_lv_ensemble(args):
     import torch
     import torch.distributed as dist
 
@@ -190,114 +311,85 @@ def run_ours(args):
     params, y0 = lv_inputs(B, seed=rank)
     t0, t1 = WORKLOAD["t_span"]
     save_at = torch.tensor([t0, t1], dtype=torch.float64)
-    cfg = ensemble.make_config(
-        field="lotka_volterra", num_derivatives=4, ode_dim=2, solver="mle", precision="float32",
-        atol=WORKLOAD["atol"], rtol=WORKLOAD["rtol"], clip_dt=True,
-    )
-    cfg64 = ensemble.make_config(
-        field="lotka_volterra", num_derivatives=4, ode_dim=2, solver="mle", precision="float64",
-        atol=WORKLOAD["atol"], rtol=WORKLOAD["rtol"], clip_dt=True,
-    )
+
+    def config(precision, variant=0):
+        return ensemble.make_config(
+            field="lotka_volterra", num_derivatives=4, ode_dim=2, solver="mle", precision=precision,
+            atol=WORKLOAD["atol"], rtol=WORKLOAD["rtol"], clip_dt=True, kernel_variant=variant,
+        )
+
     stream = torch.cuda.current_stream()
     d_params, d_y0 = params.to(device), y0.to(device)
     d_save = save_at.expand(B, 2).contiguous().to(device)
     d_dt0 = torch.full((B,), WORKLOAD["dt0"], dtype=torch.float64, device=device)
-    outs = _native.alloc_outputs(cfg, B, 2, True, device)
+    outs = _native.alloc_outputs(config("float32"), B, 2, True, device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
 
     def device_step(c):
         _native.solve_adaptive(c, d_save, d_params, d_y0, d_dt0, True, outs, stream=stream)
 
-    def timed_steps(c, K, W):
-        for _ in range(W):
-            device_step(c)
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        total = 0.0
-        for _ in range(K):
-            flush.fill_(1.0)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            device_step(c)
-            e1.record(stream)
-            e1.synchronize()
-            total += e0.elapsed_time(e1)
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        return total / 1e3
-
-    # ---- autotune the instance-to-lane mapping on this workload ----
-    def tune(base_precision, variants):
-        times = {}
-        for v in variants:
-            c = ensemble.make_config(
-                field="lotka_volterra", num_derivatives=4, ode_dim=2, solver="mle", precision=base_precision,
-                atol=WORKLOAD["atol"], rtol=WORKLOAD["rtol"], clip_dt=True, kernel_variant=v,
-            )
-            device_step(c)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            device_step(c)
-            e1.record(stream)
-            e1.synchronize()
-            times[v] = e0.elapsed_time(e1)
-        best = min(times, key=times.get)
-        return best, times
-
     names = {1: "thread per instance", 2: "8 lanes per instance, <=128 regs", 3: "8 lanes per instance, <=85 regs"}
-    best32, tune32 = tune("float32", [1, 2, 3])
-    best64, tune64 = tune("float64", [1, 2, 3])
-    cfg.kernel_variant = best32
-    cfg64.kernel_variant = best64
 
-    # ---- value: device-resident inputs, FP32 bulk ----
-    with ClockSampler(local) as clk:
-        t_dev = timed_steps(cfg, args.steps, args.warmup)
-    attempts = outs["num_attempts"].to(torch.float64).sum().item()
-    steps_acc = outs["num_steps"].to(torch.float64).sum().item()
-    status_ok = bool((outs["status"] == 0).all().item())
-    mean32 = outs["u_mean"][:, 0].clone()
-    max_attempts_inst = int(outs["num_attempts"].max().item())
+    clk = ClockSampler(local)
+    clk.__enter__()
+    try:
+        # ---- autotune the instance-to-lane mapping on this workload ----
+        def tune(precision):
+            times = {}
+            for v in names:
+                times[v] = 1e3 * timed_region(torch, stream, lambda: device_step(config(precision, v)), 1, 1)
+            return min(times, key=times.get), times
 
-    # ---- FP64 bulk (the plain per-instance float64 kernel, batched) ----
-    t_dev64 = timed_steps(cfg64, max(1, args.steps // 2), 1)
-    mean64 = outs["u_mean"][:, 0].clone()
-    attempts64 = outs["num_attempts"].to(torch.float64).sum().item()
-    k64 = max(1, args.steps // 2)
-    rel_f32_f64 = ((mean32[:, 0] - mean64[:, 0]).abs() / mean64[:, 0].abs()).max().item()
+        fixed = {"thread": 1, "lanes": 2, "lanes_compact": 3}.get(args.variant)
+        if fixed is None:
+            best32, tune32 = tune("float32")
+            best64, tune64 = tune("float64")
+        else:
+            best32 = best64 = fixed
+            tune32, tune64 = {}, {}
+        cfg, cfg64 = config("float32", best32), config("float64", best64)
 
-    # ---- e2e through the public API, pinned host buffers, copies inside ----
-    h_params, h_y0 = params.pin_memory(), y0.pin_memory()
-    h_save = save_at.expand(B, 2).contiguous().pin_memory()
-    h_dt0 = torch.full((B,), WORKLOAD["dt0"], dtype=torch.float64).pin_memory()
-    h_out = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in outs.items()}
-    h2d = sum(t.numel() * t.element_size() for t in (h_params, h_y0, h_save, h_dt0))
-    d2h = sum(t.numel() * t.element_size() for t in h_out.values())
+        # ---- value: device-resident inputs, FP32 bulk ----
+        t_dev = timed_region(torch, stream, lambda: device_step(cfg), args.steps, args.warmup, flush, world, dist)
+        attempts = outs["num_attempts"].to(torch.float64).sum().item()
+        steps_acc = outs["num_steps"].to(torch.float64).sum().item()
+        status_ok = bool((outs["status"] == 0).all().item())
+        mean32 = outs["u_mean"][:, 0].clone()
+        max_attempts_inst = int(outs["num_attempts"].max().item())
 
-    def e2e_step():
-        o = ensemble.solve_ensemble(cfg, params=h_params, y0=h_y0, save_at=h_save, dt0=h_dt0, terminal_only=True, device=device, stream=stream)
-        for k, v in o.items():
-            h_out[k].copy_(v, non_blocking=True)
+        # ---- FP64 bulk (the same kernel in float64, batched) ----
+        k64 = max(3, args.steps // 20)
+        t_dev64 = timed_region(torch, stream, lambda: device_step(cfg64), k64, 1, flush, world, dist)
+        mean64 = outs["u_mean"][:, 0].clone()
+        attempts64 = outs["num_attempts"].to(torch.float64).sum().item()
+        rel_f32_f64 = ((mean32[:, 0] - mean64[:, 0]).abs() / mean64[:, 0].abs()).max().item()
 
-    for _ in range(args.warmup):
-        e2e_step()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    t_e2e = 0.0
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        e2e_step()
-        e1.record(stream)
-        e1.synchronize()
-        t_e2e += e0.elapsed_time(e1) / 1e3
-    torch.cuda.synchronize()
+        # ---- e2e through the public API, pinned host buffers, copies inside ----
+        h_params, h_y0 = params.pin_memory(), y0.pin_memory()
+        h_save = save_at.expand(B, 2).contiguous().pin_memory()
+        h_dt0 = torch.full((B,), WORKLOAD["dt0"], dtype=torch.float64).pin_memory()
+        h_out = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in outs.items()}
+        h2d = sum(t.numel() * t.element_size() for t in (h_params, h_y0, h_save, h_dt0))
+        d2h = sum(t.numel() * t.element_size() for t in h_out.values())
+
+        def e2e_step():
+            o = ensemble.solve_ensemble(cfg, params=h_params, y0=h_y0, save_at=h_save, dt0=h_dt0, terminal_only=True,
+                                        device=device, stream=stream)
+            for k, v in o.items():
+                if not k.startswith("_"):
+                    h_out[k].copy_(v, non_blocking=True)
+
+        t_e2e = timed_region(torch, stream, e2e_step, args.steps, args.warmup, flush, world, dist)
+
+        # ---- secondary: the plain per-instance method and LML gradients ----
+        secondary = None
+        if not args.no_secondary:
+            secondary = {
+                "single_instance_lv_dynamic": single_instance(torch, _native, ensemble, device),
+                "lml_gradients_fhn": lml_gradients(torch, _native, ensemble, device),
+            }
+    finally:
+        clk.__exit__(None, None, None)
 
     if world > 1:
         tt = torch.tensor([t_dev, t_e2e, t_dev64], dtype=torch.float64, device=device)
@@ -313,9 +405,10 @@ def run_ours(args):
         if world > 1:
             dist.destroy_process_group()
         return
+    value = world * B * args.steps / t_dev
     result = {
         "metric": METRIC,
-        "value": world * B * args.steps / t_dev,
+        "value": value,
         "unit": UNIT,
         "n_gpus": world,
         "steps": args.steps,
@@ -324,7 +417,7 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 bulk + f64 time/calibration/error-norm accumulators",
+        "dtype": "f32 bulk + float-pair (48-bit) time/calibration/error-norm accumulators",
         "data": "synthetic (seeded Lotka-Volterra ensemble)",
         "config": dict(WORKLOAD, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
         "e2e": {
@@ -346,17 +439,18 @@ def run_ours(args):
             "peak": peak,
             "unit": "TFLOP/s",
             "frac": achieved / peak,
-            "traffic": None,
+            "traffic": profiled_dram_bytes(),
             "peak_source": f"measured FP32 FMA probe on this GPU ({sms} SMs); MEASURED_PEAKS.json lists only HBM and bf16",
             "flops_per_attempt": fpa,
             "attempts_per_step": attempts,
+            "note": "latency-bound: 16384 one-thread instances fill < 1 warp per SM sub-partition",
         },
         "fp64": {
             "value": world * B * k64 / t_dev64,
             "unit": UNIT,
             "ms_per_step": 1e3 * t_dev64 / k64,
             "attempts_per_step": attempts64,
-            "fp32_speedup": (B * args.steps / t_dev) / (B * k64 / t_dev64),
+            "fp32_speedup": value / (world * B * k64 / t_dev64),
             "max_rel_terminal_diff_f32_vs_f64": rel_f32_f64,
         },
         "stats": {
@@ -367,14 +461,150 @@ def run_ours(args):
         },
         "clocks": clk.summary(),
     }
+    if secondary is not None:
+        plain64 = 1e3 / secondary["single_instance_lv_dynamic"]["float64"]["ms_per_solve"]
+        secondary["fp32_batched_vs_plain_fp64_per_instance"] = value / plain64
+        result["secondary"] = secondary
     if not args.no_cpu_baseline:
         try:
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
         except Exception as e:  # the port is test infrastructure; report why it is missing
-            result["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"unavailable: {e}"}
+            result["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                      "sample": f"unavailable: {e}"}
     print(json.dumps(result))
     if world > 1:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# the other workloads (one line each)
+# ---------------------------------------------------------------------------
+
+
+def base_line(metric, value, unit, args, ms, higher, dtype, config, **extra):
+    line = {
+        "metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": higher, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+        "data": "synthetic", "config": config,
+    }
+    line.update(extra)
+    return line
+
+
+def run_lv_single(args):
+    import torch
+
+    from probdiffeq_gb300 import _native, ensemble
+    from probdiffeq_gb300 import build as native_build
+
+    native_build.build()
+    device = torch.device("cuda:0")
+    with ClockSampler(0) as clk:
+        r = single_instance(torch, _native, ensemble, device, reps=args.steps)
+    cfg = {"workload": "lotka_volterra_single", "instances": 1, "params": [0.5, 0.05, 0.5, 0.05], "y0": [20.0, 20.0],
+           "t_span": [0.0, 50.0], "num_derivatives": 4, "solver": "dynamic", "rtol": 1e-6, "atol": 1e-6}
+    print(json.dumps(base_line("single-instance solve latency (float64)", r["float64"]["ms_per_solve"], "ms", args,
+                               r["float64"]["ms_per_solve"], False, "f64", cfg, float32=r["float32"],
+                               gpu_launches=args.steps, clocks=clk.summary())))
+
+
+def run_fhn_lml(args):
+    import torch
+
+    from probdiffeq_gb300 import _native, ensemble
+    from probdiffeq_gb300 import build as native_build
+
+    native_build.build()
+    device = torch.device("cuda:0")
+    with ClockSampler(0) as clk:
+        r = lml_gradients(torch, _native, ensemble, device, reps=args.steps)
+    print(json.dumps(base_line("LML grads/s", r["float32"]["grads_per_s"], "grads/s", args, r["float32"]["ms_per_batch"],
+                               True, "f32 bulk + f64 log-pdf sum", dict(r["config"], workload="fitzhugh_nagumo_lml"),
+                               float64=r["float64"], gpu_launches=args.steps, clocks=clk.summary())))
+
+
+def run_vdp_dense(args):
+    import torch
+
+    from probdiffeq_gb300 import _native, ensemble
+    from probdiffeq_gb300 import build as native_build
+
+    native_build.build()
+    device = torch.device("cuda:0")
+    B = args.instances if args.instances != WORKLOAD["instances"] else 4096
+    g = torch.Generator().manual_seed(0)
+    mu = torch.exp(torch.rand(B, generator=g, dtype=torch.float64) * math.log(args.mu_max))
+    save_at = (torch.linspace(0.0, 1.0, 100, dtype=torch.float64)[None, :] * 2.0 * mu[:, None]).contiguous().to(device)
+    y0 = torch.tensor([[2.0, 0.0]], dtype=torch.float64).expand(B, 2).contiguous().to(device)
+    prm = mu[:, None].contiguous().to(device)
+    dt0 = torch.full((B,), 0.1, dtype=torch.float64, device=device)
+    stream = torch.cuda.current_stream()
+    res = {}
+    with ClockSampler(0) as clk:
+        for prec in args.precisions.split(","):
+            cfg = ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense", constraint="ts1",
+                                       strategy="fixedpoint", solver="dynamic", precision=prec, atol=1e-5, rtol=1e-5,
+                                       clip_dt=False, max_attempts=1 << 24)
+            outs = _native.alloc_outputs(cfg, B, 100, False, device, posterior=True)
+            t = timed_region(torch, stream, lambda: _native.solve_adaptive(cfg, save_at, prm, y0, dt0, False, outs,
+                                                                             stream=stream), args.steps, args.warmup)
+            steps = outs["num_steps"][:, -1].to(torch.float64)
+            res[prec] = {"solves_per_s": B * args.steps / t, "ms_per_step": 1e3 * t / args.steps,
+                         "accepted_steps_max": int(steps.max()), "accepted_steps_mean": float(steps.mean()),
+                         "attempts_max": int(outs["num_attempts"].max()),
+                         "status_ok": int((outs["status"] == 0).sum())}
+    first = args.precisions.split(",")[0]
+    cfg = {"workload": "van_der_pol_dense", "instances": B, "mu": f"log-uniform [1, {args.mu_max}]", "t_span": "[0, 2 mu]",
+           "num_derivatives": 3, "ssm": "dense", "constraint": "ts1", "strategy": "fixedpoint", "solver": "dynamic",
+           "save_at": 100, "rtol": 1e-5, "atol": 1e-5}
+    print(json.dumps(base_line("ensemble IVP solves/s", res[first]["solves_per_s"], "solves/s", args,
+                               res[first]["ms_per_step"], True, first, cfg, by_precision=res, gpu_launches=args.steps,
+                               clocks=clk.summary())))
+
+
+def run_burgers_blockdiag(args):
+    import numpy as np
+    import torch
+
+    from probdiffeq_gb300 import _native, ensemble
+    from probdiffeq_gb300 import build as native_build
+
+    native_build.build()
+    device = torch.device("cuda:0")
+    B, d = 64, 4096
+    rng_u0 = []
+    for s in range(B):
+        g = np.random.default_rng(s)
+        x = np.arange(d) / d
+        k = np.arange(1, 9)
+        amp = g.normal(0.0, 1.0 / k)
+        phase = g.uniform(0.0, 2 * np.pi, size=8)
+        rng_u0.append((amp[:, None] * np.sin(2 * np.pi * k[:, None] * x[None, :] + phase[:, None])).sum(axis=0))
+    u0 = torch.tensor(np.stack(rng_u0), dtype=torch.float64, device=device)
+    t1 = args.t1
+    prm = torch.full((B, 1), 0.01, dtype=torch.float64, device=device)
+    sa = torch.tensor([0.0, t1], dtype=torch.float64, device=device).expand(B, 2).contiguous()
+    dt0 = torch.full((B,), 0.1 * t1, dtype=torch.float64, device=device)
+    stream = torch.cuda.current_stream()
+    res = {}
+    with ClockSampler(0) as clk:
+        for prec in args.precisions.split(","):
+            cfg = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=d, ssm="blockdiag", solver="dynamic",
+                                       precision=prec, atol=1e-4, rtol=1e-4, clip_dt=True, max_attempts=1 << 26)
+            outs = _native.alloc_outputs(cfg, B, 2, True, device)
+            t = timed_region(torch, stream, lambda: _native.solve_adaptive(cfg, sa, prm, u0, dt0, True, outs,
+                                                                             stream=stream), args.steps, args.warmup)
+            attempts = outs["num_attempts"].to(torch.float64)
+            res[prec] = {"solves_per_s": B * args.steps / t, "ms_per_step": 1e3 * t / args.steps,
+                         "attempts_max": int(attempts.max()), "attempts_mean": float(attempts.mean()),
+                         "us_per_attempt_slowest": 1e6 * (t / args.steps) / float(attempts.max()),
+                         "status_ok": int((outs["status"] == 0).sum())}
+    first = args.precisions.split(",")[0]
+    cfg = {"workload": "burgers_blockdiag", "instances": B, "d": d, "nu_visc": 0.01, "t_span": [0.0, t1],
+           "num_derivatives": 3, "ssm": "blockdiag", "constraint": "ts0", "solver": "dynamic", "rtol": 1e-4, "atol": 1e-4}
+    print(json.dumps(base_line("ensemble IVP solves/s", res[first]["solves_per_s"], "solves/s", args,
+                               res[first]["ms_per_step"], True, first, cfg, by_precision=res, gpu_launches=args.steps,
+                               clocks=clk.summary())))
 
 
 def run_reference(args):
@@ -384,7 +614,7 @@ def run_reference(args):
     vals = []
     cb = None
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(args.cpu_seconds / max(1, args.steps))
+        cb = cpu_baseline(args.cpu_seconds / max(1, args.steps + args.warmup))
         if i >= args.warmup:
             vals.append(cb["value"])
     value = statistics.mean(vals)
@@ -412,19 +642,36 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="lv_ensemble",
+                    choices=["lv_ensemble", "lv_single", "fhn_lml", "vdp_dense", "burgers_blockdiag"])
+    ap.add_argument("--variant", default="auto", choices=["auto", "thread", "lanes", "lanes_compact"],
+                    help="lv_ensemble: instance-to-lane mapping (auto = time all three and keep the fastest)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the single-instance and LML measurements")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="ensemble size (16384 is the headline workload)")
+    ap.add_argument("--mu-max", type=float, default=1000.0, help="vdp_dense: mu ~ log-uniform [1, mu_max]")
+    ap.add_argument("--t1", type=float, default=1.0, help="burgers_blockdiag: end time")
+    ap.add_argument("--precisions", default="float32,float64", help="vdp_dense / burgers_blockdiag precisions")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
     if args.impl == "reference":
+        args.warmup = max(args.warmup, 1)
         run_reference(args)
+        return
+    if args.workload == "lv_ensemble":
+        args.warmup = max(args.warmup, 3)
+        run_lv_ensemble(args)
+    elif args.workload == "lv_single":
+        run_lv_single(args)
+    elif args.workload == "fhn_lml":
+        run_fhn_lml(args)
+    elif args.workload == "vdp_dense":
+        run_vdp_dense(args)
     else:
-        run_ours(args)
+        run_burgers_blockdiag(args)
 
 
 if __name__ == "__main__":

@@ -18,7 +18,7 @@ cudaError_t launch_bd_nu(BdArgs a, cudaStream_t stream) {
   cudaError_t e = ensure_stack<bd_adaptive_kernel<T, NU>>();
   if (e != cudaSuccess) return e;
   const int CL = a.cluster;
-  const size_t smem = size_t(a.d / CL) * sizeof(T);
+  const size_t smem = bd_smem_bytes<T, NU>(a.d / CL);
   if (smem > 48 * 1024) {
     e = cudaFuncSetAttribute(bd_adaptive_kernel<T, NU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;

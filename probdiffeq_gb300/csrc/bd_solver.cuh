@@ -13,19 +13,24 @@
 // error norm couples them through one sum over d.
 //
 // GB300 mapping: the instance's d dimensions are split contiguously over the
-// CL CTAs of a cluster.  Each attempt:
-//   1. every thread extrapolates its dimensions and writes u(t+h) of each to
-//      its CTA's shared memory;  cluster barrier;
+// CL CTAs of a cluster; a thread owns dimensions tid, tid + 256, ... of its
+// CTA and works on one of them at a time (a runtime loop, so the register
+// footprint is one dimension's and two CTAs fit on an SM).  Each attempt:
+//   1. every thread extrapolates its dimensions and stages the extrapolated
+//      means (all n coefficients) in its CTA's shared memory;  cluster barrier;
 //   2. f at its dimensions reads the two stencil neighbours, from distributed
 //      shared memory of the neighbouring CTA at the CTA boundary; the
-//      per-dimension predict/update follows; the float64 error-norm partial
-//      is reduced in the CTA and published in shared memory;  cluster barrier;
-//   3. every CTA reads all CL partials over DSMEM and takes the same
-//      accept/step decision.
+//      per-dimension predict/update follows; the error-norm partial (a wide
+//      sum: float pair in float32, double in float64) is reduced in the CTA
+//      and published in shared memory;  cluster barrier;
+//   3. every CTA sums the CL partials over DSMEM in rank order and takes the
+//      same accept/step decision.
 // The per-dimension state (mean n, lower Cholesky n(n+1)/2) lives in two
 // scratch buffers in global memory (L2-resident: 64 x 4096 x 14 floats is
-// 15 MB per buffer); the proposal is written to the other buffer, so an
-// accept is a parity flip.
+// 15 MB per buffer), coalesced across a warp's consecutive dimensions; the
+// proposal is written to the other buffer, so an accept is a parity flip.
+// Time, step size and controller follow the isotropic kernel: Wide<T> time,
+// T controller, no float64 on the attempt path of the float32 kernel.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -46,6 +51,9 @@ struct BdArgs {
   double atol, rtol, eps, damp;
   int64_t max_attempts;
   double q1[kMaxN][kMaxN];
+  float q1f[kMaxN][kMaxN];
+  float safety_f, factor_min_f, factor_max_f, exp_i_f, exp_p_f;
+  float atol_f, rtol_f, eps_f, damp_f;
   const double* save_at;
   const double* params;  // (B, 1): viscosity
   const double* y0;      // (B, d)
@@ -57,12 +65,19 @@ struct BdArgs {
   int32_t* num_steps;
   int32_t* num_attempts;
   int32_t* status;
-  void* workspace;       // 2 state buffers (B, ns, d) in T, then MLE sums (B, d) double
+  void* workspace;       // 2 state buffers (B, ns, d) in T, then MLE sums (B, d), 8 bytes each
 };
 
 template <int NU>
 PDQ_HD constexpr int bd_state_rows() {
   return (NU + 1) + (NU + 1) * (NU + 2) / 2;
+}
+
+// Dynamic shared memory per CTA: staged means (n x dl), new terms and scales
+// (2 x dl), current scales (dl), in T.
+template <typename T, int NU>
+PDQ_HD size_t bd_smem_bytes(int dl) {
+  return size_t(NU + 1 + 3) * size_t(dl) * sizeof(T);
 }
 
 // Viscous Burgers with periodic central differences (the flux-form stencil
@@ -75,10 +90,12 @@ PDQ_D T burgers_f(T left, T mid, T right, T nu_visc, T inv_dx) {
 }
 
 template <typename T, int NU>
-__global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
+__global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   constexpr int n = NU + 1;
   constexpr int NS = bd_state_rows<NU>();
   constexpr int OUT = 1;
+  constexpr bool kNarrow = sizeof(T) == sizeof(float);
+  using W = Wide<T>;
   cg::cluster_group cluster = cg::this_cluster();
   const int CL = a.cluster;
   const int rank = int(cluster.block_rank());
@@ -88,16 +105,18 @@ __global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
   const int dl = d / CL;
   const int j0 = rank * dl;
   const int tid = threadIdx.x;
-  const int dpt = (dl + kBdThreads - 1) / kBdThreads;  // <= kBdMaxDimsPerThread (host-checked)
 
   extern __shared__ unsigned char smem_raw[];
-  T* ex = reinterpret_cast<T*>(smem_raw);                 // [dl] extrapolated u(t+h) of this CTA
-  __shared__ double partial[2];                           // CTA partial sums (error norm), parity
-  __shared__ double warp_sums[kBdThreads / 32];
+  T* mps = reinterpret_cast<T*>(smem_raw);  // [n][dl] extrapolated means of this CTA's dimensions
+  T* newt = mps + n * dl;                   // [dl] whitened residual of the proposal (MLE)
+  T* sig_new = newt + dl;                   // [dl] local scale of the proposal (dynamic)
+  T* sig = sig_new + dl;                    // [dl] output scale of the current state
+  __shared__ W partial[2];                  // CTA partial sums (error norm), parity
+  __shared__ W warp_sums[kBdThreads / 32];
 
   T* const buf0 = reinterpret_cast<T*>(a.workspace);
   T* const bufs[2] = {buf0 + inst * NS * int64_t(d), buf0 + (a.B + inst) * NS * int64_t(d)};
-  double* mle_sum = reinterpret_cast<double*>(buf0 + 2 * a.B * NS * int64_t(d)) + inst * int64_t(d);
+  W* mle_sum = reinterpret_cast<W*>(buf0 + 2 * a.B * NS * int64_t(d)) + inst * int64_t(d);
 
   const T nu_visc = T(a.params[inst]);
   const T inv_dx = T(d);
@@ -138,20 +157,33 @@ __global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
     const int g = j0 + jl;
     for (int k = 0; k < n; ++k) st[k * d + g] = T(double(st[k * d + g]) * factorial(k));
     for (int r = n; r < NS; ++r) st[r * d + g] = T(0);
-    mle_sum[g] = 0.0;
+    mle_sum[g] = wide_from(0.0, T(0));
+    sig[jl] = T(1);
   }
   __threadfence();
   cluster.sync();
 
-  double t = save_at[0], dt = a.dt0[inst], pi_prev = 1.0;
+  W t = wide_from(save_at[0], T(0));
+  T dt = T(a.dt0[inst]);
+  T pi_prev = T(1);
   int cur = 0, num_steps = 0, attempts = 0, status = PDQ_INSTANCE_OK, num_data = 0, par = 0;
-  T sig[kBdMaxDimsPerThread];
-#pragma unroll
-  for (int k = 0; k < kBdMaxDimsPerThread; ++k) sig[k] = T(1);
-  const T damp = T(a.damp);
+  const T damp = cst<T>(a.damp, a.damp_f);
+  const T atol = cst<T>(a.atol, a.atol_f), rtol = cst<T>(a.rtol, a.rtol_f);
+  const T safety = cst<T>(a.safety, a.safety_f);
+  const T factor_min = cst<T>(a.factor_min, a.factor_min_f), factor_max = cst<T>(a.factor_max, a.factor_max_f);
+  const T eps = cst<T>(a.eps, a.eps_f);
   T q1_out2 = T(0);
 #pragma unroll
-  for (int j = 0; j < n; ++j) q1_out2 += T(a.q1[OUT][j]) * T(a.q1[OUT][j]);
+  for (int j = 0; j < n; ++j) q1_out2 += cst<T>(a.q1[OUT][j], a.q1f[OUT][j]) * cst<T>(a.q1[OUT][j], a.q1f[OUT][j]);
+  const T q1_out_norm = dev_sqrt(q1_out2);
+
+  auto before = [&](const W& x, const W& y) -> bool {
+    if constexpr (kNarrow) {
+      return wide_diff(y, x) > eps;
+    } else {
+      return x + a.eps < y;
+    }
+  };
 
   auto write_checkpoint = [&](int s_out, double tt) {
     const T* x = bufs[cur];
@@ -161,10 +193,8 @@ __global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
       double* um = a.u_mean + (rec * d + g) * n;
       double* uc = a.u_chol + (rec * d + g) * n * n;
       for (int i = 0; i < n; ++i) um[i] = double(x[i * d + g]);
-      int o = n;
       for (int i = 0; i < n; ++i)
         for (int j = 0; j < n; ++j) uc[i * n + j] = (j <= i) ? double(x[(n + i * (i + 1) / 2 + j) * d + g]) : 0.0;
-      (void)o;
     }
     if (rank == 0 && tid == 0) {
       a.t_out[rec] = tt;
@@ -173,27 +203,21 @@ __global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
   };
   auto write_scale = [&](int s_out) {
     const int64_t rec = inst * S_out + s_out;
-#pragma unroll
-    for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
-      const int jl = tid + k * kBdThreads;
-      if (k < dpt && jl < dl) a.output_scale[rec * d + j0 + jl] = double(sig[k]);
-    }
+    for (int jl = tid; jl < dl; jl += kBdThreads) a.output_scale[rec * d + j0 + jl] = double(sig[jl]);
   };
 
   if (!a.terminal_only) {
-    write_checkpoint(0, t);
-#pragma unroll
-    for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
-      const int jl = tid + k * kBdThreads;
-      if (k < dpt && jl < dl) a.output_scale[(inst * S_out) * d + j0 + jl] = 1.0;
-    }
+    write_checkpoint(0, wide_value(t));
+    for (int jl = tid; jl < dl; jl += kBdThreads) a.output_scale[(inst * S_out) * d + j0 + jl] = 1.0;
   }
 
   for (int s = 1; s < S && status == PDQ_INSTANCE_OK; ++s) {
-    const double t_next = save_at[s];
-    while (t + a.eps < t_next && status == PDQ_INSTANCE_OK) {
-      const double dt_use = fmin(dt, t_next - t);  // clip_dt
-      if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
+    const W t_next = wide_from(save_at[s], T(0));
+    while (before(t, t_next) && status == PDQ_INSTANCE_OK) {
+      const T remaining = wide_diff(t_next, t);
+      const bool clipped = !(dt < remaining);  // clip_dt
+      const T dt_use = clipped ? remaining : dt;
+      if (!(dev_abs(dt_use) > T(1e-14) * fmax(T(1), dev_abs(T(wide_hi(t)))))) {
         status = PDQ_INSTANCE_DT_UNDERFLOW;
         break;
       }
@@ -202,132 +226,129 @@ __global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
         break;
       }
       ++attempts;
-      const T h = T(dt_use);
+      const T h = dt_use;
       T p[n], pinv[n];
       precon<T, NU>(h, p, pinv);
-      const T sq_h = dev_sqrt(dev_abs(h));
-      const T ell = dev_sqrt(p[OUT] * p[OUT] * dev_abs(h) * q1_out2 + damp * damp);
+      const T sq_h = fast_sqrt(dev_abs(h));
+      const T ell = observed_std(p[OUT], h, q1_out_norm, damp);
       const T* x = bufs[cur];
       T* y = bufs[cur ^ 1];
 
-      // ---- phase 1: extrapolated means; u(t+h) to shared memory ----
-      T mpk[kBdMaxDimsPerThread][n];
+      // ---- phase 1: extrapolated means staged in shared memory ----
+#pragma unroll 1
+      for (int jl = tid; jl < dl; jl += kBdThreads) {
+        const int g = j0 + jl;
+        T m[n];
 #pragma unroll
-      for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
-        const int jl = tid + k * kBdThreads;
-        if (k < dpt && jl < dl) {
-          const int g = j0 + jl;
-          T m[n], mp[n];
+        for (int i = 0; i < n; ++i) m[i] = x[i * d + g];
 #pragma unroll
-          for (int i = 0; i < n; ++i) m[i] = x[i * d + g];
+        for (int i = 0; i < n; ++i) {
+          T acc = T(0);
 #pragma unroll
-          for (int i = 0; i < n; ++i) {
-            T acc = T(0);
-#pragma unroll
-            for (int kk = i; kk < n; ++kk) acc += T(iwp_a<NU>(i, kk)) * pinv[kk] * m[kk];
-            mp[i] = p[i] * acc;
-            mpk[k][i] = mp[i];
-          }
-          ex[jl] = mp[0];
+          for (int kk = i; kk < n; ++kk) acc += T(iwp_a<NU>(i, kk)) * pinv[kk] * m[kk];
+          mps[i * dl + jl] = p[i] * acc;
         }
       }
       cluster.sync();
 
       // ---- phase 2: stencil, calibration, predict, update, error partial ----
-      const T* ex_left = cluster.map_shared_rank(ex, (rank - 1 + CL) % CL);
-      const T* ex_right = cluster.map_shared_rank(ex, (rank + 1) % CL);
-      double local = 0.0;
-      T newt[kBdMaxDimsPerThread];
-      T sig_new[kBdMaxDimsPerThread];
+      const T* ex_left = cluster.map_shared_rank(mps, (rank - 1 + CL) % CL);
+      const T* ex_right = cluster.map_shared_rank(mps, (rank + 1) % CL);
+      W local = wide_from(0.0, T(0));
       T pinv_abs[n];
 #pragma unroll
       for (int i = 0; i < n; ++i) pinv_abs[i] = dev_abs(pinv[i]);
+#pragma unroll 1
+      for (int jl = tid; jl < dl; jl += kBdThreads) {
+        const int g = j0 + jl;
+        const T left = jl > 0 ? mps[jl - 1] : ex_left[dl - 1];
+        const T right = jl < dl - 1 ? mps[jl + 1] : ex_right[0];
+        T mp[n];
 #pragma unroll
-      for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
-        newt[k] = T(0);
-        sig_new[k] = T(1);
-        const int jl = tid + k * kBdThreads;
-        if (k < dpt && jl < dl) {
-          const int g = j0 + jl;
-          const T left = jl > 0 ? ex[jl - 1] : ex_left[dl - 1];
-          const T right = jl < dl - 1 ? ex[jl + 1] : ex_right[0];
-          const T f = burgers_f(left, mpk[k][0], right, nu_visc, inv_dx);
-          const T mobs = mpk[k][OUT] - f;
-          // per-dimension residual_whitened_rms of fx.marginalise(apply_flat(m))
-          const T sigma = dev_div(dev_abs(mobs), ell);
-          const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma : T(1);
-          T L[n][n];
+        for (int i = 0; i < n; ++i) mp[i] = mps[i * dl + jl];
+        const T f = burgers_f(left, mp[0], right, nu_visc, inv_dx);
+        const T mobs = mp[OUT] - f;
+        // per-dimension residual_whitened_rms of fx.marginalise(apply_flat(m))
+        const T sigma = dev_div(dev_abs(mobs), ell);
+        const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma : T(1);
+        T L[n][n];
 #pragma unroll
-          for (int i = 0; i < n; ++i)
+        for (int i = 0; i < n; ++i)
 #pragma unroll
-            for (int j = 0; j < n; ++j) L[i][j] = (j <= i) ? x[(n + i * (i + 1) / 2 + j) * d + g] : T(0);
-          // the block-diagonal marginalise scales the factor by |p_inv| (ssm_impl_blockdiag.py:32)
-          T Lp[n][n];
+          for (int j = 0; j < n; ++j) L[i][j] = (j <= i) ? x[(n + i * (i + 1) / 2 + j) * d + g] : T(0);
+        // the block-diagonal marginalise scales the factor by |p_inv| (ssm_impl_blockdiag.py:32)
+        T Lp[n][n];
+        if constexpr (kNarrow) {
+          iso_predict_chol<T, NU>(a.q1f, L, p, pinv_abs, s_pred * sq_h, Lp);
+        } else {
           iso_predict_chol<T, NU>(a.q1, L, p, pinv_abs, s_pred * sq_h, Lp);
-          T gain[n], Lnew[n][n];
-          const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew);
-          T mnew[n];
-#pragma unroll
-          for (int i = 0; i < n; ++i) mnew[i] = mpk[k][i] - gain[i] * mobs;
-          // proposal -> the other buffer
-#pragma unroll
-          for (int i = 0; i < n; ++i) y[i * d + g] = mnew[i];
-#pragma unroll
-          for (int i = 0; i < n; ++i)
-#pragma unroll
-            for (int j = 0; j <= i; ++j) y[(n + i * (i + 1) / 2 + j) * d + g] = Lnew[i][j];
-          // error_residual_std: std = |sigma| l, error = std * h; reference max(|u0|, |u1|)
-          const T err_abs = dev_abs(sigma) * ell * h;
-          const T ref = fmax(dev_abs(x[g]), dev_abs(mnew[0]));
-          const T ratio = dev_div(err_abs, T(a.atol) + T(a.rtol) * ref);
-          local += double(ratio) * double(ratio);
-          newt[k] = dev_div(dev_abs(mobs), dev_abs(R_Y));
-          sig_new[k] = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma : T(1);
         }
-      }
-      // CTA reduction of the float64 partial (warp shuffles, then warps)
+        T gain[n], Lnew[n][n];
+        const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew);
+        T mnew[n];
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) local += __shfl_xor_sync(0xffffffffu, local, off);
+        for (int i = 0; i < n; ++i) mnew[i] = mp[i] - gain[i] * mobs;
+        // proposal -> the other buffer
+#pragma unroll
+        for (int i = 0; i < n; ++i) y[i * d + g] = mnew[i];
+#pragma unroll
+        for (int i = 0; i < n; ++i)
+#pragma unroll
+          for (int j = 0; j <= i; ++j) y[(n + i * (i + 1) / 2 + j) * d + g] = Lnew[i][j];
+        // error_residual_std: std = |sigma| l = |mobs|, error = std * h; reference max(|u0|, |u1|)
+        const T err_abs = dev_abs(mobs) * h;
+        const T ref = fmax(dev_abs(x[g]), dev_abs(mnew[0]));
+        const T ratio = dev_div(err_abs, atol + rtol * ref);
+        local = wide_add_sq(local, ratio);
+        newt[jl] = dev_abs(mobs) * fast_rcp(dev_abs(R_Y));
+        sig_new[jl] = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma : T(1);
+      }
+      // CTA reduction of the wide partial (warp butterflies, then warps in order)
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) local = wide_add_wide(local, wide_shfl_xor(local, off));
       if ((tid & 31) == 0) warp_sums[tid >> 5] = local;
       __syncthreads();
       if (tid == 0) {
-        double sum = 0.0;
+        W sum = warp_sums[0];
 #pragma unroll
-        for (int w = 0; w < kBdThreads / 32; ++w) sum += warp_sums[w];
+        for (int w = 1; w < kBdThreads / 32; ++w) sum = wide_add_wide(sum, warp_sums[w]);
         partial[par] = sum;
       }
       cluster.sync();
 
       // ---- phase 3: identical decision in every CTA of the cluster ----
-      double total = 0.0;
-      for (int r = 0; r < CL; ++r) total += *cluster.map_shared_rank(&partial[par], r);
+      W total = *cluster.map_shared_rank(&partial[par], 0);
+      for (int r = 1; r < CL; ++r) total = wide_add_wide(total, *cluster.map_shared_rank(&partial[par], r));
       par ^= 1;
-      const double norm2 = total / double(d);
+      const T norm2 = T(wide_hi(total)) / T(d);
       if (!(norm2 == norm2) || isinf(norm2)) {
         status = PDQ_INSTANCE_NONFINITE;
         break;
       }
-      const T ep = dev_fpow(T(norm2), T(-0.5 / n));
-      double factor;
+      const T ep = dev_fpow(norm2, T(-0.5 / n));
+      const bool accepted = wide_le(total, T(d));
+      T factor;
       if (a.control == PDQ_CONTROL_INTEGRAL) {
-        factor = a.safety * double(ep);
+        factor = safety * ep;
       } else {
-        factor = a.safety * double(dev_fpow(ep, T(a.exp_i))) * double(dev_fpow(dev_div(ep, T(pi_prev)), T(a.exp_p)));
-        if (norm2 <= 1.0) pi_prev = double(ep);
+        factor = safety * dev_fpow(ep, cst<T>(a.exp_i, a.exp_i_f)) *
+                 dev_fpow(dev_div(ep, pi_prev), cst<T>(a.exp_p, a.exp_p_f));
+        if (accepted) pi_prev = ep;
       }
-      factor = fmax(a.factor_min, fmin(factor, a.factor_max));
+      factor = fmax(factor_min, fmin(factor, factor_max));
       dt = factor * dt_use;
-      if (norm2 <= 1.0) {
+      if (accepted) {
         cur ^= 1;
-        t = t + dt_use;
+        if constexpr (kNarrow) {
+          t = clipped ? t_next : wide_add(t, dt_use);
+        } else {
+          t = t + dt_use;
+        }
         ++num_steps;
-#pragma unroll
-        for (int k = 0; k < kBdMaxDimsPerThread; ++k) {
-          const int jl = tid + k * kBdThreads;
-          if (k < dpt && jl < dl) {
-            sig[k] = sig_new[k];
-            if (a.solver == PDQ_SOLVER_MLE) mle_sum[j0 + jl] += double(newt[k]) * double(newt[k]);
-          }
+#pragma unroll 1
+        for (int jl = tid; jl < dl; jl += kBdThreads) {
+          sig[jl] = sig_new[jl];
+          if (a.solver == PDQ_SOLVER_MLE) mle_sum[j0 + jl] = wide_add_sq(mle_sum[j0 + jl], newt[jl]);
         }
         if (a.solver == PDQ_SOLVER_MLE) ++num_data;
       }
@@ -336,7 +357,7 @@ __global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
     // clip_dt: every checkpoint is an exact landing (interp_at_t1)
     if (!a.terminal_only || s == S - 1) {
       const int s_out = a.terminal_only ? 0 : s;
-      write_checkpoint(s_out, t);
+      write_checkpoint(s_out, wide_value(t));
       if (a.solver != PDQ_SOLVER_MLE) write_scale(s_out);
     }
   }
@@ -349,7 +370,7 @@ __global__ void __launch_bounds__(kBdThreads) bd_adaptive_kernel(BdArgs a) {
       const int64_t rec = inst * S_out + s;
       for (int jl = tid; jl < dl; jl += kBdThreads) {
         const int g = j0 + jl;
-        double sc = num_data > 0 ? sqrt(mle_sum[g] / num_data) : 0.0;
+        double sc = num_data > 0 ? sqrt(wide_value(mle_sum[g]) / num_data) : 0.0;
         if (a.correct) sc /= sqrt(double(last));
         a.output_scale[rec * d + g] = sc;
         double* uc = a.u_chol + (rec * d + g) * n * n;

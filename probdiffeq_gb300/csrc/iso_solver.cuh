@@ -76,6 +76,17 @@ PDQ_D void precon(T h, T (&p)[NU + 1], T (&pinv)[NU + 1]) {
   }
 }
 
+// Observed std of the linearised TS0 residual at unit output scale,
+//   l = sqrt(p_OUT^2 |h| ||Q1[OUT]||^2 + damp^2),
+// formed as |p_OUT| sqrt|h| ||Q1[OUT]|| without squaring p_OUT: the square
+// leaves the float32 range for steps below ~1e-5 (nu = 4), while l itself
+// stays representable down to the step-underflow bound.
+template <typename T>
+PDQ_D T observed_std(T p_out, T h, T q1_out_norm, T damp) {
+  const T a = dev_abs(p_out) * fast_sqrt(dev_abs(h)) * q1_out_norm;
+  return damp == T(0) ? a : fast_sqrt(a * a + damp * damp);
+}
+
 // IWP predict of the isotropic mean (marginalise, ssm_impl_isotropic.py:81-89):
 //   mp = p * A (pinv * m)
 template <typename T, int NU, int D>
@@ -353,6 +364,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   T q1_out2 = T(0);
 #pragma unroll
   for (int j = 0; j < n; ++j) q1_out2 += cst<T>(a.q1[OUT][j], a.q1f[OUT][j]) * cst<T>(a.q1[OUT][j], a.q1f[OUT][j]);
+  const T q1_out_norm = dev_sqrt(q1_out2);
 
   if (!a.terminal_only) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, wide_value(t), 0);
 
@@ -408,7 +420,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           // fx.marginalise(apply_flat(m)) with unit scale: observed std
           // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
           // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
-          const T ell = fast_sqrt(p[OUT] * p[OUT] * dev_abs(h) * q1_out2 + damp * damp);
+          const T ell = observed_std(p[OUT], h, q1_out_norm, damp);
           const T sigma_loc = dev_div(rms_mobs, ell);
 
           const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
@@ -430,7 +442,9 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - gain[i] * mobs[j];
 
           // ---- error estimate (error_residual_std, solvers.py:925-996) ----
-          const T err_abs = dev_abs(sigma_loc) * ell * h;  // std of rescaled observed * dt^1/1!
+          // std of the observed residual rescaled by sigma_loc = rms / l is rms:
+          // error = rms * dt^1/1! (no division by a possibly tiny l)
+          const T err_abs = rms_mobs * h;
           W sumsq = wide_from(0.0, T(0));
 #pragma unroll
           for (int j = 0; j < D; ++j) {

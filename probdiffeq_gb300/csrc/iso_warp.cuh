@@ -90,6 +90,7 @@ __global__ void __launch_bounds__(256, MINB) iso_warp_kernel(IsoArgs a) {
   T q1_out2 = T(0);
 #pragma unroll
   for (int j = 0; j < n; ++j) q1_out2 += T(a.q1[OUT][j]) * T(a.q1[OUT][j]);
+  const T q1_out_norm = dev_sqrt(q1_out2);
   // this lane's column of Q1^T (bottom block of the predict matrix), unscaled,
   // and row l of the IWP transition A (zero for lanes l >= n)
   T q1col[n], arow[n];
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(256, MINB) iso_warp_kernel(IsoArgs a) {
         mobs2 += mobs[j] * mobs[j];
       }
       const T rms_mobs = dev_sqrt(mobs2 * T(1.0 / D));
-      const T ell = dev_sqrt(p[OUT] * p[OUT] * dev_abs(h) * q1_out2 + damp * damp);
+      const T ell = observed_std(p[OUT], h, q1_out_norm, damp);
       const T sigma_loc = dev_div(rms_mobs, ell);
       const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
       const T sq = s_pred * dev_sqrt(dev_abs(h));
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(256, MINB) iso_warp_kernel(IsoArgs a) {
 #pragma unroll
       for (int j = 0; j < D; ++j) mnew0[j] = shfl(mask, mrow[j], 0, LPI);
       // ---- error estimate, control, acceptance (identical in every lane) ----
-      const T err_abs = dev_abs(sigma_loc) * ell * h;
+      const T err_abs = rms_mobs * h;  // |sigma_loc| l = rms
       double sumsq = 0.0;
 #pragma unroll
       for (int j = 0; j < D; ++j) {

@@ -251,6 +251,17 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.damp = c->damp;
     a.max_attempts = c->max_attempts;
     iwp_q1(c->num_derivatives, a.q1);
+    for (int i = 0; i < pdq::kMaxN; ++i)
+      for (int j = 0; j < pdq::kMaxN; ++j) a.q1f[i][j] = float(a.q1[i][j]);
+    a.safety_f = float(a.safety);
+    a.factor_min_f = float(a.factor_min);
+    a.factor_max_f = float(a.factor_max);
+    a.exp_i_f = float(a.exp_i);
+    a.exp_p_f = float(a.exp_p);
+    a.atol_f = float(a.atol);
+    a.rtol_f = float(a.rtol);
+    a.eps_f = float(a.eps);
+    a.damp_f = float(a.damp);
     a.save_at = args->save_at;
     a.params = args->params;
     a.y0 = args->y0;

@@ -164,6 +164,17 @@ PDQ_D FloatPair wide_add_sq(FloatPair x, float y) {
   const FloatPair s = two_sum(x.hi, p);
   return fast_two_sum(s.hi, s.lo + (pe + x.lo));
 }
+// x + y for two wide values (reductions)
+PDQ_D double wide_add_wide(double x, double y) { return x + y; }
+PDQ_D FloatPair wide_add_wide(FloatPair x, FloatPair y) {
+  const FloatPair s = two_sum(x.hi, y.hi);
+  return fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+// butterfly exchange of a wide value within a warp
+PDQ_D double wide_shfl_xor(double x, int lane_mask) { return __shfl_xor_sync(0xffffffffu, x, lane_mask); }
+PDQ_D FloatPair wide_shfl_xor(FloatPair x, int lane_mask) {
+  return {__shfl_xor_sync(0xffffffffu, x.hi, lane_mask), __shfl_xor_sync(0xffffffffu, x.lo, lane_mask)};
+}
 // x - y rounded to the narrow type (the difference of two nearby times)
 PDQ_D double wide_diff(double x, double y) { return x - y; }
 PDQ_D float wide_diff(FloatPair x, FloatPair y) {
@@ -183,17 +194,29 @@ struct Factorial<0> {
   static constexpr double value = 1.0;
 };
 
-PDQ_HD constexpr double factorial(int k) { return k <= 1 ? 1.0 : k * factorial(k - 1); }
-
-PDQ_HD constexpr double binom(int n, int k) {
-  return (k < 0 || k > n) ? 0.0 : factorial(n) / (factorial(k) * factorial(n - k));
+// Small-integer combinatorics as straight loops (no recursion), so that
+// with the compile-time arguments of the unrolled kernels they fold to
+// immediates instead of becoming float64 calls inside the step loop.
+PDQ_HD constexpr double factorial(int k) {
+  double r = 1.0;
+  for (int i = 2; i <= k; ++i) r *= double(i);
+  return r;
 }
+
+PDQ_HD constexpr int binom_int(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  int r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return r;
+}
+
+PDQ_HD constexpr double binom(int n, int k) { return double(binom_int(n, k)); }
 
 // IWP transition matrix in preconditioned coordinates (the reference's
 // flip(Pascal)): A[i][j] = binom(nu - i, nu - j) for j >= i, else 0.
 template <int NU>
-PDQ_HD constexpr double iwp_a(int i, int j) {
-  return j >= i ? binom(NU - i, NU - j) : 0.0;
+PDQ_HD constexpr int iwp_a(int i, int j) {
+  return j >= i ? binom_int(NU - i, NU - j) : 0;
 }
 
 // ---------------------------------------------------------------------------
