@@ -9,8 +9,9 @@ template <typename T, int NU, class F>
 cudaError_t launch_lml_nu(const LmlArgs& a, cudaStream_t stream) {
   cudaError_t e = ensure_stack<lml_kernel<T, NU, F>>();
   if (e != cudaSuccess) return e;
-  const int block = 32;
-  lml_kernel<T, NU, F><<<unsigned((a.B + block - 1) / block), block, 0, stream>>>(a);
+  const int block = kLmlThreads;
+  const int64_t threads = a.B * a.lanes_per_sample;
+  lml_kernel<T, NU, F><<<unsigned((threads + block - 1) / block), block, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
@@ -21,11 +22,6 @@ cudaError_t launch_lml_precision(const LmlArgs& a, int nu, cudaStream_t stream) 
     case 3: return launch_lml_nu<T, 3, F>(a, stream);
     default: return cudaErrorInvalidValue;
   }
-}
-
-template <int NU, int D, int P>
-constexpr size_t lml_cond_floats() {
-  return size_t(2 * (NU + 1) * (NU + 1) + (NU + 1) * D) * (P + 1) + 2 * (NU + 1);
 }
 
 }  // namespace pdq

@@ -14,16 +14,20 @@
 //     IsotropicNormal.logpdf_flat            ssm_impl_api.py:118-124, ssm_impl_isotropic.py:217-278
 //   Taylor-mode initial derivatives          _probdiffeq/jet_expansion_algorithms.py:49-103
 //
-// Derivative: every value carries P tangents (forward mode, one direction per
-// parameter).  The rules are the reference's: qr_r has the custom JVP
-// R_dot = Q^T M_dot with Q held constant (backend/linalg.py:13-37), so the
-// reflectors / rotations computed from the values are applied to the tangent
-// matrices and the tangent of a triangular factor is a full matrix;
-// triangular solves differentiate through the triangle only (back
-// substitution on dual numbers); the time step carries no tangent (the
-// reference stops gradients through dt).  For the 3 parameters of the
-// configurations this costs about what one reverse sweep costs and needs no
-// checkpoint storage.  The log-likelihood sum and its tangents are float64.
+// Derivative: forward mode, one tangent direction per thread.  A parameter
+// sample is handled by P threads, thread k carrying d/d theta_k, and each of
+// them recomputes the value path: redundant arithmetic, but the state of one
+// thread is a value and one tangent (registers instead of local-memory
+// spills for P tangents) and the threads never communicate.  The rules are
+// the reference's: qr_r has the custom JVP R_dot = Q^T M_dot with Q held
+// constant (backend/linalg.py:13-37), so the reflectors / rotations computed
+// from the values are applied to the tangent matrices and the tangent of a
+// triangular factor is a full matrix; triangular solves differentiate
+// through the triangle only (back substitution on dual numbers); the time
+// step carries no tangent (the reference stops gradients through dt).  For
+// the 3 parameters of the configurations this needs no checkpointed
+// re-computation; the backward conditionals at the observations are stored.
+// The log-likelihood sum and its tangents are float64.
 #pragma once
 
 #include "iso_solver.cuh"
@@ -57,9 +61,14 @@ PDQ_HD Dual<T, K> dual_abs_scale(T s, const Dual<T, K>& a) {  // |s| * a for a c
   return (s < T(0) ? -s : s) * a;
 }
 
+// One warp per block: a batch of 1024 samples x 3 tangent lanes is 96
+// warps, fewer than the SMs, so each warp gets an SM to itself.
+constexpr int kLmlThreads = 32;
+
 struct LmlArgs {
   int64_t B;
   int32_t num_steps, save_every, average_pdfs, with_gradient;
+  int32_t lanes_per_sample;  // P with the gradient (one tangent direction per thread), else 1
   double t0, dt, damp;
   double q1[kMaxN][kMaxN];
   const double* params;  // (B, P)
@@ -199,18 +208,24 @@ PDQ_D void lml_marginalise(const LmlCond<T, P, NU, D>& c, const Dual<T, P> (&m)[
 }
 
 template <typename T, int NU, class F>
-__global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
+__global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
   constexpr int n = NU + 1;
   constexpr int D = F::D;
-  constexpr int P = F::P;
+  constexpr int P = F::P;   // parameters
+  constexpr int TG = 1;     // tangent directions carried by one thread
   constexpr int OUT = 1;
-  using DT = Dual<T, P>;
-  using DD = Dual<double, P>;
-  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  using DT = Dual<T, TG>;
+  using DD = Dual<double, TG>;
+  // lanes_per_sample threads per parameter sample, each carrying the tangent
+  // of one parameter (the value path is computed redundantly by each)
+  const int lanes = a.lanes_per_sample;
+  const int64_t gtid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t b = gtid / lanes;
+  const int dir = int(gtid % lanes);
   if (b >= a.B) return;
   const int num_obs = a.num_steps / a.save_every + 1;
   constexpr int CF = 2 * n * n + n * D;  // duals per stored conditional (A, X, xi)
-  T* ws = reinterpret_cast<T*>(a.workspace) + b * int64_t(num_obs - 1) * (CF * (P + 1) + 2 * n);
+  T* ws = reinterpret_cast<T*>(a.workspace) + gtid * int64_t(num_obs - 1) * (CF * (TG + 1) + 2 * n);
 
   // ---- parameters with unit tangents; Taylor-mode initial derivatives ----
   DD pd[P];
@@ -218,9 +233,9 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
 #pragma unroll
   for (int k = 0; k < P; ++k) {
     pd[k] = DD(a.params[b * P + k]);
-    pd[k].g[k] = 1.0;
+    pd[k].g[0] = (k == dir) ? 1.0 : 0.0;
     pt[k] = DT(T(pd[k].v));
-    pt[k].g[k] = T(1);
+    pt[k].g[0] = (k == dir) ? T(1) : T(0);
   }
   DD y0[D];
 #pragma unroll
@@ -235,12 +250,12 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
     for (int j = 0; j < D; ++j) {
       m[i][j].v = T(tc[i][j].v);
 #pragma unroll
-      for (int k = 0; k < P; ++k) m[i][j].g[k] = T(tc[i][j].g[k]);
+      for (int k = 0; k < TG; ++k) m[i][j].g[k] = T(tc[i][j].g[k]);
     }
 #pragma unroll
     for (int j = 0; j < n; ++j) L[i][j] = DT(T(0));
   }
-  LmlCond<T, P, NU, D> bw;
+  LmlCond<T, TG, NU, D> bw;
   lml_cond_identity(bw);
 
   // constants of the fixed step: p, p_inv, the noise factor sqrt(dt) Q1
@@ -266,7 +281,7 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
         M[n + r][c] = acc;                               // R_X_F = (A chol)^T
         M[n + r][n + c] = dev_abs(pinv[c]) * L[c][r];   // R_X = chol^T
       }
-    qr_qconst<T, P, 2 * n, 2 * n>(M);
+    qr_qconst<T, TG, 2 * n, 2 * n>(M);
     // G^T = R_Y^{-1} R12 by back substitution through the triangle
     DT Gt[n][n];
 #pragma unroll
@@ -293,7 +308,7 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
         mobs[i][j] = acc;
         mp[i][j] = p[i] * acc;
       }
-    LmlCond<T, P, NU, D> cn;  // the new backward conditional
+    LmlCond<T, TG, NU, D> cn;  // the new backward conditional
 #pragma unroll
     for (int i = 0; i < n; ++i) {
 #pragma unroll
@@ -318,7 +333,7 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
 #pragma unroll
       for (int i = 0; i < n; ++i) Tv[i] = bw.tl[i] * cn.to[i];
       DT Mm[2 * n][n];
-      LmlCond<T, P, NU, D> out;
+      LmlCond<T, TG, NU, D> out;
 #pragma unroll
       for (int i = 0; i < n; ++i) {
 #pragma unroll
@@ -341,7 +356,7 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
           out.xi[i][j] = x;
         }
       }
-      qr_qconst<T, P, 2 * n, n>(Mm);
+      qr_qconst<T, TG, 2 * n, n>(Mm);
 #pragma unroll
       for (int i = 0; i < n; ++i) {
 #pragma unroll
@@ -364,9 +379,9 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
       for (int c = 1; c <= n; ++c) Mu[r][c] = Lp[c - 1][r - 1];
     }
 #pragma unroll
-    for (int r = OUT + 1; r >= 1; --r) givens_qconst<T, P, n + 1, n + 1>(Mu, r - 1, r, 0);
+    for (int r = OUT + 1; r >= 1; --r) givens_qconst<T, TG, n + 1, n + 1>(Mu, r - 1, r, 0);
 #pragma unroll
-    for (int c = 1; c <= OUT; ++c) givens_qconst<T, P, n + 1, n + 1>(Mu, c, c + 1, c);
+    for (int c = 1; c <= OUT; ++c) givens_qconst<T, TG, n + 1, n + 1>(Mu, c, c + 1, c);
     DT res[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) res[j] = mp[OUT][j] - f[j];
@@ -384,7 +399,7 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
     }
     // ---- checkpoint at an observation: store the conditional, reset ----
     if (step % a.save_every == 0) {
-      T* dst = ws + int64_t(step / a.save_every - 1) * (CF * (P + 1) + 2 * n);
+      T* dst = ws + int64_t(step / a.save_every - 1) * (CF * (TG + 1) + 2 * n);
       int o = 0;
 #pragma unroll
       for (int i = 0; i < n; ++i)
@@ -392,10 +407,10 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
         for (int j = 0; j < n; ++j) {
           dst[o++] = bw.A[i][j].v;
 #pragma unroll
-          for (int k = 0; k < P; ++k) dst[o++] = bw.A[i][j].g[k];
+          for (int k = 0; k < TG; ++k) dst[o++] = bw.A[i][j].g[k];
           dst[o++] = bw.X[i][j].v;
 #pragma unroll
-          for (int k = 0; k < P; ++k) dst[o++] = bw.X[i][j].g[k];
+          for (int k = 0; k < TG; ++k) dst[o++] = bw.X[i][j].g[k];
         }
 #pragma unroll
       for (int i = 0; i < n; ++i)
@@ -403,7 +418,7 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
         for (int j = 0; j < D; ++j) {
           dst[o++] = bw.xi[i][j].v;
 #pragma unroll
-          for (int k = 0; k < P; ++k) dst[o++] = bw.xi[i][j].g[k];
+          for (int k = 0; k < TG; ++k) dst[o++] = bw.xi[i][j].g[k];
         }
 #pragma unroll
       for (int i = 0; i < n; ++i) {
@@ -420,32 +435,32 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
     // rv_at_t1 = posterior1.conditional.marginalise(marginal); the last step
     // lands on the last observation, so that conditional is the identity
     DT rm[n][D], rL[n][n];
-    lml_marginalise<T, P, NU, D>(bw, m, L, rm, rL);
+    lml_marginalise<T, TG, NU, D>(bw, m, L, rm, rL);
     const double LOG2PI = 1.8378770664093453;
     int num = 0;
     for (int k = num_obs - 1; k >= 0; --k) {
       if (k < num_obs - 1) {
-        LmlCond<T, P, NU, D> c;
-        const T* src = ws + int64_t(k) * (CF * (P + 1) + 2 * n);
+        LmlCond<T, TG, NU, D> c;
+        const T* src = ws + int64_t(k) * (CF * (TG + 1) + 2 * n);
         int o = 0;
         for (int i = 0; i < n; ++i)
           for (int j = 0; j < n; ++j) {
             c.A[i][j].v = src[o++];
-            for (int q = 0; q < P; ++q) c.A[i][j].g[q] = src[o++];
+            for (int q = 0; q < TG; ++q) c.A[i][j].g[q] = src[o++];
             c.X[i][j].v = src[o++];
-            for (int q = 0; q < P; ++q) c.X[i][j].g[q] = src[o++];
+            for (int q = 0; q < TG; ++q) c.X[i][j].g[q] = src[o++];
           }
         for (int i = 0; i < n; ++i)
           for (int j = 0; j < D; ++j) {
             c.xi[i][j].v = src[o++];
-            for (int q = 0; q < P; ++q) c.xi[i][j].g[q] = src[o++];
+            for (int q = 0; q < TG; ++q) c.xi[i][j].g[q] = src[o++];
           }
         for (int i = 0; i < n; ++i) {
           c.tl[i] = src[o++];
           c.to[i] = src[o++];
         }
         DT pm[n][D], pL[n][n];
-        lml_marginalise<T, P, NU, D>(c, rm, rL, pm, pL);
+        lml_marginalise<T, TG, NU, D>(c, rm, rL, pm, pL);
 #pragma unroll
         for (int i = 0; i < n; ++i) {
 #pragma unroll
@@ -465,7 +480,7 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
 #pragma unroll
         for (int c = 1; c <= n; ++c) Mo[r][c] = rL[c - 1][r - 1];
       }
-      givens_qconst<T, P, n + 1, n + 1>(Mo, 0, 1, 0);
+      givens_qconst<T, TG, n + 1, n + 1>(Mo, 0, 1, 0);
       const DT ry = Mo[0][0];
       // logpdf of the observed N(m[0], ry^2) at the data, summed over d
       DD pdf_n(0.0);
@@ -479,7 +494,7 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
         const DT w = dx / ry;
         pdf_n.v += -0.5 * (2.0 * log(double(ryv)) + double(w.v) * double(w.v) + LOG2PI);
 #pragma unroll
-        for (int q = 0; q < P; ++q)
+        for (int q = 0; q < TG; ++q)
           pdf_n.g[q] += -0.5 * (2.0 * double(ry.g[q]) / double(ry.v) + 2.0 * double(w.v) * double(w.g[q]));
 #pragma unroll
         for (int i = 0; i < n; ++i) rm[i][j] = rm[i][j] + ginv[i] * dx;
@@ -491,23 +506,22 @@ __global__ void __launch_bounds__(32) lml_kernel(LmlArgs a) {
       if (a.average_pdfs && num > 0) {
         pdf.v = (pdf.v * num + pdf_n.v) / (num + 1);
 #pragma unroll
-        for (int q = 0; q < P; ++q) pdf.g[q] = (pdf.g[q] * num + pdf_n.g[q]) / (num + 1);
+        for (int q = 0; q < TG; ++q) pdf.g[q] = (pdf.g[q] * num + pdf_n.g[q]) / (num + 1);
       } else {
         pdf.v += pdf_n.v;
 #pragma unroll
-        for (int q = 0; q < P; ++q) pdf.g[q] += pdf_n.g[q];
+        for (int q = 0; q < TG; ++q) pdf.g[q] += pdf_n.g[q];
       }
       ++num;
     }
     if (!(pdf.v == pdf.v)) status = PDQ_INSTANCE_NONFINITE;
   }
   const double nan = __longlong_as_double(0x7ff8000000000000ULL);
-  a.lml[b] = status == PDQ_INSTANCE_OK ? pdf.v : nan;
-  if (a.grad) {
-#pragma unroll
-    for (int q = 0; q < P; ++q) a.grad[b * P + q] = status == PDQ_INSTANCE_OK ? pdf.g[q] : nan;
+  if (dir == 0) {
+    a.lml[b] = status == PDQ_INSTANCE_OK ? pdf.v : nan;
+    a.status[b] = status;
   }
-  a.status[b] = status;
+  if (a.grad && dir < P) a.grad[b * P + dir] = status == PDQ_INSTANCE_OK ? pdf.g[0] : nan;
 }
 
 }  // namespace pdq

@@ -371,12 +371,15 @@ static pdq_status lml_check(const pdq_config* c, int64_t B, int32_t num_steps, i
   return PDQ_SUCCESS;
 }
 
+static int lml_num_params(const pdq_config* c) { return c->field == PDQ_FIELD_FITZHUGH_NAGUMO ? 3 : 4; }
+
 static size_t lml_bytes(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every) {
   const int n = c->num_derivatives + 1, d = c->ode_dim;
-  const int P = c->field == PDQ_FIELD_FITZHUGH_NAGUMO ? 3 : 4;
-  const size_t per = size_t(2 * n * n + n * d) * (P + 1) + 2 * n;
+  const int P = lml_num_params(c);
+  // per thread (P threads per sample, one tangent each) and stored conditional
+  const size_t per = size_t(2 * n * n + n * d) * 2 + 2 * n;
   const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
-  return size_t(B) * size_t(num_steps / save_every) * per * elem;
+  return size_t(B) * size_t(P) * size_t(num_steps / save_every) * per * elem;
 }
 
 pdq_status pdq_lml_workspace_size(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every, size_t* bytes) {
@@ -405,6 +408,7 @@ pdq_status pdq_lml_fixed_grid(const pdq_config* c, const pdq_lml_args* args, voi
   a.save_every = args->save_every;
   a.average_pdfs = args->average_pdfs ? 1 : 0;
   a.with_gradient = args->with_gradient ? 1 : 0;
+  a.lanes_per_sample = args->with_gradient ? lml_num_params(c) : 1;
   a.t0 = args->t0;
   a.dt = args->dt;
   a.damp = c->damp;
