@@ -10,6 +10,8 @@ Public modules:
   * ``probdiffeq_gb300.ivpsolve`` / ``probdiffeq_gb300.probdiffeq`` -- the
     reference's constructor and solve API, lowered to one native call;
   * ``probdiffeq_gb300.ensemble`` -- batched solves on tensors;
+  * ``probdiffeq_gb300.autograd`` -- the LML kernel as a torch.autograd.Function;
+  * ``probdiffeq_gb300.replicas`` -- sharding independent instances over ranks;
   * ``probdiffeq_gb300._native`` -- the ctypes binding of ``include/pdq.h``.
 """
 
