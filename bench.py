@@ -588,7 +588,8 @@ def run_burgers_blockdiag(args):
     with ClockSampler(0) as clk:
         for prec in args.precisions.split(","):
             cfg = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=d, ssm="blockdiag", solver="dynamic",
-                                       precision=prec, atol=1e-4, rtol=1e-4, clip_dt=True, max_attempts=1 << 26)
+                                       precision=prec, atol=1e-4, rtol=1e-4, clip_dt=True, max_attempts=1 << 26,
+                                       constraint=args.constraint or "ts0")
             outs = _native.alloc_outputs(cfg, B, 2, True, device)
             t = timed_region(torch, stream, lambda: _native.solve_adaptive(cfg, sa, prm, u0, dt0, True, outs,
                                                                              stream=stream), args.steps, args.warmup)
@@ -599,7 +600,8 @@ def run_burgers_blockdiag(args):
                          "status_ok": int((outs["status"] == 0).sum())}
     first = args.precisions.split(",")[0]
     cfg = {"workload": "burgers_blockdiag", "instances": B, "d": d, "nu_visc": 0.01, "t_span": [0.0, t1],
-           "num_derivatives": 3, "ssm": "blockdiag", "constraint": "ts0", "solver": "dynamic", "rtol": 1e-4, "atol": 1e-4}
+           "num_derivatives": 3, "ssm": "blockdiag", "constraint": args.constraint or "ts0", "solver": "dynamic",
+           "rtol": 1e-4, "atol": 1e-4}
     print(json.dumps(base_line("ensemble IVP solves/s", res[first]["solves_per_s"], "solves/s", args,
                                res[first]["ms_per_step"], True, first, cfg, by_precision=res, gpu_launches=args.steps,
                                clocks=clk.summary())))
@@ -654,6 +656,8 @@ def main():
     ap.add_argument("--mu-max", type=float, default=1000.0, help="vdp_dense: mu ~ log-uniform [1, mu_max]")
     ap.add_argument("--t1", type=float, default=1.0, help="burgers_blockdiag: end time")
     ap.add_argument("--precisions", default="float32,float64", help="vdp_dense / burgers_blockdiag precisions")
+    ap.add_argument("--constraint", default=None, choices=["ts0", "ts1"],
+                    help="burgers_blockdiag: linearisation (ts0 is the configuration's; ts1 uses the Jacobian diagonal)")
     args = ap.parse_args()
     if args.impl == "reference":
         args.warmup = max(args.warmup, 1)

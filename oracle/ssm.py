@@ -275,6 +275,34 @@ class IsoTs0:
         return IsoCond.from_linop_and_noise(linop, bias)
 
 
+class IsoTs1:
+    """IsotropicResidual (ssm_impl_isotropic.py:320-355) for the ODE residual u' - f(u).
+
+    The residual comes from ``problems.residual_from_ode`` (problems.py:518-532);
+    the Jacobian of the flat residual (1, d) w.r.t. the mean (n, d) is
+    materialised and traced along d (jacobians.py:100-106), then divided by d,
+    so every dimension shares the (1, n) linear operator; the bias is
+    r(m) - J m.
+    """
+
+    residual_order = 2  # num_tcoeffs_in_args of the residual = 1 + 1 (ssm_impl_api.py:163-165)
+
+    def __init__(self, vf, output_index=1, num_in=1):
+        self.vf, self.output_index, self.num_in = vf, output_index, num_in
+
+    def residual(self, x, t):
+        return (x[self.output_index] - self.vf(x[: self.num_in], t))[None, :]  # (1, d)
+
+    def linearize(self, rv, damp, t):
+        mean = rv.mean
+        n, d = mean.shape
+        fx = self.residual(mean, t)
+        jac = torch.func.jacfwd(lambda x: self.residual(x, t))(mean)  # (1, d, n, d)
+        trace = torch.diagonal(jac, dim1=1, dim2=3).sum(-1) / d       # (1, n)
+        bias = IsoNormal(fx - trace @ mean, torch.full((1, 1), float(damp), dtype=mean.dtype))
+        return IsoCond.from_linop_and_noise(trace, bias)
+
+
 class IsoSSM:
     """state_space_model_isotropic (ssm_impl_isotropic.py:406-482)."""
 
@@ -291,6 +319,9 @@ class IsoSSM:
 
     def constraint_ode_ts0(self, vf):
         return IsoTs0(vf)
+
+    def constraint_ode_ts1(self, vf):
+        return IsoTs1(vf)
 
 
 # --------------------------------------------------------------------------
@@ -466,6 +497,34 @@ class BdTs0:
         return BdCond.from_linop_and_noise(linop, bias)
 
 
+class BdTs1:
+    """BlockDiagResidual (ssm_impl_blockdiag.py:147-183) for the ODE residual u' - f(u).
+
+    The Jacobian of the residual (1, d) w.r.t. the coefficients (n, d) is
+    materialised and its diagonal along d taken (jacobians.py:108-113): the
+    (d, 1, n) per-dimension operators J_j = d r_j / d x[:, j]; the bias is
+    r(m) - J m per dimension.
+    """
+
+    residual_order = 2
+
+    def __init__(self, vf, output_index=1, num_in=1):
+        self.vf, self.output_index, self.num_in = vf, output_index, num_in
+
+    def residual(self, x, t):  # x (n, d) -> (1, d)
+        return (x[self.output_index] - self.vf(x[: self.num_in], t))[None, :]
+
+    def linearize(self, rv, damp, t):
+        x = rv.mean.T  # (n, d)
+        d, n = rv.mean.shape
+        fx = self.residual(x, t).T  # (d, 1)
+        jac = torch.func.jacfwd(lambda z: self.residual(z, t))(x)  # (1, d, n, d)
+        diag = torch.diagonal(jac, dim1=1, dim2=3).permute(2, 0, 1)  # (d, 1, n)
+        fx = fx - torch.einsum("din,dn->di", diag, rv.mean)
+        bias = BdNormal(fx, float(damp) * torch.ones((d, 1, 1), dtype=rv.mean.dtype))
+        return BdCond.from_linop_and_noise(diag, bias)
+
+
 class BdSSM:
     """state_space_model_blockdiag (ssm_impl_blockdiag.py:460-547)."""
 
@@ -483,6 +542,9 @@ class BdSSM:
 
     def constraint_ode_ts0(self, vf):
         return BdTs0(vf)
+
+    def constraint_ode_ts1(self, vf):
+        return BdTs1(vf)
 
 
 # --------------------------------------------------------------------------

@@ -47,6 +47,7 @@ constexpr int kBdMaxDimsPerThread = 8;
 struct BdArgs {
   int64_t B;
   int32_t S, terminal_only, solver, control, correct, d, cluster;
+  int32_t ts1;  // 1: TS1 with the Jacobian diagonal along d (per-dimension H_j = [-dfj/duj, 1, 0, ...])
   double safety, factor_min, factor_max, exp_i, exp_p;
   double atol, rtol, eps, damp;
   int64_t max_attempts;
@@ -176,6 +177,8 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
 #pragma unroll
   for (int j = 0; j < n; ++j) q1_out2 += cst<T>(a.q1[OUT][j], a.q1f[OUT][j]) * cst<T>(a.q1[OUT][j], a.q1f[OUT][j]);
   const T q1_out_norm = dev_sqrt(q1_out2);
+  const T q00 = cst<T>(a.q1[0][0], a.q1f[0][0]), q10 = cst<T>(a.q1[1][0], a.q1f[1][0]),
+          q11 = cst<T>(a.q1[1][1], a.q1f[1][1]);
 
   auto before = [&](const W& x, const W& y) -> bool {
     if constexpr (kNarrow) {
@@ -230,7 +233,13 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       T p[n], pinv[n];
       precon<T, NU>(h, p, pinv);
       const T sq_h = fast_sqrt(dev_abs(h));
-      const T ell = observed_std(p[OUT], h, q1_out_norm, damp);
+      // TS1 (ssm_impl_blockdiag.py:147-183, jacobians.py:108-113): the Burgers
+      // Jacobian's diagonal is d f_j / d u_j = -2 nu / dx^2 for every j (the
+      // central-difference flux term does not involve u_j), so H_j = [h0, 1, 0, ...]
+      // with one h0 for all dimensions
+      const T h0 = a.ts1 ? T(2) * nu_visc * inv_dx * inv_dx : T(0);
+      const T ell = a.ts1 ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
+                          : observed_std(p[OUT], h, q1_out_norm, damp);
       const T* x = bufs[cur];
       T* y = bufs[cur ^ 1];
 
@@ -284,7 +293,7 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
           iso_predict_chol<T, NU>(a.q1, L, p, pinv_abs, s_pred * sq_h, Lp);
         }
         T gain[n], Lnew[n][n];
-        const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew);
+        const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew, h0);
         T mnew[n];
 #pragma unroll
         for (int i = 0; i < n; ++i) mnew[i] = mp[i] - gain[i] * mobs;

@@ -31,6 +31,7 @@ constexpr int kMaxN = 8;
 struct IsoArgs {
   int64_t B;
   int32_t S, terminal_only, solver, control, clip_dt, correct;
+  int32_t ts1;  // 0: TS0 (H = e_1); 1: TS1 with the Jacobian trace along d (H = [-tr J_f / d, 1, 0, ...])
   double safety, factor_min, factor_max, exp_i, exp_p;
   double atol, rtol, eps, damp;
   int64_t max_attempts;
@@ -84,6 +85,16 @@ PDQ_D void precon(T h, T (&p)[NU + 1], T (&pinv)[NU + 1]) {
 template <typename T>
 PDQ_D T observed_std(T p_out, T h, T q1_out_norm, T damp) {
   const T a = dev_abs(p_out) * fast_sqrt(dev_abs(h)) * q1_out_norm;
+  return damp == T(0) ? a : fast_sqrt(a * a + damp * damp);
+}
+
+// The same for the TS1 operator H = h0 e_0 + e_1 (observed coefficient 1):
+// H L_unit = sqrt|h| (h0 |p_0| Q1[0] + |p_1| Q1[1]), and with p_0 = p_1 h / nu
+// its norm is |p_1| sqrt|h| ||(h0 (h / nu) q00 + q10, q11)||.
+template <typename T, int NU>
+PDQ_D T observed_std_ts1(T p1, T h, T h0, T q00, T q10, T q11, T damp) {
+  const T c0 = h0 * (dev_abs(h) * T(1.0 / NU)) * q00 + q10;
+  const T a = dev_abs(p1) * fast_sqrt(dev_abs(h)) * fast_sqrt(c0 * c0 + q11 * q11);
   return damp == T(0) ? a : fast_sqrt(a * a + damp * damp);
 }
 
@@ -245,20 +256,24 @@ PDQ_D void iso_predict(const Q (&q1)[kMaxN][kMaxN], const T (&m)[NU + 1][D], con
 }
 
 // revert_conditional for a TS0 observation of coefficient OUT
-// (util/cholesky_util.py:27-82, H = e_OUT, noise chol damp): a Givens chain
+// (util/cholesky_util.py:27-82, H = e_OUT, noise chol damp), or a TS1 one
+// with H = h0 e_0 + e_OUT (same sparsity of (H Lp)^T): a Givens chain
 // on [[damp, 0], [(H Lp)^T, Lp^T]].  Column 0 has nonzeros in rows 0..OUT+1;
 // eliminating it bottom-up fills one subdiagonal entry per row, which one
 // rotation per column 1..OUT removes.  Returns R_Y; gain = R12^T / R_Y and
 // Lnew = R22^T.
 template <typename T, int NU, int OUT>
-PDQ_D T ts0_update(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (&Lnew)[NU + 1][NU + 1]) {
+PDQ_D T ts0_update(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (&Lnew)[NU + 1][NU + 1],
+                   T h0 = T(0)) {
   constexpr int n = NU + 1;
   T M[n + 1][n + 1];
 #pragma unroll
   for (int c = 0; c <= n; ++c) M[0][c] = (c == 0) ? damp : T(0);
 #pragma unroll
   for (int r = 1; r <= n; ++r) {
-    M[r][0] = Lp[OUT][r - 1];
+    // (H Lp)^T with H = h0 e_0 + e_OUT (TS1) or e_OUT (h0 = 0, TS0); Lp is
+    // lower triangular, so the h0 term only reaches row 1
+    M[r][0] = (r == 1) ? Lp[OUT][0] + h0 * Lp[0][0] : Lp[OUT][r - 1];
 #pragma unroll
     for (int c = 1; c <= n; ++c) M[r][c] = (c >= r) ? Lp[c - 1][r - 1] : T(0);
   }
@@ -365,6 +380,8 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
   for (int j = 0; j < n; ++j) q1_out2 += cst<T>(a.q1[OUT][j], a.q1f[OUT][j]) * cst<T>(a.q1[OUT][j], a.q1f[OUT][j]);
   const T q1_out_norm = dev_sqrt(q1_out2);
+  const T q00 = cst<T>(a.q1[0][0], a.q1f[0][0]), q10 = cst<T>(a.q1[1][0], a.q1f[1][0]),
+          q11 = cst<T>(a.q1[1][1], a.q1f[1][1]);
 
   if (!a.terminal_only) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, wide_value(t), 0);
 
@@ -406,9 +423,21 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           // error estimate's apply_flat(previous mean) (solvers.py:943-944)
           T mp[n][D];
           iso_predict_mean<T, NU, D>(m, p, pinv, mp);
-          // TS0 linearisation at the extrapolated mean (ssm_impl_isotropic.py:304-317)
+          // TS0 linearisation at the extrapolated mean (ssm_impl_isotropic.py:304-317);
+          // TS1: H = [-tr J_f(mp_0) / d, 1, 0, ...] (ssm_impl_isotropic.py:320-355,
+          // jacobians.py:100-106), same residual mean
           T f[D];
-          F::eval(mp[0], pt, f);
+          T h0 = T(0);
+          if (a.ts1) {
+            T Jf[D][D];
+            eval_with_jacobian<F>(mp[0], pt, f, Jf);
+            T tr = T(0);
+#pragma unroll
+            for (int j = 0; j < D; ++j) tr += Jf[j][j];
+            h0 = -tr * T(1.0 / D);
+          } else {
+            F::eval(mp[0], pt, f);
+          }
           T mobs[D];
           T mobs2 = T(0);
 #pragma unroll
@@ -420,7 +449,8 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           // fx.marginalise(apply_flat(m)) with unit scale: observed std
           // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
           // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
-          const T ell = observed_std(p[OUT], h, q1_out_norm, damp);
+          const T ell = a.ts1 ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
+                              : observed_std(p[OUT], h, q1_out_norm, damp);
           const T sigma_loc = dev_div(rms_mobs, ell);
 
           const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
@@ -433,7 +463,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 
           // ---- update (revert_conditional, H = e_OUT) ----
           T gain[n], Lnew[n][n];
-          const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew);
+          const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew, h0);
           const T ry_inv = fast_rcp(R_Y);
           T mnew[n][D];
 #pragma unroll

@@ -147,7 +147,8 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
   cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
 
   if (c->ssm == PDQ_SSM_ISOTROPIC) {
-    if (c->constraint != PDQ_CONSTRAINT_TS0 || c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
+    if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
+    if (c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
     pdq::IsoArgs a;
     memset(&a, 0, sizeof(a));
     a.B = args->num_instances;
@@ -157,6 +158,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.control = c->control;
     a.clip_dt = c->clip_dt ? 1 : 0;
     a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
+    a.ts1 = c->constraint == PDQ_CONSTRAINT_TS1 ? 1 : 0;
     a.safety = c->safety;
     a.factor_min = c->factor_min;
     a.factor_max = c->factor_max;
@@ -196,7 +198,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     // kernel (8 lanes per instance) with <= 128 / <= 85 registers per lane,
     // for exact checkpoint landings only
     const bool warp = c->clip_dt && c->kernel_variant >= 2;
-    if (c->kernel_variant >= 2 && !c->clip_dt) return PDQ_ERROR_UNSUPPORTED;
+    if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1)) return PDQ_ERROR_UNSUPPORTED;
     const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : 64;
     const bool f64 = c->precision == PDQ_PRECISION_F64;
     cudaError_t err;
@@ -220,7 +222,8 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
   }
   if (c->ssm == PDQ_SSM_BLOCKDIAG) {
     if (c->field != PDQ_FIELD_BURGERS) return PDQ_ERROR_UNSUPPORTED;
-    if (c->constraint != PDQ_CONSTRAINT_TS0 || c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
+    if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
+    if (c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
     if (!c->clip_dt) return PDQ_ERROR_UNSUPPORTED;  // checkpoints by exact landing only
     if (c->num_derivatives < 2 || c->num_derivatives > 4) return PDQ_ERROR_UNSUPPORTED;
     const int d = c->ode_dim;
@@ -240,6 +243,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
     a.d = d;
     a.cluster = CL;
+    a.ts1 = c->constraint == PDQ_CONSTRAINT_TS1 ? 1 : 0;
     a.safety = c->safety;
     a.factor_min = c->factor_min;
     a.factor_max = c->factor_max;

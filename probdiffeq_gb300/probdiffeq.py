@@ -149,10 +149,11 @@ class _StateSpaceModel:
         return Constraint(self.name, "ts0", ode)
 
     def constraint_ode_ts1(self, ode, /, taylor_point=None):
+        """TS1 linearisation (ssm_impl_api.py:536-558): the full Jacobian (dense), its
+        trace along d (isotropic, ssm_impl_isotropic.py:320-355) or its diagonal
+        along d (block-diagonal, ssm_impl_blockdiag.py:147-183), at the prior mean."""
         if not isinstance(ode, Field):
             raise TypeError(ode)
-        if self.name != "dense":
-            raise NotImplementedError("TS1 is native for the dense factorisation")
         if taylor_point is not None:
             raise NotImplementedError("only the prior-mean Taylor point (taylor_point_prior) is native")
         return Constraint(self.name, "ts1", ode)

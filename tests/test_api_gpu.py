@@ -79,7 +79,7 @@ def test_api_errors_are_raised_before_launch():
         probdiffeq.ode("no_such_field", torch.ones(1))
     iso, dense = probdiffeq.state_space_model_isotropic(), probdiffeq.state_space_model_dense()
     with pytest.raises(NotImplementedError):
-        iso.constraint_ode_ts1(vf)
+        iso.constraint_ode_ts1(vf, taylor_point="map")
     tcoeffs, _ = probdiffeq.jetexpand_ode_padded_scan(num=3)(vf, (torch.tensor([20.0, 20.0]),))
     prior = iso.prior_wiener_integrated(tcoeffs)
     solver = probdiffeq.solver_dynamic(strategy=probdiffeq.strategy_filter(), constraint=dense.constraint_ode_ts0(vf))

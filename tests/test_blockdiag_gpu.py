@@ -45,26 +45,27 @@ def burgers_ic(d, seed):
     return (amp[:, None] * np.sin(2 * np.pi * k[:, None] * x[None, :] + phase[:, None])).sum(axis=0)
 
 
-def oracle_bd(u0, t1, solver="dynamic", atol=1e-4, rtol=1e-4, dtype=torch.float64):
+def oracle_bd(u0, t1, solver="dynamic", atol=1e-4, rtol=1e-4, dtype=torch.float64, constraint="ts0"):
     p = torch.tensor([NU_VISC], dtype=torch.float64)
     tc = problems.taylor_derivatives(problems.burgers, torch.tensor(u0), p, 3).to(dtype)
     S = ssm.BdSSM()
     prior = S.prior_wiener_integrated(tc)
     pt = p.to(dtype)
-    c = S.constraint_ode_ts0(lambda u, t: problems.burgers(u[0], pt))
+    vf = lambda u, t: problems.burgers(u[0], pt)  # noqa: E731
+    c = S.constraint_ode_ts1(vf) if constraint == "ts1" else S.constraint_ode_ts0(vf)
     cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE, "none": solvers.SolverPlain}[solver]
     return solvers.solve_adaptive_terminal_values(
         cls(solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c), prior, 0.0, t1, atol, rtol, dt0=0.1 * t1
     )
 
 
-def gpu_bd(u0s, t1, precision, solver="dynamic", atol=1e-4, rtol=1e-4):
+def gpu_bd(u0s, t1, precision, solver="dynamic", atol=1e-4, rtol=1e-4, constraint="ts0"):
     from probdiffeq_gb300 import ensemble
 
     u0s = torch.as_tensor(np.asarray(u0s), dtype=torch.float64)
     B, d = u0s.shape
     cfg = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=d, ssm="blockdiag", solver=solver,
-                               precision=precision, atol=atol, rtol=rtol, clip_dt=True)
+                               precision=precision, atol=atol, rtol=rtol, clip_dt=True, constraint=constraint)
     out = ensemble.solve_ensemble(cfg, params=torch.full((B, 1), NU_VISC, dtype=torch.float64), y0=u0s,
                                   save_at=torch.tensor([0.0, t1], dtype=torch.float64), dt0=0.1 * t1)
     torch.cuda.synchronize()
@@ -160,3 +161,35 @@ def test_burgers_f32_matches_f64_full_size():
     err = rel(o32["u_mean"][0, 0, :, 0], o64["u_mean"][0, 0, :, 0])
     assert err < 1e-3, err
     assert int(o32["num_steps"][0, 0]) <= 2 * int(o64["num_steps"][0, 0])
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+def test_burgers_ts1_diagonal_vs_oracle(precision):
+    """Block-diagonal TS1 (the Jacobian's diagonal along d, ssm_impl_blockdiag.py:147-183) at d = 64."""
+    d, t1 = 64, 0.05
+    u0s = [burgers_ic(d, s) for s in (1, 2)]
+    out = gpu_bd(u0s, t1, precision, constraint="ts1")
+    assert (out["status"] == 0).all()
+    for b, u0 in enumerate(u0s):
+        res = oracle_bd(u0, t1, constraint="ts1")
+        if precision == "float64":
+            compare(out, b, res, dict(u=1e-8, rows=1e-5, cov=1e-5, steps=0.0))
+            assert rel(out["output_scale"][b, 0], torch.as_tensor(res.output_scale[-1]).reshape(-1)) < 1e-6
+        else:
+            err = rel(out["u_mean"][b, 0][:, 0], res.u[-1].mean[:, 0])
+            assert err < 1e-3, err
+
+
+def test_burgers_ts1_full_size_takes_far_fewer_steps():
+    """At d = 4096 the diagonal TS1 operator carries the stiff -2 nu / dx^2 term:
+    the solve on [0, 2e-3] needs a fraction of TS0's steps and still matches
+    DOP853 to the accuracy of an rtol = 1e-4 controller."""
+    d = 4096
+    u0s = [burgers_ic(d, 3)]
+    o0 = gpu_bd(u0s, T_FULL, "float64")
+    o1 = gpu_bd(u0s, T_FULL, "float64", constraint="ts1")
+    assert (o0["status"] == 0).all() and (o1["status"] == 0).all()
+    ref = scipy.integrate.solve_ivp(burgers_rhs(d), (0.0, T_FULL), u0s[0], method="DOP853", rtol=1e-10, atol=1e-10).y[:, -1]
+    err = np.abs(o1["u_mean"][0, 0, :, 0].numpy() - ref).max() / np.abs(ref).max()
+    assert err < 2e-3, err
+    assert int(o1["num_steps"][0, 0]) * 4 < int(o0["num_steps"][0, 0]), (int(o1["num_steps"][0, 0]), int(o0["num_steps"][0, 0]))

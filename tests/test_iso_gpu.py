@@ -244,3 +244,38 @@ def test_failure_statuses_are_reported_not_trapped(variant):
     out = ensemble.solve_ensemble(cfg, params=params[:1], y0=torch.tensor([[20.0, 20.0]]), save_at=torch.tensor([0.0, 1.0]), dt0=0.0)
     torch.cuda.synchronize()
     assert int(out["status"][0]) == 2
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+@pytest.mark.parametrize("solver", ["dynamic", "mle"])
+def test_ts1_trace_linearisation(solver, precision):
+    """Isotropic TS1 (Jacobian trace along d, ssm_impl_isotropic.py:320-355) on
+    van der Pol (mu = 2, its Jacobian trace varies along the solution) vs the oracle."""
+    from probdiffeq_gb300 import ensemble
+
+    params = torch.tensor([[2.0], [1.5]], dtype=torch.float64)
+    y0 = torch.tensor([[2.0, 0.0], [1.0, 1.0]], dtype=torch.float64)
+    save_at = [0.0, 3.0]
+    cfg = ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, constraint="ts1", solver=solver,
+                               precision=precision, atol=1e-5, rtol=1e-5, clip_dt=True)
+    out = ensemble.solve_ensemble(cfg, params=params, y0=y0, save_at=torch.tensor(save_at), dt0=0.1, terminal_only=True)
+    torch.cuda.synchronize()
+    out = {k: v.cpu() for k, v in out.items() if not k.startswith("_")}
+    assert (out["status"] == 0).all()
+    for b in range(2):
+        fn = problems.FIELDS["van_der_pol"]
+        tc = problems.taylor_derivatives(fn, y0[b], params[b], 3)
+        S = ssm.IsoSSM()
+        c = S.constraint_ode_ts1(lambda u, t, p=params[b]: fn(u[0], p))
+        cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE}[solver]
+        res = solvers.solve_adaptive_save_at(cls(solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c),
+                                             S.prior_wiener_integrated(tc), save_at, 1e-5, 1e-5, clip_dt=True, dt0=0.1)
+        o = res.u[-1]
+        if precision == "float64":
+            compare_record(out["u_mean"][b, 0], out["u_chol"][b, 0], o.mean, o.cholesky, out["num_steps"][b, 0],
+                           res.num_steps[-1], tolerances("float64"))
+            assert abs(float(out["output_scale"][b, 0]) - float(res.output_scale[-1])) <= 1e-6 * abs(float(res.output_scale[-1]))
+        else:
+            err_u = float((out["u_mean"][b, 0, 0] - o.mean[0]).abs().max() / o.mean[0].abs().max())
+            assert err_u < 1e-3, err_u
+            assert abs(int(out["num_steps"][b, 0]) - res.num_steps[-1]) <= max(2, math.ceil(0.1 * res.num_steps[-1]))

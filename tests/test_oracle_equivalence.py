@@ -180,3 +180,81 @@ def test_blockdiag_equals_per_dimension_dense_on_diagonal_ode():
         for a, b in zip(ubd, ud):
             assert allclose(a.mean[j], b.mean)
             assert allclose(a.cholesky[j] @ a.cholesky[j].T, b.cholesky @ b.cholesky.T)
+
+
+def test_dense_ts1_equals_isotropic_ts1_on_isotropic_ode():
+    """tests/test_probdiffeq/test_calibration/test_dynamic_across_factorisations.py:10-64 with TS1.
+
+    For an isotropic field f(u) = s u + t the dense TS1 operator is
+    [-s I, I, 0] and the isotropic one, the Jacobian trace along d divided by
+    d (ssm_impl_isotropic.py:320-355), is [-s, 1, 0]: the solvers agree.
+    """
+    g = torch.Generator().manual_seed(1)
+    scalar = torch.randn((), generator=g)
+    u0 = torch.randn(5, generator=g)
+
+    def vf(u, t):
+        return scalar * u[0] + t
+
+    tc = torch.stack([u0, scalar * u0, scalar * scalar * u0 + 1.0])
+    ts = np.linspace(0.0, 10.0, 7)
+    outs = []
+    for S in (ssm.DenseSSM(), ssm.IsoSSM()):
+        prior = S.prior_wiener_integrated(tc)
+        if isinstance(S, ssm.DenseSSM):
+            c = S.constraint_ode_ts1(vf, lambda u, t: scalar * torch.eye(5, dtype=u.dtype), 5)
+        else:
+            c = S.constraint_ode_ts1(vf)
+        solver = solvers.SolverDynamic(solvers.StrategyFixedPoint(), c)
+        outs.append(solvers.solve_adaptive_save_at(solver, solvers.ErrorResidualStd(c), prior, ts, 1e-3, 1e-3))
+    dn, iso = outs
+    assert dn.num_steps == iso.num_steps
+    for a, b in zip(dn.u, iso.u):
+        ma, Ca = a.to_multivariate_normal()
+        mb, Cb = b.to_multivariate_normal()
+        assert allclose(ma, mb)
+        assert allclose(Ca, Cb)
+
+
+def test_blockdiag_ts1_equals_per_dimension_dense_ts1_on_diagonal_ode():
+    """tests/test_probdiffeq/test_calibration/test_dynamic_across_factorisations.py:67-145 (TS1, fixed grid).
+
+    The block-diagonal TS1 operators are the Jacobian's diagonal along d
+    (ssm_impl_blockdiag.py:147-183); on a diagonal field they equal the d
+    one-dimensional dense TS1 operators.
+    """
+    g = torch.Generator().manual_seed(2)
+    lam = -torch.rand(3, generator=g)
+    u0 = torch.randn(3, generator=g)
+    grid = np.linspace(0.0, 1.0, 6)
+    tc = torch.stack([u0, lam * u0, lam * lam * u0])
+    S = ssm.BdSSM()
+    c = S.constraint_ode_ts1(lambda u, t: lam * u[0] + t)
+    _, ubd, _, _, _ = solvers.solve_fixed_grid(solvers.SolverDynamic(solvers.StrategyFilter(), c), S.prior_wiener_integrated(tc), grid)
+    for j in range(3):
+        D = ssm.DenseSSM()
+        cj = D.constraint_ode_ts1(lambda u, t, j=j: lam[j] * u[0] + t, lambda u, t, j=j: lam[j].reshape(1, 1).to(u.dtype), 1)
+        _, ud, _, _, _ = solvers.solve_fixed_grid(
+            solvers.SolverDynamic(solvers.StrategyFilter(), cj), D.prior_wiener_integrated(tc[:, j : j + 1]), grid
+        )
+        for a, b in zip(ubd, ud):
+            assert allclose(a.mean[j], b.mean)
+            assert allclose(a.cholesky[j] @ a.cholesky[j].T, b.cholesky @ b.cholesky.T)
+
+
+def test_ts1_differs_from_ts0_only_through_the_jacobian_term():
+    """With a field whose Jacobian trace is zero (f(u) = (u1, -u0)) TS1 reduces to TS0."""
+    u0 = torch.tensor([1.0, 0.5], dtype=torch.float64)
+
+    def vf(u, t):
+        return torch.stack([u[0][1], -u[0][0]])
+
+    tc = torch.stack([u0, vf(u0[None], 0.0), -u0, -vf(u0[None], 0.0)])
+    S = ssm.IsoSSM()
+    res = []
+    for c in (S.constraint_ode_ts0(vf), S.constraint_ode_ts1(vf)):
+        res.append(solvers.solve_adaptive_terminal_values(
+            solvers.SolverMLE(solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c), S.prior_wiener_integrated(tc),
+            0.0, 2.0, 1e-6, 1e-6))
+    assert res[0].num_steps[-1] == res[1].num_steps[-1]
+    assert allclose(res[0].u[-1].mean, res[1].u[-1].mean)
