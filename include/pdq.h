@@ -53,11 +53,12 @@ enum { PDQ_CONSTRAINT_TS0 = 0, PDQ_CONSTRAINT_TS1 = 1 };
 enum { PDQ_STRATEGY_FILTER = 0, PDQ_STRATEGY_FIXEDPOINT = 1 };
 /* solver / solver_mle / solver_dynamic (solvers.py:318-767). */
 enum { PDQ_SOLVER_PLAIN = 0, PDQ_SOLVER_MLE = 1, PDQ_SOLVER_DYNAMIC = 2 };
-/* error_residual_std (solvers.py:850-996). */
-enum { PDQ_ERROR_RESIDUAL_STD = 0 };
+/* error_residual_std (solvers.py:850-996) / error_state_std (solvers.py:999-1098, derivative_idx 0). */
+enum { PDQ_ERROR_RESIDUAL_STD = 0, PDQ_ERROR_STATE_STD = 1 };
 /* control_integral / control_proportional_integral (controllers.py:24-84). */
 enum { PDQ_CONTROL_INTEGRAL = 0, PDQ_CONTROL_PROPORTIONAL_INTEGRAL = 1 };
-/* Bulk arithmetic precision; time, calibration and error-norm sums are float64 always. */
+/* Bulk arithmetic precision.  Time, calibration and error-norm sums are float64 in
+ * PDQ_PRECISION_F64 and float pairs (48-bit significand) in PDQ_PRECISION_F32. */
 enum { PDQ_PRECISION_F32 = 0, PDQ_PRECISION_F64 = 1 };
 /* Registered device vector fields (autonomous, first order). */
 enum {

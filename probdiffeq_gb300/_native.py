@@ -19,7 +19,7 @@ SSM = {"isotropic": 0, "blockdiag": 1, "dense": 2}
 CONSTRAINT = {"ts0": 0, "ts1": 1}
 STRATEGY = {"filter": 0, "fixedpoint": 1}
 SOLVER = {"none": 0, "mle": 1, "dynamic": 2}
-ERROR = {"residual_std": 0}
+ERROR = {"residual_std": 0, "state_std": 1}
 CONTROL = {"integral": 0, "proportional_integral": 1}
 PRECISION = {"float32": 0, "float64": 1}
 FIELD = {"lotka_volterra": 0, "van_der_pol": 1, "fitzhugh_nagumo": 2, "burgers": 3}

@@ -48,6 +48,7 @@ struct BdArgs {
   int64_t B;
   int32_t S, terminal_only, solver, control, correct, d, cluster;
   int32_t ts1;  // 1: TS1 with the Jacobian diagonal along d (per-dimension H_j = [-dfj/duj, 1, 0, ...])
+  int32_t state_error;  // 0: error_residual_std; 1: error_state_std (derivative 0)
   double safety, factor_min, factor_max, exp_i, exp_p;
   double atol, rtol, eps, damp;
   int64_t max_attempts;
@@ -240,6 +241,9 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       const T h0 = a.ts1 ? T(2) * nu_visc * inv_dx * inv_dx : T(0);
       const T ell = a.ts1 ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
                           : observed_std(p[OUT], h, q1_out_norm, damp);
+      // error_state_std: the conditioned unit-scale std of u is the same for
+      // every dimension (one H, one unit-scale factor), so it is formed once
+      const T std0 = a.state_error ? state_std0<T, NU, OUT>(a, p, h, damp, h0) : T(0);
       const T* x = bufs[cur];
       T* y = bufs[cur ^ 1];
 
@@ -304,8 +308,9 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
         for (int i = 0; i < n; ++i)
 #pragma unroll
           for (int j = 0; j <= i; ++j) y[(n + i * (i + 1) / 2 + j) * d + g] = Lnew[i][j];
-        // error_residual_std: std = |sigma| l = |mobs|, error = std * h; reference max(|u0|, |u1|)
-        const T err_abs = dev_abs(mobs) * h;
+        // error_residual_std: std = |sigma| l = |mobs|, error = std * h;
+        // error_state_std: sigma_j * std0 (dt^0/0! = 1); reference max(|u0|, |u1|)
+        const T err_abs = a.state_error ? dev_abs(sigma) * std0 : dev_abs(mobs) * h;
         const T ref = fmax(dev_abs(x[g]), dev_abs(mnew[0]));
         const T ratio = dev_div(err_abs, atol + rtol * ref);
         local = wide_add_sq(local, ratio);

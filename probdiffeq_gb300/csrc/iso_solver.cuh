@@ -32,6 +32,7 @@ struct IsoArgs {
   int64_t B;
   int32_t S, terminal_only, solver, control, clip_dt, correct;
   int32_t ts1;  // 0: TS0 (H = e_1); 1: TS1 with the Jacobian trace along d (H = [-tr J_f / d, 1, 0, ...])
+  int32_t state_error;  // 0: error_residual_std; 1: error_state_std (derivative 0)
   double safety, factor_min, factor_max, exp_i, exp_p;
   double atol, rtol, eps, damp;
   int64_t max_attempts;
@@ -292,6 +293,28 @@ PDQ_D T ts0_update(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (
   return R_Y;
 }
 
+// error_state_std: posterior std of coefficient 0 after conditioning the
+// unit-scale extrapolation N(., (|p| sqrt|h| Q1)(...)^T) on the linearised
+// residual (the Givens update of ts0_update applied to that factor; its row 0
+// is (L00, 0, ...), so the std is |L00|).
+template <typename T, int NU, int OUT, typename A>
+PDQ_D T state_std0(const A& a, const T (&p)[NU + 1], T h, T damp, T h0) {
+  constexpr int n = NU + 1;
+  constexpr bool kNarrow = sizeof(T) == sizeof(float);
+  const T sq = fast_sqrt(dev_abs(h));
+  T Lu[n][n];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+      const T q = kNarrow ? T(a.q1f[i][j]) : T(a.q1[i][j]);
+      Lu[i][j] = (j <= i) ? dev_abs(p[i]) * sq * q : T(0);
+    }
+  T g[n], Lc[n][n];
+  ts0_update<T, NU, OUT>(Lu, damp, g, Lc, h0);
+  return dev_abs(Lc[0][0]);
+}
+
 template <typename T, int NU, int D>
 PDQ_D void write_record(const IsoArgs& a, int64_t b, int s_out, int S_out, const T (&m)[NU + 1][D],
                         const T (&L)[NU + 1][NU + 1], double scale, double t, int steps) {
@@ -472,9 +495,17 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - gain[i] * mobs[j];
 
           // ---- error estimate (error_residual_std, solvers.py:925-996) ----
-          // std of the observed residual rescaled by sigma_loc = rms / l is rms:
-          // error = rms * dt^1/1! (no division by a possibly tiny l)
-          const T err_abs = rms_mobs * h;
+          // error_residual_std: the std of the observed residual rescaled by
+          // sigma_loc = rms / l is rms, error = rms * dt^1/1! (no division by a
+          // possibly tiny l).  error_state_std (solvers.py:1037-1098): condition the
+          // unit-scale extrapolation (chol |p| sqrt|h| Q1) on the same
+          // linearisation; error = sigma_loc * (posterior std of u), dt^0/0! = 1
+          T err_abs;
+          if (a.state_error) {
+            err_abs = sigma_loc * state_std0<T, NU, OUT>(a, p, h, damp, h0);
+          } else {
+            err_abs = rms_mobs * h;
+          }
           W sumsq = wide_from(0.0, T(0));
 #pragma unroll
           for (int j = 0; j < D; ++j) {

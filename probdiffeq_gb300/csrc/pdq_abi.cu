@@ -56,7 +56,7 @@ pdq_status validate_common(const pdq_config* c) {
   if (c->solver < PDQ_SOLVER_PLAIN || c->solver > PDQ_SOLVER_DYNAMIC) return PDQ_ERROR_INVALID_VALUE;
   if (c->control != PDQ_CONTROL_INTEGRAL && c->control != PDQ_CONTROL_PROPORTIONAL_INTEGRAL)
     return PDQ_ERROR_INVALID_VALUE;
-  if (c->error != PDQ_ERROR_RESIDUAL_STD) return PDQ_ERROR_UNSUPPORTED;
+  if (c->error != PDQ_ERROR_RESIDUAL_STD && c->error != PDQ_ERROR_STATE_STD) return PDQ_ERROR_INVALID_VALUE;
   if (!(c->atol >= 0) || !(c->rtol >= 0) || !(c->atol + c->rtol > 0)) return PDQ_ERROR_INVALID_VALUE;
   if (!(c->eps >= 0) || !(c->damp >= 0)) return PDQ_ERROR_INVALID_VALUE;
   if (!(c->factor_min > 0) || !(c->factor_max >= c->factor_min) || !(c->safety > 0)) return PDQ_ERROR_INVALID_VALUE;
@@ -159,6 +159,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.clip_dt = c->clip_dt ? 1 : 0;
     a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
     a.ts1 = c->constraint == PDQ_CONSTRAINT_TS1 ? 1 : 0;
+    a.state_error = c->error == PDQ_ERROR_STATE_STD ? 1 : 0;
     a.safety = c->safety;
     a.factor_min = c->factor_min;
     a.factor_max = c->factor_max;
@@ -198,7 +199,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     // kernel (8 lanes per instance) with <= 128 / <= 85 registers per lane,
     // for exact checkpoint landings only
     const bool warp = c->clip_dt && c->kernel_variant >= 2;
-    if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1)) return PDQ_ERROR_UNSUPPORTED;
+    if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1 || a.state_error)) return PDQ_ERROR_UNSUPPORTED;
     const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : 64;
     const bool f64 = c->precision == PDQ_PRECISION_F64;
     cudaError_t err;
@@ -244,6 +245,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.d = d;
     a.cluster = CL;
     a.ts1 = c->constraint == PDQ_CONSTRAINT_TS1 ? 1 : 0;
+    a.state_error = c->error == PDQ_ERROR_STATE_STD ? 1 : 0;
     a.safety = c->safety;
     a.factor_min = c->factor_min;
     a.factor_max = c->factor_max;
@@ -284,6 +286,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
   }
   if (c->ssm == PDQ_SSM_DENSE) {
+    if (c->error != PDQ_ERROR_RESIDUAL_STD) return PDQ_ERROR_UNSUPPORTED;
     if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
     if (c->strategy != PDQ_STRATEGY_FILTER && c->strategy != PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_INVALID_VALUE;

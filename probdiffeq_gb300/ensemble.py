@@ -37,6 +37,7 @@ def make_config(
     exponent_proportional=0.4,
     max_attempts=DEFAULT_MAX_ATTEMPTS,
     kernel_variant=0,
+    error="residual_std",
 ):
     """Build a ``pdq_config`` (include/pdq.h) from keyword arguments."""
     cfg = _native.config_default(ssm, field, num_derivatives, ode_dim)
@@ -44,6 +45,7 @@ def make_config(
     cfg.strategy = _native.STRATEGY[strategy]
     cfg.solver = _native.SOLVER[solver]
     cfg.control = _native.CONTROL[control]
+    cfg.error = _native.ERROR[error]
     cfg.precision = _native.PRECISION[precision]
     cfg.atol, cfg.rtol, cfg.eps, cfg.damp = float(atol), float(rtol), float(eps), float(damp)
     cfg.clip_dt = 1 if clip_dt else 0

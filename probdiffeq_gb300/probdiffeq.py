@@ -33,6 +33,7 @@ __all__ = [
     "solver_mle",
     "solver_dynamic",
     "error_residual_std",
+    "error_state_std",
     "jacobian_materialize",
     "loss_lml_timeseries",
 ]
@@ -260,6 +261,24 @@ class loss_lml_timeseries:
             raise NotImplementedError("observations of the solution (tcoeff_index=0) only")
 
 
+@dataclasses.dataclass(frozen=True)
+class error_state_std:
+    """State-std error estimate (solvers.py:999-1098): the posterior std of u after
+    conditioning the unit-scale extrapolation on the linearised residual, times
+    the local calibration; cached linearisation, derivative 0."""
+
+    constraint: Constraint
+    error_norm: Optional[Any] = None
+    re_linearize_before_error: bool = False
+    derivative_idx: int = 0
+    error_per_unit_step: bool = False
+
+    def __post_init__(self):
+        if (self.error_norm is not None or self.re_linearize_before_error or self.derivative_idx != 0
+                or self.error_per_unit_step):
+            raise NotImplementedError("only the default error_state_std is native")
+
+
 def _field_dim(field, y0):
     d = _FIELD_DIMS[field.name]
     return y0.shape[-1] if d is None else d
@@ -280,6 +299,7 @@ def lower(solver_obj, error, control, *, num_derivatives, y0, precision, atol, r
                   exponent_proportional=ctrl.exponent_proportional)
     else:
         kw.update(control="integral")
+    kw["error"] = "state_std" if isinstance(error, error_state_std) else "residual_std"
     return ensemble.make_config(
         field=c.field.name, num_derivatives=num_derivatives, ode_dim=_field_dim(c.field, y0), ssm=c.ssm,
         constraint=c.kind, strategy=solver_obj.strategy.name, solver=solver_obj.kind, precision=precision,

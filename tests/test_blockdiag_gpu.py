@@ -193,3 +193,28 @@ def test_burgers_ts1_full_size_takes_far_fewer_steps():
     err = np.abs(o1["u_mean"][0, 0, :, 0].numpy() - ref).max() / np.abs(ref).max()
     assert err < 2e-3, err
     assert int(o1["num_steps"][0, 0]) * 4 < int(o0["num_steps"][0, 0]), (int(o1["num_steps"][0, 0]), int(o0["num_steps"][0, 0]))
+
+
+def test_burgers_error_state_std_vs_oracle():
+    """error_state_std with per-dimension calibration (solvers.py:999-1098), d = 64, float64."""
+    from probdiffeq_gb300 import ensemble
+
+    d, t1 = 64, 0.05
+    u0s = [burgers_ic(d, s) for s in (1, 2)]
+    u0t = torch.as_tensor(np.asarray(u0s), dtype=torch.float64)
+    cfg = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=d, ssm="blockdiag", solver="dynamic",
+                               precision="float64", atol=1e-4, rtol=1e-4, clip_dt=True, error="state_std")
+    out = ensemble.solve_ensemble(cfg, params=torch.full((2, 1), NU_VISC, dtype=torch.float64), y0=u0t,
+                                  save_at=torch.tensor([0.0, t1], dtype=torch.float64), dt0=0.1 * t1)
+    torch.cuda.synchronize()
+    out = {k: v.cpu() for k, v in out.items() if not k.startswith("_") and v is not None}
+    assert (out["status"] == 0).all()
+    p = torch.tensor([NU_VISC], dtype=torch.float64)
+    for b, u0 in enumerate(u0s):
+        tc = problems.taylor_derivatives(problems.burgers, torch.tensor(u0), p, 3)
+        S = ssm.BdSSM()
+        c = S.constraint_ode_ts0(lambda u, t: problems.burgers(u[0], p))
+        res = solvers.solve_adaptive_terminal_values(solvers.SolverDynamic(solvers.StrategyFilter(), c),
+                                                     solvers.ErrorStateStd(c), S.prior_wiener_integrated(tc),
+                                                     0.0, t1, 1e-4, 1e-4, dt0=0.1 * t1)
+        compare(out, b, res, dict(u=1e-8, rows=1e-5, cov=1e-5, steps=0.0))

@@ -279,3 +279,32 @@ def test_ts1_trace_linearisation(solver, precision):
             err_u = float((out["u_mean"][b, 0, 0] - o.mean[0]).abs().max() / o.mean[0].abs().max())
             assert err_u < 1e-3, err_u
             assert abs(int(out["num_steps"][b, 0]) - res.num_steps[-1]) <= max(2, math.ceil(0.1 * res.num_steps[-1]))
+
+
+@pytest.mark.parametrize("constraint", ["ts0", "ts1"])
+@pytest.mark.parametrize("solver", ["dynamic", "mle"])
+def test_error_state_std(solver, constraint):
+    """error_state_std (solvers.py:999-1098) on Lotka--Volterra, float64, vs the oracle."""
+    from probdiffeq_gb300 import ensemble
+
+    params, y0 = lv_instances(3, seed=4)
+    save_at = [0.0, 8.0]
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=3, ode_dim=2, constraint=constraint,
+                               solver=solver, precision="float64", atol=1e-5, rtol=1e-5, clip_dt=True,
+                               error="state_std")
+    out = ensemble.solve_ensemble(cfg, params=params, y0=y0, save_at=torch.tensor(save_at), dt0=0.1, terminal_only=True)
+    torch.cuda.synchronize()
+    out = {k: v.cpu() for k, v in out.items() if not k.startswith("_")}
+    assert (out["status"] == 0).all()
+    for b in range(3):
+        fn = problems.FIELDS["lotka_volterra"]
+        tc = problems.taylor_derivatives(fn, y0[b], params[b], 3)
+        S = ssm.IsoSSM()
+        vf = lambda u, t, p=params[b]: fn(u[0], p)  # noqa: E731
+        c = S.constraint_ode_ts1(vf) if constraint == "ts1" else S.constraint_ode_ts0(vf)
+        cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE}[solver]
+        res = solvers.solve_adaptive_save_at(cls(solvers.StrategyFilter(), c), solvers.ErrorStateStd(c),
+                                             S.prior_wiener_integrated(tc), save_at, 1e-5, 1e-5, clip_dt=True, dt0=0.1)
+        o = res.u[-1]
+        compare_record(out["u_mean"][b, 0], out["u_chol"][b, 0], o.mean, o.cholesky, out["num_steps"][b, 0],
+                       res.num_steps[-1], tolerances("float64"))
