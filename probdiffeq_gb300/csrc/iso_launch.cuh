@@ -29,20 +29,22 @@ cudaError_t launch_iso_warp_nu(const IsoArgs& a, int minb, cudaStream_t stream) 
   return cudaGetLastError();
 }
 
-template <typename T, int NU, class F>
+template <typename T, int NU, class F, bool FP>
 cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
-  auto kernel = interp ? iso_adaptive_kernel<T, NU, F, true> : iso_adaptive_kernel<T, NU, F, false>;
-  cudaError_t e = interp ? ensure_stack<iso_adaptive_kernel<T, NU, F, true>>()
-                         : ensure_stack<iso_adaptive_kernel<T, NU, F, false>>();
+  auto kernel = interp ? iso_adaptive_kernel<T, NU, F, true, FP> : iso_adaptive_kernel<T, NU, F, false, FP>;
+  cudaError_t e = interp ? ensure_stack<iso_adaptive_kernel<T, NU, F, true, FP>>()
+                         : ensure_stack<iso_adaptive_kernel<T, NU, F, false, FP>>();
   if (e != cudaSuccess) return e;
   const unsigned grid = unsigned((a.B + block - 1) / block);
   kernel<<<grid, block, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
-template <typename T, class F>
+template <typename T, class F, bool FP = false>
 cudaError_t launch_iso_precision(const IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block) {
-  if (block <= 0) {  // lane-cooperative variant (clip_dt only); -block = min blocks per SM
+  if constexpr (FP) {
+    if (block <= 0) return cudaErrorInvalidValue;  // the lane-cooperative kernel is filter-only
+  } else if (block <= 0) {  // lane-cooperative variant (clip_dt only); -block = min blocks per SM
     const int minb = -block;
     switch (nu) {
       case 1: return launch_iso_warp_nu<T, 1, F>(a, minb, stream);
@@ -54,11 +56,11 @@ cudaError_t launch_iso_precision(const IsoArgs& a, int nu, bool interp, cudaStre
     }
   }
   switch (nu) {
-    case 1: return launch_iso_nu<T, 1, F>(a, interp, stream, block);
-    case 2: return launch_iso_nu<T, 2, F>(a, interp, stream, block);
-    case 3: return launch_iso_nu<T, 3, F>(a, interp, stream, block);
-    case 4: return launch_iso_nu<T, 4, F>(a, interp, stream, block);
-    case 5: return launch_iso_nu<T, 5, F>(a, interp, stream, block);
+    case 1: return launch_iso_nu<T, 1, F, FP>(a, interp, stream, block);
+    case 2: return launch_iso_nu<T, 2, F, FP>(a, interp, stream, block);
+    case 3: return launch_iso_nu<T, 3, F, FP>(a, interp, stream, block);
+    case 4: return launch_iso_nu<T, 4, F, FP>(a, interp, stream, block);
+    case 5: return launch_iso_nu<T, 5, F, FP>(a, interp, stream, block);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -76,8 +78,20 @@ PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_vdp_f32)
 PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_vdp_f64)
 PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fhn_f32)
 PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fhn_f64)
+// the same with the fixed-point smoother
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fp_lv_f32)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fp_lv_f64)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fp_vdp_f32)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fp_vdp_f64)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fp_fhn_f32)
+PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fp_fhn_f64)
 
 #define PDQ_DEFINE_ISO_LAUNCH(NAME, T, F)                                                       \
   cudaError_t NAME(const pdq::IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block) { \
     return pdq::launch_iso_precision<T, F>(a, nu, interp, stream, block);                       \
+  }
+
+#define PDQ_DEFINE_ISO_FP_LAUNCH(NAME, T, F)                                                    \
+  cudaError_t NAME(const pdq::IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block) { \
+    return pdq::launch_iso_precision<T, F, true>(a, nu, interp, stream, block);                 \
   }

@@ -53,6 +53,7 @@ struct IsoArgs {
   int32_t* num_steps;
   int32_t* num_attempts;
   int32_t* status;
+  void* workspace;  // fixed-point smoother: (B, S - 1) backward conditionals in T
 };
 
 // A constant in the kernel's precision: the float copy for float, else the double.
@@ -335,9 +336,253 @@ PDQ_D void write_record(const IsoArgs& a, int64_t b, int s_out, int S_out, const
   a.num_steps[rec] = steps;
 }
 
+// ---------------------------------------------------------------------------
+// Fixed-point smoother pieces in the isotropic factorisation
+// (IsotropicLatentCond, ssm_impl_isotropic.py:72-140): a backward conditional
+// x_prev | x = N(to * (A (tl * x) + xi), (|to| X)(|to| X)^T) with A, X (n, n)
+// shared by all d dimensions and xi (n, d).
+// ---------------------------------------------------------------------------
+
+template <typename T, int NU, int D>
+struct IsoBackward {
+  T A[NU + 1][NU + 1];
+  T xi[NU + 1][D];
+  T X[NU + 1][NU + 1];  // lower triangular
+  T tl[NU + 1];
+  T to[NU + 1];
+};
+
+template <int NU, int D>
+PDQ_HD constexpr int iso_cond_floats() {
+  return (NU + 1) * (NU + 1) + (NU + 1) * D + (NU + 1) * (NU + 2) / 2 + 2 * (NU + 1);
+}
+
+template <typename T, int NU, int D>
+PDQ_D void iso_cond_identity(IsoBackward<T, NU, D>& c) {
+  constexpr int n = NU + 1;
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+      c.A[i][j] = (i == j) ? T(1) : T(0);
+      c.X[i][j] = T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < D; ++j) c.xi[i][j] = T(0);
+    c.tl[i] = T(1);
+    c.to[i] = T(1);
+  }
+}
+
+template <typename T, int NU, int D>
+PDQ_D void iso_cond_store(T* base, const IsoBackward<T, NU, D>& c) {
+  constexpr int n = NU + 1;
+  int o = 0;
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) base[o++] = c.A[i][j];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) base[o++] = c.xi[i][j];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) base[o++] = c.X[i][j];
+#pragma unroll
+  for (int i = 0; i < n; ++i) base[o++] = c.tl[i];
+#pragma unroll
+  for (int i = 0; i < n; ++i) base[o++] = c.to[i];
+}
+
+template <typename T, int NU, int D>
+PDQ_D void iso_cond_load(const T* base, IsoBackward<T, NU, D>& c) {
+  constexpr int n = NU + 1;
+  int o = 0;
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) c.A[i][j] = base[o++];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) c.xi[i][j] = base[o++];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) c.X[i][j] = (j <= i) ? base[o++] : T(0);
+#pragma unroll
+  for (int i = 0; i < n; ++i) c.tl[i] = base[o++];
+#pragma unroll
+  for (int i = 0; i < n; ++i) c.to[i] = base[o++];
+}
+
+// transition(h, s).revert(rv) (ssm_impl_isotropic.py:107-133 with the IWP
+// transition :367-378): the predicted Cholesky factor and the backward
+// conditional.  M = [[R_YX, 0], [R_X_F, R_X]] with R_YX = (s sqrt|h| Q1)^T,
+// R_X_F = (A cl)^T, R_X = cl^T, cl = |p_inv| L; R = qr_r(M); the predicted
+// factor is |p| R_Y^T, G^T = R_Y^{-1} R12, the conditional's noise factor R22^T.
+template <typename T, int NU, int D, typename Q>
+PDQ_D void iso_prior_revert(const Q (&q1)[kMaxN][kMaxN], const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1],
+                            const T (&p)[NU + 1], const T (&pinv)[NU + 1], T scale_q, T (&Lp)[NU + 1][NU + 1],
+                            IsoBackward<T, NU, D>& cond) {
+  constexpr int n = NU + 1;
+  T M[2 * n][2 * n];
+  T cl[n][n];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) cl[i][j] = (j <= i) ? dev_abs(pinv[i]) * L[i][j] : T(0);
+#pragma unroll
+  for (int r = 0; r < n; ++r)
+#pragma unroll
+    for (int c = 0; c < n; ++c) {
+      M[r][c] = (r <= c) ? scale_q * T(q1[c][r]) : T(0);
+      M[r][n + c] = T(0);
+      T acc = T(0);
+#pragma unroll
+      for (int k = c; k < n; ++k) acc += T(iwp_a<NU>(c, k)) * cl[k][r];
+      M[n + r][c] = acc;
+      M[n + r][n + c] = cl[c][r];
+    }
+  householder_r<T, 2 * n, 2 * n>(M);
+  T Gt[n][n];
+#pragma unroll
+  for (int col = 0; col < n; ++col)
+#pragma unroll
+    for (int i = n - 1; i >= 0; --i) {
+      T acc = M[i][n + col];
+#pragma unroll
+      for (int k = i + 1; k < n; ++k) acc -= M[i][k] * Gt[k][col];
+      Gt[i][col] = acc / M[i][i];
+    }
+  T mean_l[n][D], mobs[n][D];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) mean_l[i][j] = pinv[i] * m[i][j];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = i; k < n; ++k) acc += T(iwp_a<NU>(i, k)) * mean_l[k][j];
+      mobs[i][j] = acc;
+    }
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T acc = mean_l[i][j];
+#pragma unroll
+      for (int k = 0; k < n; ++k) acc -= Gt[k][i] * mobs[k][j];
+      cond.xi[i][j] = acc;
+    }
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+      cond.A[i][j] = Gt[j][i];
+      cond.X[i][j] = (j <= i) ? M[n + j][n + i] : T(0);
+      Lp[i][j] = (j <= i) ? dev_abs(p[i]) * M[j][i] : T(0);
+    }
+    cond.tl[i] = T(1) / p[i];
+    cond.to[i] = T(1) / pinv[i];
+  }
+}
+
+// outer.merge(inner) (ssm_impl_isotropic.py:91-105)
+template <typename T, int NU, int D>
+PDQ_D void iso_cond_merge(const IsoBackward<T, NU, D>& o, const IsoBackward<T, NU, D>& in,
+                          IsoBackward<T, NU, D>& out) {
+  constexpr int n = NU + 1;
+  T Tv[n];
+#pragma unroll
+  for (int i = 0; i < n; ++i) Tv[i] = o.tl[i] * in.to[i];
+  T M[2 * n][n];
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+      T g = T(0), r1 = T(0);
+#pragma unroll
+      for (int k = 0; k < n; ++k) {
+        g += o.A[i][k] * Tv[k] * in.A[k][j];
+        r1 += o.A[i][k] * dev_abs(Tv[k]) * in.X[k][j];
+      }
+      out.A[i][j] = g;
+      M[j][i] = r1;
+      M[n + j][i] = o.X[i][j];
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      T x = o.xi[i][d];
+#pragma unroll
+      for (int k = 0; k < n; ++k) x += o.A[i][k] * Tv[k] * in.xi[k][d];
+      out.xi[i][d] = x;
+    }
+  }
+  householder_r<T, 2 * n, n>(M);
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < n; ++j) out.X[i][j] = (j <= i) ? M[j][i] : T(0);
+    out.tl[i] = in.tl[i];
+    out.to[i] = o.to[i];
+  }
+}
+
+// cond.marginalise(rv) (ssm_impl_isotropic.py:81-89)
+template <typename T, int NU, int D>
+PDQ_D void iso_cond_marginalise(const IsoBackward<T, NU, D>& c, const T (&m)[NU + 1][D],
+                                const T (&L)[NU + 1][NU + 1], T (&mo)[NU + 1][D], T (&Lo)[NU + 1][NU + 1]) {
+  constexpr int n = NU + 1;
+  T M[2 * n][n];
+#pragma unroll
+  for (int r = 0; r < n; ++r)
+#pragma unroll
+    for (int col = 0; col < n; ++col) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = 0; k < n; ++k) acc += c.A[col][k] * c.tl[k] * L[k][r];
+      M[r][col] = acc;
+      M[n + r][col] = c.X[col][r];
+    }
+  householder_r<T, 2 * n, n>(M);
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      T acc = c.xi[i][d];
+#pragma unroll
+      for (int k = 0; k < n; ++k) acc += c.A[i][k] * c.tl[k] * m[k][d];
+      mo[i][d] = c.to[i] * acc;
+    }
+#pragma unroll
+    for (int j = 0; j < n; ++j) Lo[i][j] = (j <= i) ? dev_abs(c.to[i]) * M[j][i] : T(0);
+  }
+}
+
+template <typename T, int NU, int D>
+PDQ_D void write_normal_iso(const IsoArgs& a, int64_t rec, const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1]) {
+  constexpr int n = NU + 1;
+  double* um = a.u_mean + rec * (n * D);
+  double* uc = a.u_chol + rec * (n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < D; ++j) um[i * D + j] = double(m[i][j]);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) uc[i * n + j] = double(L[i][j]);
+}
+
 // One adaptive solve per thread.  INTERP: keep the interpolation state
-// (needed unless clip_dt makes every checkpoint an exact landing).
-template <typename T, int NU, class F, bool INTERP>
+// (needed unless clip_dt makes every checkpoint an exact landing).  FP: the
+// fixed-point smoother (estimators_and_losses.py:473-591): every step also
+// forms the prior's backward conditional and merges it into the running one;
+// at each checkpoint the running conditional goes to the workspace and
+// resets to the identity; after the last step the backward pass
+// (Smoother.finalize, MarkovSequence.evaluate_marginals, :156-178, 437-470)
+// marginalises from the terminal state through the stored conditionals.
+template <typename T, int NU, class F, bool INTERP, bool FP = false>
 __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   constexpr int n = NU + 1;
   constexpr int D = F::D;
@@ -384,6 +629,15 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
       for (int j = 0; j < n; ++j) Li[i][j] = T(0);
     }
+  }
+
+  // fixed-point smoother: running backward conditional of step_from (bw) and
+  // of interp_from (bwi); dead code without FP
+  IsoBackward<T, NU, D> bw, bwi;
+  T* const ws = FP ? reinterpret_cast<T*>(a.workspace) + b * int64_t(S - 1) * iso_cond_floats<NU, D>() : nullptr;
+  if constexpr (FP) {
+    iso_cond_identity(bw);
+    if constexpr (INTERP) iso_cond_identity(bwi);
   }
 
   W t = wide_from(save_at[0], T(0));
@@ -478,7 +732,14 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 
           const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
           T Lp[n][n];
-          if constexpr (kNarrow) {
+          IsoBackward<T, NU, D> cnew;  // fixed-point: the prior's backward conditional of this step
+          if constexpr (FP) {
+            if constexpr (kNarrow) {
+              iso_prior_revert<T, NU, D>(a.q1f, m, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp, cnew);
+            } else {
+              iso_prior_revert<T, NU, D>(a.q1, m, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp, cnew);
+            }
+          } else if constexpr (kNarrow) {
             iso_predict_chol<T, NU>(a.q1f, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp);
           } else {
             iso_predict_chol<T, NU>(a.q1, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
@@ -545,6 +806,12 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
                 for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
               }
+              if constexpr (FP) bwi = bw;
+            }
+            if constexpr (FP) {
+              IsoBackward<T, NU, D> merged;
+              iso_cond_merge(bw, cnew, merged);
+              bw = merged;
             }
             // a step clipped to the checkpoint lands on it exactly in float
             // pairs; float64 adds as the reference does
@@ -584,7 +851,34 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           const T h = T(wide_diff(t_next, ti));
           T p[n], pinv[n], mp[n][D], Lp[n][n];
           precon<T, NU>(h, p, pinv);
-          if constexpr (kNarrow) {
+          if constexpr (FP) {
+            // estimators_and_losses.py:549-591: the extrapolation to t_next
+            // closes the checkpoint's conditional (bwi merged with it); the
+            // step_from state keeps its marginal with the conditional from
+            // t_next to t, merged into the identity
+            IsoBackward<T, NU, D> c0, m0, c1, idc, m1;
+            iso_predict_mean<T, NU, D>(mi, p, pinv, mp);
+            if constexpr (kNarrow) {
+              iso_prior_revert<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp, c0);
+            } else {
+              iso_prior_revert<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp, c0);
+            }
+            iso_cond_merge(bwi, c0, m0);
+            iso_cond_store(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), m0);
+            const T h1 = T(wide_diff(t, t_next));
+            T p1[n], pinv1[n], mp1[n][D], Lp1[n][n];
+            precon<T, NU>(h1, p1, pinv1);
+            if constexpr (kNarrow) {
+              iso_prior_revert<T, NU, D>(a.q1f, mp, Lp, p1, pinv1, sigma_sf * dev_sqrt(dev_abs(h1)), Lp1, c1);
+            } else {
+              iso_prior_revert<T, NU, D>(a.q1, mp, Lp, p1, pinv1, sigma_sf * dev_sqrt(dev_abs(h1)), Lp1, c1);
+            }
+            (void)mp1;
+            iso_cond_identity(idc);
+            iso_cond_merge(idc, c1, m1);
+            bw = m1;
+            iso_cond_identity(bwi);
+          } else if constexpr (kNarrow) {
             iso_predict<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
           } else {
             iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
@@ -602,6 +896,12 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
       } else {
         // interp_at_t1: the state itself is the solution (estimators_and_losses.py:416-421)
         if (record) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), wide_value(t), num_steps);
+        if constexpr (FP) {
+          // estimators_and_losses.py:534-547: close the checkpoint's conditional, reset
+          iso_cond_store(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), bw);
+          iso_cond_identity(bw);
+          if constexpr (INTERP) iso_cond_identity(bwi);
+        }
         if constexpr (INTERP) {
           ti = t;
 #pragma unroll
@@ -614,6 +914,30 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
         }
       }
       cont = before(t, t_next);
+    }
+  }
+
+  // ---- fixed-point backward pass: marginals at the checkpoints ----
+  if constexpr (FP) {
+    if (status == PDQ_INSTANCE_OK) {
+      T rm[n][D], rL[n][n];
+      iso_cond_marginalise(bw, m, L, rm, rL);
+      for (int s = S - 1; s >= 1; --s) {
+        if (!a.terminal_only || s == S - 1) write_normal_iso<T, NU, D>(a, b * S_out + (a.terminal_only ? 0 : s), rm, rL);
+        if (a.terminal_only) break;
+        IsoBackward<T, NU, D> c;
+        iso_cond_load(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), c);
+        T pm[n][D], pL[n][n];
+        iso_cond_marginalise(c, rm, rL, pm, pL);
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+#pragma unroll
+          for (int j = 0; j < D; ++j) rm[i][j] = pm[i][j];
+#pragma unroll
+          for (int j = 0; j < n; ++j) rL[i][j] = pL[i][j];
+        }
+        if (s == 1) write_normal_iso<T, NU, D>(a, b * S_out, rm, rL);
+      }
     }
   }
 

@@ -124,6 +124,12 @@ pdq_status pdq_workspace_size(const pdq_config* c, int64_t num_instances, int32_
     const size_t rows = size_t(nu + 1) + size_t(nu + 1) * (nu + 2) / 2;
     *bytes = 2 * size_t(num_instances) * rows * size_t(c->ode_dim) * elem + size_t(num_instances) * c->ode_dim * 8;
   }
+  if (c->ssm == PDQ_SSM_ISOTROPIC && c->strategy == PDQ_STRATEGY_FIXEDPOINT) {
+    const int n = c->num_derivatives + 1, d = c->ode_dim;
+    const size_t floats = size_t(n) * n + size_t(n) * d + size_t(n) * (n + 1) / 2 + 2 * size_t(n);
+    const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
+    *bytes = size_t(num_instances) * size_t(num_save_at - 1) * floats * elem;
+  }
   if (c->ssm == PDQ_SSM_DENSE && c->strategy == PDQ_STRATEGY_FIXEDPOINT) {
     const int N = (c->num_derivatives + 1) * c->ode_dim;
     const size_t floats = size_t(N) * N + N + size_t(N) * (N + 1) / 2 + 2 * N;
@@ -148,7 +154,13 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
 
   if (c->ssm == PDQ_SSM_ISOTROPIC) {
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
-    if (c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
+    if (c->strategy != PDQ_STRATEGY_FILTER && c->strategy != PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_INVALID_VALUE;
+    const bool fp = c->strategy == PDQ_STRATEGY_FIXEDPOINT;
+    if (fp) {
+      size_t need = 0;
+      pdq_workspace_size(c, args->num_instances, args->num_save_at, &need);
+      if (workspace == nullptr || workspace_bytes < need) return PDQ_ERROR_WORKSPACE;
+    }
     pdq::IsoArgs a;
     memset(&a, 0, sizeof(a));
     a.B = args->num_instances;
@@ -199,26 +211,30 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     // kernel (8 lanes per instance) with <= 128 / <= 85 registers per lane,
     // for exact checkpoint landings only
     const bool warp = c->clip_dt && c->kernel_variant >= 2;
-    if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1 || a.state_error)) return PDQ_ERROR_UNSUPPORTED;
+    if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1 || a.state_error || fp)) return PDQ_ERROR_UNSUPPORTED;
+    a.workspace = workspace;
     const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : 64;
     const bool f64 = c->precision == PDQ_PRECISION_F64;
     cudaError_t err;
+    using IsoLaunch = cudaError_t (*)(const pdq::IsoArgs&, int, bool, cudaStream_t, int);
+    IsoLaunch launch = nullptr;
     switch (c->field) {
       case PDQ_FIELD_LOTKA_VOLTERRA:
-        err = f64 ? pdq_launch_iso_lv_f64(a, c->num_derivatives, interp, stream, block)
-                  : pdq_launch_iso_lv_f32(a, c->num_derivatives, interp, stream, block);
+        launch = fp ? (f64 ? pdq_launch_iso_fp_lv_f64 : pdq_launch_iso_fp_lv_f32)
+                    : (f64 ? pdq_launch_iso_lv_f64 : pdq_launch_iso_lv_f32);
         break;
       case PDQ_FIELD_VAN_DER_POL:
-        err = f64 ? pdq_launch_iso_vdp_f64(a, c->num_derivatives, interp, stream, block)
-                  : pdq_launch_iso_vdp_f32(a, c->num_derivatives, interp, stream, block);
+        launch = fp ? (f64 ? pdq_launch_iso_fp_vdp_f64 : pdq_launch_iso_fp_vdp_f32)
+                    : (f64 ? pdq_launch_iso_vdp_f64 : pdq_launch_iso_vdp_f32);
         break;
       case PDQ_FIELD_FITZHUGH_NAGUMO:
-        err = f64 ? pdq_launch_iso_fhn_f64(a, c->num_derivatives, interp, stream, block)
-                  : pdq_launch_iso_fhn_f32(a, c->num_derivatives, interp, stream, block);
+        launch = fp ? (f64 ? pdq_launch_iso_fp_fhn_f64 : pdq_launch_iso_fp_fhn_f32)
+                    : (f64 ? pdq_launch_iso_fhn_f64 : pdq_launch_iso_fhn_f32);
         break;
       default:
         return PDQ_ERROR_UNSUPPORTED;
     }
+    err = launch(a, c->num_derivatives, interp, stream, block);
     return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
   }
   if (c->ssm == PDQ_SSM_BLOCKDIAG) {

@@ -308,3 +308,56 @@ def test_error_state_std(solver, constraint):
         o = res.u[-1]
         compare_record(out["u_mean"][b, 0], out["u_chol"][b, 0], o.mean, o.cholesky, out["num_steps"][b, 0],
                        res.num_steps[-1], tolerances("float64"))
+
+
+@pytest.mark.parametrize("clip_dt", [False, True])
+@pytest.mark.parametrize("solver", ["dynamic", "mle"])
+def test_fixedpoint_smoother_save_at(solver, clip_dt):
+    """strategy_smoother_fixedpoint in the isotropic kernel (estimators_and_losses.py:473-591):
+    smoothed marginals at every checkpoint after the backward pass, float64, vs the oracle."""
+    from probdiffeq_gb300 import ensemble
+
+    params, y0 = lv_instances(2, seed=5)
+    save_at = [0.0, 1.3, 2.0, 3.7, 5.0]
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=3, ode_dim=2, strategy="fixedpoint",
+                               solver=solver, precision="float64", atol=1e-5, rtol=1e-5, clip_dt=clip_dt)
+    out = ensemble.solve_ensemble(cfg, params=params, y0=y0, save_at=torch.tensor(save_at), dt0=0.1,
+                                  terminal_only=False)
+    torch.cuda.synchronize()
+    out = {k: v.cpu() for k, v in out.items() if not k.startswith("_") and v is not None}
+    assert (out["status"] == 0).all()
+    for b in range(2):
+        fn = problems.FIELDS["lotka_volterra"]
+        tc = problems.taylor_derivatives(fn, y0[b], params[b], 3)
+        S = ssm.IsoSSM()
+        c = S.constraint_ode_ts0(lambda u, t, p=params[b]: fn(u[0], p))
+        cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE}[solver]
+        res = solvers.solve_adaptive_save_at(cls(solvers.StrategyFixedPoint(), c), solvers.ErrorResidualStd(c),
+                                             S.prior_wiener_integrated(tc), save_at, 1e-5, 1e-5, clip_dt=clip_dt,
+                                             dt0=0.1)
+        for s in range(len(save_at)):
+            o = res.u[s]
+            steps_o = 0 if s == 0 else res.num_steps[s - 1]
+            compare_record(out["u_mean"][b, s], out["u_chol"][b, s], o.mean, o.cholesky, out["num_steps"][b, s],
+                           steps_o, tolerances("float64"))
+            assert abs(float(out["t"][b, s]) - save_at[s]) < 1e-9
+        if solver == "mle":
+            assert abs(float(out["output_scale"][b, -1]) - float(res.output_scale[-1])) <= 1e-6 * float(res.output_scale[-1])
+
+
+def test_fixedpoint_smoother_float32_terminal():
+    """Float32 fixed-point smoother: terminal values and the smoothed initial state."""
+    from probdiffeq_gb300 import ensemble
+
+    params, y0 = lv_instances(4, seed=6)
+    save_at = [0.0, 2.5, 5.0]
+    outs = {}
+    for prec in ("float32", "float64"):
+        cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=3, ode_dim=2, strategy="fixedpoint",
+                                   solver="mle", precision=prec, atol=1e-4, rtol=1e-4, clip_dt=False)
+        o = ensemble.solve_ensemble(cfg, params=params, y0=y0, save_at=torch.tensor(save_at), dt0=0.1, terminal_only=False)
+        torch.cuda.synchronize()
+        outs[prec] = {k: v.cpu() for k, v in o.items() if not k.startswith("_") and v is not None}
+        assert (outs[prec]["status"] == 0).all()
+    m32, m64 = outs["float32"]["u_mean"][:, :, 0], outs["float64"]["u_mean"][:, :, 0]
+    assert float(((m32 - m64).abs() / m64.abs()).max()) < 1e-3
