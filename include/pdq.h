@@ -26,8 +26,18 @@
 #ifndef PDQ_H_
 #define PDQ_H_
 
+#if defined(__CUDACC_RTC__)
+/* runtime compilation (NVRTC) of the solver templates with a user vector
+ * field: no C library headers there */
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+typedef unsigned long size_t;
+#else
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -42,7 +52,8 @@ typedef enum pdq_status {
   PDQ_ERROR_CUDA = 3,
   PDQ_ERROR_WORKSPACE = 4,
   PDQ_ERROR_ABI_VERSION = 5,
-  PDQ_ERROR_STATIC_SCRATCH = 6
+  PDQ_ERROR_STATIC_SCRATCH = 6,
+  PDQ_ERROR_COMPILE = 7
 } pdq_status;
 
 /* State-space factorisation (probdiffeq/_probdiffeq/ssm_impl_*.py). */
@@ -65,7 +76,8 @@ enum {
   PDQ_FIELD_LOTKA_VOLTERRA = 0, /* params (a, b, c, d), d = 2 */
   PDQ_FIELD_VAN_DER_POL = 1,    /* params (mu), d = 2 */
   PDQ_FIELD_FITZHUGH_NAGUMO = 2,/* params (a, b, c), d = 2 */
-  PDQ_FIELD_BURGERS = 3         /* params (nu), periodic grid, any d */
+  PDQ_FIELD_BURGERS = 3,        /* params (nu), periodic grid, any d */
+  PDQ_FIELD_USER_BASE = 1000    /* ids returned by pdq_register_field */
 };
 
 /* Per-instance run-time status. */
@@ -141,26 +153,38 @@ typedef struct pdq_lml_args {
 } pdq_lml_args;
 
 /* ABI version compiled into the library. */
+#if !defined(__CUDACC_RTC__)
 uint32_t pdq_abi_version(void);
+#endif
 
 /* Human-readable name of a status code (static storage). */
+#if !defined(__CUDACC_RTC__)
 const char* pdq_status_string(pdq_status status);
+#endif
 
 /* Fill a config with the reference's defaults for the given factorisation:
  * filter strategy, solver_dynamic, error_residual_std, control_integral,
  * TS0, float32 bulk, clip_dt 1, eps 1e-8, damp 0, atol = rtol = 1e-6. */
+#if !defined(__CUDACC_RTC__)
 pdq_status pdq_config_default(pdq_config* config, int32_t ssm, int32_t field, int32_t num_derivatives, int32_t ode_dim);
+#endif
 
 /* Device scratch the solve needs, in bytes (0 for configurations without scratch). */
+#if !defined(__CUDACC_RTC__)
 pdq_status pdq_workspace_size(const pdq_config* config, int64_t num_instances, int32_t num_save_at, size_t* bytes);
+#endif
 
 /* Adaptive solve of B independent instances; see the file header. */
+#if !defined(__CUDACC_RTC__)
 pdq_status pdq_solve_adaptive(const pdq_config* config, const pdq_adaptive_args* args, void* workspace,
                               size_t workspace_bytes, void* stream);
+#endif
 
 /* Device scratch of pdq_lml_fixed_grid in bytes. */
+#if !defined(__CUDACC_RTC__)
 pdq_status pdq_lml_workspace_size(const pdq_config* config, int64_t num_instances, int32_t num_steps, int32_t save_every,
                                   size_t* bytes);
+#endif
 
 /* Log-marginal likelihood of time-series data, and its gradient with respect
  * to the vector-field parameters, for B parameter samples:
@@ -172,8 +196,10 @@ pdq_status pdq_lml_workspace_size(const pdq_config* config, int64_t num_instance
  * The gradient follows the reference's differentiation rules (qr_r's custom
  * JVP, probdiffeq/backend/linalg.py:13-37; no gradient through dt).
  * config: ssm isotropic, constraint TS0, strategy fixedpoint, solver plain. */
+#if !defined(__CUDACC_RTC__)
 pdq_status pdq_lml_fixed_grid(const pdq_config* config, const pdq_lml_args* args, void* workspace, size_t workspace_bytes,
                               void* stream);
+#endif
 
 /* Size of the scratch array inside the library used by pdq_lml_fixed_grid_static. */
 #define PDQ_LML_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
@@ -189,7 +215,31 @@ pdq_status pdq_lml_fixed_grid(const pdq_config* config, const pdq_lml_args* args
  * make it before any stream capture.  All calls share the array: calls whose
  * launches overlap on the GPU race.  Allocates nothing (no cudaMalloc or
  * cudaFree). */
+#if !defined(__CUDACC_RTC__)
 pdq_status pdq_lml_fixed_grid_static(const pdq_config* config, const pdq_lml_args* args, void* stream);
+#endif
+
+/* Register a vector field given as CUDA C++ source, compiled at run time
+ * (NVRTC) into the isotropic solver.  Replaces passing a Python callable to
+ * probdiffeq.ode (probdiffeq/_probdiffeq/problems.py:283-295); the registry
+ * of device functors is the boundary's plugin seam for new models.
+ * `source` defines, at namespace scope,
+ *   struct Field {
+ *     static constexpr int D = <state dimension>, P = <number of parameters>;
+ *     template <typename S, typename T> PDQ_HD static void eval(const S* u, const T* p, S* out);
+ *   };
+ * generic over the scalar S (float, double, Taylor jets, dual numbers).  On
+ * success *field_id (>= PDQ_FIELD_USER_BASE) goes into pdq_config.field
+ * (isotropic factorisation; dim and num_params must match D and P).
+ * Compiler diagnostics are copied to `log` (host buffer, may be NULL);
+ * errors return PDQ_ERROR_COMPILE.  The source is validated by compiling one
+ * variant now; each variant used later is compiled and loaded on first use
+ * (so the first solve of a variant takes seconds, then it is cached).
+ * Host pointers; thread-safe. */
+#if !defined(__CUDACC_RTC__)
+pdq_status pdq_register_field(const char* name, const char* source, int32_t dim, int32_t num_params,
+                              int32_t* field_id, char* log, size_t log_bytes);
+#endif
 
 #ifdef __cplusplus
 }

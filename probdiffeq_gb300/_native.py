@@ -128,6 +128,11 @@ SIGNATURES = {
         ctypes.c_int,
         [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlArgs), ctypes.c_void_p],
     ),
+    "pdq_register_field": (
+        ctypes.c_int,
+        [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+         ctypes.c_char_p, ctypes.c_size_t],
+    ),
     "pdq_probe_fp32_fma": (
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
@@ -174,6 +179,22 @@ def status_string(status):
 def check(status, where):
     if status != 0:
         raise NativeError(status, where)
+
+
+def register_field(name, source, dim, num_params):
+    """Compile a user vector field (CUDA C++ source of ``struct Field``) with
+    NVRTC (``pdq_register_field``); returns its field id and makes ``name``
+    usable wherever a field name is accepted.  Raises NativeError with the
+    compiler log on failure."""
+    lib = load()
+    fid = ctypes.c_int32(-1)
+    log = ctypes.create_string_buffer(1 << 16)
+    st = lib.pdq_register_field(name.encode(), source.encode(), int(dim), int(num_params), ctypes.byref(fid), log,
+                                ctypes.sizeof(log))
+    if st != 0:
+        raise NativeError(st, "pdq_register_field:\n" + log.value.decode(errors="replace"))
+    FIELD[name] = fid.value
+    return fid.value
 
 
 def config_default(ssm, field, num_derivatives, ode_dim):

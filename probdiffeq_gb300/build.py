@@ -30,7 +30,39 @@ NVCC_FLAGS = [
     "-fPIC",
     "-I" + INCLUDE,
     "-I" + CSRC,
+    "-I" + BUILD,
 ]
+
+# Headers compiled at run time (NVRTC) together with user vector fields; they
+# are embedded in the library as string literals.
+EMBEDDED_HEADERS = [
+    ("pdq.h", os.path.join(INCLUDE, "pdq.h")),
+    ("pdq_device.cuh", os.path.join(CSRC, "pdq_device.cuh")),
+    ("iso_solver.cuh", os.path.join(CSRC, "iso_solver.cuh")),
+]
+
+
+def write_embedded_headers():
+    """Generate ``_build/pdq_embedded_headers.inc`` (raw string literals of the headers)."""
+    os.makedirs(BUILD, exist_ok=True)
+    names, bodies = [], []
+    for name, path in EMBEDDED_HEADERS:
+        with open(path) as f:
+            text = f.read()
+        delim = "PDQHDR"
+        if ")" + delim + '"' in text:
+            raise RuntimeError(f"{name} contains the raw-string delimiter")
+        names.append('"' + name + '"')
+        bodies.append('R"' + delim + "(" + text + ")" + delim + '"')
+    out = "// generated by probdiffeq_gb300/build.py from the solver headers\n"
+    out += f"static const int kPdqHeaderCount = {len(names)};\n"
+    out += "static const char* const kPdqHeaderNames[] = {" + ", ".join(names) + "};\n"
+    out += "static const char* const kPdqHeaderSources[] = {\n" + ",\n".join(bodies) + "};\n"
+    path = os.path.join(BUILD, "pdq_embedded_headers.inc")
+    old = open(path).read() if os.path.exists(path) else None
+    if old != out:
+        with open(path, "w") as f:
+            f.write(out)
 
 
 def nvcc_path():
@@ -61,6 +93,7 @@ def build(force=False, verbose=False):
         return LIB
     nvcc = nvcc_path()
     os.makedirs(BUILD, exist_ok=True)
+    write_embedded_headers()
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
@@ -77,7 +110,7 @@ def build(force=False, verbose=False):
     with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-gencode", GENCODE, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc, "-gencode", GENCODE, "-shared", "-o", tmp, *objs, "-lnvrtc"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

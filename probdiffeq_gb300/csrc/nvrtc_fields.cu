@@ -1,0 +1,187 @@
+// User vector fields compiled at run time (NVRTC) into the isotropic solver.
+//
+// The reference takes any Python callable as the vector field
+// (probdiffeq.ode, _probdiffeq/problems.py:283-295) and traces it into the
+// solver.  Here a field is CUDA C++ source of a functor
+//
+//   struct Field {
+//     static constexpr int D = ...;   // state dimension
+//     static constexpr int P = ...;   // number of parameters
+//     template <typename S, typename T>
+//     PDQ_HD static void eval(const S* u, const T* p, S* out);  // out = f(u; p)
+//   };
+//
+// written generically over the scalar S (float, double, Taylor jets, dual
+// numbers: +, -, * and multiplication / division by parameters), exactly
+// like the built-in fields, so one definition yields f, its Jacobian and the
+// Taylor-mode initial derivatives.  pdq_register_field compiles the source
+// with the solver templates (headers embedded in this library) for sm_103a
+// and reports compiler errors; each (precision, nu, interpolation, strategy)
+// variant is compiled and loaded on first use and cached.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "iso_solver.cuh"
+#include "nvrtc_fields.h"
+#include "pdq.h"
+#include "pdq_embedded_headers.inc"  // kPdqHeaderCount, kPdqHeaderNames, kPdqHeaderSources (generated)
+
+namespace {
+
+struct UserField {
+  std::string name, source;
+  int dim = 0, params = 0;
+  std::mutex mu;
+  // (f64, nu, interp, fixedpoint) -> loaded kernel
+  std::map<std::tuple<int, int, int, int>, cudaKernel_t> kernels;
+  std::vector<cudaLibrary_t> libraries;
+};
+
+std::mutex g_registry_mu;
+std::vector<std::unique_ptr<UserField>> g_fields;
+
+UserField* lookup(int32_t field) {
+  std::lock_guard<std::mutex> lock(g_registry_mu);
+  const int64_t k = int64_t(field) - PDQ_FIELD_USER_BASE;
+  if (k < 0 || k >= int64_t(g_fields.size())) return nullptr;
+  return g_fields[size_t(k)].get();
+}
+
+std::string kernel_expression(bool f64, int nu, bool interp, bool fp) {
+  return std::string("pdq::iso_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
+         ", pdq_user::Field, " + (interp ? "true" : "false") + ", " + (fp ? "true" : "false") + ">";
+}
+
+void copy_log(const std::string& text, char* log, size_t log_bytes) {
+  if (log == nullptr || log_bytes == 0) return;
+  const size_t n = text.size() < log_bytes - 1 ? text.size() : log_bytes - 1;
+  std::memcpy(log, text.data(), n);
+  log[n] = '\0';
+}
+
+// Compile the solver templates with the field source; returns the cubin and
+// the lowered (mangled) names of the requested kernel instantiations.
+pdq_status compile(const std::string& source, const std::vector<std::string>& expressions, std::string* cubin,
+                   std::vector<std::string>* lowered, std::string* log) {
+  const std::string program = "#include \"iso_solver.cuh\"\nnamespace pdq_user {\n" + source + "\n}  // namespace pdq_user\n";
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, program.c_str(), "user_field.cu", kPdqHeaderCount, kPdqHeaderSources,
+                         kPdqHeaderNames) != NVRTC_SUCCESS)
+    return PDQ_ERROR_COMPILE;
+  for (const auto& e : expressions) nvrtcAddNameExpression(prog, e.c_str());
+  const char* options[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-lineinfo"};
+  const nvrtcResult rc = nvrtcCompileProgram(prog, 3, options);
+  size_t log_size = 0;
+  nvrtcGetProgramLogSize(prog, &log_size);
+  std::string text(log_size, '\0');
+  if (log_size > 0) nvrtcGetProgramLog(prog, &text[0]);
+  if (log) *log = text;
+  if (rc != NVRTC_SUCCESS) {
+    nvrtcDestroyProgram(&prog);
+    return PDQ_ERROR_COMPILE;
+  }
+  size_t size = 0;
+  if (nvrtcGetCUBINSize(prog, &size) != NVRTC_SUCCESS || size == 0) {
+    nvrtcDestroyProgram(&prog);
+    return PDQ_ERROR_COMPILE;
+  }
+  cubin->assign(size, '\0');
+  nvrtcGetCUBIN(prog, &(*cubin)[0]);
+  lowered->clear();
+  for (const auto& e : expressions) {
+    const char* name = nullptr;
+    if (nvrtcGetLoweredName(prog, e.c_str(), &name) != NVRTC_SUCCESS || name == nullptr) {
+      nvrtcDestroyProgram(&prog);
+      return PDQ_ERROR_COMPILE;
+    }
+    lowered->emplace_back(name);
+  }
+  nvrtcDestroyProgram(&prog);
+  return PDQ_SUCCESS;
+}
+
+bool nonempty(const char* s) { return s != nullptr && s[0] != '\0'; }
+
+}  // namespace
+
+extern "C" pdq_status pdq_register_field(const char* name, const char* source, int32_t dim, int32_t num_params,
+                                         int32_t* field_id, char* log, size_t log_bytes) {
+  if (field_id == nullptr || !nonempty(name) || !nonempty(source) ||
+      dim < 1 || dim > 64 || num_params < 0 || num_params > 64)
+    return PDQ_ERROR_INVALID_VALUE;
+  // validate by compiling one variant (no device needed)
+  std::string cubin, text;
+  std::vector<std::string> lowered;
+  const pdq_status st = compile(source, {kernel_expression(false, 2, false, false)}, &cubin, &lowered, &text);
+  copy_log(text, log, log_bytes);
+  if (st != PDQ_SUCCESS) return st;
+  auto f = std::make_unique<UserField>();
+  f->name = name;
+  f->source = source;
+  f->dim = dim;
+  f->params = num_params;
+  std::lock_guard<std::mutex> lock(g_registry_mu);
+  *field_id = PDQ_FIELD_USER_BASE + int32_t(g_fields.size());
+  g_fields.push_back(std::move(f));
+  return PDQ_SUCCESS;
+}
+
+int pdq_user_field_dim(int32_t field) {
+  UserField* f = lookup(field);
+  return f ? f->dim : 0;
+}
+
+int pdq_user_field_params(int32_t field) {
+  UserField* f = lookup(field);
+  return f ? f->params : -1;
+}
+
+cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, int nu, bool interp, bool fp,
+                                cudaStream_t stream, int block) {
+  UserField* f = lookup(field);
+  if (f == nullptr || nu < 1 || nu > 5) return cudaErrorInvalidValue;
+  cudaKernel_t kernel = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(f->mu);
+    const auto key = std::make_tuple(f64 ? 1 : 0, nu, interp ? 1 : 0, fp ? 1 : 0);
+    auto it = f->kernels.find(key);
+    if (it != f->kernels.end()) {
+      kernel = it->second;
+    } else {
+      std::string cubin, text;
+      std::vector<std::string> lowered;
+      if (compile(f->source, {kernel_expression(f64, nu, interp, fp)}, &cubin, &lowered, &text) != PDQ_SUCCESS)
+        return cudaErrorInvalidSource;
+      cudaLibrary_t lib = nullptr;
+      cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+      if (e != cudaSuccess) return e;
+      e = cudaLibraryGetKernel(&kernel, lib, lowered[0].c_str());
+      if (e != cudaSuccess) return e;
+      // the per-thread stack limit must cover the kernel's frame (as for the built-in kernels)
+      cudaFuncAttributes attr;
+      e = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(kernel));
+      if (e != cudaSuccess) return e;
+      size_t cur = 0;
+      e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
+      if (e != cudaSuccess) return e;
+      if (attr.localSizeBytes + 1024 > cur) {
+        e = cudaDeviceSetLimit(cudaLimitStackSize, attr.localSizeBytes + 1024);
+        if (e != cudaSuccess) return e;
+      }
+      f->libraries.push_back(lib);
+      f->kernels.emplace(key, kernel);
+    }
+  }
+  pdq::IsoArgs args = a;
+  void* params[] = {&args};
+  const unsigned grid = unsigned((a.B + block - 1) / block);
+  return cudaLaunchKernel(reinterpret_cast<const void*>(kernel), dim3(grid), dim3(unsigned(block)), params, 0, stream);
+}

@@ -1,0 +1,16 @@
+// Internal interface between the C ABI dispatch and the run-time compiled
+// user vector fields (nvrtc_fields.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "iso_solver.cuh"
+
+// State dimension / number of parameters of a registered user field (0 / -1 if unknown).
+int pdq_user_field_dim(int32_t field);
+int pdq_user_field_params(int32_t field);
+
+// Launch the isotropic kernel instantiated for a registered user field;
+// compiles and loads the variant on first use.
+cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, int nu, bool interp, bool fp,
+                                cudaStream_t stream, int block);

@@ -7,6 +7,7 @@
 #include "dense_launch.cuh"
 #include "lml_launch.cuh"
 #include "iso_launch.cuh"
+#include "nvrtc_fields.h"
 #include "pdq.h"
 
 namespace {
@@ -33,6 +34,7 @@ void iwp_q1(int nu, double (&q)[pdq::kMaxN][pdq::kMaxN]) {
 }
 
 int field_dim(int field) {
+  if (field >= PDQ_FIELD_USER_BASE) return pdq_user_field_dim(field);
   switch (field) {
     case PDQ_FIELD_LOTKA_VOLTERRA:
     case PDQ_FIELD_VAN_DER_POL:
@@ -79,6 +81,7 @@ const char* pdq_status_string(pdq_status s) {
     case PDQ_ERROR_WORKSPACE: return "workspace too small";
     case PDQ_ERROR_ABI_VERSION: return "ABI version mismatch";
     case PDQ_ERROR_STATIC_SCRATCH: return "problem exceeds the library's static scratch array";
+    case PDQ_ERROR_COMPILE: return "run-time compilation of the vector field failed";
     default: return "unknown status";
   }
 }
@@ -216,6 +219,11 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : 64;
     const bool f64 = c->precision == PDQ_PRECISION_F64;
     cudaError_t err;
+    if (c->field >= PDQ_FIELD_USER_BASE) {
+      if (warp) return PDQ_ERROR_UNSUPPORTED;
+      err = pdq_launch_iso_user(a, c->field, f64, c->num_derivatives, interp, fp, stream, block);
+      return err == cudaSuccess ? PDQ_SUCCESS : (err == cudaErrorInvalidSource ? PDQ_ERROR_COMPILE : PDQ_ERROR_CUDA);
+    }
     using IsoLaunch = cudaError_t (*)(const pdq::IsoArgs&, int, bool, cudaStream_t, int);
     IsoLaunch launch = nullptr;
     switch (c->field) {

@@ -6,8 +6,10 @@
 // fully unrolled.
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <cuda_runtime.h>
 #include <stdint.h>
+#endif
 
 #include "pdq.h"
 
@@ -16,6 +18,7 @@
 
 namespace pdq {
 
+#if !defined(__CUDACC_RTC__)
 // Raise this context's per-thread stack limit to what `kernel` needs (its
 // local frame plus headroom for calls) before its first launch.  Kernels
 // whose frame exceeds the default limit (1 KB) otherwise overrun the stack.
@@ -48,6 +51,7 @@ inline cudaError_t ensure_stack() {
   if (e == cudaSuccess && bit) __atomic_fetch_or(&ready, bit, __ATOMIC_RELEASE);
   return e;
 }
+#endif  // !__CUDACC_RTC__
 
 // ---------------------------------------------------------------------------
 // Scalar helpers

@@ -21,6 +21,7 @@ from . import _native
 
 __all__ = [
     "ode",
+    "register_field",
     "Field",
     "jetexpand_ode_padded_scan",
     "jetexpand_ode_unroll",
@@ -56,6 +57,23 @@ class Field:
     jacobian: Any = None
     num_tcoeffs_in_args: int = 1
     tcoeff_indices_output: tuple = (1,)
+
+
+def register_field(name, source, *, dim, num_params):
+    """Register a vector field given as CUDA C++ source, compiled at run time.
+
+    The counterpart of passing a Python callable to ``probdiffeq.ode``
+    (problems.py:283-295): ``source`` defines ``struct Field`` with
+    ``static constexpr int D, P`` and a generic
+    ``template <typename S, typename T> PDQ_HD static void eval(const S* u, const T* p, S* out)``
+    (see ``include/pdq.h``, ``pdq_register_field``).  Afterwards
+    ``ode(name, params)`` describes it (isotropic factorisation).
+    """
+    if name in _FIELD_DIMS and name in _native.FIELD and _native.FIELD[name] < 1000:
+        raise ValueError(f"{name!r} is a built-in field")
+    _native.register_field(name, source, dim, num_params)
+    _FIELD_DIMS[name] = int(dim)
+    _FIELD_PARAMS[name] = int(num_params)
 
 
 def ode(name, params, *, jacobian=None):
