@@ -126,8 +126,13 @@ typedef struct pdq_adaptive_args {
   int32_t* num_steps;     /* (B, S_out) accepted steps up to each output */
   int32_t* num_attempts;  /* (B,) total attempts (accepted + rejected) */
   int32_t* status;        /* (B,) PDQ_INSTANCE_* */
-  /* optional outputs (NULL: not written); dense factorisation only, N = n*d */
-  double* cond_A;           /* (B, S-1, N, N) fixed-point smoother: backward conditional of each checkpoint */
+  /* optional outputs of the fixed-point smoother (NULL: not written; all or
+   * none): the posterior's backward conditional between consecutive
+   * checkpoints and the filtering marginals.  Dense, N = n*d: shapes below;
+   * isotropic: cond_A (B, S-1, n, n), cond_noise_mean (B, S-1, n, d),
+   * cond_noise_chol (B, S-1, n, n), cond_to_* (B, S-1, n), filter_mean
+   * (B, S, n, d), filter_chol (B, S, n, n). */
+  double* cond_A;           /* (B, S-1, N, N) */
   double* cond_noise_mean;  /* (B, S-1, N) */
   double* cond_noise_chol;  /* (B, S-1, N, N) */
   double* cond_to_latent;   /* (B, S-1, N) */
@@ -217,6 +222,35 @@ pdq_status pdq_lml_fixed_grid(const pdq_config* config, const pdq_lml_args* args
  * cudaFree). */
 #if !defined(__CUDACC_RTC__)
 pdq_status pdq_lml_fixed_grid_static(const pdq_config* config, const pdq_lml_args* args, void* stream);
+#endif
+
+/* Posterior samples of a fixed-point smoother solution, MarkovSequence.sample
+ * (probdiffeq/_probdiffeq/estimators_and_losses.py:233-273): draw the last
+ * point from its marginal, then walk the backward conditionals to the first
+ * point with cond.apply_flat (mean to_observed * (A (to_latent * x)) +
+ * noise_mean, factor |to_observed| noise_chol).  The standard-normal draws
+ * come in `normals`; as in the reference's isotropic sample_flat, one
+ * n-vector per point is shared by the d dimensions.  Device pointers. */
+typedef struct pdq_sample_args {
+  int32_t ssm;              /* PDQ_SSM_ISOTROPIC or PDQ_SSM_DENSE */
+  int32_t num_derivatives;  /* nu; n = nu + 1 */
+  int32_t ode_dim;          /* d; dense N = n * d */
+  int32_t num_points;       /* S: the marginal at point S-1 and S-1 conditionals */
+  int64_t num_instances;    /* B */
+  int32_t num_samples;      /* K per instance */
+  const double* marginal_mean;     /* iso (B, n, d) | dense (B, N): the marginal at the last point */
+  const double* marginal_chol;     /* iso (B, n, n) | dense (B, N, N) */
+  const double* cond_A;            /* as in pdq_adaptive_args */
+  const double* cond_noise_mean;
+  const double* cond_noise_chol;
+  const double* cond_to_latent;
+  const double* cond_to_observed;
+  const double* normals;           /* iso (B, K, S, n) | dense (B, K, S, N) */
+  double* samples;                 /* iso (B, K, S, n, d) | dense (B, K, S, N) */
+} pdq_sample_args;
+
+#if !defined(__CUDACC_RTC__)
+pdq_status pdq_sample_markov(const pdq_sample_args* args, void* stream);
 #endif
 
 /* Register a vector field given as CUDA C++ source, compiled at run time

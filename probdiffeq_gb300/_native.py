@@ -81,6 +81,26 @@ class PdqAdaptiveArgs(ctypes.Structure):
     ]
 
 
+class PdqSampleArgs(ctypes.Structure):
+    _fields_ = [
+        ("ssm", ctypes.c_int32),
+        ("num_derivatives", ctypes.c_int32),
+        ("ode_dim", ctypes.c_int32),
+        ("num_points", ctypes.c_int32),
+        ("num_instances", ctypes.c_int64),
+        ("num_samples", ctypes.c_int32),
+        ("marginal_mean", ctypes.c_void_p),
+        ("marginal_chol", ctypes.c_void_p),
+        ("cond_A", ctypes.c_void_p),
+        ("cond_noise_mean", ctypes.c_void_p),
+        ("cond_noise_chol", ctypes.c_void_p),
+        ("cond_to_latent", ctypes.c_void_p),
+        ("cond_to_observed", ctypes.c_void_p),
+        ("normals", ctypes.c_void_p),
+        ("samples", ctypes.c_void_p),
+    ]
+
+
 class PdqLmlArgs(ctypes.Structure):
     _fields_ = [
         ("num_instances", ctypes.c_int64),
@@ -128,6 +148,7 @@ SIGNATURES = {
         ctypes.c_int,
         [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlArgs), ctypes.c_void_p],
     ),
+    "pdq_sample_markov": (ctypes.c_int, [ctypes.POINTER(PdqSampleArgs), ctypes.c_void_p]),
     "pdq_register_field": (
         ctypes.c_int,
         [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
@@ -279,6 +300,16 @@ def alloc_outputs(cfg, B, S, terminal_only, device, posterior=False):
         mean_shape, chol_shape = (B, S_out, d, n), (B, S_out, d, n, n)
     else:
         mean_shape, chol_shape = (B, S_out, n, d), (B, S_out, n, n)
+        if posterior:
+            extra = {
+                "cond_A": torch.empty((B, S - 1, n, n), **f64),
+                "cond_noise_mean": torch.empty((B, S - 1, n, d), **f64),
+                "cond_noise_chol": torch.empty((B, S - 1, n, n), **f64),
+                "cond_to_latent": torch.empty((B, S - 1, n), **f64),
+                "cond_to_observed": torch.empty((B, S - 1, n), **f64),
+                "filter_mean": torch.empty((B, S, n, d), **f64),
+                "filter_chol": torch.empty((B, S, n, n), **f64),
+            }
     return {
         **extra,
         "u_mean": torch.empty(mean_shape, **f64),
@@ -319,3 +350,25 @@ def lml_fixed_grid(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every,
           "pdq_lml_fixed_grid")
     outputs["_workspace"] = ws
     return outputs
+
+
+def sample_markov(ssm, num_derivatives, ode_dim, marginal_mean, marginal_chol, posterior, normals, stream=None):
+    """Call pdq_sample_markov on device float64 tensors; returns the samples tensor.
+
+    marginal_*: the last point's marginal (B, ...); posterior: the fixed-point
+    outputs ``cond_*`` (B, S - 1, ...); normals (B, K, S, n) isotropic or
+    (B, K, S, N) dense.
+    """
+    B, K, S = normals.shape[0], normals.shape[1], normals.shape[2]
+    n = num_derivatives + 1
+    shape = (B, K, S, n, ode_dim) if ssm == "isotropic" else (B, K, S, n * ode_dim)
+    samples = torch.empty(shape, dtype=torch.float64, device=normals.device)
+    a = PdqSampleArgs()
+    a.ssm, a.num_derivatives, a.ode_dim, a.num_points = SSM[ssm], num_derivatives, ode_dim, S
+    a.num_instances, a.num_samples = B, K
+    a.marginal_mean, a.marginal_chol = _ptr(marginal_mean.contiguous()), _ptr(marginal_chol.contiguous())
+    for k in ("cond_A", "cond_noise_mean", "cond_noise_chol", "cond_to_latent", "cond_to_observed"):
+        setattr(a, k, _ptr(posterior[k]) if posterior is not None else None)
+    a.normals, a.samples = _ptr(normals), _ptr(samples)
+    check(load().pdq_sample_markov(ctypes.byref(a), _stream_handle(stream)), "pdq_sample_markov")
+    return samples

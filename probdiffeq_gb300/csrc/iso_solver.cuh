@@ -54,6 +54,16 @@ struct IsoArgs {
   int32_t* num_attempts;
   int32_t* status;
   void* workspace;  // fixed-point smoother: (B, S - 1) backward conditionals in T
+  // optional fixed-point outputs (nullptr: not written): the posterior's
+  // backward conditionals between consecutive checkpoints and the filtering
+  // marginals at the checkpoints
+  double* cond_A;            // (B, S - 1, n, n)
+  double* cond_noise_mean;   // (B, S - 1, n, d)
+  double* cond_noise_chol;   // (B, S - 1, n, n), calibrated
+  double* cond_to_latent;    // (B, S - 1, n)
+  double* cond_to_observed;  // (B, S - 1, n)
+  double* filter_mean;       // (B, S, n, d)
+  double* filter_chol;       // (B, S, n, n), calibrated
 };
 
 // A constant in the kernel's precision: the float copy for float, else the double.
@@ -564,6 +574,29 @@ PDQ_D void iso_cond_marginalise(const IsoBackward<T, NU, D>& c, const T (&m)[NU 
 }
 
 template <typename T, int NU, int D>
+PDQ_D void write_filter(const IsoArgs& a, int64_t rec, const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1]) {
+  constexpr int n = NU + 1;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < D; ++j) a.filter_mean[rec * (n * D) + i * D + j] = double(m[i][j]);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) a.filter_chol[rec * (n * n) + i * n + j] = double(L[i][j]);
+}
+
+template <typename T, int NU, int D>
+PDQ_D void write_cond_iso(const IsoArgs& a, int64_t cr, const IsoBackward<T, NU, D>& c, double cal) {
+  constexpr int n = NU + 1;
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < n; ++j) {
+      a.cond_A[cr * n * n + i * n + j] = double(c.A[i][j]);
+      a.cond_noise_chol[cr * n * n + i * n + j] = double(c.X[i][j]) * cal;
+    }
+    for (int j = 0; j < D; ++j) a.cond_noise_mean[cr * n * D + i * D + j] = double(c.xi[i][j]);
+    a.cond_to_latent[cr * n + i] = double(c.tl[i]);
+    a.cond_to_observed[cr * n + i] = double(c.to[i]);
+  }
+}
+
+template <typename T, int NU, int D>
 PDQ_D void write_normal_iso(const IsoArgs& a, int64_t rec, const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1]) {
   constexpr int n = NU + 1;
   double* um = a.u_mean + rec * (n * D);
@@ -661,6 +694,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           q11 = cst<T>(a.q1[1][1], a.q1f[1][1]);
 
   if (!a.terminal_only) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, wide_value(t), 0);
+  if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S, m, L);
 
   // t + eps < t_next (float64: exactly the reference's comparison; float
   // pairs: the difference, rounded once, against eps)
@@ -884,6 +918,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
           }
           if (record) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), wide_value(t_next), num_steps);
+          if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, mp, Lp);
           ti = t_next;
 #pragma unroll
           for (int i = 0; i < n; ++i) {
@@ -896,6 +931,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
       } else {
         // interp_at_t1: the state itself is the solution (estimators_and_losses.py:416-421)
         if (record) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), wide_value(t), num_steps);
+        if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, m, L);
         if constexpr (FP) {
           // estimators_and_losses.py:534-547: close the checkpoint's conditional, reset
           iso_cond_store(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), bw);
@@ -920,13 +956,21 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   // ---- fixed-point backward pass: marginals at the checkpoints ----
   if constexpr (FP) {
     if (status == PDQ_INSTANCE_OK) {
+      // the calibrated scale multiplies every Cholesky factor (finalize below);
+      // the optional conditional outputs take it here
+      double cal = 1.0;
+      if (a.solver == PDQ_SOLVER_MLE) {
+        cal = num_data > 0 ? sqrt(wide_value(mle_sumsq) / num_data) : 0.0;
+        if (a.correct) cal /= sqrt(double(num_steps));
+      }
       T rm[n][D], rL[n][n];
       iso_cond_marginalise(bw, m, L, rm, rL);
       for (int s = S - 1; s >= 1; --s) {
         if (!a.terminal_only || s == S - 1) write_normal_iso<T, NU, D>(a, b * S_out + (a.terminal_only ? 0 : s), rm, rL);
-        if (a.terminal_only) break;
         IsoBackward<T, NU, D> c;
         iso_cond_load(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), c);
+        if (a.cond_A) write_cond_iso<T, NU, D>(a, b * (S - 1) + (s - 1), c, cal);
+        if (a.terminal_only) continue;
         T pm[n][D], pL[n][n];
         iso_cond_marginalise(c, rm, rL, pm, pL);
 #pragma unroll
@@ -955,6 +999,8 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
         for (int k = 0; k < n * n; ++k) uc[k] *= scale;
         a.output_scale[rec] = scale;
       }
+      if (FP && a.filter_chol)
+        for (int k = 0; k < S * n * n; ++k) a.filter_chol[b * S * n * n + k] *= scale;
     }
   } else {
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);

@@ -216,6 +216,18 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     const bool warp = c->clip_dt && c->kernel_variant >= 2;
     if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1 || a.state_error || fp)) return PDQ_ERROR_UNSUPPORTED;
     a.workspace = workspace;
+    if (fp) {
+      a.cond_A = args->cond_A;
+      a.cond_noise_mean = args->cond_noise_mean;
+      a.cond_noise_chol = args->cond_noise_chol;
+      a.cond_to_latent = args->cond_to_latent;
+      a.cond_to_observed = args->cond_to_observed;
+      a.filter_mean = args->filter_mean;
+      a.filter_chol = args->filter_chol;
+      if ((a.cond_A || a.filter_mean) && (!a.cond_A || !a.cond_noise_mean || !a.cond_noise_chol || !a.cond_to_latent ||
+                                          !a.cond_to_observed || !a.filter_mean || !a.filter_chol))
+        return PDQ_ERROR_INVALID_VALUE;
+    }
     const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : 64;
     const bool f64 = c->precision == PDQ_PRECISION_F64;
     cudaError_t err;

@@ -86,6 +86,7 @@ class Solution:
     num_attempts: torch.Tensor
     status: torch.Tensor
     posterior: Any = None
+    ode_dim: Any = None
 
 
 def _prior_inputs(prior):
@@ -124,6 +125,7 @@ def _run(prior, solver, error, control, save_at, *, atol, rtol, dt0, eps, damp, 
         num_attempts=out["num_attempts"],
         status=out["status"],
         posterior=post,
+        ode_dim=y0.shape[-1],
     )
 
 
@@ -162,15 +164,20 @@ def solve_fixed_grid(*, solver, precision="float32", device="cuda"):
     """
     if not solver.is_suitable_for_save_every_step:
         warnings.warn(f"Solver {solver} should not be used in solve_fixed_grid (fixedpoint).", stacklevel=2)
+    if solver.strategy.name == "fixedinterval":
+        # every grid point is a checkpoint: the fixed-point conditionals are the per-step ones
+        strategy = type(solver.strategy)()
+        strategy._on_grid = True
+        solver = dataclasses.replace(solver, strategy=strategy)
 
-    def solve(u, /, *, grid, damp=0.0, stream=None):
+    def solve(u, /, *, grid, damp=0.0, posterior=False, stream=None):
         grid = torch.as_tensor(grid, dtype=torch.float64)
         span = float((grid[..., -1] - grid[..., 0]).abs().max())
         # eps far above the rounding of t, far below any grid spacing
         eps = 1e-12 * max(1.0, float(grid.abs().max()))
         return _run(u, solver, None, control_integral(factor_max=1e30), grid, atol=float("inf"), rtol=0.0,
                     dt0=10.0 * span + 1.0, eps=eps, damp=damp, clip_dt=True, terminal_only=False,
-                    precision=precision, device=device, stream=stream)
+                    precision=precision, device=device, posterior=posterior, stream=stream)
 
     return solve
 

@@ -30,6 +30,7 @@ __all__ = [
     "state_space_model_dense",
     "strategy_filter",
     "strategy_smoother_fixedpoint",
+    "strategy_smoother_fixedinterval",
     "solver",
     "solver_mle",
     "solver_dynamic",
@@ -212,6 +213,21 @@ class strategy_smoother_fixedpoint:
     is_suitable_for_save_every_step = False
 
 
+class strategy_smoother_fixedinterval:
+    """estimators_and_losses.py:594-717: the smoother with a backward conditional per step.
+
+    Native on fixed grids (``ivpsolve.solve_fixed_grid``): there every grid
+    point is a checkpoint, so the fixed-point kernel's conditionals between
+    checkpoints are exactly the per-step conditionals and its smoothed
+    marginals are the fixed-interval smoother's (the equivalence of the
+    reference's test_smoother_fixedinterval_vs_fixedpoint.py).
+    """
+
+    name = "fixedinterval"
+    is_suitable_for_save_at = False
+    is_suitable_for_save_every_step = True
+
+
 @dataclasses.dataclass(frozen=True)
 class _Solver:
     strategy: Any
@@ -297,6 +313,14 @@ class error_state_std:
             raise NotImplementedError("only the default error_state_std is native")
 
 
+def _native_strategy(strategy):
+    if strategy.name == "fixedinterval":
+        if not getattr(strategy, "_on_grid", False):
+            raise NotImplementedError("strategy_smoother_fixedinterval is native with ivpsolve.solve_fixed_grid only")
+        return "fixedpoint"
+    return strategy.name
+
+
 def _field_dim(field, y0):
     d = _FIELD_DIMS[field.name]
     return y0.shape[-1] if d is None else d
@@ -320,7 +344,7 @@ def lower(solver_obj, error, control, *, num_derivatives, y0, precision, atol, r
     kw["error"] = "state_std" if isinstance(error, error_state_std) else "residual_std"
     return ensemble.make_config(
         field=c.field.name, num_derivatives=num_derivatives, ode_dim=_field_dim(c.field, y0), ssm=c.ssm,
-        constraint=c.kind, strategy=solver_obj.strategy.name, solver=solver_obj.kind, precision=precision,
+        constraint=c.kind, strategy=_native_strategy(solver_obj.strategy), solver=solver_obj.kind, precision=precision,
         atol=atol, rtol=rtol, clip_dt=clip_dt, eps=eps, damp=damp,
         correct_asymptotic_underconfidence=solver_obj.correct_asymptotic_underconfidence, **kw,
     )

@@ -106,3 +106,49 @@ def test_lml_through_the_api():
     v, g = oracle_lml(thetas[0].numpy(), data, 0.01, num_steps, 10)
     assert abs(float(lml[0]) - v) <= 1e-9 * abs(v)
     assert np.abs(grad[0].cpu().numpy() - g).max() <= 1e-6 * np.linalg.norm(g)
+
+
+@pytest.mark.parametrize("ssm_name", ["isotropic", "dense"])
+def test_fixed_grid_fixedinterval_smoother_and_posterior_samples(ssm_name):
+    """solve_fixed_grid with strategy_smoother_fixedinterval (estimators_and_losses.py:594-717),
+    then posterior samples.
+
+    The reference's solve_fixed_grid hands the last state -- whose backward
+    conditional is the last step's, not the identity that Smoother.finalize
+    assumes (estimators_and_losses.py:455-458) -- to finalize, so its
+    terminal marginal is not the filter's; the smoother's posterior on the
+    grid is what the reference's save-every-step path computes, and equals
+    the fixed-point smoother with a checkpoint at every grid point
+    (test_smoother_fixedinterval_vs_fixedpoint.py).  That is the comparison.
+    """
+    from probdiffeq_gb300 import markov
+
+    y0 = torch.tensor([[20.0, 20.0]], dtype=torch.float64)
+    vf = probdiffeq.ode("lotka_volterra", LV)
+    tcoeffs, _ = probdiffeq.jetexpand_ode_padded_scan(num=3)(vf, (y0,), t=0.0)
+    S_ = probdiffeq.state_space_model_isotropic() if ssm_name == "isotropic" else probdiffeq.state_space_model_dense()
+    iwp = S_.prior_wiener_integrated(tcoeffs)
+    ts0 = S_.constraint_ode_ts0(vf)
+    solver = probdiffeq.solver_mle(strategy=probdiffeq.strategy_smoother_fixedinterval(), constraint=ts0)
+    grid = torch.linspace(0.0, 2.0, 11, dtype=torch.float64)
+    sol = ivpsolve.solve_fixed_grid(solver=solver, precision="float64")(iwp, grid=grid, posterior=True)
+    torch.cuda.synchronize()
+    assert (sol.status == 0).all()
+
+    tc = problems.taylor_derivatives(problems.lotka_volterra, y0[0], LV, 3)
+    So = ssm.IsoSSM() if ssm_name == "isotropic" else ssm.DenseSSM()
+    vfo = lambda u, t: problems.lotka_volterra(u[0], LV)  # noqa: E731
+    c = So.constraint_ode_ts0(vfo) if ssm_name == "isotropic" else So.constraint_ode_ts0(vfo, 2)
+    uo = solvers.solve_fixed_steps_save_at(solvers.SolverMLE(solvers.StrategyFixedPoint(), c),
+                                           So.prior_wiener_integrated(tc), 0.0, 0.2, 10, 1)[0]
+    for s, o in enumerate(uo):
+        mo, Co = o.to_multivariate_normal()
+        m = sol.u.mean_flat[0, s].cpu().reshape(-1)
+        L = sol.u.cholesky_flat[0, s].cpu()
+        C = L @ L.T
+        if ssm_name == "isotropic":
+            C = torch.kron(C, torch.eye(2, dtype=torch.float64))
+        assert float((m - mo).abs().max() / mo.abs().max()) < 1e-9
+        assert float((C - Co).abs().max() / Co.abs().max().clamp_min(1e-300)) < 1e-7
+    smp = markov.sample(sol, 7, generator=torch.Generator(device="cuda").manual_seed(3))
+    assert smp.shape[:3] == (1, 7, 11) and torch.isfinite(smp).all()
