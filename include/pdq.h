@@ -103,7 +103,8 @@ typedef struct pdq_config {
   int32_t clip_dt;        /* RejectionLoop clip_dt (solvers_via_adaptive_steps.py:300-301) */
   int32_t correct_asymptotic_underconfidence; /* solver_mle (solvers.py:456-457) */
   int32_t kernel_variant;  /* isotropic mapping: 0 auto, 1 one thread per instance,
-                              2 / 3 eight lanes per instance with <= 128 / <= 85 registers (clip_dt only) */
+                              2 / 3 eight lanes per instance with <= 128 / <= 85 registers (clip_dt only);
+                              dense: 2 eight lanes per instance, otherwise one thread per instance */
   double safety, factor_min, factor_max;           /* controller (defaults 0.95, 0.2, 10) */
   double exponent_integral, exponent_proportional; /* PI controller (0.3, 0.4) */
   double atol, rtol, eps, damp;                    /* solve(...) arguments */

@@ -378,7 +378,8 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.workspace = workspace;
     const bool ts1 = c->constraint == PDQ_CONSTRAINT_TS1;
     const bool f64 = c->precision == PDQ_PRECISION_F64;
-    const int block = 32;
+    // kernel_variant 2: eight lanes per instance (shared-memory state); otherwise one thread per instance
+    const int block = c->kernel_variant == 2 ? 0 : 1;
     cudaError_t err;
     switch (c->field) {
       case PDQ_FIELD_LOTKA_VOLTERRA:

@@ -40,12 +40,12 @@ def oracle_vdp(mu, save_at, strategy="fixedpoint", constraint="ts1", solver="dyn
 
 
 def gpu_dense(field, params, y0, save_at, precision, strategy="fixedpoint", constraint="ts1", solver="dynamic",
-              atol=1e-5, rtol=1e-5, nu=3, posterior=True, clip_dt=False, terminal_only=False):
+              atol=1e-5, rtol=1e-5, nu=3, posterior=True, clip_dt=False, terminal_only=False, variant=0):
     from probdiffeq_gb300 import _native, ensemble
 
     cfg = ensemble.make_config(
         field=field, num_derivatives=nu, ode_dim=2, ssm="dense", constraint=constraint, strategy=strategy,
-        solver=solver, precision=precision, atol=atol, rtol=rtol, clip_dt=clip_dt,
+        solver=solver, precision=precision, atol=atol, rtol=rtol, clip_dt=clip_dt, kernel_variant=variant,
     )
     params = torch.as_tensor(params, dtype=torch.float64)
     y0 = torch.as_tensor(y0, dtype=torch.float64)
@@ -95,13 +95,18 @@ def f32_tol(o64, o32):
 TOL64 = dict(u=1e-8, rows=1e-5, cov=1e-5)
 
 
+VARIANTS = {"thread": 1, "lanes": 2}
+
+
+@pytest.mark.parametrize("variant", ["thread", "lanes"])
 @pytest.mark.parametrize("precision", ["float64", "float32"])
 @pytest.mark.parametrize("mu", [1.0, 3.0])
-def test_vdp_fixedpoint_ts1_save_at(mu, precision):
-    """Smoothed marginals at the checkpoints, the backward pass included."""
+def test_vdp_fixedpoint_ts1_save_at(mu, precision, variant):
+    """Smoothed marginals at the checkpoints, the backward pass included, for
+    both instance-to-thread mappings."""
     save_at = np.linspace(0.0, 2.0 * mu, 8)
     res = oracle_vdp(mu, save_at)
-    out = gpu_dense("van_der_pol", [[mu]], [[2.0, 0.0]], save_at, precision)
+    out = gpu_dense("van_der_pol", [[mu]], [[2.0, 0.0]], save_at, precision, variant=VARIANTS[variant])
     assert int(out["status"][0]) == 0
     if precision == "float32":
         r32 = oracle_vdp(mu, save_at, dtype=torch.float32)
@@ -125,11 +130,13 @@ def test_vdp_fixedpoint_ts1_save_at(mu, precision):
             assert rel(out["filter_mean"][0, s], f.mean) < 1e-6
 
 
-def test_vdp_filter_ts0_and_mle():
+@pytest.mark.parametrize("variant", ["thread", "lanes"])
+def test_vdp_filter_ts0_and_mle(variant):
     """Dense TS0 with the filter and MLE calibration, float64."""
     save_at = np.linspace(0.0, 2.0, 5)
     res = oracle_vdp(1.0, save_at, strategy="filter", constraint="ts0", solver="mle")
-    out = gpu_dense("van_der_pol", [[1.0]], [[2.0, 0.0]], save_at, "float64", strategy="filter", constraint="ts0", solver="mle")
+    out = gpu_dense("van_der_pol", [[1.0]], [[2.0, 0.0]], save_at, "float64", strategy="filter", constraint="ts0", solver="mle",
+                    variant=VARIANTS[variant])
     assert int(out["status"][0]) == 0
     for s in range(len(save_at)):
         check(out["u_mean"][0, s], out["u_chol"][0, s], res.u[s], TOL64)
@@ -156,15 +163,18 @@ def test_dense_equals_isotropic_on_lotka_volterra():
     assert rel(Ld @ Ld.T, Ci) < 1e-7
 
 
-def test_dense_batch_and_workspace_errors():
-    """Several instances in one launch; too small a workspace is rejected before launch."""
+@pytest.mark.parametrize("variant", ["thread", "lanes"])
+def test_dense_batch_and_workspace_errors(variant):
+    """Several instances in one launch (five: a partly filled block for the
+    lane mapping); too small a workspace is rejected before launch."""
     import ctypes
 
     from probdiffeq_gb300 import _native, ensemble
 
-    mus = [1.0, 1.5, 2.0]
+    mus = [1.0, 1.5, 2.0, 1.25, 1.75]
     save_at = np.linspace(0.0, 2.0, 4)
-    out = gpu_dense("van_der_pol", [[m] for m in mus], [[2.0, 0.0]] * 3, save_at, "float64", posterior=False)
+    out = gpu_dense("van_der_pol", [[m] for m in mus], [[2.0, 0.0]] * len(mus), save_at, "float64", posterior=False,
+                    variant=VARIANTS[variant])
     for b, mu in enumerate(mus):
         res = oracle_vdp(mu, np.linspace(0.0, 2.0, 4))
         check(out["u_mean"][b, -1], out["u_chol"][b, -1], res.u[-1], TOL64)
