@@ -61,7 +61,10 @@ enum { PDQ_SSM_ISOTROPIC = 0, PDQ_SSM_BLOCKDIAG = 1, PDQ_SSM_DENSE = 2 };
 /* Linearisation: constraint_ode_ts0 / constraint_ode_ts1 (ssm_impl_api.py:520-558). */
 enum { PDQ_CONSTRAINT_TS0 = 0, PDQ_CONSTRAINT_TS1 = 1 };
 /* strategy_filter / strategy_smoother_fixedpoint (estimators_and_losses.py:347-591). */
-enum { PDQ_STRATEGY_FILTER = 0, PDQ_STRATEGY_FIXEDPOINT = 1 };
+enum { PDQ_STRATEGY_FILTER = 0, PDQ_STRATEGY_FIXEDPOINT = 1,
+       PDQ_STRATEGY_FIXEDINTERVAL = 2 /* pdq_offgrid_marginals only: a solve on a grid lowers the
+                                          fixed-interval smoother to FIXEDPOINT with every grid point
+                                          a checkpoint */ };
 /* solver / solver_mle / solver_dynamic (solvers.py:318-767). */
 enum { PDQ_SOLVER_PLAIN = 0, PDQ_SOLVER_MLE = 1, PDQ_SOLVER_DYNAMIC = 2 };
 /* error_residual_std (solvers.py:850-996) / error_state_std (solvers.py:999-1098, derivative_idx 0). */
@@ -252,6 +255,44 @@ typedef struct pdq_sample_args {
 
 #if !defined(__CUDACC_RTC__)
 pdq_status pdq_sample_markov(const pdq_sample_args* args, void* stream);
+#endif
+
+/* Marginals at off-grid times of a solution on a grid: solver.offgrid_marginals
+ * (probdiffeq/_probdiffeq/solvers.py:149-203).  For each query t the
+ * interval comes from searchsorted(t_grid, t) = index; the transitions from
+ * t_grid[index-1] to t and from t to t_grid[index] use output_scale[index].
+ *   PDQ_STRATEGY_FILTER: the marginal at index-1 predicted to t
+ *     (estimators_and_losses.py:403-414);
+ *   PDQ_STRATEGY_FIXEDINTERVAL: the filtering marginal at index-1 reverted
+ *     to t, that reverted to t_grid[index], and the smoothed marginal at
+ *     index marginalised through the resulting backward conditional
+ *     (estimators_and_losses.py:674-709).
+ * PDQ_STRATEGY_FIXEDPOINT returns PDQ_ERROR_UNSUPPORTED (the reference raises
+ * NotImplementedError).  A query on a grid point returns that point's
+ * marginal; one outside [t_grid[0], t_grid[S-1]] (or NaN) returns NaN.
+ * Float64; isotropic (nu 1..5, d <= 64) and dense (nu 2..3, d = 2).  Device
+ * pointers; one thread per (instance, query). */
+typedef struct pdq_offgrid_args {
+  int32_t ssm;              /* PDQ_SSM_ISOTROPIC or PDQ_SSM_DENSE */
+  int32_t strategy;         /* PDQ_STRATEGY_FILTER or PDQ_STRATEGY_FIXEDINTERVAL */
+  int32_t num_derivatives;  /* nu; n = nu + 1 */
+  int32_t ode_dim;          /* d; dense N = n * d */
+  int64_t num_instances;    /* B */
+  int32_t num_points;       /* S grid points per instance (t0 included) */
+  int32_t num_queries;      /* Q query times per instance */
+  const double* t;             /* (B, S) the grid, increasing */
+  const double* u_mean;        /* iso (B, S, n, d) | dense (B, S, N): marginals at the grid points */
+  const double* u_chol;        /* iso (B, S, n, n) | dense (B, S, N, N) */
+  const double* filter_mean;   /* FIXEDINTERVAL: filtering marginals at the grid points, shapes as u_* */
+  const double* filter_chol;
+  const double* output_scale;  /* (B, S) */
+  const double* t_query;       /* (B, Q) */
+  double* mean_out;            /* iso (B, Q, n, d) | dense (B, Q, N) */
+  double* chol_out;            /* iso (B, Q, n, n) | dense (B, Q, N, N) */
+} pdq_offgrid_args;
+
+#if !defined(__CUDACC_RTC__)
+pdq_status pdq_offgrid_marginals(const pdq_offgrid_args* args, void* stream);
 #endif
 
 /* Register a vector field given as CUDA C++ source, compiled at run time

@@ -568,6 +568,26 @@ def solve_fixed_steps_save_at(solver, prior, t0, dt, num_steps, save_every, damp
     return u, posterior
 
 
+def solve_grid_save_every_point(solver, prior, grid, damp=0.0):
+    """``solve_adaptive_save_at`` with the grid as checkpoints when every step is
+    accepted and lands exactly on the next grid point (the ``interp_at_t1``
+    branch at each point, solvers_via_adaptive_steps.py:362-375): the filter's
+    and the fixed-point smoother's solution at every grid point.  With the
+    fixed-point smoother this is the fixed-interval smoother's posterior on
+    the grid (test_smoother_fixedinterval_vs_fixedpoint.py:50-86)."""
+    grid = [float(g) for g in grid]
+    state0 = solver.init(grid[0], prior, damp)
+    s, prev = state0, state0
+    saved = []
+    for a, b in zip(grid[:-1], grid[1:]):
+        s = solver.step(s, b - a, damp)
+        s = dataclasses.replace(s, t=b)
+        sol, (s, prev) = solver.interpolate_fwd_at_t1(b, prev, s)
+        saved.append(sol)
+    u, posterior, scales = solver.userfriendly_output(state0, saved, s)
+    return AdaptiveResult(grid, u, posterior, scales, [x.num_steps for x in saved], len(saved), len(saved))
+
+
 # --------------------------------------------------------------------------
 # Log-marginal likelihood (estimators_and_losses.py:20-105, 180-218)
 # --------------------------------------------------------------------------
@@ -616,6 +636,36 @@ def loss_lml_terminal_values(u, marginal, std, tcoeff_index=0):
     marg = model.marginalise(marginal)
     data = u.reshape(1, -1) if marginal.kind == "isotropic" else u
     return marg.logpdf(data)
+
+
+def offgrid_marginals(solver, t, result, prior):
+    """solver.offgrid_marginals(t, solution=...) (solvers.py:149-203).
+
+    ``result`` is a save-every-step or fixed-grid solution.  The query t must
+    lie strictly inside (t0, t1) and off the grid (the reference does not
+    check either).  index = searchsorted(ts, t); the strategies'
+    interpolate_offgrid_marginals: the filter predicts from the marginal at
+    ts[index-1] (estimators_and_losses.py:403-414); the fixed-interval smoother
+    reverts the filtering marginal at ts[index-1] to t and t to ts[index], and
+    marginalises the smoothed marginal at ts[index] through the second
+    backward conditional (:674-709).  The transitions use
+    output_scale[index] (JAX clamps the index for the MLE solver's shorter
+    scale array; its entries are all equal).
+    """
+    if solver.strategy.name == "fixedpoint":
+        raise NotImplementedError
+    ts = torch.tensor([float(s) for s in result.t], dtype=torch.float64)
+    index = int(torch.searchsorted(ts, torch.tensor(float(t), dtype=torch.float64)))
+    t0, t1 = float(ts[index - 1]), float(ts[index])
+    scale = result.output_scale[min(index, len(result.output_scale) - 1)]
+    transition_t0_t = prior.transition(t - t0, scale)
+    transition_t_t1 = prior.transition(t1 - t, scale)
+    if solver.strategy.name == "filter":
+        return transition_t0_t.marginalise(result.posterior[index - 1])
+    filtering = result.posterior["filtering"][index - 1]
+    extrapolated_t, _ = transition_t0_t.revert(filtering, solve_triu=linalg.solve_triu)
+    _, conditional_t1_to_t = transition_t_t1.revert(extrapolated_t, solve_triu=linalg.solve_triu)
+    return conditional_t1_to_t.marginalise(result.u[index])
 
 
 def solve_adaptive_save_every_step(solver, error, prior, t0, t1, atol, rtol, control=None, clip_dt=False, dt0=0.1, eps=1e-8, damp=0.0):

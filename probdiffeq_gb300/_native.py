@@ -101,6 +101,27 @@ class PdqSampleArgs(ctypes.Structure):
     ]
 
 
+class PdqOffgridArgs(ctypes.Structure):
+    _fields_ = [
+        ("ssm", ctypes.c_int32),
+        ("strategy", ctypes.c_int32),
+        ("num_derivatives", ctypes.c_int32),
+        ("ode_dim", ctypes.c_int32),
+        ("num_instances", ctypes.c_int64),
+        ("num_points", ctypes.c_int32),
+        ("num_queries", ctypes.c_int32),
+        ("t", ctypes.c_void_p),
+        ("u_mean", ctypes.c_void_p),
+        ("u_chol", ctypes.c_void_p),
+        ("filter_mean", ctypes.c_void_p),
+        ("filter_chol", ctypes.c_void_p),
+        ("output_scale", ctypes.c_void_p),
+        ("t_query", ctypes.c_void_p),
+        ("mean_out", ctypes.c_void_p),
+        ("chol_out", ctypes.c_void_p),
+    ]
+
+
 class PdqLmlArgs(ctypes.Structure):
     _fields_ = [
         ("num_instances", ctypes.c_int64),
@@ -149,6 +170,7 @@ SIGNATURES = {
         [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlArgs), ctypes.c_void_p],
     ),
     "pdq_sample_markov": (ctypes.c_int, [ctypes.POINTER(PdqSampleArgs), ctypes.c_void_p]),
+    "pdq_offgrid_marginals": (ctypes.c_int, [ctypes.POINTER(PdqOffgridArgs), ctypes.c_void_p]),
     "pdq_register_field": (
         ctypes.c_int,
         [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
@@ -366,9 +388,48 @@ def sample_markov(ssm, num_derivatives, ode_dim, marginal_mean, marginal_chol, p
     a = PdqSampleArgs()
     a.ssm, a.num_derivatives, a.ode_dim, a.num_points = SSM[ssm], num_derivatives, ode_dim, S
     a.num_instances, a.num_samples = B, K
-    a.marginal_mean, a.marginal_chol = _ptr(marginal_mean.contiguous()), _ptr(marginal_chol.contiguous())
+    # keep the contiguous copies alive until the launch is enqueued
+    marginal_mean, marginal_chol = marginal_mean.contiguous(), marginal_chol.contiguous()
+    a.marginal_mean, a.marginal_chol = _ptr(marginal_mean), _ptr(marginal_chol)
     for k in ("cond_A", "cond_noise_mean", "cond_noise_chol", "cond_to_latent", "cond_to_observed"):
         setattr(a, k, _ptr(posterior[k]) if posterior is not None else None)
     a.normals, a.samples = _ptr(normals), _ptr(samples)
     check(load().pdq_sample_markov(ctypes.byref(a), _stream_handle(stream)), "pdq_sample_markov")
     return samples
+
+
+OFFGRID_STRATEGY = {"filter": 0, "fixedinterval": 2}
+
+
+def offgrid_marginals(ssm, strategy, num_derivatives, ode_dim, t, u_mean, u_chol, output_scale, t_query,
+                      filter_mean=None, filter_chol=None, stream=None):
+    """Call pdq_offgrid_marginals on device float64 tensors; returns (mean, chol) at the queries.
+
+    t, output_scale: (B, S); u_*, filter_*: the grid marginals (B, S, ...);
+    t_query: (B, Q).  ``strategy``: "filter" or "fixedinterval" (which needs
+    the filtering marginals).
+    """
+    if strategy not in OFFGRID_STRATEGY:
+        raise NotImplementedError(f"off-grid marginals are not defined for the {strategy} strategy")
+    f64 = lambda x: None if x is None else x.to(torch.float64).contiguous()
+    t, u_mean, u_chol, output_scale, t_query = map(f64, (t, u_mean, u_chol, output_scale, t_query))
+    filter_mean, filter_chol = f64(filter_mean), f64(filter_chol)
+    B, S = t.shape
+    Q = t_query.shape[1]
+    n = num_derivatives + 1
+    if ssm == "isotropic":
+        mshape, cshape = (B, Q, n, ode_dim), (B, Q, n, n)
+    else:
+        N = n * ode_dim
+        mshape, cshape = (B, Q, N), (B, Q, N, N)
+    mean = torch.empty(mshape, dtype=torch.float64, device=t.device)
+    chol = torch.empty(cshape, dtype=torch.float64, device=t.device)
+    a = PdqOffgridArgs()
+    a.ssm, a.strategy, a.num_derivatives, a.ode_dim = SSM[ssm], OFFGRID_STRATEGY[strategy], num_derivatives, ode_dim
+    a.num_instances, a.num_points, a.num_queries = B, S, Q
+    a.t, a.u_mean, a.u_chol, a.output_scale, a.t_query = map(_ptr, (t, u_mean, u_chol, output_scale, t_query))
+    a.filter_mean = _ptr(filter_mean) if filter_mean is not None else None
+    a.filter_chol = _ptr(filter_chol) if filter_chol is not None else None
+    a.mean_out, a.chol_out = _ptr(mean), _ptr(chol)
+    check(load().pdq_offgrid_marginals(ctypes.byref(a), _stream_handle(stream)), "pdq_offgrid_marginals")
+    return mean, chol

@@ -5,6 +5,7 @@
 
 #include "bd_launch.cuh"
 #include "dense_launch.cuh"
+#include "offgrid.h"
 #include "lml_launch.cuh"
 #include "iso_launch.cuh"
 #include "nvrtc_fields.h"
@@ -476,3 +477,26 @@ pdq_status pdq_lml_fixed_grid(const pdq_config* c, const pdq_lml_args* args, voi
 }
 
 }  // extern "C"
+
+extern "C" pdq_status pdq_offgrid_marginals(const pdq_offgrid_args* args, void* stream) {
+  if (args == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  const pdq_offgrid_args& a = *args;
+  if (a.num_instances < 0 || a.num_points < 1 || a.num_queries < 0 || a.ode_dim < 1) return PDQ_ERROR_INVALID_VALUE;
+  if (a.strategy == PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_UNSUPPORTED;
+  if (a.strategy != PDQ_STRATEGY_FILTER && a.strategy != PDQ_STRATEGY_FIXEDINTERVAL) return PDQ_ERROR_INVALID_VALUE;
+  if (a.ssm == PDQ_SSM_ISOTROPIC) {
+    if (a.num_derivatives < 1 || a.num_derivatives > 5 || a.ode_dim > 64) return PDQ_ERROR_UNSUPPORTED;
+  } else if (a.ssm == PDQ_SSM_DENSE) {
+    if (a.num_derivatives < 2 || a.num_derivatives > 3 || a.ode_dim != 2) return PDQ_ERROR_UNSUPPORTED;
+  } else {
+    return PDQ_ERROR_UNSUPPORTED;
+  }
+  if (a.num_instances * int64_t(a.num_queries) == 0) return PDQ_SUCCESS;
+  if (!a.t || !a.u_mean || !a.u_chol || !a.output_scale || !a.t_query || !a.mean_out || !a.chol_out ||
+      (a.strategy == PDQ_STRATEGY_FIXEDINTERVAL && (!a.filter_mean || !a.filter_chol)))
+    return PDQ_ERROR_INVALID_VALUE;
+  double q1[pdq::kMaxN][pdq::kMaxN];
+  iwp_q1(a.num_derivatives, q1);
+  const cudaError_t e = pdq_launch_offgrid(a, q1, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+}

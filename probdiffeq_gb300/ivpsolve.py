@@ -170,7 +170,9 @@ def solve_fixed_grid(*, solver, precision="float32", device="cuda"):
         strategy._on_grid = True
         solver = dataclasses.replace(solver, strategy=strategy)
 
-    def solve(u, /, *, grid, damp=0.0, posterior=False, stream=None):
+    def solve(u, /, *, grid, damp=0.0, posterior=None, stream=None):
+        # the fixed-interval smoother keeps its posterior (off-grid marginals need the filtering marginals)
+        posterior = solver.strategy.name == "fixedinterval" if posterior is None else posterior
         grid = torch.as_tensor(grid, dtype=torch.float64)
         span = float((grid[..., -1] - grid[..., 0]).abs().max())
         # eps far above the rounding of t, far below any grid spacing

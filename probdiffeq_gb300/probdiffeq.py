@@ -203,6 +203,7 @@ class strategy_filter:
     name = "filter"
     is_suitable_for_save_at = True
     is_suitable_for_save_every_step = True
+    is_suitable_for_offgrid_marginals = True
 
 
 class strategy_smoother_fixedpoint:
@@ -211,6 +212,7 @@ class strategy_smoother_fixedpoint:
     name = "fixedpoint"
     is_suitable_for_save_at = True
     is_suitable_for_save_every_step = False
+    is_suitable_for_offgrid_marginals = False
 
 
 class strategy_smoother_fixedinterval:
@@ -226,6 +228,7 @@ class strategy_smoother_fixedinterval:
     name = "fixedinterval"
     is_suitable_for_save_at = False
     is_suitable_for_save_every_step = True
+    is_suitable_for_offgrid_marginals = True
 
 
 @dataclasses.dataclass(frozen=True)
@@ -242,6 +245,52 @@ class _Solver:
     @property
     def is_suitable_for_save_every_step(self):
         return self.strategy.is_suitable_for_save_every_step
+
+    @property
+    def is_suitable_for_offgrid_marginals(self):
+        return self.strategy.is_suitable_for_offgrid_marginals
+
+    def offgrid_marginals(self, t, *, solution, stream=None):
+        """Marginals at times off the solution's grid (solvers.py:149-203), on the GPU.
+
+        ``solution`` is a filter or fixed-interval-smoother solution on a grid
+        (``ivpsolve.solve_fixed_grid``; the smoother's solve keeps the
+        filtering marginals this needs).  ``t``: a scalar, a (Q,) vector
+        shared by the instances, or (B, Q).  Each query interval is
+        searchsorted(grid, t) = index, with the transitions at
+        output_scale[index]; t must lie strictly inside the grid's span and
+        off the grid points (the reference checks neither; here a grid point
+        returns its marginal and a time outside the span NaN).  Returns an
+        ``ivpsolve.Normal`` with a query axis after the batch axis (none for a
+        scalar ``t``).
+        """
+        import torch
+
+        from . import _native
+        from .ivpsolve import Normal
+
+        if not self.is_suitable_for_offgrid_marginals:
+            raise NotImplementedError
+        ssm = self.constraint.ssm
+        if ssm == "blockdiag":
+            raise NotImplementedError("off-grid marginals are native for the isotropic and dense factorisations")
+        post = solution.posterior or {}
+        if self.strategy.name == "fixedinterval" and "filter_mean" not in post:
+            raise ValueError("off-grid marginals of a smoother need its filtering marginals: "
+                             "solve with posterior=True")
+        grid = solution.t if solution.t.ndim == 2 else solution.t[None]
+        B = grid.shape[0]
+        tq = torch.as_tensor(t, dtype=torch.float64, device=grid.device)
+        scalar = tq.ndim == 0
+        tq = tq.reshape(1, -1).expand(B, -1) if tq.ndim <= 1 else tq
+        d = solution.ode_dim
+        n = solution.u.mean_flat.shape[-2] if ssm == "isotropic" else solution.u.mean_flat.shape[-1] // d
+        mean, chol = _native.offgrid_marginals(
+            ssm, self.strategy.name, n - 1, d, grid, solution.u.mean_flat, solution.u.cholesky_flat,
+            solution.output_scale, tq, post.get("filter_mean"), post.get("filter_chol"), stream=stream)
+        if scalar:
+            mean, chol = mean[:, 0], chol[:, 0]
+        return Normal(mean, chol, ssm)
 
 
 def solver(*, strategy, constraint, constraint_init=None):

@@ -92,3 +92,22 @@ def test_missing_buffers_are_rejected(lib):
     assert lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), None, 0, None) == 1
     args.num_save_at = 1
     assert lib.pdq_solve_adaptive(ctypes.byref(cfg), ctypes.byref(args), None, 0, None) == 1
+
+
+def test_offgrid_arguments_are_checked_before_launch(lib):
+    """pdq_offgrid_marginals: the fixed-point smoother is unsupported (the
+    reference raises NotImplementedError, solvers.py:163-164); missing
+    buffers are rejected; an empty query set launches nothing."""
+    from probdiffeq_gb300 import _native
+
+    a = _native.PdqOffgridArgs()
+    a.ssm, a.strategy, a.num_derivatives, a.ode_dim = 0, 1, 2, 2
+    a.num_instances, a.num_points, a.num_queries = 2, 5, 3
+    assert lib.pdq_offgrid_marginals(None, None) == 1
+    assert lib.pdq_offgrid_marginals(ctypes.byref(a), None) == 2  # fixed-point: unsupported
+    a.strategy = 2
+    assert lib.pdq_offgrid_marginals(ctypes.byref(a), None) == 1  # buffers missing
+    a.ssm = 1
+    assert lib.pdq_offgrid_marginals(ctypes.byref(a), None) == 2  # block-diagonal: not native
+    a.ssm, a.num_queries = 2, 0
+    assert lib.pdq_offgrid_marginals(ctypes.byref(a), None) == 0
