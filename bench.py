@@ -193,6 +193,30 @@ def cpu_baseline(seconds_budget=15.0):
     }
 
 
+def timed_pipeline(torch, pipe, submit, K, W, world=1, dist=None):
+    """W untimed batches, then K batches enqueued back to back on the
+    pipeline's streams; one CUDA-event pair from the first upload to the
+    last download; returns seconds."""
+    for k in range(W):
+        submit(k)
+    pipe.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(pipe.streams["upload"])
+    for k in range(K):
+        submit(W + k)
+    e1.record(pipe.streams["download"])
+    e1.synchronize()
+    pipe.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    return e0.elapsed_time(e1) / 1e3
+
+
 def timed_region(torch, stream, fn, K, W, flush=None, world=1, dist=None):
     """W untimed calls, then K calls each bracketed by CUDA events; returns seconds."""
     for _ in range(W):
@@ -294,7 +318,7 @@ def run_lv_ensemble(args):
     import torch
     import torch.distributed as dist
 
-    from probdiffeq_gb300 import _native, ensemble, replicas
+    from probdiffeq_gb300 import _native, ensemble, pipeline, replicas
     from probdiffeq_gb300 import build as native_build
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -364,22 +388,24 @@ def run_lv_ensemble(args):
         attempts64 = outs["num_attempts"].to(torch.float64).sum().item()
         rel_f32_f64 = ((mean32[:, 0] - mean64[:, 0]).abs() / mean64[:, 0].abs()).max().item()
 
-        # ---- e2e through the public API, pinned host buffers, copies inside ----
+        # ---- e2e through the public API: pinned host inputs -> solve -> pinned host outputs every step,
+        # uploads / solves / downloads of consecutive batches overlapped on three streams ----
         h_params, h_y0 = params.pin_memory(), y0.pin_memory()
         h_save = save_at.expand(B, 2).contiguous().pin_memory()
         h_dt0 = torch.full((B,), WORKLOAD["dt0"], dtype=torch.float64).pin_memory()
-        h_out = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in outs.items()}
+        pipe = pipeline.EnsemblePipeline(cfg, B, 2, params.shape[1], terminal_only=True, device=device, depth=2,
+                                         graph=not args.no_graph)
+        h_outs = [pipe.alloc_host_outputs() for _ in range(2)]
         h2d = sum(t.numel() * t.element_size() for t in (h_params, h_y0, h_save, h_dt0))
-        d2h = sum(t.numel() * t.element_size() for t in h_out.values())
+        d2h = sum(t.numel() * t.element_size() for t in h_outs[0].values())
 
-        def e2e_step():
-            o = ensemble.solve_ensemble(cfg, params=h_params, y0=h_y0, save_at=h_save, dt0=h_dt0, terminal_only=True,
-                                        device=device, stream=stream)
-            for k, v in o.items():
-                if not k.startswith("_"):
-                    h_out[k].copy_(v, non_blocking=True)
+        def e2e_submit(k):
+            with torch.cuda.stream(pipe.streams["upload"]):
+                flush.fill_(1.0)  # evict L2 before this batch's upload
+            pipe.submit(h_params, h_y0, h_save, h_dt0, h_outs[k % 2])
 
-        t_e2e = timed_region(torch, stream, e2e_step, args.steps, args.warmup, flush, world, dist)
+        t_e2e = timed_pipeline(torch, pipe, e2e_submit, args.steps, args.warmup, world, dist)
+        e2e_ok = all(bool((h["status"] == 0).all()) for h in h_outs) and torch.equal(h_outs[0]["u_mean"][:, 0], mean32.cpu())
 
         # ---- secondary: the plain per-instance method and LML gradients ----
         secondary = None
@@ -423,6 +449,10 @@ def run_lv_ensemble(args):
             "unit": UNIT,
             "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h,
+            "path": "probdiffeq_gb300.pipeline.EnsemblePipeline: 2 slots, upload / compute / download streams"
+                    + ("" if args.no_graph else ", solver launch replayed from a CUDA graph"),
+            "l2": "flushed (256 MiB write) on the upload stream before each batch's upload",
+            "outputs_match_device_run": e2e_ok,
         },
         "gpu_launches": args.steps,
         "autotune": {
@@ -652,6 +682,7 @@ def main():
     ap.add_argument("--variant", default="auto", choices=["auto", "thread", "lanes", "lanes_compact"],
                     help="lv_ensemble: instance-to-lane mapping (auto = time all three and keep the fastest)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="e2e: launch the solver eagerly instead of from CUDA graphs")
     ap.add_argument("--no-secondary", action="store_true", help="skip the single-instance and LML measurements")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="ensemble size (16384 is the headline workload)")

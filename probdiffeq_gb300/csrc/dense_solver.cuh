@@ -30,6 +30,7 @@ namespace pdq {
 struct DenseArgs {
   int64_t B;
   int32_t S, terminal_only, solver, control, clip_dt, correct, fixedpoint;
+  int32_t state_error;  // 0: error_residual_std; 1: error_state_std (derivative 0)
   double safety, factor_min, factor_max, exp_i, exp_p;
   double atol, rtol, eps, damp;
   int64_t max_attempts;
@@ -539,14 +540,47 @@ __global__ void __launch_bounds__(32) dense_adaptive_kernel(DenseArgs a) {
 #pragma unroll
             for (int j = 0; j < N; ++j) xnew.L[i][j] = (j <= i) ? M2[D + j][D + i] : T(0);
           }
-          // error_residual_std: std of the rescaled observed = sigma * row norms of Lo
+          // error_residual_std: std of the rescaled observed = sigma * row norms of Lo, times dt;
+          // error_state_std (solvers.py:999-1098): sigma * the posterior std of coefficient 0 of the
+          // unit-scale extrapolation conditioned on the linearisation, times dt^0 / 0!
+          T std_state[D];
+          if (a.state_error) {
+            T M3[D + N][D + N];
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+#pragma unroll
+              for (int j = 0; j < D + N; ++j) M3[i][j] = (i == j) ? damp : T(0);
+#pragma unroll
+            for (int rr = 0; rr < N; ++rr) {
+#pragma unroll
+              for (int aa = 0; aa < D; ++aa) {  // (J Lu)^T
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+                  if (k % D == rr % D && rr / D <= k / D) acc += fx.J[aa][k] * dev_abs(p[k]) * sqh * T(a.q1[k / D][rr / D]);
+                M3[D + rr][aa] = acc;
+              }
+#pragma unroll
+              for (int c = 0; c < N; ++c)
+                M3[D + rr][D + c] = (c % D == rr % D && rr / D <= c / D)
+                                        ? dev_abs(p[c]) * sqh * T(a.q1[c / D][rr / D]) : T(0);  // Lu^T
+            }
+            householder_r<T, D + N, D + N>(M3);
+#pragma unroll
+            for (int j = 0; j < D; ++j) {
+              T rn = T(0);
+#pragma unroll
+              for (int k = 0; k <= j; ++k) rn += M3[D + k][D + j] * M3[D + k][D + j];
+              std_state[j] = dev_sqrt(rn);
+            }
+          }
           double sumsq = 0.0;
 #pragma unroll
           for (int j = 0; j < D; ++j) {
             T rn = T(0);
 #pragma unroll
             for (int k = 0; k <= j; ++k) rn += Mo[k][j] * Mo[k][j];
-            const T err_abs = dev_abs(sigma_loc) * dev_sqrt(rn) * h;
+            const T err_abs = a.state_error ? dev_abs(sigma_loc) * std_state[j] : dev_abs(sigma_loc) * dev_sqrt(rn) * h;
             const T ref = fmax(dev_abs(x.m[j]), dev_abs(xnew.m[j]));
             const T ratio = dev_div(err_abs, T(a.atol) + T(a.rtol) * ref);
             sumsq += double(ratio) * double(ratio);

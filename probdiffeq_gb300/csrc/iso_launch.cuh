@@ -29,15 +29,24 @@ cudaError_t launch_iso_warp_nu(const IsoArgs& a, int minb, cudaStream_t stream) 
   return cudaGetLastError();
 }
 
-template <typename T, int NU, class F, bool FP>
-cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
-  auto kernel = interp ? iso_adaptive_kernel<T, NU, F, true, FP> : iso_adaptive_kernel<T, NU, F, false, FP>;
-  cudaError_t e = interp ? ensure_stack<iso_adaptive_kernel<T, NU, F, true, FP>>()
-                         : ensure_stack<iso_adaptive_kernel<T, NU, F, false, FP>>();
+template <typename T, int NU, class F, bool INTERP, bool FP, bool GEN>
+cudaError_t launch_iso_kernel(const IsoArgs& a, cudaStream_t stream, int block) {
+  cudaError_t e = ensure_stack<iso_adaptive_kernel<T, NU, F, INTERP, FP, GEN>>();
   if (e != cudaSuccess) return e;
   const unsigned grid = unsigned((a.B + block - 1) / block);
-  kernel<<<grid, block, 0, stream>>>(a);
+  iso_adaptive_kernel<T, NU, F, INTERP, FP, GEN><<<grid, block, 0, stream>>>(a);
   return cudaGetLastError();
+}
+
+// The fixed-point smoother and TS1 / error_state_std take the general
+// instantiation; the filter with TS0 and error_residual_std the lean one.
+template <typename T, int NU, class F, bool FP>
+cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
+  if (FP || a.ts1 || a.state_error)
+    return interp ? launch_iso_kernel<T, NU, F, true, FP, true>(a, stream, block)
+                  : launch_iso_kernel<T, NU, F, false, FP, true>(a, stream, block);
+  return interp ? launch_iso_kernel<T, NU, F, true, FP, FP>(a, stream, block)
+                : launch_iso_kernel<T, NU, F, false, FP, FP>(a, stream, block);
 }
 
 template <typename T, class F, bool FP = false>

@@ -274,7 +274,7 @@ PDQ_D void iso_predict(const Q (&q1)[kMaxN][kMaxN], const T (&m)[NU + 1][D], con
 // eliminating it bottom-up fills one subdiagonal entry per row, which one
 // rotation per column 1..OUT removes.  Returns R_Y; gain = R12^T / R_Y and
 // Lnew = R22^T.
-template <typename T, int NU, int OUT>
+template <typename T, int NU, int OUT, bool H0 = true>
 PDQ_D T ts0_update(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (&Lnew)[NU + 1][NU + 1],
                    T h0 = T(0)) {
   constexpr int n = NU + 1;
@@ -285,7 +285,11 @@ PDQ_D T ts0_update(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (
   for (int r = 1; r <= n; ++r) {
     // (H Lp)^T with H = h0 e_0 + e_OUT (TS1) or e_OUT (h0 = 0, TS0); Lp is
     // lower triangular, so the h0 term only reaches row 1
-    M[r][0] = (r == 1) ? Lp[OUT][0] + h0 * Lp[0][0] : Lp[OUT][r - 1];
+    if constexpr (H0) {
+      M[r][0] = (r == 1) ? Lp[OUT][0] + h0 * Lp[0][0] : Lp[OUT][r - 1];
+    } else {
+      M[r][0] = Lp[OUT][r - 1];
+    }
 #pragma unroll
     for (int c = 1; c <= n; ++c) M[r][c] = (c >= r) ? Lp[c - 1][r - 1] : T(0);
   }
@@ -615,7 +619,10 @@ PDQ_D void write_normal_iso(const IsoArgs& a, int64_t rec, const T (&m)[NU + 1][
 // resets to the identity; after the last step the backward pass
 // (Smoother.finalize, MarkovSequence.evaluate_marginals, :156-178, 437-470)
 // marginalises from the terminal state through the stored conditionals.
-template <typename T, int NU, class F, bool INTERP, bool FP = false>
+// GEN: TS1 and error_state_std are available (run-time switches); the
+// instantiation without them serves TS0 with error_residual_std, whose
+// attempt is then free of their branches and of the TS1 term in the update.
+template <typename T, int NU, class F, bool INTERP, bool FP = false, bool GEN = true>
 __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   constexpr int n = NU + 1;
   constexpr int D = F::D;
@@ -739,7 +746,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           // jacobians.py:100-106), same residual mean
           T f[D];
           T h0 = T(0);
-          if (a.ts1) {
+          if (GEN && a.ts1) {
             T Jf[D][D];
             eval_with_jacobian<F>(mp[0], pt, f, Jf);
             T tr = T(0);
@@ -760,7 +767,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           // fx.marginalise(apply_flat(m)) with unit scale: observed std
           // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
           // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
-          const T ell = a.ts1 ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
+          const T ell = (GEN && a.ts1) ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
                               : observed_std(p[OUT], h, q1_out_norm, damp);
           const T sigma_loc = dev_div(rms_mobs, ell);
 
@@ -781,7 +788,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 
           // ---- update (revert_conditional, H = e_OUT) ----
           T gain[n], Lnew[n][n];
-          const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew, h0);
+          const T R_Y = ts0_update<T, NU, OUT, GEN>(Lp, damp, gain, Lnew, h0);
           const T ry_inv = fast_rcp(R_Y);
           T mnew[n][D];
 #pragma unroll
@@ -796,7 +803,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           // unit-scale extrapolation (chol |p| sqrt|h| Q1) on the same
           // linearisation; error = sigma_loc * (posterior std of u), dt^0/0! = 1
           T err_abs;
-          if (a.state_error) {
+          if (GEN && a.state_error) {
             err_abs = sigma_loc * state_std0<T, NU, OUT>(a, p, h, damp, h0);
           } else {
             err_abs = rms_mobs * h;

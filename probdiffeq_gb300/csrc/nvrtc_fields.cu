@@ -40,8 +40,8 @@ struct UserField {
   std::string name, source;
   int dim = 0, params = 0;
   std::mutex mu;
-  // (f64, nu, interp, fixedpoint) -> loaded kernel
-  std::map<std::tuple<int, int, int, int>, cudaKernel_t> kernels;
+  // (f64, nu, interp, fixedpoint, general) -> loaded kernel
+  std::map<std::tuple<int, int, int, int, int>, cudaKernel_t> kernels;
   std::vector<cudaLibrary_t> libraries;
 };
 
@@ -55,9 +55,11 @@ UserField* lookup(int32_t field) {
   return g_fields[size_t(k)].get();
 }
 
-std::string kernel_expression(bool f64, int nu, bool interp, bool fp) {
+// gen: the instantiation with TS1 / error_state_std (as the built-in fields' dispatch)
+std::string kernel_expression(bool f64, int nu, bool interp, bool fp, bool gen) {
   return std::string("pdq::iso_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
-         ", pdq_user::Field, " + (interp ? "true" : "false") + ", " + (fp ? "true" : "false") + ">";
+         ", pdq_user::Field, " + (interp ? "true" : "false") + ", " + (fp ? "true" : "false") + ", " +
+         (gen ? "true" : "false") + ">";
 }
 
 void copy_log(const std::string& text, char* log, size_t log_bytes) {
@@ -120,7 +122,7 @@ extern "C" pdq_status pdq_register_field(const char* name, const char* source, i
   // validate by compiling one variant (no device needed)
   std::string cubin, text;
   std::vector<std::string> lowered;
-  const pdq_status st = compile(source, {kernel_expression(false, 2, false, false)}, &cubin, &lowered, &text);
+  const pdq_status st = compile(source, {kernel_expression(false, 2, false, false, false)}, &cubin, &lowered, &text);
   copy_log(text, log, log_bytes);
   if (st != PDQ_SUCCESS) return st;
   auto f = std::make_unique<UserField>();
@@ -151,14 +153,15 @@ cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, 
   cudaKernel_t kernel = nullptr;
   {
     std::lock_guard<std::mutex> lock(f->mu);
-    const auto key = std::make_tuple(f64 ? 1 : 0, nu, interp ? 1 : 0, fp ? 1 : 0);
+    const bool gen = fp || a.ts1 || a.state_error;
+    const auto key = std::make_tuple(f64 ? 1 : 0, nu, interp ? 1 : 0, fp ? 1 : 0, gen ? 1 : 0);
     auto it = f->kernels.find(key);
     if (it != f->kernels.end()) {
       kernel = it->second;
     } else {
       std::string cubin, text;
       std::vector<std::string> lowered;
-      if (compile(f->source, {kernel_expression(f64, nu, interp, fp)}, &cubin, &lowered, &text) != PDQ_SUCCESS)
+      if (compile(f->source, {kernel_expression(f64, nu, interp, fp, gen)}, &cubin, &lowered, &text) != PDQ_SUCCESS)
         return cudaErrorInvalidSource;
       cudaLibrary_t lib = nullptr;
       cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);

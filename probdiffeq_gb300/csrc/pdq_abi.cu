@@ -323,7 +323,8 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
   }
   if (c->ssm == PDQ_SSM_DENSE) {
-    if (c->error != PDQ_ERROR_RESIDUAL_STD) return PDQ_ERROR_UNSUPPORTED;
+    // error_state_std: the thread-per-instance mapping
+    if (c->error == PDQ_ERROR_STATE_STD && c->kernel_variant == 2) return PDQ_ERROR_UNSUPPORTED;
     if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
     if (c->strategy != PDQ_STRATEGY_FILTER && c->strategy != PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_INVALID_VALUE;
@@ -347,6 +348,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.clip_dt = c->clip_dt ? 1 : 0;
     a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
     a.fixedpoint = fp ? 1 : 0;
+    a.state_error = c->error == PDQ_ERROR_STATE_STD ? 1 : 0;
     a.safety = c->safety;
     a.factor_min = c->factor_min;
     a.factor_max = c->factor_max;

@@ -24,7 +24,8 @@ from oracle import problems, solvers, ssm
 pytestmark = pytest.mark.gpu
 
 
-def oracle_vdp(mu, save_at, strategy="fixedpoint", constraint="ts1", solver="dynamic", atol=1e-5, rtol=1e-5, dtype=torch.float64):
+def oracle_vdp(mu, save_at, strategy="fixedpoint", constraint="ts1", solver="dynamic", atol=1e-5, rtol=1e-5, dtype=torch.float64,
+               error="residual_std"):
     p = torch.tensor([mu], dtype=torch.float64)
     y0 = torch.tensor([2.0, 0.0], dtype=torch.float64)
     tc = problems.taylor_derivatives(problems.van_der_pol, y0, p, 3).to(dtype)
@@ -36,16 +37,19 @@ def oracle_vdp(mu, save_at, strategy="fixedpoint", constraint="ts1", solver="dyn
     c = D.constraint_ode_ts1(vf, jac, 2) if constraint == "ts1" else D.constraint_ode_ts0(vf, 2)
     strat = solvers.StrategyFixedPoint() if strategy == "fixedpoint" else solvers.StrategyFilter()
     cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE, "none": solvers.SolverPlain}[solver]
-    return solvers.solve_adaptive_save_at(cls(strat, c), solvers.ErrorResidualStd(c), prior, save_at, atol, rtol)
+    err = solvers.ErrorStateStd(c) if error == "state_std" else solvers.ErrorResidualStd(c)
+    return solvers.solve_adaptive_save_at(cls(strat, c), err, prior, save_at, atol, rtol)
 
 
 def gpu_dense(field, params, y0, save_at, precision, strategy="fixedpoint", constraint="ts1", solver="dynamic",
-              atol=1e-5, rtol=1e-5, nu=3, posterior=True, clip_dt=False, terminal_only=False, variant=0):
+              atol=1e-5, rtol=1e-5, nu=3, posterior=True, clip_dt=False, terminal_only=False, variant=0,
+              error="residual_std"):
     from probdiffeq_gb300 import _native, ensemble
 
     cfg = ensemble.make_config(
         field=field, num_derivatives=nu, ode_dim=2, ssm="dense", constraint=constraint, strategy=strategy,
         solver=solver, precision=precision, atol=atol, rtol=rtol, clip_dt=clip_dt, kernel_variant=variant,
+        error=error,
     )
     params = torch.as_tensor(params, dtype=torch.float64)
     y0 = torch.as_tensor(y0, dtype=torch.float64)
@@ -140,6 +144,28 @@ def test_vdp_filter_ts0_and_mle(variant):
     assert int(out["status"][0]) == 0
     for s in range(len(save_at)):
         check(out["u_mean"][0, s], out["u_chol"][0, s], res.u[s], TOL64)
+
+
+@pytest.mark.parametrize("solver,strategy", [("dynamic", "fixedpoint"), ("mle", "filter")])
+def test_vdp_error_state_std(solver, strategy):
+    """error_state_std (solvers.py:999-1098) in the dense factorisation: the
+    posterior std of u after conditioning the unit-scale extrapolation on
+    the TS1 linearisation, float64, vs the oracle's ErrorStateStd."""
+    mu = 2.0
+    save_at = np.linspace(0.0, 2.0 * mu, 6)
+    res = oracle_vdp(mu, save_at, strategy=strategy, solver=solver, error="state_std")
+    out = gpu_dense("van_der_pol", [[mu]], [[2.0, 0.0]], save_at, "float64", strategy=strategy, solver=solver,
+                    error="state_std", posterior=False)
+    assert int(out["status"][0]) == 0
+    steps_o = [0] + list(res.num_steps)
+    for s in range(len(save_at)):
+        check(out["u_mean"][0, s], out["u_chol"][0, s], res.u[s], TOL64)
+        assert abs(int(out["num_steps"][0, s]) - steps_o[s]) <= 1
+    # the lane-cooperative mapping does not implement it
+    from probdiffeq_gb300 import _native
+
+    with pytest.raises(_native.NativeError):
+        gpu_dense("van_der_pol", [[mu]], [[2.0, 0.0]], save_at, "float64", error="state_std", variant=2)
 
 
 def test_dense_equals_isotropic_on_lotka_volterra():
