@@ -318,7 +318,7 @@ def run_lv_ensemble(args):
     import torch
     import torch.distributed as dist
 
-    from probdiffeq_gb300 import _native, ensemble, pipeline, replicas
+    from probdiffeq_gb300 import _native, autotune, ensemble, pipeline, replicas
     from probdiffeq_gb300 import build as native_build
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -336,10 +336,11 @@ def run_lv_ensemble(args):
     t0, t1 = WORKLOAD["t_span"]
     save_at = torch.tensor([t0, t1], dtype=torch.float64)
 
-    def config(precision, variant=0):
+    def config(precision, variant=0, ipb=0):
         return ensemble.make_config(
             field="lotka_volterra", num_derivatives=4, ode_dim=2, solver="mle", precision=precision,
             atol=WORKLOAD["atol"], rtol=WORKLOAD["rtol"], clip_dt=True, kernel_variant=variant,
+            instances_per_block=ipb,
         )
 
     stream = torch.cuda.current_stream()
@@ -354,24 +355,24 @@ def run_lv_ensemble(args):
 
     names = {1: "thread per instance", 2: "8 lanes per instance, <=128 regs", 3: "8 lanes per instance, <=85 regs"}
 
+    def label(cand):
+        return f"{names[cand[0]]}, {cand[1] or 'default'} instances per CTA"
+
     clk = ClockSampler(local)
     clk.__enter__()
     try:
-        # ---- autotune the instance-to-lane mapping on this workload ----
+        # ---- the library autotuner picks the mapping and instances per CTA on this batch ----
         def tune(precision):
-            times = {}
-            for v in names:
-                times[v] = 1e3 * timed_region(torch, stream, lambda: device_step(config(precision, v)), 1, 1)
-            return min(times, key=times.get), times
+            return autotune.tune(config(precision), d_save, d_params, d_y0, d_dt0, True, stream=stream)
 
         fixed = {"thread": 1, "lanes": 2, "lanes_compact": 3}.get(args.variant)
         if fixed is None:
             best32, tune32 = tune("float32")
             best64, tune64 = tune("float64")
         else:
-            best32 = best64 = fixed
+            best32 = best64 = (fixed, 0)
             tune32, tune64 = {}, {}
-        cfg, cfg64 = config("float32", best32), config("float64", best64)
+        cfg, cfg64 = config("float32", *best32), config("float64", *best64)
 
         # ---- value: device-resident inputs, FP32 bulk ----
         t_dev = timed_region(torch, stream, lambda: device_step(cfg), args.steps, args.warmup, flush, world, dist)
@@ -456,10 +457,10 @@ def run_lv_ensemble(args):
         },
         "gpu_launches": args.steps,
         "autotune": {
-            "float32": {names[k]: v for k, v in tune32.items()},
-            "float64": {names[k]: v for k, v in tune64.items()},
-            "unit": "ms per ensemble solve (one timed solve after one warm-up)",
-            "chosen": {"float32": names[best32], "float64": names[best64]},
+            "float32": {label(k): v for k, v in tune32.items()},
+            "float64": {label(k): v for k, v in tune64.items()},
+            "unit": "ms per ensemble solve (probdiffeq_gb300.autotune: one timed solve after one warm-up)",
+            "chosen": {"float32": label(best32), "float64": label(best64)},
         },
         "roofline": {
             "bound": "fp32",

@@ -43,7 +43,7 @@ typedef unsigned long size_t;
 extern "C" {
 #endif
 
-#define PDQ_ABI_VERSION 1u
+#define PDQ_ABI_VERSION 2u
 
 typedef enum pdq_status {
   PDQ_SUCCESS = 0,
@@ -112,6 +112,11 @@ typedef struct pdq_config {
   double exponent_integral, exponent_proportional; /* PI controller (0.3, 0.4) */
   double atol, rtol, eps, damp;                    /* solve(...) arguments */
   int64_t max_attempts;   /* bound on step attempts per instance (the reference has none) */
+  int32_t instances_per_block; /* instances per CTA; 0: default.  Isotropic: 32 or 64 (one thread
+                                  each; default 64), 8, 16 or 32 (eight lanes each; default 32);
+                                  dense: 8, 16 or 32 (one thread each; default 32), 1 to 4 (eight
+                                  lanes each; default 4); block-diagonal: 0 */
+  int32_t reserved0;      /* 0 */
 } pdq_config;
 
 typedef struct pdq_adaptive_args {

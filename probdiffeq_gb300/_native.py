@@ -12,7 +12,7 @@ import torch
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libpdq_gb300.so")
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # enums (include/pdq.h)
 SSM = {"isotropic": 0, "blockdiag": 1, "dense": 2}
@@ -23,6 +23,7 @@ ERROR = {"residual_std": 0, "state_std": 1}
 CONTROL = {"integral": 0, "proportional_integral": 1}
 PRECISION = {"float32": 0, "float64": 1}
 FIELD = {"lotka_volterra": 0, "van_der_pol": 1, "fitzhugh_nagumo": 2, "burgers": 3}
+FIELD_USER_BASE = 1000  # PDQ_FIELD_USER_BASE: ids of fields registered at run time
 INSTANCE_STATUS = {0: "ok", 1: "max_steps", 2: "dt_underflow", 3: "nonfinite"}
 
 
@@ -52,6 +53,8 @@ class PdqConfig(ctypes.Structure):
         ("eps", ctypes.c_double),
         ("damp", ctypes.c_double),
         ("max_attempts", ctypes.c_int64),
+        ("instances_per_block", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
     ]
 
 

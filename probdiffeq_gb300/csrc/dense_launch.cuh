@@ -6,19 +6,20 @@
 
 namespace pdq {
 
-// Lane-cooperative kernel: one instance per warp (lanes 0-7), four warps per
-// block, their states in dynamic shared memory.
+// Lane-cooperative kernel: one instance per warp (lanes 0-7), up to four
+// warps per block (instances_per_block), their states in dynamic shared memory.
 template <typename T, int NU, class F, bool TS1, bool FP>
 cudaError_t launch_dense_coop(const DenseArgs& a, cudaStream_t stream) {
   constexpr int N = (NU + 1) * F::D;
-  constexpr int groups = 4;
+  constexpr int max_groups = 4;
+  const int groups = a.instances_per_block > 0 ? a.instances_per_block : max_groups;
   const size_t smem = size_t(groups) * sizeof(CoopState<T, N, F::D>);
   static bool attr_set = false;  // per process; the attribute is per function, device-independent in practice
   cudaError_t e = ensure_stack<dense_coop_kernel<T, NU, F, TS1, FP>>();
   if (e != cudaSuccess) return e;
   if (!attr_set) {
     e = cudaFuncSetAttribute(dense_coop_kernel<T, NU, F, TS1, FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(smem));
+                             int(max_groups * sizeof(CoopState<T, N, F::D>)));
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
@@ -30,7 +31,7 @@ cudaError_t launch_dense_coop(const DenseArgs& a, cudaStream_t stream) {
 template <typename T, int NU, class F, bool TS1, bool FP>
 cudaError_t launch_dense_variant(const DenseArgs& a, cudaStream_t stream, int block) {
   if (block != 1) return launch_dense_coop<T, NU, F, TS1, FP>(a, stream);
-  block = 32;  // one thread per instance
+  block = a.instances_per_block > 0 ? a.instances_per_block : 32;  // one thread per instance
   auto kernel = dense_adaptive_kernel<T, NU, F, TS1, FP>;
   cudaError_t e = ensure_stack<dense_adaptive_kernel<T, NU, F, TS1, FP>>();
   if (e != cudaSuccess) return e;

@@ -13,7 +13,7 @@ constexpr int kIsoLanes = 8;
 // 3 caps it at 85 (more resident warps, a few spills to L1).
 template <typename T, int NU, class F>
 cudaError_t launch_iso_warp_nu(const IsoArgs& a, int minb, cudaStream_t stream) {
-  const int block = 256;
+  const int block = kIsoLanes * (a.instances_per_block > 0 ? a.instances_per_block : 32);
   const int64_t threads = a.B * kIsoLanes;
   const unsigned grid = unsigned((threads + block - 1) / block);
   cudaError_t e;

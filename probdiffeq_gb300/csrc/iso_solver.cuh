@@ -33,6 +33,7 @@ struct IsoArgs {
   int32_t S, terminal_only, solver, control, clip_dt, correct;
   int32_t ts1;  // 0: TS0 (H = e_1); 1: TS1 with the Jacobian trace along d (H = [-tr J_f / d, 1, 0, ...])
   int32_t state_error;  // 0: error_residual_std; 1: error_state_std (derivative 0)
+  int32_t instances_per_block;  // launch shape (read by the launchers only)
   double safety, factor_min, factor_max, exp_i, exp_p;
   double atol, rtol, eps, damp;
   int64_t max_attempts;

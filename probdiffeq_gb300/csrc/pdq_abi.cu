@@ -64,6 +64,11 @@ pdq_status validate_common(const pdq_config* c) {
   if (!(c->eps >= 0) || !(c->damp >= 0)) return PDQ_ERROR_INVALID_VALUE;
   if (!(c->factor_min > 0) || !(c->factor_max >= c->factor_min) || !(c->safety > 0)) return PDQ_ERROR_INVALID_VALUE;
   if (c->max_attempts < 1) return PDQ_ERROR_INVALID_VALUE;
+  if (c->reserved0 != 0) return PDQ_ERROR_INVALID_VALUE;
+  // launch shapes any mapping accepts (each mapping checks its own subset)
+  const int ipb = c->instances_per_block;
+  if (!(ipb == 0 || (ipb >= 1 && ipb <= 4) || ipb == 8 || ipb == 16 || ipb == 32 || ipb == 64))
+    return PDQ_ERROR_INVALID_VALUE;
   return PDQ_SUCCESS;
 }
 
@@ -216,6 +221,10 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     // for exact checkpoint landings only
     const bool warp = c->clip_dt && c->kernel_variant >= 2;
     if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1 || a.state_error || fp)) return PDQ_ERROR_UNSUPPORTED;
+    const int ipb = c->instances_per_block;
+    if (warp ? !(ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32) : !(ipb == 0 || ipb == 32 || ipb == 64))
+      return PDQ_ERROR_INVALID_VALUE;
+    a.instances_per_block = ipb;
     a.workspace = workspace;
     if (fp) {
       a.cond_A = args->cond_A;
@@ -229,7 +238,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
                                           !a.cond_to_observed || !a.filter_mean || !a.filter_chol))
         return PDQ_ERROR_INVALID_VALUE;
     }
-    const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : 64;
+    const int block = warp ? -(c->kernel_variant == 2 ? 2 : 3) : (ipb > 0 ? ipb : 64);
     const bool f64 = c->precision == PDQ_PRECISION_F64;
     cudaError_t err;
     if (c->field >= PDQ_FIELD_USER_BASE) {
@@ -260,6 +269,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
   }
   if (c->ssm == PDQ_SSM_BLOCKDIAG) {
     if (c->field != PDQ_FIELD_BURGERS) return PDQ_ERROR_UNSUPPORTED;
+    if (c->instances_per_block != 0) return PDQ_ERROR_INVALID_VALUE;  // one cluster per instance
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
     if (c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
     if (!c->clip_dt) return PDQ_ERROR_UNSUPPORTED;  // checkpoints by exact landing only
@@ -325,6 +335,11 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
   if (c->ssm == PDQ_SSM_DENSE) {
     // error_state_std: the thread-per-instance mapping
     if (c->error == PDQ_ERROR_STATE_STD && c->kernel_variant == 2) return PDQ_ERROR_UNSUPPORTED;
+    {
+      const int ipb = c->instances_per_block;
+      if (c->kernel_variant == 2 ? !(ipb >= 0 && ipb <= 4) : !(ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32))
+        return PDQ_ERROR_INVALID_VALUE;
+    }
     if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
     if (c->strategy != PDQ_STRATEGY_FILTER && c->strategy != PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_INVALID_VALUE;
@@ -349,6 +364,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
     a.fixedpoint = fp ? 1 : 0;
     a.state_error = c->error == PDQ_ERROR_STATE_STD ? 1 : 0;
+    a.instances_per_block = c->instances_per_block;
     a.safety = c->safety;
     a.factor_min = c->factor_min;
     a.factor_max = c->factor_max;
@@ -413,6 +429,7 @@ static pdq_status lml_check(const pdq_config* c, int64_t B, int32_t num_steps, i
     return PDQ_ERROR_UNSUPPORTED;
   if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
   if (c->field != PDQ_FIELD_FITZHUGH_NAGUMO && c->field != PDQ_FIELD_LOTKA_VOLTERRA) return PDQ_ERROR_UNSUPPORTED;
+  if (c->instances_per_block != 0) return PDQ_ERROR_INVALID_VALUE;
   if (c->field == PDQ_FIELD_LOTKA_VOLTERRA && c->precision != PDQ_PRECISION_F64) return PDQ_ERROR_UNSUPPORTED;
   if (B < 0 || num_steps < 1 || save_every < 1 || num_steps % save_every != 0) return PDQ_ERROR_INVALID_VALUE;
   return PDQ_SUCCESS;

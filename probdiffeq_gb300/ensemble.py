@@ -38,6 +38,7 @@ def make_config(
     max_attempts=DEFAULT_MAX_ATTEMPTS,
     kernel_variant=0,
     error="residual_std",
+    instances_per_block=0,
 ):
     """Build a ``pdq_config`` (include/pdq.h) from keyword arguments."""
     cfg = _native.config_default(ssm, field, num_derivatives, ode_dim)
@@ -54,6 +55,7 @@ def make_config(
     cfg.exponent_integral, cfg.exponent_proportional = float(exponent_integral), float(exponent_proportional)
     cfg.max_attempts = int(max_attempts)
     cfg.kernel_variant = {"auto": 0, "thread": 1, "lanes": 2, "lanes_compact": 3}.get(kernel_variant, kernel_variant)
+    cfg.instances_per_block = int(instances_per_block)
     return cfg
 
 
@@ -64,11 +66,15 @@ def _dev(x, device, B=None, cols=None):
     return t.to(device, non_blocking=True).contiguous()
 
 
-def solve_ensemble(cfg, *, params, y0, save_at, dt0=0.1, terminal_only=True, device="cuda", stream=None, outputs=None):
+def solve_ensemble(cfg, *, params, y0, save_at, dt0=0.1, terminal_only=True, device="cuda", stream=None, outputs=None,
+                   autotune=False):
     """Solve B instances; returns the dict of output device tensors.
 
     params (B, P), y0 (B, d), save_at (S,) shared or (B, S) per instance,
-    dt0 scalar or (B,).  Output layout as in include/pdq.h.
+    dt0 scalar or (B,).  Output layout as in include/pdq.h.  ``autotune``:
+    pick the instance-to-thread mapping and instances per CTA by timing the
+    candidates on this batch (once per configuration and batch-size class;
+    ``probdiffeq_gb300.autotune``).
     """
     y0 = _dev(y0, device)
     B = y0.shape[0]
@@ -86,5 +92,9 @@ def solve_ensemble(cfg, *, params, y0, save_at, dt0=0.1, terminal_only=True, dev
     S = save_at.shape[1]
     if outputs is None:
         outputs = _native.alloc_outputs(cfg, B, S, terminal_only, device)
+    if autotune:
+        from . import autotune as tuner
+
+        cfg = tuner.tuned_config(cfg, save_at, params, y0, dt0, terminal_only, stream=stream)
     _native.solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream=stream)
     return outputs

@@ -71,6 +71,11 @@ def test_malformed_configs_are_rejected_before_launch(lib):
     bad.append(cfg)
     cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2, atol=0.0, rtol=0.0)
     bad.append(cfg)
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2, instances_per_block=48)
+    bad.append(cfg)
+    cfg = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2)
+    cfg.reserved0 = 1
+    bad.append(cfg)
     for cfg in bad:
         ws = ctypes.c_size_t(0)
         st = lib.pdq_workspace_size(ctypes.byref(cfg), 4, 2, ctypes.byref(ws))
