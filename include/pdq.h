@@ -148,6 +148,17 @@ typedef struct pdq_adaptive_args {
   double* cond_to_observed; /* (B, S-1, N) */
   double* filter_mean;      /* (B, S, N) filtering marginals at the checkpoints */
   double* filter_chol;      /* (B, S, N, N) */
+  /* optional forward-mode sensitivities of the mean records (NULL: not
+   * computed; isotropic TS0 filter with error_residual_std, built-in fields):
+   * d u_mean / d params (B, S_out, n, d, P) and d u_mean / d y0
+   * (B, S_out, n, d, d), through the Taylor-mode initialisation and every
+   * accepted step, with the step sizes held constant (the reference stops
+   * gradients through dt).  The covariance of a TS0 solve does not depend on
+   * params or y0 (H = e_1), so u_chol has no sensitivity apart from the MLE
+   * output scale, which is not differentiated here.  The launch runs P + d
+   * threads per instance. */
+  double* u_mean_d_params;
+  double* u_mean_d_y0;
 } pdq_adaptive_args;
 
 typedef struct pdq_lml_args {

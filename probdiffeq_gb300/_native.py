@@ -81,6 +81,8 @@ class PdqAdaptiveArgs(ctypes.Structure):
         ("cond_to_observed", ctypes.c_void_p),
         ("filter_mean", ctypes.c_void_p),
         ("filter_chol", ctypes.c_void_p),
+        ("u_mean_d_params", ctypes.c_void_p),
+        ("u_mean_d_y0", ctypes.c_void_p),
     ]
 
 
@@ -275,7 +277,7 @@ def solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream
     args.dt0 = _ptr(dt0)
     for k in ("u_mean", "u_chol", "output_scale", "t", "num_steps", "num_attempts", "status"):
         setattr(args, k, _ptr(outputs[k]))
-    for k in OPTIONAL_OUTPUTS:
+    for k in OPTIONAL_OUTPUTS + SENSITIVITY_OUTPUTS:
         setattr(args, k, _ptr(outputs.get(k)))
     lib = load()
     ws_bytes = workspace_size(cfg, B, save_at.shape[1])
@@ -292,6 +294,7 @@ def solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream
 
 
 OPTIONAL_OUTPUTS = ("cond_A", "cond_noise_mean", "cond_noise_chol", "cond_to_latent", "cond_to_observed", "filter_mean", "filter_chol")
+SENSITIVITY_OUTPUTS = ("u_mean_d_params", "u_mean_d_y0")
 
 
 def workspace_size(cfg, B, S):
@@ -300,8 +303,10 @@ def workspace_size(cfg, B, S):
     return int(ws.value)
 
 
-def alloc_outputs(cfg, B, S, terminal_only, device, posterior=False):
-    """Output tensors; ``posterior`` adds the dense smoother's conditionals and filtering marginals."""
+def alloc_outputs(cfg, B, S, terminal_only, device, posterior=False, num_params=None):
+    """Output tensors; ``posterior`` adds the smoother's conditionals and filtering
+    marginals; ``num_params`` (isotropic) adds the mean records' sensitivities
+    ``u_mean_d_params`` (B, S_out, n, d, P) and ``u_mean_d_y0`` (B, S_out, n, d, d)."""
     n = cfg.num_derivatives + 1
     d = cfg.ode_dim
     S_out = 1 if terminal_only else S
@@ -335,6 +340,11 @@ def alloc_outputs(cfg, B, S, terminal_only, device, posterior=False):
                 "filter_mean": torch.empty((B, S, n, d), **f64),
                 "filter_chol": torch.empty((B, S, n, n), **f64),
             }
+    if num_params is not None:
+        if cfg.ssm != SSM["isotropic"]:
+            raise NotImplementedError("sensitivities: isotropic factorisation")
+        extra["u_mean_d_params"] = torch.empty((B, S_out, n, d, int(num_params)), **f64)
+        extra["u_mean_d_y0"] = torch.empty((B, S_out, n, d, d), **f64)
     return {
         **extra,
         "u_mean": torch.empty(mean_shape, **f64),

@@ -14,7 +14,7 @@ import torch
 
 from . import _native, ensemble
 
-__all__ = ["lml"]
+__all__ = ["lml", "terminal_values"]
 
 
 class _LmlFixedGrid(torch.autograd.Function):
@@ -51,3 +51,41 @@ def lml(params, y0, data, std, *, field="fitzhugh_nagumo", num_derivatives=3, dt
                                constraint="ts0", strategy="fixedpoint", solver="none", precision=precision, damp=damp)
     return _LmlFixedGrid.apply(params, y0, data, std, cfg, float(t0), float(dt), int(num_steps), int(save_every),
                                bool(average_pdfs), stream)
+
+
+class _TerminalValues(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, params, y0, cfg, t0, t1, dt0, stream):
+        grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
+        out = ensemble.solve_ensemble(cfg, params=params.detach().contiguous(), y0=y0.detach().contiguous(),
+                                      save_at=torch.tensor([float(t0), float(t1)], dtype=torch.float64), dt0=dt0,
+                                      terminal_only=True, device=y0.device, stream=stream, sensitivities=grad)
+        if grad:
+            ctx.save_for_backward(out["u_mean_d_params"][:, 0], out["u_mean_d_y0"][:, 0])
+        ctx.mark_non_differentiable(out["status"])
+        return out["u_mean"][:, 0], out["status"]
+
+    @staticmethod
+    def backward(ctx, g_mean, g_status):
+        d_params, d_y0 = ctx.saved_tensors
+        g_params = torch.einsum("bij,bijk->bk", g_mean, d_params) if ctx.needs_input_grad[0] else None
+        g_y0 = torch.einsum("bij,bijk->bk", g_mean, d_y0) if ctx.needs_input_grad[1] else None
+        return g_params, g_y0, None, None, None, None, None
+
+
+def terminal_values(params, y0, *, t0, t1, field="lotka_volterra", num_derivatives=4, solver="mle", atol=1e-6,
+                    rtol=1e-6, dt0=0.1, precision="float64", stream=None):
+    """Differentiable terminal values of an isotropic TS0 filter solve.
+
+    params (B, P) and y0 (B, d) float64 CUDA tensors (``requires_grad`` for
+    gradients).  Returns (u_mean (B, n, d) -- the Taylor coefficients at t1 --,
+    status (B,) int32).  The backward pass contracts the cotangent with the
+    forward-mode sensitivities the same launch computed (P + d threads per
+    instance), the counterpart of ``jax.grad`` through
+    ``solve_adaptive_terminal_values`` with its stop-gradient on the step size
+    (probdiffeq/_ivpsolve/solvers_via_adaptive_steps.py:16-43, 294-301).
+    """
+    cfg = ensemble.make_config(field=field, num_derivatives=num_derivatives, ode_dim=y0.shape[-1], ssm="isotropic",
+                               constraint="ts0", strategy="filter", solver=solver, precision=precision, atol=atol,
+                               rtol=rtol, clip_dt=True)
+    return _TerminalValues.apply(params, y0, cfg, float(t0), float(t1), dt0, stream)

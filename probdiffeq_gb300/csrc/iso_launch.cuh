@@ -38,10 +38,25 @@ cudaError_t launch_iso_kernel(const IsoArgs& a, cudaStream_t stream, int block) 
   return cudaGetLastError();
 }
 
+// Forward-mode sensitivities: P + d threads per instance.
+template <typename T, int NU, class F, bool INTERP>
+cudaError_t launch_iso_tangents(const IsoArgs& a, cudaStream_t stream, int block) {
+  cudaError_t e = ensure_stack<iso_adaptive_kernel<T, NU, F, INTERP, false, false, true>>();
+  if (e != cudaSuccess) return e;
+  const int64_t threads = a.B * int64_t(F::P + F::D);
+  const unsigned grid = unsigned((threads + block - 1) / block);
+  iso_adaptive_kernel<T, NU, F, INTERP, false, false, true><<<grid, block, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
 // The fixed-point smoother and TS1 / error_state_std take the general
 // instantiation; the filter with TS0 and error_residual_std the lean one.
 template <typename T, int NU, class F, bool FP>
 cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
+  if constexpr (!FP) {
+    if (a.tangents) return interp ? launch_iso_tangents<T, NU, F, true>(a, stream, block)
+                                  : launch_iso_tangents<T, NU, F, false>(a, stream, block);
+  }
   if (FP || a.ts1 || a.state_error)
     return interp ? launch_iso_kernel<T, NU, F, true, FP, true>(a, stream, block)
                   : launch_iso_kernel<T, NU, F, false, FP, true>(a, stream, block);

@@ -34,6 +34,7 @@ struct IsoArgs {
   int32_t ts1;  // 0: TS0 (H = e_1); 1: TS1 with the Jacobian trace along d (H = [-tr J_f / d, 1, 0, ...])
   int32_t state_error;  // 0: error_residual_std; 1: error_state_std (derivative 0)
   int32_t instances_per_block;  // launch shape (read by the launchers only)
+  int32_t tangents;  // 1: d u_mean / d (params, y0) by forward mode (P + d threads per instance)
   double safety, factor_min, factor_max, exp_i, exp_p;
   double atol, rtol, eps, damp;
   int64_t max_attempts;
@@ -64,7 +65,11 @@ struct IsoArgs {
   double* cond_to_latent;    // (B, S - 1, n)
   double* cond_to_observed;  // (B, S - 1, n)
   double* filter_mean;       // (B, S, n, d)
-  double* filter_chol;       // (B, S, n, n), calibrated
+  double* filter_chol;
+  // forward-mode sensitivities of the mean records (optional): d u_mean / d params
+  // (B, S_out, n, d, P) and d u_mean / d y0 (B, S_out, n, d, d)
+  double* tan_params;
+  double* tan_y0;       // (B, S, n, n), calibrated
 };
 
 // A constant in the kernel's precision: the float copy for float, else the double.
@@ -612,6 +617,17 @@ PDQ_D void write_normal_iso(const IsoArgs& a, int64_t rec, const T (&m)[NU + 1][
     for (int j = 0; j < n; ++j) uc[i * n + j] = double(L[i][j]);
 }
 
+// Sensitivity record: direction k < P is d / d params[k], k >= P is d / d y0[k - P].
+template <typename T, int NU, int D, int P>
+PDQ_D void write_tangent(const IsoArgs& a, int64_t rec, int k, const T (&dm)[NU + 1][D]) {
+  constexpr int n = NU + 1;
+  double* out = k < P ? a.tan_params : a.tan_y0;
+  const int dirs = k < P ? P : D, kk = k < P ? k : k - P;
+  if (out == nullptr) return;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < D; ++j) out[((rec * n + i) * D + j) * dirs + kk] = double(dm[i][j]);
+}
+
 // One adaptive solve per thread.  INTERP: keep the interpolation state
 // (needed unless clip_dt makes every checkpoint an exact landing).  FP: the
 // fixed-point smoother (estimators_and_losses.py:473-591): every step also
@@ -623,13 +639,24 @@ PDQ_D void write_normal_iso(const IsoArgs& a, int64_t rec, const T (&m)[NU + 1][
 // GEN: TS1 and error_state_std are available (run-time switches); the
 // instantiation without them serves TS0 with error_residual_std, whose
 // attempt is then free of their branches and of the TS1 term in the update.
-template <typename T, int NU, class F, bool INTERP, bool FP = false, bool GEN = true>
+// TAN (TS0 filter): forward-mode sensitivities of the mean, P + d threads per
+// instance, thread k carrying d / d params[k] (k < P) or d / d y0[k - P].
+// Every thread recomputes the same value path (same steps, same records);
+// thread 0 writes the values.  The step size carries no tangent (the
+// reference stops gradients through dt), and with H = e_1 the covariance
+// recursion does not depend on the parameters, so the tangent of an update
+// is dm' = dmp - gain (dmp_1 - df), dmp = p A p^-1 dm, df = J_f dmp_0 + df/dtheta.
+template <typename T, int NU, class F, bool INTERP, bool FP = false, bool GEN = true, bool TAN = false>
 __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   constexpr int n = NU + 1;
   constexpr int D = F::D;
   constexpr int P = F::P;
   constexpr int OUT = 1;  // ODE u' = f(u): observe coefficient 1 (problems.py:283-295)
-  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  static_assert(!(TAN && (FP || GEN)), "sensitivities: TS0 filter only");
+  const int64_t gtid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t b = TAN ? gtid / (P + D) : gtid;
+  const int kdir = TAN ? int(gtid % (P + D)) : 0;
+  const bool primary = kdir == 0;  // writes the values
   if (b >= a.B) return;
 
   const int S = a.S;
@@ -656,6 +683,27 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
     for (int j = 0; j < D; ++j) m[i][j] = T(tc[i][j]);
 #pragma unroll
     for (int j = 0; j < n; ++j) L[i][j] = T(0);
+  }
+  // tangents of m and of the interpolation state (TAN only): the Taylor
+  // coefficients' derivative along this thread's direction
+  T dm[n][D], dmi[n][D];
+  if constexpr (TAN) {
+    Dual<double, 1> yd[D], prd[P], tcd[n][D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      yd[j] = Dual<double, 1>(y0[j]);
+      yd[j].g[0] = (kdir == P + j) ? 1.0 : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      prd[k] = Dual<double, 1>(pd[k]);
+      prd[k].g[0] = (kdir == k) ? 1.0 : 0.0;
+    }
+    taylor_init<F, NU>(yd, prd, tcd);
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) dm[i][j] = dmi[i][j] = T(tcd[i][j].g[0]);
   }
   // interpolation state (interp_from); dead code when INTERP is false
   T mi[n][D], Li[n][n];
@@ -701,7 +749,10 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   const T q00 = cst<T>(a.q1[0][0], a.q1f[0][0]), q10 = cst<T>(a.q1[1][0], a.q1f[1][0]),
           q11 = cst<T>(a.q1[1][1], a.q1f[1][1]);
 
-  if (!a.terminal_only) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, wide_value(t), 0);
+  if (!a.terminal_only) {
+    if (primary) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, wide_value(t), 0);
+    if constexpr (TAN) write_tangent<T, NU, D, P>(a, b * S_out, kdir, dm);
+  }
   if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S, m, L);
 
   // t + eps < t_next (float64: exactly the reference's comparison; float
@@ -796,6 +847,27 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           for (int i = 0; i < n; ++i)
 #pragma unroll
             for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - gain[i] * mobs[j];
+          T dmnew[n][D];
+          if constexpr (TAN) {
+            T dmp[n][D];
+            iso_predict_mean<T, NU, D>(dm, p, pinv, dmp);
+            Dual<T, 1> ud[D], prd[P], fd[D];
+#pragma unroll
+            for (int j = 0; j < D; ++j) {
+              ud[j] = Dual<T, 1>(mp[0][j]);
+              ud[j].g[0] = dmp[0][j];
+            }
+#pragma unroll
+            for (int k = 0; k < P; ++k) {
+              prd[k] = Dual<T, 1>(pt[k]);
+              prd[k].g[0] = (kdir == k) ? T(1) : T(0);
+            }
+            F::eval(ud, prd, fd);
+#pragma unroll
+            for (int i = 0; i < n; ++i)
+#pragma unroll
+              for (int j = 0; j < D; ++j) dmnew[i][j] = dmp[i][j] - gain[i] * (dmp[OUT][j] - fd[j].g[0]);
+          }
 
           // ---- error estimate (error_residual_std, solvers.py:925-996) ----
           // error_residual_std: the std of the observed residual rescaled by
@@ -849,6 +921,18 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
                 for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
               }
               if constexpr (FP) bwi = bw;
+              if constexpr (TAN) {
+#pragma unroll
+                for (int i = 0; i < n; ++i)
+#pragma unroll
+                  for (int j = 0; j < D; ++j) dmi[i][j] = dm[i][j];
+              }
+            }
+            if constexpr (TAN) {
+#pragma unroll
+              for (int i = 0; i < n; ++i)
+#pragma unroll
+                for (int j = 0; j < D; ++j) dm[i][j] = dmnew[i][j];
             }
             if constexpr (FP) {
               IsoBackward<T, NU, D> merged;
@@ -925,8 +1009,17 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           } else {
             iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
           }
-          if (record) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), wide_value(t_next), num_steps);
+          if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), wide_value(t_next), num_steps);
           if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, mp, Lp);
+          if constexpr (TAN) {
+            T dmp[n][D];
+            iso_predict_mean<T, NU, D>(dmi, p, pinv, dmp);
+            if (record) write_tangent<T, NU, D, P>(a, b * S_out + s_out, kdir, dmp);
+#pragma unroll
+            for (int i = 0; i < n; ++i)
+#pragma unroll
+              for (int j = 0; j < D; ++j) dmi[i][j] = dmp[i][j];
+          }
           ti = t_next;
 #pragma unroll
           for (int i = 0; i < n; ++i) {
@@ -938,7 +1031,16 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
         }
       } else {
         // interp_at_t1: the state itself is the solution (estimators_and_losses.py:416-421)
-        if (record) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), wide_value(t), num_steps);
+        if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), wide_value(t), num_steps);
+        if constexpr (TAN) {
+          if (record) write_tangent<T, NU, D, P>(a, b * S_out + s_out, kdir, dm);
+          if constexpr (INTERP) {
+#pragma unroll
+            for (int i = 0; i < n; ++i)
+#pragma unroll
+              for (int j = 0; j < D; ++j) dmi[i][j] = dm[i][j];
+          }
+        }
         if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, m, L);
         if constexpr (FP) {
           // estimators_and_losses.py:534-547: close the checkpoint's conditional, reset
@@ -993,6 +1095,17 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
     }
   }
 
+  if constexpr (TAN) {
+    if (status != PDQ_INSTANCE_OK) {
+      T nan_dm[n][D];
+#pragma unroll
+      for (int i = 0; i < n; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) nan_dm[i][j] = T(__longlong_as_double(0x7ff8000000000000ULL));
+      for (int s = 0; s < S_out; ++s) write_tangent<T, NU, D, P>(a, b * S_out + s, kdir, nan_dm);
+    }
+    if (!primary) return;
+  }
   // ---- finalize: calibrated output scale (solvers.py:439-480, 601-633, 735-767) ----
   if (status == PDQ_INSTANCE_OK) {
     if (a.solver == PDQ_SOLVER_MLE) {

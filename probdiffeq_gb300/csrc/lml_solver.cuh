@@ -35,28 +35,6 @@
 namespace pdq {
 
 template <typename T, int K>
-PDQ_HD Dual<T, K> operator/(const Dual<T, K>& a, const Dual<T, K>& b) {
-  Dual<T, K> r;
-  const T inv = T(1) / b.v;
-  r.v = a.v * inv;
-#pragma unroll
-  for (int k = 0; k < K; ++k) r.g[k] = (a.g[k] - r.v * b.g[k]) * inv;
-  return r;
-}
-template <typename T, int K>
-PDQ_HD Dual<T, K> operator/(const Dual<T, K>& a, T b) {
-  Dual<T, K> r;
-  const T inv = T(1) / b;
-  r.v = a.v * inv;
-#pragma unroll
-  for (int k = 0; k < K; ++k) r.g[k] = a.g[k] * inv;
-  return r;
-}
-template <typename T, int K>
-PDQ_HD Dual<T, K> operator/(T a, const Dual<T, K>& b) {
-  return Dual<T, K>(a) / b;
-}
-template <typename T, int K>
 PDQ_HD Dual<T, K> dual_abs_scale(T s, const Dual<T, K>& a) {  // |s| * a for a constant s
   return (s < T(0) ? -s : s) * a;
 }

@@ -221,6 +221,11 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     // for exact checkpoint landings only
     const bool warp = c->clip_dt && c->kernel_variant >= 2;
     if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1 || a.state_error || fp)) return PDQ_ERROR_UNSUPPORTED;
+    a.tan_params = args->u_mean_d_params;
+    a.tan_y0 = args->u_mean_d_y0;
+    a.tangents = (a.tan_params || a.tan_y0) ? 1 : 0;
+    if (a.tangents && (a.ts1 || a.state_error || fp || c->kernel_variant >= 2 || c->field >= PDQ_FIELD_USER_BASE))
+      return PDQ_ERROR_UNSUPPORTED;
     const int ipb = c->instances_per_block;
     if (warp ? !(ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32) : !(ipb == 0 || ipb == 32 || ipb == 64))
       return PDQ_ERROR_INVALID_VALUE;
@@ -270,6 +275,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
   if (c->ssm == PDQ_SSM_BLOCKDIAG) {
     if (c->field != PDQ_FIELD_BURGERS) return PDQ_ERROR_UNSUPPORTED;
     if (c->instances_per_block != 0) return PDQ_ERROR_INVALID_VALUE;  // one cluster per instance
+    if (args->u_mean_d_params || args->u_mean_d_y0) return PDQ_ERROR_UNSUPPORTED;
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
     if (c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
     if (!c->clip_dt) return PDQ_ERROR_UNSUPPORTED;  // checkpoints by exact landing only
@@ -335,6 +341,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
   if (c->ssm == PDQ_SSM_DENSE) {
     // error_state_std: the thread-per-instance mapping
     if (c->error == PDQ_ERROR_STATE_STD && c->kernel_variant == 2) return PDQ_ERROR_UNSUPPORTED;
+    if (args->u_mean_d_params || args->u_mean_d_y0) return PDQ_ERROR_UNSUPPORTED;
     {
       const int ipb = c->instances_per_block;
       if (c->kernel_variant == 2 ? !(ipb >= 0 && ipb <= 4) : !(ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32))

@@ -406,6 +406,28 @@ PDQ_HD Dual<T, K> operator-(const Dual<T, K>& a, T s) {
   return r;
 }
 
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator/(const Dual<T, K>& a, const Dual<T, K>& b) {
+  Dual<T, K> r;
+  const T inv = T(1) / b.v;
+  r.v = a.v * inv;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = (a.g[k] - r.v * b.g[k]) * inv;
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator/(const Dual<T, K>& a, T b) {
+  Dual<T, K> r;
+  const T inv = T(1) / b;
+  r.v = a.v * inv;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.g[k] = a.g[k] * inv;
+  return r;
+}
+template <typename T, int K>
+PDQ_HD Dual<T, K> operator/(T a, const Dual<T, K>& b) {
+  return Dual<T, K>(a) / b;
+}
 // f(u) and the Jacobian J[i][j] = df_i/du_j of a registered field.
 template <class F, typename T>
 PDQ_HD void eval_with_jacobian(const T* u, const T* p, T* f, T (&J)[F::D][F::D]) {

@@ -67,14 +67,16 @@ def _dev(x, device, B=None, cols=None):
 
 
 def solve_ensemble(cfg, *, params, y0, save_at, dt0=0.1, terminal_only=True, device="cuda", stream=None, outputs=None,
-                   autotune=False):
+                   autotune=False, sensitivities=False):
     """Solve B instances; returns the dict of output device tensors.
 
     params (B, P), y0 (B, d), save_at (S,) shared or (B, S) per instance,
     dt0 scalar or (B,).  Output layout as in include/pdq.h.  ``autotune``:
     pick the instance-to-thread mapping and instances per CTA by timing the
     candidates on this batch (once per configuration and batch-size class;
-    ``probdiffeq_gb300.autotune``).
+    ``probdiffeq_gb300.autotune``).  ``sensitivities`` (isotropic TS0 filter):
+    also d u_mean / d params and d u_mean / d y0 by forward mode
+    (``u_mean_d_params`` (B, S_out, n, d, P), ``u_mean_d_y0`` (B, S_out, n, d, d)).
     """
     y0 = _dev(y0, device)
     B = y0.shape[0]
@@ -91,7 +93,8 @@ def solve_ensemble(cfg, *, params, y0, save_at, dt0=0.1, terminal_only=True, dev
     dt0 = dt0.to(device, non_blocking=True).contiguous()
     S = save_at.shape[1]
     if outputs is None:
-        outputs = _native.alloc_outputs(cfg, B, S, terminal_only, device)
+        outputs = _native.alloc_outputs(cfg, B, S, terminal_only, device,
+                                        num_params=params.shape[1] if sensitivities else None)
     if autotune:
         from . import autotune as tuner
 
