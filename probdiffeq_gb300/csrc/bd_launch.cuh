@@ -13,14 +13,14 @@ inline int bd_cluster_size(int d) {
   return cl;
 }
 
-template <typename T, int NU>
-cudaError_t launch_bd_nu(BdArgs a, cudaStream_t stream) {
-  cudaError_t e = ensure_stack<bd_adaptive_kernel<T, NU>>();
+template <typename T, int NU, bool FP>
+cudaError_t launch_bd_kernel(BdArgs a, cudaStream_t stream) {
+  cudaError_t e = ensure_stack<bd_adaptive_kernel<T, NU, FP>>();
   if (e != cudaSuccess) return e;
   const int CL = a.cluster;
   const size_t smem = bd_smem_bytes<T, NU>(a.d / CL);
   if (smem > 48 * 1024) {
-    e = cudaFuncSetAttribute(bd_adaptive_kernel<T, NU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    e = cudaFuncSetAttribute(bd_adaptive_kernel<T, NU, FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
   }
   cudaLaunchConfig_t cfg = {};
@@ -35,9 +35,14 @@ cudaError_t launch_bd_nu(BdArgs a, cudaStream_t stream) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  e = cudaLaunchKernelEx(&cfg, bd_adaptive_kernel<T, NU>, a);
+  e = cudaLaunchKernelEx(&cfg, bd_adaptive_kernel<T, NU, FP>, a);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
+}
+
+template <typename T, int NU>
+cudaError_t launch_bd_nu(const BdArgs& a, cudaStream_t stream) {
+  return a.fixedpoint ? launch_bd_kernel<T, NU, true>(a, stream) : launch_bd_kernel<T, NU, false>(a, stream);
 }
 
 template <typename T>

@@ -31,6 +31,16 @@
 // proposal is written to the other buffer, so an accept is a parity flip.
 // Time, step size and controller follow the isotropic kernel: Wide<T> time,
 // T controller, no float64 on the attempt path of the float32 kernel.
+//
+// FP: the fixed-point smoother (estimators_and_losses.py:473-591 with the
+// block-diagonal revert / merge, ssm_impl_blockdiag.py:45-102), per
+// dimension: every attempt reverts the prior transition instead of
+// marginalising it and merges the backward conditional into the running one;
+// the running conditionals (iso_cond_floats<NU, 1> numbers per dimension)
+// live in two more parity buffers next to the state, are copied out at every
+// checkpoint (exact landings) and reset to the identity; after the last step
+// the backward pass marginalises each dimension's terminal state through the
+// stored conditionals (Smoother.finalize, MarkovSequence.evaluate_marginals).
 #pragma once
 
 #include <cooperative_groups.h>
@@ -49,6 +59,7 @@ struct BdArgs {
   int32_t S, terminal_only, solver, control, correct, d, cluster;
   int32_t ts1;  // 1: TS1 with the Jacobian diagonal along d (per-dimension H_j = [-dfj/duj, 1, 0, ...])
   int32_t state_error;  // 0: error_residual_std; 1: error_state_std (derivative 0)
+  int32_t fixedpoint;   // 1: the fixed-point smoother
   double safety, factor_min, factor_max, exp_i, exp_p;
   double atol, rtol, eps, damp;
   int64_t max_attempts;
@@ -60,15 +71,57 @@ struct BdArgs {
   const double* params;  // (B, 1): viscosity
   const double* y0;      // (B, d)
   const double* dt0;
-  double* u_mean;        // (B, S_out, d, n)
+  double* u_mean;        // (B, S_out, d, n); the fixed-point smoother writes the smoothed marginals
   double* u_chol;        // (B, S_out, d, n, n)
   double* output_scale;  // (B, S_out, d)
   double* t_out;
   int32_t* num_steps;
   int32_t* num_attempts;
   int32_t* status;
-  void* workspace;       // 2 state buffers (B, ns, d) in T, then MLE sums (B, d), 8 bytes each
+  void* workspace;       // 2 state buffers (B, ns, d) in T, then MLE sums (B, d), 8 bytes each;
+                         // FP: then 2 conditional buffers (B, cf, d) and the checkpoints' (B, S - 1, cf, d) in T
 };
+
+// Conditional of one dimension in a strided buffer (element e of dimension g at e * d + g).
+template <typename T, int NU>
+PDQ_D void bd_cond_store(T* base, int64_t stride, const IsoBackward<T, NU, 1>& c) {
+  constexpr int n = NU + 1;
+  int o = 0;
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) base[(o++) * stride] = c.A[i][j];
+#pragma unroll
+  for (int i = 0; i < n; ++i) base[(o++) * stride] = c.xi[i][0];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) base[(o++) * stride] = c.X[i][j];
+#pragma unroll
+  for (int i = 0; i < n; ++i) base[(o++) * stride] = c.tl[i];
+#pragma unroll
+  for (int i = 0; i < n; ++i) base[(o++) * stride] = c.to[i];
+}
+
+template <typename T, int NU>
+PDQ_D void bd_cond_load(const T* base, int64_t stride, IsoBackward<T, NU, 1>& c) {
+  constexpr int n = NU + 1;
+  int o = 0;
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) c.A[i][j] = base[(o++) * stride];
+#pragma unroll
+  for (int i = 0; i < n; ++i) c.xi[i][0] = base[(o++) * stride];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) c.X[i][j] = (j <= i) ? base[(o++) * stride] : T(0);
+#pragma unroll
+  for (int i = 0; i < n; ++i) c.tl[i] = base[(o++) * stride];
+#pragma unroll
+  for (int i = 0; i < n; ++i) c.to[i] = base[(o++) * stride];
+}
 
 template <int NU>
 PDQ_HD constexpr int bd_state_rows() {
@@ -91,10 +144,11 @@ PDQ_D T burgers_f(T left, T mid, T right, T nu_visc, T inv_dx) {
   return -flux + nu_visc * lap;
 }
 
-template <typename T, int NU>
+template <typename T, int NU, bool FP = false>
 __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   constexpr int n = NU + 1;
   constexpr int NS = bd_state_rows<NU>();
+  constexpr int CF = iso_cond_floats<NU, 1>();
   constexpr int OUT = 1;
   constexpr bool kNarrow = sizeof(T) == sizeof(float);
   using W = Wide<T>;
@@ -119,6 +173,10 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   T* const buf0 = reinterpret_cast<T*>(a.workspace);
   T* const bufs[2] = {buf0 + inst * NS * int64_t(d), buf0 + (a.B + inst) * NS * int64_t(d)};
   W* mle_sum = reinterpret_cast<W*>(buf0 + 2 * a.B * NS * int64_t(d)) + inst * int64_t(d);
+  // FP: running conditionals (parity buffers like the state) and the checkpoints'
+  T* const cond0 = reinterpret_cast<T*>(reinterpret_cast<W*>(buf0 + 2 * a.B * NS * int64_t(d)) + a.B * int64_t(d));
+  T* const cbufs[2] = {cond0 + inst * CF * int64_t(d), cond0 + (a.B + inst) * CF * int64_t(d)};
+  T* const ckpt = cond0 + 2 * a.B * CF * int64_t(d) + inst * int64_t(a.S - 1) * CF * int64_t(d);
 
   const T nu_visc = T(a.params[inst]);
   const T inv_dx = T(d);
@@ -161,6 +219,11 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
     for (int r = n; r < NS; ++r) st[r * d + g] = T(0);
     mle_sum[g] = wide_from(0.0, T(0));
     sig[jl] = T(1);
+    if constexpr (FP) {
+      IsoBackward<T, NU, 1> id;
+      iso_cond_identity(id);
+      bd_cond_store<T, NU>(cbufs[0] + g, d, id);
+    }
   }
   __threadfence();
   cluster.sync();
@@ -291,7 +354,21 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
           for (int j = 0; j < n; ++j) L[i][j] = (j <= i) ? x[(n + i * (i + 1) / 2 + j) * d + g] : T(0);
         // the block-diagonal marginalise scales the factor by |p_inv| (ssm_impl_blockdiag.py:32)
         T Lp[n][n];
-        if constexpr (kNarrow) {
+        if constexpr (FP) {
+          // revert (ssm_impl_blockdiag.py:69-102), merge into the running conditional (:45-67)
+          T mcol[n][1];
+#pragma unroll
+          for (int i = 0; i < n; ++i) mcol[i][0] = x[i * d + g];
+          IsoBackward<T, NU, 1> cnew, bwj, merged;
+          if constexpr (kNarrow) {
+            iso_prior_revert<T, NU, 1>(a.q1f, mcol, L, p, pinv, s_pred * sq_h, Lp, cnew);
+          } else {
+            iso_prior_revert<T, NU, 1>(a.q1, mcol, L, p, pinv, s_pred * sq_h, Lp, cnew);
+          }
+          bd_cond_load<T, NU>(cbufs[cur] + g, d, bwj);
+          iso_cond_merge(bwj, cnew, merged);
+          bd_cond_store<T, NU>(cbufs[cur ^ 1] + g, d, merged);
+        } else if constexpr (kNarrow) {
           iso_predict_chol<T, NU>(a.q1f, L, p, pinv_abs, s_pred * sq_h, Lp);
         } else {
           iso_predict_chol<T, NU>(a.q1, L, p, pinv_abs, s_pred * sq_h, Lp);
@@ -373,6 +450,59 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       const int s_out = a.terminal_only ? 0 : s;
       write_checkpoint(s_out, wide_value(t));
       if (a.solver != PDQ_SOLVER_MLE) write_scale(s_out);
+    }
+    if constexpr (FP) {
+      // close the checkpoint's conditional, reset (estimators_and_losses.py:534-547)
+      IsoBackward<T, NU, 1> c, id;
+      iso_cond_identity(id);
+#pragma unroll 1
+      for (int jl = tid; jl < dl; jl += kBdThreads) {
+        const int g = j0 + jl;
+        bd_cond_load<T, NU>(cbufs[cur] + g, d, c);
+        bd_cond_store<T, NU>(ckpt + int64_t(s - 1) * CF * d + g, d, c);
+        bd_cond_store<T, NU>(cbufs[cur] + g, d, id);
+      }
+    }
+  }
+
+  // ---- fixed-point backward pass: smoothed marginals at the checkpoints ----
+  if constexpr (FP) {
+    if (status == PDQ_INSTANCE_OK) {
+      const T* x = bufs[cur];
+      auto write_marginal = [&](int s_out, int g, const T (&rm)[n][1], const T (&rL)[n][n]) {
+        const int64_t rec = inst * S_out + s_out;
+        double* um = a.u_mean + (rec * d + g) * n;
+        double* uc = a.u_chol + (rec * d + g) * n * n;
+        for (int i = 0; i < n; ++i) um[i] = double(rm[i][0]);
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) uc[i * n + j] = double(rL[i][j]);
+      };
+#pragma unroll 1
+      for (int jl = tid; jl < dl; jl += kBdThreads) {
+        const int g = j0 + jl;
+        // the terminal state itself: the last checkpoint reset the running conditional
+        T rm[n][1], rL[n][n];
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+          rm[i][0] = x[i * d + g];
+#pragma unroll
+          for (int j = 0; j < n; ++j) rL[i][j] = (j <= i) ? x[(n + i * (i + 1) / 2 + j) * d + g] : T(0);
+        }
+        if (a.terminal_only) continue;  // the terminal record is the filter's (written above)
+        for (int s = S - 1; s >= 1; --s) {
+          IsoBackward<T, NU, 1> c;
+          bd_cond_load<T, NU>(ckpt + int64_t(s - 1) * CF * d + g, d, c);
+          T pm[n][1], pL[n][n];
+          iso_cond_marginalise(c, rm, rL, pm, pL);
+#pragma unroll
+          for (int i = 0; i < n; ++i) {
+            rm[i][0] = pm[i][0];
+#pragma unroll
+            for (int j = 0; j < n; ++j) rL[i][j] = pL[i][j];
+          }
+          write_marginal(s - 1, g, rm, rL);
+        }
+      }
     }
   }
 

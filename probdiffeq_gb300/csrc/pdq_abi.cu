@@ -132,6 +132,12 @@ pdq_status pdq_workspace_size(const pdq_config* c, int64_t num_instances, int32_
     const int nu = c->num_derivatives;
     const size_t rows = size_t(nu + 1) + size_t(nu + 1) * (nu + 2) / 2;
     *bytes = 2 * size_t(num_instances) * rows * size_t(c->ode_dim) * elem + size_t(num_instances) * c->ode_dim * 8;
+    if (c->strategy == PDQ_STRATEGY_FIXEDPOINT) {
+      // running conditionals (2 parity buffers) and one per checkpoint interval, per dimension
+      const size_t n = size_t(nu + 1);
+      const size_t cf = n * n + n + n * (n + 1) / 2 + 2 * n;
+      *bytes += (2 + size_t(num_save_at - 1)) * size_t(num_instances) * cf * size_t(c->ode_dim) * elem;
+    }
   }
   if (c->ssm == PDQ_SSM_ISOTROPIC && c->strategy == PDQ_STRATEGY_FIXEDPOINT) {
     const int n = c->num_derivatives + 1, d = c->ode_dim;
@@ -277,8 +283,11 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     if (c->instances_per_block != 0) return PDQ_ERROR_INVALID_VALUE;  // one cluster per instance
     if (args->u_mean_d_params || args->u_mean_d_y0) return PDQ_ERROR_UNSUPPORTED;
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
-    if (c->strategy != PDQ_STRATEGY_FILTER) return PDQ_ERROR_UNSUPPORTED;
+    if (c->strategy != PDQ_STRATEGY_FILTER && c->strategy != PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_INVALID_VALUE;
     if (!c->clip_dt) return PDQ_ERROR_UNSUPPORTED;  // checkpoints by exact landing only
+    if (args->cond_A || args->cond_noise_mean || args->cond_noise_chol || args->cond_to_latent ||
+        args->cond_to_observed || args->filter_mean || args->filter_chol)
+      return PDQ_ERROR_UNSUPPORTED;  // the posterior's conditionals stay in the workspace
     if (c->num_derivatives < 2 || c->num_derivatives > 4) return PDQ_ERROR_UNSUPPORTED;
     const int d = c->ode_dim;
     if (d < 3) return PDQ_ERROR_INVALID_VALUE;
@@ -299,6 +308,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.cluster = CL;
     a.ts1 = c->constraint == PDQ_CONSTRAINT_TS1 ? 1 : 0;
     a.state_error = c->error == PDQ_ERROR_STATE_STD ? 1 : 0;
+    a.fixedpoint = c->strategy == PDQ_STRATEGY_FIXEDPOINT ? 1 : 0;
     a.safety = c->safety;
     a.factor_min = c->factor_min;
     a.factor_max = c->factor_max;

@@ -218,3 +218,74 @@ def test_burgers_error_state_std_vs_oracle():
                                                      solvers.ErrorStateStd(c), S.prior_wiener_integrated(tc),
                                                      0.0, t1, 1e-4, 1e-4, dt0=0.1 * t1)
         compare(out, b, res, dict(u=1e-8, rows=1e-5, cov=1e-5, steps=0.0))
+
+
+def compare_record(gm, gc, o, tol):
+    err_u = rel(gm[:, 0], o.mean[:, 0])
+    err_rows = max(rel(gm[:, i], o.mean[:, i]) for i in range(o.mean.shape[1]))
+    cg = gc @ gc.transpose(-1, -2)
+    co = o.cholesky @ o.cholesky.transpose(-1, -2)
+    if float(co.abs().max()) == 0.0:  # the exact initial coefficients at t0
+        err_cov = float(cg.abs().max())
+    else:
+        err_cov = max(rel(cg[j], co[j]) for j in range(co.shape[0]) if float(co[j].abs().max()) > 0)
+    msg = f"u {err_u:.2e} rows {err_rows:.2e} cov {err_cov:.2e}"
+    assert err_u <= tol["u"] and err_rows <= tol["rows"] and err_cov <= tol["cov"], msg
+
+
+@pytest.mark.parametrize("solver", ["dynamic", "mle"])
+def test_burgers_fixedpoint_smoother_vs_oracle(solver):
+    """strategy_smoother_fixedpoint in the block-diagonal kernel (estimators_and_losses.py:473-591,
+    ssm_impl_blockdiag.py:45-102): smoothed marginals at every checkpoint, d = 64, float64."""
+    from probdiffeq_gb300 import ensemble
+
+    d, t1 = 64, 0.05
+    save_at = np.linspace(0.0, t1, 5)
+    u0s = [burgers_ic(d, s) for s in (3, 4)]
+    u0t = torch.as_tensor(np.asarray(u0s), dtype=torch.float64)
+    cfg = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=d, ssm="blockdiag", solver=solver,
+                               strategy="fixedpoint", precision="float64", atol=1e-4, rtol=1e-4, clip_dt=True)
+    out = ensemble.solve_ensemble(cfg, params=torch.full((2, 1), NU_VISC, dtype=torch.float64), y0=u0t,
+                                  save_at=torch.tensor(save_at), dt0=0.1 * t1, terminal_only=False)
+    torch.cuda.synchronize()
+    out = {k: v.cpu() for k, v in out.items() if not k.startswith("_") and v is not None}
+    assert (out["status"] == 0).all()
+    p = torch.tensor([NU_VISC], dtype=torch.float64)
+    cls = {"dynamic": solvers.SolverDynamic, "mle": solvers.SolverMLE}[solver]
+    for b, u0 in enumerate(u0s):
+        tc = problems.taylor_derivatives(problems.burgers, torch.tensor(u0), p, 3)
+        S = ssm.BdSSM()
+        c = S.constraint_ode_ts0(lambda u, t: problems.burgers(u[0], p))
+        res = solvers.solve_adaptive_save_at(cls(solvers.StrategyFixedPoint(), c), solvers.ErrorResidualStd(c),
+                                             S.prior_wiener_integrated(tc), save_at, 1e-4, 1e-4, clip_dt=True,
+                                             dt0=0.1 * t1)
+        steps_o = [0] + list(res.num_steps)
+        for s in range(len(save_at)):
+            compare_record(out["u_mean"][b, s], out["u_chol"][b, s], res.u[s], dict(u=1e-8, rows=1e-5, cov=1e-5))
+            assert int(out["num_steps"][b, s]) == steps_o[s]
+
+
+def test_burgers_fixedpoint_full_size_float32():
+    """d = 4096 in float32: the smoothed terminal record is the filter's, the
+    smoothed t0 record the exact initial coefficients, all records finite."""
+    from probdiffeq_gb300 import ensemble
+
+    d, t1 = 4096, 2e-4
+    u0s = [burgers_ic(d, s) for s in (1, 2)]
+    u0t = torch.as_tensor(np.asarray(u0s), dtype=torch.float64)
+    outs = {}
+    for strategy in ("filter", "fixedpoint"):
+        cfg = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=d, ssm="blockdiag", solver="dynamic",
+                                   strategy=strategy, precision="float32", atol=1e-4, rtol=1e-4, clip_dt=True,
+                                   max_attempts=1 << 26)
+        outs[strategy] = ensemble.solve_ensemble(cfg, params=torch.full((2, 1), NU_VISC, dtype=torch.float64),
+                                                 y0=u0t, save_at=torch.linspace(0.0, t1, 4, dtype=torch.float64),
+                                                 dt0=0.1 * t1, terminal_only=False)
+        torch.cuda.synchronize()
+    f, s = outs["filter"], outs["fixedpoint"]
+    assert (s["status"] == 0).all()
+    assert torch.equal(s["num_steps"], f["num_steps"])
+    assert torch.isfinite(s["u_mean"]).all() and torch.isfinite(s["u_chol"]).all()
+    # float32: the smoother predicts through the revert's 2n x 2n QR, the filter through the 2n x n one
+    assert rel(s["u_mean"][:, -1, :, 0].cpu(), f["u_mean"][:, -1, :, 0].cpu()) < 1e-3
+    assert rel(s["u_mean"][:, 0, :, 0].cpu(), u0t) < 1e-5
