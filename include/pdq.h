@@ -322,7 +322,8 @@ pdq_status pdq_offgrid_marginals(const pdq_offgrid_args* args, void* stream);
  *   };
  * generic over the scalar S (float, double, Taylor jets, dual numbers).  On
  * success *field_id (>= PDQ_FIELD_USER_BASE) goes into pdq_config.field
- * (isotropic factorisation; dim and num_params must match D and P).
+ * (isotropic and dense factorisations -- the dense TS1 Jacobian comes from the
+ * same definition; dim and num_params must match D and P).
  * Compiler diagnostics are copied to `log` (host buffer, may be NULL);
  * errors return PDQ_ERROR_COMPILE.  The source is validated by compiling one
  * variant now; each variant used later is compiled and loaded on first use

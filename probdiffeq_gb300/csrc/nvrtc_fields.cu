@@ -13,11 +13,13 @@
 //
 // written generically over the scalar S (float, double, Taylor jets, dual
 // numbers: +, -, * and multiplication / division by parameters), exactly
-// like the built-in fields, so one definition yields f, its Jacobian and the
-// Taylor-mode initial derivatives.  pdq_register_field compiles the source
-// with the solver templates (headers embedded in this library) for sm_103a
-// and reports compiler errors; each (precision, nu, interpolation, strategy)
-// variant is compiled and loaded on first use and cached.
+// like the built-in fields, so one definition yields f, its Jacobian (the
+// dense TS1 linearisation) and the Taylor-mode initial derivatives.
+// pdq_register_field compiles the source with the solver templates (headers
+// embedded in this library) for sm_103a and reports compiler errors; each
+// variant of the isotropic kernel (precision, nu, interpolation, strategy)
+// and of the dense one (precision, nu, TS0/TS1, strategy) is compiled and
+// loaded on first use and cached.
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
@@ -29,6 +31,7 @@
 #include <tuple>
 #include <vector>
 
+#include "dense_solver.cuh"
 #include "iso_solver.cuh"
 #include "nvrtc_fields.h"
 #include "pdq.h"
@@ -40,8 +43,8 @@ struct UserField {
   std::string name, source;
   int dim = 0, params = 0;
   std::mutex mu;
-  // (f64, nu, interp, fixedpoint, general) -> loaded kernel
-  std::map<std::tuple<int, int, int, int, int>, cudaKernel_t> kernels;
+  // (kernel expression) -> loaded kernel
+  std::map<std::string, cudaKernel_t> kernels;
   std::vector<cudaLibrary_t> libraries;
 };
 
@@ -55,11 +58,17 @@ UserField* lookup(int32_t field) {
   return g_fields[size_t(k)].get();
 }
 
+const char* tf(bool b) { return b ? "true" : "false"; }
+
 // gen: the instantiation with TS1 / error_state_std (as the built-in fields' dispatch)
 std::string kernel_expression(bool f64, int nu, bool interp, bool fp, bool gen) {
   return std::string("pdq::iso_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
-         ", pdq_user::Field, " + (interp ? "true" : "false") + ", " + (fp ? "true" : "false") + ", " +
-         (gen ? "true" : "false") + ">";
+         ", pdq_user::Field, " + tf(interp) + ", " + tf(fp) + ", " + tf(gen) + ">";
+}
+
+std::string dense_expression(bool f64, int nu, bool ts1, bool fp) {
+  return std::string("pdq::dense_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
+         ", pdq_user::Field, " + tf(ts1) + ", " + tf(fp) + ">";
 }
 
 void copy_log(const std::string& text, char* log, size_t log_bytes) {
@@ -72,8 +81,9 @@ void copy_log(const std::string& text, char* log, size_t log_bytes) {
 // Compile the solver templates with the field source; returns the cubin and
 // the lowered (mangled) names of the requested kernel instantiations.
 pdq_status compile(const std::string& source, const std::vector<std::string>& expressions, std::string* cubin,
-                   std::vector<std::string>* lowered, std::string* log) {
-  const std::string program = "#include \"iso_solver.cuh\"\nnamespace pdq_user {\n" + source + "\n}  // namespace pdq_user\n";
+                   std::vector<std::string>* lowered, std::string* log, const char* header = "iso_solver.cuh") {
+  const std::string program =
+      std::string("#include \"") + header + "\"\nnamespace pdq_user {\n" + source + "\n}  // namespace pdq_user\n";
   nvrtcProgram prog;
   if (nvrtcCreateProgram(&prog, program.c_str(), "user_field.cu", kPdqHeaderCount, kPdqHeaderSources,
                          kPdqHeaderNames) != NVRTC_SUCCESS)
@@ -146,45 +156,66 @@ int pdq_user_field_params(int32_t field) {
   return f ? f->params : -1;
 }
 
+namespace {
+
+// The kernel for `expression` (compiled with `header`), loaded on first use.
+cudaError_t user_kernel(UserField* f, const std::string& expression, const char* header, cudaKernel_t* kernel) {
+  std::lock_guard<std::mutex> lock(f->mu);
+  auto it = f->kernels.find(expression);
+  if (it != f->kernels.end()) {
+    *kernel = it->second;
+    return cudaSuccess;
+  }
+  std::string cubin, text;
+  std::vector<std::string> lowered;
+  if (compile(f->source, {expression}, &cubin, &lowered, &text, header) != PDQ_SUCCESS) return cudaErrorInvalidSource;
+  cudaLibrary_t lib = nullptr;
+  cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) return e;
+  e = cudaLibraryGetKernel(kernel, lib, lowered[0].c_str());
+  if (e != cudaSuccess) return e;
+  // the per-thread stack limit must cover the kernel's frame (as for the built-in kernels)
+  cudaFuncAttributes attr;
+  e = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(*kernel));
+  if (e != cudaSuccess) return e;
+  size_t cur = 0;
+  e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
+  if (e != cudaSuccess) return e;
+  if (attr.localSizeBytes + 1024 > cur) {
+    e = cudaDeviceSetLimit(cudaLimitStackSize, attr.localSizeBytes + 1024);
+    if (e != cudaSuccess) return e;
+  }
+  f->libraries.push_back(lib);
+  f->kernels.emplace(expression, *kernel);
+  return cudaSuccess;
+}
+
+}  // namespace
+
 cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, int nu, bool interp, bool fp,
                                 cudaStream_t stream, int block) {
   UserField* f = lookup(field);
   if (f == nullptr || nu < 1 || nu > 5) return cudaErrorInvalidValue;
+  const bool gen = fp || a.ts1 || a.state_error;
   cudaKernel_t kernel = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(f->mu);
-    const bool gen = fp || a.ts1 || a.state_error;
-    const auto key = std::make_tuple(f64 ? 1 : 0, nu, interp ? 1 : 0, fp ? 1 : 0, gen ? 1 : 0);
-    auto it = f->kernels.find(key);
-    if (it != f->kernels.end()) {
-      kernel = it->second;
-    } else {
-      std::string cubin, text;
-      std::vector<std::string> lowered;
-      if (compile(f->source, {kernel_expression(f64, nu, interp, fp, gen)}, &cubin, &lowered, &text) != PDQ_SUCCESS)
-        return cudaErrorInvalidSource;
-      cudaLibrary_t lib = nullptr;
-      cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
-      if (e != cudaSuccess) return e;
-      e = cudaLibraryGetKernel(&kernel, lib, lowered[0].c_str());
-      if (e != cudaSuccess) return e;
-      // the per-thread stack limit must cover the kernel's frame (as for the built-in kernels)
-      cudaFuncAttributes attr;
-      e = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(kernel));
-      if (e != cudaSuccess) return e;
-      size_t cur = 0;
-      e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
-      if (e != cudaSuccess) return e;
-      if (attr.localSizeBytes + 1024 > cur) {
-        e = cudaDeviceSetLimit(cudaLimitStackSize, attr.localSizeBytes + 1024);
-        if (e != cudaSuccess) return e;
-      }
-      f->libraries.push_back(lib);
-      f->kernels.emplace(key, kernel);
-    }
-  }
+  cudaError_t e = user_kernel(f, kernel_expression(f64, nu, interp, fp, gen), "iso_solver.cuh", &kernel);
+  if (e != cudaSuccess) return e;
   pdq::IsoArgs args = a;
   void* params[] = {&args};
+  const unsigned grid = unsigned((a.B + block - 1) / block);
+  return cudaLaunchKernel(reinterpret_cast<const void*>(kernel), dim3(grid), dim3(unsigned(block)), params, 0, stream);
+}
+
+cudaError_t pdq_launch_dense_user(const pdq::DenseArgs& a, int32_t field, bool f64, int nu, bool ts1, bool fp,
+                                  cudaStream_t stream) {
+  UserField* f = lookup(field);
+  if (f == nullptr || nu < 2 || nu > 3) return cudaErrorInvalidValue;
+  cudaKernel_t kernel = nullptr;
+  cudaError_t e = user_kernel(f, dense_expression(f64, nu, ts1, fp), "dense_solver.cuh", &kernel);
+  if (e != cudaSuccess) return e;
+  pdq::DenseArgs args = a;
+  void* params[] = {&args};
+  const int block = a.instances_per_block > 0 ? a.instances_per_block : 32;  // one thread per instance
   const unsigned grid = unsigned((a.B + block - 1) / block);
   return cudaLaunchKernel(reinterpret_cast<const void*>(kernel), dim3(grid), dim3(unsigned(block)), params, 0, stream);
 }

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include "dense_solver.cuh"
 #include "iso_solver.cuh"
 
 // State dimension / number of parameters of a registered user field (0 / -1 if unknown).
@@ -14,3 +15,7 @@ int pdq_user_field_params(int32_t field);
 // compiles and loads the variant on first use.
 cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, int nu, bool interp, bool fp,
                                 cudaStream_t stream, int block);
+
+// The same for the dense kernel (one thread per instance).
+cudaError_t pdq_launch_dense_user(const pdq::DenseArgs& a, int32_t field, bool f64, int nu, bool ts1, bool fp,
+                                  cudaStream_t stream);

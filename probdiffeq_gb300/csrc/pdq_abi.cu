@@ -417,6 +417,11 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     // kernel_variant 2: eight lanes per instance (shared-memory state); otherwise one thread per instance
     const int block = c->kernel_variant == 2 ? 0 : 1;
     cudaError_t err;
+    if (c->field >= PDQ_FIELD_USER_BASE) {
+      if (c->kernel_variant == 2) return PDQ_ERROR_UNSUPPORTED;  // run-time fields: one thread per instance
+      err = pdq_launch_dense_user(a, c->field, f64, c->num_derivatives, ts1, fp, stream);
+      return err == cudaSuccess ? PDQ_SUCCESS : (err == cudaErrorInvalidSource ? PDQ_ERROR_COMPILE : PDQ_ERROR_CUDA);
+    }
     switch (c->field) {
       case PDQ_FIELD_LOTKA_VOLTERRA:
         err = f64 ? pdq_launch_dense_lv_f64(a, c->num_derivatives, ts1, fp, stream, block)

@@ -68,7 +68,8 @@ def register_field(name, source, *, dim, num_params):
     ``static constexpr int D, P`` and a generic
     ``template <typename S, typename T> PDQ_HD static void eval(const S* u, const T* p, S* out)``
     (see ``include/pdq.h``, ``pdq_register_field``).  Afterwards
-    ``ode(name, params)`` describes it (isotropic factorisation).
+    ``ode(name, params)`` describes it (isotropic and dense factorisations;
+    the dense TS1 linearisation takes its Jacobian from the same definition).
     """
     if name in _FIELD_DIMS and name in _native.FIELD and _native.FIELD[name] < 1000:
         raise ValueError(f"{name!r} is a built-in field")

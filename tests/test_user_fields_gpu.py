@@ -1,4 +1,4 @@
-"""Run-time compiled vector fields in the isotropic solver (GPU).
+"""Run-time compiled vector fields in the isotropic and dense solvers (GPU).
 
 * The Lotka--Volterra source, registered at run time, reproduces the
   built-in Lotka--Volterra kernel (same templates, same arithmetic) exactly,
@@ -67,3 +67,62 @@ def test_runtime_fields_match_the_oracle(case):
         o = res.u[-1]
         compare_record(out["u_mean"][b, -1], out["u_chol"][b, -1], o.mean, o.cholesky, out["num_steps"][b, -1],
                        res.num_steps[-1], tolerances("float64"))
+
+
+def _solve_dense(field, params, y0, save_at, precision, constraint="ts1", strategy="fixedpoint", solver="dynamic",
+                 tol=1e-6, nu=3):
+    cfg = ensemble.make_config(field=field, num_derivatives=nu, ode_dim=y0.shape[1], ssm="dense", constraint=constraint,
+                               strategy=strategy, solver=solver, precision=precision, atol=tol, rtol=tol,
+                               clip_dt=False)
+    out = ensemble.solve_ensemble(cfg, params=params, y0=y0, save_at=torch.tensor(save_at, dtype=torch.float64),
+                                  dt0=0.1, terminal_only=False)
+    torch.cuda.synchronize()
+    return {k: v.cpu() for k, v in out.items() if not k.startswith("_") and v is not None}
+
+
+def test_runtime_lotka_volterra_equals_the_builtin_dense_kernel(precision="float32"):
+    """The dense TS1 fixed-point kernel instantiated at run time for the
+    Lotka--Volterra source equals the built-in one bit for bit (float32; each
+    dense variant takes about a minute of NVRTC compilation on first use)."""
+    if "gpu_test_lv" not in _native.FIELD:
+        _native.register_field("gpu_test_lv", user_fields.LOTKA_VOLTERRA, 2, 4)
+    params, y0 = lv_instances(9, seed=11)
+    save_at = [0.0, 2.0, 5.0]
+    a = _solve_dense("lotka_volterra", params, y0, save_at, precision)
+    b = _solve_dense("gpu_test_lv", params, y0, save_at, precision)
+    for k in ("u_mean", "u_chol", "output_scale", "t", "num_steps", "num_attempts", "status"):
+        assert torch.equal(a[k], b[k]), k
+
+
+def test_runtime_lorenz_dense_ts1_matches_the_oracle():
+    """Lorenz-63 (d = 3, N = 12) in the dense factorisation with TS1 (the
+    Jacobian by dual numbers from the registered source), fixed-point
+    smoother, float64, vs the oracle with the Jacobian by torch autograd.
+    Lorenz-63 is chaotic: over [0, 0.5] the tolerances are solution 1e-7,
+    rows / covariances 1e-4, steps +-1."""
+    if "gpu_test_lorenz" not in _native.FIELD:
+        _native.register_field("gpu_test_lorenz", user_fields.LORENZ, 3, 3)
+    params = torch.tensor([[10.0, 28.0, 8.0 / 3.0], [10.0, 20.0, 2.0]], dtype=torch.float64)
+    y0 = torch.tensor([[1.0, 1.0, 1.0], [-2.0, 0.5, 10.0]], dtype=torch.float64)
+    save_at = [0.0, 0.25, 0.5]
+    out = _solve_dense("gpu_test_lorenz", params, y0, save_at, "float64")
+    assert (out["status"] == 0).all()
+    for b in range(2):
+        tc = problems.taylor_derivatives(user_fields.lorenz, y0[b], params[b], 3)
+        S = ssm.DenseSSM()
+        vf = lambda u, t, p=params[b]: user_fields.lorenz(u[0], p)  # noqa: E731
+        jac = lambda u, t, p=params[b]: problems.jacobian(user_fields.lorenz, u, p)  # noqa: E731
+        c = S.constraint_ode_ts1(vf, jac, 3)
+        res = solvers.solve_adaptive_save_at(solvers.SolverDynamic(solvers.StrategyFixedPoint(), c),
+                                             solvers.ErrorResidualStd(c), S.prior_wiener_integrated(tc), save_at,
+                                             1e-6, 1e-6, dt0=0.1)
+        steps_o = [0] + list(res.num_steps)
+        for s in range(len(save_at)):
+            o = res.u[s]
+            m, L = out["u_mean"][b, s], out["u_chol"][b, s]
+            mo, Co = o.to_multivariate_normal()
+            assert float((m[:3] - mo[:3]).abs().max() / mo[:3].abs().max()) < 1e-7
+            assert float((m - mo).abs().max() / mo.abs().max()) < 1e-4
+            C = L @ L.T
+            assert float((C - Co).abs().max() / Co.abs().max().clamp_min(1e-300)) < 1e-4
+            assert abs(int(out["num_steps"][b, s]) - steps_o[s]) <= 1
