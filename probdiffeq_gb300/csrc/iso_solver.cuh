@@ -765,14 +765,20 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
     }
   };
 
-  for (int s = 1; s < S && status == PDQ_INSTANCE_OK; ++s) {
-    const W t_next = wide_from(save_at[s], T(0));
-    bool cont = true;
-    while (cont && status == PDQ_INSTANCE_OK) {
+  // One attempt per iteration: the rejection loop and the loop over
+  // checkpoints are flattened into one, so a lane whose attempt is rejected
+  // retries in the next iteration while the other lanes of its warp go on
+  // (a nested retry loop would hold them at its exit, making every accepted
+  // step of a warp cost as many attempts as its slowest lane needs).  Per
+  // instance the sequence of attempts, checkpoint branches and records is the
+  // nested loop's (solvers_via_adaptive_steps.py:196-375).
+  int s = 1;
+  W t_next = wide_from(save_at[1], T(0));
+  while (s < S) {
       if (before(t, t_next)) {
-        // ---- rejection loop (solvers_via_adaptive_steps.py:249-328) ----
+        // ---- one attempt of the rejection loop (solvers_via_adaptive_steps.py:249-328) ----
         bool accepted = false;
-        while (!accepted) {
+        {
           const T remaining = wide_diff(t_next, t);
           const bool clipped = a.clip_dt && !(dt < remaining);
           const T dt_use = clipped ? remaining : dt;
@@ -963,8 +969,8 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
             sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
           }
         }
+        if (!accepted) continue;  // retry in the next iteration
       }
-      if (status != PDQ_INSTANCE_OK) break;
       // ---- checkpoint branch (solvers_via_adaptive_steps.py:242-247) ----
       const int s_out = a.terminal_only ? 0 : s;
       const bool record = (!a.terminal_only) || (s == S - 1);
@@ -1059,8 +1065,10 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           }
         }
       }
-      cont = before(t, t_next);
-    }
+      if (!before(t, t_next)) {  // checkpoint s done
+        ++s;
+        if (s < S) t_next = wide_from(save_at[s], T(0));
+      }
   }
 
   // ---- fixed-point backward pass: marginals at the checkpoints ----
