@@ -411,13 +411,16 @@ __global__ void __launch_bounds__(32) dense_adaptive_kernel(DenseArgs a) {
   }
   if (a.filter_mean) write_normal(a.filter_mean + (b * S) * N, a.filter_chol + (b * S) * N * N, x);
 
-  for (int s = 1; s < S && status == PDQ_INSTANCE_OK; ++s) {
-    const double t_next = save_at[s];
-    bool cont = true;
-    while (cont && status == PDQ_INSTANCE_OK) {
+  // One attempt per iteration (the retry loop flattened into the checkpoint
+  // loop): a rejected lane retries in the next iteration without holding the
+  // other instances of its warp; per instance the sequence of attempts and
+  // checkpoint branches is unchanged (solvers_via_adaptive_steps.py:196-375).
+  int s = 1;
+  double t_next = save_at[1];
+  while (s < S) {
       if (t + a.eps < t_next) {
         bool accepted = false;
-        while (!accepted) {
+        {
           const double dt_use = a.clip_dt ? fmin(dt, t_next - t) : dt;
           if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
             status = PDQ_INSTANCE_DT_UNDERFLOW;
@@ -629,8 +632,8 @@ __global__ void __launch_bounds__(32) dense_adaptive_kernel(DenseArgs a) {
             sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
           }
         }
+        if (!accepted) continue;  // retry in the next iteration
       }
-      if (status != PDQ_INSTANCE_OK) break;
       const bool record = (!a.terminal_only) || (s == S - 1);
       const int s_out = a.terminal_only ? 0 : s;
       const int64_t rec = b * S_out + s_out;
@@ -682,8 +685,10 @@ __global__ void __launch_bounds__(32) dense_adaptive_kernel(DenseArgs a) {
         }
         if (a.filter_mean) write_normal(a.filter_mean + (b * S + s) * N, a.filter_chol + (b * S + s) * N * N, x);
       }
-      cont = t + a.eps < t_next;
-    }
+      if (!(t + a.eps < t_next)) {  // checkpoint s done
+        ++s;
+        if (s < S) t_next = save_at[s];
+      }
   }
 
   // ---- finalize (solvers.py:439-480, 601-633, 735-767) ----
