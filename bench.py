@@ -549,7 +549,8 @@ def run_fhn_lml(args):
         r = lml_gradients(torch, _native, ensemble, device, reps=args.steps)
     print(json.dumps(base_line("LML grads/s", r["float32"]["grads_per_s"], "grads/s", args, r["float32"]["ms_per_batch"],
                                True, "f32 bulk + f64 log-pdf sum", dict(r["config"], workload="fitzhugh_nagumo_lml"),
-                               float64=r["float64"], gpu_launches=args.steps, clocks=clk.summary())))
+                               float64=r["float64"], gpu_launches=2 * args.steps,  # plan check + per-sample kernel
+                               clocks=clk.summary())))
 
 
 def run_vdp_dense(args):

@@ -205,7 +205,13 @@ pdq_status pdq_solve_adaptive(const pdq_config* config, const pdq_adaptive_args*
                               size_t workspace_bytes, void* stream);
 #endif
 
-/* Device scratch of pdq_lml_fixed_grid in bytes. */
+/* Device scratch of pdq_lml_fixed_grid in bytes.  Its leading part holds
+ * the covariance plan shared by all parameter samples (with TS0, the
+ * uncalibrated solver and a fixed step the covariances do not depend on the
+ * parameters), keyed by (dt, damp, num_steps, save_every, nu, precision): a
+ * call whose key equals the one stored in the workspace reuses the plan, so
+ * a caller that writes into the workspace between calls must zero its first
+ * 256 bytes. */
 #if !defined(__CUDACC_RTC__)
 pdq_status pdq_lml_workspace_size(const pdq_config* config, int64_t num_instances, int32_t num_steps, int32_t save_every,
                                   size_t* bytes);

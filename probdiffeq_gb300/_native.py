@@ -357,6 +357,9 @@ def alloc_outputs(cfg, B, S, terminal_only, device, posterior=False, num_params=
     }
 
 
+_LML_WORKSPACES = {}
+
+
 def lml_fixed_grid(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every, average_pdfs=False, gradient=True,
                    stream=None, workspace=None, outputs=None):
     """Call pdq_lml_fixed_grid on device tensors (float64, contiguous); returns (lml, grad, status)."""
@@ -373,8 +376,17 @@ def lml_fixed_grid(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every,
     nbytes = ctypes.c_size_t(0)
     check(lib.pdq_lml_workspace_size(ctypes.byref(cfg), B, num_steps, save_every, ctypes.byref(nbytes)), "pdq_lml_workspace_size")
     ws = workspace
-    if ws is None or ws.numel() * ws.element_size() < nbytes.value:
-        ws = torch.empty(max(1, nbytes.value), dtype=torch.uint8, device=dev)
+    if ws is None:
+        # one persistent workspace per device, stream and size: its leading covariance plan is
+        # reused by later calls with the same grid (a freed block could be partly rewritten by
+        # other tensors); calls on one stream are ordered, so they may share it
+        key = (str(dev), _stream_handle(stream).value, int(nbytes.value))
+        ws = _LML_WORKSPACES.get(key)
+        if ws is None:
+            ws = torch.zeros(max(1, nbytes.value), dtype=torch.uint8, device=dev)
+            _LML_WORKSPACES[key] = ws
+    elif ws.numel() * ws.element_size() < nbytes.value:
+        raise ValueError("the LML workspace is smaller than pdq_lml_workspace_size")
     a = PdqLmlArgs()
     a.num_instances, a.num_steps, a.save_every = B, num_steps, save_every
     a.average_pdfs, a.with_gradient = int(bool(average_pdfs)), int(bool(gradient))

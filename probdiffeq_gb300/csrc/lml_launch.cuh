@@ -7,7 +7,13 @@ namespace pdq {
 
 template <typename T, int NU, class F>
 cudaError_t launch_lml_nu(const LmlArgs& a, cudaStream_t stream) {
-  cudaError_t e = ensure_stack<lml_kernel<T, NU, F>>();
+  // the shared covariance plan (skipped on the device when the workspace holds it already)
+  cudaError_t e = ensure_stack<lml_plan_kernel<T, NU>>();
+  if (e != cudaSuccess) return e;
+  lml_plan_kernel<T, NU><<<1, 32, 0, stream>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = ensure_stack<lml_kernel<T, NU, F>>();
   if (e != cudaSuccess) return e;
   const int block = kLmlThreads;
   const int64_t threads = a.B * a.lanes_per_sample;

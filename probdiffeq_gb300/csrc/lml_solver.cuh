@@ -28,6 +28,22 @@
 // the 3 parameters of the configurations this needs no checkpointed
 // re-computation; the backward conditionals at the observations are stored.
 // The log-likelihood sum and its tangents are float64.
+//
+// Shared covariance plan.  With TS0 (H = e_1), the uncalibrated solver, a
+// fixed step and exact initial coefficients, every covariance-side quantity
+// of the forward pass -- predicted factors, reverts, gains, merged backward
+// conditionals -- is the same for every parameter sample and carries no
+// tangent.  lml_plan_kernel computes them once, with the same arithmetic the
+// per-sample pass used (dual numbers with zero tangents, qr_qconst /
+// givens_qconst), into a plan in the workspace: per step the update gain, the
+// revert's gain transpose, the accumulated backward A and the merge scaling;
+// per observation interval the merged conditional's A, noise factor,
+// to_latent and to_observed; the terminal factor.  lml_kernel then runs only
+// the mean recursion (matrix-vector products with the plan's tables, the
+// vector field on dual numbers) per sample and tangent: the same formulas in
+// the same order, so the values are the per-sample computation's.  The plan
+// starts with a key (dt, damp, steps, observation spacing, nu, precision) and
+// is rebuilt only when the key in the workspace differs.
 #pragma once
 
 #include "iso_solver.cuh"
@@ -56,8 +72,28 @@ struct LmlArgs {
   double* lml;           // (B,)
   double* grad;          // (B, P) or nullptr
   int32_t* status;       // (B,)
-  void* workspace;       // (B, num_obs - 1) conditionals with tangents, T
+  void* plan;            // the shared covariance plan (lml_plan_elems<T, NU> after a 256-byte key)
+  void* workspace;       // (B * lanes, num_obs - 1) backward-conditional offsets xi with tangents, T
 };
+
+// Plan layout (in T, after the 256-byte key): per step g[n], Acn[n][n] (the
+// revert's gain transpose), bwA[n][n] and Tv[n] (the accumulated backward A
+// and the merge scaling before the step); per observation interval
+// A[n][n], X[n][n], tl[n], to[n]; the terminal factor rL[n][n].
+template <int NU>
+PDQ_HD constexpr int lml_plan_step() {
+  return 2 * (NU + 1) * (NU + 1) + 2 * (NU + 1);
+}
+template <int NU>
+PDQ_HD constexpr int lml_plan_obs() {
+  return 2 * (NU + 1) * (NU + 1) + 2 * (NU + 1);
+}
+PDQ_HD int64_t lml_plan_elems(int nu, int num_steps, int save_every) {
+  const int64_t n = nu + 1;
+  const int64_t per = 2 * n * n + 2 * n;
+  return int64_t(num_steps) * per + int64_t(num_steps / save_every) * per + n * n;
+}
+constexpr int kLmlPlanKeyBytes = 256;
 
 // Householder QR (R x C, R >= C) of a dual matrix with the Q-constant tangent
 // rule: reflectors from the values; the values become R (zeros below), the
@@ -185,6 +221,152 @@ PDQ_D void lml_marginalise(const LmlCond<T, P, NU, D>& c, const Dual<T, P> (&m)[
   }
 }
 
+// The covariance side of the forward pass, once for all samples (one thread).
+template <typename T, int NU>
+__global__ void lml_plan_kernel(LmlArgs a) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  constexpr int n = NU + 1;
+  constexpr int OUT = 1;
+  using DT = Dual<T, 1>;
+  double* key = reinterpret_cast<double*>(a.plan);
+  const double want[7] = {1.2345678901234567e89, a.dt, a.damp, double(a.num_steps), double(a.save_every), double(NU),
+                          double(sizeof(T))};
+  bool same = key[7] == 1.0;
+  for (int i = 0; i < 7; ++i) same = same && __double_as_longlong(key[i]) == __double_as_longlong(want[i]);
+  if (same) return;
+  key[7] = 0.0;
+  T* const plan = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(a.plan) + kLmlPlanKeyBytes);
+  T* const obs_tbl = plan + int64_t(a.num_steps) * lml_plan_step<NU>();
+
+  DT L[n][n];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) L[i][j] = DT(T(0));
+  LmlCond<T, 1, NU, 1> bw;  // xi unused (means are per sample)
+  lml_cond_identity(bw);
+  const T h = T(a.dt);
+  T p[n], pinv[n];
+  precon<T, NU>(h, p, pinv);
+  const T sq = dev_sqrt(dev_abs(h));
+  const T damp = T(a.damp);
+  for (int step = 1; step <= a.num_steps; ++step) {
+    T* tbl = plan + int64_t(step - 1) * lml_plan_step<NU>();
+    // revert (transition.revert(marginal))
+    DT M[2 * n][2 * n];
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c) {
+        M[r][c] = DT((r <= c) ? sq * T(a.q1[c][r]) : T(0));
+        M[r][n + c] = DT(T(0));
+        DT acc(T(0));
+        for (int k = c; k < n; ++k) acc = acc + T(iwp_a<NU>(c, k)) * (dev_abs(pinv[k]) * L[k][r]);
+        M[n + r][c] = acc;
+        M[n + r][n + c] = dev_abs(pinv[c]) * L[c][r];
+      }
+    qr_qconst<T, 1, 2 * n, 2 * n>(M);
+    DT Gt[n][n];
+    for (int col = 0; col < n; ++col)
+      for (int i = n - 1; i >= 0; --i) {
+        DT acc = M[i][n + col];
+        for (int k = i + 1; k < n; ++k) acc = acc - M[i][k] * Gt[k][col];
+        Gt[i][col] = acc / M[i][i];
+      }
+    LmlCond<T, 1, NU, 1> cn;
+    DT Lp[n][n];
+    for (int i = 0; i < n; ++i) {
+      for (int j = 0; j < n; ++j) {
+        cn.A[i][j] = Gt[j][i];
+        cn.X[i][j] = M[n + j][n + i];
+        Lp[i][j] = dual_abs_scale(p[i], M[j][i]);
+      }
+      cn.tl[i] = T(1) / p[i];
+      cn.to[i] = T(1) / pinv[i];
+    }
+    // merge (ssm_impl_isotropic.py:91-105): the tables carry bw.A and Tv for the xi recursion
+    T Tv[n];
+    for (int i = 0; i < n; ++i) Tv[i] = bw.tl[i] * cn.to[i];
+    T* const g_t = tbl;
+    T* const acn_t = tbl + n;
+    T* const bwa_t = acn_t + n * n;
+    T* const tv_t = bwa_t + n * n;
+    for (int i = 0; i < n; ++i) {
+      tv_t[i] = Tv[i];
+      for (int j = 0; j < n; ++j) {
+        acn_t[i * n + j] = cn.A[i][j].v;
+        bwa_t[i * n + j] = bw.A[i][j].v;
+      }
+    }
+    {
+      DT Mm[2 * n][n];
+      LmlCond<T, 1, NU, 1> out;
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          DT g(T(0)), r1(T(0));
+          for (int k = 0; k < n; ++k) {
+            g = g + bw.A[i][k] * (Tv[k] * cn.A[k][j]);
+            r1 = r1 + bw.A[i][k] * (dev_abs(Tv[k]) * cn.X[k][j]);
+          }
+          out.A[i][j] = g;
+          Mm[j][i] = r1;
+          Mm[n + j][i] = bw.X[i][j];
+        }
+      qr_qconst<T, 1, 2 * n, n>(Mm);
+      for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) out.X[i][j] = Mm[j][i];
+        out.tl[i] = cn.tl[i];
+        out.to[i] = bw.to[i];
+      }
+      for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+          bw.A[i][j] = out.A[i][j];
+          bw.X[i][j] = out.X[i][j];
+        }
+        bw.tl[i] = out.tl[i];
+        bw.to[i] = out.to[i];
+      }
+    }
+    // update (Givens, H = e_1): the gain and the corrected factor
+    DT Mu[n + 1][n + 1];
+    for (int c = 0; c <= n; ++c) Mu[0][c] = DT(c == 0 ? damp : T(0));
+    for (int r = 1; r <= n; ++r) {
+      Mu[r][0] = Lp[OUT][r - 1];
+      for (int c = 1; c <= n; ++c) Mu[r][c] = Lp[c - 1][r - 1];
+    }
+    for (int r = OUT + 1; r >= 1; --r) givens_qconst<T, 1, n + 1, n + 1>(Mu, r - 1, r, 0);
+    for (int c = 1; c <= OUT; ++c) givens_qconst<T, 1, n + 1, n + 1>(Mu, c, c + 1, c);
+    for (int i = 0; i < n; ++i) {
+      const DT g = Mu[0][i + 1] / Mu[0][0];
+      g_t[i] = g.v;
+      for (int j = 0; j < n; ++j) L[i][j] = Mu[j + 1][i + 1];
+    }
+    // observation: the merged conditional goes to the table, reset
+    if (step % a.save_every == 0) {
+      T* o = obs_tbl + int64_t(step / a.save_every - 1) * lml_plan_obs<NU>();
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          o[i * n + j] = bw.A[i][j].v;
+          o[n * n + i * n + j] = bw.X[i][j].v;
+        }
+      for (int i = 0; i < n; ++i) {
+        o[2 * n * n + i] = bw.tl[i];
+        o[2 * n * n + n + i] = bw.to[i];
+      }
+      lml_cond_identity(bw);
+    }
+  }
+  // rv_at_t1: the terminal marginal through the (identity) conditional -- its factor
+  {
+    DT m0[n][1], rm[n][1], rL[n][n];
+    for (int i = 0; i < n; ++i) m0[i][0] = DT(T(0));
+    lml_marginalise<T, 1, NU, 1>(bw, m0, L, rm, rL);
+    T* term = obs_tbl + int64_t(a.num_steps / a.save_every) * lml_plan_obs<NU>();
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) term[i * n + j] = rL[i][j].v;
+  }
+  __threadfence();
+  for (int i = 0; i < 7; ++i) key[i] = want[i];
+  __threadfence();
+  key[7] = 1.0;
+}
+
 template <typename T, int NU, class F>
 __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
   constexpr int n = NU + 1;
@@ -195,15 +377,17 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
   using DT = Dual<T, TG>;
   using DD = Dual<double, TG>;
   // lanes_per_sample threads per parameter sample, each carrying the tangent
-  // of one parameter (the value path is computed redundantly by each)
+  // of one parameter (the mean recursion is computed by each)
   const int lanes = a.lanes_per_sample;
   const int64_t gtid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t b = gtid / lanes;
   const int dir = int(gtid % lanes);
   if (b >= a.B) return;
   const int num_obs = a.num_steps / a.save_every + 1;
-  constexpr int CF = 2 * n * n + n * D;  // duals per stored conditional (A, X, xi)
-  T* ws = reinterpret_cast<T*>(a.workspace) + gtid * int64_t(num_obs - 1) * (CF * (TG + 1) + 2 * n);
+  constexpr int XF = n * D * (TG + 1);  // numbers per stored offset xi (values and tangents)
+  T* ws = reinterpret_cast<T*>(a.workspace) + gtid * int64_t(num_obs - 1) * XF;
+  const T* const plan = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(a.plan) + kLmlPlanKeyBytes);
+  const T* const obs_tbl = plan + int64_t(a.num_steps) * lml_plan_step<NU>();
 
   // ---- parameters with unit tangents; Taylor-mode initial derivatives ----
   DD pd[P];
@@ -221,57 +405,30 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
   DD tc[n][D];
   taylor_init<F, NU>(y0, pd, tc);
 
-  DT m[n][D], L[n][n];
+  DT m[n][D], bxi[n][D];
 #pragma unroll
-  for (int i = 0; i < n; ++i) {
+  for (int i = 0; i < n; ++i)
 #pragma unroll
     for (int j = 0; j < D; ++j) {
       m[i][j].v = T(tc[i][j].v);
 #pragma unroll
       for (int k = 0; k < TG; ++k) m[i][j].g[k] = T(tc[i][j].g[k]);
+      bxi[i][j] = DT(T(0));
     }
-#pragma unroll
-    for (int j = 0; j < n; ++j) L[i][j] = DT(T(0));
-  }
-  LmlCond<T, TG, NU, D> bw;
-  lml_cond_identity(bw);
 
-  // constants of the fixed step: p, p_inv, the noise factor sqrt(dt) Q1
   const T h = T(a.dt);
   T p[n], pinv[n];
   precon<T, NU>(h, p, pinv);
-  const T sq = dev_sqrt(dev_abs(h));
-  const T damp = T(a.damp);
 
   int status = PDQ_INSTANCE_OK;
   for (int step = 1; step <= a.num_steps; ++step) {
-    // ---- fixed-point predict: transition.revert(marginal), merged into bw ----
-    DT M[2 * n][2 * n];
-#pragma unroll
-    for (int r = 0; r < n; ++r)
-#pragma unroll
-      for (int c = 0; c < n; ++c) {
-        M[r][c] = DT((r <= c) ? sq * T(a.q1[c][r]) : T(0));  // R_YX = (sqrt(dt) Q1)^T
-        M[r][n + c] = DT(T(0));
-        DT acc(T(0));
-#pragma unroll
-        for (int k = c; k < n; ++k) acc = acc + T(iwp_a<NU>(c, k)) * (dev_abs(pinv[k]) * L[k][r]);
-        M[n + r][c] = acc;                               // R_X_F = (A chol)^T
-        M[n + r][n + c] = dev_abs(pinv[c]) * L[c][r];   // R_X = chol^T
-      }
-    qr_qconst<T, TG, 2 * n, 2 * n>(M);
-    // G^T = R_Y^{-1} R12 by back substitution through the triangle
-    DT Gt[n][n];
-#pragma unroll
-    for (int col = 0; col < n; ++col)
-#pragma unroll
-      for (int i = n - 1; i >= 0; --i) {
-        DT acc = M[i][n + col];
-#pragma unroll
-        for (int k = i + 1; k < n; ++k) acc = acc - M[i][k] * Gt[k][col];
-        Gt[i][col] = acc / M[i][i];
-      }
-    DT mean_l[n][D], mobs[n][D], mp[n][D], Lp[n][n];
+    const T* tbl = plan + int64_t(step - 1) * lml_plan_step<NU>();
+    const T* g_t = tbl;
+    const T* acn_t = tbl + n;
+    const T* bwa_t = acn_t + n * n;
+    const T* tv_t = bwa_t + n * n;
+    // ---- predicted mean and the revert's offset xi = mean_l - Gt^T A1 mean_l ----
+    DT mean_l[n][D], mobs[n][D], mp[n][D];
 #pragma unroll
     for (int i = 0; i < n; ++i)
 #pragma unroll
@@ -286,157 +443,102 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
         mobs[i][j] = acc;
         mp[i][j] = p[i] * acc;
       }
-    LmlCond<T, TG, NU, D> cn;  // the new backward conditional
+    DT cxi[n][D];
 #pragma unroll
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n; ++i)
 #pragma unroll
       for (int j = 0; j < D; ++j) {
         DT acc = mean_l[i][j];
 #pragma unroll
-        for (int k = 0; k < n; ++k) acc = acc - Gt[k][i] * mobs[k][j];
-        cn.xi[i][j] = acc;
+        for (int k = 0; k < n; ++k) acc = acc - acn_t[i * n + k] * mobs[k][j];
+        cxi[i][j] = acc;
       }
+    // ---- merge: bw.xi + bw.A (Tv * xi) ----
+    DT nxi[n][D];
 #pragma unroll
-      for (int j = 0; j < n; ++j) {
-        cn.A[i][j] = Gt[j][i];
-        cn.X[i][j] = M[n + j][n + i];  // R_XY^T
-        Lp[i][j] = dual_abs_scale(p[i], M[j][i]);
+    for (int i = 0; i < n; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        DT x = bxi[i][j];
+#pragma unroll
+        for (int k = 0; k < n; ++k) x = x + bwa_t[i * n + k] * (tv_t[k] * cxi[k][j]);
+        nxi[i][j] = x;
       }
-      cn.tl[i] = T(1) / p[i];
-      cn.to[i] = T(1) / pinv[i];
-    }
-    // merge: bw <- bw.merge(cn) (ssm_impl_isotropic.py:91-105)
-    {
-      T Tv[n];
-#pragma unroll
-      for (int i = 0; i < n; ++i) Tv[i] = bw.tl[i] * cn.to[i];
-      DT Mm[2 * n][n];
-      LmlCond<T, TG, NU, D> out;
-#pragma unroll
-      for (int i = 0; i < n; ++i) {
-#pragma unroll
-        for (int j = 0; j < n; ++j) {
-          DT g(T(0)), r1(T(0));
-#pragma unroll
-          for (int k = 0; k < n; ++k) {
-            g = g + bw.A[i][k] * (Tv[k] * cn.A[k][j]);
-            r1 = r1 + bw.A[i][k] * (dev_abs(Tv[k]) * cn.X[k][j]);
-          }
-          out.A[i][j] = g;
-          Mm[j][i] = r1;
-          Mm[n + j][i] = bw.X[i][j];
-        }
-#pragma unroll
-        for (int j = 0; j < D; ++j) {
-          DT x = bw.xi[i][j];
-#pragma unroll
-          for (int k = 0; k < n; ++k) x = x + bw.A[i][k] * (Tv[k] * cn.xi[k][j]);
-          out.xi[i][j] = x;
-        }
-      }
-      qr_qconst<T, TG, 2 * n, n>(Mm);
-#pragma unroll
-      for (int i = 0; i < n; ++i) {
-#pragma unroll
-        for (int j = 0; j < n; ++j) out.X[i][j] = Mm[j][i];
-        out.tl[i] = cn.tl[i];
-        out.to[i] = bw.to[i];
-      }
-      bw = out;
-    }
-    // ---- TS0 linearisation at the predicted mean; update (Givens, H = e_1) ----
+    // ---- TS0 linearisation at the predicted mean; update with the plan's gain ----
     DT f[D];
     F::eval(mp[0], pt, f);
-    DT Mu[n + 1][n + 1];
-#pragma unroll
-    for (int c = 0; c <= n; ++c) Mu[0][c] = DT(c == 0 ? damp : T(0));
-#pragma unroll
-    for (int r = 1; r <= n; ++r) {
-      Mu[r][0] = Lp[OUT][r - 1];
-#pragma unroll
-      for (int c = 1; c <= n; ++c) Mu[r][c] = Lp[c - 1][r - 1];
-    }
-#pragma unroll
-    for (int r = OUT + 1; r >= 1; --r) givens_qconst<T, TG, n + 1, n + 1>(Mu, r - 1, r, 0);
-#pragma unroll
-    for (int c = 1; c <= OUT; ++c) givens_qconst<T, TG, n + 1, n + 1>(Mu, c, c + 1, c);
     DT res[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) res[j] = mp[OUT][j] - f[j];
 #pragma unroll
     for (int i = 0; i < n; ++i) {
-      const DT g = Mu[0][i + 1] / Mu[0][0];
+      const T g = g_t[i];
 #pragma unroll
-      for (int j = 0; j < D; ++j) m[i][j] = mp[i][j] - g * res[j];
-#pragma unroll
-      for (int j = 0; j < n; ++j) L[i][j] = Mu[j + 1][i + 1];
+      for (int j = 0; j < D; ++j) {
+        m[i][j] = mp[i][j] - g * res[j];
+        bxi[i][j] = nxi[i][j];
+      }
     }
     if (!(m[0][0].v == m[0][0].v)) {
       status = PDQ_INSTANCE_NONFINITE;
       break;
     }
-    // ---- checkpoint at an observation: store the conditional, reset ----
+    // ---- checkpoint at an observation: store the offset, reset ----
     if (step % a.save_every == 0) {
-      T* dst = ws + int64_t(step / a.save_every - 1) * (CF * (TG + 1) + 2 * n);
+      T* dst = ws + int64_t(step / a.save_every - 1) * XF;
       int o = 0;
 #pragma unroll
       for (int i = 0; i < n; ++i)
 #pragma unroll
-        for (int j = 0; j < n; ++j) {
-          dst[o++] = bw.A[i][j].v;
-#pragma unroll
-          for (int k = 0; k < TG; ++k) dst[o++] = bw.A[i][j].g[k];
-          dst[o++] = bw.X[i][j].v;
-#pragma unroll
-          for (int k = 0; k < TG; ++k) dst[o++] = bw.X[i][j].g[k];
-        }
-#pragma unroll
-      for (int i = 0; i < n; ++i)
-#pragma unroll
         for (int j = 0; j < D; ++j) {
-          dst[o++] = bw.xi[i][j].v;
+          dst[o++] = bxi[i][j].v;
 #pragma unroll
-          for (int k = 0; k < TG; ++k) dst[o++] = bw.xi[i][j].g[k];
+          for (int k = 0; k < TG; ++k) dst[o++] = bxi[i][j].g[k];
+          bxi[i][j] = DT(T(0));
         }
-#pragma unroll
-      for (int i = 0; i < n; ++i) {
-        dst[o++] = bw.tl[i];
-        dst[o++] = bw.to[i];
-      }
-      lml_cond_identity(bw);
     }
   }
 
   // ---- LML: reverse Kalman filter over the data (evaluate_lml) ----
   DD pdf(0.0);
   if (status == PDQ_INSTANCE_OK) {
-    // rv_at_t1 = posterior1.conditional.marginalise(marginal); the last step
-    // lands on the last observation, so that conditional is the identity
+    // rv_at_t1: the last step lands on the last observation, so the
+    // conditional is the identity: the mean is m, the factor the plan's
     DT rm[n][D], rL[n][n];
-    lml_marginalise<T, TG, NU, D>(bw, m, L, rm, rL);
+    const T* term = obs_tbl + int64_t(num_obs - 1) * lml_plan_obs<NU>();
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) rm[i][j] = m[i][j];
+#pragma unroll
+      for (int j = 0; j < n; ++j) rL[i][j] = DT(term[i * n + j]);
+    }
     const double LOG2PI = 1.8378770664093453;
     int num = 0;
     for (int k = num_obs - 1; k >= 0; --k) {
       if (k < num_obs - 1) {
         LmlCond<T, TG, NU, D> c;
-        const T* src = ws + int64_t(k) * (CF * (TG + 1) + 2 * n);
-        int o = 0;
-        for (int i = 0; i < n; ++i)
-          for (int j = 0; j < n; ++j) {
-            c.A[i][j].v = src[o++];
-            for (int q = 0; q < TG; ++q) c.A[i][j].g[q] = src[o++];
-            c.X[i][j].v = src[o++];
-            for (int q = 0; q < TG; ++q) c.X[i][j].g[q] = src[o++];
-          }
-        for (int i = 0; i < n; ++i)
-          for (int j = 0; j < D; ++j) {
-            c.xi[i][j].v = src[o++];
-            for (int q = 0; q < TG; ++q) c.xi[i][j].g[q] = src[o++];
-          }
+        const T* o = obs_tbl + int64_t(k) * lml_plan_obs<NU>();
+        const T* src = ws + int64_t(k) * XF;
+#pragma unroll
         for (int i = 0; i < n; ++i) {
-          c.tl[i] = src[o++];
-          c.to[i] = src[o++];
+#pragma unroll
+          for (int j = 0; j < n; ++j) {
+            c.A[i][j] = DT(o[i * n + j]);
+            c.X[i][j] = DT(o[n * n + i * n + j]);
+          }
+          c.tl[i] = o[2 * n * n + i];
+          c.to[i] = o[2 * n * n + n + i];
         }
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < n; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) {
+            c.xi[i][j].v = src[q++];
+#pragma unroll
+            for (int t = 0; t < TG; ++t) c.xi[i][j].g[t] = src[q++];
+          }
         DT pm[n][D], pL[n][n];
         lml_marginalise<T, TG, NU, D>(c, rm, rL, pm, pL);
 #pragma unroll

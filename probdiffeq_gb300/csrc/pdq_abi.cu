@@ -459,13 +459,22 @@ static pdq_status lml_check(const pdq_config* c, int64_t B, int32_t num_steps, i
 
 static int lml_num_params(const pdq_config* c) { return c->field == PDQ_FIELD_FITZHUGH_NAGUMO ? 3 : 4; }
 
+// Workspace: the shared covariance plan (key + tables, rounded to 256 bytes),
+// then per thread (P threads per sample, one tangent each) the backward
+// conditionals' offsets xi (values and tangents) at the observations.
+static size_t lml_plan_bytes(const pdq_config* c, int32_t num_steps, int32_t save_every) {
+  const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
+  const size_t raw = size_t(pdq::kLmlPlanKeyBytes) +
+                     size_t(pdq::lml_plan_elems(c->num_derivatives, num_steps, save_every)) * elem;
+  return (raw + 255) / 256 * 256;
+}
+
 static size_t lml_bytes(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every) {
   const int n = c->num_derivatives + 1, d = c->ode_dim;
   const int P = lml_num_params(c);
-  // per thread (P threads per sample, one tangent each) and stored conditional
-  const size_t per = size_t(2 * n * n + n * d) * 2 + 2 * n;
+  const size_t per = size_t(n) * d * 2;
   const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
-  return size_t(B) * size_t(P) * size_t(num_steps / save_every) * per * elem;
+  return lml_plan_bytes(c, num_steps, save_every) + size_t(B) * size_t(P) * size_t(num_steps / save_every) * per * elem;
 }
 
 pdq_status pdq_lml_workspace_size(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every, size_t* bytes) {
@@ -506,7 +515,8 @@ pdq_status pdq_lml_fixed_grid(const pdq_config* c, const pdq_lml_args* args, voi
   a.lml = args->lml;
   a.grad = args->with_gradient ? args->grad : nullptr;
   a.status = args->status;
-  a.workspace = workspace;
+  a.plan = workspace;
+  a.workspace = static_cast<unsigned char*>(workspace) + lml_plan_bytes(c, args->num_steps, args->save_every);
   cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
   cudaError_t err;
   if (c->field == PDQ_FIELD_FITZHUGH_NAGUMO)
