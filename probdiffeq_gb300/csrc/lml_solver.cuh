@@ -38,12 +38,16 @@
 // givens_qconst), into a plan in the workspace: per step the update gain, the
 // revert's gain transpose, the accumulated backward A and the merge scaling;
 // per observation interval the merged conditional's A, noise factor,
-// to_latent and to_observed; the terminal factor.  lml_kernel then runs only
-// the mean recursion (matrix-vector products with the plan's tables, the
-// vector field on dual numbers) per sample and tangent: the same formulas in
-// the same order, so the values are the per-sample computation's.  The plan
-// starts with a key (dt, damp, steps, observation spacing, nu, precision) and
-// is rebuilt only when the key in the workspace differs.
+// to_latent and to_observed; the terminal factor; the backward pass's
+// covariance side (it depends on the observation noise std but not on the
+// parameters): per observation the observed std ry and the gain column.
+// lml_kernel then runs only the mean recursion (matrix-vector products with
+// the plan's tables, staged through shared memory a chunk of steps at a time
+// by the warp, the vector field on dual numbers) per sample and tangent: the
+// same formulas in the same order, so the values are the per-sample
+// computation's.  The plan starts with a key (dt, damp, steps, observation
+// spacing, nu, precision, and a copy of std) and is rebuilt only when the
+// key in the workspace differs.
 #pragma once
 
 #include "iso_solver.cuh"
@@ -79,7 +83,11 @@ struct LmlArgs {
 // Plan layout (in T, after the 256-byte key): per step g[n], Acn[n][n] (the
 // revert's gain transpose), bwA[n][n] and Tv[n] (the accumulated backward A
 // and the merge scaling before the step); per observation interval
-// A[n][n], X[n][n], tl[n], to[n]; the terminal factor rL[n][n].
+// A[n][n], X[n][n], tl[n], to[n]; the terminal factor rL[n][n]; per
+// observation ry and ginv[n]; then (8-byte aligned) the std the plan was
+// built for, in double.
+constexpr int kLmlPlanKeyBytes = 256;
+
 template <int NU>
 PDQ_HD constexpr int lml_plan_step() {
   return 2 * (NU + 1) * (NU + 1) + 2 * (NU + 1);
@@ -91,9 +99,23 @@ PDQ_HD constexpr int lml_plan_obs() {
 PDQ_HD int64_t lml_plan_elems(int nu, int num_steps, int save_every) {
   const int64_t n = nu + 1;
   const int64_t per = 2 * n * n + 2 * n;
-  return int64_t(num_steps) * per + int64_t(num_steps / save_every) * per + n * n;
+  const int64_t num_obs = num_steps / save_every + 1;
+  return int64_t(num_steps) * per + (num_obs - 1) * per + n * n + num_obs * (n + 1);
 }
-constexpr int kLmlPlanKeyBytes = 256;
+// Offset in bytes (from the plan's start, key included) of the std copy.
+PDQ_HD int64_t lml_plan_std_offset(int nu, int num_steps, int save_every, int elem) {
+  const int64_t raw = kLmlPlanKeyBytes + lml_plan_elems(nu, num_steps, save_every) * elem;
+  return (raw + 7) / 8 * 8;
+}
+// Plan bytes in total (key, tables, std copy), a multiple of 256.
+PDQ_HD int64_t lml_plan_total_bytes(int nu, int num_steps, int save_every, int elem) {
+  const int64_t num_obs = num_steps / save_every + 1;
+  const int64_t raw = lml_plan_std_offset(nu, num_steps, save_every, elem) + num_obs * 8;
+  return (raw + 255) / 256 * 256;
+}
+// Steps of plan tables staged in shared memory at a time.
+constexpr int kLmlChunk = 32;
+
 
 // Householder QR (R x C, R >= C) of a dual matrix with the Q-constant tangent
 // rule: reflectors from the values; the values become R (zeros below), the
@@ -231,8 +253,12 @@ __global__ void lml_plan_kernel(LmlArgs a) {
   double* key = reinterpret_cast<double*>(a.plan);
   const double want[7] = {1.2345678901234567e89, a.dt, a.damp, double(a.num_steps), double(a.save_every), double(NU),
                           double(sizeof(T))};
+  const int num_obs = a.num_steps / a.save_every + 1;
+  double* const std_copy = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(a.plan) +
+                                                     lml_plan_std_offset(NU, a.num_steps, a.save_every, int(sizeof(T))));
   bool same = key[7] == 1.0;
   for (int i = 0; i < 7; ++i) same = same && __double_as_longlong(key[i]) == __double_as_longlong(want[i]);
+  for (int k = 0; same && k < num_obs; ++k) same = __double_as_longlong(std_copy[k]) == __double_as_longlong(a.std[k]);
   if (same) return;
   key[7] = 0.0;
   T* const plan = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(a.plan) + kLmlPlanKeyBytes);
@@ -353,14 +379,48 @@ __global__ void lml_plan_kernel(LmlArgs a) {
     }
   }
   // rv_at_t1: the terminal marginal through the (identity) conditional -- its factor
-  {
-    DT m0[n][1], rm[n][1], rL[n][n];
-    for (int i = 0; i < n; ++i) m0[i][0] = DT(T(0));
-    lml_marginalise<T, 1, NU, 1>(bw, m0, L, rm, rL);
-    T* term = obs_tbl + int64_t(a.num_steps / a.save_every) * lml_plan_obs<NU>();
+  DT m0[n][1], rm[n][1], rL[n][n];
+  for (int i = 0; i < n; ++i) m0[i][0] = DT(T(0));
+  lml_marginalise<T, 1, NU, 1>(bw, m0, L, rm, rL);
+  T* const term = obs_tbl + int64_t(num_obs - 1) * lml_plan_obs<NU>();
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) term[i * n + j] = rL[i][j].v;
+  // the backward pass's covariance side: marginalise through each stored
+  // conditional, then bayes_rule with to_derivative(0, std_k) (Givens)
+  T* const bay = term + n * n;
+  for (int k = num_obs - 1; k >= 0; --k) {
+    if (k < num_obs - 1) {
+      LmlCond<T, 1, NU, 1> c;
+      const T* o = obs_tbl + int64_t(k) * lml_plan_obs<NU>();
+      for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+          c.A[i][j] = DT(o[i * n + j]);
+          c.X[i][j] = DT(o[n * n + i * n + j]);
+        }
+        c.xi[i][0] = DT(T(0));
+        c.tl[i] = o[2 * n * n + i];
+        c.to[i] = o[2 * n * n + n + i];
+      }
+      DT pm[n][1], pL[n][n];
+      lml_marginalise<T, 1, NU, 1>(c, m0, rL, pm, pL);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) rL[i][j] = pL[i][j];
+    }
+    const T sk = T(a.std[k]);
+    DT Mo[n + 1][n + 1];
+    for (int c = 0; c <= n; ++c) Mo[0][c] = DT(c == 0 ? sk : T(0));
+    for (int r = 1; r <= n; ++r) {
+      Mo[r][0] = rL[0][r - 1];
+      for (int c = 1; c <= n; ++c) Mo[r][c] = rL[c - 1][r - 1];
+    }
+    givens_qconst<T, 1, n + 1, n + 1>(Mo, 0, 1, 0);
+    const DT ry = Mo[0][0];
+    bay[k * (n + 1)] = ry.v;
+    for (int i = 0; i < n; ++i) bay[k * (n + 1) + 1 + i] = (Mo[0][i + 1] / ry).v;
     for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) term[i * n + j] = rL[i][j].v;
+      for (int j = 0; j < n; ++j) rL[i][j] = Mo[j + 1][i + 1];
   }
+  for (int k = 0; k < num_obs; ++k) std_copy[k] = a.std[k];
   __threadfence();
   for (int i = 0; i < 7; ++i) key[i] = want[i];
   __threadfence();
@@ -380,14 +440,18 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
   // of one parameter (the mean recursion is computed by each)
   const int lanes = a.lanes_per_sample;
   const int64_t gtid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int64_t b = gtid / lanes;
+  // threads past the batch stay for the warp's cooperative staging of the plan
+  const bool valid = gtid < a.B * lanes;
+  const int64_t b = valid ? gtid / lanes : 0;
   const int dir = int(gtid % lanes);
-  if (b >= a.B) return;
+  const int lane = threadIdx.x & 31;
   const int num_obs = a.num_steps / a.save_every + 1;
   constexpr int XF = n * D * (TG + 1);  // numbers per stored offset xi (values and tangents)
-  T* ws = reinterpret_cast<T*>(a.workspace) + gtid * int64_t(num_obs - 1) * XF;
+  T* ws = reinterpret_cast<T*>(a.workspace) + (valid ? gtid : 0) * int64_t(num_obs - 1) * XF;
   const T* const plan = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(a.plan) + kLmlPlanKeyBytes);
   const T* const obs_tbl = plan + int64_t(a.num_steps) * lml_plan_step<NU>();
+  constexpr int kStep = lml_plan_step<NU>();
+  __shared__ T stage[kLmlChunk * kStep];  // one warp per block
 
   // ---- parameters with unit tangents; Taylor-mode initial derivatives ----
   DD pd[P];
@@ -422,7 +486,17 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
 
   int status = PDQ_INSTANCE_OK;
   for (int step = 1; step <= a.num_steps; ++step) {
-    const T* tbl = plan + int64_t(step - 1) * lml_plan_step<NU>();
+    const int within = (step - 1) % kLmlChunk;
+    if (within == 0) {
+      // stage the next chunk of step tables (coalesced, the whole warp)
+      const int count = min(kLmlChunk, a.num_steps - (step - 1)) * kStep;
+      const T* src = plan + int64_t(step - 1) * kStep;
+      __syncwarp();
+      for (int e = lane; e < count; e += 32) stage[e] = src[e];
+      __syncwarp();
+    }
+    if (!valid || status != PDQ_INSTANCE_OK) continue;
+    const T* tbl = stage + within * kStep;
     const T* g_t = tbl;
     const T* acn_t = tbl + n;
     const T* bwa_t = acn_t + n * n;
@@ -480,8 +554,8 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       }
     }
     if (!(m[0][0].v == m[0][0].v)) {
-      status = PDQ_INSTANCE_NONFINITE;
-      break;
+      status = PDQ_INSTANCE_NONFINITE;  // stays in the loop for the staging
+      continue;
     }
     // ---- checkpoint at an observation: store the offset, reset ----
     if (step % a.save_every == 0) {
@@ -499,90 +573,58 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
     }
   }
 
+  if (!valid) return;
   // ---- LML: reverse Kalman filter over the data (evaluate_lml) ----
   DD pdf(0.0);
   if (status == PDQ_INSTANCE_OK) {
     // rv_at_t1: the last step lands on the last observation, so the
-    // conditional is the identity: the mean is m, the factor the plan's
-    DT rm[n][D], rL[n][n];
-    const T* term = obs_tbl + int64_t(num_obs - 1) * lml_plan_obs<NU>();
+    // conditional is the identity and the mean is m; the covariance side
+    // (marginalise, bayes_rule) comes from the plan
+    DT rm[n][D];
 #pragma unroll
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n; ++i)
 #pragma unroll
       for (int j = 0; j < D; ++j) rm[i][j] = m[i][j];
-#pragma unroll
-      for (int j = 0; j < n; ++j) rL[i][j] = DT(term[i * n + j]);
-    }
+    const T* const bay = obs_tbl + int64_t(num_obs - 1) * lml_plan_obs<NU>() + n * n;
     const double LOG2PI = 1.8378770664093453;
     int num = 0;
     for (int k = num_obs - 1; k >= 0; --k) {
       if (k < num_obs - 1) {
-        LmlCond<T, TG, NU, D> c;
+        // cond.marginalise (ssm_impl_isotropic.py:81-89), mean part
         const T* o = obs_tbl + int64_t(k) * lml_plan_obs<NU>();
         const T* src = ws + int64_t(k) * XF;
-#pragma unroll
-        for (int i = 0; i < n; ++i) {
-#pragma unroll
-          for (int j = 0; j < n; ++j) {
-            c.A[i][j] = DT(o[i * n + j]);
-            c.X[i][j] = DT(o[n * n + i * n + j]);
-          }
-          c.tl[i] = o[2 * n * n + i];
-          c.to[i] = o[2 * n * n + n + i];
-        }
-        int q = 0;
+        DT pm[n][D];
 #pragma unroll
         for (int i = 0; i < n; ++i)
 #pragma unroll
           for (int j = 0; j < D; ++j) {
-            c.xi[i][j].v = src[q++];
+            DT acc;
+            acc.v = src[(i * D + j) * (TG + 1)];
 #pragma unroll
-            for (int t = 0; t < TG; ++t) c.xi[i][j].g[t] = src[q++];
+            for (int t = 0; t < TG; ++t) acc.g[t] = src[(i * D + j) * (TG + 1) + 1 + t];
+#pragma unroll
+            for (int q = 0; q < n; ++q) acc = acc + o[i * n + q] * (o[2 * n * n + q] * rm[q][j]);
+            pm[i][j] = o[2 * n * n + n + i] * acc;
           }
-        DT pm[n][D], pL[n][n];
-        lml_marginalise<T, TG, NU, D>(c, rm, rL, pm, pL);
 #pragma unroll
-        for (int i = 0; i < n; ++i) {
+        for (int i = 0; i < n; ++i)
 #pragma unroll
           for (int j = 0; j < D; ++j) rm[i][j] = pm[i][j];
-#pragma unroll
-          for (int j = 0; j < n; ++j) rL[i][j] = pL[i][j];
-        }
       }
       // model_k = to_derivative(0, std_k); bayes_rule_and_logpdf_tree
-      const T s = T(a.std[k]);
-      DT Mo[n + 1][n + 1];
-#pragma unroll
-      for (int c = 0; c <= n; ++c) Mo[0][c] = DT(c == 0 ? s : T(0));
-#pragma unroll
-      for (int r = 1; r <= n; ++r) {
-        Mo[r][0] = rL[0][r - 1];
-#pragma unroll
-        for (int c = 1; c <= n; ++c) Mo[r][c] = rL[c - 1][r - 1];
-      }
-      givens_qconst<T, TG, n + 1, n + 1>(Mo, 0, 1, 0);
-      const DT ry = Mo[0][0];
-      // logpdf of the observed N(m[0], ry^2) at the data, summed over d
+      const T ry = bay[k * (n + 1)];
       DD pdf_n(0.0);
-      DT ginv[n];
-#pragma unroll
-      for (int i = 0; i < n; ++i) ginv[i] = Mo[0][i + 1] / ry;
-      const T ryv = ry.v < T(0) ? -ry.v : ry.v;
+      const T ryv = ry < T(0) ? -ry : ry;
 #pragma unroll
       for (int j = 0; j < D; ++j) {
         const DT dx = DT(T(a.data[int64_t(k) * D + j])) - rm[0][j];
         const DT w = dx / ry;
         pdf_n.v += -0.5 * (2.0 * log(double(ryv)) + double(w.v) * double(w.v) + LOG2PI);
 #pragma unroll
-        for (int q = 0; q < TG; ++q)
-          pdf_n.g[q] += -0.5 * (2.0 * double(ry.g[q]) / double(ry.v) + 2.0 * double(w.v) * double(w.g[q]));
+        for (int q = 0; q < TG; ++q) pdf_n.g[q] += -0.5 * (2.0 * double(w.v) * double(w.g[q]));
 #pragma unroll
-        for (int i = 0; i < n; ++i) rm[i][j] = rm[i][j] + ginv[i] * dx;
+        for (int i = 0; i < n; ++i) rm[i][j] = rm[i][j] + bay[k * (n + 1) + 1 + i] * dx;
       }
-#pragma unroll
-      for (int i = 0; i < n; ++i)
-#pragma unroll
-        for (int j = 0; j < n; ++j) rL[i][j] = Mo[j + 1][i + 1];
       if (a.average_pdfs && num > 0) {
         pdf.v = (pdf.v * num + pdf_n.v) / (num + 1);
 #pragma unroll

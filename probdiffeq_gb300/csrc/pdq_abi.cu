@@ -463,10 +463,8 @@ static int lml_num_params(const pdq_config* c) { return c->field == PDQ_FIELD_FI
 // then per thread (P threads per sample, one tangent each) the backward
 // conditionals' offsets xi (values and tangents) at the observations.
 static size_t lml_plan_bytes(const pdq_config* c, int32_t num_steps, int32_t save_every) {
-  const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
-  const size_t raw = size_t(pdq::kLmlPlanKeyBytes) +
-                     size_t(pdq::lml_plan_elems(c->num_derivatives, num_steps, save_every)) * elem;
-  return (raw + 255) / 256 * 256;
+  const int elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
+  return size_t(pdq::lml_plan_total_bytes(c->num_derivatives, num_steps, save_every, elem));
 }
 
 static size_t lml_bytes(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every) {
