@@ -85,7 +85,7 @@ struct LmlArgs {
 // and the merge scaling before the step); per observation interval
 // A[n][n], X[n][n], tl[n], to[n]; the terminal factor rL[n][n]; per
 // observation ry and ginv[n]; then (8-byte aligned) the std the plan was
-// built for, in double.
+// built for and log|ry| per observation, in double.
 constexpr int kLmlPlanKeyBytes = 256;
 
 template <int NU>
@@ -107,10 +107,10 @@ PDQ_HD int64_t lml_plan_std_offset(int nu, int num_steps, int save_every, int el
   const int64_t raw = kLmlPlanKeyBytes + lml_plan_elems(nu, num_steps, save_every) * elem;
   return (raw + 7) / 8 * 8;
 }
-// Plan bytes in total (key, tables, std copy), a multiple of 256.
+// Plan bytes in total (key, tables, std copy, log|ry|), a multiple of 256.
 PDQ_HD int64_t lml_plan_total_bytes(int nu, int num_steps, int save_every, int elem) {
   const int64_t num_obs = num_steps / save_every + 1;
-  const int64_t raw = lml_plan_std_offset(nu, num_steps, save_every, elem) + num_obs * 8;
+  const int64_t raw = lml_plan_std_offset(nu, num_steps, save_every, elem) + 2 * num_obs * 8;
   return (raw + 255) / 256 * 256;
 }
 // Steps of plan tables staged in shared memory at a time.
@@ -416,6 +416,7 @@ __global__ void lml_plan_kernel(LmlArgs a) {
     givens_qconst<T, 1, n + 1, n + 1>(Mo, 0, 1, 0);
     const DT ry = Mo[0][0];
     bay[k * (n + 1)] = ry.v;
+    std_copy[num_obs + k] = log(double(ry.v < T(0) ? -ry.v : ry.v));  // log|ry| in double
     for (int i = 0; i < n; ++i) bay[k * (n + 1) + 1 + i] = (Mo[0][i + 1] / ry).v;
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j) rL[i][j] = Mo[j + 1][i + 1];
@@ -586,6 +587,9 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
 #pragma unroll
       for (int j = 0; j < D; ++j) rm[i][j] = m[i][j];
     const T* const bay = obs_tbl + int64_t(num_obs - 1) * lml_plan_obs<NU>() + n * n;
+    const double* const logry = reinterpret_cast<const double*>(
+                                    reinterpret_cast<const unsigned char*>(a.plan) +
+                                    lml_plan_std_offset(NU, a.num_steps, a.save_every, int(sizeof(T)))) + num_obs;
     const double LOG2PI = 1.8378770664093453;
     int num = 0;
     for (int k = num_obs - 1; k >= 0; --k) {
@@ -613,13 +617,13 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       }
       // model_k = to_derivative(0, std_k); bayes_rule_and_logpdf_tree
       const T ry = bay[k * (n + 1)];
+      const double lr = logry[k];
       DD pdf_n(0.0);
-      const T ryv = ry < T(0) ? -ry : ry;
 #pragma unroll
       for (int j = 0; j < D; ++j) {
         const DT dx = DT(T(a.data[int64_t(k) * D + j])) - rm[0][j];
         const DT w = dx / ry;
-        pdf_n.v += -0.5 * (2.0 * log(double(ryv)) + double(w.v) * double(w.v) + LOG2PI);
+        pdf_n.v += -0.5 * (2.0 * lr + double(w.v) * double(w.v) + LOG2PI);
 #pragma unroll
         for (int q = 0; q < TG; ++q) pdf_n.g[q] += -0.5 * (2.0 * double(w.v) * double(w.g[q]));
 #pragma unroll
