@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
   const T* const plan = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(a.plan) + kLmlPlanKeyBytes);
   const T* const obs_tbl = plan + int64_t(a.num_steps) * lml_plan_step<NU>();
   constexpr int kStep = lml_plan_step<NU>();
-  __shared__ T stage[kLmlChunk * kStep];  // one warp per block
+  __shared__ __align__(16) T stage[kLmlChunk * kStep];  // one warp per block
 
   // ---- parameters with unit tangents; Taylor-mode initial derivatives ----
   DD pd[P];
@@ -497,9 +497,36 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       __syncwarp();
     }
     if (!valid || status != PDQ_INSTANCE_OK) continue;
-    const T* tbl = stage + within * kStep;
-    const T* g_t = tbl;
-    const T* acn_t = tbl + n;
+    // this step's tables into registers in one batch of 16-byte loads, so
+    // their latency overlaps instead of preceding each use
+    T tb[kStep];
+    {
+      const T* tbl = stage + within * kStep;
+      if constexpr (sizeof(T) == 4 && kStep % 4 == 0) {
+        const float4* v = reinterpret_cast<const float4*>(tbl);
+#pragma unroll
+        for (int e = 0; e < kStep / 4; ++e) {
+          const float4 x = v[e];
+          tb[4 * e] = x.x;
+          tb[4 * e + 1] = x.y;
+          tb[4 * e + 2] = x.z;
+          tb[4 * e + 3] = x.w;
+        }
+      } else if constexpr (sizeof(T) == 8 && kStep % 2 == 0) {
+        const double2* v = reinterpret_cast<const double2*>(tbl);
+#pragma unroll
+        for (int e = 0; e < kStep / 2; ++e) {
+          const double2 x = v[e];
+          tb[2 * e] = x.x;
+          tb[2 * e + 1] = x.y;
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < kStep; ++e) tb[e] = tbl[e];
+      }
+    }
+    const T* g_t = tb;
+    const T* acn_t = tb + n;
     const T* bwa_t = acn_t + n * n;
     const T* tv_t = bwa_t + n * n;
     // ---- predicted mean and the revert's offset xi = mean_l - Gt^T A1 mean_l ----
