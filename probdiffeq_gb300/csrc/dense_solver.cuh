@@ -418,277 +418,277 @@ __global__ void __launch_bounds__(32) dense_adaptive_kernel(DenseArgs a) {
   int s = 1;
   double t_next = save_at[1];
   while (s < S) {
-      if (t + a.eps < t_next) {
-        bool accepted = false;
-        {
-          const double dt_use = a.clip_dt ? fmin(dt, t_next - t) : dt;
-          if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
-            status = PDQ_INSTANCE_DT_UNDERFLOW;
-            break;
-          }
-          if (attempts >= a.max_attempts) {
-            status = PDQ_INSTANCE_MAX_STEPS;
-            break;
-          }
-          ++attempts;
-          const T h = T(dt_use);
-          T p[N], pinv[N];
-          dense_precon<T, NU, D>(h, p, pinv);
-          // u = transition(h, 1).apply_flat(mean): mean mp, chol |p| sqrt|h| Q
-          T mp[N];
+    if (t + a.eps < t_next) {
+      bool accepted = false;
+      {
+        const double dt_use = a.clip_dt ? fmin(dt, t_next - t) : dt;
+        if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
+          status = PDQ_INSTANCE_DT_UNDERFLOW;
+          break;
+        }
+        if (attempts >= a.max_attempts) {
+          status = PDQ_INSTANCE_MAX_STEPS;
+          break;
+        }
+        ++attempts;
+        const T h = T(dt_use);
+        T p[N], pinv[N];
+        dense_precon<T, NU, D>(h, p, pinv);
+        // u = transition(h, 1).apply_flat(mean): mean mp, chol |p| sqrt|h| Q
+        T mp[N];
 #pragma unroll
-          for (int i = 0; i < N; ++i) {
+        for (int i = 0; i < N; ++i) {
+          T acc = T(0);
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            if (k % D == i % D) acc += T(iwp_a<NU>(i / D, k / D)) * pinv[k] * x.m[k];
+          mp[i] = p[i] * acc;
+        }
+        DLin<T, N, D> fx;
+        dense_linearize<T, NU, F, TS1>(mp, pt, fx);
+        // observed = fx.marginalise(u): mean r = J mp + b, chol from qr of [(J Lu)^T; damp I]
+        T r[D];
+#pragma unroll
+        for (int aa = 0; aa < D; ++aa) {
+          T acc = fx.b[aa];
+#pragma unroll
+          for (int k = 0; k < N; ++k) acc += fx.J[aa][k] * mp[k];
+          r[aa] = acc;
+        }
+        T Mo[N + D][D];
+        const T sqh = dev_sqrt(dev_abs(h));
+#pragma unroll
+        for (int rr = 0; rr < N; ++rr)
+#pragma unroll
+          for (int aa = 0; aa < D; ++aa) {
+            // (J Lu)[aa][rr], Lu = |p| sqrt|h| Q
             T acc = T(0);
 #pragma unroll
             for (int k = 0; k < N; ++k)
-              if (k % D == i % D) acc += T(iwp_a<NU>(i / D, k / D)) * pinv[k] * x.m[k];
-            mp[i] = p[i] * acc;
+              if (k % D == rr % D && rr / D <= k / D) acc += fx.J[aa][k] * dev_abs(p[k]) * sqh * T(a.q1[k / D][rr / D]);
+            Mo[rr][aa] = acc;
           }
-          DLin<T, N, D> fx;
-          dense_linearize<T, NU, F, TS1>(mp, pt, fx);
-          // observed = fx.marginalise(u): mean r = J mp + b, chol from qr of [(J Lu)^T; damp I]
-          T r[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) Mo[N + i][j] = (i == j) ? damp : T(0);
+        householder_r<T, N + D, D>(Mo);
+        // observed chol Lo = R^T (lower); sigma = ||Lo^{-1} r|| / sqrt(d)
+        T w[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          T acc = r[i];
+#pragma unroll
+          for (int k = 0; k < i; ++k) acc -= Mo[k][i] * w[k];
+          w[i] = dev_div(acc, Mo[i][i]);
+        }
+        T ww = T(0);
+#pragma unroll
+        for (int i = 0; i < D; ++i) ww += w[i] * w[i];
+        const T sigma_loc = dev_sqrt(ww * T(1.0 / D));
+
+        const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
+        DNormal<T, N> pred;
+        DCond<T, N> cnew, merged;
+        if constexpr (FP) {
+          prior_revert<T, NU, D>(a.q1, x, h, s_pred, pred, cnew);
+          cond_merge<T, N>(bw, cnew, merged);
+        } else {
+          prior_marginalise<T, NU, D>(a.q1, x, h, s_pred, pred);
+        }
+        // update: fx.revert(pred): M2 = [[damp I, 0], [(J Lp)^T, Lp^T]]
+        T M2[D + N][D + N];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = 0; j < D + N; ++j) M2[i][j] = (i == j) ? damp : T(0);
+#pragma unroll
+        for (int rr = 0; rr < N; ++rr) {
 #pragma unroll
           for (int aa = 0; aa < D; ++aa) {
-            T acc = fx.b[aa];
+            T acc = T(0);
 #pragma unroll
-            for (int k = 0; k < N; ++k) acc += fx.J[aa][k] * mp[k];
-            r[aa] = acc;
+            for (int k = 0; k < N; ++k) acc += fx.J[aa][k] * pred.L[k][rr];
+            M2[D + rr][aa] = acc;
           }
-          T Mo[N + D][D];
-          const T sqh = dev_sqrt(dev_abs(h));
 #pragma unroll
-          for (int rr = 0; rr < N; ++rr)
+          for (int c = 0; c < N; ++c) M2[D + rr][D + c] = pred.L[c][rr];
+        }
+        householder_r<T, D + N, D + N>(M2);
+        // G = solve_triu(R_Y, R12)^T (N x d); residual of the predicted mean
+        T Gt[D][N];
 #pragma unroll
-            for (int aa = 0; aa < D; ++aa) {
-              // (J Lu)[aa][rr], Lu = |p| sqrt|h| Q
+        for (int col = 0; col < N; ++col)
+#pragma unroll
+          for (int i = D - 1; i >= 0; --i) {
+            T acc = M2[i][D + col];
+#pragma unroll
+            for (int k = i + 1; k < D; ++k) acc -= M2[i][k] * Gt[k][col];
+            Gt[i][col] = dev_div(acc, M2[i][i]);
+          }
+        T ro[D];
+#pragma unroll
+        for (int aa = 0; aa < D; ++aa) {
+          T acc = fx.b[aa];
+#pragma unroll
+          for (int k = 0; k < N; ++k) acc += fx.J[aa][k] * pred.m[k];
+          ro[aa] = acc;
+        }
+        DNormal<T, N> xnew;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          T acc = pred.m[i];
+#pragma unroll
+          for (int aa = 0; aa < D; ++aa) acc -= Gt[aa][i] * ro[aa];
+          xnew.m[i] = acc;
+#pragma unroll
+          for (int j = 0; j < N; ++j) xnew.L[i][j] = (j <= i) ? M2[D + j][D + i] : T(0);
+        }
+        // error_residual_std: std of the rescaled observed = sigma * row norms of Lo, times dt;
+        // error_state_std (solvers.py:999-1098): sigma * the posterior std of coefficient 0 of the
+        // unit-scale extrapolation conditioned on the linearisation, times dt^0 / 0!
+        T std_state[D];
+        if (a.state_error) {
+          T M3[D + N][D + N];
+#pragma unroll
+          for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = 0; j < D + N; ++j) M3[i][j] = (i == j) ? damp : T(0);
+#pragma unroll
+          for (int rr = 0; rr < N; ++rr) {
+#pragma unroll
+            for (int aa = 0; aa < D; ++aa) {  // (J Lu)^T
               T acc = T(0);
 #pragma unroll
               for (int k = 0; k < N; ++k)
                 if (k % D == rr % D && rr / D <= k / D) acc += fx.J[aa][k] * dev_abs(p[k]) * sqh * T(a.q1[k / D][rr / D]);
-              Mo[rr][aa] = acc;
+              M3[D + rr][aa] = acc;
             }
 #pragma unroll
-          for (int i = 0; i < D; ++i)
-#pragma unroll
-            for (int j = 0; j < D; ++j) Mo[N + i][j] = (i == j) ? damp : T(0);
-          householder_r<T, N + D, D>(Mo);
-          // observed chol Lo = R^T (lower); sigma = ||Lo^{-1} r|| / sqrt(d)
-          T w[D];
-#pragma unroll
-          for (int i = 0; i < D; ++i) {
-            T acc = r[i];
-#pragma unroll
-            for (int k = 0; k < i; ++k) acc -= Mo[k][i] * w[k];
-            w[i] = dev_div(acc, Mo[i][i]);
+            for (int c = 0; c < N; ++c)
+              M3[D + rr][D + c] = (c % D == rr % D && rr / D <= c / D)
+                                      ? dev_abs(p[c]) * sqh * T(a.q1[c / D][rr / D]) : T(0);  // Lu^T
           }
-          T ww = T(0);
-#pragma unroll
-          for (int i = 0; i < D; ++i) ww += w[i] * w[i];
-          const T sigma_loc = dev_sqrt(ww * T(1.0 / D));
-
-          const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
-          DNormal<T, N> pred;
-          DCond<T, N> cnew, merged;
-          if constexpr (FP) {
-            prior_revert<T, NU, D>(a.q1, x, h, s_pred, pred, cnew);
-            cond_merge<T, N>(bw, cnew, merged);
-          } else {
-            prior_marginalise<T, NU, D>(a.q1, x, h, s_pred, pred);
-          }
-          // update: fx.revert(pred): M2 = [[damp I, 0], [(J Lp)^T, Lp^T]]
-          T M2[D + N][D + N];
-#pragma unroll
-          for (int i = 0; i < D; ++i)
-#pragma unroll
-            for (int j = 0; j < D + N; ++j) M2[i][j] = (i == j) ? damp : T(0);
-#pragma unroll
-          for (int rr = 0; rr < N; ++rr) {
-#pragma unroll
-            for (int aa = 0; aa < D; ++aa) {
-              T acc = T(0);
-#pragma unroll
-              for (int k = 0; k < N; ++k) acc += fx.J[aa][k] * pred.L[k][rr];
-              M2[D + rr][aa] = acc;
-            }
-#pragma unroll
-            for (int c = 0; c < N; ++c) M2[D + rr][D + c] = pred.L[c][rr];
-          }
-          householder_r<T, D + N, D + N>(M2);
-          // G = solve_triu(R_Y, R12)^T (N x d); residual of the predicted mean
-          T Gt[D][N];
-#pragma unroll
-          for (int col = 0; col < N; ++col)
-#pragma unroll
-            for (int i = D - 1; i >= 0; --i) {
-              T acc = M2[i][D + col];
-#pragma unroll
-              for (int k = i + 1; k < D; ++k) acc -= M2[i][k] * Gt[k][col];
-              Gt[i][col] = dev_div(acc, M2[i][i]);
-            }
-          T ro[D];
-#pragma unroll
-          for (int aa = 0; aa < D; ++aa) {
-            T acc = fx.b[aa];
-#pragma unroll
-            for (int k = 0; k < N; ++k) acc += fx.J[aa][k] * pred.m[k];
-            ro[aa] = acc;
-          }
-          DNormal<T, N> xnew;
-#pragma unroll
-          for (int i = 0; i < N; ++i) {
-            T acc = pred.m[i];
-#pragma unroll
-            for (int aa = 0; aa < D; ++aa) acc -= Gt[aa][i] * ro[aa];
-            xnew.m[i] = acc;
-#pragma unroll
-            for (int j = 0; j < N; ++j) xnew.L[i][j] = (j <= i) ? M2[D + j][D + i] : T(0);
-          }
-          // error_residual_std: std of the rescaled observed = sigma * row norms of Lo, times dt;
-          // error_state_std (solvers.py:999-1098): sigma * the posterior std of coefficient 0 of the
-          // unit-scale extrapolation conditioned on the linearisation, times dt^0 / 0!
-          T std_state[D];
-          if (a.state_error) {
-            T M3[D + N][D + N];
-#pragma unroll
-            for (int i = 0; i < D; ++i)
-#pragma unroll
-              for (int j = 0; j < D + N; ++j) M3[i][j] = (i == j) ? damp : T(0);
-#pragma unroll
-            for (int rr = 0; rr < N; ++rr) {
-#pragma unroll
-              for (int aa = 0; aa < D; ++aa) {  // (J Lu)^T
-                T acc = T(0);
-#pragma unroll
-                for (int k = 0; k < N; ++k)
-                  if (k % D == rr % D && rr / D <= k / D) acc += fx.J[aa][k] * dev_abs(p[k]) * sqh * T(a.q1[k / D][rr / D]);
-                M3[D + rr][aa] = acc;
-              }
-#pragma unroll
-              for (int c = 0; c < N; ++c)
-                M3[D + rr][D + c] = (c % D == rr % D && rr / D <= c / D)
-                                        ? dev_abs(p[c]) * sqh * T(a.q1[c / D][rr / D]) : T(0);  // Lu^T
-            }
-            householder_r<T, D + N, D + N>(M3);
-#pragma unroll
-            for (int j = 0; j < D; ++j) {
-              T rn = T(0);
-#pragma unroll
-              for (int k = 0; k <= j; ++k) rn += M3[D + k][D + j] * M3[D + k][D + j];
-              std_state[j] = dev_sqrt(rn);
-            }
-          }
-          double sumsq = 0.0;
+          householder_r<T, D + N, D + N>(M3);
 #pragma unroll
           for (int j = 0; j < D; ++j) {
             T rn = T(0);
 #pragma unroll
-            for (int k = 0; k <= j; ++k) rn += Mo[k][j] * Mo[k][j];
-            const T err_abs = a.state_error ? dev_abs(sigma_loc) * std_state[j] : dev_abs(sigma_loc) * dev_sqrt(rn) * h;
-            const T ref = fmax(dev_abs(x.m[j]), dev_abs(xnew.m[j]));
-            const T ratio = dev_div(err_abs, T(a.atol) + T(a.rtol) * ref);
-            sumsq += double(ratio) * double(ratio);
-          }
-          const double norm2 = sumsq * (1.0 / D);
-          if (!(norm2 == norm2) || isinf(norm2)) {
-            status = PDQ_INSTANCE_NONFINITE;
-            break;
-          }
-          const T ep = dev_fpow(T(norm2), T(-0.5 / n));
-          double factor;
-          if (a.control == PDQ_CONTROL_INTEGRAL) {
-            factor = a.safety * double(ep);
-          } else {
-            factor = a.safety * double(dev_fpow(ep, T(a.exp_i))) * double(dev_fpow(dev_div(ep, T(pi_prev)), T(a.exp_p)));
-            if (norm2 <= 1.0) pi_prev = double(ep);
-          }
-          factor = fmax(a.factor_min, fmin(factor, a.factor_max));
-          dt = factor * dt_use;
-          accepted = norm2 <= 1.0;
-          if (accepted) {
-            ti = t;
-            xi_ = x;
-            if constexpr (FP) bwi = bw;
-            t = t + dt_use;
-            ++num_steps;
-            x = xnew;
-            if constexpr (FP) bw = merged;
-            if (a.solver == PDQ_SOLVER_MLE) {
-              // new term: ||R_Y^{-T}... observed residual whitened by R_Y (d x d)
-              T wv[D];
-#pragma unroll
-              for (int i = 0; i < D; ++i) {
-                T acc = ro[i];
-#pragma unroll
-                for (int k = 0; k < i; ++k) acc -= M2[k][i] * wv[k];
-                wv[i] = dev_div(acc, M2[i][i]);
-              }
-              T q = T(0);
-#pragma unroll
-              for (int i = 0; i < D; ++i) q += wv[i] * wv[i];
-              mle_sumsq += double(q) * (1.0 / D);
-              ++num_data;
-            }
-            sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
+            for (int k = 0; k <= j; ++k) rn += M3[D + k][D + j] * M3[D + k][D + j];
+            std_state[j] = dev_sqrt(rn);
           }
         }
-        if (!accepted) continue;  // retry in the next iteration
-      }
-      const bool record = (!a.terminal_only) || (s == S - 1);
-      const int s_out = a.terminal_only ? 0 : s;
-      const int64_t rec = b * S_out + s_out;
-      if (t + a.eps < t_next) {
-        // interp_skip
-      } else if (t > t_next + a.eps) {
-        // interp_beyond_t1 (solvers.py:205-269)
-        const T h0 = T(t_next - ti), h1 = T(t - t_next);
-        DNormal<T, N> ext_t;
-        if constexpr (FP) {
-          // estimators_and_losses.py:549-591
-          DCond<T, N> c0, m0, c1, idc, m1;
-          DNormal<T, N> ext_t1;
-          prior_revert<T, NU, D>(a.q1, xi_, h0, sigma_sf, ext_t, c0);
-          cond_merge<T, N>(bwi, c0, m0);  // extrapolated_t.conditional
-          prior_revert<T, NU, D>(a.q1, ext_t, h1, sigma_sf, ext_t1, c1);
-          cond_identity(idc);
-          cond_merge<T, N>(idc, c1, m1);  // extrapolated_t1.conditional
-          store_cond(ws + int64_t(s - 1) * cond_floats<N>(), m0);
-          bw = m1;          // step_from keeps its marginal, new conditional
-          xi_ = ext_t;      // interp_from = previous_new
-          cond_identity(bwi);
+        double sumsq = 0.0;
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          T rn = T(0);
+#pragma unroll
+          for (int k = 0; k <= j; ++k) rn += Mo[k][j] * Mo[k][j];
+          const T err_abs = a.state_error ? dev_abs(sigma_loc) * std_state[j] : dev_abs(sigma_loc) * dev_sqrt(rn) * h;
+          const T ref = fmax(dev_abs(x.m[j]), dev_abs(xnew.m[j]));
+          const T ratio = dev_div(err_abs, T(a.atol) + T(a.rtol) * ref);
+          sumsq += double(ratio) * double(ratio);
+        }
+        const double norm2 = sumsq * (1.0 / D);
+        if (!(norm2 == norm2) || isinf(norm2)) {
+          status = PDQ_INSTANCE_NONFINITE;
+          break;
+        }
+        const T ep = dev_fpow(T(norm2), T(-0.5 / n));
+        double factor;
+        if (a.control == PDQ_CONTROL_INTEGRAL) {
+          factor = a.safety * double(ep);
         } else {
-          prior_marginalise<T, NU, D>(a.q1, xi_, h0, sigma_sf, ext_t);
-          xi_ = ext_t;
+          factor = a.safety * double(dev_fpow(ep, T(a.exp_i))) * double(dev_fpow(dev_div(ep, T(pi_prev)), T(a.exp_p)));
+          if (norm2 <= 1.0) pi_prev = double(ep);
         }
-        ti = t_next;
-        if (record) {
-          write_normal(a.u_mean + rec * N, a.u_chol + rec * N * N, ext_t);
-          a.output_scale[rec] = double(sigma_sf);
-          a.t_out[rec] = t_next;
-          a.num_steps[rec] = num_steps;
+        factor = fmax(a.factor_min, fmin(factor, a.factor_max));
+        dt = factor * dt_use;
+        accepted = norm2 <= 1.0;
+        if (accepted) {
+          ti = t;
+          xi_ = x;
+          if constexpr (FP) bwi = bw;
+          t = t + dt_use;
+          ++num_steps;
+          x = xnew;
+          if constexpr (FP) bw = merged;
+          if (a.solver == PDQ_SOLVER_MLE) {
+            // new term: ||R_Y^{-T}... observed residual whitened by R_Y (d x d)
+            T wv[D];
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+              T acc = ro[i];
+#pragma unroll
+              for (int k = 0; k < i; ++k) acc -= M2[k][i] * wv[k];
+              wv[i] = dev_div(acc, M2[i][i]);
+            }
+            T q = T(0);
+#pragma unroll
+            for (int i = 0; i < D; ++i) q += wv[i] * wv[i];
+            mle_sumsq += double(q) * (1.0 / D);
+            ++num_data;
+          }
+          sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
         }
-        if (a.filter_mean) write_normal(a.filter_mean + (b * S + s) * N, a.filter_chol + (b * S + s) * N * N, ext_t);
+      }
+      if (!accepted) continue;  // retry in the next iteration
+    }
+    const bool record = (!a.terminal_only) || (s == S - 1);
+    const int s_out = a.terminal_only ? 0 : s;
+    const int64_t rec = b * S_out + s_out;
+    if (t + a.eps < t_next) {
+      // interp_skip
+    } else if (t > t_next + a.eps) {
+      // interp_beyond_t1 (solvers.py:205-269)
+      const T h0 = T(t_next - ti), h1 = T(t - t_next);
+      DNormal<T, N> ext_t;
+      if constexpr (FP) {
+        // estimators_and_losses.py:549-591
+        DCond<T, N> c0, m0, c1, idc, m1;
+        DNormal<T, N> ext_t1;
+        prior_revert<T, NU, D>(a.q1, xi_, h0, sigma_sf, ext_t, c0);
+        cond_merge<T, N>(bwi, c0, m0);  // extrapolated_t.conditional
+        prior_revert<T, NU, D>(a.q1, ext_t, h1, sigma_sf, ext_t1, c1);
+        cond_identity(idc);
+        cond_merge<T, N>(idc, c1, m1);  // extrapolated_t1.conditional
+        store_cond(ws + int64_t(s - 1) * cond_floats<N>(), m0);
+        bw = m1;          // step_from keeps its marginal, new conditional
+        xi_ = ext_t;      // interp_from = previous_new
+        cond_identity(bwi);
       } else {
-        // interp_at_t1 (solvers.py:271-315)
-        if constexpr (FP) {
-          store_cond(ws + int64_t(s - 1) * cond_floats<N>(), bw);
-          cond_identity(bw);
-          cond_identity(bwi);
-        }
-        xi_ = x;
-        ti = t;
-        if (record) {
-          write_normal(a.u_mean + rec * N, a.u_chol + rec * N * N, x);
-          a.output_scale[rec] = double(sigma_sf);
-          a.t_out[rec] = t;
-          a.num_steps[rec] = num_steps;
-        }
-        if (a.filter_mean) write_normal(a.filter_mean + (b * S + s) * N, a.filter_chol + (b * S + s) * N * N, x);
+        prior_marginalise<T, NU, D>(a.q1, xi_, h0, sigma_sf, ext_t);
+        xi_ = ext_t;
       }
-      if (!(t + a.eps < t_next)) {  // checkpoint s done
-        ++s;
-        if (s < S) t_next = save_at[s];
+      ti = t_next;
+      if (record) {
+        write_normal(a.u_mean + rec * N, a.u_chol + rec * N * N, ext_t);
+        a.output_scale[rec] = double(sigma_sf);
+        a.t_out[rec] = t_next;
+        a.num_steps[rec] = num_steps;
       }
+      if (a.filter_mean) write_normal(a.filter_mean + (b * S + s) * N, a.filter_chol + (b * S + s) * N * N, ext_t);
+    } else {
+      // interp_at_t1 (solvers.py:271-315)
+      if constexpr (FP) {
+        store_cond(ws + int64_t(s - 1) * cond_floats<N>(), bw);
+        cond_identity(bw);
+        cond_identity(bwi);
+      }
+      xi_ = x;
+      ti = t;
+      if (record) {
+        write_normal(a.u_mean + rec * N, a.u_chol + rec * N * N, x);
+        a.output_scale[rec] = double(sigma_sf);
+        a.t_out[rec] = t;
+        a.num_steps[rec] = num_steps;
+      }
+      if (a.filter_mean) write_normal(a.filter_mean + (b * S + s) * N, a.filter_chol + (b * S + s) * N * N, x);
+    }
+    if (!(t + a.eps < t_next)) {  // checkpoint s done
+      ++s;
+      if (s < S) t_next = save_at[s];
+    }
   }
 
   // ---- finalize (solvers.py:439-480, 601-633, 735-767) ----

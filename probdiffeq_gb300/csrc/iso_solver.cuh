@@ -775,300 +775,300 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   int s = 1;
   W t_next = wide_from(save_at[1], T(0));
   while (s < S) {
-      if (before(t, t_next)) {
-        // ---- one attempt of the rejection loop (solvers_via_adaptive_steps.py:249-328) ----
-        bool accepted = false;
-        {
-          const T remaining = wide_diff(t_next, t);
-          const bool clipped = a.clip_dt && !(dt < remaining);
-          const T dt_use = clipped ? remaining : dt;
-          if (!(dev_abs(dt_use) > T(1e-14) * fmax(T(1), dev_abs(T(wide_hi(t)))))) {
-            status = PDQ_INSTANCE_DT_UNDERFLOW;
-            break;
-          }
-          if (attempts >= a.max_attempts) {
-            status = PDQ_INSTANCE_MAX_STEPS;
-            break;
-          }
-          ++attempts;
-          const T h = dt_use;
-          T p[n], pinv[n];
-          precon<T, NU>(h, p, pinv);
+    if (before(t, t_next)) {
+      // ---- one attempt of the rejection loop (solvers_via_adaptive_steps.py:249-328) ----
+      bool accepted = false;
+      {
+        const T remaining = wide_diff(t_next, t);
+        const bool clipped = a.clip_dt && !(dt < remaining);
+        const T dt_use = clipped ? remaining : dt;
+        if (!(dev_abs(dt_use) > T(1e-14) * fmax(T(1), dev_abs(T(wide_hi(t)))))) {
+          status = PDQ_INSTANCE_DT_UNDERFLOW;
+          break;
+        }
+        if (attempts >= a.max_attempts) {
+          status = PDQ_INSTANCE_MAX_STEPS;
+          break;
+        }
+        ++attempts;
+        const T h = dt_use;
+        T p[n], pinv[n];
+        precon<T, NU>(h, p, pinv);
 
-          // extrapolated mean: the same for every calibration mode, and the
-          // error estimate's apply_flat(previous mean) (solvers.py:943-944)
-          T mp[n][D];
-          iso_predict_mean<T, NU, D>(m, p, pinv, mp);
-          // TS0 linearisation at the extrapolated mean (ssm_impl_isotropic.py:304-317);
-          // TS1: H = [-tr J_f(mp_0) / d, 1, 0, ...] (ssm_impl_isotropic.py:320-355,
-          // jacobians.py:100-106), same residual mean
-          T f[D];
-          T h0 = T(0);
-          if (GEN && a.ts1) {
-            T Jf[D][D];
-            eval_with_jacobian<F>(mp[0], pt, f, Jf);
-            T tr = T(0);
+        // extrapolated mean: the same for every calibration mode, and the
+        // error estimate's apply_flat(previous mean) (solvers.py:943-944)
+        T mp[n][D];
+        iso_predict_mean<T, NU, D>(m, p, pinv, mp);
+        // TS0 linearisation at the extrapolated mean (ssm_impl_isotropic.py:304-317);
+        // TS1: H = [-tr J_f(mp_0) / d, 1, 0, ...] (ssm_impl_isotropic.py:320-355,
+        // jacobians.py:100-106), same residual mean
+        T f[D];
+        T h0 = T(0);
+        if (GEN && a.ts1) {
+          T Jf[D][D];
+          eval_with_jacobian<F>(mp[0], pt, f, Jf);
+          T tr = T(0);
 #pragma unroll
-            for (int j = 0; j < D; ++j) tr += Jf[j][j];
-            h0 = -tr * T(1.0 / D);
+          for (int j = 0; j < D; ++j) tr += Jf[j][j];
+          h0 = -tr * T(1.0 / D);
+        } else {
+          F::eval(mp[0], pt, f);
+        }
+        T mobs[D];
+        T mobs2 = T(0);
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          mobs[j] = mp[OUT][j] - f[j];
+          mobs2 += mobs[j] * mobs[j];
+        }
+        const T rms_mobs = fast_sqrt(mobs2 * T(1.0 / D));
+        // fx.marginalise(apply_flat(m)) with unit scale: observed std
+        // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
+        // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
+        const T ell = (GEN && a.ts1) ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
+                            : observed_std(p[OUT], h, q1_out_norm, damp);
+        const T sigma_loc = dev_div(rms_mobs, ell);
+
+        const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
+        T Lp[n][n];
+        IsoBackward<T, NU, D> cnew;  // fixed-point: the prior's backward conditional of this step
+        if constexpr (FP) {
+          if constexpr (kNarrow) {
+            iso_prior_revert<T, NU, D>(a.q1f, m, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp, cnew);
           } else {
-            F::eval(mp[0], pt, f);
+            iso_prior_revert<T, NU, D>(a.q1, m, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp, cnew);
           }
-          T mobs[D];
-          T mobs2 = T(0);
+        } else if constexpr (kNarrow) {
+          iso_predict_chol<T, NU>(a.q1f, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp);
+        } else {
+          iso_predict_chol<T, NU>(a.q1, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
+        }
+
+        // ---- update (revert_conditional, H = e_OUT) ----
+        T gain[n], Lnew[n][n];
+        const T R_Y = ts0_update<T, NU, OUT, GEN>(Lp, damp, gain, Lnew, h0);
+        const T ry_inv = fast_rcp(R_Y);
+        T mnew[n][D];
+#pragma unroll
+        for (int i = 0; i < n; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - gain[i] * mobs[j];
+        T dmnew[n][D];
+        if constexpr (TAN) {
+          T dmp[n][D];
+          iso_predict_mean<T, NU, D>(dm, p, pinv, dmp);
+          Dual<T, 1> ud[D], prd[P], fd[D];
 #pragma unroll
           for (int j = 0; j < D; ++j) {
-            mobs[j] = mp[OUT][j] - f[j];
-            mobs2 += mobs[j] * mobs[j];
+            ud[j] = Dual<T, 1>(mp[0][j]);
+            ud[j].g[0] = dmp[0][j];
           }
-          const T rms_mobs = fast_sqrt(mobs2 * T(1.0 / D));
-          // fx.marginalise(apply_flat(m)) with unit scale: observed std
-          // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
-          // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
-          const T ell = (GEN && a.ts1) ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
-                              : observed_std(p[OUT], h, q1_out_norm, damp);
-          const T sigma_loc = dev_div(rms_mobs, ell);
-
-          const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
-          T Lp[n][n];
-          IsoBackward<T, NU, D> cnew;  // fixed-point: the prior's backward conditional of this step
-          if constexpr (FP) {
-            if constexpr (kNarrow) {
-              iso_prior_revert<T, NU, D>(a.q1f, m, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp, cnew);
-            } else {
-              iso_prior_revert<T, NU, D>(a.q1, m, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp, cnew);
-            }
-          } else if constexpr (kNarrow) {
-            iso_predict_chol<T, NU>(a.q1f, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp);
-          } else {
-            iso_predict_chol<T, NU>(a.q1, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
+#pragma unroll
+          for (int k = 0; k < P; ++k) {
+            prd[k] = Dual<T, 1>(pt[k]);
+            prd[k].g[0] = (kdir == k) ? T(1) : T(0);
           }
-
-          // ---- update (revert_conditional, H = e_OUT) ----
-          T gain[n], Lnew[n][n];
-          const T R_Y = ts0_update<T, NU, OUT, GEN>(Lp, damp, gain, Lnew, h0);
-          const T ry_inv = fast_rcp(R_Y);
-          T mnew[n][D];
+          F::eval(ud, prd, fd);
 #pragma unroll
           for (int i = 0; i < n; ++i)
 #pragma unroll
-            for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - gain[i] * mobs[j];
-          T dmnew[n][D];
-          if constexpr (TAN) {
-            T dmp[n][D];
-            iso_predict_mean<T, NU, D>(dm, p, pinv, dmp);
-            Dual<T, 1> ud[D], prd[P], fd[D];
-#pragma unroll
-            for (int j = 0; j < D; ++j) {
-              ud[j] = Dual<T, 1>(mp[0][j]);
-              ud[j].g[0] = dmp[0][j];
-            }
-#pragma unroll
-            for (int k = 0; k < P; ++k) {
-              prd[k] = Dual<T, 1>(pt[k]);
-              prd[k].g[0] = (kdir == k) ? T(1) : T(0);
-            }
-            F::eval(ud, prd, fd);
-#pragma unroll
-            for (int i = 0; i < n; ++i)
-#pragma unroll
-              for (int j = 0; j < D; ++j) dmnew[i][j] = dmp[i][j] - gain[i] * (dmp[OUT][j] - fd[j].g[0]);
-          }
+            for (int j = 0; j < D; ++j) dmnew[i][j] = dmp[i][j] - gain[i] * (dmp[OUT][j] - fd[j].g[0]);
+        }
 
-          // ---- error estimate (error_residual_std, solvers.py:925-996) ----
-          // error_residual_std: the std of the observed residual rescaled by
-          // sigma_loc = rms / l is rms, error = rms * dt^1/1! (no division by a
-          // possibly tiny l).  error_state_std (solvers.py:1037-1098): condition the
-          // unit-scale extrapolation (chol |p| sqrt|h| Q1) on the same
-          // linearisation; error = sigma_loc * (posterior std of u), dt^0/0! = 1
-          T err_abs;
-          if (GEN && a.state_error) {
-            err_abs = sigma_loc * state_std0<T, NU, OUT>(a, p, h, damp, h0);
-          } else {
-            err_abs = rms_mobs * h;
-          }
-          W sumsq = wide_from(0.0, T(0));
+        // ---- error estimate (error_residual_std, solvers.py:925-996) ----
+        // error_residual_std: the std of the observed residual rescaled by
+        // sigma_loc = rms / l is rms, error = rms * dt^1/1! (no division by a
+        // possibly tiny l).  error_state_std (solvers.py:1037-1098): condition the
+        // unit-scale extrapolation (chol |p| sqrt|h| Q1) on the same
+        // linearisation; error = sigma_loc * (posterior std of u), dt^0/0! = 1
+        T err_abs;
+        if (GEN && a.state_error) {
+          err_abs = sigma_loc * state_std0<T, NU, OUT>(a, p, h, damp, h0);
+        } else {
+          err_abs = rms_mobs * h;
+        }
+        W sumsq = wide_from(0.0, T(0));
 #pragma unroll
-          for (int j = 0; j < D; ++j) {
-            const T ref = fmax(dev_abs(m[0][j]), dev_abs(mnew[0][j]));
-            const T ratio = dev_div(err_abs, atol + rtol * ref);
-            sumsq = wide_add_sq(sumsq, ratio);
-          }
-          // error_norm^2 = sumsq / D; accepted iff error_power = error_norm^(-1/n)
-          // >= 1, i.e. iff sumsq <= D (decided on the wide sum)
-          const T norm2 = T(wide_hi(sumsq)) * T(1.0 / D);
-          if (!(norm2 == norm2) || isinf(norm2)) {
-            status = PDQ_INSTANCE_NONFINITE;
-            break;
-          }
-          const T ep = dev_fpow(norm2, T(-0.5 / n));
-          accepted = wide_le(sumsq, T(D));
+        for (int j = 0; j < D; ++j) {
+          const T ref = fmax(dev_abs(m[0][j]), dev_abs(mnew[0][j]));
+          const T ratio = dev_div(err_abs, atol + rtol * ref);
+          sumsq = wide_add_sq(sumsq, ratio);
+        }
+        // error_norm^2 = sumsq / D; accepted iff error_power = error_norm^(-1/n)
+        // >= 1, i.e. iff sumsq <= D (decided on the wide sum)
+        const T norm2 = T(wide_hi(sumsq)) * T(1.0 / D);
+        if (!(norm2 == norm2) || isinf(norm2)) {
+          status = PDQ_INSTANCE_NONFINITE;
+          break;
+        }
+        const T ep = dev_fpow(norm2, T(-0.5 / n));
+        accepted = wide_le(sumsq, T(D));
 
-          // ---- controller (controllers.py:24-84) ----
-          T factor;
-          if (a.control == PDQ_CONTROL_INTEGRAL) {
-            factor = safety * ep;
-          } else {
-            const T gi = dev_fpow(ep, cst<T>(a.exp_i, a.exp_i_f));
-            const T gp = dev_fpow(dev_div(ep, pi_prev), cst<T>(a.exp_p, a.exp_p_f));
-            factor = safety * gi * gp;
-            if (accepted) pi_prev = ep;
-          }
-          factor = fmax(factor_min, fmin(factor, factor_max));
-          dt = factor * dt_use;
-          if (accepted) {
-            if constexpr (INTERP) {
-              ti = t;
+        // ---- controller (controllers.py:24-84) ----
+        T factor;
+        if (a.control == PDQ_CONTROL_INTEGRAL) {
+          factor = safety * ep;
+        } else {
+          const T gi = dev_fpow(ep, cst<T>(a.exp_i, a.exp_i_f));
+          const T gp = dev_fpow(dev_div(ep, pi_prev), cst<T>(a.exp_p, a.exp_p_f));
+          factor = safety * gi * gp;
+          if (accepted) pi_prev = ep;
+        }
+        factor = fmax(factor_min, fmin(factor, factor_max));
+        dt = factor * dt_use;
+        if (accepted) {
+          if constexpr (INTERP) {
+            ti = t;
 #pragma unroll
-              for (int i = 0; i < n; ++i) {
+            for (int i = 0; i < n; ++i) {
 #pragma unroll
-                for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
+              for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
 #pragma unroll
-                for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
-              }
-              if constexpr (FP) bwi = bw;
-              if constexpr (TAN) {
-#pragma unroll
-                for (int i = 0; i < n; ++i)
-#pragma unroll
-                  for (int j = 0; j < D; ++j) dmi[i][j] = dm[i][j];
-              }
+              for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
             }
+            if constexpr (FP) bwi = bw;
             if constexpr (TAN) {
 #pragma unroll
               for (int i = 0; i < n; ++i)
 #pragma unroll
-                for (int j = 0; j < D; ++j) dm[i][j] = dmnew[i][j];
+                for (int j = 0; j < D; ++j) dmi[i][j] = dm[i][j];
             }
-            if constexpr (FP) {
-              IsoBackward<T, NU, D> merged;
-              iso_cond_merge(bw, cnew, merged);
-              bw = merged;
-            }
-            // a step clipped to the checkpoint lands on it exactly in float
-            // pairs; float64 adds as the reference does
-            if constexpr (kNarrow) {
-              t = clipped ? t_next : wide_add(t, dt_use);
-            } else {
-              t = t + dt_use;
-            }
-            ++num_steps;
-#pragma unroll
-            for (int i = 0; i < n; ++i) {
-#pragma unroll
-              for (int j = 0; j < D; ++j) m[i][j] = mnew[i][j];
-#pragma unroll
-              for (int j = 0; j < n; ++j) L[i][j] = Lnew[i][j];
-            }
-            if (a.solver == PDQ_SOLVER_MLE) {
-              // running scale via hypot recurrence == RMS of new terms (solvers.py:421-424)
-              const T new_term = rms_mobs * dev_abs(ry_inv);
-              mle_sumsq = wide_add_sq(mle_sumsq, new_term);
-              ++num_data;
-            }
-            sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
           }
-        }
-        if (!accepted) continue;  // retry in the next iteration
-      }
-      // ---- checkpoint branch (solvers_via_adaptive_steps.py:242-247) ----
-      const int s_out = a.terminal_only ? 0 : s;
-      const bool record = (!a.terminal_only) || (s == S - 1);
-      if (before(t, t_next)) {
-        // interp_skip: keep stepping towards the checkpoint
-      } else if (INTERP && before(t_next, t)) {
-        if constexpr (INTERP) {
-          // interp_beyond_t1: predict from interp_from to t_next
-          // (solvers.py:205-269, estimators_and_losses.py:403-414)
-          const T h = T(wide_diff(t_next, ti));
-          T p[n], pinv[n], mp[n][D], Lp[n][n];
-          precon<T, NU>(h, p, pinv);
-          if constexpr (FP) {
-            // estimators_and_losses.py:549-591: the extrapolation to t_next
-            // closes the checkpoint's conditional (bwi merged with it); the
-            // step_from state keeps its marginal with the conditional from
-            // t_next to t, merged into the identity
-            IsoBackward<T, NU, D> c0, m0, c1, idc, m1;
-            iso_predict_mean<T, NU, D>(mi, p, pinv, mp);
-            if constexpr (kNarrow) {
-              iso_prior_revert<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp, c0);
-            } else {
-              iso_prior_revert<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp, c0);
-            }
-            iso_cond_merge(bwi, c0, m0);
-            iso_cond_store(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), m0);
-            const T h1 = T(wide_diff(t, t_next));
-            T p1[n], pinv1[n], mp1[n][D], Lp1[n][n];
-            precon<T, NU>(h1, p1, pinv1);
-            if constexpr (kNarrow) {
-              iso_prior_revert<T, NU, D>(a.q1f, mp, Lp, p1, pinv1, sigma_sf * dev_sqrt(dev_abs(h1)), Lp1, c1);
-            } else {
-              iso_prior_revert<T, NU, D>(a.q1, mp, Lp, p1, pinv1, sigma_sf * dev_sqrt(dev_abs(h1)), Lp1, c1);
-            }
-            (void)mp1;
-            iso_cond_identity(idc);
-            iso_cond_merge(idc, c1, m1);
-            bw = m1;
-            iso_cond_identity(bwi);
-          } else if constexpr (kNarrow) {
-            iso_predict<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
-          } else {
-            iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
-          }
-          if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), wide_value(t_next), num_steps);
-          if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, mp, Lp);
           if constexpr (TAN) {
-            T dmp[n][D];
-            iso_predict_mean<T, NU, D>(dmi, p, pinv, dmp);
-            if (record) write_tangent<T, NU, D, P>(a, b * S_out + s_out, kdir, dmp);
 #pragma unroll
             for (int i = 0; i < n; ++i)
 #pragma unroll
-              for (int j = 0; j < D; ++j) dmi[i][j] = dmp[i][j];
+              for (int j = 0; j < D; ++j) dm[i][j] = dmnew[i][j];
           }
-          ti = t_next;
+          if constexpr (FP) {
+            IsoBackward<T, NU, D> merged;
+            iso_cond_merge(bw, cnew, merged);
+            bw = merged;
+          }
+          // a step clipped to the checkpoint lands on it exactly in float
+          // pairs; float64 adds as the reference does
+          if constexpr (kNarrow) {
+            t = clipped ? t_next : wide_add(t, dt_use);
+          } else {
+            t = t + dt_use;
+          }
+          ++num_steps;
 #pragma unroll
           for (int i = 0; i < n; ++i) {
 #pragma unroll
-            for (int j = 0; j < D; ++j) mi[i][j] = mp[i][j];
+            for (int j = 0; j < D; ++j) m[i][j] = mnew[i][j];
 #pragma unroll
-            for (int j = 0; j < n; ++j) Li[i][j] = Lp[i][j];
+            for (int j = 0; j < n; ++j) L[i][j] = Lnew[i][j];
           }
-        }
-      } else {
-        // interp_at_t1: the state itself is the solution (estimators_and_losses.py:416-421)
-        if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), wide_value(t), num_steps);
-        if constexpr (TAN) {
-          if (record) write_tangent<T, NU, D, P>(a, b * S_out + s_out, kdir, dm);
-          if constexpr (INTERP) {
-#pragma unroll
-            for (int i = 0; i < n; ++i)
-#pragma unroll
-              for (int j = 0; j < D; ++j) dmi[i][j] = dm[i][j];
+          if (a.solver == PDQ_SOLVER_MLE) {
+            // running scale via hypot recurrence == RMS of new terms (solvers.py:421-424)
+            const T new_term = rms_mobs * dev_abs(ry_inv);
+            mle_sumsq = wide_add_sq(mle_sumsq, new_term);
+            ++num_data;
           }
+          sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
         }
-        if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, m, L);
+      }
+      if (!accepted) continue;  // retry in the next iteration
+    }
+    // ---- checkpoint branch (solvers_via_adaptive_steps.py:242-247) ----
+    const int s_out = a.terminal_only ? 0 : s;
+    const bool record = (!a.terminal_only) || (s == S - 1);
+    if (before(t, t_next)) {
+      // interp_skip: keep stepping towards the checkpoint
+    } else if (INTERP && before(t_next, t)) {
+      if constexpr (INTERP) {
+        // interp_beyond_t1: predict from interp_from to t_next
+        // (solvers.py:205-269, estimators_and_losses.py:403-414)
+        const T h = T(wide_diff(t_next, ti));
+        T p[n], pinv[n], mp[n][D], Lp[n][n];
+        precon<T, NU>(h, p, pinv);
         if constexpr (FP) {
-          // estimators_and_losses.py:534-547: close the checkpoint's conditional, reset
-          iso_cond_store(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), bw);
-          iso_cond_identity(bw);
-          if constexpr (INTERP) iso_cond_identity(bwi);
-        }
-        if constexpr (INTERP) {
-          ti = t;
-#pragma unroll
-          for (int i = 0; i < n; ++i) {
-#pragma unroll
-            for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
-#pragma unroll
-            for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
+          // estimators_and_losses.py:549-591: the extrapolation to t_next
+          // closes the checkpoint's conditional (bwi merged with it); the
+          // step_from state keeps its marginal with the conditional from
+          // t_next to t, merged into the identity
+          IsoBackward<T, NU, D> c0, m0, c1, idc, m1;
+          iso_predict_mean<T, NU, D>(mi, p, pinv, mp);
+          if constexpr (kNarrow) {
+            iso_prior_revert<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp, c0);
+          } else {
+            iso_prior_revert<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp, c0);
           }
+          iso_cond_merge(bwi, c0, m0);
+          iso_cond_store(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), m0);
+          const T h1 = T(wide_diff(t, t_next));
+          T p1[n], pinv1[n], mp1[n][D], Lp1[n][n];
+          precon<T, NU>(h1, p1, pinv1);
+          if constexpr (kNarrow) {
+            iso_prior_revert<T, NU, D>(a.q1f, mp, Lp, p1, pinv1, sigma_sf * dev_sqrt(dev_abs(h1)), Lp1, c1);
+          } else {
+            iso_prior_revert<T, NU, D>(a.q1, mp, Lp, p1, pinv1, sigma_sf * dev_sqrt(dev_abs(h1)), Lp1, c1);
+          }
+          (void)mp1;
+          iso_cond_identity(idc);
+          iso_cond_merge(idc, c1, m1);
+          bw = m1;
+          iso_cond_identity(bwi);
+        } else if constexpr (kNarrow) {
+          iso_predict<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
+        } else {
+          iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
+        }
+        if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), wide_value(t_next), num_steps);
+        if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, mp, Lp);
+        if constexpr (TAN) {
+          T dmp[n][D];
+          iso_predict_mean<T, NU, D>(dmi, p, pinv, dmp);
+          if (record) write_tangent<T, NU, D, P>(a, b * S_out + s_out, kdir, dmp);
+#pragma unroll
+          for (int i = 0; i < n; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) dmi[i][j] = dmp[i][j];
+        }
+        ti = t_next;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+#pragma unroll
+          for (int j = 0; j < D; ++j) mi[i][j] = mp[i][j];
+#pragma unroll
+          for (int j = 0; j < n; ++j) Li[i][j] = Lp[i][j];
         }
       }
-      if (!before(t, t_next)) {  // checkpoint s done
-        ++s;
-        if (s < S) t_next = wide_from(save_at[s], T(0));
+    } else {
+      // interp_at_t1: the state itself is the solution (estimators_and_losses.py:416-421)
+      if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), wide_value(t), num_steps);
+      if constexpr (TAN) {
+        if (record) write_tangent<T, NU, D, P>(a, b * S_out + s_out, kdir, dm);
+        if constexpr (INTERP) {
+#pragma unroll
+          for (int i = 0; i < n; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) dmi[i][j] = dm[i][j];
+        }
       }
+      if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, m, L);
+      if constexpr (FP) {
+        // estimators_and_losses.py:534-547: close the checkpoint's conditional, reset
+        iso_cond_store(ws + int64_t(s - 1) * iso_cond_floats<NU, D>(), bw);
+        iso_cond_identity(bw);
+        if constexpr (INTERP) iso_cond_identity(bwi);
+      }
+      if constexpr (INTERP) {
+        ti = t;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+#pragma unroll
+          for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
+#pragma unroll
+          for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
+        }
+      }
+    }
+    if (!before(t, t_next)) {  // checkpoint s done
+      ++s;
+      if (s < S) t_next = wide_from(save_at[s], T(0));
+    }
   }
 
   // ---- fixed-point backward pass: marginals at the checkpoints ----
