@@ -35,17 +35,18 @@
 // conditionals -- is the same for every parameter sample and carries no
 // tangent.  lml_plan_kernel computes them once, with the same arithmetic the
 // per-sample pass used (dual numbers with zero tangents, qr_qconst /
-// givens_qconst), into a plan in the workspace: per step the update gain, the
-// revert's gain transpose, the accumulated backward A and the merge scaling;
+// givens_qconst), into a plan in the workspace: per step the update gain and
+// the matrix K that maps the mean before the step to the increment of the
+// merged backward conditional's offset (xi <- xi + K m, K = bw.A diag(Tv)
+// (I - G^T A1) diag(p_inv), formed in double);
 // per observation interval the merged conditional's A, noise factor,
 // to_latent and to_observed; the terminal factor; the backward pass's
 // covariance side (it depends on the observation noise std but not on the
 // parameters): per observation the observed std ry and the gain column.
 // lml_kernel then runs only the mean recursion (matrix-vector products with
 // the plan's tables, staged through shared memory a chunk of steps at a time
-// by the warp, the vector field on dual numbers) per sample and tangent: the
-// same formulas in the same order, so the values are the per-sample
-// computation's.  The plan starts with a key (dt, damp, steps, observation
+// by the warp, the vector field on dual numbers) per sample and tangent.  The
+// plan starts with a key (dt, damp, steps, observation
 // spacing, nu, precision, and a copy of std) and is rebuilt only when the
 // key in the workspace differs.
 #pragma once
@@ -80,9 +81,8 @@ struct LmlArgs {
   void* workspace;       // (B * lanes, num_obs - 1) backward-conditional offsets xi with tangents, T
 };
 
-// Plan layout (in T, after the 256-byte key): per step g[n], Acn[n][n] (the
-// revert's gain transpose), bwA[n][n] and Tv[n] (the accumulated backward A
-// and the merge scaling before the step); per observation interval
+// Plan layout (in T, after the 256-byte key): per step g[n] and K[n][n]; per
+// observation interval
 // A[n][n], X[n][n], tl[n], to[n]; the terminal factor rL[n][n]; per
 // observation ry and ginv[n]; then (8-byte aligned) the std the plan was
 // built for and log|ry| per observation, in double.
@@ -90,7 +90,7 @@ constexpr int kLmlPlanKeyBytes = 256;
 
 template <int NU>
 PDQ_HD constexpr int lml_plan_step() {
-  return 2 * (NU + 1) * (NU + 1) + 2 * (NU + 1);
+  return (NU + 1) * (NU + 1) + (NU + 1);
 }
 template <int NU>
 PDQ_HD constexpr int lml_plan_obs() {
@@ -98,9 +98,9 @@ PDQ_HD constexpr int lml_plan_obs() {
 }
 PDQ_HD int64_t lml_plan_elems(int nu, int num_steps, int save_every) {
   const int64_t n = nu + 1;
-  const int64_t per = 2 * n * n + 2 * n;
+  const int64_t step = n * n + n, per = 2 * n * n + 2 * n;
   const int64_t num_obs = num_steps / save_every + 1;
-  return int64_t(num_steps) * per + (num_obs - 1) * per + n * n + num_obs * (n + 1);
+  return int64_t(num_steps) * step + (num_obs - 1) * per + n * n + num_obs * (n + 1);
 }
 // Offset in bytes (from the plan's start, key included) of the std copy.
 PDQ_HD int64_t lml_plan_std_offset(int nu, int num_steps, int save_every, int elem) {
@@ -306,19 +306,27 @@ __global__ void lml_plan_kernel(LmlArgs a) {
       cn.tl[i] = T(1) / p[i];
       cn.to[i] = T(1) / pinv[i];
     }
-    // merge (ssm_impl_isotropic.py:91-105): the tables carry bw.A and Tv for the xi recursion
+    // merge (ssm_impl_isotropic.py:91-105).  The offsets are linear in the
+    // mean m before the step: the revert's xi = (I - G^T A1) diag(p_inv) m and
+    // the merged xi += bw.A diag(Tv) xi_revert, so xi += K m with K formed here
     T Tv[n];
     for (int i = 0; i < n; ++i) Tv[i] = bw.tl[i] * cn.to[i];
     T* const g_t = tbl;
-    T* const acn_t = tbl + n;
-    T* const bwa_t = acn_t + n * n;
-    T* const tv_t = bwa_t + n * n;
-    for (int i = 0; i < n; ++i) {
-      tv_t[i] = Tv[i];
-      for (int j = 0; j < n; ++j) {
-        acn_t[i * n + j] = cn.A[i][j].v;
-        bwa_t[i * n + j] = bw.A[i][j].v;
-      }
+    T* const k_t = tbl + n;
+    {
+      double C[n][n];  // (I - G^T A1) diag(p_inv)
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j) {
+          double acc = (k == j) ? 1.0 : 0.0;
+          for (int l = 0; l <= j; ++l) acc -= double(cn.A[k][l].v) * double(iwp_a<NU>(l, j));
+          C[k][j] = acc * double(pinv[j]);
+        }
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double acc = 0.0;
+          for (int k = 0; k < n; ++k) acc += double(bw.A[i][k].v) * double(Tv[k]) * C[k][j];
+          k_t[i * n + j] = T(acc);
+        }
     }
     {
       DT Mm[2 * n][n];
@@ -526,10 +534,8 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       }
     }
     const T* g_t = tb;
-    const T* acn_t = tb + n;
-    const T* bwa_t = acn_t + n * n;
-    const T* tv_t = bwa_t + n * n;
-    // ---- predicted mean and the revert's offset xi = mean_l - Gt^T A1 mean_l ----
+    const T* k_t = tb + n;
+    // ---- predicted mean ----
     DT mean_l[n][D], mobs[n][D], mp[n][D];
 #pragma unroll
     for (int i = 0; i < n; ++i)
@@ -545,17 +551,7 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
         mobs[i][j] = acc;
         mp[i][j] = p[i] * acc;
       }
-    DT cxi[n][D];
-#pragma unroll
-    for (int i = 0; i < n; ++i)
-#pragma unroll
-      for (int j = 0; j < D; ++j) {
-        DT acc = mean_l[i][j];
-#pragma unroll
-        for (int k = 0; k < n; ++k) acc = acc - acn_t[i * n + k] * mobs[k][j];
-        cxi[i][j] = acc;
-      }
-    // ---- merge: bw.xi + bw.A (Tv * xi) ----
+    // ---- the merged backward conditional's offset: xi + K m (revert and merge) ----
     DT nxi[n][D];
 #pragma unroll
     for (int i = 0; i < n; ++i)
@@ -563,7 +559,7 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       for (int j = 0; j < D; ++j) {
         DT x = bxi[i][j];
 #pragma unroll
-        for (int k = 0; k < n; ++k) x = x + bwa_t[i * n + k] * (tv_t[k] * cxi[k][j]);
+        for (int k = 0; k < n; ++k) x = x + k_t[i * n + k] * m[k][j];
         nxi[i][j] = x;
       }
     // ---- TS0 linearisation at the predicted mean; update with the plan's gain ----
