@@ -20,6 +20,7 @@ LML-gradient throughput under ``secondary``.
 Other workloads, one JSON line each (``--workload``):
   lv_single          one LV instance, dynamic calibration, float64 and float32
   fhn_lml            LML + gradient for 1024 FitzHugh--Nagumo parameter samples
+                     (forward-mode kernel, and the adjoint pdq_lml_fwd + pdq_lml_bwd)
   vdp_dense          4096 stiff van der Pol instances, dense TS1, fixed-point
                      smoother, 100 checkpoints (minutes per solve at mu <= 1000)
   burgers_blockdiag  64 viscous Burgers instances, d = 4096, blockdiag TS0
@@ -305,6 +306,29 @@ def lml_gradients(torch, _native, ensemble, device, precisions=("float32", "floa
             "ms_per_batch": 1e3 * t / reps,
             "all_status_ok": bool((holder["status"] == 0).all().item()),
         }
+        # reverse mode: pdq_lml_fwd (value, sqrt(N) checkpoints) then pdq_lml_bwd (adjoint pass)
+        adj = {}
+
+        def fwd_call():
+            adj["fwd"] = _native.lml_fwd(cfg, thetas, y0, data, std, t0=0.0, dt=0.01, num_steps=num_steps,
+                                         save_every=10, stream=stream, workspace=adj.get("ws"),
+                                         outputs=adj.get("fwd_out"))
+            adj["ws"] = adj["fwd"]["_workspace"]
+            adj["fwd_out"] = {k: adj["fwd"][k] for k in ("lml", "status")}
+
+        def bwd_call():
+            adj["bwd"] = _native.lml_bwd(adj["fwd"], None, outputs=adj.get("bwd"))
+
+        t_fwd = timed_region(torch, stream, fwd_call, reps, 3)
+        t_bwd = timed_region(torch, stream, bwd_call, reps, 3)
+        g_fm, g_adj = holder["grad"], adj["bwd"]["grad"]
+        res[prec]["adjoint"] = {
+            "grads_per_s": B * reps / (t_fwd + t_bwd),
+            "ms_fwd": 1e3 * t_fwd / reps,
+            "ms_bwd": 1e3 * t_bwd / reps,
+            "checkpoint_every": int(round(num_steps ** 0.5)),
+            "max_rel_diff_vs_forward_mode": float(((g_adj - g_fm).abs().amax(1) / g_fm.norm(dim=1)).max()),
+        }
     res["config"] = {"samples": B, "num_steps": num_steps, "observations": int(data.shape[0]), "num_derivatives": 3}
     return res
 
@@ -549,7 +573,8 @@ def run_fhn_lml(args):
         r = lml_gradients(torch, _native, ensemble, device, reps=args.steps)
     print(json.dumps(base_line("LML grads/s", r["float32"]["grads_per_s"], "grads/s", args, r["float32"]["ms_per_batch"],
                                True, "f32 bulk + f64 log-pdf sum", dict(r["config"], workload="fitzhugh_nagumo_lml"),
-                               float64=r["float64"], gpu_launches=2 * args.steps,  # plan check + per-sample kernel
+                               float64=r["float64"], adjoint=r["float32"]["adjoint"],
+                               gpu_launches=2 * args.steps,  # plan check + per-sample kernel
                                clocks=clk.summary())))
 
 

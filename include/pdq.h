@@ -232,6 +232,42 @@ pdq_status pdq_lml_fixed_grid(const pdq_config* config, const pdq_lml_args* args
                               void* stream);
 #endif
 
+/* The same LML with its gradient by reverse mode (an adjoint pass), split
+ * into the forward and backward halves of a custom VJP: the counterpart of
+ * jax.vjp / jax.grad of loss_lml_timeseries through solve_fixed_grid with
+ * the fixed-point smoother (probdiffeq/_probdiffeq/estimators_and_losses.py:
+ * 53-105, 180-218, 526-547; probdiffeq/_ivpsolve/solvers_via_fixed_steps.py:
+ * 11-34), i.e. the fwd/bwd pair a jax.custom_vjp or torch.autograd.Function
+ * binds.  pdq_lml_fwd writes lml and status and leaves in the workspace what
+ * the backward pass needs: the state every checkpoint_every steps (sqrt(N)
+ * checkpointing: 0 selects round(sqrt(num_steps))), the backward
+ * conditionals' offsets and the LML recursion's innovations.  pdq_lml_bwd
+ * then reads them (same args, same workspace, untouched in between),
+ * recomputes each segment of checkpoint_every steps from its checkpoint and
+ * differentiates it in reverse, writing
+ *   lml.grad (B, P) = cotangent * d lml / d params   (if not NULL)
+ *   grad_y0  (B, d) = cotangent * d lml / d y0       (if not NULL)
+ * (cotangent NULL: ones).  Samples whose status is not PDQ_INSTANCE_OK get
+ * NaN gradients.  The derivative is the forward-mode one of
+ * pdq_lml_fixed_grid (the same rules), at a cost independent of P.
+ * lml.with_gradient is ignored.  The workspace must be 16-byte aligned. */
+typedef struct pdq_lml_adjoint_args {
+  pdq_lml_args lml;          /* inputs, lml / status (written by fwd, status read by bwd), grad (bwd) */
+  int32_t checkpoint_every;  /* steps between stored states, 0 <= C <= num_steps (0: round(sqrt(num_steps))) */
+  int32_t reserved0;         /* 0 */
+  const double* cotangent;   /* (B,) d loss / d lml for pdq_lml_bwd, or NULL for ones */
+  double* grad_y0;           /* (B, d) output of pdq_lml_bwd, or NULL */
+} pdq_lml_adjoint_args;
+
+#if !defined(__CUDACC_RTC__)
+pdq_status pdq_lml_adjoint_workspace_size(const pdq_config* config, int64_t num_instances, int32_t num_steps,
+                                          int32_t save_every, int32_t checkpoint_every, size_t* bytes);
+pdq_status pdq_lml_fwd(const pdq_config* config, const pdq_lml_adjoint_args* args, void* workspace,
+                       size_t workspace_bytes, void* stream);
+pdq_status pdq_lml_bwd(const pdq_config* config, const pdq_lml_adjoint_args* args, void* workspace,
+                       size_t workspace_bytes, void* stream);
+#endif
+
 /* Size of the scratch array inside the library used by pdq_lml_fixed_grid_static. */
 #define PDQ_LML_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 

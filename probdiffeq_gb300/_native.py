@@ -146,6 +146,16 @@ class PdqLmlArgs(ctypes.Structure):
     ]
 
 
+
+class PdqLmlAdjointArgs(ctypes.Structure):
+    _fields_ = [
+        ("lml", PdqLmlArgs),
+        ("checkpoint_every", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
+        ("cotangent", ctypes.c_void_p),
+        ("grad_y0", ctypes.c_void_p),
+    ]
+
 # Every symbol include/pdq.h declares, with its ctypes signature.
 SIGNATURES = {
     "pdq_abi_version": (ctypes.c_uint32, []),
@@ -169,6 +179,21 @@ SIGNATURES = {
     "pdq_lml_fixed_grid": (
         ctypes.c_int,
         [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlArgs), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "pdq_lml_adjoint_workspace_size": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+         ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "pdq_lml_fwd": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlAdjointArgs), ctypes.c_void_p, ctypes.c_size_t,
+         ctypes.c_void_p],
+    ),
+    "pdq_lml_bwd": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlAdjointArgs), ctypes.c_void_p, ctypes.c_size_t,
+         ctypes.c_void_p],
     ),
     "pdq_lml_fixed_grid_static": (
         ctypes.c_int,
@@ -398,6 +423,78 @@ def lml_fixed_grid(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every,
     outputs["_workspace"] = ws
     return outputs
 
+
+
+def lml_adjoint_workspace_bytes(cfg, B, num_steps, save_every, checkpoint_every=0):
+    """pdq_lml_adjoint_workspace_size: bytes of the plan plus the residuals of B samples."""
+    lib = load()
+    nbytes = ctypes.c_size_t(0)
+    check(lib.pdq_lml_adjoint_workspace_size(ctypes.byref(cfg), B, num_steps, save_every, checkpoint_every,
+                                             ctypes.byref(nbytes)), "pdq_lml_adjoint_workspace_size")
+    return int(nbytes.value)
+
+
+def lml_fwd(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every, average_pdfs=False, checkpoint_every=0,
+            stream=None, workspace=None, outputs=None):
+    """Call pdq_lml_fwd on device tensors (float64, contiguous).
+
+    Returns a dict with ``lml`` (B,), ``status`` (B,) and the state that
+    :func:`lml_bwd` needs (the argument struct and the workspace holding the
+    plan and the residuals; keep it untouched until the backward call).
+    """
+    lib = load()
+    B = y0.shape[0]
+    dev = y0.device
+    if outputs is None:
+        outputs = {
+            "lml": torch.empty(B, dtype=torch.float64, device=dev),
+            "status": torch.empty(B, dtype=torch.int32, device=dev),
+        }
+    nbytes = lml_adjoint_workspace_bytes(cfg, B, num_steps, save_every, checkpoint_every)
+    ws = workspace
+    if ws is None:
+        ws = torch.zeros(max(1, nbytes), dtype=torch.uint8, device=dev)
+    elif ws.numel() * ws.element_size() < nbytes:
+        raise ValueError("the LML workspace is smaller than pdq_lml_adjoint_workspace_size")
+    a = PdqLmlAdjointArgs()
+    a.lml.num_instances, a.lml.num_steps, a.lml.save_every = B, num_steps, save_every
+    a.lml.average_pdfs, a.lml.with_gradient = int(bool(average_pdfs)), 0
+    a.lml.t0, a.lml.dt = float(t0), float(dt)
+    a.lml.params, a.lml.y0, a.lml.data, a.lml.std = _ptr(params), _ptr(y0), _ptr(data), _ptr(std)
+    a.lml.lml, a.lml.status = _ptr(outputs["lml"]), _ptr(outputs["status"])
+    a.checkpoint_every = int(checkpoint_every)
+    check(lib.pdq_lml_fwd(ctypes.byref(cfg), ctypes.byref(a), _ptr(ws), ctypes.c_size_t(nbytes), _stream_handle(stream)),
+          "pdq_lml_fwd")
+    outputs["_workspace"] = ws
+    # the inputs stay referenced: the backward call reads them again
+    outputs["_saved"] = (cfg, a, nbytes, params, y0, data, std, stream)
+    return outputs
+
+
+def lml_bwd(fwd, cotangent=None, *, params_grad=True, y0_grad=False, outputs=None):
+    """Call pdq_lml_bwd for the residuals of :func:`lml_fwd`'s call ``fwd``.
+
+    cotangent: (B,) float64 device tensor (d loss / d lml) or None for ones.
+    Returns ``{"grad": (B, P) or None, "grad_y0": (B, d) or None}``.
+    """
+    lib = load()
+    cfg, a0, nbytes, params, y0, data, std, stream = fwd["_saved"]
+    B, P, D = y0.shape[0], params.shape[1], y0.shape[1]
+    if outputs is None:
+        outputs = {
+            "grad": torch.empty((B, P), dtype=torch.float64, device=y0.device) if params_grad else None,
+            "grad_y0": torch.empty((B, D), dtype=torch.float64, device=y0.device) if y0_grad else None,
+        }
+    a = PdqLmlAdjointArgs.from_buffer_copy(a0)
+    if cotangent is not None:
+        cotangent = cotangent.detach().to(dtype=torch.float64).contiguous()
+    a.cotangent = _ptr(cotangent)
+    a.lml.grad = _ptr(outputs.get("grad"))
+    a.grad_y0 = _ptr(outputs.get("grad_y0"))
+    check(lib.pdq_lml_bwd(ctypes.byref(cfg), ctypes.byref(a), _ptr(fwd["_workspace"]), ctypes.c_size_t(nbytes),
+                          _stream_handle(stream)), "pdq_lml_bwd")
+    outputs["_cotangent"] = cotangent
+    return outputs
 
 def sample_markov(ssm, num_derivatives, ode_dim, marginal_mean, marginal_chol, posterior, normals, stream=None):
     """Call pdq_sample_markov on device float64 tensors; returns the samples tensor.

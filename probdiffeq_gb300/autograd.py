@@ -1,13 +1,18 @@
 """The LML kernel as a ``torch.autograd.Function``.
 
 ``lml(params, y0, data, std, ...)`` returns the log-marginal likelihood of
-each parameter sample (one native launch, the same C ABI as
-``pdq_lml_fixed_grid``); its backward multiplies the incoming cotangent into
-the parameter gradient that the forward launch already computed (forward-mode
-tangents inside the kernel, one direction per thread), so ``loss.backward()``
-through it costs no second launch.  This is the torch counterpart of the
+each parameter sample.  Two gradient modes, the torch counterpart of the
 reference's ``jax.grad`` of ``loss_lml_timeseries``
-(probdiffeq/_probdiffeq/estimators_and_losses.py:53-105).
+(probdiffeq/_probdiffeq/estimators_and_losses.py:53-105):
+
+* ``mode="forward"`` (``pdq_lml_fixed_grid``): the forward launch computes the
+  parameter gradient with forward-mode tangents (one direction per thread);
+  the backward multiplies the incoming cotangent into it, no second launch.
+* ``mode="adjoint"`` (``pdq_lml_fwd`` / ``pdq_lml_bwd``): the forward launch
+  computes the value and stores sqrt(N)-checkpointed residuals; the backward
+  launch runs the adjoint pass for the incoming cotangent and gives the
+  gradient with respect to ``params`` and ``y0``, at a cost independent of
+  the number of parameters.
 """
 
 import torch
@@ -36,19 +41,46 @@ class _LmlFixedGrid(torch.autograd.Function):
         return g_params, None, None, None, None, None, None, None, None, None, None
 
 
+class _LmlAdjoint(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, params, y0, data, std, cfg, t0, dt, num_steps, save_every, average_pdfs, checkpoint_every,
+                stream):
+        fwd = _native.lml_fwd(
+            cfg, params.detach().contiguous(), y0.detach().contiguous(), data.contiguous(), std.contiguous(),
+            t0=t0, dt=dt, num_steps=num_steps, save_every=save_every, average_pdfs=average_pdfs,
+            checkpoint_every=checkpoint_every, stream=stream,
+        )
+        ctx.fwd = fwd
+        ctx.mark_non_differentiable(fwd["status"])
+        return fwd["lml"], fwd["status"]
+
+    @staticmethod
+    def backward(ctx, g_lml, g_status):
+        want_p, want_y0 = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        out = _native.lml_bwd(ctx.fwd, g_lml, params_grad=want_p, y0_grad=want_y0)
+        return (out["grad"], out["grad_y0"], None, None, None, None, None, None, None, None, None, None)
+
+
 def lml(params, y0, data, std, *, field="fitzhugh_nagumo", num_derivatives=3, dt, num_steps, save_every,
-        t0=0.0, average_pdfs=False, precision="float64", damp=0.0, stream=None):
+        t0=0.0, average_pdfs=False, precision="float64", damp=0.0, mode="forward", checkpoint_every=0, stream=None):
     """Differentiable LML of observations under the fixed-point-smoother posterior.
 
     params (B, P) float64 CUDA tensor (``requires_grad`` for gradients), y0 (B, d),
     data (num_steps // save_every + 1, d), std (same length).  Returns
-    (lml (B,), status (B,) int32); ``lml.sum().backward()`` fills ``params.grad``.
-    Gradients with respect to y0, data and std are not provided.
+    (lml (B,), status (B,) int32); ``lml.sum().backward()`` fills ``params.grad``
+    (and, with ``mode="adjoint"``, ``y0.grad``).  ``checkpoint_every`` (adjoint
+    mode): steps between stored states, 0 for round(sqrt(num_steps)).
+    Gradients with respect to data and std are not provided.
     """
     if num_steps % save_every != 0 or data.shape[0] != num_steps // save_every + 1:
         raise ValueError("The standard deviation container differs from what was expected.")
     cfg = ensemble.make_config(field=field, num_derivatives=num_derivatives, ode_dim=y0.shape[-1], ssm="isotropic",
                                constraint="ts0", strategy="fixedpoint", solver="none", precision=precision, damp=damp)
+    if mode == "adjoint":
+        return _LmlAdjoint.apply(params, y0, data, std, cfg, float(t0), float(dt), int(num_steps), int(save_every),
+                                 bool(average_pdfs), int(checkpoint_every), stream)
+    if mode != "forward":
+        raise ValueError(f"unknown gradient mode {mode!r} (expected 'forward' or 'adjoint')")
     return _LmlFixedGrid.apply(params, y0, data, std, cfg, float(t0), float(dt), int(num_steps), int(save_every),
                                bool(average_pdfs), stream)
 

@@ -14,8 +14,11 @@
 // by cudaGetSymbolAddress.  That set-up happens on the first call on each
 // device, so the first call should come before any stream capture.
 // Every call shares the one array: calls whose launches overlap on the GPU
-// race on it.  The kernel writes every scratch entry before reading it, so
-// nothing needs clearing between calls.
+// race on it.  Nothing needs clearing between calls: the covariance plan at
+// the head of the array is reused only when its key (a sentinel, a validity
+// flag set last, and the grid, prior, precision and noise levels) matches the
+// call's, which a zero-initialised or stale array cannot do by accident, and
+// every other scratch entry is written before it is read.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -6,6 +6,7 @@
 #include "bd_launch.cuh"
 #include "dense_launch.cuh"
 #include "offgrid.h"
+#include "lml_adj_launch.cuh"
 #include "lml_launch.cuh"
 #include "iso_launch.cuh"
 #include "nvrtc_fields.h"
@@ -523,6 +524,103 @@ pdq_status pdq_lml_fixed_grid(const pdq_config* c, const pdq_lml_args* args, voi
   else
     err = pdq_launch_lml_lv_f64(a, c->num_derivatives, stream);
   return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+}
+
+
+// ---- adjoint (reverse-mode) LML: pdq_lml_fwd / pdq_lml_bwd ----
+
+// Steps between stored states: the caller's, or round(sqrt(num_steps)).
+static int32_t lml_adj_ckpt(int32_t num_steps, int32_t checkpoint_every) {
+  if (checkpoint_every != 0) return checkpoint_every;
+  const int32_t c = int32_t(lround(sqrt(double(num_steps))));
+  return c < 1 ? 1 : c;
+}
+
+static pdq_status lml_adj_check(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every,
+                                int32_t checkpoint_every) {
+  pdq_status st = lml_check(c, B, num_steps, save_every);
+  if (st != PDQ_SUCCESS) return st;
+  if (checkpoint_every < 0 || checkpoint_every > num_steps) return PDQ_ERROR_INVALID_VALUE;
+  return PDQ_SUCCESS;
+}
+
+// Workspace: the shared covariance plan (the layout pdq_lml_fixed_grid uses),
+// then the residuals of every sample (lml_adjoint.cuh).
+static size_t lml_adj_bytes(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every, int32_t ckpt) {
+  const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
+  const pdq::LmlAdjLayout L(c->num_derivatives, c->ode_dim, num_steps, save_every, ckpt);
+  return lml_plan_bytes(c, num_steps, save_every) + size_t(B) * size_t(L.total) * elem;
+}
+
+pdq_status pdq_lml_adjoint_workspace_size(const pdq_config* c, int64_t B, int32_t num_steps, int32_t save_every,
+                                          int32_t checkpoint_every, size_t* bytes) {
+  if (bytes == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  pdq_status st = lml_adj_check(c, B, num_steps, save_every, checkpoint_every);
+  if (st != PDQ_SUCCESS) return st;
+  *bytes = lml_adj_bytes(c, B, num_steps, save_every, lml_adj_ckpt(num_steps, checkpoint_every));
+  return PDQ_SUCCESS;
+}
+
+static pdq_status lml_adj_launch(const pdq_config* c, const pdq_lml_adjoint_args* args, void* workspace,
+                                 size_t workspace_bytes, void* stream_ptr, bool backward) {
+  if (args == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  const pdq_lml_args& l = args->lml;
+  pdq_status st = lml_adj_check(c, l.num_instances, l.num_steps, l.save_every, args->checkpoint_every);
+  if (st != PDQ_SUCCESS) return st;
+  if (args->reserved0 != 0) return PDQ_ERROR_INVALID_VALUE;
+  if (l.num_instances == 0) return PDQ_SUCCESS;
+  if (!l.params || !l.y0 || !l.data || !l.std || !l.status || !(l.dt > 0)) return PDQ_ERROR_INVALID_VALUE;
+  if (!backward && !l.lml) return PDQ_ERROR_INVALID_VALUE;
+  if (backward && !l.grad && !args->grad_y0) return PDQ_ERROR_INVALID_VALUE;
+  const int32_t ckpt = lml_adj_ckpt(l.num_steps, args->checkpoint_every);
+  if (workspace == nullptr || reinterpret_cast<uintptr_t>(workspace) % 16 != 0 ||
+      workspace_bytes < lml_adj_bytes(c, l.num_instances, l.num_steps, l.save_every, ckpt))
+    return PDQ_ERROR_WORKSPACE;
+  pdq::LmlAdjArgs aa;
+  memset(&aa, 0, sizeof(aa));
+  pdq::LmlArgs& a = aa.base;
+  a.B = l.num_instances;
+  a.num_steps = l.num_steps;
+  a.save_every = l.save_every;
+  a.average_pdfs = l.average_pdfs ? 1 : 0;
+  a.with_gradient = 0;
+  a.lanes_per_sample = 1;
+  a.t0 = l.t0;
+  a.dt = l.dt;
+  a.damp = c->damp;
+  iwp_q1(c->num_derivatives, a.q1);
+  a.params = l.params;
+  a.y0 = l.y0;
+  a.data = l.data;
+  a.std = l.std;
+  a.lml = l.lml;
+  a.grad = l.grad;
+  a.status = l.status;
+  a.plan = workspace;
+  a.workspace = nullptr;
+  aa.ckpt = ckpt;
+  aa.num_ckpt = int32_t((int64_t(l.num_steps) + ckpt - 1) / ckpt);
+  aa.cotangent = args->cotangent;
+  aa.grad_y0 = args->grad_y0;
+  aa.res = static_cast<unsigned char*>(workspace) + lml_plan_bytes(c, l.num_steps, l.save_every);
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+  cudaError_t err;
+  if (c->field == PDQ_FIELD_FITZHUGH_NAGUMO)
+    err = c->precision == PDQ_PRECISION_F64 ? pdq_launch_lml_adj_fhn_f64(aa, c->num_derivatives, backward, stream)
+                                            : pdq_launch_lml_adj_fhn_f32(aa, c->num_derivatives, backward, stream);
+  else
+    err = pdq_launch_lml_adj_lv_f64(aa, c->num_derivatives, backward, stream);
+  return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+}
+
+pdq_status pdq_lml_fwd(const pdq_config* c, const pdq_lml_adjoint_args* args, void* workspace, size_t workspace_bytes,
+                       void* stream) {
+  return lml_adj_launch(c, args, workspace, workspace_bytes, stream, false);
+}
+
+pdq_status pdq_lml_bwd(const pdq_config* c, const pdq_lml_adjoint_args* args, void* workspace, size_t workspace_bytes,
+                       void* stream) {
+  return lml_adj_launch(c, args, workspace, workspace_bytes, stream, true);
 }
 
 }  // extern "C"

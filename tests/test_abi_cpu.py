@@ -116,3 +116,49 @@ def test_offgrid_arguments_are_checked_before_launch(lib):
     assert lib.pdq_offgrid_marginals(ctypes.byref(a), None) == 2  # block-diagonal: not native
     a.ssm, a.num_queries = 2, 0
     assert lib.pdq_offgrid_marginals(ctypes.byref(a), None) == 0
+
+
+def test_lml_adjoint_arguments_are_checked_before_launch(lib):
+    """pdq_lml_adjoint_workspace_size / pdq_lml_fwd / pdq_lml_bwd reject bad
+    checkpoint spacings, missing buffers, a missing or misaligned workspace
+    and a non-zero reserved field before any CUDA call; an empty batch
+    launches nothing."""
+    from probdiffeq_gb300 import _native, ensemble
+
+    cfg = ensemble.make_config(field="fitzhugh_nagumo", num_derivatives=3, ode_dim=2, ssm="isotropic",
+                               strategy="fixedpoint", solver="none", precision="float32")
+    nb = ctypes.c_size_t(0)
+    assert lib.pdq_lml_adjoint_workspace_size(ctypes.byref(cfg), 8, 2000, 10, 0, ctypes.byref(nb)) == 0
+    # plan + 8 samples x (45 states + 200 offsets) x 8 + 201 x 2 innovations + 45 x 2 predicted u, float32
+    per_sample = (45 * 8 + 200 * 8 + 201 * 2 + 45 * 2) * 4
+    assert nb.value - 8 * per_sample > 0 and (nb.value - 8 * per_sample) % 256 == 0
+    small = ctypes.c_size_t(0)
+    assert lib.pdq_lml_adjoint_workspace_size(ctypes.byref(cfg), 8, 2000, 10, 2000, ctypes.byref(small)) == 0
+    assert small.value > 0
+    assert lib.pdq_lml_adjoint_workspace_size(ctypes.byref(cfg), 8, 2000, 10, -1, ctypes.byref(nb)) == 1
+    assert lib.pdq_lml_adjoint_workspace_size(ctypes.byref(cfg), 8, 2000, 10, 2001, ctypes.byref(nb)) == 1
+    assert lib.pdq_lml_adjoint_workspace_size(ctypes.byref(cfg), 8, 2000, 7, 0, ctypes.byref(nb)) == 1
+    bad = ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="isotropic",
+                               strategy="fixedpoint", solver="none", precision="float64")
+    assert lib.pdq_lml_adjoint_workspace_size(ctypes.byref(bad), 8, 2000, 10, 0, ctypes.byref(nb)) == 2
+
+    a = _native.PdqLmlAdjointArgs()
+    a.lml.num_instances, a.lml.num_steps, a.lml.save_every, a.lml.dt = 8, 2000, 10, 0.01
+    assert lib.pdq_lml_fwd(ctypes.byref(cfg), None, None, 0, None) == 1
+    assert lib.pdq_lml_fwd(ctypes.byref(cfg), ctypes.byref(a), None, 0, None) == 1  # buffers missing
+    fake = ctypes.c_void_p(4096)  # never dereferenced: the checks fail first
+    for name in ("params", "y0", "data", "std", "lml", "status"):
+        setattr(a.lml, name, fake)
+    assert lib.pdq_lml_fwd(ctypes.byref(cfg), ctypes.byref(a), None, 0, None) == 4  # no workspace
+    big = ctypes.c_size_t(1 << 40)
+    assert lib.pdq_lml_fwd(ctypes.byref(cfg), ctypes.byref(a), ctypes.c_void_p(4096 + 8), big, None) == 4  # misaligned
+    assert lib.pdq_lml_bwd(ctypes.byref(cfg), ctypes.byref(a), fake, big, None) == 1  # no gradient output
+    a.reserved0 = 1
+    assert lib.pdq_lml_fwd(ctypes.byref(cfg), ctypes.byref(a), fake, big, None) == 1
+    a.reserved0 = 0
+    a.checkpoint_every = 2001
+    assert lib.pdq_lml_fwd(ctypes.byref(cfg), ctypes.byref(a), fake, big, None) == 1
+    a.checkpoint_every = 0
+    a.lml.num_instances = 0
+    assert lib.pdq_lml_fwd(ctypes.byref(cfg), ctypes.byref(a), None, 0, None) == 0
+    assert lib.pdq_lml_bwd(ctypes.byref(cfg), ctypes.byref(a), None, 0, None) == 0
