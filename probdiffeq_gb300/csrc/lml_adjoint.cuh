@@ -40,7 +40,11 @@
 //
 // Residual layout (type T, after the plan): element e of sample b at
 // res[e * B + b], so the 32 samples of a warp, which run in lock step on the
-// fixed grid, touch consecutive addresses.  Per sample:
+// fixed grid, touch consecutive addresses.  The plan's step tables reach the
+// warp through shared memory, a chunk of kLmlChunk steps at a time (one
+// memory latency per chunk), in either direction; what a step or an
+// observation reads from the residuals is loaded one step or observation
+// ahead.  Per sample:
 //   [0, S n d)              the state at steps 0, C, 2C, ... (S = ceil(N / C))
 //   [OX, OX + (K-1) n d)    xi_k (forward pass); the adjoint of xi_k (backward pass)
 //   [ODX, ODX + K d)        dx_k, the innovations of the LML recursion
@@ -74,33 +78,99 @@ struct LmlAdjLayout {
   }
 };
 
-// The plan tables of one step (g[n], K[n][n]) into registers, with 16-byte
-// loads through the read-only path (every lane of a warp reads the same
-// address, so each load is one broadcast).
+// The warp copies the step tables of chunk c (steps c * kLmlChunk + 1 ...,
+// at most kLmlChunk of them) into shared memory with coalesced loads: one
+// memory latency per chunk instead of one per step.  Every lane of the warp
+// must call it at the same point (the fixed grid keeps the lanes in lock
+// step; lanes without a sample stay in the loops for this).
 template <typename T, int KS>
-PDQ_D void lml_load_step_table(const T* __restrict__ src, T (&dst)[KS]) {
+PDQ_D void lml_stage_chunk(T* stage, const T* plan, int chunk, int num_steps, int lane) {
+  const int first = chunk * kLmlChunk;
+  const int count = min(kLmlChunk, num_steps - first) * KS;
+  const T* src = plan + int64_t(first) * KS;
+#if defined(__CUDA_ARCH__)
+  __syncwarp();
+  for (int e = lane; e < count; e += 32) stage[e] = src[e];
+  __syncwarp();
+#else
+  // host runs of the kernel bodies execute one lane at a time: it stages the whole chunk
+  (void)lane;
+  for (int e = 0; e < count; ++e) stage[e] = src[e];
+#endif
+}
+
+// One step's tables (g[n], K[n][n]) from the shared-memory stage into
+// registers with 16-byte loads.
+template <typename T, int KS>
+PDQ_D void lml_read_step_table(const T* tbl, T (&dst)[KS]) {
   if constexpr (sizeof(T) == 4 && KS % 4 == 0) {
-    const float4* v = reinterpret_cast<const float4*>(src);
+    const float4* v = reinterpret_cast<const float4*>(tbl);
 #pragma unroll
     for (int e = 0; e < KS / 4; ++e) {
-      const float4 x = __ldg(v + e);
+      const float4 x = v[e];
       dst[4 * e] = x.x;
       dst[4 * e + 1] = x.y;
       dst[4 * e + 2] = x.z;
       dst[4 * e + 3] = x.w;
     }
   } else if constexpr (sizeof(T) == 8 && KS % 2 == 0) {
-    const double2* v = reinterpret_cast<const double2*>(src);
+    const double2* v = reinterpret_cast<const double2*>(tbl);
 #pragma unroll
     for (int e = 0; e < KS / 2; ++e) {
-      const double2 x = __ldg(v + e);
+      const double2 x = v[e];
       dst[2 * e] = x.x;
       dst[2 * e + 1] = x.y;
     }
   } else {
 #pragma unroll
-    for (int e = 0; e < KS; ++e) dst[e] = __ldg(src + e);
+    for (int e = 0; e < KS; ++e) dst[e] = tbl[e];
   }
+}
+
+// What the LML recursion reads at observation k: the marginalisation's
+// tables and offset (k < K-1), the observed std and gain, log|ry| and the
+// data.  Loaded one observation ahead so the loads overlap the arithmetic.
+template <typename T, int n, int D>
+struct LmlObs {
+  T xi[n][D];  // offset xi_k (value pass) or innovation dx_k in xi[0] (adjoint pass)
+  T A[n][n], tl[n], to[n];
+  T ry, gain[n];
+  double lr, y[D];
+};
+
+template <typename T, int NU, int D>
+PDQ_D void lml_load_obs(LmlObs<T, NU + 1, D>& o, int k, int num_obs, const T* obs_tbl, const T* bay,
+                        const double* logry, const double* data, const T* res, int64_t ox, int64_t odx, int64_t B,
+                        bool adjoint) {
+  constexpr int n = NU + 1;
+  if (k < num_obs - 1) {
+    const T* t = obs_tbl + int64_t(k) * lml_plan_obs<NU>();
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+#pragma unroll
+      for (int q = 0; q < n; ++q) o.A[i][q] = t[i * n + q];
+      o.tl[i] = t[2 * n * n + i];
+      o.to[i] = t[2 * n * n + n + i];
+    }
+  }
+  if (adjoint) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) o.xi[0][j] = res[(odx + int64_t(k) * D + j) * B];
+  } else {
+    if (k < num_obs - 1) {
+      const T* x = res + (ox + int64_t(k) * n * D) * B;
+#pragma unroll
+      for (int i = 0; i < n; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) o.xi[i][j] = x[int64_t(i * D + j) * B];
+    }
+    o.lr = logry[k];
+#pragma unroll
+    for (int j = 0; j < D; ++j) o.y[j] = data[int64_t(k) * D + j];
+  }
+  o.ry = bay[k * (n + 1)];
+#pragma unroll
+  for (int i = 0; i < n; ++i) o.gain[i] = bay[k * (n + 1) + 1 + i];
 }
 
 // One step of the mean recursion on values: predict, TS0 update with the
@@ -141,8 +211,11 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
   constexpr int P = F::P;
   constexpr int kStep = lml_plan_step<NU>();
   const int64_t B = a.B;
-  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (b >= B) return;
+  const int64_t gb = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  // lanes past the batch stay for the warp's staging of the plan
+  const bool valid = gb < B;
+  const int64_t b = valid ? gb : 0;
+  const int lane = threadIdx.x & 31;
   const int N = a.num_steps;
   const int C = aa.ckpt;
   const int num_obs = N / a.save_every + 1;
@@ -150,6 +223,7 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
   T* const res = reinterpret_cast<T*>(aa.res) + b;  // element e at res[e * B]
   const T* const plan = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(a.plan) + kLmlPlanKeyBytes);
   const T* const obs_tbl = plan + int64_t(N) * kStep;
+  __shared__ __align__(16) T stage[kLmlChunk * kStep];  // one warp per block
 
   // ---- parameters; Taylor-mode initial derivatives in double ----
   double pd[P];
@@ -171,18 +245,19 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
     for (int j = 0; j < D; ++j) {
       m[i][j] = T(tc[i][j]);
       bxi[i][j] = T(0);
-      res[int64_t(i * D + j) * B] = m[i][j];  // checkpoint 0
+      if (valid) res[int64_t(i * D + j) * B] = m[i][j];  // checkpoint 0
     }
   const T h = T(a.dt);
   T p[n], pinv[n];
   precon<T, NU>(h, p, pinv);
 
   int status = PDQ_INSTANCE_OK;
-  T tb[kStep];
-  lml_load_step_table<T, kStep>(plan, tb);
   for (int s = 1; s <= N; ++s) {
-    T tn[kStep];
-    if (s < N) lml_load_step_table<T, kStep>(plan + int64_t(s) * kStep, tn);
+    const int within = (s - 1) % kLmlChunk;
+    if (within == 0) lml_stage_chunk<T, kStep>(stage, plan, (s - 1) / kLmlChunk, N, lane);
+    if (!valid || status != PDQ_INSTANCE_OK) continue;
+    T tb[kStep];
+    lml_read_step_table<T, kStep>(stage + within * kStep, tb);
     // the merged backward conditional's offset: xi + K m (m before the step)
 #pragma unroll
     for (int i = 0; i < n; ++i)
@@ -196,8 +271,8 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
     T mp0[D];
     lml_value_step<T, NU, F>(m, tb, p, pinv, th, mp0);
     if (!(m[0][0] == m[0][0])) {
-      status = PDQ_INSTANCE_NONFINITE;
-      break;
+      status = PDQ_INSTANCE_NONFINITE;  // stays in the loop for the staging
+      continue;
     }
     if (s % a.save_every == 0) {
       T* dst = res + (L.ox + int64_t(s / a.save_every - 1) * n * D) * B;
@@ -216,11 +291,8 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
 #pragma unroll
         for (int j = 0; j < D; ++j) dst[int64_t(i * D + j) * B] = m[i][j];
     }
-    if (s < N) {
-#pragma unroll
-      for (int e = 0; e < kStep; ++e) tb[e] = tn[e];
-    }
   }
+  if (!valid) return;
 
   // ---- LML: reverse Kalman filter over the data (evaluate_lml), storing the innovations ----
   double pdf = 0.0;
@@ -235,43 +307,43 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
                                     reinterpret_cast<const unsigned char*>(a.plan) +
                                     lml_plan_std_offset(NU, N, a.save_every, int(sizeof(T)))) + num_obs;
     const double LOG2PI = 1.8378770664093453;
+    LmlObs<T, n, D> cur, nxt;
+    lml_load_obs<T, NU, D>(cur, num_obs - 1, num_obs, obs_tbl, bay, logry, a.data, res, L.ox, L.odx, B, false);
     int num = 0;
     for (int k = num_obs - 1; k >= 0; --k) {
+      if (k > 0) lml_load_obs<T, NU, D>(nxt, k - 1, num_obs, obs_tbl, bay, logry, a.data, res, L.ox, L.odx, B, false);
       if (k < num_obs - 1) {
-        const T* o = obs_tbl + int64_t(k) * lml_plan_obs<NU>();
-        const T* xi = res + (L.ox + int64_t(k) * n * D) * B;
         T pm[n][D];
 #pragma unroll
         for (int i = 0; i < n; ++i)
 #pragma unroll
           for (int j = 0; j < D; ++j) {
-            T acc = xi[int64_t(i * D + j) * B];
+            T acc = cur.xi[i][j];
 #pragma unroll
-            for (int q = 0; q < n; ++q) acc = acc + o[i * n + q] * (o[2 * n * n + q] * rm[q][j]);
-            pm[i][j] = o[2 * n * n + n + i] * acc;
+            for (int q = 0; q < n; ++q) acc = acc + cur.A[i][q] * (cur.tl[q] * rm[q][j]);
+            pm[i][j] = cur.to[i] * acc;
           }
 #pragma unroll
         for (int i = 0; i < n; ++i)
 #pragma unroll
           for (int j = 0; j < D; ++j) rm[i][j] = pm[i][j];
       }
-      const T ry = bay[k * (n + 1)];
-      const double lr = logry[k];
       double pdf_n = 0.0;
 #pragma unroll
       for (int j = 0; j < D; ++j) {
-        const T dx = T(a.data[int64_t(k) * D + j]) - rm[0][j];
+        const T dx = T(cur.y[j]) - rm[0][j];
         res[(L.odx + int64_t(k) * D + j) * B] = dx;
-        const T w = dx / ry;
-        pdf_n += -0.5 * (2.0 * lr + double(w) * double(w) + LOG2PI);
+        const T w = dx / cur.ry;
+        pdf_n += -0.5 * (2.0 * cur.lr + double(w) * double(w) + LOG2PI);
 #pragma unroll
-        for (int i = 0; i < n; ++i) rm[i][j] = rm[i][j] + bay[k * (n + 1) + 1 + i] * dx;
+        for (int i = 0; i < n; ++i) rm[i][j] = rm[i][j] + cur.gain[i] * dx;
       }
       if (a.average_pdfs && num > 0)
         pdf = (pdf * num + pdf_n) / (num + 1);
       else
         pdf += pdf_n;
       ++num;
+      if (k > 0) cur = nxt;
     }
     if (!(pdf == pdf)) status = PDQ_INSTANCE_NONFINITE;
   }
@@ -289,10 +361,15 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
   constexpr int NT = D + P;  // tangent directions of the Jacobian evaluation
   constexpr int kStep = lml_plan_step<NU>();
   const int64_t B = a.B;
-  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (b >= B) return;
+  const int64_t gb = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool in_batch = gb < B;
+  const int64_t b = in_batch ? gb : 0;
+  const int lane = threadIdx.x & 31;
   const double nan = __longlong_as_double(0x7ff8000000000000ULL);
-  if (a.status[b] != PDQ_INSTANCE_OK) {
+  // samples whose value pass failed get NaN gradients; their lanes (and
+  // lanes past the batch) stay for the warp's staging of the plan
+  const bool valid = in_batch && a.status[b] == PDQ_INSTANCE_OK;
+  if (in_batch && !valid) {
     if (a.grad) {
 #pragma unroll
       for (int q = 0; q < P; ++q) a.grad[b * P + q] = nan;
@@ -301,7 +378,6 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
 #pragma unroll
       for (int j = 0; j < D; ++j) aa.grad_y0[b * D + j] = nan;
     }
-    return;
   }
   const int N = a.num_steps;
   const int C = aa.ckpt;
@@ -311,8 +387,10 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
   const T* const plan = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(a.plan) + kLmlPlanKeyBytes);
   const T* const obs_tbl = plan + int64_t(N) * kStep;
   const T* const bay = obs_tbl + int64_t(num_obs - 1) * lml_plan_obs<NU>() + n * n;
+  __shared__ __align__(16) T stage[kLmlChunk * kStep];  // one warp per block
   // d loss / d pdf_k: the cotangent, divided by the number of terms for averaged pdfs
-  const double scale = (aa.cotangent ? aa.cotangent[b] : 1.0) / (a.average_pdfs ? double(num_obs) : 1.0);
+  const double scale =
+      valid ? (aa.cotangent ? aa.cotangent[b] : 1.0) / (a.average_pdfs ? double(num_obs) : 1.0) : 0.0;
 
   // ---- the LML recursion in reverse: adjoints of xi_k and of the terminal mean ----
   T rb[n][D];
@@ -320,38 +398,44 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
   for (int i = 0; i < n; ++i)
 #pragma unroll
     for (int j = 0; j < D; ++j) rb[i][j] = T(0);
-  for (int k = 0; k < num_obs; ++k) {
-    const double ry = double(bay[k * (n + 1)]);
+  if (valid) {
+    LmlObs<T, n, D> cur, nxt;
+    lml_load_obs<T, NU, D>(cur, 0, num_obs, obs_tbl, bay, nullptr, nullptr, res, L.ox, L.odx, B, true);
+    for (int k = 0; k < num_obs; ++k) {
+      if (k + 1 < num_obs)
+        lml_load_obs<T, NU, D>(nxt, k + 1, num_obs, obs_tbl, bay, nullptr, nullptr, res, L.ox, L.odx, B, true);
+      const double ry = double(cur.ry);
 #pragma unroll
-    for (int j = 0; j < D; ++j) {
-      // r <- r + gain dx, dx = y - r[0], pdf = -0.5 (dx / ry)^2 + ...
-      T t = T(0);
+      for (int j = 0; j < D; ++j) {
+        // r <- r + gain dx, dx = y - r[0], pdf = -0.5 (dx / ry)^2 + ...
+        T t = T(0);
 #pragma unroll
-      for (int i = 0; i < n; ++i) t += bay[k * (n + 1) + 1 + i] * rb[i][j];
-      const double dx = double(res[(L.odx + int64_t(k) * D + j) * B]);
-      rb[0][j] -= t + T(-scale * (dx / ry) / ry);
-    }
-    if (k < num_obs - 1) {
-      // r = to . (xi_k + A_k (tl . r))
-      const T* o = obs_tbl + int64_t(k) * lml_plan_obs<NU>();
-      T* xib = res + (L.ox + int64_t(k) * n * D) * B;
-      T x[n][D];
+        for (int i = 0; i < n; ++i) t += cur.gain[i] * rb[i][j];
+        const double dx = double(cur.xi[0][j]);
+        rb[0][j] -= t + T(-scale * (dx / ry) / ry);
+      }
+      if (k < num_obs - 1) {
+        // r = to . (xi_k + A_k (tl . r))
+        T* xib = res + (L.ox + int64_t(k) * n * D) * B;
+        T x[n][D];
 #pragma unroll
-      for (int i = 0; i < n; ++i)
+        for (int i = 0; i < n; ++i)
 #pragma unroll
-        for (int j = 0; j < D; ++j) {
-          x[i][j] = o[2 * n * n + n + i] * rb[i][j];
-          xib[int64_t(i * D + j) * B] = x[i][j];
-        }
+          for (int j = 0; j < D; ++j) {
+            x[i][j] = cur.to[i] * rb[i][j];
+            xib[int64_t(i * D + j) * B] = x[i][j];
+          }
 #pragma unroll
-      for (int q = 0; q < n; ++q)
+        for (int q = 0; q < n; ++q)
 #pragma unroll
-        for (int j = 0; j < D; ++j) {
-          T acc = T(0);
+          for (int j = 0; j < D; ++j) {
+            T acc = T(0);
 #pragma unroll
-          for (int i = 0; i < n; ++i) acc += o[i * n + q] * x[i][j];
-          rb[q][j] = o[2 * n * n + q] * acc;
-        }
+            for (int i = 0; i < n; ++i) acc += cur.A[i][q] * x[i][j];
+            rb[q][j] = cur.tl[q] * acc;
+          }
+      }
+      if (k + 1 < num_obs) cur = nxt;
     }
   }
 
@@ -375,6 +459,13 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
 #pragma unroll
     for (int j = 0; j < D; ++j) mb[i][j] = rb[i][j];
 
+  int staged = -1;            // chunk of step tables in `stage`
+  int kobs = -1, knext = -1;  // observation intervals of xib and of the prefetched xin
+  T xib[n][D], xin[n][D];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) xib[i][j] = xin[i][j] = T(0);
   for (int seg = aa.num_ckpt - 1; seg >= 0; --seg) {
     const int s0 = seg * C;
     const int s1 = min(N, s0 + C);
@@ -385,39 +476,66 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
 #pragma unroll
       for (int i = 0; i < n; ++i)
 #pragma unroll
-        for (int j = 0; j < D; ++j) m[i][j] = src[int64_t(i * D + j) * B];
-      T tb[kStep];
-      lml_load_step_table<T, kStep>(plan + int64_t(s0) * kStep, tb);
+        for (int j = 0; j < D; ++j) m[i][j] = valid ? src[int64_t(i * D + j) * B] : T(0);
       for (int s = s0 + 1; s <= s1; ++s) {
-        T tn[kStep];
-        if (s < s1) lml_load_step_table<T, kStep>(plan + int64_t(s) * kStep, tn);
+        const int c = (s - 1) / kLmlChunk;
+        if (c != staged) {
+          lml_stage_chunk<T, kStep>(stage, plan, c, N, lane);
+          staged = c;
+        }
+        if (!valid) continue;
+        T tb[kStep];
+        lml_read_step_table<T, kStep>(stage + (s - 1 - c * kLmlChunk) * kStep, tb);
         T mp0[D];
         lml_value_step<T, NU, F>(m, tb, p, pinv, th, mp0);
 #pragma unroll
         for (int j = 0; j < D; ++j) res[(L.osb + int64_t(s - s0 - 1) * D + j) * B] = mp0[j];
-        if (s < s1) {
-#pragma unroll
-          for (int e = 0; e < kStep; ++e) tb[e] = tn[e];
-        }
       }
     }
     // differentiate the segment's steps, last to first
-    int kobs = -1;
-    T xib[n][D];
-    T tb[kStep];
-    lml_load_step_table<T, kStep>(plan + int64_t(s1 - 1) * kStep, tb);
+    T u1[D];  // the predicted u of the next step to differentiate (loaded one step ahead)
+#pragma unroll
+    for (int j = 0; j < D; ++j) u1[j] = valid ? res[(L.osb + int64_t(s1 - s0 - 1) * D + j) * B] : T(0);
     for (int s = s1; s > s0; --s) {
-      T tn[kStep];
-      if (s - 1 > s0) lml_load_step_table<T, kStep>(plan + int64_t(s - 2) * kStep, tn);
+      const int c = (s - 1) / kLmlChunk;
+      if (c != staged) {
+        lml_stage_chunk<T, kStep>(stage, plan, c, N, lane);
+        staged = c;
+      }
+      if (!valid) continue;
+      T u[D];
+#pragma unroll
+      for (int j = 0; j < D; ++j) u[j] = u1[j];
+      if (s - 1 > s0) {
+#pragma unroll
+        for (int j = 0; j < D; ++j) u1[j] = res[(L.osb + int64_t(s - s0 - 2) * D + j) * B];
+      }
       const int k = (s - 1) / a.save_every;  // the observation interval step s belongs to
       if (k != kobs) {
-        const T* src = res + (L.ox + int64_t(k) * n * D) * B;
+        if (k == knext) {
 #pragma unroll
-        for (int i = 0; i < n; ++i)
+          for (int i = 0; i < n; ++i)
 #pragma unroll
-          for (int j = 0; j < D; ++j) xib[i][j] = src[int64_t(i * D + j) * B];
+            for (int j = 0; j < D; ++j) xib[i][j] = xin[i][j];
+        } else {
+          const T* x = res + (L.ox + int64_t(k) * n * D) * B;
+#pragma unroll
+          for (int i = 0; i < n; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) xib[i][j] = x[int64_t(i * D + j) * B];
+        }
         kobs = k;
+        knext = k - 1;
+        if (knext >= 0) {
+          const T* x = res + (L.ox + int64_t(knext) * n * D) * B;
+#pragma unroll
+          for (int i = 0; i < n; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) xin[i][j] = x[int64_t(i * D + j) * B];
+        }
       }
+      T tb[kStep];
+      lml_read_step_table<T, kStep>(stage + (s - 1 - c * kLmlChunk) * kStep, tb);
       // m' = mp - g (mp[1] - f(mp[0]))
       T rbar[D];
 #pragma unroll
@@ -436,18 +554,18 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
       for (int j = 0; j < D; ++j) mpb[1][j] += rbar[j];
       // f(mp[0], theta): Jacobian on dual numbers (directions: u, then theta)
       {
-        Dual<T, NT> u[D], pt[P], f[D];
+        Dual<T, NT> ud[D], pt[P], f[D];
 #pragma unroll
         for (int j = 0; j < D; ++j) {
-          u[j] = Dual<T, NT>(res[(L.osb + int64_t(s - s0 - 1) * D + j) * B]);
-          u[j].g[j] = T(1);
+          ud[j] = Dual<T, NT>(u[j]);
+          ud[j].g[j] = T(1);
         }
 #pragma unroll
         for (int q = 0; q < P; ++q) {
           pt[q] = Dual<T, NT>(th[q]);
           pt[q].g[D + q] = T(1);
         }
-        F::eval(u, pt, f);
+        F::eval(ud, pt, f);
 #pragma unroll
         for (int j = 0; j < D; ++j) {
           T acc = T(0);
@@ -476,12 +594,9 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
           for (int i = 0; i < n; ++i) x += tb[n + i * n + k2] * xib[i][j];
           mb[k2][j] = x;
         }
-      if (s - 1 > s0) {
-#pragma unroll
-        for (int e = 0; e < kStep; ++e) tb[e] = tn[e];
-      }
     }
   }
+  if (!valid) return;
 
   // ---- the Taylor-mode initialisation: d m_0 / d (theta, y0) on dual numbers ----
   constexpr int NI = P + D;
@@ -522,4 +637,3 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
 }
 
 }  // namespace pdq
-

@@ -1,0 +1,136 @@
+"""Generate the golden fixtures in this directory from the oracle.
+
+    python tests/golden/make_golden.py
+
+The oracle (``oracle/``, the float64 CPU restatement of the reference, pinned
+to the reference's own known-answer and equivalence tests) is run on small
+seeded inputs; inputs and outputs are written as JSON.  The reference itself
+is JAX code that cannot be installed in this environment, so these fixtures
+come from the restatement.  ``tests/test_golden_cpu.py`` re-runs the oracle
+against them; ``tests/test_golden_gpu.py`` checks the CUDA kernels against
+them without running the oracle.
+
+Fixtures:
+  iwp.json         A1 = flip(Pascal), Q1 = lower sqrt of flip(Hilbert) for
+                   nu = 2, 3, 4 and the Taylor preconditioner at dt = 1.234
+                   (_probdiffeq/utilities.py:57-84)
+  lv_filter.json   4 Lotka--Volterra instances, isotropic TS0, filter,
+                   error_residual_std, integral control, nu = 4, dt0 = 0.1:
+                   solver_mle terminal values at t1 = 5 with clip_dt, and
+                   solver_dynamic at save_at (0, 0.7, 2, 3.3, 5) by
+                   interpolation; means, Cholesky factors, output scales and
+                   accepted steps
+  fhn_lml.json     FitzHugh--Nagumo LML on 200 steps of 0.01 with 21
+                   observations (data included), 2 parameter samples with
+                   perturbed initial values: lml, d lml / d params,
+                   d lml / d y0 (PyTorch reverse mode through the oracle)
+"""
+
+import json
+import os
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+NOMINAL_LV = [0.5, 0.05, 0.5, 0.05]
+
+
+def iwp_fixture():
+    from oracle import ssm
+
+    out = {}
+    for nu in (2, 3, 4):
+        A, Q = ssm.system_matrices_1d_iwp(nu)
+        p, p_inv = ssm.preconditioner_taylor(nu)(1.234)
+        out[str(nu)] = {"A": A.tolist(), "Q": Q.tolist(), "p": p.tolist(), "p_inv": p_inv.tolist(), "dt": 1.234}
+    return out
+
+
+def lv_inputs():
+    g = torch.Generator().manual_seed(11)
+    params = torch.tensor(NOMINAL_LV, dtype=torch.float64) * torch.exp(
+        0.2 * torch.randn((4, 4), generator=g, dtype=torch.float64))
+    y0 = 10.0 + 20.0 * torch.rand((4, 2), generator=g, dtype=torch.float64)
+    return params, y0
+
+
+def lv_filter_fixture(params=None, y0=None):
+    """Two configurations, both with the isotropic TS0 filter and nu = 4:
+    solver_mle, clip_dt, terminal values at t1 = 5 (rtol = atol = 1e-6); and
+    solver_dynamic, save_at (0, 0.7, 2, 3.3, 5) reached by interpolation
+    (no clip_dt, rtol = atol = 1e-5)."""
+    from oracle import problems, solvers, ssm
+
+    if params is None:
+        params, y0 = lv_inputs()
+    runs = {
+        "mle_terminal": dict(cls=solvers.SolverMLE, save_at=[0.0, 5.0], tol=1e-6, clip_dt=True),
+        "dynamic_save_at": dict(cls=solvers.SolverDynamic, save_at=[0.0, 0.7, 2.0, 3.3, 5.0], tol=1e-5, clip_dt=False),
+    }
+    out = {"params": params.tolist(), "y0": y0.tolist(), "num_derivatives": 4, "dt0": 0.1}
+    for name, r in runs.items():
+        records = []
+        for b in range(params.shape[0]):
+            tc = problems.taylor_derivatives(problems.lotka_volterra, y0[b], params[b], 4)
+            S = ssm.IsoSSM()
+            c = S.constraint_ode_ts0(lambda u, t, p=params[b]: problems.lotka_volterra(u[0], p))
+            res = solvers.solve_adaptive_save_at(
+                r["cls"](solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c), S.prior_wiener_integrated(tc),
+                r["save_at"], r["tol"], r["tol"], control=solvers.ControlIntegral(), clip_dt=r["clip_dt"], dt0=0.1,
+            )
+            records.append({
+                "u_mean": [u.mean.tolist() for u in res.u],
+                "u_chol": [u.cholesky.tolist() for u in res.u],
+                "output_scale": [float(s) for s in res.output_scale],
+                "num_steps": [int(s) for s in res.num_steps],
+            })
+        out[name] = {"save_at": r["save_at"], "rtol": r["tol"], "atol": r["tol"], "clip_dt": r["clip_dt"],
+                     "records": records}
+    return out
+
+
+def fhn_lml_fixture(inputs=None):
+    from tests import lml_problem
+    from tests.lml_oracle import lml_value_and_grads
+
+    dt, save_every = 0.01, 10
+    if inputs is None:
+        num_steps, data = lml_problem.observations(t1=2.0, dt=dt, save_every=save_every)
+        thetas = lml_problem.theta_samples(2, seed=12)
+        y0s = np.tile(lml_problem.U0, (2, 1)) + np.array([[0.0, 0.0], [0.05, -0.02]])
+    else:
+        num_steps, data, thetas, y0s = inputs
+    out = {"dt": dt, "num_steps": num_steps, "save_every": save_every, "std": lml_problem.STD,
+           "data": np.asarray(data).tolist(), "params": np.asarray(thetas).tolist(), "y0": np.asarray(y0s).tolist(),
+           "lml": [], "grad": [], "grad_y0": []}
+    for b in range(len(thetas)):
+        v, g, gy = lml_value_and_grads(np.asarray(thetas[b]), np.asarray(y0s[b]), np.asarray(data), dt, num_steps,
+                                       save_every)
+        out["lml"].append(v)
+        out["grad"].append(g.tolist())
+        out["grad_y0"].append(gy.tolist())
+    return out
+
+
+def load(name):
+    with open(os.path.join(HERE, name)) as f:
+        return json.load(f)
+
+
+def main():
+    torch.set_default_dtype(torch.float64)
+    for name, fn in (("iwp.json", iwp_fixture), ("lv_filter.json", lv_filter_fixture),
+                     ("fhn_lml.json", fhn_lml_fixture)):
+        with open(os.path.join(HERE, name), "w") as f:
+            json.dump(fn(), f, indent=1)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()
