@@ -252,8 +252,12 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
   precon<T, NU>(h, p, pinv);
 
   int status = PDQ_INSTANCE_OK;
+  // counters and running pointers instead of run-time divisions per step
+  int to_obs = a.save_every, to_ckpt = C;
+  T* xi_dst = res + L.ox * B;          // offset of the next observation interval
+  T* ck_dst = res + int64_t(n) * D * B;  // checkpoint 1
   for (int s = 1; s <= N; ++s) {
-    const int within = (s - 1) % kLmlChunk;
+    const int within = (s - 1) & (kLmlChunk - 1);
     if (within == 0) lml_stage_chunk<T, kStep>(stage, plan, (s - 1) / kLmlChunk, N, lane);
     if (!valid || status != PDQ_INSTANCE_OK) continue;
     T tb[kStep];
@@ -274,22 +278,26 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
       status = PDQ_INSTANCE_NONFINITE;  // stays in the loop for the staging
       continue;
     }
-    if (s % a.save_every == 0) {
-      T* dst = res + (L.ox + int64_t(s / a.save_every - 1) * n * D) * B;
+    if (--to_obs == 0) {
+      to_obs = a.save_every;
 #pragma unroll
       for (int i = 0; i < n; ++i)
 #pragma unroll
         for (int j = 0; j < D; ++j) {
-          dst[int64_t(i * D + j) * B] = bxi[i][j];
+          xi_dst[int64_t(i * D + j) * B] = bxi[i][j];
           bxi[i][j] = T(0);
         }
+      xi_dst += int64_t(n) * D * B;
     }
-    if (s % C == 0 && s < N) {
-      T* dst = res + int64_t(s / C) * n * D * B;
+    if (--to_ckpt == 0) {
+      to_ckpt = C;
+      if (s < N) {
 #pragma unroll
-      for (int i = 0; i < n; ++i)
+        for (int i = 0; i < n; ++i)
 #pragma unroll
-        for (int j = 0; j < D; ++j) dst[int64_t(i * D + j) * B] = m[i][j];
+          for (int j = 0; j < D; ++j) ck_dst[int64_t(i * D + j) * B] = m[i][j];
+        ck_dst += int64_t(n) * D * B;
+      }
     }
   }
   if (!valid) return;
@@ -477,6 +485,7 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
       for (int i = 0; i < n; ++i)
 #pragma unroll
         for (int j = 0; j < D; ++j) m[i][j] = valid ? src[int64_t(i * D + j) * B] : T(0);
+      T* sb = res + L.osb * B;  // predicted u of step s0 + 1, then onwards
       for (int s = s0 + 1; s <= s1; ++s) {
         const int c = (s - 1) / kLmlChunk;
         if (c != staged) {
@@ -489,13 +498,18 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
         T mp0[D];
         lml_value_step<T, NU, F>(m, tb, p, pinv, th, mp0);
 #pragma unroll
-        for (int j = 0; j < D; ++j) res[(L.osb + int64_t(s - s0 - 1) * D + j) * B] = mp0[j];
+        for (int j = 0; j < D; ++j) sb[int64_t(j) * B] = mp0[j];
+        sb += int64_t(D) * B;
       }
     }
     // differentiate the segment's steps, last to first
+    const T* sb = res + (L.osb + int64_t(s1 - s0 - 1) * D) * B;  // predicted u of step s1, then backwards
     T u1[D];  // the predicted u of the next step to differentiate (loaded one step ahead)
 #pragma unroll
-    for (int j = 0; j < D; ++j) u1[j] = valid ? res[(L.osb + int64_t(s1 - s0 - 1) * D + j) * B] : T(0);
+    for (int j = 0; j < D; ++j) u1[j] = valid ? sb[int64_t(j) * B] : T(0);
+    // observation interval k of step s and its position r within it: s - 1 = k save_every + r
+    int k = (s1 - 1) / a.save_every;
+    int r = (s1 - 1) - k * a.save_every;
     for (int s = s1; s > s0; --s) {
       const int c = (s - 1) / kLmlChunk;
       if (c != staged) {
@@ -507,10 +521,10 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
 #pragma unroll
       for (int j = 0; j < D; ++j) u[j] = u1[j];
       if (s - 1 > s0) {
+        sb -= int64_t(D) * B;
 #pragma unroll
-        for (int j = 0; j < D; ++j) u1[j] = res[(L.osb + int64_t(s - s0 - 2) * D + j) * B];
+        for (int j = 0; j < D; ++j) u1[j] = sb[int64_t(j) * B];
       }
-      const int k = (s - 1) / a.save_every;  // the observation interval step s belongs to
       if (k != kobs) {
         if (k == knext) {
 #pragma unroll
@@ -594,6 +608,10 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
           for (int i = 0; i < n; ++i) x += tb[n + i * n + k2] * xib[i][j];
           mb[k2][j] = x;
         }
+      if (--r < 0) {
+        r = a.save_every - 1;
+        --k;
+      }
     }
   }
   if (!valid) return;

@@ -494,6 +494,8 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
   precon<T, NU>(h, p, pinv);
 
   int status = PDQ_INSTANCE_OK;
+  int to_obs = a.save_every;  // steps to the next observation (a counter, not a division per step)
+  T* obs_dst = ws;            // stored offset of the next observation interval
   for (int step = 1; step <= a.num_steps; ++step) {
     const int within = (step - 1) % kLmlChunk;
     if (within == 0) {
@@ -582,8 +584,10 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       continue;
     }
     // ---- checkpoint at an observation: store the offset, reset ----
-    if (step % a.save_every == 0) {
-      T* dst = ws + int64_t(step / a.save_every - 1) * XF;
+    if (--to_obs == 0) {
+      to_obs = a.save_every;
+      T* dst = obs_dst;
+      obs_dst += XF;
       int o = 0;
 #pragma unroll
       for (int i = 0; i < n; ++i)
