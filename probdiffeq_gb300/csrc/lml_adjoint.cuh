@@ -336,16 +336,19 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_fwd_kernel(LmlAdjArgs aa)
 #pragma unroll
           for (int j = 0; j < D; ++j) rm[i][j] = pm[i][j];
       }
-      double pdf_n = 0.0;
+      // the whitened residual's squared norm in the bulk type; the log-pdf
+      // and the sum over observations in double
+      T ww = T(0);
 #pragma unroll
       for (int j = 0; j < D; ++j) {
         const T dx = T(cur.y[j]) - rm[0][j];
         res[(L.odx + int64_t(k) * D + j) * B] = dx;
         const T w = dx / cur.ry;
-        pdf_n += -0.5 * (2.0 * cur.lr + double(w) * double(w) + LOG2PI);
+        ww += w * w;
 #pragma unroll
         for (int i = 0; i < n; ++i) rm[i][j] = rm[i][j] + cur.gain[i] * dx;
       }
+      const double pdf_n = -0.5 * (double(D) * (2.0 * cur.lr + LOG2PI) + double(ww));
       if (a.average_pdfs && num > 0)
         pdf = (pdf * num + pdf_n) / (num + 1);
       else
@@ -399,6 +402,7 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
   // d loss / d pdf_k: the cotangent, divided by the number of terms for averaged pdfs
   const double scale =
       valid ? (aa.cotangent ? aa.cotangent[b] : 1.0) / (a.average_pdfs ? double(num_obs) : 1.0) : 0.0;
+  const T tscale = T(scale);
 
   // ---- the LML recursion in reverse: adjoints of xi_k and of the terminal mean ----
   T rb[n][D];
@@ -412,15 +416,14 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
     for (int k = 0; k < num_obs; ++k) {
       if (k + 1 < num_obs)
         lml_load_obs<T, NU, D>(nxt, k + 1, num_obs, obs_tbl, bay, nullptr, nullptr, res, L.ox, L.odx, B, true);
-      const double ry = double(cur.ry);
 #pragma unroll
       for (int j = 0; j < D; ++j) {
-        // r <- r + gain dx, dx = y - r[0], pdf = -0.5 (dx / ry)^2 + ...
+        // r <- r + gain dx, dx = y - r[0], pdf = -0.5 (dx / ry)^2 + ...: d pdf / d dx = -dx / ry^2
         T t = T(0);
 #pragma unroll
         for (int i = 0; i < n; ++i) t += cur.gain[i] * rb[i][j];
-        const double dx = double(cur.xi[0][j]);
-        rb[0][j] -= t + T(-scale * (dx / ry) / ry);
+        const T w = cur.xi[0][j] / cur.ry;
+        rb[0][j] -= t - tscale * (w / cur.ry);
       }
       if (k < num_obs - 1) {
         // r = to . (xi_k + A_k (tl . r))
@@ -458,9 +461,15 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
   const T h = T(a.dt);
   T p[n], pinv[n];
   precon<T, NU>(h, p, pinv);
+  // d lml / d theta: partial sums over an observation interval in the bulk
+  // type (thp), added to the double total (thb) once per interval
   double thb[P];
+  T thp[P];
 #pragma unroll
-  for (int q = 0; q < P; ++q) thb[q] = 0.0;
+  for (int q = 0; q < P; ++q) {
+    thb[q] = 0.0;
+    thp[q] = T(0);
+  }
   T mb[n][D];  // adjoint of the mean after the current step
 #pragma unroll
   for (int i = 0; i < n; ++i)
@@ -592,7 +601,7 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
           T acc = T(0);
 #pragma unroll
           for (int l = 0; l < D; ++l) acc += f[l].g[D + q] * rbar[l];
-          thb[q] -= double(acc);
+          thp[q] -= acc;
         }
       }
       // mp = p . A1 (p^-1 . m), and xi_k += K m
@@ -611,39 +620,47 @@ __global__ void __launch_bounds__(kLmlThreads) lml_adj_bwd_kernel(LmlAdjArgs aa)
       if (--r < 0) {
         r = a.save_every - 1;
         --k;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+          thb[q] += double(thp[q]);
+          thp[q] = T(0);
+        }
       }
     }
   }
   if (!valid) return;
+#pragma unroll
+  for (int q = 0; q < P; ++q) thb[q] += double(thp[q]);
 
-  // ---- the Taylor-mode initialisation: d m_0 / d (theta, y0) on dual numbers ----
+  // ---- the Taylor-mode initialisation: d m_0 / d (theta, y0) on dual numbers (bulk type) ----
   constexpr int NI = P + D;
-  Dual<double, NI> pdd[P], ydd[D];
+  Dual<T, NI> pdd[P], ydd[D];
 #pragma unroll
   for (int q = 0; q < P; ++q) {
-    pdd[q] = Dual<double, NI>(pd[q]);
-    pdd[q].g[q] = 1.0;
+    pdd[q] = Dual<T, NI>(th[q]);
+    pdd[q].g[q] = T(1);
   }
 #pragma unroll
   for (int j = 0; j < D; ++j) {
-    ydd[j] = Dual<double, NI>(a.y0[b * D + j]);
-    ydd[j].g[P + j] = 1.0;
+    ydd[j] = Dual<T, NI>(T(a.y0[b * D + j]));
+    ydd[j].g[P + j] = T(1);
   }
-  Dual<double, NI> tcd[n][D];
+  Dual<T, NI> tcd[n][D];
   taylor_init<F, NU>(ydd, pdd, tcd);
-  double yb[D];
+  T acc[NI];
 #pragma unroll
-  for (int j = 0; j < D; ++j) yb[j] = 0.0;
+  for (int q = 0; q < NI; ++q) acc[q] = T(0);
 #pragma unroll
   for (int i = 0; i < n; ++i)
 #pragma unroll
-    for (int j = 0; j < D; ++j) {
-      const double w = double(mb[i][j]);
+    for (int j = 0; j < D; ++j)
 #pragma unroll
-      for (int q = 0; q < P; ++q) thb[q] += w * tcd[i][j].g[q];
+      for (int q = 0; q < NI; ++q) acc[q] += mb[i][j] * tcd[i][j].g[q];
 #pragma unroll
-      for (int l = 0; l < D; ++l) yb[l] += w * tcd[i][j].g[P + l];
-    }
+  for (int q = 0; q < P; ++q) thb[q] += double(acc[q]);
+  double yb[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) yb[j] = double(acc[P + j]);
   if (a.grad) {
 #pragma unroll
     for (int q = 0; q < P; ++q) a.grad[b * P + q] = thb[q];

@@ -645,17 +645,26 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       // model_k = to_derivative(0, std_k); bayes_rule_and_logpdf_tree
       const T ry = bay[k * (n + 1)];
       const double lr = logry[k];
-      DD pdf_n(0.0);
+      // the whitened residual's squared norm (and its tangent) in the bulk
+      // type; the log-pdf and the sum over observations in double (few
+      // float64 operations: the FP64 pipe issues at 1/64 of the FP32 rate)
+      T ww = T(0), wg[TG];
+#pragma unroll
+      for (int q = 0; q < TG; ++q) wg[q] = T(0);
 #pragma unroll
       for (int j = 0; j < D; ++j) {
         const DT dx = DT(T(a.data[int64_t(k) * D + j])) - rm[0][j];
         const DT w = dx / ry;
-        pdf_n.v += -0.5 * (2.0 * lr + double(w.v) * double(w.v) + LOG2PI);
+        ww += w.v * w.v;
 #pragma unroll
-        for (int q = 0; q < TG; ++q) pdf_n.g[q] += -0.5 * (2.0 * double(w.v) * double(w.g[q]));
+        for (int q = 0; q < TG; ++q) wg[q] += w.v * w.g[q];
 #pragma unroll
         for (int i = 0; i < n; ++i) rm[i][j] = rm[i][j] + bay[k * (n + 1) + 1 + i] * dx;
       }
+      DD pdf_n;
+      pdf_n.v = -0.5 * (double(D) * (2.0 * lr + LOG2PI) + double(ww));
+#pragma unroll
+      for (int q = 0; q < TG; ++q) pdf_n.g[q] = -double(wg[q]);
       if (a.average_pdfs && num > 0) {
         pdf.v = (pdf.v * num + pdf_n.v) / (num + 1);
 #pragma unroll
