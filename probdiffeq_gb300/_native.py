@@ -434,6 +434,14 @@ def lml_adjoint_workspace_bytes(cfg, B, num_steps, save_every, checkpoint_every=
     return int(nbytes.value)
 
 
+# Free adjoint workspaces per (device, stream, size).  A workspace holds the
+# shared covariance plan (built on the device the first time, in
+# milliseconds) followed by one call's residuals; a workspace whose backward
+# call has been enqueued (lml_bwd(..., release=True)) may serve the next
+# forward call on the same stream, which then reuses its plan.
+_LML_ADJ_POOL = {}
+
+
 def lml_fwd(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every, average_pdfs=False, checkpoint_every=0,
             stream=None, workspace=None, outputs=None):
     """Call pdq_lml_fwd on device tensors (float64, contiguous).
@@ -441,6 +449,8 @@ def lml_fwd(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every, averag
     Returns a dict with ``lml`` (B,), ``status`` (B,) and the state that
     :func:`lml_bwd` needs (the argument struct and the workspace holding the
     plan and the residuals; keep it untouched until the backward call).
+    Without ``workspace`` one is taken from the pool of released workspaces
+    of this device, stream and size, or allocated.
     """
     lib = load()
     B = y0.shape[0]
@@ -452,8 +462,11 @@ def lml_fwd(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every, averag
         }
     nbytes = lml_adjoint_workspace_bytes(cfg, B, num_steps, save_every, checkpoint_every)
     ws = workspace
+    pool_key = None
     if ws is None:
-        ws = torch.zeros(max(1, nbytes), dtype=torch.uint8, device=dev)
+        pool_key = (str(dev), _stream_handle(stream).value, int(nbytes))
+        free = _LML_ADJ_POOL.get(pool_key)
+        ws = free.pop() if free else torch.zeros(max(1, nbytes), dtype=torch.uint8, device=dev)
     elif ws.numel() * ws.element_size() < nbytes:
         raise ValueError("the LML workspace is smaller than pdq_lml_adjoint_workspace_size")
     a = PdqLmlAdjointArgs()
@@ -468,15 +481,33 @@ def lml_fwd(cfg, params, y0, data, std, *, t0, dt, num_steps, save_every, averag
     outputs["_workspace"] = ws
     # the inputs stay referenced: the backward call reads them again
     outputs["_saved"] = (cfg, a, nbytes, params, y0, data, std, stream)
+    outputs["_pool_key"] = pool_key
     return outputs
 
 
-def lml_bwd(fwd, cotangent=None, *, params_grad=True, y0_grad=False, outputs=None):
+def lml_release(fwd):
+    """Return the workspace of :func:`lml_fwd`'s call ``fwd`` to the pool (its
+    residuals are then no longer available to :func:`lml_bwd`).  Launches
+    already enqueued on the call's stream still see them: a later forward
+    call on that stream runs after them."""
+    key = fwd.get("_pool_key")
+    ws = fwd.pop("_workspace", None)
+    fwd["_released"] = True
+    if key is not None and ws is not None:
+        _LML_ADJ_POOL.setdefault(key, []).append(ws)
+
+
+def lml_bwd(fwd, cotangent=None, *, params_grad=True, y0_grad=False, outputs=None, release=False):
     """Call pdq_lml_bwd for the residuals of :func:`lml_fwd`'s call ``fwd``.
 
     cotangent: (B,) float64 device tensor (d loss / d lml) or None for ones.
     Returns ``{"grad": (B, P) or None, "grad_y0": (B, d) or None}``.
+    ``release=True`` returns the workspace to the pool after enqueueing the
+    launch (no further backward call on ``fwd``).
     """
+    if fwd.get("_released"):
+        raise RuntimeError("the residuals of this LML forward call were released after its backward call; "
+                           "run the forward call again to differentiate it again")
     lib = load()
     cfg, a0, nbytes, params, y0, data, std, stream = fwd["_saved"]
     B, P, D = y0.shape[0], params.shape[1], y0.shape[1]
@@ -494,6 +525,8 @@ def lml_bwd(fwd, cotangent=None, *, params_grad=True, y0_grad=False, outputs=Non
     check(lib.pdq_lml_bwd(ctypes.byref(cfg), ctypes.byref(a), _ptr(fwd["_workspace"]), ctypes.c_size_t(nbytes),
                           _stream_handle(stream)), "pdq_lml_bwd")
     outputs["_cotangent"] = cotangent
+    if release:
+        lml_release(fwd)
     return outputs
 
 def sample_markov(ssm, num_derivatives, ode_dim, marginal_mean, marginal_chol, posterior, normals, stream=None):

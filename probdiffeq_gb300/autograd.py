@@ -50,14 +50,19 @@ class _LmlAdjoint(torch.autograd.Function):
             t0=t0, dt=dt, num_steps=num_steps, save_every=save_every, average_pdfs=average_pdfs,
             checkpoint_every=checkpoint_every, stream=stream,
         )
-        ctx.fwd = fwd
         ctx.mark_non_differentiable(fwd["status"])
+        if ctx.needs_input_grad[0] or ctx.needs_input_grad[1]:
+            ctx.fwd = fwd
+        else:
+            _native.lml_release(fwd)  # no backward will come: the workspace serves the next call
         return fwd["lml"], fwd["status"]
 
     @staticmethod
     def backward(ctx, g_lml, g_status):
         want_p, want_y0 = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
-        out = _native.lml_bwd(ctx.fwd, g_lml, params_grad=want_p, y0_grad=want_y0)
+        # one backward per forward: the workspace (with its plan) goes back to
+        # the pool for the next forward call on this stream
+        out = _native.lml_bwd(ctx.fwd, g_lml, params_grad=want_p, y0_grad=want_y0, release=True)
         return (out["grad"], out["grad_y0"], None, None, None, None, None, None, None, None, None, None)
 
 
