@@ -1,13 +1,14 @@
-// Runs the float64 adjoint LML kernels (FitzHugh-Nagumo, nu = 3) on the CPU:
+// Runs the float64 adjoint LML kernels on the CPU:
 // the plan kernel's single thread, then lml_adj_fwd_kernel and
 // lml_adj_bwd_kernel for every sample as its own "thread" (they need no
 // cooperation between threads).  Buffers have the exact sizes the library
 // computes, so AddressSanitizer flags any access outside them.
 //
-// Input file (whitespace-separated): B N save_every C average_pdfs, then
-// params (B x 3), y0 (B x 2), data (K x 2), std (K), cotangent (B), dt,
-// Q1 (4 x 4, row-major), K = N / save_every + 1.
-// Output: one line per sample: status lml grad[3] grad_y0[2].
+// Input file (whitespace-separated): field nu B N save_every C average_pdfs,
+// then params (B x P), y0 (B x 2), data (K x 2), std (K), cotangent (B), dt,
+// Q1 ((nu + 1) x (nu + 1), row-major), K = N / save_every + 1; field 0 is
+// FitzHugh-Nagumo (P = 3), field 1 Lotka-Volterra (P = 4); nu is 2 or 3.
+// Output: one line per sample: status lml grad[P] grad_y0[2].
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -24,29 +25,24 @@ static bool read_all(FILE* in, std::vector<double>& v) {
   return true;
 }
 
-int main(int argc, char** argv) {
-  if (argc != 2) return 2;
-  FILE* in = fopen(argv[1], "r");
-  if (!in) return 2;
-  long long B;
-  int N, se, C, avg;
-  if (fscanf(in, "%lld %d %d %d %d", &B, &N, &se, &C, &avg) != 5) return 2;
-  if (B < 1 || N < 1 || se < 1 || N % se != 0 || C < 1 || C > N) return 2;
+template <int NU, class F>
+static int run(FILE* in, long long B, int N, int se, int C, int avg) {
+  constexpr int P = F::P;
+  constexpr int n = NU + 1;
   const int K = N / se + 1;
-  std::vector<double> params(B * 3), y0(B * 2), data(K * 2), stdv(K), cot(B), dt(1), q1(16);
+  std::vector<double> params(B * P), y0(B * 2), data(K * 2), stdv(K), cot(B), dt(1), q1(n * n);
   if (!read_all(in, params) || !read_all(in, y0) || !read_all(in, data) || !read_all(in, stdv) ||
       !read_all(in, cot) || !read_all(in, dt) || !read_all(in, q1))
     return 2;
-  fclose(in);
 
-  const int64_t plan_bytes = lml_plan_total_bytes(3, N, se, 8);
-  const LmlAdjLayout L(3, 2, N, se, C);
+  const int64_t plan_bytes = lml_plan_total_bytes(NU, N, se, 8);
+  const LmlAdjLayout L(NU, 2, N, se, C);
   const int64_t res_elems = int64_t(B) * L.total;
   unsigned char* plan = static_cast<unsigned char*>(calloc(plan_bytes, 1));
   double* res = static_cast<double*>(malloc(res_elems * 8));
   // NaN everywhere: a residual read before it is written poisons the result
   for (int64_t i = 0; i < res_elems; ++i) res[i] = __longlong_as_double(0x7ff8000000000001LL);
-  std::vector<double> lml(B), grad(B * 3), gy0(B * 2);
+  std::vector<double> lml(B), grad(B * P), gy0(B * 2);
   std::vector<int32_t> status(B);
 
   LmlAdjArgs aa;
@@ -58,8 +54,8 @@ int main(int argc, char** argv) {
   a.average_pdfs = avg;
   a.lanes_per_sample = 1;
   a.dt = dt[0];
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) a.q1[i][j] = q1[i * 4 + j];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) a.q1[i][j] = q1[i * n + j];
   a.params = params.data();
   a.y0 = y0.data();
   a.data = data.data();
@@ -77,21 +73,39 @@ int main(int argc, char** argv) {
   blockDim = {uint32_t(kLmlThreads), 1, 1};
   blockIdx = {0, 0, 0};
   threadIdx = {0, 0, 0};
-  lml_plan_kernel<double, 3>(a);
+  lml_plan_kernel<double, NU>(a);
   const long long padded = (B + kLmlThreads - 1) / kLmlThreads * kLmlThreads;  // the launch's grid
   for (int pass = 0; pass < 2; ++pass)
     for (long long t = 0; t < padded; ++t) {
       blockIdx = {uint32_t(t / kLmlThreads), 0, 0};
       threadIdx = {uint32_t(t % kLmlThreads), 0, 0};
       if (pass == 0)
-        lml_adj_fwd_kernel<double, 3, FitzHughNagumo>(aa);
+        lml_adj_fwd_kernel<double, NU, F>(aa);
       else
-        lml_adj_bwd_kernel<double, 3, FitzHughNagumo>(aa);
+        lml_adj_bwd_kernel<double, NU, F>(aa);
     }
-  for (long long b = 0; b < B; ++b)
-    printf("%d %.17g %.17g %.17g %.17g %.17g %.17g\n", status[b], lml[b], grad[b * 3], grad[b * 3 + 1],
-           grad[b * 3 + 2], gy0[b * 2], gy0[b * 2 + 1]);
+  for (long long b = 0; b < B; ++b) {
+    printf("%d %.17g", status[b], lml[b]);
+    for (int q = 0; q < P; ++q) printf(" %.17g", grad[b * P + q]);
+    printf(" %.17g %.17g\n", gy0[b * 2], gy0[b * 2 + 1]);
+  }
   free(plan);
   free(res);
   return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc != 2) return 2;
+  FILE* in = fopen(argv[1], "r");
+  if (!in) return 2;
+  long long B;
+  int field, nu, N, se, C, avg;
+  if (fscanf(in, "%d %d %lld %d %d %d %d", &field, &nu, &B, &N, &se, &C, &avg) != 7) return 2;
+  if (B < 1 || N < 1 || se < 1 || N % se != 0 || C < 1 || C > N) return 2;
+  int rc = 2;
+  if (field == 0 && nu == 3) rc = run<3, FitzHughNagumo>(in, B, N, se, C, avg);
+  if (field == 0 && nu == 2) rc = run<2, FitzHughNagumo>(in, B, N, se, C, avg);
+  if (field == 1 && nu == 3) rc = run<3, LotkaVolterra>(in, B, N, se, C, avg);
+  fclose(in);
+  return rc;
 }

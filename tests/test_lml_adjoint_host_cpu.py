@@ -8,8 +8,9 @@ on buffers of exactly the size the library computes.  This pins the adjoint
 algebra and the residual layout without a GPU: value, d/d params and d/d y0
 against the oracle's PyTorch reverse mode to 1e-10 relative, for sqrt(N),
 single-step, ragged and whole-grid checkpoint spacings, averaged pdfs and
-non-unit cotangents.  The GPU tests check the same kernels compiled for
-sm_103a.
+non-unit cotangents, for FitzHugh--Nagumo with nu = 3 and nu = 2 and for
+Lotka--Volterra (four parameters).  The GPU tests check the same kernels
+compiled for sm_103a.
 """
 
 import os
@@ -51,11 +52,12 @@ def q1_iwp(nu):
     return np.linalg.cholesky(H)
 
 
-def run(harness, tmp_path, thetas, y0s, data, dt, num_steps, save_every, ckpt, average, cot):
+def run(harness, tmp_path, thetas, y0s, data, dt, num_steps, save_every, ckpt, average, cot, field=0, nu=3,
+        std=lml_problem.STD):
     B = len(thetas)
-    head = [B, num_steps, save_every, ckpt, int(average)]
-    body = np.concatenate([np.ravel(thetas), np.ravel(y0s), np.ravel(data), np.full(data.shape[0], lml_problem.STD),
-                           np.asarray(cot, dtype=float), [dt], np.ravel(q1_iwp(3))])
+    head = [field, nu, B, num_steps, save_every, ckpt, int(average)]
+    body = np.concatenate([np.ravel(thetas), np.ravel(y0s), np.ravel(data), np.full(data.shape[0], std),
+                           np.asarray(cot, dtype=float), [dt], np.ravel(q1_iwp(nu))])
     path = tmp_path / "input.txt"
     path.write_text(" ".join(str(int(v)) for v in head) + " " + " ".join(repr(float(v)) for v in body))
     res = subprocess.run([harness, str(path)], capture_output=True, text=True, timeout=600)
@@ -79,3 +81,34 @@ def test_host_adjoint_matches_oracle_reverse_mode(harness, tmp_path, t1, ckpt, a
         assert abs(out[b, 1] - v) <= 1e-10 * abs(v), (out[b, 1], v)
         assert np.abs(out[b, 2:5] - cot[b] * g).max() <= 1e-10 * np.linalg.norm(cot[b] * g), (out[b, 2:5], g)
         assert np.abs(out[b, 5:7] - cot[b] * gy).max() <= 1e-10 * np.linalg.norm(cot[b] * gy), (out[b, 5:7], gy)
+
+
+@pytest.mark.parametrize("field,nu", [("fitzhugh_nagumo", 2), ("lotka_volterra", 3)])
+def test_host_adjoint_other_instantiations(harness, tmp_path, field, nu):
+    """The library's other adjoint instantiations: FitzHugh--Nagumo with
+    nu = 2, and Lotka--Volterra (four parameters) on seeded synthetic data."""
+    rng = np.random.default_rng(3)
+    if field == "fitzhugh_nagumo":
+        dt, num_steps, save_every, std = 0.01, 200, 10, lml_problem.STD
+        _, data = lml_problem.observations(t1=2.0, dt=dt, save_every=save_every)
+        thetas = lml_problem.theta_samples(2, seed=4)
+        y0s = np.tile(lml_problem.U0, (2, 1))
+        code = 0
+    else:
+        dt, num_steps, save_every, std = 0.05, 200, 20, 0.5
+        data = 20.0 + 5.0 * rng.standard_normal((num_steps // save_every + 1, 2))
+        thetas = np.array([0.5, 0.05, 0.5, 0.05]) * np.exp(0.1 * rng.standard_normal((2, 4)))
+        y0s = 20.0 + rng.uniform(-2, 2, (2, 2))
+        code = 1
+    cot = [1.0, -2.0]
+    out = run(harness, tmp_path, thetas, y0s, data, dt, num_steps, save_every, 11, False, cot, field=code, nu=nu,
+              std=std)
+    P = thetas.shape[1]
+    assert out.shape == (2, 2 + P + 2)
+    for b in range(2):
+        v, g, gy = lml_value_and_grads(thetas[b], y0s[b], data, dt, num_steps, save_every, field=field,
+                                       num_derivatives=nu, std=std)
+        assert out[b, 0] == 0
+        assert abs(out[b, 1] - v) <= 1e-10 * abs(v), (out[b, 1], v)
+        assert np.abs(out[b, 2:2 + P] - cot[b] * g).max() <= 1e-10 * np.linalg.norm(cot[b] * g), (out[b, 2:2 + P], g)
+        assert np.abs(out[b, 2 + P:] - cot[b] * gy).max() <= 1e-10 * np.linalg.norm(cot[b] * gy), (out[b, 2 + P:], gy)
