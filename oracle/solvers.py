@@ -634,7 +634,12 @@ def loss_lml_terminal_values(u, marginal, std, tcoeff_index=0):
     """loss_lml_terminal_values (estimators_and_losses.py:20-50)."""
     model = marginal.to_derivative(tcoeff_index, std)
     marg = model.marginalise(marginal)
-    data = u.reshape(1, -1) if marginal.kind == "isotropic" else u
+    if marginal.kind == "isotropic":
+        data = u.reshape(1, -1)
+    elif marginal.kind == "blockdiag":
+        data = u.reshape(-1, 1)
+    else:
+        data = u
     return marg.logpdf(data)
 
 

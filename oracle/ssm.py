@@ -377,6 +377,16 @@ class BdNormal:
     def prototype_output_scale(self):
         return torch.ones(self.mean.shape[0], dtype=self.mean.dtype)
 
+    def to_derivative(self, i, std):
+        """ssm_impl_blockdiag.py:367-377: observe coefficient i of every
+        dimension with noise std (d,); linop (d, 1, n) selects it."""
+        d, n = self.mean.shape
+        linop = torch.zeros((d, 1, n), dtype=self.mean.dtype)
+        linop[:, 0, i] = 1.0
+        std = torch.as_tensor(std, dtype=self.mean.dtype).reshape(d)
+        noise = BdNormal(torch.zeros((d, 1), dtype=self.mean.dtype), std.reshape(d, 1, 1).clone())
+        return BdCond.from_linop_and_noise(linop, noise)
+
     def select(self, i):
         return BdNormal(self.mean[i], self.cholesky[i])
 

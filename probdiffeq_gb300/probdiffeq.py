@@ -38,6 +38,7 @@ __all__ = [
     "error_state_std",
     "jacobian_materialize",
     "loss_lml_timeseries",
+    "loss_lml_terminal_values",
 ]
 
 _FIELD_DIMS = {"lotka_volterra": 2, "van_der_pol": 2, "fitzhugh_nagumo": 2, "burgers": None}
@@ -343,6 +344,75 @@ class loss_lml_timeseries:
     def __post_init__(self):
         if self.tcoeff_index != 0:
             raise NotImplementedError("observations of the solution (tcoeff_index=0) only")
+
+
+class loss_lml_terminal_values:
+    """Log-marginal likelihood of terminal-value data
+    (estimators_and_losses.py:20-50): the log-pdf of ``u`` under the
+    marginal's coefficient ``tcoeff_index`` observed with noise ``std``
+    (``marginals.to_derivative(tcoeff_index, std).marginalise(marginals)``).
+
+    ``loss = loss_lml_terminal_values(); loss(u, marginals=sol.u, std=std)``
+    evaluates it for a batch of solutions at once (the reference's
+    ``jax.vmap`` axis): ``marginals`` an ``ivpsolve.Normal`` whose leading
+    axes are batch axes (e.g. ``(B, 1)`` from ``solve_adaptive_terminal_values``),
+    ``u`` the data broadcastable to the observed coefficient's shape (d per
+    instance), ``std`` one scalar per instance for the isotropic
+    factorisation and one value per dimension for the dense and
+    block-diagonal ones (or a single such container for all instances).
+    Returns one log-pdf per instance.  The arithmetic is torch on the
+    marginals' device, so it is differentiable through their means (the
+    ``autograd.terminal_values`` sensitivities).
+    """
+
+    def __init__(self, *, tcoeff_index=0):
+        self.tcoeff_index = int(tcoeff_index)
+
+    @staticmethod
+    def _raise(std, expected, u):
+        msg = "The standard deviation container differs from what was expected."
+        msg += f" Expected: shape={tuple(expected)}."
+        msg += f" Received: shape={tuple(std.shape)}."
+        msg += f" For reference: data-shape={tuple(u.shape)}."
+        raise ValueError(msg)
+
+    def __call__(self, u, /, *, marginals, std):
+        import math
+
+        k = self.tcoeff_index
+        mean, chol = marginals.mean_flat, marginals.cholesky_flat
+        u = torch.as_tensor(u, dtype=mean.dtype, device=mean.device)
+        std = torch.as_tensor(std, dtype=mean.dtype, device=mean.device)
+        log2pi = math.log(2.0 * math.pi)
+        if marginals.ssm == "isotropic":
+            batch = mean.shape[:-2]
+            if std.shape not in ((), batch):
+                self._raise(std, batch, u)
+            mu = mean[..., k, :]  # (..., d)
+            var = (chol[..., k, :] ** 2).sum(-1) + std**2  # one variance shared by the d dimensions
+            d = mu.shape[-1]
+            maha = ((u - mu) ** 2).sum(-1) / var
+            return -0.5 * (maha + d * torch.log(var) + d * log2pi)
+        if marginals.ssm == "blockdiag":
+            batch, d = mean.shape[:-2], mean.shape[-2]
+            if std.shape not in ((d,), batch + (d,)):
+                self._raise(std, batch + (d,), u)
+            mu = mean[..., k]  # (..., d)
+            var = (chol[..., k, :] ** 2).sum(-1) + std**2  # (..., d)
+            return -0.5 * (((u - mu) ** 2 / var) + torch.log(var) + log2pi).sum(-1)
+        if marginals.ssm == "dense":
+            d = u.shape[-1]
+            batch = mean.shape[:-1]
+            if std.shape not in ((d,), batch + (d,)):
+                self._raise(std, batch + (d,), u)
+            mu = mean[..., k * d:(k + 1) * d]
+            rows = chol[..., k * d:(k + 1) * d, :]
+            cov = rows @ rows.transpose(-1, -2) + torch.diag_embed(std.expand(batch + (d,)) ** 2)
+            L = torch.linalg.cholesky(cov)
+            w = torch.linalg.solve_triangular(L, (u - mu).unsqueeze(-1), upper=False).squeeze(-1)
+            logdet = 2.0 * torch.log(torch.diagonal(L, dim1=-2, dim2=-1)).sum(-1)
+            return -0.5 * ((w**2).sum(-1) + logdet + d * log2pi)
+        raise ValueError(f"unknown factorisation {marginals.ssm!r}")
 
 
 @dataclasses.dataclass(frozen=True)
