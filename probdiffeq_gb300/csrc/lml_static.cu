@@ -23,6 +23,7 @@
 
 #include <mutex>
 
+#include "pdq_nvtx.h"
 #include "pdq.h"
 
 namespace {
@@ -55,6 +56,7 @@ cudaError_t static_scratch(void** out) {
 }  // namespace
 
 extern "C" pdq_status pdq_lml_fixed_grid_static(const pdq_config* config, const pdq_lml_args* args, void* stream) {
+  pdq::NvtxRange nvtx_range("pdq_lml_fixed_grid_static");
   if (args == nullptr) return PDQ_ERROR_INVALID_VALUE;
   size_t need = 0;
   const pdq_status st =

@@ -31,6 +31,7 @@
 #include <tuple>
 #include <vector>
 
+#include "pdq_nvtx.h"
 #include "dense_solver.cuh"
 #include "iso_solver.cuh"
 #include "nvrtc_fields.h"
@@ -126,6 +127,7 @@ bool nonempty(const char* s) { return s != nullptr && s[0] != '\0'; }
 
 extern "C" pdq_status pdq_register_field(const char* name, const char* source, int32_t dim, int32_t num_params,
                                          int32_t* field_id, char* log, size_t log_bytes) {
+  pdq::NvtxRange nvtx_range("pdq_register_field");
   if (field_id == nullptr || !nonempty(name) || !nonempty(source) ||
       dim < 1 || dim > 64 || num_params < 0 || num_params > 64)
     return PDQ_ERROR_INVALID_VALUE;

@@ -3,6 +3,7 @@
 #include <math.h>
 #include <string.h>
 
+#include "pdq_nvtx.h"
 #include "bd_launch.cuh"
 #include "dense_launch.cuh"
 #include "offgrid.h"
@@ -157,6 +158,7 @@ pdq_status pdq_workspace_size(const pdq_config* c, int64_t num_instances, int32_
 
 pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args, void* workspace,
                               size_t workspace_bytes, void* stream_ptr) {
+  pdq::NvtxRange nvtx_range("pdq_solve_adaptive");
   (void)workspace;
   (void)workspace_bytes;
   pdq_status st = validate_common(c);
@@ -486,6 +488,7 @@ pdq_status pdq_lml_workspace_size(const pdq_config* c, int64_t B, int32_t num_st
 
 pdq_status pdq_lml_fixed_grid(const pdq_config* c, const pdq_lml_args* args, void* workspace, size_t workspace_bytes,
                               void* stream_ptr) {
+  pdq::NvtxRange nvtx_range("pdq_lml_fixed_grid");
   if (args == nullptr) return PDQ_ERROR_INVALID_VALUE;
   pdq_status st = lml_check(c, args->num_instances, args->num_steps, args->save_every);
   if (st != PDQ_SUCCESS) return st;
@@ -615,17 +618,20 @@ static pdq_status lml_adj_launch(const pdq_config* c, const pdq_lml_adjoint_args
 
 pdq_status pdq_lml_fwd(const pdq_config* c, const pdq_lml_adjoint_args* args, void* workspace, size_t workspace_bytes,
                        void* stream) {
+  pdq::NvtxRange nvtx_range("pdq_lml_fwd");
   return lml_adj_launch(c, args, workspace, workspace_bytes, stream, false);
 }
 
 pdq_status pdq_lml_bwd(const pdq_config* c, const pdq_lml_adjoint_args* args, void* workspace, size_t workspace_bytes,
                        void* stream) {
+  pdq::NvtxRange nvtx_range("pdq_lml_bwd");
   return lml_adj_launch(c, args, workspace, workspace_bytes, stream, true);
 }
 
 }  // extern "C"
 
 extern "C" pdq_status pdq_offgrid_marginals(const pdq_offgrid_args* args, void* stream) {
+  pdq::NvtxRange nvtx_range("pdq_offgrid_marginals");
   if (args == nullptr) return PDQ_ERROR_INVALID_VALUE;
   const pdq_offgrid_args& a = *args;
   if (a.num_instances < 0 || a.num_points < 1 || a.num_queries < 0 || a.ode_dim < 1) return PDQ_ERROR_INVALID_VALUE;

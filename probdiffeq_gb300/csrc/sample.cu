@@ -4,6 +4,7 @@
 // conditionals of an instance are read by all its samples (L1/L2 hits).
 #include <cuda_runtime.h>
 
+#include "pdq_nvtx.h"
 #include "pdq.h"
 
 namespace {
@@ -99,6 +100,7 @@ __global__ void sample_dense_kernel(pdq_sample_args a) {
 }  // namespace
 
 extern "C" pdq_status pdq_sample_markov(const pdq_sample_args* args, void* stream_ptr) {
+  pdq::NvtxRange nvtx_range("pdq_sample_markov");
   if (args == nullptr) return PDQ_ERROR_INVALID_VALUE;
   const pdq_sample_args& a = *args;
   if (a.num_instances < 0 || a.num_samples < 0 || a.num_points < 1 || a.num_derivatives < 1 || a.ode_dim < 1)
