@@ -6,7 +6,7 @@ reference's qr_r rule, backend/linalg.py:13-37) and central finite
 differences, over sqrt(N), ragged, single-step and single-segment checkpoint
 spacings.  Tolerances: float64 -- adjoint vs forward mode 1e-9 relative to
 the gradient's norm, vs the oracle 1e-6 (short horizon) / 1e-5 (2000 steps),
-vs central differences 1e-4 (the spec bar); float32 -- 5e-2 vs the
+vs central differences 1e-4 (the accuracy target for gradients); float32 -- 5e-2 vs the
 float64 oracle, as for the forward-mode kernel.
 """
 
@@ -98,7 +98,7 @@ def test_adjoint_full_horizon_matches_oracle():
 
 
 def test_adjoint_matches_central_finite_differences():
-    """Spec bar: the adjoint gradient within 1e-4 relative of central
+    """Accuracy target: the adjoint gradient within 1e-4 relative of central
     differences of the LML, for the parameters and the initial values."""
     dt, save_every = 0.01, 10
     num_steps, data = lml_problem.observations(t1=2.0, dt=dt, save_every=save_every)

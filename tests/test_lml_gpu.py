@@ -6,7 +6,7 @@ average_pdfs=False) and differentiates it with PyTorch autograd using the
 reference's qr_r rule (Q held constant, backend/linalg.py:13-37); central
 finite differences pin both.  Tolerances: float64 -- LML 1e-9 relative,
 gradient 1e-6 relative to its norm (and vs finite differences 1e-4, the
-spec bar); float32 -- LML 1e-3, gradient 5e-2 relative.
+accuracy target for gradients); float32 -- LML 1e-3, gradient 5e-2 relative.
 """
 
 import numpy as np
@@ -71,7 +71,7 @@ def test_lml_and_gradient_short_horizon(precision):
 
 
 def test_gradient_matches_central_finite_differences():
-    """Spec bar: adjoint-free gradients within 1e-4 relative of central FD (float64)."""
+    """Accuracy target: forward-mode gradients within 1e-4 relative of central FD (float64)."""
     dt, save_every = 0.01, 10
     num_steps, data = lml_problem.observations(t1=2.0, dt=dt, save_every=save_every)
     th = lml_problem.theta_samples(1, seed=2)[0]

@@ -8,7 +8,7 @@ reference stops gradients through them), and against central finite
 differences on a fixed grid (where the step sequence cannot change).
 Float64; tolerances relative to the largest entry: 1e-9 vs the oracle on a
 grid, 1e-8 (Lotka-Volterra) or 1e-5 (rounding-sensitive step sequences) with
-adaptive steps, 1e-4 vs finite differences (the spec bar).
+adaptive steps, 1e-4 vs finite differences (the accuracy target for gradients).
 """
 
 import pytest
