@@ -185,14 +185,21 @@ def solve_fixed_grid(*, solver, precision="float32", device="cuda"):
 
 
 def lml_fixed_grid(prior, data, std, *, dt, num_steps, save_every, loss=None, gradient=True, precision="float64",
-                   t0=0.0, device="cuda", stream=None):
+                   t0=0.0, device="cuda", stream=None, checkpoint_every=0):
     """LML of observations under the fixed-point-smoother posterior, and d LML / d params.
 
     The fixed grid t0 + k dt, k = 0..num_steps, observed at every save_every-th
     point (t0 included); loss_lml_timeseries semantics
     (estimators_and_losses.py:53-105) with the uncalibrated solver and TS0.
-    Returns (lml (B,), grad (B, P) or None, status (B,)).
+    ``gradient``: True (or "forward") for forward-mode tangents in the same
+    launch, "adjoint" for the reverse-mode pair pdq_lml_fwd / pdq_lml_bwd
+    (sqrt(N) step checkpointing, ``checkpoint_every`` steps between stored
+    states, 0 for round(sqrt(num_steps))), False for the value only.
+    Returns (lml (B,), grad (B, P) or None, status (B,)); with "adjoint" a
+    fourth item, d LML / d y0 (B, d).
     """
+    if gradient not in (True, False, "forward", "adjoint"):
+        raise ValueError(f"gradient must be True, False, 'forward' or 'adjoint', not {gradient!r}")
     from .probdiffeq import loss_lml_timeseries
 
     loss = loss_lml_timeseries() if loss is None else loss
@@ -206,9 +213,15 @@ def lml_fixed_grid(prior, data, std, *, dt, num_steps, save_every, loss=None, gr
     if num_steps % save_every != 0 or data.shape[0] != num_steps // save_every + 1:
         raise ValueError("The standard deviation container differs from what was expected.")
     dev = torch.device(device)
+    params, y0 = params.to(dev).contiguous(), y0.to(dev).contiguous()
+    data, std = data.to(dev).contiguous(), std.to(dev).contiguous()
+    if gradient == "adjoint":
+        fwd = _native.lml_fwd(cfg, params, y0, data, std, t0=t0, dt=dt, num_steps=num_steps, save_every=save_every,
+                              average_pdfs=loss.average_pdfs, checkpoint_every=checkpoint_every, stream=stream)
+        bwd = _native.lml_bwd(fwd, None, params_grad=True, y0_grad=True, release=True)
+        return fwd["lml"], bwd["grad"], fwd["status"], bwd["grad_y0"]
     out = _native.lml_fixed_grid(
-        cfg, params.to(dev).contiguous(), y0.to(dev).contiguous(), data.to(dev).contiguous(), std.to(dev).contiguous(),
-        t0=t0, dt=dt, num_steps=num_steps, save_every=save_every, average_pdfs=loss.average_pdfs, gradient=gradient,
-        stream=stream,
+        cfg, params, y0, data, std, t0=t0, dt=dt, num_steps=num_steps, save_every=save_every,
+        average_pdfs=loss.average_pdfs, gradient=bool(gradient), stream=stream,
     )
     return out["lml"], out.get("grad"), out["status"]

@@ -108,3 +108,30 @@ def test_no_gradient_releases_at_once_and_double_backward_is_refused(fake):
     _native.lml_bwd(fwd, None, release=True)
     with pytest.raises(RuntimeError, match="released"):
         _native.lml_bwd(fwd, None)
+
+
+def test_ivpsolve_lml_fixed_grid_adjoint_mode_plumbing(fake):
+    """ivpsolve.lml_fixed_grid(gradient="adjoint") runs the forward and the
+    backward call on one workspace, returns (lml, d/d params, status,
+    d/d y0) and pools the workspace; an unknown mode is refused."""
+    import numpy as np
+
+    from probdiffeq_gb300 import _native, ivpsolve, probdiffeq
+
+    thetas = torch.tensor([[0.2, 0.2, 3.0], [0.21, 0.19, 3.1]], dtype=torch.float64)
+    y0 = torch.tensor(np.tile([-1.0, 1.0], (2, 1)), dtype=torch.float64)
+    vf = probdiffeq.ode("fitzhugh_nagumo", thetas)
+    tcoeffs, _ = probdiffeq.jetexpand_ode_padded_scan(num=3)(vf, (y0,))
+    prior = probdiffeq.state_space_model_isotropic().prior_wiener_integrated(tcoeffs)
+    data = np.zeros((21, 2))
+    out = ivpsolve.lml_fixed_grid(prior, data, 0.01, dt=0.01, num_steps=200, save_every=10, gradient="adjoint",
+                                  device="cpu", stream=STREAM)
+    assert len(out) == 4
+    lml, grad, status, grad_y0 = out
+    assert lml.shape == (2,) and grad.shape == (2, 3) and status.shape == (2,) and grad_y0.shape == (2, 2)
+    assert [k for k, _ in fake.calls] == ["fwd", "bwd"]
+    assert fake.calls[0][1] == fake.calls[1][1]
+    assert sum(len(v) for v in _native._LML_ADJ_POOL.values()) == 1
+    with pytest.raises(ValueError, match="gradient must be"):
+        ivpsolve.lml_fixed_grid(prior, data, 0.01, dt=0.01, num_steps=200, save_every=10, gradient="reverse",
+                                device="cpu", stream=STREAM)
