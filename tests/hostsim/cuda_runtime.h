@@ -59,6 +59,9 @@ inline float rsqrtf(float a) { return 1.0f / std::sqrt(a); }
 inline double rsqrt(double a) { return 1.0 / std::sqrt(a); }
 using std::fabs;
 using std::fmax;
+using std::isfinite;
+using std::isinf;
+using std::isnan;
 using std::max;
 using std::min;
 using std::pow;

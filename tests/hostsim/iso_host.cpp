@@ -1,0 +1,116 @@
+// Runs the float64 isotropic adaptive kernel (iso_adaptive_kernel, one thread
+// per instance, Lotka-Volterra) on the CPU, every instance as its own
+// "thread", on buffers of exactly the sizes the library uses, so
+// AddressSanitizer flags any access outside them.  Filter strategy; the
+// instantiation the library launches for the configuration: the lean one
+// (TS0, error_residual_std) with exact checkpoint landings (clip_dt) or with
+// interpolation.
+//
+// Input file (whitespace-separated): nu B S solver control clip_dt
+// terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
+// dt0 (B), Q1 ((nu + 1) x (nu + 1), row-major).  solver / control take the
+// PDQ_SOLVER_* / PDQ_CONTROL_* codes.
+// Output: per instance a line "status attempts", then per output record a
+// line "t num_steps output_scale u_mean[n d] u_chol[n n]".
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "iso_solver.cuh"
+
+thread_local pdq_host_uint3 threadIdx, blockIdx, blockDim;
+
+using namespace pdq;
+
+static bool read_all(FILE* in, std::vector<double>& v) {
+  for (double& x : v)
+    if (fscanf(in, "%lf", &x) != 1) return false;
+  return true;
+}
+
+template <int NU, bool INTERP>
+static int run(FILE* in, long long B, int S, int solver, int control, int clip_dt, int terminal_only) {
+  using F = LotkaVolterra;
+  constexpr int n = NU + 1;
+  constexpr int D = F::D;
+  constexpr int P = F::P;
+  std::vector<double> tol(2), save_at(B * S), params(B * P), y0(B * D), dt0(B), q1(n * n);
+  if (!read_all(in, tol) || !read_all(in, save_at) || !read_all(in, params) || !read_all(in, y0) ||
+      !read_all(in, dt0) || !read_all(in, q1))
+    return 2;
+  const int S_out = terminal_only ? 1 : S;
+  std::vector<double> u_mean(B * S_out * n * D), u_chol(B * S_out * n * n), scale(B * S_out), t(B * S_out);
+  std::vector<int32_t> steps(B * S_out), attempts(B), status(B);
+
+  IsoArgs a;
+  memset(&a, 0, sizeof(a));
+  a.B = B;
+  a.S = S;
+  a.terminal_only = terminal_only;
+  a.solver = solver;
+  a.control = control;
+  a.clip_dt = clip_dt;
+  a.correct = 1;  // solver_mle(correct_asymptotic_underconfidence=True), the default
+  // control_integral / control_proportional_integral defaults (controllers.py:24-84)
+  a.safety = 0.95;
+  a.factor_min = 0.2;
+  a.factor_max = 10.0;
+  a.exp_i = 0.3;
+  a.exp_p = 0.4;
+  a.atol = tol[0];
+  a.rtol = tol[1];
+  a.eps = 1e-8;
+  a.damp = 0.0;
+  a.max_attempts = int64_t(1) << 20;  // pdq_config_default
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) a.q1[i][j] = q1[i * n + j];
+  a.save_at = save_at.data();
+  a.params = params.data();
+  a.y0 = y0.data();
+  a.dt0 = dt0.data();
+  a.u_mean = u_mean.data();
+  a.u_chol = u_chol.data();
+  a.output_scale = scale.data();
+  a.t_out = t.data();
+  a.num_steps = steps.data();
+  a.num_attempts = attempts.data();
+  a.status = status.data();
+
+  const int block = 64;
+  blockDim = {uint32_t(block), 1, 1};
+  const long long padded = (B + block - 1) / block * block;  // the launch's grid
+  for (long long g = 0; g < padded; ++g) {
+    blockIdx = {uint32_t(g / block), 0, 0};
+    threadIdx = {uint32_t(g % block), 0, 0};
+    iso_adaptive_kernel<double, NU, F, INTERP, false, false>(a);
+  }
+  for (long long b = 0; b < B; ++b) {
+    printf("%d %d\n", status[b], attempts[b]);
+    for (int k = 0; k < S_out; ++k) {
+      const long long r = b * S_out + k;
+      printf("%.17g %d %.17g", t[r], steps[r], scale[r]);
+      for (int e = 0; e < n * D; ++e) printf(" %.17g", u_mean[r * n * D + e]);
+      for (int e = 0; e < n * n; ++e) printf(" %.17g", u_chol[r * n * n + e]);
+      printf("\n");
+    }
+  }
+  return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc != 2) return 2;
+  FILE* in = fopen(argv[1], "r");
+  if (!in) return 2;
+  long long B;
+  int nu, S, solver, control, clip_dt, terminal_only;
+  if (fscanf(in, "%d %lld %d %d %d %d %d", &nu, &B, &S, &solver, &control, &clip_dt, &terminal_only) != 7) return 2;
+  if (B < 1 || S < 2) return 2;
+  int rc = 2;
+  const bool interp = !clip_dt;
+  if (nu == 4) rc = interp ? run<4, true>(in, B, S, solver, control, clip_dt, terminal_only)
+                           : run<4, false>(in, B, S, solver, control, clip_dt, terminal_only);
+  if (nu == 2) rc = interp ? run<2, true>(in, B, S, solver, control, clip_dt, terminal_only)
+                           : run<2, false>(in, B, S, solver, control, clip_dt, terminal_only);
+  fclose(in);
+  return rc;
+}
