@@ -20,6 +20,9 @@ Fixtures:
                    solver_dynamic at save_at (0, 0.7, 2, 3.3, 5) by
                    interpolation; means, Cholesky factors, output scales and
                    accepted steps
+  vdp_dense.json   van der Pol (mu = 1, 3), dense TS1, fixed-point smoother,
+                   solver_dynamic, rtol = atol = 1e-5, 8 save points by
+                   interpolation: smoothed means, Cholesky factors, steps
   fhn_lml.json     FitzHugh--Nagumo LML on 200 steps of 0.01 with 21
                    observations (data included), 2 parameter samples with
                    perturbed initial values: lml, d lml / d params,
@@ -95,6 +98,36 @@ def lv_filter_fixture(params=None, y0=None):
     return out
 
 
+def vdp_dense_fixture(mus=None):
+    """Dense TS1 van der Pol (first order), fixed-point smoother, dynamic
+    calibration, error_residual_std, integral control, nu = 3,
+    rtol = atol = 1e-5, save_at = linspace(0, 2 mu, 8) reached by
+    interpolation: smoothed means, Cholesky factors and accepted steps at the
+    save points."""
+    from oracle import problems, solvers, ssm
+
+    mus = [1.0, 3.0] if mus is None else mus
+    out = {"mu": list(mus), "y0": [2.0, 0.0], "num_derivatives": 3, "rtol": 1e-5, "atol": 1e-5, "dt0": 0.1,
+           "save_at": [], "records": []}
+    for mu in mus:
+        save_at = np.linspace(0.0, 2.0 * mu, 8)
+        p = torch.tensor([mu], dtype=torch.float64)
+        tc = problems.taylor_derivatives(problems.van_der_pol, torch.tensor([2.0, 0.0], dtype=torch.float64), p, 3)
+        D = ssm.DenseSSM()
+        c = D.constraint_ode_ts1(lambda u, t: problems.van_der_pol(u[0], p),
+                                 lambda u, t: problems.jacobian(problems.van_der_pol, u, p), 2)
+        res = solvers.solve_adaptive_save_at(solvers.SolverDynamic(solvers.StrategyFixedPoint(), c),
+                                             solvers.ErrorResidualStd(c), D.prior_wiener_integrated(tc),
+                                             save_at, 1e-5, 1e-5)
+        out["save_at"].append(save_at.tolist())
+        out["records"].append({
+            "u_mean": [u.mean.tolist() for u in res.u],
+            "u_chol": [u.cholesky.tolist() for u in res.u],
+            "num_steps": [int(s) for s in res.num_steps],
+        })
+    return out
+
+
 def fhn_lml_fixture(inputs=None):
     from tests import lml_problem
     from tests.lml_oracle import lml_value_and_grads
@@ -126,7 +159,7 @@ def load(name):
 def main():
     torch.set_default_dtype(torch.float64)
     for name, fn in (("iwp.json", iwp_fixture), ("lv_filter.json", lv_filter_fixture),
-                     ("fhn_lml.json", fhn_lml_fixture)):
+                     ("vdp_dense.json", vdp_dense_fixture), ("fhn_lml.json", fhn_lml_fixture)):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(fn(), f, indent=1)
         print("wrote", name)

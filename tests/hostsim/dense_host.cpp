@@ -1,0 +1,105 @@
+// Runs the float64 dense adaptive kernel (dense_adaptive_kernel, one thread
+// per instance) on the CPU for van der Pol with TS1 and the fixed-point
+// smoother, every instance as its own "thread", on buffers of exactly the
+// sizes the library uses (the per-instance backward conditionals in the
+// scratch included), so AddressSanitizer flags any access outside them.
+//
+// Input file (whitespace-separated): B S solver control clip_dt, then
+// atol rtol, save_at (B x S), params (B x 1), y0 (B x 2), dt0 (B),
+// Q1 (4 x 4, row-major); nu = 3.
+// Output: per instance a line "status attempts", then per save point a line
+// "t num_steps u_mean[N] u_chol[N N]", N = 8.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "dense_solver.cuh"
+
+thread_local pdq_host_uint3 threadIdx, blockIdx, blockDim;
+
+using namespace pdq;
+
+static bool read_all(FILE* in, std::vector<double>& v) {
+  for (double& x : v)
+    if (fscanf(in, "%lf", &x) != 1) return false;
+  return true;
+}
+
+int main(int argc, char** argv) {
+  using F = VanDerPol;
+  constexpr int NU = 3;
+  constexpr int n = NU + 1;
+  constexpr int D = F::D;
+  constexpr int N = n * D;
+  if (argc != 2) return 2;
+  FILE* in = fopen(argv[1], "r");
+  if (!in) return 2;
+  long long B;
+  int S, solver, control, clip_dt;
+  if (fscanf(in, "%lld %d %d %d %d", &B, &S, &solver, &control, &clip_dt) != 5) return 2;
+  if (B < 1 || S < 2) return 2;
+  std::vector<double> tol(2), save_at(B * S), params(B * F::P), y0(B * D), dt0(B), q1(n * n);
+  if (!read_all(in, tol) || !read_all(in, save_at) || !read_all(in, params) || !read_all(in, y0) ||
+      !read_all(in, dt0) || !read_all(in, q1))
+    return 2;
+  fclose(in);
+  std::vector<double> u_mean(B * S * N), u_chol(B * S * N * N), scale(B * S), t(B * S);
+  std::vector<int32_t> steps(B * S), attempts(B), status(B);
+  double* ws = static_cast<double*>(malloc(size_t(B) * (S - 1) * cond_floats<N>() * sizeof(double)));
+
+  DenseArgs a;
+  memset(&a, 0, sizeof(a));
+  a.B = B;
+  a.S = S;
+  a.terminal_only = 0;
+  a.solver = solver;
+  a.control = control;
+  a.clip_dt = clip_dt;
+  a.correct = 1;
+  a.fixedpoint = 1;
+  a.safety = 0.95;
+  a.factor_min = 0.2;
+  a.factor_max = 10.0;
+  a.exp_i = 0.3;
+  a.exp_p = 0.4;
+  a.atol = tol[0];
+  a.rtol = tol[1];
+  a.eps = 1e-8;
+  a.damp = 0.0;
+  a.max_attempts = int64_t(1) << 20;  // pdq_config_default
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) a.q1[i][j] = q1[i * n + j];
+  a.save_at = save_at.data();
+  a.params = params.data();
+  a.y0 = y0.data();
+  a.dt0 = dt0.data();
+  a.u_mean = u_mean.data();
+  a.u_chol = u_chol.data();
+  a.output_scale = scale.data();
+  a.t_out = t.data();
+  a.num_steps = steps.data();
+  a.num_attempts = attempts.data();
+  a.status = status.data();
+  a.workspace = ws;
+
+  const int block = 32;
+  blockDim = {uint32_t(block), 1, 1};
+  const long long padded = (B + block - 1) / block * block;  // the launch's grid
+  for (long long g = 0; g < padded; ++g) {
+    blockIdx = {uint32_t(g / block), 0, 0};
+    threadIdx = {uint32_t(g % block), 0, 0};
+    dense_adaptive_kernel<double, NU, F, true, true>(a);
+  }
+  for (long long b = 0; b < B; ++b) {
+    printf("%d %d\n", status[b], attempts[b]);
+    for (int k = 0; k < S; ++k) {
+      const long long r = b * S + k;
+      printf("%.17g %d", t[r], steps[r]);
+      for (int e = 0; e < N; ++e) printf(" %.17g", u_mean[r * N + e]);
+      for (int e = 0; e < N * N; ++e) printf(" %.17g", u_chol[r * N * N + e]);
+      printf("\n");
+    }
+  }
+  free(ws);
+  return 0;
+}

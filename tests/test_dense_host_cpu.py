@@ -1,0 +1,61 @@
+"""The dense kernel's float64 body run on the CPU against the golden fixture.
+
+``tests/hostsim/dense_host.cpp`` compiles ``dense_adaptive_kernel`` (one
+thread per instance; van der Pol, TS1 with the Jacobian on dual numbers, the
+fixed-point smoother with its scratch of backward conditionals and the
+backward pass) with the host compiler under AddressSanitizer and UBSan, and
+runs it on the inputs of ``tests/golden/vdp_dense.json`` (the oracle's
+smoothed marginals at 8 save points reached by interpolation, mu = 1 and
+3).  Tolerances of the GPU parity tests (float64): the solution within 1e-8,
+every Taylor row and L L^T within 1e-5, accepted steps within +-1.
+"""
+
+import numpy as np
+import pytest
+
+from tests import hostsim
+from tests.golden import make_golden
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    return hostsim.compile_harness("dense_host.cpp", tmp_path_factory.mktemp("hostsim") / "dense_host")
+
+
+def q1_iwp(nu):
+    n = nu + 1
+    H = np.array([[1.0 / (2 * nu + 1 - i - j) for j in range(n)] for i in range(n)])
+    return np.linalg.cholesky(H)
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path):
+    gold = make_golden.load("vdp_dense.json")
+    mus = gold["mu"]
+    B, S, d, N = len(mus), len(gold["save_at"][0]), 2, 8
+    head = [B, S, 2, 0, 0]  # solver_dynamic, control_integral, interpolation (no clip_dt)
+    body = np.concatenate([[gold["atol"], gold["rtol"]], np.ravel(gold["save_at"]), mus,
+                           np.tile(gold["y0"], B), np.full(B, gold["dt0"]), q1_iwp(3).ravel()])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lines = hostsim.run_harness(harness, path)
+    assert len(lines) == B * (1 + S)
+    for b, rec in enumerate(gold["records"]):
+        status, attempts = (int(x) for x in lines[b * (1 + S)].split())
+        assert status == 0 and attempts > 0
+        steps_o = [0] + rec["num_steps"]
+        for s in range(S):
+            vals = [float(x) for x in lines[b * (1 + S) + 1 + s].split()]
+            t, steps = vals[0], int(vals[1])
+            gm = np.array(vals[2:2 + N])
+            gc = np.array(vals[2 + N:]).reshape(N, N)
+            om, oc = np.array(rec["u_mean"][s]), np.array(rec["u_chol"][s])
+            assert abs(t - gold["save_at"][b][s]) < 1e-7
+            assert rel(gm[:d], om[:d]) <= 1e-8, (b, s)
+            for i in range(N // d):
+                assert rel(gm[i * d:(i + 1) * d], om[i * d:(i + 1) * d]) <= 1e-5, (b, s, i)
+            assert rel(gc @ gc.T, oc @ oc.T) <= 1e-5, (b, s)
+            assert abs(steps - steps_o[s]) <= 1, (b, s, steps, steps_o[s])

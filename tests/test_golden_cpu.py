@@ -53,3 +53,12 @@ def test_fhn_lml_fixture():
     close(now["lml"], gold["lml"])
     close(now["grad"], gold["grad"], 1e-9)
     close(now["grad_y0"], gold["grad_y0"], 1e-9)
+
+
+def test_vdp_dense_fixture():
+    gold = make_golden.load("vdp_dense.json")
+    now = make_golden.vdp_dense_fixture(gold["mu"])
+    for rg, rn in zip(gold["records"], now["records"]):
+        assert rg["num_steps"] == rn["num_steps"]
+        close(rn["u_mean"], rg["u_mean"])
+        close(rn["u_chol"], rg["u_chol"])

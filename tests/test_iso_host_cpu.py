@@ -12,36 +12,18 @@ within +-1, the MLE output scale within 1e-6.  The same source compiled for
 sm_103a is checked against the same fixtures by ``tests/test_golden_gpu.py``.
 """
 
-import os
-import shutil
-import subprocess
-
 import numpy as np
 import pytest
 
+from tests import hostsim
 from tests.golden import make_golden
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-ROOT = os.path.dirname(HERE)
 SOLVER = {"mle": 1, "dynamic": 2}
 
 
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
-    cxx = shutil.which("g++")
-    if cxx is None:
-        pytest.skip("no host C++ compiler")
-    exe = str(tmp_path_factory.mktemp("hostsim") / "iso_host")
-    cmd = [cxx, "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
-           "-I" + os.path.join(HERE, "hostsim"), "-I" + os.path.join(ROOT, "include"),
-           "-I" + os.path.join(ROOT, "probdiffeq_gb300", "csrc"), os.path.join(HERE, "hostsim", "iso_host.cpp"),
-           "-o", exe]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0 and "sanitize" in res.stderr:
-        cmd = [c for c in cmd if "sanitize" not in c]
-        res = subprocess.run(cmd, capture_output=True, text=True)
-    assert res.returncode == 0, res.stderr[-4000:]
-    return exe
+    return hostsim.compile_harness("iso_host.cpp", tmp_path_factory.mktemp("hostsim") / "iso_host")
 
 
 def q1_iwp(nu):
@@ -64,9 +46,7 @@ def test_host_iso_kernel_matches_golden_records(harness, tmp_path, run):
                            np.full(B, gold["dt0"]), q1_iwp(nu).ravel()])
     path = tmp_path / "input.txt"
     path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
-    res = subprocess.run([harness, str(path)], capture_output=True, text=True, timeout=600)
-    assert res.returncode == 0, res.stderr[-4000:]
-    lines = res.stdout.strip().splitlines()
+    lines = hostsim.run_harness(harness, path)
     points = [S - 1] if terminal else list(range(S))
     per = 1 + len(points)
     assert len(lines) == B * per

@@ -13,36 +13,18 @@ Lotka--Volterra (four parameters).  The GPU tests check the same kernels
 compiled for sm_103a.
 """
 
-import os
-import shutil
-import subprocess
-
 import numpy as np
 import pytest
 
+from tests import hostsim
 from tests import lml_problem
 from tests.lml_oracle import lml_value_and_grads
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-ROOT = os.path.dirname(HERE)
 
 
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
-    cxx = shutil.which("g++")
-    if cxx is None:
-        pytest.skip("no host C++ compiler")
-    exe = str(tmp_path_factory.mktemp("hostsim") / "lml_adjoint_host")
-    cmd = [cxx, "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
-           "-I" + os.path.join(HERE, "hostsim"), "-I" + os.path.join(ROOT, "include"),
-           "-I" + os.path.join(ROOT, "probdiffeq_gb300", "csrc"), os.path.join(HERE, "hostsim", "lml_adjoint_host.cpp"),
-           "-o", exe]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0 and "sanitize" in res.stderr:
-        cmd = [c for c in cmd if "sanitize" not in c]  # a toolchain without the sanitizer runtimes
-        res = subprocess.run(cmd, capture_output=True, text=True)
-    assert res.returncode == 0, res.stderr[-4000:]
-    return exe
+    return hostsim.compile_harness("lml_adjoint_host.cpp", tmp_path_factory.mktemp("hostsim") / "lml_adjoint_host")
 
 
 def q1_iwp(nu):
@@ -60,9 +42,7 @@ def run(harness, tmp_path, thetas, y0s, data, dt, num_steps, save_every, ckpt, a
                            np.asarray(cot, dtype=float), [dt], np.ravel(q1_iwp(nu))])
     path = tmp_path / "input.txt"
     path.write_text(" ".join(str(int(v)) for v in head) + " " + " ".join(repr(float(v)) for v in body))
-    res = subprocess.run([harness, str(path)], capture_output=True, text=True, timeout=600)
-    assert res.returncode == 0, res.stderr[-4000:]
-    return np.array([[float(x) for x in line.split()] for line in res.stdout.strip().splitlines()])
+    return np.array([[float(x) for x in line.split()] for line in hostsim.run_harness(harness, path)])
 
 
 @pytest.mark.parametrize("t1,ckpt,average", [(2.0, 14, False), (2.0, 1, False), (2.0, 7, True), (2.0, 200, False),
