@@ -20,6 +20,12 @@ Fixtures:
                    solver_dynamic at save_at (0, 0.7, 2, 3.3, 5) by
                    interpolation; means, Cholesky factors, output scales and
                    accepted steps
+  lv_fixedpoint.json  2 Lotka--Volterra instances, isotropic TS0, fixed-point
+                   smoother, solver_mle, clip_dt, nu = 3, 5 save points:
+                   smoothed means, Cholesky factors, steps, output scale
+  lv_sensitivities.json  2 Lotka--Volterra instances, isotropic TS0 filter,
+                   solver_mle, clip_dt, nu = 3, 4 save points: means and
+                   d u_mean / d params, d u_mean / d y0 (reverse mode)
   vdp_dense.json   van der Pol (mu = 1, 3), dense TS1, fixed-point smoother,
                    solver_dynamic, rtol = atol = 1e-5, 8 save points by
                    interpolation: smoothed means, Cholesky factors, steps
@@ -98,6 +104,74 @@ def lv_filter_fixture(params=None, y0=None):
     return out
 
 
+def lv_fixedpoint_fixture(params=None, y0=None):
+    """Isotropic TS0 fixed-point smoother, solver_mle, clip_dt, nu = 3,
+    rtol = atol = 1e-5, save_at (0, 1.3, 2, 3.7, 5), two Lotka--Volterra
+    instances: smoothed means, Cholesky factors, steps, output scale."""
+    from oracle import problems, solvers, ssm
+
+    if params is None:
+        params, y0 = lv_inputs()
+        params, y0 = params[:2], y0[:2]
+    save_at = [0.0, 1.3, 2.0, 3.7, 5.0]
+    out = {"params": params.tolist(), "y0": y0.tolist(), "num_derivatives": 3, "save_at": save_at, "rtol": 1e-5,
+           "atol": 1e-5, "dt0": 0.1, "records": []}
+    for b in range(params.shape[0]):
+        tc = problems.taylor_derivatives(problems.lotka_volterra, y0[b], params[b], 3)
+        S = ssm.IsoSSM()
+        c = S.constraint_ode_ts0(lambda u, t, p=params[b]: problems.lotka_volterra(u[0], p))
+        res = solvers.solve_adaptive_save_at(solvers.SolverMLE(solvers.StrategyFixedPoint(), c),
+                                             solvers.ErrorResidualStd(c), S.prior_wiener_integrated(tc), save_at,
+                                             1e-5, 1e-5, clip_dt=True, dt0=0.1)
+        out["records"].append({
+            "u_mean": [u.mean.tolist() for u in res.u],
+            "u_chol": [u.cholesky.tolist() for u in res.u],
+            "output_scale": [float(s) for s in res.output_scale],
+            "num_steps": [int(s) for s in res.num_steps],
+        })
+    return out
+
+
+def lv_sensitivities_fixture(params=None, y0=None):
+    """d u_mean / d params and d u_mean / d y0 of the isotropic TS0 filter
+    (solver_mle, clip_dt, nu = 3, rtol = atol = 1e-6) at save_at
+    linspace(0, 5, 4), two Lotka--Volterra instances: PyTorch reverse mode
+    through the oracle, the step sizes held constant as in the reference."""
+    from oracle import problems, solvers, ssm
+
+    if params is None:
+        params, y0 = lv_inputs()
+        params, y0 = params[2:], y0[2:]
+    save_at = [0.0, 5.0 / 3.0, 10.0 / 3.0, 5.0]
+    out = {"params": params.tolist(), "y0": y0.tolist(), "num_derivatives": 3, "save_at": save_at, "rtol": 1e-6,
+           "atol": 1e-6, "dt0": 0.1, "records": []}
+    for b in range(params.shape[0]):
+        p = params[b].clone().requires_grad_(True)
+        y = y0[b].clone().requires_grad_(True)
+        tc = problems.taylor_derivatives(problems.lotka_volterra, y, p, 3)
+        S = ssm.IsoSSM()
+        c = S.constraint_ode_ts0(lambda u, t: problems.lotka_volterra(u[0], p))
+        res = solvers.solve_adaptive_save_at(solvers.SolverMLE(solvers.StrategyFilter(), c), solvers.ErrorResidualStd(c),
+                                             S.prior_wiener_integrated(tc), save_at, 1e-6, 1e-6, clip_dt=True, dt0=0.1)
+        rec = {"u_mean": [], "d_params": [], "d_y0": [], "num_steps": [int(s) for s in res.num_steps]}
+        for u in res.u:
+            m = u.mean
+            jp = torch.zeros(m.shape + p.shape, dtype=torch.float64)
+            jy = torch.zeros(m.shape + y.shape, dtype=torch.float64)
+            for i in range(m.shape[0]):
+                for j in range(m.shape[1]):
+                    if not m[i, j].requires_grad:
+                        continue
+                    gp, gy = torch.autograd.grad(m[i, j], (p, y), retain_graph=True, allow_unused=True)
+                    jp[i, j] = gp if gp is not None else 0.0
+                    jy[i, j] = gy if gy is not None else 0.0
+            rec["u_mean"].append(m.detach().tolist())
+            rec["d_params"].append(jp.tolist())
+            rec["d_y0"].append(jy.tolist())
+        out["records"].append(rec)
+    return out
+
+
 def vdp_dense_fixture(mus=None):
     """Dense TS1 van der Pol (first order), fixed-point smoother, dynamic
     calibration, error_residual_std, integral control, nu = 3,
@@ -159,6 +233,7 @@ def load(name):
 def main():
     torch.set_default_dtype(torch.float64)
     for name, fn in (("iwp.json", iwp_fixture), ("lv_filter.json", lv_filter_fixture),
+                     ("lv_fixedpoint.json", lv_fixedpoint_fixture), ("lv_sensitivities.json", lv_sensitivities_fixture),
                      ("vdp_dense.json", vdp_dense_fixture), ("fhn_lml.json", fhn_lml_fixture)):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(fn(), f, indent=1)

@@ -1,17 +1,20 @@
 // Runs the float64 isotropic adaptive kernel (iso_adaptive_kernel, one thread
 // per instance, Lotka-Volterra) on the CPU, every instance as its own
 // "thread", on buffers of exactly the sizes the library uses, so
-// AddressSanitizer flags any access outside them.  Filter strategy; the
-// instantiation the library launches for the configuration: the lean one
-// (TS0, error_residual_std) with exact checkpoint landings (clip_dt) or with
-// interpolation.
+// AddressSanitizer flags any access outside them.  The instantiations the
+// library launches for TS0 with error_residual_std, with exact checkpoint
+// landings (clip_dt) or with interpolation: mode 0 the filter (the lean
+// instantiation), mode 1 the fixed-point smoother (its scratch of backward
+// conditionals and the backward pass), mode 2 the filter with forward-mode
+// sensitivities (P + d threads per instance).
 //
-// Input file (whitespace-separated): nu B S solver control clip_dt
+// Input file (whitespace-separated): mode nu B S solver control clip_dt
 // terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
 // dt0 (B), Q1 ((nu + 1) x (nu + 1), row-major).  solver / control take the
 // PDQ_SOLVER_* / PDQ_CONTROL_* codes.
 // Output: per instance a line "status attempts", then per output record a
-// line "t num_steps output_scale u_mean[n d] u_chol[n n]".
+// line "t num_steps output_scale u_mean[n d] u_chol[n n]" (mode 2: followed
+// by d u_mean / d params [n d 4] and d u_mean / d y0 [n d 2]).
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -28,7 +31,7 @@ static bool read_all(FILE* in, std::vector<double>& v) {
   return true;
 }
 
-template <int NU, bool INTERP>
+template <int NU, bool INTERP, int MODE>
 static int run(FILE* in, long long B, int S, int solver, int control, int clip_dt, int terminal_only) {
   using F = LotkaVolterra;
   constexpr int n = NU + 1;
@@ -41,6 +44,8 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   const int S_out = terminal_only ? 1 : S;
   std::vector<double> u_mean(B * S_out * n * D), u_chol(B * S_out * n * n), scale(B * S_out), t(B * S_out);
   std::vector<int32_t> steps(B * S_out), attempts(B), status(B);
+  std::vector<double> tan_p(MODE == 2 ? B * S_out * n * D * P : 0), tan_y(MODE == 2 ? B * S_out * n * D * D : 0);
+  std::vector<double> ws(MODE == 1 ? B * (S - 1) * iso_cond_floats<NU, D>() : 0);
 
   IsoArgs a;
   memset(&a, 0, sizeof(a));
@@ -75,14 +80,23 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   a.num_steps = steps.data();
   a.num_attempts = attempts.data();
   a.status = status.data();
+  if (MODE == 1) a.workspace = ws.data();
+  if (MODE == 2) {
+    a.tan_params = tan_p.data();
+    a.tan_y0 = tan_y.data();
+    a.tangents = 1;
+  }
 
   const int block = 64;
   blockDim = {uint32_t(block), 1, 1};
-  const long long padded = (B + block - 1) / block * block;  // the launch's grid
+  const long long threads = MODE == 2 ? B * (P + D) : B;
+  const long long padded = (threads + block - 1) / block * block;  // the launch's grid
   for (long long g = 0; g < padded; ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
-    iso_adaptive_kernel<double, NU, F, INTERP, false, false>(a);
+    if constexpr (MODE == 0) iso_adaptive_kernel<double, NU, F, INTERP, false, false>(a);
+    if constexpr (MODE == 1) iso_adaptive_kernel<double, NU, F, INTERP, true, true>(a);
+    if constexpr (MODE == 2) iso_adaptive_kernel<double, NU, F, INTERP, false, false, true>(a);
   }
   for (long long b = 0; b < B; ++b) {
     printf("%d %d\n", status[b], attempts[b]);
@@ -91,6 +105,10 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
       printf("%.17g %d %.17g", t[r], steps[r], scale[r]);
       for (int e = 0; e < n * D; ++e) printf(" %.17g", u_mean[r * n * D + e]);
       for (int e = 0; e < n * n; ++e) printf(" %.17g", u_chol[r * n * n + e]);
+      if (MODE == 2) {
+        for (int e = 0; e < n * D * P; ++e) printf(" %.17g", tan_p[r * n * D * P + e]);
+        for (int e = 0; e < n * D * D; ++e) printf(" %.17g", tan_y[r * n * D * D + e]);
+      }
       printf("\n");
     }
   }
@@ -102,15 +120,22 @@ int main(int argc, char** argv) {
   FILE* in = fopen(argv[1], "r");
   if (!in) return 2;
   long long B;
-  int nu, S, solver, control, clip_dt, terminal_only;
-  if (fscanf(in, "%d %lld %d %d %d %d %d", &nu, &B, &S, &solver, &control, &clip_dt, &terminal_only) != 7) return 2;
+  int mode, nu, S, solver, control, clip_dt, terminal_only;
+  if (fscanf(in, "%d %d %lld %d %d %d %d %d", &mode, &nu, &B, &S, &solver, &control, &clip_dt, &terminal_only) != 8)
+    return 2;
   if (B < 1 || S < 2) return 2;
   int rc = 2;
   const bool interp = !clip_dt;
-  if (nu == 4) rc = interp ? run<4, true>(in, B, S, solver, control, clip_dt, terminal_only)
-                           : run<4, false>(in, B, S, solver, control, clip_dt, terminal_only);
-  if (nu == 2) rc = interp ? run<2, true>(in, B, S, solver, control, clip_dt, terminal_only)
-                           : run<2, false>(in, B, S, solver, control, clip_dt, terminal_only);
+  const int args_ok = (mode == 0 || mode == 1 || mode == 2) && (nu == 3 || nu == 4);
+  if (!args_ok) return 2;
+#define PDQ_HOST_RUN(NU_, MODE_)                                                              \
+  rc = interp ? run<NU_, true, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)     \
+              : run<NU_, false, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)
+  if (nu == 4 && mode == 0) PDQ_HOST_RUN(4, 0);
+  if (nu == 3 && mode == 0) PDQ_HOST_RUN(3, 0);
+  if (nu == 3 && mode == 1) PDQ_HOST_RUN(3, 1);
+  if (nu == 3 && mode == 2) PDQ_HOST_RUN(3, 2);
+#undef PDQ_HOST_RUN
   fclose(in);
   return rc;
 }

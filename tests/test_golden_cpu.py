@@ -62,3 +62,23 @@ def test_vdp_dense_fixture():
         assert rg["num_steps"] == rn["num_steps"]
         close(rn["u_mean"], rg["u_mean"])
         close(rn["u_chol"], rg["u_chol"])
+
+
+def test_lv_fixedpoint_fixture():
+    gold = make_golden.load("lv_fixedpoint.json")
+    now = make_golden.lv_fixedpoint_fixture(torch.tensor(gold["params"]), torch.tensor(gold["y0"]))
+    for rg, rn in zip(gold["records"], now["records"]):
+        assert rg["num_steps"] == rn["num_steps"]
+        close(rn["u_mean"], rg["u_mean"])
+        close(rn["u_chol"], rg["u_chol"])
+        close(rn["output_scale"], rg["output_scale"])
+
+
+def test_lv_sensitivities_fixture():
+    gold = make_golden.load("lv_sensitivities.json")
+    now = make_golden.lv_sensitivities_fixture(torch.tensor(gold["params"]), torch.tensor(gold["y0"]))
+    for rg, rn in zip(gold["records"], now["records"]):
+        assert rg["num_steps"] == rn["num_steps"]
+        close(rn["u_mean"], rg["u_mean"])
+        close(rn["d_params"], rg["d_params"], 1e-9)
+        close(rn["d_y0"], rg["d_y0"], 1e-9)

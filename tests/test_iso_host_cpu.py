@@ -1,5 +1,6 @@
-"""The headline isotropic kernel's float64 body run on the CPU against the
-golden fixtures.
+"""The isotropic kernel's float64 bodies run on the CPU against the golden
+fixtures: the headline filter instantiation, the fixed-point smoother and
+the forward-mode sensitivities.
 
 ``tests/hostsim/iso_host.cpp`` compiles ``iso_adaptive_kernel`` (one thread
 per instance, Lotka--Volterra, the lean TS0 / error_residual_std
@@ -41,7 +42,7 @@ def test_host_iso_kernel_matches_golden_records(harness, tmp_path, run):
     B, S = params.shape[0], len(r["save_at"])
     terminal = run == "mle_terminal"
     solver = SOLVER["mle" if terminal else "dynamic"]
-    head = [nu, B, S, solver, 0, int(r["clip_dt"]), int(terminal)]
+    head = [0, nu, B, S, solver, 0, int(r["clip_dt"]), int(terminal)]
     body = np.concatenate([[r["atol"], r["rtol"]], np.tile(r["save_at"], B), params.ravel(), y0.ravel(),
                            np.full(B, gold["dt0"]), q1_iwp(nu).ravel()])
     path = tmp_path / "input.txt"
@@ -70,3 +71,73 @@ def test_host_iso_kernel_matches_golden_records(harness, tmp_path, run):
             if terminal:
                 so = rec["output_scale"][-1]
                 assert abs(scale - so) <= 1e-6 * abs(so), (scale, so)
+
+
+def _run(harness, tmp_path, mode, gold, solver, clip_dt, terminal):
+    nu = gold["num_derivatives"]
+    params, y0 = np.array(gold["params"]), np.array(gold["y0"])
+    B, S = params.shape[0], len(gold["save_at"])
+    head = [mode, nu, B, S, solver, 0, int(clip_dt), int(terminal)]
+    body = np.concatenate([[gold["atol"], gold["rtol"]], np.tile(gold["save_at"], B), params.ravel(), y0.ravel(),
+                           np.full(B, gold["dt0"]), q1_iwp(nu).ravel()])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lines = hostsim.run_harness(harness, path)
+    assert len(lines) == B * (1 + S)
+    return lines
+
+
+def test_host_iso_fixed_point_smoother_matches_golden_records(harness, tmp_path):
+    """Fixed-point smoother (scratch of backward conditionals, backward pass),
+    solver_mle, clip_dt: smoothed marginals at every save point."""
+    gold = make_golden.load("lv_fixedpoint.json")
+    nu, n, d = gold["num_derivatives"], gold["num_derivatives"] + 1, 2
+    S = len(gold["save_at"])
+    lines = _run(harness, tmp_path, 1, gold, SOLVER["mle"], True, False)
+    for b, rec in enumerate(gold["records"]):
+        status, _ = (int(x) for x in lines[b * (1 + S)].split())
+        assert status == 0
+        for s in range(S):
+            vals = [float(x) for x in lines[b * (1 + S) + 1 + s].split()]
+            gm = np.array(vals[3:3 + n * d]).reshape(n, d)
+            gc = np.array(vals[3 + n * d:]).reshape(n, n)
+            om, oc = np.array(rec["u_mean"][s]), np.array(rec["u_chol"][s])
+            assert float(np.abs(gm[0] - om[0]).max() / np.abs(om[0]).max()) <= 1e-9, (b, s)
+            for i in range(n):
+                assert float(np.abs(gm[i] - om[i]).max() / max(np.abs(om[i]).max(), 1e-300)) <= 1e-6, (b, s, i)
+            cg, co = gc @ gc.T, oc @ oc.T
+            assert float(np.abs(cg - co).max() / max(np.abs(co).max(), 1e-300)) <= 1e-6, (b, s)
+            steps_o = 0 if s == 0 else rec["num_steps"][s - 1]
+            assert abs(int(vals[1]) - steps_o) <= 1
+        so = rec["output_scale"][-1]
+        assert abs(vals[2] - so) <= 1e-6 * abs(so)
+
+
+def test_host_iso_sensitivities_match_golden_reverse_mode(harness, tmp_path):
+    """Forward-mode sensitivities (P + d threads per instance) against the
+    oracle's reverse mode: 1e-9 (values) / 1e-8 (sensitivities) relative when
+    the accepted-step counts agree, the solver tolerance (1e-6 / 1e-5)
+    otherwise."""
+    gold = make_golden.load("lv_sensitivities.json")
+    nu, n, d, P = gold["num_derivatives"], gold["num_derivatives"] + 1, 2, 4
+    S = len(gold["save_at"])
+    lines = _run(harness, tmp_path, 2, gold, SOLVER["mle"], True, False)
+    for b, rec in enumerate(gold["records"]):
+        status, _ = (int(x) for x in lines[b * (1 + S)].split())
+        assert status == 0
+        for s in range(S):
+            vals = np.array([float(x) for x in lines[b * (1 + S) + 1 + s].split()])
+            o = 3
+            gm = vals[o:o + n * d].reshape(n, d)
+            o += n * d + n * n
+            gp = vals[o:o + n * d * P].reshape(n, d, P)
+            gy = vals[o + n * d * P:].reshape(n, d, d)
+            om, op, oy = np.array(rec["u_mean"][s]), np.array(rec["d_params"][s]), np.array(rec["d_y0"][s])
+            steps_o = 0 if s == 0 else rec["num_steps"][s - 1]
+            same = int(vals[1]) == steps_o
+            assert abs(int(vals[1]) - steps_o) <= 1
+            tol_v, tol_g = (1e-9, 1e-8) if same else (1e-6, 1e-5)
+            rel = lambda g, w: float(np.abs(g - w).max() / max(np.abs(w).max(), 1e-300))  # noqa: E731
+            assert rel(gm, om) < tol_v, (b, s)
+            assert rel(gp, op) < tol_g, (b, s, rel(gp, op))
+            assert rel(gy, oy) < tol_g, (b, s, rel(gy, oy))
