@@ -21,7 +21,13 @@
  *     synchronisation inside the calls;
  *   - configuration errors return a non-zero pdq_status before any launch;
  *     run-time failures are reported per instance in the status array
- *     (never a trap).
+ *     (never a trap);
+ *   - the first call of an entry point on a device may raise the context's
+ *     per-thread stack limit for its kernels (a one-time, synchronising
+ *     cudaDeviceSetLimit); make it before capturing a stream into a graph,
+ *     later calls only enqueue launches;
+ *   - every entry point opens an NVTX range named after itself (visible to
+ *     ncu --nvtx and Nsight Systems).
  */
 #ifndef PDQ_H_
 #define PDQ_H_
