@@ -90,19 +90,31 @@ PDQ_D T dev_fmax_abs(T a, T b) {
 // the normal range (the QR and rotation code checks sums of squares against
 // [1e-30, 1e36] before using these).  In float64 they are the exact ops.
 PDQ_D float fast_sqrt(float x) {
+#if defined(__CUDA_ARCH__)
   float r;
   asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
+#else
+  return sqrtf(x);  // host runs of the kernel bodies (tests)
+#endif
 }
 PDQ_D float fast_rsqrt(float x) {
+#if defined(__CUDA_ARCH__)
   float r;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
+#else
+  return 1.0f / sqrtf(x);  // host runs of the kernel bodies (tests)
+#endif
 }
 PDQ_D float fast_rcp(float x) {
+#if defined(__CUDA_ARCH__)
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
+#else
+  return 1.0f / x;  // host runs of the kernel bodies (tests)
+#endif
 }
 PDQ_D double fast_sqrt(double x) { return sqrt(x); }
 PDQ_D double fast_rsqrt(double x) { return rsqrt(x); }

@@ -1,5 +1,6 @@
-// Runs the float64 isotropic adaptive kernel (iso_adaptive_kernel, one thread
-// per instance, Lotka-Volterra) on the CPU, every instance as its own
+// Runs the isotropic adaptive kernel (iso_adaptive_kernel, one thread per
+// instance, Lotka-Volterra; float64, or float32 bulk with float-pair
+// accumulators) on the CPU, every instance as its own
 // "thread", on buffers of exactly the sizes the library uses, so
 // AddressSanitizer flags any access outside them.  The instantiations the
 // library launches for TS0 with error_residual_std, with exact checkpoint
@@ -8,8 +9,8 @@
 // conditionals and the backward pass), mode 2 the filter with forward-mode
 // sensitivities (P + d threads per instance).
 //
-// Input file (whitespace-separated): mode nu B S solver control clip_dt
-// terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
+// Input file (whitespace-separated): precision (0 float32, 1 float64) mode nu
+// B S solver control clip_dt terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
 // dt0 (B), Q1 ((nu + 1) x (nu + 1), row-major).  solver / control take the
 // PDQ_SOLVER_* / PDQ_CONTROL_* codes.
 // Output: per instance a line "status attempts", then per output record a
@@ -31,7 +32,7 @@ static bool read_all(FILE* in, std::vector<double>& v) {
   return true;
 }
 
-template <int NU, bool INTERP, int MODE>
+template <typename T, int NU, bool INTERP, int MODE>
 static int run(FILE* in, long long B, int S, int solver, int control, int clip_dt, int terminal_only) {
   using F = LotkaVolterra;
   constexpr int n = NU + 1;
@@ -45,7 +46,7 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   std::vector<double> u_mean(B * S_out * n * D), u_chol(B * S_out * n * n), scale(B * S_out), t(B * S_out);
   std::vector<int32_t> steps(B * S_out), attempts(B), status(B);
   std::vector<double> tan_p(MODE == 2 ? B * S_out * n * D * P : 0), tan_y(MODE == 2 ? B * S_out * n * D * D : 0);
-  std::vector<double> ws(MODE == 1 ? B * (S - 1) * iso_cond_floats<NU, D>() : 0);
+  std::vector<T> ws(MODE == 1 ? B * (S - 1) * iso_cond_floats<NU, D>() : 0);
 
   IsoArgs a;
   memset(&a, 0, sizeof(a));
@@ -68,7 +69,20 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   a.damp = 0.0;
   a.max_attempts = int64_t(1) << 20;  // pdq_config_default
   for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) a.q1[i][j] = q1[i * n + j];
+    for (int j = 0; j < n; ++j) {
+      a.q1[i][j] = q1[i * n + j];
+      a.q1f[i][j] = float(q1[i * n + j]);
+    }
+  // float copies of the constants (read by the float32 kernels)
+  a.safety_f = float(a.safety);
+  a.factor_min_f = float(a.factor_min);
+  a.factor_max_f = float(a.factor_max);
+  a.exp_i_f = float(a.exp_i);
+  a.exp_p_f = float(a.exp_p);
+  a.atol_f = float(a.atol);
+  a.rtol_f = float(a.rtol);
+  a.eps_f = float(a.eps);
+  a.damp_f = float(a.damp);
   a.save_at = save_at.data();
   a.params = params.data();
   a.y0 = y0.data();
@@ -94,9 +108,9 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   for (long long g = 0; g < padded; ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
-    if constexpr (MODE == 0) iso_adaptive_kernel<double, NU, F, INTERP, false, false>(a);
-    if constexpr (MODE == 1) iso_adaptive_kernel<double, NU, F, INTERP, true, true>(a);
-    if constexpr (MODE == 2) iso_adaptive_kernel<double, NU, F, INTERP, false, false, true>(a);
+    if constexpr (MODE == 0) iso_adaptive_kernel<T, NU, F, INTERP, false, false>(a);
+    if constexpr (MODE == 1) iso_adaptive_kernel<T, NU, F, INTERP, true, true>(a);
+    if constexpr (MODE == 2) iso_adaptive_kernel<T, NU, F, INTERP, false, false, true>(a);
   }
   for (long long b = 0; b < B; ++b) {
     printf("%d %d\n", status[b], attempts[b]);
@@ -120,17 +134,20 @@ int main(int argc, char** argv) {
   FILE* in = fopen(argv[1], "r");
   if (!in) return 2;
   long long B;
-  int mode, nu, S, solver, control, clip_dt, terminal_only;
-  if (fscanf(in, "%d %d %lld %d %d %d %d %d", &mode, &nu, &B, &S, &solver, &control, &clip_dt, &terminal_only) != 8)
+  int prec, mode, nu, S, solver, control, clip_dt, terminal_only;
+  if (fscanf(in, "%d %d %d %lld %d %d %d %d %d", &prec, &mode, &nu, &B, &S, &solver, &control, &clip_dt,
+             &terminal_only) != 9)
     return 2;
   if (B < 1 || S < 2) return 2;
   int rc = 2;
   const bool interp = !clip_dt;
   const int args_ok = (mode == 0 || mode == 1 || mode == 2) && (nu == 3 || nu == 4);
   if (!args_ok) return 2;
-#define PDQ_HOST_RUN(NU_, MODE_)                                                              \
-  rc = interp ? run<NU_, true, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)     \
-              : run<NU_, false, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)
+#define PDQ_HOST_RUN(NU_, MODE_)                                                                        \
+  rc = prec ? (interp ? run<double, NU_, true, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)    \
+                      : run<double, NU_, false, MODE_>(in, B, S, solver, control, clip_dt, terminal_only))  \
+            : (interp ? run<float, NU_, true, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)     \
+                      : run<float, NU_, false, MODE_>(in, B, S, solver, control, clip_dt, terminal_only))
   if (nu == 4 && mode == 0) PDQ_HOST_RUN(4, 0);
   if (nu == 3 && mode == 0) PDQ_HOST_RUN(3, 0);
   if (nu == 3 && mode == 1) PDQ_HOST_RUN(3, 1);

@@ -42,7 +42,7 @@ def test_host_iso_kernel_matches_golden_records(harness, tmp_path, run):
     B, S = params.shape[0], len(r["save_at"])
     terminal = run == "mle_terminal"
     solver = SOLVER["mle" if terminal else "dynamic"]
-    head = [0, nu, B, S, solver, 0, int(r["clip_dt"]), int(terminal)]
+    head = [1, 0, nu, B, S, solver, 0, int(r["clip_dt"]), int(terminal)]
     body = np.concatenate([[r["atol"], r["rtol"]], np.tile(r["save_at"], B), params.ravel(), y0.ravel(),
                            np.full(B, gold["dt0"]), q1_iwp(nu).ravel()])
     path = tmp_path / "input.txt"
@@ -77,7 +77,7 @@ def _run(harness, tmp_path, mode, gold, solver, clip_dt, terminal):
     nu = gold["num_derivatives"]
     params, y0 = np.array(gold["params"]), np.array(gold["y0"])
     B, S = params.shape[0], len(gold["save_at"])
-    head = [mode, nu, B, S, solver, 0, int(clip_dt), int(terminal)]
+    head = [1, mode, nu, B, S, solver, 0, int(clip_dt), int(terminal)]
     body = np.concatenate([[gold["atol"], gold["rtol"]], np.tile(gold["save_at"], B), params.ravel(), y0.ravel(),
                            np.full(B, gold["dt0"]), q1_iwp(nu).ravel()])
     path = tmp_path / "input.txt"
@@ -141,3 +141,35 @@ def test_host_iso_sensitivities_match_golden_reverse_mode(harness, tmp_path):
             assert rel(gm, om) < tol_v, (b, s)
             assert rel(gp, op) < tol_g, (b, s, rel(gp, op))
             assert rel(gy, oy) < tol_g, (b, s, rel(gy, oy))
+
+
+def test_host_iso_float32_kernel_against_golden_records(harness, tmp_path):
+    """The float32 headline instantiation (bulk float32, time and
+    accumulators in float pairs): the solution row within 1e-4 and u' within
+    1e-2 of the float64 oracle, a valid covariance and output scale, accepted
+    steps within 10 % (the float32 bounds of the GPU parity tests)."""
+    gold = make_golden.load("lv_filter.json")
+    r = gold["mle_terminal"]
+    nu, n, d = gold["num_derivatives"], gold["num_derivatives"] + 1, 2
+    params, y0 = np.array(gold["params"]), np.array(gold["y0"])
+    B, S = params.shape[0], len(r["save_at"])
+    head = [0, 0, nu, B, S, SOLVER["mle"], 0, 1, 1]
+    body = np.concatenate([[r["atol"], r["rtol"]], np.tile(r["save_at"], B), params.ravel(), y0.ravel(),
+                           np.full(B, gold["dt0"]), q1_iwp(nu).ravel()])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lines = hostsim.run_harness(harness, path)
+    assert len(lines) == 2 * B
+    for b, rec in enumerate(r["records"]):
+        status, _ = (int(x) for x in lines[2 * b].split())
+        assert status == 0
+        vals = [float(x) for x in lines[2 * b + 1].split()]
+        gm = np.array(vals[3:3 + n * d]).reshape(n, d)
+        gc = np.array(vals[3 + n * d:]).reshape(n, n)
+        om = np.array(rec["u_mean"][-1])
+        assert float(np.abs(gm[0] - om[0]).max() / np.abs(om[0]).max()) <= 1e-4, b
+        assert float(np.abs(gm[1] - om[1]).max() / np.abs(om[1]).max()) <= 1e-2, b
+        assert np.isfinite(gc).all() and (np.diag(gc @ gc.T) >= 0).all()
+        assert np.isfinite(vals[2]) and vals[2] > 0
+        steps_o = rec["num_steps"][-1]
+        assert abs(int(vals[1]) - steps_o) <= max(1, int(np.ceil(0.1 * steps_o))), (int(vals[1]), steps_o)
