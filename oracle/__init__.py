@@ -18,7 +18,12 @@ machines, so the reference itself cannot run.  The restatement is pinned to
 the reference's own known-answer tests and equivalence tests (see
 ``tests/test_oracle_*.py``), to closed-form results, and to a
 high-accuracy classical ODE solver (scipy DOP853), which is what the
-reference's own accuracy tests compare against.
+reference's own accuracy tests compare against.  One exception: the
+log-marginal-likelihood's values and gradients are parity unpinned by the
+reference, whose tests only check that they are finite; here they are
+pinned by internal consistency only (PyTorch reverse mode through the
+restatement against central finite differences, and forward-mode and
+adjoint kernels against both).
 
 ``oracle/port`` holds a plain-C float64 port of the isotropic TS0 adaptive
 solver (the ensemble configuration) used as the timed CPU baseline.
