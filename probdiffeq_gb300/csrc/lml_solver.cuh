@@ -502,9 +502,14 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       // stage the next chunk of step tables (coalesced, the whole warp)
       const int count = min(kLmlChunk, a.num_steps - (step - 1)) * kStep;
       const T* src = plan + int64_t(step - 1) * kStep;
+#if defined(__CUDA_ARCH__)
       __syncwarp();
       for (int e = lane; e < count; e += 32) stage[e] = src[e];
       __syncwarp();
+#else
+      // host runs of the kernel body execute one lane at a time: it stages the whole chunk
+      for (int e = 0; e < count; ++e) stage[e] = src[e];
+#endif
     }
     if (!valid || status != PDQ_INSTANCE_OK) continue;
     // this step's tables into registers in one batch of 16-byte loads, so

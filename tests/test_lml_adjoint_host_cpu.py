@@ -1,4 +1,5 @@
-"""The adjoint LML kernels' float64 bodies run on the CPU against the oracle.
+"""The LML kernels' float64 bodies run on the CPU against the oracle: the
+adjoint pair and the forward-mode kernel.
 
 ``tests/hostsim`` compiles the kernel templates of ``lml_adjoint.cuh`` with
 the host compiler (a stand-in for ``cuda_runtime.h`` turns the CUDA
@@ -92,3 +93,31 @@ def test_host_adjoint_other_instantiations(harness, tmp_path, field, nu):
         assert abs(out[b, 1] - v) <= 1e-10 * abs(v), (out[b, 1], v)
         assert np.abs(out[b, 2:2 + P] - cot[b] * g).max() <= 1e-10 * np.linalg.norm(cot[b] * g), (out[b, 2:2 + P], g)
         assert np.abs(out[b, 2 + P:] - cot[b] * gy).max() <= 1e-10 * np.linalg.norm(cot[b] * gy), (out[b, 2 + P:], gy)
+
+
+@pytest.fixture(scope="module")
+def forward_harness(tmp_path_factory):
+    return hostsim.compile_harness("lml_forward_host.cpp", tmp_path_factory.mktemp("hostsim") / "lml_forward_host")
+
+
+@pytest.mark.parametrize("t1,average", [(2.0, False), (2.0, True), (20.0, False)])
+def test_host_forward_mode_lml_matches_oracle(forward_harness, tmp_path, t1, average):
+    """The forward-mode kernel (the LML benchmark's kernel, P tangent
+    threads per sample) on the CPU: value and d/d params against the
+    oracle's reverse mode to 1e-10, on the 2000-step benchmark grid too."""
+    dt, save_every = 0.01, 10
+    num_steps, data = lml_problem.observations(t1=t1, dt=dt, save_every=save_every)
+    thetas = lml_problem.theta_samples(3, seed=1)
+    y0s = np.tile(lml_problem.U0, (3, 1))
+    head = [0, 3, 3, num_steps, save_every, int(average)]
+    body = np.concatenate([thetas.ravel(), y0s.ravel(), np.ravel(data), np.full(data.shape[0], lml_problem.STD), [dt],
+                           np.ravel(q1_iwp(3))])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(int(v)) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    out = np.array([[float(x) for x in line.split()] for line in hostsim.run_harness(forward_harness, path)])
+    assert out.shape == (3, 5)
+    for b in range(3):
+        v, g, _ = lml_value_and_grads(thetas[b], y0s[b], data, dt, num_steps, save_every, average_pdfs=average)
+        assert out[b, 0] == 0
+        assert abs(out[b, 1] - v) <= 1e-10 * abs(v), (out[b, 1], v)
+        assert np.abs(out[b, 2:5] - g).max() <= 1e-10 * np.linalg.norm(g), (out[b, 2:5], g)
