@@ -7,7 +7,9 @@
 // landings (clip_dt) or with interpolation: mode 0 the filter (the lean
 // instantiation), mode 1 the fixed-point smoother (its scratch of backward
 // conditionals and the backward pass), mode 2 the filter with forward-mode
-// sensitivities (P + d threads per instance).
+// sensitivities (P + d threads per instance), modes 3 and 4 the general
+// filter instantiation with error_state_std, with TS0 (3) or TS1 (4, the
+// Jacobian trace along d).
 //
 // Input file (whitespace-separated): precision (0 float32, 1 float64) mode nu
 // B S solver control clip_dt terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
@@ -95,6 +97,10 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   a.num_attempts = attempts.data();
   a.status = status.data();
   if (MODE == 1) a.workspace = ws.data();
+  if (MODE == 3 || MODE == 4) {
+    a.state_error = 1;
+    a.ts1 = MODE == 4 ? 1 : 0;
+  }
   if (MODE == 2) {
     a.tan_params = tan_p.data();
     a.tan_y0 = tan_y.data();
@@ -111,6 +117,7 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
     if constexpr (MODE == 0) iso_adaptive_kernel<T, NU, F, INTERP, false, false>(a);
     if constexpr (MODE == 1) iso_adaptive_kernel<T, NU, F, INTERP, true, true>(a);
     if constexpr (MODE == 2) iso_adaptive_kernel<T, NU, F, INTERP, false, false, true>(a);
+    if constexpr (MODE == 3 || MODE == 4) iso_adaptive_kernel<T, NU, F, INTERP, false, true>(a);
   }
   for (long long b = 0; b < B; ++b) {
     printf("%d %d\n", status[b], attempts[b]);
@@ -141,7 +148,7 @@ int main(int argc, char** argv) {
   if (B < 1 || S < 2) return 2;
   int rc = 2;
   const bool interp = !clip_dt;
-  const int args_ok = (mode == 0 || mode == 1 || mode == 2) && (nu == 3 || nu == 4);
+  const int args_ok = (mode >= 0 && mode <= 4) && (nu == 3 || nu == 4);
   if (!args_ok) return 2;
 #define PDQ_HOST_RUN(NU_, MODE_)                                                                        \
   rc = prec ? (interp ? run<double, NU_, true, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)    \
@@ -152,6 +159,8 @@ int main(int argc, char** argv) {
   if (nu == 3 && mode == 0) PDQ_HOST_RUN(3, 0);
   if (nu == 3 && mode == 1) PDQ_HOST_RUN(3, 1);
   if (nu == 3 && mode == 2) PDQ_HOST_RUN(3, 2);
+  if (nu == 3 && mode == 3) PDQ_HOST_RUN(3, 3);
+  if (nu == 3 && mode == 4) PDQ_HOST_RUN(3, 4);
 #undef PDQ_HOST_RUN
   fclose(in);
   return rc;

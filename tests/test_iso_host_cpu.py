@@ -83,7 +83,7 @@ def _run(harness, tmp_path, mode, gold, solver, clip_dt, terminal):
     path = tmp_path / "input.txt"
     path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
     lines = hostsim.run_harness(harness, path)
-    assert len(lines) == B * (1 + S)
+    assert len(lines) == B * (1 + (1 if terminal else S))
     return lines
 
 
@@ -173,3 +173,42 @@ def test_host_iso_float32_kernel_against_golden_records(harness, tmp_path):
         assert np.isfinite(vals[2]) and vals[2] > 0
         steps_o = rec["num_steps"][-1]
         assert abs(int(vals[1]) - steps_o) <= max(1, int(np.ceil(0.1 * steps_o))), (int(vals[1]), steps_o)
+
+
+@pytest.mark.parametrize("constraint", ["ts0", "ts1"])
+def test_host_iso_error_state_std_matches_oracle(harness, tmp_path, constraint):
+    """The general instantiation with error_state_std (solvers.py:999-1098),
+    TS0 and TS1 (trace of the Jacobian along d), solver_mle, clip_dt, on two
+    Lotka--Volterra instances of the golden inputs, against the oracle run
+    here (float64 tolerances of the GPU parity tests)."""
+    import torch
+
+    from oracle import problems, solvers, ssm
+
+    gold = make_golden.load("lv_fixedpoint.json")
+    gold = dict(gold, save_at=[0.0, 8.0])
+    nu, n, d = 3, 4, 2
+    mode = 3 if constraint == "ts0" else 4
+    lines = _run(harness, tmp_path, mode, gold, SOLVER["mle"], True, True)
+    for b in range(2):
+        p, y = torch.tensor(gold["params"][b]), torch.tensor(gold["y0"][b])
+        fn = problems.FIELDS["lotka_volterra"]
+        tc = problems.taylor_derivatives(fn, y, p, nu)
+        S = ssm.IsoSSM()
+        vf = lambda u, t, p=p: fn(u[0], p)  # noqa: E731
+        c = S.constraint_ode_ts1(vf) if constraint == "ts1" else S.constraint_ode_ts0(vf)
+        res = solvers.solve_adaptive_save_at(solvers.SolverMLE(solvers.StrategyFilter(), c), solvers.ErrorStateStd(c),
+                                             S.prior_wiener_integrated(tc), gold["save_at"], 1e-5, 1e-5, clip_dt=True,
+                                             dt0=0.1)
+        status, _ = (int(x) for x in lines[2 * b].split())
+        assert status == 0
+        vals = [float(x) for x in lines[2 * b + 1].split()]
+        gm = np.array(vals[3:3 + n * d]).reshape(n, d)
+        gc = np.array(vals[3 + n * d:]).reshape(n, n)
+        om, oc = res.u[-1].mean.numpy(), res.u[-1].cholesky.numpy()
+        assert float(np.abs(gm[0] - om[0]).max() / np.abs(om[0]).max()) <= 1e-9
+        for i in range(n):
+            assert float(np.abs(gm[i] - om[i]).max() / max(np.abs(om[i]).max(), 1e-300)) <= 1e-6, i
+        cg, co = gc @ gc.T, oc @ oc.T
+        assert float(np.abs(cg - co).max() / max(np.abs(co).max(), 1e-300)) <= 1e-6
+        assert abs(int(vals[1]) - res.num_steps[-1]) <= 1
