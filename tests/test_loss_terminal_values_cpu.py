@@ -10,7 +10,6 @@ the reference's ValueError (its test_lml_terminal_values.py checks the
 message).
 """
 
-import numpy as np
 import pytest
 import torch
 

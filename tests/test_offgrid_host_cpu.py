@@ -12,7 +12,6 @@ smoother in the isotropic and dense factorisations.
 
 import numpy as np
 import pytest
-import torch
 
 from oracle import solvers
 from tests import hostsim
