@@ -25,6 +25,14 @@ __all__ = [
     "Field",
     "jetexpand_ode_padded_scan",
     "jetexpand_ode_unroll",
+    "jetexpand_ode_via_jvp",
+    "jetexpand_ode_doubling_unroll",
+    "taylor_point_prior",
+    "taylor_point_maximum_a_posteriori",
+    "error_norm_scale_then_rms",
+    "error_norm_rms_then_scale",
+    "system_matrices_1d_iwp",
+    "preconditioner_taylor",
     "state_space_model_isotropic",
     "state_space_model_blockdiag",
     "state_space_model_dense",
@@ -133,6 +141,76 @@ def jetexpand_ode_unroll(*, num):
     return _JetExpand(num)
 
 
+def jetexpand_ode_via_jvp(*, num):
+    """Taylor coefficients by recursive forward-mode differentiation
+    (jet_expansion_algorithms.py:180-225): the same exact coefficients, here
+    computed by the solver kernels' jet recursion."""
+    return _JetExpand(num)
+
+
+def jetexpand_ode_doubling_unroll(*, num_doublings):
+    """Taylor coefficients by Newton's doubling (jet_expansion_algorithms.py:228-260):
+    2**num_doublings coefficients, i.e. 2**num_doublings - 1 derivatives, here
+    computed by the solver kernels' jet recursion."""
+    if num_doublings < 1:
+        raise ValueError("num_doublings must be positive")
+    return _JetExpand(2**num_doublings - 1)
+
+
+class taylor_point_prior:
+    """Linearise at the prior mean (taylor_points.py:150-156), the native TS1 point."""
+
+
+class taylor_point_maximum_a_posteriori:
+    """Linearise at the maximum-a-posteriori point (taylor_points.py:159-...);
+    not native: ``constraint_ode_ts1`` raises NotImplementedError for it."""
+
+    def __init__(self, nlstsq=None):
+        self.nlstsq = nlstsq
+
+
+def system_matrices_1d_iwp(num_derivatives):
+    """A = flip(Pascal) and Q = the lower square root of flip(Hilbert), with a
+    non-negative diagonal (utilities.py:57-71): the IWP's one-dimensional
+    transition matrix and noise factor at unit step, float64 on the host.
+    The kernels use the same matrices (A folded into the code as integer
+    binomials, Q computed on the host in long double)."""
+    import math
+
+    import decimal
+
+    n = num_derivatives + 1
+    A = torch.tensor([[float(math.comb(n - 1 - i, j - i)) if j >= i else 0.0 for j in range(n)] for i in range(n)],
+                     dtype=torch.float64)
+    # Cholesky factor of flip(Hilbert) in 40-digit decimal arithmetic (the
+    # matrix is ill-conditioned: a float64 factorisation loses ~4 digits)
+    with decimal.localcontext(decimal.Context(prec=40)):
+        one = decimal.Decimal(1)
+        H = [[one / (2 * num_derivatives + 1 - i - j) for j in range(n)] for i in range(n)]
+        L = [[decimal.Decimal(0)] * n for _ in range(n)]
+        for j in range(n):
+            L[j][j] = (H[j][j] - sum((L[j][k] * L[j][k] for k in range(j)), decimal.Decimal(0))).sqrt()
+            for i in range(j + 1, n):
+                L[i][j] = (H[i][j] - sum((L[i][k] * L[j][k] for k in range(j)), decimal.Decimal(0))) / L[j][j]
+        Q = torch.tensor([[float(x) for x in row] for row in L], dtype=torch.float64)
+    return A, Q
+
+
+def preconditioner_taylor(num_derivatives):
+    """The Taylor preconditioner (utilities.py:74-84): precon(dt) returns
+    p_i = dt^(nu - i) / (nu - i)! and its inverse, float64 on the host."""
+    import math
+
+    powers = torch.arange(num_derivatives, -1, -1, dtype=torch.float64)
+    scales = torch.tensor([float(math.factorial(int(k))) for k in powers], dtype=torch.float64)
+
+    def precon(dt):
+        dt = torch.as_tensor(dt, dtype=torch.float64)
+        return torch.pow(dt, powers) / scales, torch.pow(dt, -powers) * scales
+
+    return precon
+
+
 @dataclasses.dataclass(frozen=True)
 class Prior:
     """An integrated Wiener process prior (ssm_impl_*.py prior_wiener_integrated)."""
@@ -176,7 +254,7 @@ class _StateSpaceModel:
         along d (block-diagonal, ssm_impl_blockdiag.py:147-183), at the prior mean."""
         if not isinstance(ode, Field):
             raise TypeError(ode)
-        if taylor_point is not None:
+        if taylor_point is not None and not isinstance(taylor_point, taylor_point_prior):
             raise NotImplementedError("only the prior-mean Taylor point (taylor_point_prior) is native")
         return Constraint(self.name, "ts1", ode)
 
@@ -318,6 +396,28 @@ def solver_dynamic(*, strategy, constraint, constraint_init=None, re_linearize_a
 
 
 @dataclasses.dataclass(frozen=True)
+class error_norm_scale_then_rms:
+    """Error normalisation: scale by atol + rtol |reference|, then the RMS
+    (solvers.py:770-791).  The native default (with the 2-norm)."""
+
+    norm_order: Any = None
+
+
+@dataclasses.dataclass(frozen=True)
+class error_norm_rms_then_scale:
+    """Error normalisation: the RMS, then scale by atol + rtol RMS(reference)
+    (solvers.py:794-811).  Not native: the error estimators raise
+    NotImplementedError for it."""
+
+    norm_order: Any = None
+
+
+def _native_error_norm(error_norm):
+    """True when ``error_norm`` is the kernels' normalisation (the default)."""
+    return error_norm is None or (isinstance(error_norm, error_norm_scale_then_rms) and error_norm.norm_order is None)
+
+
+@dataclasses.dataclass(frozen=True)
 class error_residual_std:
     """Residual-std error estimate (solvers.py:850-996), cached linearisation."""
 
@@ -327,7 +427,7 @@ class error_residual_std:
     error_per_unit_step: bool = False
 
     def __post_init__(self):
-        if self.error_norm is not None or self.re_linearize_before_error or self.error_per_unit_step:
+        if not _native_error_norm(self.error_norm) or self.re_linearize_before_error or self.error_per_unit_step:
             raise NotImplementedError("only the default error_residual_std is native")
 
 
@@ -428,7 +528,7 @@ class error_state_std:
     error_per_unit_step: bool = False
 
     def __post_init__(self):
-        if (self.error_norm is not None or self.re_linearize_before_error or self.derivative_idx != 0
+        if (not _native_error_norm(self.error_norm) or self.re_linearize_before_error or self.derivative_idx != 0
                 or self.error_per_unit_step):
             raise NotImplementedError("only the default error_state_std is native")
 
