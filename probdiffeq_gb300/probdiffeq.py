@@ -162,7 +162,7 @@ class taylor_point_prior:
 
 
 class taylor_point_maximum_a_posteriori:
-    """Linearise at the maximum-a-posteriori point (taylor_points.py:159-180);
+    """Linearise at the maximum-a-posteriori point (taylor_points.py:159-175);
     not native: ``constraint_ode_ts1`` raises NotImplementedError for it."""
 
     def __init__(self, nlstsq=None):
