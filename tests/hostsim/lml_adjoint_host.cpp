@@ -1,10 +1,12 @@
-// Runs the float64 adjoint LML kernels on the CPU:
+// Runs the adjoint LML kernels on the CPU (float64; float32 bulk for
+// FitzHugh-Nagumo nu = 3):
 // the plan kernel's single thread, then lml_adj_fwd_kernel and
 // lml_adj_bwd_kernel for every sample as its own "thread" (they need no
 // cooperation between threads).  Buffers have the exact sizes the library
 // computes, so AddressSanitizer flags any access outside them.
 //
-// Input file (whitespace-separated): field nu B N save_every C average_pdfs,
+// Input file (whitespace-separated): precision (0 float32 bulk, 1 float64)
+// field nu B N save_every C average_pdfs,
 // then params (B x P), y0 (B x 2), data (K x 2), std (K), cotangent (B), dt,
 // Q1 ((nu + 1) x (nu + 1), row-major), K = N / save_every + 1; field 0 is
 // FitzHugh-Nagumo (P = 3), field 1 Lotka-Volterra (P = 4); nu is 2 or 3.
@@ -25,7 +27,7 @@ static bool read_all(FILE* in, std::vector<double>& v) {
   return true;
 }
 
-template <int NU, class F>
+template <typename T, int NU, class F>
 static int run(FILE* in, long long B, int N, int se, int C, int avg) {
   constexpr int P = F::P;
   constexpr int n = NU + 1;
@@ -35,13 +37,13 @@ static int run(FILE* in, long long B, int N, int se, int C, int avg) {
       !read_all(in, cot) || !read_all(in, dt) || !read_all(in, q1))
     return 2;
 
-  const int64_t plan_bytes = lml_plan_total_bytes(NU, N, se, 8);
+  const int64_t plan_bytes = lml_plan_total_bytes(NU, N, se, int(sizeof(T)));
   const LmlAdjLayout L(NU, 2, N, se, C);
   const int64_t res_elems = int64_t(B) * L.total;
   unsigned char* plan = static_cast<unsigned char*>(calloc(plan_bytes, 1));
-  double* res = static_cast<double*>(malloc(res_elems * 8));
+  T* res = static_cast<T*>(malloc(res_elems * sizeof(T)));
   // NaN everywhere: a residual read before it is written poisons the result
-  for (int64_t i = 0; i < res_elems; ++i) res[i] = __longlong_as_double(0x7ff8000000000001LL);
+  for (int64_t i = 0; i < res_elems; ++i) res[i] = T(__longlong_as_double(0x7ff8000000000001LL));
   std::vector<double> lml(B), grad(B * P), gy0(B * 2);
   std::vector<int32_t> status(B);
 
@@ -73,16 +75,16 @@ static int run(FILE* in, long long B, int N, int se, int C, int avg) {
   blockDim = {uint32_t(kLmlThreads), 1, 1};
   blockIdx = {0, 0, 0};
   threadIdx = {0, 0, 0};
-  lml_plan_kernel<double, NU>(a);
+  lml_plan_kernel<T, NU>(a);
   const long long padded = (B + kLmlThreads - 1) / kLmlThreads * kLmlThreads;  // the launch's grid
   for (int pass = 0; pass < 2; ++pass)
     for (long long t = 0; t < padded; ++t) {
       blockIdx = {uint32_t(t / kLmlThreads), 0, 0};
       threadIdx = {uint32_t(t % kLmlThreads), 0, 0};
       if (pass == 0)
-        lml_adj_fwd_kernel<double, NU, F>(aa);
+        lml_adj_fwd_kernel<T, NU, F>(aa);
       else
-        lml_adj_bwd_kernel<double, NU, F>(aa);
+        lml_adj_bwd_kernel<T, NU, F>(aa);
     }
   for (long long b = 0; b < B; ++b) {
     printf("%d %.17g", status[b], lml[b]);
@@ -99,13 +101,14 @@ int main(int argc, char** argv) {
   FILE* in = fopen(argv[1], "r");
   if (!in) return 2;
   long long B;
-  int field, nu, N, se, C, avg;
-  if (fscanf(in, "%d %d %lld %d %d %d %d", &field, &nu, &B, &N, &se, &C, &avg) != 7) return 2;
+  int prec, field, nu, N, se, C, avg;
+  if (fscanf(in, "%d %d %d %lld %d %d %d %d", &prec, &field, &nu, &B, &N, &se, &C, &avg) != 8) return 2;
   if (B < 1 || N < 1 || se < 1 || N % se != 0 || C < 1 || C > N) return 2;
   int rc = 2;
-  if (field == 0 && nu == 3) rc = run<3, FitzHughNagumo>(in, B, N, se, C, avg);
-  if (field == 0 && nu == 2) rc = run<2, FitzHughNagumo>(in, B, N, se, C, avg);
-  if (field == 1 && nu == 3) rc = run<3, LotkaVolterra>(in, B, N, se, C, avg);
+  if (prec == 1 && field == 0 && nu == 3) rc = run<double, 3, FitzHughNagumo>(in, B, N, se, C, avg);
+  if (prec == 1 && field == 0 && nu == 2) rc = run<double, 2, FitzHughNagumo>(in, B, N, se, C, avg);
+  if (prec == 1 && field == 1 && nu == 3) rc = run<double, 3, LotkaVolterra>(in, B, N, se, C, avg);
+  if (prec == 0 && field == 0 && nu == 3) rc = run<float, 3, FitzHughNagumo>(in, B, N, se, C, avg);
   fclose(in);
   return rc;
 }

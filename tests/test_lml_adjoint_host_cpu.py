@@ -36,9 +36,9 @@ def q1_iwp(nu):
 
 
 def run(harness, tmp_path, thetas, y0s, data, dt, num_steps, save_every, ckpt, average, cot, field=0, nu=3,
-        std=lml_problem.STD):
+        std=lml_problem.STD, precision=1):
     B = len(thetas)
-    head = [field, nu, B, num_steps, save_every, ckpt, int(average)]
+    head = [precision, field, nu, B, num_steps, save_every, ckpt, int(average)]
     body = np.concatenate([np.ravel(thetas), np.ravel(y0s), np.ravel(data), np.full(data.shape[0], std),
                            np.asarray(cot, dtype=float), [dt], np.ravel(q1_iwp(nu))])
     path = tmp_path / "input.txt"
@@ -121,3 +121,21 @@ def test_host_forward_mode_lml_matches_oracle(forward_harness, tmp_path, t1, ave
         assert out[b, 0] == 0
         assert abs(out[b, 1] - v) <= 1e-10 * abs(v), (out[b, 1], v)
         assert np.abs(out[b, 2:5] - g).max() <= 1e-10 * np.linalg.norm(g), (out[b, 2:5], g)
+
+
+def test_host_float32_adjoint_against_oracle(harness, tmp_path):
+    """The float32 adjoint (float32 bulk; log-pdf sums and the parameter
+    adjoint's totals in float64) on the 2000-step benchmark grid: value
+    within 1e-3 and gradients within 5e-2 of the float64 oracle, the bounds
+    of the GPU float32 tests."""
+    dt, save_every = 0.01, 10
+    num_steps, data = lml_problem.observations(t1=20.0, dt=dt, save_every=save_every)
+    thetas = lml_problem.theta_samples(2, seed=1)
+    y0s = np.tile(lml_problem.U0, (2, 1))
+    out = run(harness, tmp_path, thetas, y0s, data, dt, num_steps, save_every, 45, False, [1.0, 1.0], precision=0)
+    for b in range(2):
+        v, g, gy = lml_value_and_grads(thetas[b], y0s[b], data, dt, num_steps, save_every)
+        assert out[b, 0] == 0
+        assert abs(out[b, 1] - v) <= 1e-3 * abs(v), (out[b, 1], v)
+        assert np.abs(out[b, 2:5] - g).max() <= 5e-2 * np.linalg.norm(g), (out[b, 2:5], g)
+        assert np.abs(out[b, 5:7] - gy).max() <= 5e-2 * np.linalg.norm(gy), (out[b, 5:7], gy)
