@@ -1,14 +1,15 @@
 // Runs the float64 dense adaptive kernel (dense_adaptive_kernel, one thread
-// per instance) on the CPU for van der Pol with TS1 and the fixed-point
-// smoother, every instance as its own "thread", on buffers of exactly the
-// sizes the library uses (the per-instance backward conditionals in the
-// scratch included), so AddressSanitizer flags any access outside them.
+// per instance, TS1 with the Jacobian on dual numbers) on the CPU, every
+// instance as its own "thread", on buffers of exactly the sizes the library
+// uses (the fixed-point smoother's scratch of backward conditionals
+// included), so AddressSanitizer flags any access outside them.
 //
-// Input file (whitespace-separated): B S solver control clip_dt, then
-// atol rtol, save_at (B x S), params (B x 1), y0 (B x 2), dt0 (B),
-// Q1 (4 x 4, row-major); nu = 3.
+// Input file (whitespace-separated): field (0 Lotka-Volterra, 1 van der Pol)
+// nu (2 or 3) strategy (0 filter, 1 fixed-point smoother) B S solver control
+// clip_dt, then atol rtol, save_at (B x S), params (B x P), y0 (B x 2),
+// dt0 (B), Q1 ((nu + 1) x (nu + 1), row-major).
 // Output: per instance a line "status attempts", then per save point a line
-// "t num_steps u_mean[N] u_chol[N N]", N = 8.
+// "t num_steps u_mean[N] u_chol[N N]", N = (nu + 1) 2.
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -25,27 +26,18 @@ static bool read_all(FILE* in, std::vector<double>& v) {
   return true;
 }
 
-int main(int argc, char** argv) {
-  using F = VanDerPol;
-  constexpr int NU = 3;
+template <int NU, class F, bool FP>
+static int run(FILE* in, long long B, int S, int solver, int control, int clip_dt) {
   constexpr int n = NU + 1;
   constexpr int D = F::D;
   constexpr int N = n * D;
-  if (argc != 2) return 2;
-  FILE* in = fopen(argv[1], "r");
-  if (!in) return 2;
-  long long B;
-  int S, solver, control, clip_dt;
-  if (fscanf(in, "%lld %d %d %d %d", &B, &S, &solver, &control, &clip_dt) != 5) return 2;
-  if (B < 1 || S < 2) return 2;
   std::vector<double> tol(2), save_at(B * S), params(B * F::P), y0(B * D), dt0(B), q1(n * n);
   if (!read_all(in, tol) || !read_all(in, save_at) || !read_all(in, params) || !read_all(in, y0) ||
       !read_all(in, dt0) || !read_all(in, q1))
     return 2;
-  fclose(in);
   std::vector<double> u_mean(B * S * N), u_chol(B * S * N * N), scale(B * S), t(B * S);
   std::vector<int32_t> steps(B * S), attempts(B), status(B);
-  double* ws = static_cast<double*>(malloc(size_t(B) * (S - 1) * cond_floats<N>() * sizeof(double)));
+  std::vector<double> ws(FP ? size_t(B) * (S - 1) * cond_floats<N>() : 0);
 
   DenseArgs a;
   memset(&a, 0, sizeof(a));
@@ -56,7 +48,7 @@ int main(int argc, char** argv) {
   a.control = control;
   a.clip_dt = clip_dt;
   a.correct = 1;
-  a.fixedpoint = 1;
+  a.fixedpoint = FP ? 1 : 0;
   a.safety = 0.95;
   a.factor_min = 0.2;
   a.factor_max = 10.0;
@@ -80,7 +72,7 @@ int main(int argc, char** argv) {
   a.num_steps = steps.data();
   a.num_attempts = attempts.data();
   a.status = status.data();
-  a.workspace = ws;
+  a.workspace = FP ? ws.data() : nullptr;
 
   const int block = 32;
   blockDim = {uint32_t(block), 1, 1};
@@ -88,7 +80,7 @@ int main(int argc, char** argv) {
   for (long long g = 0; g < padded; ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
-    dense_adaptive_kernel<double, NU, F, true, true>(a);
+    dense_adaptive_kernel<double, NU, F, true, FP>(a);
   }
   for (long long b = 0; b < B; ++b) {
     printf("%d %d\n", status[b], attempts[b]);
@@ -100,6 +92,21 @@ int main(int argc, char** argv) {
       printf("\n");
     }
   }
-  free(ws);
   return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc != 2) return 2;
+  FILE* in = fopen(argv[1], "r");
+  if (!in) return 2;
+  long long B;
+  int field, nu, fp, S, solver, control, clip_dt;
+  if (fscanf(in, "%d %d %d %lld %d %d %d %d", &field, &nu, &fp, &B, &S, &solver, &control, &clip_dt) != 8) return 2;
+  if (B < 1 || S < 2) return 2;
+  int rc = 2;
+  if (field == 1 && nu == 3 && fp) rc = run<3, VanDerPol, true>(in, B, S, solver, control, clip_dt);
+  if (field == 0 && nu == 2 && fp) rc = run<2, LotkaVolterra, true>(in, B, S, solver, control, clip_dt);
+  if (field == 0 && nu == 2 && !fp) rc = run<2, LotkaVolterra, false>(in, B, S, solver, control, clip_dt);
+  fclose(in);
+  return rc;
 }

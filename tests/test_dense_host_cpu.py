@@ -36,7 +36,7 @@ def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path)
     gold = make_golden.load("vdp_dense.json")
     mus = gold["mu"]
     B, S, d, N = len(mus), len(gold["save_at"][0]), 2, 8
-    head = [B, S, 2, 0, 0]  # solver_dynamic, control_integral, interpolation (no clip_dt)
+    head = [1, 3, 1, B, S, 2, 0, 0]  # van der Pol, nu = 3, fixed point; solver_dynamic, control_integral, no clip_dt
     body = np.concatenate([[gold["atol"], gold["rtol"]], np.ravel(gold["save_at"]), mus,
                            np.tile(gold["y0"], B), np.full(B, gold["dt0"]), q1_iwp(3).ravel()])
     path = tmp_path / "input.txt"
@@ -59,3 +59,47 @@ def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path)
                 assert rel(gm[i * d:(i + 1) * d], om[i * d:(i + 1) * d]) <= 1e-5, (b, s, i)
             assert rel(gc @ gc.T, oc @ oc.T) <= 1e-5, (b, s)
             assert abs(steps - steps_o[s]) <= 1, (b, s, steps, steps_o[s])
+
+
+def _run_lv(harness, tmp_path, strategy, solver, save_at, tol):
+    head = [0, 2, 1 if strategy == "smoother" else 0, 1, len(save_at), solver, 0, 0]
+    body = np.concatenate([[tol, tol], save_at, [0.5, 0.05, 0.5, 0.05], [20.0, 20.0], [0.1], q1_iwp(2).ravel()])
+    path = tmp_path / f"input_{len(save_at)}.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lines = hostsim.run_harness(harness, path)
+    assert int(lines[0].split()[0]) == 0
+    return [np.array([float(x) for x in line.split()[2:]]) for line in lines[1:]]
+
+
+@pytest.mark.parametrize("solver", [0, 1, 2])
+@pytest.mark.parametrize("strategy", ["filter", "smoother"])
+def test_host_dense_kernel_behaviour_close_to_t1(harness, tmp_path, strategy, solver):
+    """The reference's test_dense_output/test_behaviour_close_to_t1.py:58-94
+    on the dense kernel: Lotka--Volterra, TS1, nu = 2, tol 1e-1, 30 save
+    points up to the second-to-last point of the oracle's save-every-step
+    grid; dropping the last save point leaves every other marginal unchanged
+    (the reference's float64 allclose: atol sqrt(eps), rtol 10 sqrt(eps))."""
+    import torch
+
+    from oracle import problems, solvers, ssm
+
+    S = ssm.DenseSSM()
+    p = torch.tensor([0.5, 0.05, 0.5, 0.05], dtype=torch.float64)
+    tc = problems.taylor_derivatives(problems.lotka_volterra, torch.tensor([20.0, 20.0], dtype=torch.float64), p, 2)
+    c = S.constraint_ode_ts1(lambda u, t: problems.lotka_volterra(u[0], p),
+                             lambda u, t: problems.jacobian(problems.lotka_volterra, u, p), 2)
+    cls = {0: solvers.SolverPlain, 1: solvers.SolverMLE, 2: solvers.SolverDynamic}[solver]
+    strat = solvers.StrategyFilter() if strategy == "filter" else solvers.StrategyFixedInterval()
+    every = solvers.solve_adaptive_save_every_step(cls(strat, c), solvers.ErrorResidualStd(c),
+                                                   S.prior_wiener_integrated(tc), 0.0, 2.0, 1e-1, 1e-1)
+    ts = np.linspace(float(every.t[0]), float(every.t[-2]), 30)
+    full = _run_lv(harness, tmp_path, strategy, solver, ts, 1e-1)
+    cut = _run_lv(harness, tmp_path, strategy, solver, ts[:-1], 1e-1)
+    assert len(full) == 30 and len(cut) == 29
+    tol = np.sqrt(np.finfo(np.float64).eps)
+    N = 6
+    for a, b in zip(full[:-1], cut):
+        ma, La = a[:N], a[N:].reshape(N, N)
+        mb, Lb = b[:N], b[N:].reshape(N, N)
+        assert np.allclose(ma, mb, atol=tol, rtol=10 * tol)
+        assert np.allclose(La @ La.T, Lb @ Lb.T, atol=tol, rtol=10 * tol)

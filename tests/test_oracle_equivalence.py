@@ -258,3 +258,31 @@ def test_ts1_differs_from_ts0_only_through_the_jacobian_term():
             0.0, 2.0, 1e-6, 1e-6))
     assert res[0].num_steps[-1] == res[1].num_steps[-1]
     assert allclose(res[0].u[-1].mean, res[1].u[-1].mean)
+
+
+@pytest.mark.parametrize("solver_name", ["none", "mle", "dynamic"])
+@pytest.mark.parametrize("strategy", ["filter", "smoother"])
+def test_behaviour_close_to_t1(strategy, solver_name):
+    """test_dense_output/test_behaviour_close_to_t1.py:58-94: dense TS1 on
+    Lotka--Volterra (nu = 2, tol 1e-1, 30 save points between t0 and the
+    second-to-last point of the save-every-step grid); solving with the last
+    save point removed leaves every other marginal unchanged -- for the
+    smoother this checks that marginals close to t1 are informed by the
+    overstepped state."""
+    cls = {"none": solvers.SolverPlain, "mle": solvers.SolverMLE, "dynamic": solvers.SolverDynamic}[solver_name]
+    S = make_ssm("dense")
+    tc = problems.taylor_derivatives(problems.lotka_volterra, torch.tensor([20.0, 20.0]), LV_P, 2)
+    prior = S.prior_wiener_integrated(tc)
+    c = S.constraint_ode_ts1(lv, lv_jac, 2)
+    every_strategy = solvers.StrategyFilter() if strategy == "filter" else solvers.StrategyFixedInterval()
+    at_strategy = solvers.StrategyFilter() if strategy == "filter" else solvers.StrategyFixedPoint()
+    every = solvers.solve_adaptive_save_every_step(cls(every_strategy, c), solvers.ErrorResidualStd(c), prior, 0.0, 2.0,
+                                                   1e-1, 1e-1)
+    ts = np.linspace(float(every.t[0]), float(every.t[-2]), 30)
+    full = solvers.solve_adaptive_save_at(cls(at_strategy, c), solvers.ErrorResidualStd(c), prior, ts, 1e-1, 1e-1)
+    cut = solvers.solve_adaptive_save_at(cls(at_strategy, c), solvers.ErrorResidualStd(c), prior, ts[:-1], 1e-1, 1e-1)
+    assert len(full.u) == 30 and len(cut.u) == 29
+    for a, b in zip(full.u[:-1], cut.u):
+        ma, Ca = a.to_multivariate_normal()
+        mb, Cb = b.to_multivariate_normal()
+        assert allclose(ma, mb) and allclose(Ca, Cb)
