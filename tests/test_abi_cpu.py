@@ -162,3 +162,28 @@ def test_lml_adjoint_arguments_are_checked_before_launch(lib):
     a.lml.num_instances = 0
     assert lib.pdq_lml_fwd(ctypes.byref(cfg), ctypes.byref(a), None, 0, None) == 0
     assert lib.pdq_lml_bwd(ctypes.byref(cfg), ctypes.byref(a), None, 0, None) == 0
+
+
+def test_sample_markov_arguments_are_checked_before_launch(lib):
+    """pdq_sample_markov: negative or empty sizes, factorisations without a
+    native sampler and missing buffers are rejected before any launch; an
+    empty batch launches nothing."""
+    from probdiffeq_gb300 import _native
+
+    assert lib.pdq_sample_markov(None, None) == 1
+    a = _native.PdqSampleArgs()
+    a.ssm, a.num_derivatives, a.ode_dim, a.num_points = 0, 2, 2, 5
+    a.num_instances, a.num_samples = 2, 3
+    assert lib.pdq_sample_markov(ctypes.byref(a), None) == 1  # buffers missing
+    a.num_samples = -1
+    assert lib.pdq_sample_markov(ctypes.byref(a), None) == 1
+    a.num_samples, a.num_points = 3, 0
+    assert lib.pdq_sample_markov(ctypes.byref(a), None) == 1
+    a.num_points, a.ssm = 5, 1
+    assert lib.pdq_sample_markov(ctypes.byref(a), None) == 2  # block-diagonal: no native sampler
+    a.ssm, a.num_derivatives = 0, 9
+    assert lib.pdq_sample_markov(ctypes.byref(a), None) == 2  # n beyond the isotropic kernel's bound
+    a.ssm, a.num_derivatives, a.ode_dim = 2, 3, 20
+    assert lib.pdq_sample_markov(ctypes.byref(a), None) == 2  # N = 80 beyond the dense bound
+    a.ode_dim, a.num_instances = 2, 0
+    assert lib.pdq_sample_markov(ctypes.byref(a), None) == 0
