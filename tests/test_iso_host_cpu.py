@@ -212,3 +212,41 @@ def test_host_iso_error_state_std_matches_oracle(harness, tmp_path, constraint):
         cg, co = gc @ gc.T, oc @ oc.T
         assert float(np.abs(cg - co).max() / max(np.abs(co).max(), 1e-300)) <= 1e-6
         assert abs(int(vals[1]) - res.num_steps[-1]) <= 1
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_host_headline_kernel_on_the_benchmark_distribution(harness, tmp_path, precision):
+    """The headline configuration on its own input distribution (32 of the
+    benchmark's Lotka--Volterra instances, t in [0, 50], nu = 4, MLE,
+    rtol = atol = 1e-6, clip_dt) against the float64 C port of the reference
+    algorithm (the CPU baseline): float64 -- terminal u within 1e-9 relative,
+    accepted steps within +-1, the output scale within 1e-6; float32 bulk --
+    u within 1e-3 relative (the full horizon accumulates the float32 rounding
+    of every step) and accepted steps within 10 %."""
+    import bench
+    from oracle.port import port
+
+    params, y0 = (x.numpy() for x in bench.lv_inputs(32, seed=0))
+    ref = port.solve_iso_terminal("lotka_volterra", params, y0, 4, "mle", atol=1e-6, rtol=1e-6, t0=0.0, t1=50.0,
+                                  threads=1)
+    nu, n, d, B = 4, 5, 2, 32
+    head = [precision, 0, nu, B, 2, SOLVER["mle"], 0, 1, 1]
+    body = np.concatenate([[1e-6, 1e-6], np.tile([0.0, 50.0], B), params.ravel(), y0.ravel(), np.full(B, 0.1),
+                           q1_iwp(nu).ravel()])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lines = hostsim.run_harness(harness, path)
+    assert len(lines) == 2 * B
+    for b in range(B):
+        status, _ = (int(x) for x in lines[2 * b].split())
+        assert status == 0
+        vals = [float(x) for x in lines[2 * b + 1].split()]
+        u = np.array(vals[3:3 + n * d]).reshape(n, d)[0]
+        ru = ref["mean"][b, 0]
+        err = float(np.abs(u - ru).max() / np.abs(ru).max())
+        steps, rsteps = int(vals[1]), int(ref["num_steps"][b])
+        if precision == 1:
+            assert err <= 1e-9 and abs(steps - rsteps) <= 1, (b, err, steps, rsteps)
+            assert abs(vals[2] - ref["output_scale"][b]) <= 1e-6 * abs(ref["output_scale"][b])
+        else:
+            assert err <= 1e-3 and abs(steps - rsteps) <= max(1, int(0.1 * rsteps)), (b, err, steps, rsteps)
