@@ -335,7 +335,11 @@ pdq_status pdq_sample_markov(const pdq_sample_args* args, void* stream);
  * NotImplementedError).  A query on a grid point returns that point's
  * marginal; one outside [t_grid[0], t_grid[S-1]] (or NaN) returns NaN.
  * Float64; isotropic (nu 1..5, d <= 64) and dense (nu 2..3, d = 2).  Device
- * pointers; one thread per (instance, query). */
+ * pointers; one thread per (instance, query).  A block-diagonal solution is
+ * d independent one-dimensional models with per-dimension output scales:
+ * pass it as PDQ_SSM_ISOTROPIC with ode_dim 1 and B * d instances (instance
+ * b * d + j = dimension j of instance b, its mean (S, n, 1), factor
+ * (S, n, n) and output scale (S) taken from that dimension). */
 typedef struct pdq_offgrid_args {
   int32_t ssm;              /* PDQ_SSM_ISOTROPIC or PDQ_SSM_DENSE */
   int32_t strategy;         /* PDQ_STRATEGY_FILTER or PDQ_STRATEGY_FIXEDINTERVAL */

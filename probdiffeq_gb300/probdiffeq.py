@@ -343,6 +343,12 @@ class _Solver:
         returns its marginal and a time outside the span NaN).  Returns an
         ``ivpsolve.Normal`` with a query axis after the batch axis (none for a
         scalar ``t``).
+
+        Block-diagonal solutions (means (B, S, d, n), factors (B, S, d, n, n),
+        output scales (B, S, d)) are d independent one-dimensional isotropic
+        models (ssm_impl_blockdiag.py:406-432 transitions each dimension with
+        its own scale), so they run on the isotropic kernel as B * d
+        instances of dimension 1.
         """
         import torch
 
@@ -352,8 +358,6 @@ class _Solver:
         if not self.is_suitable_for_offgrid_marginals:
             raise NotImplementedError
         ssm = self.constraint.ssm
-        if ssm == "blockdiag":
-            raise NotImplementedError("off-grid marginals are native for the isotropic and dense factorisations")
         post = solution.posterior or {}
         if self.strategy.name == "fixedinterval" and "filter_mean" not in post:
             raise ValueError("off-grid marginals of a smoother need its filtering marginals: "
@@ -364,13 +368,49 @@ class _Solver:
         scalar = tq.ndim == 0
         tq = tq.reshape(1, -1).expand(B, -1) if tq.ndim <= 1 else tq
         d = solution.ode_dim
-        n = solution.u.mean_flat.shape[-2] if ssm == "isotropic" else solution.u.mean_flat.shape[-1] // d
-        mean, chol = _native.offgrid_marginals(
-            ssm, self.strategy.name, n - 1, d, grid, solution.u.mean_flat, solution.u.cholesky_flat,
-            solution.output_scale, tq, post.get("filter_mean"), post.get("filter_chol"), stream=stream)
+        if ssm == "blockdiag":
+            mean, chol = _blockdiag_offgrid(self.strategy.name, grid, solution, post, tq, stream)
+        else:
+            n = solution.u.mean_flat.shape[-2] if ssm == "isotropic" else solution.u.mean_flat.shape[-1] // d
+            mean, chol = _native.offgrid_marginals(
+                ssm, self.strategy.name, n - 1, d, grid, solution.u.mean_flat, solution.u.cholesky_flat,
+                solution.output_scale, tq, post.get("filter_mean"), post.get("filter_chol"), stream=stream)
         if scalar:
             mean, chol = mean[:, 0], chol[:, 0]
         return Normal(mean, chol, ssm)
+
+
+def _blockdiag_offgrid(strategy, grid, solution, post, tq, stream):
+    """Off-grid marginals of a block-diagonal grid solution through the
+    isotropic kernel: dimension j of instance b becomes instance b * d + j
+    with ode_dim 1, the grid and query times repeated per dimension, the
+    output scale of that dimension as its scalar scale.  Returns means
+    (B, Q, d, n) and factors (B, Q, d, n, n)."""
+    from . import _native
+
+    B, S = grid.shape
+    um = solution.u.mean_flat.reshape(B, S, *solution.u.mean_flat.shape[-2:])
+    d, n = um.shape[-2:]
+    if solution.output_scale.shape[-1] != d:
+        raise ValueError("The output-scale has the wrong shape.")
+
+    def per_dim_mean(m):  # (B, S, d, n) -> (B * d, S, n, 1)
+        return m.reshape(B, S, d, n).permute(0, 2, 1, 3).reshape(B * d, S, n, 1)
+
+    def per_dim_chol(c):  # (B, S, d, n, n) -> (B * d, S, n, n)
+        return c.reshape(B, S, d, n, n).permute(0, 2, 1, 3, 4).reshape(B * d, S, n, n)
+
+    fm, fc = post.get("filter_mean"), post.get("filter_chol")
+    mean, chol = _native.offgrid_marginals(
+        "isotropic", strategy, n - 1, 1, grid.repeat_interleave(d, dim=0), per_dim_mean(um),
+        per_dim_chol(solution.u.cholesky_flat),
+        solution.output_scale.reshape(B, S, d).permute(0, 2, 1).reshape(B * d, S),
+        tq.repeat_interleave(d, dim=0), None if fm is None else per_dim_mean(fm),
+        None if fc is None else per_dim_chol(fc), stream=stream)
+    Q = tq.shape[1]
+    mean = mean.reshape(B, d, Q, n).permute(0, 2, 1, 3).contiguous()
+    chol = chol.reshape(B, d, Q, n, n).permute(0, 2, 1, 3, 4).contiguous()
+    return mean, chol
 
 
 def solver(*, strategy, constraint, constraint_init=None):

@@ -4,9 +4,10 @@
 // AddressSanitizer flags any access outside them.
 //
 // Input file (whitespace-separated): ssm (0 isotropic, 2 dense) strategy
-// (0 filter, 2 fixed-interval) nu B S Q, then t (B x S), u_mean, u_chol,
+// (0 filter, 2 fixed-interval) nu B S Q d, then t (B x S), u_mean, u_chol,
 // output_scale (B x S), t_query (B x Q), filter_mean and filter_chol
-// (fixed-interval only), Q1 ((nu + 1) x (nu + 1), row-major); d = 2.
+// (fixed-interval only), Q1 ((nu + 1) x (nu + 1), row-major).  d is the
+// ODE dimension: 1 to 8 for the isotropic kernel, 2 for the dense one.
 // Output: one line per query: mean (flat) chol (flat).
 #include <cstdio>
 #include <cstdlib>
@@ -26,11 +27,12 @@ int main(int argc, char** argv) {
   if (argc != 2) return 2;
   FILE* in = fopen(argv[1], "r");
   if (!in) return 2;
-  int ssm, strategy, nu, S, Q;
+  int ssm, strategy, nu, S, Q, d;
   long long B;
-  if (fscanf(in, "%d %d %d %lld %d %d", &ssm, &strategy, &nu, &B, &S, &Q) != 6) return 2;
+  if (fscanf(in, "%d %d %d %lld %d %d %d", &ssm, &strategy, &nu, &B, &S, &Q, &d) != 7) return 2;
   if (!(nu == 2 || nu == 3) || (ssm != 0 && ssm != 2) || B < 1 || S < 2 || Q < 1) return 2;
-  const int d = 2, n = nu + 1, N = n * d;
+  if (ssm == 0 ? (d < 1 || d > 8) : d != 2) return 2;
+  const int n = nu + 1, N = n * d;
   const int mean_sz = ssm == 0 ? n * d : N, chol_sz = ssm == 0 ? n * n : N * N;
   const bool fi = strategy == 2;
   std::vector<double> t(B * S), um(B * S * mean_sz), uc(B * S * chol_sz), scale(B * S), tq(B * Q);

@@ -139,3 +139,32 @@ def test_offgrid_marginals_errors():
     sol = ivpsolve.solve_fixed_grid(solver=fi, precision="float64")(iwp, grid=grid, posterior=False)
     with pytest.raises(ValueError, match="filtering marginals"):
         fi.offgrid_marginals(0.3, solution=sol)
+
+
+@pytest.mark.parametrize("strategy", ["filter", "smoother"])
+def test_blockdiag_offgrid_marginals_match_oracle(strategy):
+    """Block-diagonal grid solutions (the oracle's, for two initial values,
+    moved to the device) through the isotropic kernel as B * d instances of
+    dimension 1, against the oracle's block-diagonal off-grid marginals."""
+    from tests.test_offgrid_blockdiag_cpu import NU, Y0S, api_solution, oracle_grid
+
+    grid = np.linspace(0.0, 2.0, 9)
+    queries = np.array([0.1, 0.6, 1.3, 1.9])
+    oracles = [oracle_grid(strategy, "dynamic", grid, y0) for y0 in Y0S]
+    sol = api_solution([res for _, res, _ in oracles], strategy, grid)
+    sol.t, sol.output_scale = sol.t.cuda(), sol.output_scale.cuda()
+    sol.u = ivpsolve.Normal(sol.u.mean_flat.cuda(), sol.u.cholesky_flat.cuda(), "blockdiag")
+    if sol.posterior is not None:
+        sol.posterior = {k: v.cuda() for k, v in sol.posterior.items()}
+    S_ = probdiffeq.state_space_model_blockdiag()
+    strat = probdiffeq.strategy_filter() if strategy == "filter" else probdiffeq.strategy_smoother_fixedinterval()
+    solver = probdiffeq.solver_dynamic(strategy=strat, constraint=S_.constraint_ode_ts1(probdiffeq.ode("lotka_volterra", LV)))
+    out = solver.offgrid_marginals(torch.tensor(queries), solution=sol)
+    torch.cuda.synchronize()
+    assert tuple(out.mean_flat.shape) == (len(Y0S), len(queries), 2, NU + 1)
+    for b, (o_solver, res, o_prior) in enumerate(oracles):
+        for q, t in enumerate(queries):
+            o = solvers.offgrid_marginals(o_solver, float(t), res, o_prior)
+            L = out.cholesky_flat[b, q].cpu()
+            assert rel(out.mean_flat[b, q].cpu(), o.mean) < 1e-9, (b, q)
+            assert rel(L @ L.transpose(-1, -2), o.cholesky @ o.cholesky.transpose(-1, -2)) < 1e-7, (b, q)

@@ -57,7 +57,7 @@ def test_host_offgrid_kernels_match_oracle(harness, tmp_path, kind, strategy, so
         parts += [np.concatenate([m.mean.reshape(-1).numpy() for m in filt]),
                   np.concatenate([m.cholesky.reshape(-1).numpy() for m in filt])]
     parts.append(q1_iwp(nu).ravel())
-    head = [0 if kind == "isotropic" else 2, 0 if strategy == "filter" else 2, nu, 1, S, Q]
+    head = [0 if kind == "isotropic" else 2, 0 if strategy == "filter" else 2, nu, 1, S, Q, 2]
     path = tmp_path / "input.txt"
     path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in np.concatenate(parts)))
     lines = hostsim.run_harness(harness, path)
