@@ -161,3 +161,23 @@ def test_blockdiag_offgrid_checks_the_output_scale_shape():
                                        constraint=S_.constraint_ode_ts1(probdiffeq.ode("lotka_volterra", LV_P)))
     with pytest.raises(ValueError, match="wrong shape"):
         solver.offgrid_marginals(0.5, solution=sol)
+
+
+def test_blockdiag_offgrid_per_instance_queries(harness, tmp_path, monkeypatch):
+    """(B, Q) query times that differ between instances, on a uniform grid:
+    each instance's dimensions see that instance's queries."""
+    grid = np.linspace(0.0, 2.0, 9)
+    tq = torch.tensor([[0.1, 0.6, 1.9], [0.4, 1.1, 1.6]], dtype=torch.float64)
+    oracles = [oracle_grid("filter", "mle", grid, y0) for y0 in Y0S]
+    sol = api_solution([res for _, res, _ in oracles], "filter", grid)
+    monkeypatch.setattr(_native, "offgrid_marginals", host_offgrid(harness, tmp_path))
+    S_ = probdiffeq.state_space_model_blockdiag()
+    solver = probdiffeq.solver_mle(strategy=probdiffeq.strategy_filter(),
+                                   constraint=S_.constraint_ode_ts1(probdiffeq.ode("lotka_volterra", LV_P)))
+    out = solver.offgrid_marginals(tq, solution=sol)
+    for b, (o_solver, res, o_prior) in enumerate(oracles):
+        for q in range(tq.shape[1]):
+            o = solvers.offgrid_marginals(o_solver, float(tq[b, q]), res, o_prior)
+            L = out.cholesky_flat[b, q]
+            assert rel(out.mean_flat[b, q], o.mean) < 1e-9, (b, q)
+            assert rel(L @ L.transpose(-1, -2), o.cholesky @ o.cholesky.transpose(-1, -2)) < 1e-7, (b, q)
