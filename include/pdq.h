@@ -278,8 +278,9 @@ pdq_status pdq_lml_bwd(const pdq_config* config, const pdq_lml_adjoint_args* arg
 #define PDQ_LML_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 
 /* pdq_lml_fixed_grid without any allocation, for callers that cannot call
- * cudaMalloc (code running under stream capture, plugin hosts that pass only
- * input and output buffers, allocation-free loops).  No counterpart in the
+ * cudaMalloc (plugin hosts that pass only input and output buffers, such as
+ * custom-call interfaces without a scratch operand, and loops whose
+ * allocation policy forbids it).  No counterpart in the
  * reference: it is an addition of this library.  The scratch is a 32 MiB
  * array inside the library (held on every GPU that loads it, until exit);
  * problems whose scratch (pdq_lml_workspace_size) exceeds

@@ -1,9 +1,8 @@
 // Allocation-free variant of pdq_lml_fixed_grid.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA stream is
-// being captured into a graph, plugin hosts that only hand over the input and
-// output buffers of a call (a custom-call interface without a scratch
-// operand), or latency-critical loops that forbid allocation.  This entry
+// Some callers cannot call cudaMalloc: plugin hosts that only hand over the
+// input and output buffers of a call (a custom-call interface without a
+// scratch operand), or latency-critical loops that forbid allocation.  This entry
 // point serves them by using a scratch array that lives in the library
 // itself: a file-scope __device__ array of PDQ_LML_STATIC_SCRATCH_BYTES
 // (32 MiB).  Every GPU on which the library is loaded holds the array until

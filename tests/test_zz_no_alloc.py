@@ -1,8 +1,8 @@
 """The allocation-free LML entry point (pdq_lml_fixed_grid_static).
 
-It serves callers that cannot allocate device memory (stream capture, plugin
-hosts that pass only input/output buffers): its scratch is an array inside
-the library.  Called through the C ABI, twice in a row, it must reproduce the
+It serves callers that cannot allocate device memory (plugin hosts that pass
+only input/output buffers, loops whose allocation policy forbids it): its
+scratch is an array inside the library.  Called through the C ABI, twice in a row, it must reproduce the
 allocating entry point pdq_lml_fixed_grid within the LML tests' float64
 tolerance (value 1e-9 relative, gradient 1e-6 relative to its norm).  This
 file is collected last so a run that stops at the first failure has run
