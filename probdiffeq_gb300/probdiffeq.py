@@ -47,6 +47,9 @@ __all__ = [
     "jacobian_materialize",
     "loss_lml_timeseries",
     "loss_lml_terminal_values",
+    "ProbabilisticSolver",
+    "ProbabilisticSolution",
+    "StateSpaceModel",
 ]
 
 _FIELD_DIMS = {"lotka_volterra": 2, "van_der_pol": 2, "fitzhugh_nagumo": 2, "burgers": None}
@@ -411,6 +414,20 @@ def _blockdiag_offgrid(strategy, grid, solution, post, tq, stream):
     mean = mean.reshape(B, d, Q, n).permute(0, 2, 1, 3).contiguous()
     chol = chol.reshape(B, d, Q, n, n).permute(0, 2, 1, 3, 4).contiguous()
     return mean, chol
+
+
+ProbabilisticSolver = _Solver  # the type behind solver / solver_mle / solver_dynamic (solvers.py:72-147)
+StateSpaceModel = _StateSpaceModel  # the type of the state_space_model_* factories (ssm_impl_api.py:300-587)
+
+
+def __getattr__(name):
+    """``ProbabilisticSolution`` (solvers.py:33-69) is ``ivpsolve.Solution``,
+    imported on first use (ivpsolve imports this module)."""
+    if name == "ProbabilisticSolution":
+        from .ivpsolve import Solution
+
+        return Solution
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")
 
 
 def solver(*, strategy, constraint, constraint_init=None):

@@ -77,3 +77,20 @@ def test_taylor_mode_constructors_describe_the_same_coefficients():
     assert torch.equal(a.y0, b.y0) and b.field is vf
     with pytest.raises(ValueError):
         probdiffeq.jetexpand_ode_doubling_unroll(num_doublings=0)
+
+
+def test_reference_type_names():
+    """The reference's public type names (solvers.py:35, 72; ssm_impl_api.py:300)
+    name the mirror's types, so annotations and isinstance checks carry over."""
+    from probdiffeq_gb300 import ivpsolve, probdiffeq
+
+    assert probdiffeq.ProbabilisticSolution is ivpsolve.Solution
+    ts0 = probdiffeq.state_space_model_isotropic().constraint_ode_ts0(
+        probdiffeq.ode("lotka_volterra", [0.5, 0.05, 0.5, 0.05]))
+    assert isinstance(probdiffeq.solver_mle(strategy=probdiffeq.strategy_filter(), constraint=ts0),
+                      probdiffeq.ProbabilisticSolver)
+    for ssm in (probdiffeq.state_space_model_isotropic(), probdiffeq.state_space_model_blockdiag(),
+                probdiffeq.state_space_model_dense()):
+        assert isinstance(ssm, probdiffeq.StateSpaceModel)
+    with pytest.raises(AttributeError):
+        probdiffeq.no_such_name
