@@ -49,15 +49,16 @@ cudaError_t launch_iso_tangents(const IsoArgs& a, cudaStream_t stream, int block
   return cudaGetLastError();
 }
 
-// The fixed-point smoother and TS1 / error_state_std take the general
-// instantiation; the filter with TS0 and error_residual_std the lean one.
+// The fixed-point smoother, TS1, error_state_std and a damped update take
+// the general instantiation; the filter with undamped TS0 and
+// error_residual_std the lean one (whose update is the single-QR array form).
 template <typename T, int NU, class F, bool FP>
 cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
   if constexpr (!FP) {
     if (a.tangents) return interp ? launch_iso_tangents<T, NU, F, true>(a, stream, block)
                                   : launch_iso_tangents<T, NU, F, false>(a, stream, block);
   }
-  if (FP || a.ts1 || a.state_error)
+  if (FP || a.ts1 || a.state_error || a.damp != 0.0)
     return interp ? launch_iso_kernel<T, NU, F, true, FP, true>(a, stream, block)
                   : launch_iso_kernel<T, NU, F, false, FP, true>(a, stream, block);
   return interp ? launch_iso_kernel<T, NU, F, true, FP, FP>(a, stream, block)

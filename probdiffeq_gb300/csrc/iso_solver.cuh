@@ -83,15 +83,23 @@ PDQ_D T cst(double d, float f) {
 }
 
 // Preconditioner p_i = h^(NU-i)/(NU-i)!, p_inv_i = 1/p_i (utilities.py:74-84).
+// The powers by repeated squaring, so the chain from h is ~log2(NU) products
+// (it starts every attempt's dependency chain).
 template <typename T, int NU>
 PDQ_D void precon(T h, T (&p)[NU + 1], T (&pinv)[NU + 1]) {
   const T hinv = fast_rcp(h);
-  p[NU] = T(1);
-  pinv[NU] = T(1);
+  T hp[NU + 1], hm[NU + 1];
+  hp[0] = T(1);
+  hm[0] = T(1);
 #pragma unroll
-  for (int i = NU - 1; i >= 0; --i) {
-    p[i] = p[i + 1] * h * T(1.0 / (NU - i));
-    pinv[i] = pinv[i + 1] * hinv * T(NU - i);
+  for (int k = 1; k <= NU; ++k) {
+    hp[k] = (k == 1) ? h : ((k & 1) ? hp[k - 1] * h : hp[k / 2] * hp[k / 2]);
+    hm[k] = (k == 1) ? hinv : ((k & 1) ? hm[k - 1] * hinv : hm[k / 2] * hm[k / 2]);
+  }
+#pragma unroll
+  for (int i = 0; i <= NU; ++i) {
+    p[i] = hp[NU - i] * T(1.0 / factorial(NU - i));
+    pinv[i] = hm[NU - i] * T(factorial(NU - i));
   }
 }
 
@@ -136,6 +144,86 @@ PDQ_D void iso_predict_mean(const T (&m)[NU + 1][D], const T (&p)[NU + 1], const
       for (int k = i; k < n; ++k) acc += T(iwp_a<NU>(i, k)) * x[k][j];
       mp[i][j] = p[i] * acc;
     }
+}
+
+// The same predict in increment form, mp_i = m_i + incr_i with
+//   incr_i = p_i sum_{k>i} A_ik pinv_k m_k
+// (A_ii = 1, so p_i pinv_i m_i = m_i in exact arithmetic).  For the step
+// sizes of an adaptive solve the increment is small against m_i, so formed
+// in the bulk type and added to a wide m_i it leaves the sum accurate to the
+// wide type; the product form rounds m_i itself at every step.
+template <typename T, int NU, int D>
+PDQ_D void iso_mean_increment(const T (&m)[NU + 1][D], const T (&p)[NU + 1], const T (&pinv)[NU + 1],
+                              T (&incr)[NU + 1][D]) {
+  constexpr int n = NU + 1;
+  T x[n][D];
+#pragma unroll
+  for (int i = 1; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) x[i][j] = pinv[i] * m[i][j];
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = i + 1; k < n; ++k) acc += T(iwp_a<NU>(i, k)) * x[k][j];
+      incr[i][j] = p[i] * acc;
+    }
+}
+
+// The isotropic mean is carried with its solution and first-derivative rows
+// wide: the bulk-type rows m (all n) and, for float, the low parts lo of rows
+// 0 and 1 (a float pair per entry).  The TS0 residual u' - f(u) reads exactly
+// these two rows, so they carry the accuracy the error estimate needs; for
+// double the low parts stay zero and cost nothing.
+template <typename T>
+PDQ_D Wide<T> wide_pair(T hi, T lo) {
+  if constexpr (sizeof(T) == sizeof(float)) {
+    return FloatPair(hi, lo);
+  } else {
+    return hi;  // the low parts of double means are zero
+  }
+}
+
+// out = m + d with the wide rows (0, 1) summed in the wide type, rows >= 2 in T
+// (out may alias m).
+template <typename T, int NU, int D>
+PDQ_D void iso_mean_add(const T (&m)[NU + 1][D], const T (&lo)[2][D], const T (&d)[NU + 1][D],
+                        T (&out)[NU + 1][D], T (&out_lo)[2][D]) {
+  constexpr int n = NU + 1;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      if constexpr (sizeof(T) == sizeof(float)) {
+        const FloatPair s = FloatPair(m[i][j], lo[i][j]) + d[i][j];
+        out[i][j] = s.hi;
+        out_lo[i][j] = s.lo;
+      } else {
+        out[i][j] = m[i][j] + d[i][j];
+        out_lo[i][j] = T(0);
+      }
+    }
+#pragma unroll
+  for (int i = 2; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) out[i][j] = m[i][j] + d[i][j];
+}
+
+// TS0 residual mobs_j = mp_1j - f_j(mp_0) of the extrapolated mean (mp, lo),
+// with the field evaluated in the wide type at the wide solution row and the
+// wide parameters, rounded once to T.
+template <class F, typename T, int NU>
+PDQ_D void iso_residual(const T (&mp)[NU + 1][F::D], const T (&lo)[2][F::D], const Wide<T> (&pw)[F::P],
+                        T (&mobs)[F::D]) {
+  constexpr int D = F::D;
+  Wide<T> u[D], f[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) u[j] = wide_pair(mp[0][j], lo[0][j]);
+  F::eval(u, pw, f);
+#pragma unroll
+  for (int j = 0; j < D; ++j) mobs[j] = T(wide_hi(wide_pair(mp[1][j], lo[1][j]) - f[j]));
 }
 
 // IWP predict of the isotropic Cholesky factor (marginalise, ssm_impl_isotropic.py:81-89):
@@ -265,6 +353,203 @@ PDQ_D void iso_predict_chol(const Q (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1][NU
     for (int j = 0; j < n; ++j) Lp[i][j] = (j <= i) ? dev_abs(p[i]) * X[j][i] : T(0);
 }
 
+// Branch-free twin of iso_predict_chol: the same unnormalised reflectors
+// without the per-column range test, so the predict is straight-line code the
+// compiler interleaves with the rest of the attempt.  Returns false when some
+// column's sum of squares left [1e-30, 1e36]; the results are then unusable
+// and the caller reruns the attempt with iso_predict_chol.
+template <typename T, int NU, typename Q>
+PDQ_D bool iso_predict_chol_fast(const Q (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
+                                 const T (&pinv)[NU + 1], T scale_q, T (&Lp)[NU + 1][NU + 1]) {
+  constexpr int n = NU + 1;
+  T X[n][n];
+  T U[n][n];
+  T PL[n][n];
+#pragma unroll
+  for (int k = 0; k < n; ++k)
+#pragma unroll
+    for (int r = 0; r < n; ++r) PL[k][r] = pinv[k] * L[k][r];
+#pragma unroll
+  for (int c = 0; c < n; ++c)
+#pragma unroll
+    for (int r = 0; r < n; ++r) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = (c > r ? c : r); k < n; ++k) acc += T(iwp_a<NU>(c, k)) * PL[k][r];
+      X[r][c] = acc;
+      U[r][c] = (r <= c) ? scale_q * T(q1[c][r]) : T(0);
+    }
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < n; ++c) {
+    T e0 = T(0), e1 = T(0);
+#pragma unroll
+    for (int r = c + 1; r < n; ++r) {
+      if ((r & 1) == 0) e0 += X[r][c] * X[r][c];
+      else e1 += X[r][c] * X[r][c];
+    }
+#pragma unroll
+    for (int i = 0; i <= c; ++i) {
+      if ((i & 1) == 0) e0 += U[i][c] * U[i][c];
+      else e1 += U[i][c] * U[i][c];
+    }
+    const T alpha = X[c][c];
+    const T nrm2 = alpha * alpha + (e0 + e1);
+    ok = ok && !norm2_out_of_range(nrm2);
+    const T nrm = fast_sqrt(nrm2);
+    const T s = dev_abs(alpha) + nrm;
+    const T v0 = alpha >= T(0) ? s : -s;
+    const T g = fast_rcp(nrm * s);
+#pragma unroll
+    for (int j = c + 1; j < n; ++j) {
+      T d0 = T(0), d1 = T(0);
+#pragma unroll
+      for (int r = c + 1; r < n; ++r) {
+        if ((r & 1) == 0) d0 += X[r][c] * X[r][j];
+        else d1 += X[r][c] * X[r][j];
+      }
+#pragma unroll
+      for (int i = 0; i <= c; ++i) {
+        if ((i & 1) == 0) d0 += U[i][c] * U[i][j];
+        else d1 += U[i][c] * U[i][j];
+      }
+      const T w = (v0 * X[c][j] + (d0 + d1)) * g;
+      X[c][j] -= w * v0;
+#pragma unroll
+      for (int r = c + 1; r < n; ++r) X[r][j] -= w * X[r][c];
+#pragma unroll
+      for (int i = 0; i <= c; ++i) U[i][j] -= w * U[i][c];
+    }
+    X[c][c] = alpha >= T(0) ? -nrm : nrm;
+  }
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < n; ++j) Lp[i][j] = (j <= i) ? dev_abs(p[i]) * X[j][i] : T(0);
+  return ok;
+}
+
+// One unnormalised Householder reflector of a register matrix with a
+// compile-time sparsity pattern: column COL, pivot row PIV, the column's
+// other nonzero rows in the bit mask BELOW, applied to the columns in the
+// bit mask COLS (rows outside PIV and BELOW are not touched).  Branch-free;
+// clears ok when the column's sum of squares leaves [1e-30, 1e36].
+template <typename T, int R, int C, int COL, int PIV, unsigned BELOW, unsigned COLS>
+PDQ_D void hh_step(T (&Z)[R][C], bool& ok) {
+  T e0 = T(0), e1 = T(0);
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    if ((BELOW >> r) & 1u) {
+      if (r & 1) e1 += Z[r][COL] * Z[r][COL];
+      else e0 += Z[r][COL] * Z[r][COL];
+    }
+  }
+  const T alpha = Z[PIV][COL];
+  const T nrm2 = alpha * alpha + (e0 + e1);
+  ok = ok && !norm2_out_of_range(nrm2);
+  const T nrm = fast_sqrt(nrm2);
+  const T s = dev_abs(alpha) + nrm;
+  const T v0 = alpha >= T(0) ? s : -s;
+  const T g = fast_rcp(nrm * s);
+#pragma unroll
+  for (int j = 0; j < C; ++j) {
+    if ((COLS >> j) & 1u) {
+      T d0 = T(0), d1 = T(0);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if ((BELOW >> r) & 1u) {
+          if (r & 1) d1 += Z[r][COL] * Z[r][j];
+          else d0 += Z[r][COL] * Z[r][j];
+        }
+      }
+      const T w = (v0 * Z[PIV][j] + (d0 + d1)) * g;
+      Z[PIV][j] -= w * v0;
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if ((BELOW >> r) & 1u) Z[r][j] -= w * Z[r][COL];
+    }
+  }
+  Z[PIV][COL] = alpha >= T(0) ? -nrm : nrm;
+}
+
+// Reflectors of the columns c = 3..n of the joint predict-update matrix
+// (below): pivot row c (X row c, or U row 0 for c = n), the nonzeros below
+// it X rows c+1..n-1 and U rows 0..c-1, applied to columns c+1..n.
+template <typename T, int n, int c>
+PDQ_D void joint_tail(T (&Z)[2 * n][n + 1], bool& ok) {
+  if constexpr (c <= n) {
+    constexpr unsigned x_below = ((1u << n) - 1u) & ~((1u << (c + 1)) - 1u);
+    constexpr unsigned u_rows = ((1u << c) - 1u) << n;
+    constexpr unsigned below = (c < n) ? (x_below | u_rows) : (u_rows & ~(1u << n));
+    constexpr unsigned cols = ((1u << (n + 1)) - 1u) & ~((1u << (c + 1)) - 1u);
+    hh_step<T, 2 * n, n + 1, c, c, below, cols>(Z, ok);
+    joint_tail<T, n, c + 1>(Z, ok);
+  }
+}
+
+// IWP predict and TS0 update (H = e_1, damp = 0) in one orthogonal
+// triangularisation -- the array form of the square-root Kalman filter.
+// With the preconditioned stacked factor Z = [X; U] (2n x n, X = (A pinv L)^T,
+// U = s sqrt|h| Q1^T upper triangular, as in iso_predict_chol), the
+// reference's two QRs (marginalise, then revert_conditional on
+// [(H Lp)^T, Lp^T] = Q^T [Z e_1, Z] diag(|p_1|, |p|)) equal one QR of [Z e_1, Z]:
+//   R' = qr_r([Z e_1, Z]) = [[r_y, r12], [0, R22]],
+//   R_Y = |p_1| r_y,  gain_j = r12_j |p_j| / R_Y,  Lnew = diag(|p|) R22^T.
+// Column 0 and column 2 are the same vector, so after the first reflector
+// column 2 is r_y e_0 (gain_1 = 1: the observed coefficient becomes f) and
+// R22 has a zero in its second diagonal entry (the observed coefficient's
+// posterior variance is zero); the other n reflectors are structured
+// (U is triangular).  Row 0 of R' -- R_Y and the gain -- is final after
+// the first reflector, so the error estimate overlaps the rest.  Clears ok
+// when a sum of squares left the safe range (the caller then reruns the
+// attempt with iso_predict_chol and ts0_update).
+template <typename T, int NU, typename Q>
+PDQ_D T iso_predict_update_fast(const Q (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
+                                const T (&pinv)[NU + 1], T scale_q, T (&gain)[NU + 1], T (&Lnew)[NU + 1][NU + 1],
+                                bool& ok) {
+  constexpr int n = NU + 1;
+  static_assert(n >= 2, "the joint update needs the observed coefficient 1");
+  T Z[2 * n][n + 1];
+  T PL[n][n];
+#pragma unroll
+  for (int k = 0; k < n; ++k)
+#pragma unroll
+    for (int r = 0; r < n; ++r) PL[k][r] = pinv[k] * L[k][r];
+  // column c + 1 of Z is column c of [X; U]; column 0 is column 1 of [X; U]
+#pragma unroll
+  for (int c = 0; c < n; ++c)
+#pragma unroll
+    for (int r = 0; r < n; ++r) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = (c > r ? c : r); k < n; ++k) acc += T(iwp_a<NU>(c, k)) * PL[k][r];
+      Z[r][c + 1] = acc;
+      Z[n + r][c + 1] = (r <= c) ? scale_q * T(q1[c][r]) : T(0);
+    }
+#pragma unroll
+  for (int r = 0; r < 2 * n; ++r) Z[r][0] = Z[r][2];
+  constexpr unsigned x_rows = (1u << n) - 1u;
+  constexpr unsigned u01 = 3u << n;
+  constexpr unsigned all_cols = (1u << (n + 1)) - 1u;
+  // column 0 (pivot X row 0; X rows 1.., U rows 0, 1), applied to columns 1, 3..n
+  hh_step<T, 2 * n, n + 1, 0, 0, (x_rows & ~1u) | u01, all_cols & ~5u>(Z, ok);
+#pragma unroll
+  for (int r = 0; r < 2 * n; ++r) Z[r][2] = (r == 0) ? Z[0][0] : T(0);
+  // column 1 (pivot X row 1; X rows 2.., U rows 0, 1), applied to columns 3..n
+  hh_step<T, 2 * n, n + 1, 1, 1, (x_rows & ~3u) | u01, all_cols & ~7u>(Z, ok);
+  joint_tail<T, n, 3>(Z, ok);
+
+  const T ap1 = dev_abs(p[1]);
+  const T r_inv = fast_rcp(Z[0][0]) * dev_abs(pinv[1]);
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+    gain[i] = (i == 1) ? T(1) : Z[0][i + 1] * r_inv * dev_abs(p[i]);
+#pragma unroll
+    for (int j = 0; j < n; ++j) Lnew[i][j] = (j <= i) ? dev_abs(p[i]) * Z[j + 1][i + 1] : T(0);
+  }
+  return ap1 * Z[0][0];
+}
+
 template <typename T, int NU, int D, typename Q>
 PDQ_D void iso_predict(const Q (&q1)[kMaxN][kMaxN], const T (&m)[NU + 1][D], const T (&L)[NU + 1][NU + 1],
                        const T (&p)[NU + 1], const T (&pinv)[NU + 1], T scale_q, T (&mp)[NU + 1][D],
@@ -314,6 +599,63 @@ PDQ_D T ts0_update(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (
   return R_Y;
 }
 
+// Branch-free twin of ts0_update (rotations by the single-instruction
+// reciprocal square root, a zero pair rotated by the identity).  Clears ok
+// when a rotation's sum of squares left [1e-30, 1e36]; the caller then
+// reruns the attempt with ts0_update.
+template <typename T, int NR, int NC>
+PDQ_D void givens_rows_fast(T (&M)[NR][NC], int a, int b, int c0, bool& ok) {
+  const T x = M[a][c0], y = M[b][c0];
+  const T r2 = x * x + y * y;
+  ok = ok && (r2 == T(0) || !norm2_out_of_range(r2));
+  const T inv = fast_rsqrt(r2);
+  const bool zero = r2 == T(0);
+  const T cs = zero ? T(1) : x * inv;
+  const T sn = zero ? T(0) : y * inv;
+#pragma unroll
+  for (int j = 0; j < NC; ++j) {
+    if (j > c0) {
+      const T ma = M[a][j], mb = M[b][j];
+      M[a][j] = cs * ma + sn * mb;
+      M[b][j] = cs * mb - sn * ma;
+    }
+  }
+  M[a][c0] = zero ? x : r2 * inv;
+  M[b][c0] = T(0);
+}
+
+template <typename T, int NU, int OUT, bool H0 = true>
+PDQ_D T ts0_update_fast(const T (&Lp)[NU + 1][NU + 1], T damp, T (&gain)[NU + 1], T (&Lnew)[NU + 1][NU + 1], bool& ok,
+                        T h0 = T(0)) {
+  constexpr int n = NU + 1;
+  T M[n + 1][n + 1];
+#pragma unroll
+  for (int c = 0; c <= n; ++c) M[0][c] = (c == 0) ? damp : T(0);
+#pragma unroll
+  for (int r = 1; r <= n; ++r) {
+    if constexpr (H0) {
+      M[r][0] = (r == 1) ? Lp[OUT][0] + h0 * Lp[0][0] : Lp[OUT][r - 1];
+    } else {
+      M[r][0] = Lp[OUT][r - 1];
+    }
+#pragma unroll
+    for (int c = 1; c <= n; ++c) M[r][c] = (c >= r) ? Lp[c - 1][r - 1] : T(0);
+  }
+#pragma unroll
+  for (int r = OUT + 1; r >= 1; --r) givens_rows_fast<T, n + 1, n + 1>(M, r - 1, r, 0, ok);
+#pragma unroll
+  for (int c = 1; c <= OUT; ++c) givens_rows_fast<T, n + 1, n + 1>(M, c, c + 1, c, ok);
+  const T R_Y = M[0][0];
+  const T ry_inv = fast_rcp(R_Y);
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+    gain[i] = M[0][i + 1] * ry_inv;
+#pragma unroll
+    for (int j = 0; j < n; ++j) Lnew[i][j] = (j <= i) ? M[j + 1][i + 1] : T(0);
+  }
+  return R_Y;
+}
+
 // error_state_std: posterior std of coefficient 0 after conditioning the
 // unit-scale extrapolation N(., (|p| sqrt|h| Q1)(...)^T) on the linearised
 // residual (the Givens update of ts0_update applied to that factor; its row 0
@@ -338,7 +680,7 @@ PDQ_D T state_std0(const A& a, const T (&p)[NU + 1], T h, T damp, T h0) {
 
 template <typename T, int NU, int D>
 PDQ_D void write_record(const IsoArgs& a, int64_t b, int s_out, int S_out, const T (&m)[NU + 1][D],
-                        const T (&L)[NU + 1][NU + 1], double scale, double t, int steps) {
+                        const T (&lo)[2][D], const T (&L)[NU + 1][NU + 1], double scale, double t, int steps) {
   constexpr int n = NU + 1;
   const int64_t rec = b * S_out + s_out;
   double* um = a.u_mean + rec * (n * D);
@@ -347,6 +689,12 @@ PDQ_D void write_record(const IsoArgs& a, int64_t b, int s_out, int S_out, const
   for (int i = 0; i < n; ++i)
 #pragma unroll
     for (int j = 0; j < D; ++j) um[i * D + j] = double(m[i][j]);
+  if constexpr (sizeof(T) == sizeof(float)) {
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) um[i * D + j] += double(lo[i][j]);
+  }
 #pragma unroll
   for (int i = 0; i < n; ++i)
 #pragma unroll
@@ -354,6 +702,18 @@ PDQ_D void write_record(const IsoArgs& a, int64_t b, int s_out, int S_out, const
   a.output_scale[rec] = scale;
   a.t_out[rec] = t;
   a.num_steps[rec] = steps;
+}
+
+// A record of a mean without wide rows.
+template <typename T, int NU, int D>
+PDQ_D void write_record(const IsoArgs& a, int64_t b, int s_out, int S_out, const T (&m)[NU + 1][D],
+                        const T (&L)[NU + 1][NU + 1], double scale, double t, int steps) {
+  T lo[2][D];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) lo[i][j] = T(0);
+  write_record<T, NU, D>(a, b, s_out, S_out, m, lo, L, scale, t, steps);
 }
 
 // ---------------------------------------------------------------------------
@@ -668,15 +1028,20 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
   for (int k = 0; k < P; ++k) pd[k] = a.params[b * P + k];
   T pt[P];
+  Wide<T> pw[P];  // the parameters in the wide type (the residual's field evaluation)
 #pragma unroll
-  for (int k = 0; k < P; ++k) pt[k] = T(pd[k]);
+  for (int k = 0; k < P; ++k) {
+    pt[k] = T(pd[k]);
+    pw[k] = wide_from(pd[k], T(0));
+  }
   double y0[D];
 #pragma unroll
   for (int j = 0; j < D; ++j) y0[j] = a.y0[b * D + j];
   double tc[n][D];
   taylor_init<F, NU>(y0, pd, tc);
 
-  T m[n][D], L[n][n];
+  // mean (rows 0 and 1 wide: m plus the low parts mlo) and Cholesky factor
+  T m[n][D], mlo[2][D], L[n][n];
 #pragma unroll
   for (int i = 0; i < n; ++i) {
 #pragma unroll
@@ -684,6 +1049,10 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
     for (int j = 0; j < n; ++j) L[i][j] = T(0);
   }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) mlo[i][j] = T(wide_lo(wide_from(tc[i][j], T(0))));
   // tangents of m and of the interpolation state (TAN only): the Taylor
   // coefficients' derivative along this thread's direction
   T dm[n][D], dmi[n][D];
@@ -706,7 +1075,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
       for (int j = 0; j < D; ++j) dm[i][j] = dmi[i][j] = T(tcd[i][j].g[0]);
   }
   // interpolation state (interp_from); dead code when INTERP is false
-  T mi[n][D], Li[n][n];
+  T mi[n][D], milo[2][D], Li[n][n];
   using W = Wide<T>;
   constexpr bool kNarrow = sizeof(T) == sizeof(float);
   W ti = wide_from(save_at[0], T(0));
@@ -718,6 +1087,10 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
       for (int j = 0; j < n; ++j) Li[i][j] = T(0);
     }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) milo[i][j] = mlo[i][j];
   }
 
   // fixed-point smoother: running backward conditional of step_from (bw) and
@@ -750,7 +1123,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           q11 = cst<T>(a.q1[1][1], a.q1f[1][1]);
 
   if (!a.terminal_only) {
-    if (primary) write_record<T, NU, D>(a, b, 0, S_out, m, L, 1.0, wide_value(t), 0);
+    if (primary) write_record<T, NU, D>(a, b, 0, S_out, m, mlo, L, 1.0, wide_value(t), 0);
     if constexpr (TAN) write_tangent<T, NU, D, P>(a, b * S_out, kdir, dm);
   }
   if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S, m, L);
@@ -774,86 +1147,116 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   // nested loop's (solvers_via_adaptive_steps.py:196-375).
   int s = 1;
   W t_next = wide_from(save_at[1], T(0));
+  bool safe_next = false;  // the next attempt takes the range-checked predict and update
   while (s < S) {
     if (before(t, t_next)) {
       // ---- one attempt of the rejection loop (solvers_via_adaptive_steps.py:249-328) ----
-      bool accepted = false;
-      {
-        const T remaining = wide_diff(t_next, t);
-        const bool clipped = a.clip_dt && !(dt < remaining);
-        const T dt_use = clipped ? remaining : dt;
-        if (!(dev_abs(dt_use) > T(1e-14) * fmax(T(1), dev_abs(T(wide_hi(t)))))) {
-          status = PDQ_INSTANCE_DT_UNDERFLOW;
-          break;
-        }
-        if (attempts >= a.max_attempts) {
-          status = PDQ_INSTANCE_MAX_STEPS;
-          break;
-        }
-        ++attempts;
-        const T h = dt_use;
+      const T remaining = wide_diff(t_next, t);
+      const bool clipped = a.clip_dt && !(dt < remaining);
+      const T dt_use = clipped ? remaining : dt;
+      if (!(dev_abs(dt_use) > T(1e-14) * fmax(T(1), dev_abs(T(wide_hi(t)))))) {
+        status = PDQ_INSTANCE_DT_UNDERFLOW;
+        break;
+      }
+      if (attempts >= a.max_attempts) {
+        status = PDQ_INSTANCE_MAX_STEPS;
+        break;
+      }
+      ++attempts;
+      const T h = dt_use;
+      // The attempt's arithmetic, a generic lambda instantiated twice: with
+      // the branch-free predict and update (SAFE false), and with the
+      // range-checked ones (SAFE true), which rerun an attempt whose sums of
+      // squares left the safe range.  Each instantiation is one block of
+      // straight-line code, so the compiler interleaves the mean, the
+      // residual, the QR and the error estimate.
+      T mnew[n][D], mnewlo[2][D], dmnew[n][D], Lnew[n][n];
+      T rms_mobs, sigma_loc, ry_inv, dt_new, pi_new;
+      bool accepted, nonfinite, ok;
+      IsoBackward<T, NU, D> cnew;  // fixed-point: the prior's backward conditional of this step
+      auto attempt = [&](auto safe_tag) {
+        constexpr bool SAFE = decltype(safe_tag)::value;
         T p[n], pinv[n];
         precon<T, NU>(h, p, pinv);
 
         // extrapolated mean: the same for every calibration mode, and the
-        // error estimate's apply_flat(previous mean) (solvers.py:943-944)
-        T mp[n][D];
-        iso_predict_mean<T, NU, D>(m, p, pinv, mp);
-        // TS0 linearisation at the extrapolated mean (ssm_impl_isotropic.py:304-317);
+        // error estimate's apply_flat(previous mean) (solvers.py:943-944),
+        // in increment form with rows 0 and 1 wide
+        T incr[n][D], mp[n][D], mplo[2][D];
+        iso_mean_increment<T, NU, D>(m, p, pinv, incr);
+        iso_mean_add<T, NU, D>(m, mlo, incr, mp, mplo);
+        // TS0 linearisation at the extrapolated mean (ssm_impl_isotropic.py:304-317):
+        // the residual mp_1 - f(mp_0), the field evaluated in the wide type;
         // TS1: H = [-tr J_f(mp_0) / d, 1, 0, ...] (ssm_impl_isotropic.py:320-355,
         // jacobians.py:100-106), same residual mean
-        T f[D];
         T h0 = T(0);
         if (GEN && a.ts1) {
-          T Jf[D][D];
+          T f[D], Jf[D][D];
           eval_with_jacobian<F>(mp[0], pt, f, Jf);
           T tr = T(0);
 #pragma unroll
           for (int j = 0; j < D; ++j) tr += Jf[j][j];
           h0 = -tr * T(1.0 / D);
-        } else {
-          F::eval(mp[0], pt, f);
         }
+        static_assert(OUT == 1, "the residual observes coefficient 1");
         T mobs[D];
+        iso_residual<F, T, NU>(mp, mplo, pw, mobs);
         T mobs2 = T(0);
 #pragma unroll
-        for (int j = 0; j < D; ++j) {
-          mobs[j] = mp[OUT][j] - f[j];
-          mobs2 += mobs[j] * mobs[j];
-        }
-        const T rms_mobs = fast_sqrt(mobs2 * T(1.0 / D));
+        for (int j = 0; j < D; ++j) mobs2 += mobs[j] * mobs[j];
+        rms_mobs = fast_sqrt(mobs2 * T(1.0 / D));
         // fx.marginalise(apply_flat(m)) with unit scale: observed std
         // l = sqrt(|p_OUT|^2 |h| ||Q1[OUT]||^2 + damp^2), and the local scale
         // residual_whitened_rms = rms(mobs) / l (solvers.py:553-566, 955-957)
         const T ell = (GEN && a.ts1) ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
-                            : observed_std(p[OUT], h, q1_out_norm, damp);
-        const T sigma_loc = dev_div(rms_mobs, ell);
+                                     : observed_std(p[OUT], h, q1_out_norm, damp);
+        sigma_loc = dev_div(rms_mobs, ell);
 
+        // ---- predict (marginalise) and update (revert_conditional, H = e_OUT) ----
         const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
-        T Lp[n][n];
-        IsoBackward<T, NU, D> cnew;  // fixed-point: the prior's backward conditional of this step
+        const T scale_q = s_pred * (kNarrow ? fast_sqrt(dev_abs(h)) : dev_sqrt(dev_abs(h)));
+        T Lp[n][n], gain[n], R_Y;
+        ok = true;
         if constexpr (FP) {
           if constexpr (kNarrow) {
-            iso_prior_revert<T, NU, D>(a.q1f, m, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp, cnew);
+            iso_prior_revert<T, NU, D>(a.q1f, m, L, p, pinv, scale_q, Lp, cnew);
           } else {
-            iso_prior_revert<T, NU, D>(a.q1, m, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp, cnew);
+            iso_prior_revert<T, NU, D>(a.q1, m, L, p, pinv, scale_q, Lp, cnew);
           }
-        } else if constexpr (kNarrow) {
-          iso_predict_chol<T, NU>(a.q1f, L, p, pinv, s_pred * fast_sqrt(dev_abs(h)), Lp);
+          R_Y = ts0_update<T, NU, OUT, GEN>(Lp, damp, gain, Lnew, h0);
+        } else if constexpr (SAFE) {
+          if constexpr (kNarrow) {
+            iso_predict_chol<T, NU>(a.q1f, L, p, pinv, scale_q, Lp);
+          } else {
+            iso_predict_chol<T, NU>(a.q1, L, p, pinv, scale_q, Lp);
+          }
+          R_Y = ts0_update<T, NU, OUT, GEN>(Lp, damp, gain, Lnew, h0);
+        } else if ((!GEN && !TAN) || (damp == T(0) && !(GEN && a.ts1))) {
+          // TS0 without damping (always so in the lean instantiation, by the
+          // launchers' dispatch): the predict and the update in one QR
+          if constexpr (kNarrow) {
+            R_Y = iso_predict_update_fast<T, NU>(a.q1f, L, p, pinv, scale_q, gain, Lnew, ok);
+          } else {
+            R_Y = iso_predict_update_fast<T, NU>(a.q1, L, p, pinv, scale_q, gain, Lnew, ok);
+          }
         } else {
-          iso_predict_chol<T, NU>(a.q1, L, p, pinv, s_pred * dev_sqrt(dev_abs(h)), Lp);
+          if constexpr (kNarrow) {
+            ok = iso_predict_chol_fast<T, NU>(a.q1f, L, p, pinv, scale_q, Lp);
+          } else {
+            ok = iso_predict_chol_fast<T, NU>(a.q1, L, p, pinv, scale_q, Lp);
+          }
+          R_Y = ts0_update_fast<T, NU, OUT, GEN>(Lp, damp, gain, Lnew, ok, h0);
         }
-
-        // ---- update (revert_conditional, H = e_OUT) ----
-        T gain[n], Lnew[n][n];
-        const T R_Y = ts0_update<T, NU, OUT, GEN>(Lp, damp, gain, Lnew, h0);
-        const T ry_inv = fast_rcp(R_Y);
-        T mnew[n][D];
+        ry_inv = fast_rcp(R_Y);
+        // mnew = mp - gain mobs = m + (incr - gain mobs), the wide rows summed wide
+        {
+          T dlt[n][D];
 #pragma unroll
-        for (int i = 0; i < n; ++i)
+          for (int i = 0; i < n; ++i)
 #pragma unroll
-          for (int j = 0; j < D; ++j) mnew[i][j] = mp[i][j] - gain[i] * mobs[j];
-        T dmnew[n][D];
+            for (int j = 0; j < D; ++j) dlt[i][j] = incr[i][j] - gain[i] * mobs[j];
+          iso_mean_add<T, NU, D>(m, mlo, dlt, mnew, mnewlo);
+        }
         if constexpr (TAN) {
           T dmp[n][D];
           iso_predict_mean<T, NU, D>(dm, p, pinv, dmp);
@@ -897,77 +1300,104 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
         // error_norm^2 = sumsq / D; accepted iff error_power = error_norm^(-1/n)
         // >= 1, i.e. iff sumsq <= D (decided on the wide sum)
         const T norm2 = T(wide_hi(sumsq)) * T(1.0 / D);
-        if (!(norm2 == norm2) || isinf(norm2)) {
-          status = PDQ_INSTANCE_NONFINITE;
-          break;
-        }
+        nonfinite = !(norm2 == norm2) || isinf(norm2);
         const T ep = dev_fpow(norm2, T(-0.5 / n));
         accepted = wide_le(sumsq, T(D));
 
         // ---- controller (controllers.py:24-84) ----
         T factor;
+        pi_new = pi_prev;
         if (a.control == PDQ_CONTROL_INTEGRAL) {
           factor = safety * ep;
         } else {
           const T gi = dev_fpow(ep, cst<T>(a.exp_i, a.exp_i_f));
           const T gp = dev_fpow(dev_div(ep, pi_prev), cst<T>(a.exp_p, a.exp_p_f));
           factor = safety * gi * gp;
-          if (accepted) pi_prev = ep;
+          if (accepted) pi_new = ep;
         }
         factor = fmax(factor_min, fmin(factor, factor_max));
-        dt = factor * dt_use;
-        if (accepted) {
-          if constexpr (INTERP) {
-            ti = t;
+        dt_new = factor * dt_use;
+      };
+      if constexpr (FP) {
+        attempt(BoolTag<true>{});
+      } else if (safe_next) {
+        attempt(BoolTag<true>{});
+        safe_next = false;
+      } else {
+        attempt(BoolTag<false>{});
+        if (!ok) {  // rerun with the range-checked predict and update
+          safe_next = true;
+          --attempts;
+          continue;
+        }
+      }
+      // (tested after the controller so the attempt stays straight-line code;
+      // a non-finite attempt is never accepted)
+      if (nonfinite) {
+        status = PDQ_INSTANCE_NONFINITE;
+        break;
+      }
+      dt = dt_new;
+      pi_prev = pi_new;
+      if (accepted) {
+        if constexpr (INTERP) {
+          ti = t;
 #pragma unroll
-            for (int i = 0; i < n; ++i) {
+          for (int i = 0; i < n; ++i) {
 #pragma unroll
-              for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
+            for (int j = 0; j < D; ++j) mi[i][j] = m[i][j];
 #pragma unroll
-              for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
-            }
-            if constexpr (FP) bwi = bw;
-            if constexpr (TAN) {
-#pragma unroll
-              for (int i = 0; i < n; ++i)
-#pragma unroll
-                for (int j = 0; j < D; ++j) dmi[i][j] = dm[i][j];
-            }
+            for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
           }
+#pragma unroll
+          for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) milo[i][j] = mlo[i][j];
+          if constexpr (FP) bwi = bw;
           if constexpr (TAN) {
 #pragma unroll
             for (int i = 0; i < n; ++i)
 #pragma unroll
-              for (int j = 0; j < D; ++j) dm[i][j] = dmnew[i][j];
+              for (int j = 0; j < D; ++j) dmi[i][j] = dm[i][j];
           }
-          if constexpr (FP) {
-            IsoBackward<T, NU, D> merged;
-            iso_cond_merge(bw, cnew, merged);
-            bw = merged;
-          }
-          // a step clipped to the checkpoint lands on it exactly in float
-          // pairs; float64 adds as the reference does
-          if constexpr (kNarrow) {
-            t = clipped ? t_next : wide_add(t, dt_use);
-          } else {
-            t = t + dt_use;
-          }
-          ++num_steps;
-#pragma unroll
-          for (int i = 0; i < n; ++i) {
-#pragma unroll
-            for (int j = 0; j < D; ++j) m[i][j] = mnew[i][j];
-#pragma unroll
-            for (int j = 0; j < n; ++j) L[i][j] = Lnew[i][j];
-          }
-          if (a.solver == PDQ_SOLVER_MLE) {
-            // running scale via hypot recurrence == RMS of new terms (solvers.py:421-424)
-            const T new_term = rms_mobs * dev_abs(ry_inv);
-            mle_sumsq = wide_add_sq(mle_sumsq, new_term);
-            ++num_data;
-          }
-          sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
         }
+        if constexpr (TAN) {
+#pragma unroll
+          for (int i = 0; i < n; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) dm[i][j] = dmnew[i][j];
+        }
+        if constexpr (FP) {
+          IsoBackward<T, NU, D> merged;
+          iso_cond_merge(bw, cnew, merged);
+          bw = merged;
+        }
+        // a step clipped to the checkpoint lands on it exactly in float
+        // pairs; float64 adds as the reference does
+        if constexpr (kNarrow) {
+          t = clipped ? t_next : wide_add(t, dt_use);
+        } else {
+          t = t + dt_use;
+        }
+        ++num_steps;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+#pragma unroll
+          for (int j = 0; j < D; ++j) m[i][j] = mnew[i][j];
+#pragma unroll
+          for (int j = 0; j < n; ++j) L[i][j] = Lnew[i][j];
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) mlo[i][j] = mnewlo[i][j];
+        if (a.solver == PDQ_SOLVER_MLE) {
+          // running scale via hypot recurrence == RMS of new terms (solvers.py:421-424)
+          const T new_term = rms_mobs * dev_abs(ry_inv);
+          mle_sumsq = wide_add_sq(mle_sumsq, new_term);
+          ++num_data;
+        }
+        sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
       }
       if (!accepted) continue;  // retry in the next iteration
     }
@@ -981,15 +1411,19 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
         // interp_beyond_t1: predict from interp_from to t_next
         // (solvers.py:205-269, estimators_and_losses.py:403-414)
         const T h = T(wide_diff(t_next, ti));
-        T p[n], pinv[n], mp[n][D], Lp[n][n];
+        T p[n], pinv[n], mp[n][D], mplo[2][D], Lp[n][n];
         precon<T, NU>(h, p, pinv);
+        {
+          T incr[n][D];
+          iso_mean_increment<T, NU, D>(mi, p, pinv, incr);
+          iso_mean_add<T, NU, D>(mi, milo, incr, mp, mplo);
+        }
         if constexpr (FP) {
           // estimators_and_losses.py:549-591: the extrapolation to t_next
           // closes the checkpoint's conditional (bwi merged with it); the
           // step_from state keeps its marginal with the conditional from
           // t_next to t, merged into the identity
           IsoBackward<T, NU, D> c0, m0, c1, idc, m1;
-          iso_predict_mean<T, NU, D>(mi, p, pinv, mp);
           if constexpr (kNarrow) {
             iso_prior_revert<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp, c0);
           } else {
@@ -1011,11 +1445,11 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           bw = m1;
           iso_cond_identity(bwi);
         } else if constexpr (kNarrow) {
-          iso_predict<T, NU, D>(a.q1f, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
+          iso_predict_chol<T, NU>(a.q1f, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp);
         } else {
-          iso_predict<T, NU, D>(a.q1, mi, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), mp, Lp);
+          iso_predict_chol<T, NU>(a.q1, Li, p, pinv, sigma_sf * dev_sqrt(dev_abs(h)), Lp);
         }
-        if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, mp, Lp, double(sigma_sf), wide_value(t_next), num_steps);
+        if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, mp, mplo, Lp, double(sigma_sf), wide_value(t_next), num_steps);
         if (FP && a.filter_mean) write_filter<T, NU, D>(a, b * S + s, mp, Lp);
         if constexpr (TAN) {
           T dmp[n][D];
@@ -1034,10 +1468,14 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
           for (int j = 0; j < n; ++j) Li[i][j] = Lp[i][j];
         }
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) milo[i][j] = mplo[i][j];
       }
     } else {
       // interp_at_t1: the state itself is the solution (estimators_and_losses.py:416-421)
-      if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, m, L, double(sigma_sf), wide_value(t), num_steps);
+      if (record && primary) write_record<T, NU, D>(a, b, s_out, S_out, m, mlo, L, double(sigma_sf), wide_value(t), num_steps);
       if constexpr (TAN) {
         if (record) write_tangent<T, NU, D, P>(a, b * S_out + s_out, kdir, dm);
         if constexpr (INTERP) {
@@ -1063,6 +1501,10 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
           for (int j = 0; j < n; ++j) Li[i][j] = L[i][j];
         }
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) milo[i][j] = mlo[i][j];
       }
     }
     if (!before(t, t_next)) {  // checkpoint s done

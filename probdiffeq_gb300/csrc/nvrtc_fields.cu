@@ -61,7 +61,7 @@ UserField* lookup(int32_t field) {
 
 const char* tf(bool b) { return b ? "true" : "false"; }
 
-// gen: the instantiation with TS1 / error_state_std (as the built-in fields' dispatch)
+// gen: the instantiation with TS1 / error_state_std / damping (as the built-in fields' dispatch)
 std::string kernel_expression(bool f64, int nu, bool interp, bool fp, bool gen) {
   return std::string("pdq::iso_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
          ", pdq_user::Field, " + tf(interp) + ", " + tf(fp) + ", " + tf(gen) + ">";
@@ -90,8 +90,9 @@ pdq_status compile(const std::string& source, const std::vector<std::string>& ex
                          kPdqHeaderNames) != NVRTC_SUCCESS)
     return PDQ_ERROR_COMPILE;
   for (const auto& e : expressions) nvrtcAddNameExpression(prog, e.c_str());
-  const char* options[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-lineinfo"};
-  const nvrtcResult rc = nvrtcCompileProgram(prog, 3, options);
+  // -default-device: the kernels' local lambdas (unannotated) are device code
+  const char* options[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-lineinfo", "-default-device"};
+  const nvrtcResult rc = nvrtcCompileProgram(prog, 4, options);
   size_t log_size = 0;
   nvrtcGetProgramLogSize(prog, &log_size);
   std::string text(log_size, '\0');
@@ -198,7 +199,8 @@ cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, 
                                 cudaStream_t stream, int block) {
   UserField* f = lookup(field);
   if (f == nullptr || nu < 1 || nu > 5) return cudaErrorInvalidValue;
-  const bool gen = fp || a.ts1 || a.state_error;
+  // (the lean instantiation's single-QR update needs TS0 without damping)
+  const bool gen = fp || a.ts1 || a.state_error || a.damp != 0.0;
   cudaKernel_t kernel = nullptr;
   cudaError_t e = user_kernel(f, kernel_expression(f64, nu, interp, fp, gen), "iso_solver.cuh", &kernel);
   if (e != cudaSuccess) return e;

@@ -133,17 +133,106 @@ PDQ_D double fast_rcp(double x) { return 1.0 / x; }
 
 struct FloatPair {
   float hi, lo;
+  FloatPair() = default;
+  PDQ_HD constexpr FloatPair(float h, float l) : hi(h), lo(l) {}
+  // exact conversions (the vector fields write constants as T(1), T(3))
+  PDQ_HD constexpr FloatPair(float x) : hi(x), lo(0.0f) {}
+  PDQ_HD constexpr FloatPair(int x) : hi(float(x)), lo(0.0f) {}
 };
 
-PDQ_D FloatPair two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  return {s, (a - (s - bb)) + (b - bb)};
+// The sums and products of the error-free transformations use the _rn
+// intrinsics, which the compiler never contracts into an FMA: a product
+// fused into the following sum would break the transformation's exactness.
+// (Host runs of the kernel bodies compile with FMA contraction off.)
+PDQ_HD float add_rn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fadd_rn(a, b);
+#else
+  return a + b;
+#endif
 }
-PDQ_D FloatPair fast_two_sum(float a, float b) {  // requires |a| >= |b| or a == 0
-  const float s = a + b;
-  return {s, b - (s - a)};
+PDQ_HD float sub_rn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
 }
+PDQ_HD float mul_rn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+// a / b to a few ulp (single-instruction reciprocal and a product)
+PDQ_HD float div_approx(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+PDQ_HD FloatPair two_sum(float a, float b) {
+  const float s = add_rn(a, b);
+  const float bb = sub_rn(s, a);
+  return {s, add_rn(sub_rn(a, sub_rn(s, bb)), sub_rn(b, bb))};
+}
+PDQ_HD FloatPair fast_two_sum(float a, float b) {  // requires |a| >= |b| or a == 0
+  const float s = add_rn(a, b);
+  return {s, sub_rn(b, sub_rn(s, a))};
+}
+
+// ---------------------------------------------------------------------------
+// Float-pair arithmetic (the "double-float" number type of Dekker 1971 with
+// the error-free sum of Knuth and the FMA product), ~44 significant bits.
+// The float32 isotropic kernels evaluate the TS0 residual u' - f(u) in it:
+// the residual is a difference of two numbers of the size of the solution's
+// derivative and, at rtol 1e-6, about 1e-5 of them, so formed in float32 its
+// rounding (the state's and the field's, ~1e-7 of the terms) puts a noise
+// floor under the error estimate that rejects and shortens steps float64
+// accepts.  Every field is generic over its scalar type, so the same source
+// evaluates in pairs.  Accuracy ~2^-44 relative per operation (the "sloppy"
+// sum, which loses it only under cancellation of the low parts).
+// ---------------------------------------------------------------------------
+
+PDQ_HD FloatPair operator-(FloatPair a) { return {-a.hi, -a.lo}; }
+PDQ_HD FloatPair operator+(FloatPair a, FloatPair b) {
+  const FloatPair s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, add_rn(s.lo, add_rn(a.lo, b.lo)));
+}
+PDQ_HD FloatPair operator+(FloatPair a, float b) {
+  const FloatPair s = two_sum(a.hi, b);
+  return fast_two_sum(s.hi, add_rn(s.lo, a.lo));
+}
+PDQ_HD FloatPair operator+(float a, FloatPair b) { return b + a; }
+PDQ_HD FloatPair operator-(FloatPair a, FloatPair b) { return a + (-b); }
+PDQ_HD FloatPair operator-(FloatPair a, float b) { return a + (-b); }
+PDQ_HD FloatPair operator-(float a, FloatPair b) { return (-b) + a; }
+PDQ_HD FloatPair operator*(FloatPair a, FloatPair b) {
+  const float p = mul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+PDQ_HD FloatPair operator*(FloatPair a, float b) {
+  const float p = mul_rn(a.hi, b);
+  float e = fmaf(a.hi, b, -p);
+  e = fmaf(a.lo, b, e);
+  return fast_two_sum(p, e);
+}
+PDQ_HD FloatPair operator*(float a, FloatPair b) { return b * a; }
+// quotient by one correction step: q = a / b to float accuracy, then the
+// float remainder a - q b, formed exactly in pairs, divided once more
+PDQ_HD FloatPair operator/(FloatPair a, FloatPair b) {
+  const float q = div_approx(a.hi, b.hi);
+  const FloatPair r = a - b * q;
+  return fast_two_sum(q, div_approx(r.hi, b.hi));
+}
+PDQ_HD FloatPair& operator+=(FloatPair& a, FloatPair b) { return a = a + b; }
+PDQ_HD FloatPair& operator-=(FloatPair& a, FloatPair b) { return a = a - b; }
+PDQ_HD FloatPair& operator*=(FloatPair& a, FloatPair b) { return a = a * b; }
 
 template <typename T>
 struct WideOf {
@@ -165,6 +254,8 @@ PDQ_D double wide_value(double x) { return x; }
 PDQ_D double wide_value(FloatPair x) { return double(x.hi) + double(x.lo); }
 PDQ_D double wide_hi(double x) { return x; }
 PDQ_D float wide_hi(FloatPair x) { return x.hi; }
+PDQ_D double wide_lo(double) { return 0.0; }
+PDQ_D float wide_lo(FloatPair x) { return x.lo; }
 
 // x + y for a narrow y
 PDQ_D double wide_add(double x, double y) { return x + y; }
@@ -200,6 +291,12 @@ PDQ_D float wide_diff(FloatPair x, FloatPair y) {
 // x <= c for a narrow constant c
 PDQ_D bool wide_le(double x, double c) { return x <= c; }
 PDQ_D bool wide_le(FloatPair x, float c) { return x.hi < c || (x.hi == c && x.lo <= 0.0f); }
+
+// A compile-time boolean as a type (selects an instantiation of a generic lambda).
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
+};
 
 template <int K>
 struct Factorial {
