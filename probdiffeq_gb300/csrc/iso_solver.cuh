@@ -83,23 +83,15 @@ PDQ_D T cst(double d, float f) {
 }
 
 // Preconditioner p_i = h^(NU-i)/(NU-i)!, p_inv_i = 1/p_i (utilities.py:74-84).
-// The powers by repeated squaring, so the chain from h is ~log2(NU) products
-// (it starts every attempt's dependency chain).
 template <typename T, int NU>
 PDQ_D void precon(T h, T (&p)[NU + 1], T (&pinv)[NU + 1]) {
   const T hinv = fast_rcp(h);
-  T hp[NU + 1], hm[NU + 1];
-  hp[0] = T(1);
-  hm[0] = T(1);
+  p[NU] = T(1);
+  pinv[NU] = T(1);
 #pragma unroll
-  for (int k = 1; k <= NU; ++k) {
-    hp[k] = (k == 1) ? h : ((k & 1) ? hp[k - 1] * h : hp[k / 2] * hp[k / 2]);
-    hm[k] = (k == 1) ? hinv : ((k & 1) ? hm[k - 1] * hinv : hm[k / 2] * hm[k / 2]);
-  }
-#pragma unroll
-  for (int i = 0; i <= NU; ++i) {
-    p[i] = hp[NU - i] * T(1.0 / factorial(NU - i));
-    pinv[i] = hm[NU - i] * T(factorial(NU - i));
+  for (int i = NU - 1; i >= 0; --i) {
+    p[i] = p[i + 1] * h * T(1.0 / (NU - i));
+    pinv[i] = pinv[i + 1] * hinv * T(NU - i);
   }
 }
 
@@ -503,13 +495,12 @@ PDQ_D void joint_tail(T (&Z)[2 * n][n + 1], bool& ok) {
 // the first reflector, so the error estimate overlaps the rest.  Clears ok
 // when a sum of squares left the safe range (the caller then reruns the
 // attempt with iso_predict_chol and ts0_update).
-template <typename T, int NU, typename Q>
-PDQ_D T iso_predict_update_fast(const Q (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
-                                const T (&pinv)[NU + 1], T scale_q, T (&gain)[NU + 1], T (&Lnew)[NU + 1][NU + 1],
-                                bool& ok) {
+// The pieces of the joint predict-update (used in this order; a
+// warp-specialised kernel publishes the gain between the third and fourth):
+// the X rows of Z from L (independent of the noise scale) ...
+template <typename T, int NU>
+PDQ_D void joint_x(const T (&L)[NU + 1][NU + 1], const T (&pinv)[NU + 1], T (&Z)[2 * (NU + 1)][NU + 2]) {
   constexpr int n = NU + 1;
-  static_assert(n >= 2, "the joint update needs the observed coefficient 1");
-  T Z[2 * n][n + 1];
   T PL[n][n];
 #pragma unroll
   for (int k = 0; k < n; ++k)
@@ -524,10 +515,29 @@ PDQ_D T iso_predict_update_fast(const Q (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1
 #pragma unroll
       for (int k = (c > r ? c : r); k < n; ++k) acc += T(iwp_a<NU>(c, k)) * PL[k][r];
       Z[r][c + 1] = acc;
-      Z[n + r][c + 1] = (r <= c) ? scale_q * T(q1[c][r]) : T(0);
     }
 #pragma unroll
-  for (int r = 0; r < 2 * n; ++r) Z[r][0] = Z[r][2];
+  for (int r = 0; r < n; ++r) Z[r][0] = Z[r][2];
+}
+
+// ... the U rows (the scaled process-noise factor) ...
+template <typename T, int NU, typename Q>
+PDQ_D void joint_u(const Q (&q1)[kMaxN][kMaxN], T scale_q, T (&Z)[2 * (NU + 1)][NU + 2]) {
+  constexpr int n = NU + 1;
+#pragma unroll
+  for (int c = 0; c < n; ++c)
+#pragma unroll
+    for (int r = 0; r < n; ++r) Z[n + r][c + 1] = (r <= c) ? scale_q * T(q1[c][r]) : T(0);
+#pragma unroll
+  for (int r = 0; r < n; ++r) Z[n + r][0] = Z[n + r][2];
+}
+
+// ... the first reflector, which finalises row 0 of R': returns R_Y, writes the gain ...
+template <typename T, int NU>
+PDQ_D T joint_first(T (&Z)[2 * (NU + 1)][NU + 2], const T (&p)[NU + 1], const T (&pinv)[NU + 1], T (&gain)[NU + 1],
+                    bool& ok) {
+  constexpr int n = NU + 1;
+  static_assert(n >= 2, "the joint update needs the observed coefficient 1");
   constexpr unsigned x_rows = (1u << n) - 1u;
   constexpr unsigned u01 = 3u << n;
   constexpr unsigned all_cols = (1u << (n + 1)) - 1u;
@@ -535,19 +545,39 @@ PDQ_D T iso_predict_update_fast(const Q (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1
   hh_step<T, 2 * n, n + 1, 0, 0, (x_rows & ~1u) | u01, all_cols & ~5u>(Z, ok);
 #pragma unroll
   for (int r = 0; r < 2 * n; ++r) Z[r][2] = (r == 0) ? Z[0][0] : T(0);
+  const T r_inv = fast_rcp(Z[0][0]) * dev_abs(pinv[1]);
+#pragma unroll
+  for (int i = 0; i < n; ++i) gain[i] = (i == 1) ? T(1) : Z[0][i + 1] * r_inv * dev_abs(p[i]);
+  return dev_abs(p[1]) * Z[0][0];
+}
+
+// ... and the other reflectors, which give the updated factor.
+template <typename T, int NU>
+PDQ_D void joint_rest(T (&Z)[2 * (NU + 1)][NU + 2], const T (&p)[NU + 1], T (&Lnew)[NU + 1][NU + 1], bool& ok) {
+  constexpr int n = NU + 1;
+  constexpr unsigned x_rows = (1u << n) - 1u;
+  constexpr unsigned u01 = 3u << n;
+  constexpr unsigned all_cols = (1u << (n + 1)) - 1u;
   // column 1 (pivot X row 1; X rows 2.., U rows 0, 1), applied to columns 3..n
   hh_step<T, 2 * n, n + 1, 1, 1, (x_rows & ~3u) | u01, all_cols & ~7u>(Z, ok);
   joint_tail<T, n, 3>(Z, ok);
-
-  const T ap1 = dev_abs(p[1]);
-  const T r_inv = fast_rcp(Z[0][0]) * dev_abs(pinv[1]);
 #pragma unroll
-  for (int i = 0; i < n; ++i) {
-    gain[i] = (i == 1) ? T(1) : Z[0][i + 1] * r_inv * dev_abs(p[i]);
+  for (int i = 0; i < n; ++i)
 #pragma unroll
     for (int j = 0; j < n; ++j) Lnew[i][j] = (j <= i) ? dev_abs(p[i]) * Z[j + 1][i + 1] : T(0);
-  }
-  return ap1 * Z[0][0];
+}
+
+template <typename T, int NU, typename Q>
+PDQ_D T iso_predict_update_fast(const Q (&q1)[kMaxN][kMaxN], const T (&L)[NU + 1][NU + 1], const T (&p)[NU + 1],
+                                const T (&pinv)[NU + 1], T scale_q, T (&gain)[NU + 1], T (&Lnew)[NU + 1][NU + 1],
+                                bool& ok) {
+  constexpr int n = NU + 1;
+  T Z[2 * n][n + 1];
+  joint_x<T, NU>(L, pinv, Z);
+  joint_u<T, NU>(q1, scale_q, Z);
+  const T R_Y = joint_first<T, NU>(Z, p, pinv, gain, ok);
+  joint_rest<T, NU>(Z, p, Lnew, ok);
+  return R_Y;
 }
 
 template <typename T, int NU, int D, typename Q>
