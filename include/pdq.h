@@ -217,8 +217,9 @@ pdq_status pdq_solve_adaptive(const pdq_config* config, const pdq_adaptive_args*
 /* Device scratch of pdq_lml_fixed_grid in bytes.  Its leading part holds
  * the covariance plan shared by all parameter samples (with TS0, the
  * uncalibrated solver and a fixed step the covariances do not depend on the
- * parameters), keyed by (dt, damp, num_steps, save_every, nu, precision): a
- * call whose key equals the one stored in the workspace reuses the plan, so
+ * parameters), keyed by (dt, damp, num_steps, save_every, nu, precision)
+ * and a bit-exact copy of the per-observation noise std: a call whose key
+ * equals the one stored in the workspace reuses the plan, so
  * a caller that writes into the workspace between calls must zero its first
  * 256 bytes. */
 #if !defined(__CUDACC_RTC__)

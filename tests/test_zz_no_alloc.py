@@ -68,6 +68,28 @@ def test_static_scratch_entry_point_matches_allocating_entry_point():
         gerr = (out[1] - ref[1]).abs().max(dim=1).values / ref[1].norm(dim=1)
         assert float(gerr.max()) <= 1e-6
 
+    # a call whose plan key differs from the one the array holds (another
+    # noise std, another grid length) must rebuild the plan, not reuse it
+    for std_k, steps_k in ((2.0 * std, num_steps), (std[: (num_steps // 2) // 10 + 1], num_steps // 2)):
+        data_k = data[: std_k.shape[0]].contiguous()
+        need_k = ctypes.c_size_t(0)
+        assert lib.pdq_lml_workspace_size(ctypes.byref(cfg), B, steps_k, 10, ctypes.byref(need_k)) == 0
+        ws_k = torch.zeros(need_k.value, dtype=torch.uint8, device="cuda")
+        ref_k = [torch.empty(B, **f64), torch.empty((B, 3), **f64), torch.empty(B, dtype=torch.int32, device="cuda")]
+        a = _args(_native, B, thetas, y0, data_k, std_k, *ref_k, steps_k, 10)
+        assert lib.pdq_lml_fixed_grid(ctypes.byref(cfg), ctypes.byref(a), ctypes.c_void_p(ws_k.data_ptr()), need_k,
+                                      stream) == 0
+        out = [torch.full((B,), float("nan"), **f64), torch.full((B, 3), float("nan"), **f64),
+               torch.full((B,), -1, dtype=torch.int32, device="cuda")]
+        a = _args(_native, B, thetas, y0, data_k, std_k, *out, steps_k, 10)
+        assert lib.pdq_lml_fixed_grid_static(ctypes.byref(cfg), ctypes.byref(a), stream) == 0
+        torch.cuda.synchronize()
+        assert (ref_k[2] == 0).all() and (out[2] == 0).all()
+        assert torch.allclose(out[0], ref_k[0], rtol=1e-9, atol=0.0)
+        assert not torch.allclose(out[0], ref[0], rtol=1e-6, atol=0.0)  # a different problem, a different LML
+        gerr = (out[1] - ref_k[1]).abs().max(dim=1).values / ref_k[1].norm(dim=1)
+        assert float(gerr.max()) <= 1e-6
+
 
 def test_static_scratch_rejects_problems_beyond_its_size():
     from probdiffeq_gb300 import _native, ensemble
