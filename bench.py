@@ -390,8 +390,7 @@ def run_lv_ensemble(args):
     def device_step(c):
         _native.solve_adaptive(c, d_save, d_params, d_y0, d_dt0, True, outs, stream=stream)
 
-    names = {1: "thread per instance", 2: "8 lanes per instance, <=128 regs", 3: "8 lanes per instance, <=85 regs",
-             4: "warp-specialised: covariance warp + control warp"}
+    names = {1: "thread per instance", 2: "8 lanes per instance, <=128 regs", 3: "8 lanes per instance, <=85 regs"}
 
     def label(cand):
         return f"{names[cand[0]]}, {cand[1] or 'default'} instances per CTA"
@@ -403,7 +402,7 @@ def run_lv_ensemble(args):
         def tune(precision):
             return autotune.tune(config(precision), d_save, d_params, d_y0, d_dt0, True, stream=stream)
 
-        fixed = {"thread": 1, "lanes": 2, "lanes_compact": 3, "pair": 4}.get(args.variant)
+        fixed = {"thread": 1, "lanes": 2, "lanes_compact": 3}.get(args.variant)
         if fixed is None:
             best32, tune32 = tune("float32")
             best64, tune64 = tune("float64")
@@ -715,9 +714,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lv_ensemble",
                     choices=["lv_ensemble", "lv_single", "fhn_lml", "vdp_dense", "burgers_blockdiag"])
-    ap.add_argument("--variant", default="auto", choices=["auto", "thread", "lanes", "lanes_compact", "pair"],
-                    help="lv_ensemble: instance-to-lane mapping (auto: the library autotuner times the candidates "
-                         "and keeps the fastest)")
+    ap.add_argument("--variant", default="auto", choices=["auto", "thread", "lanes", "lanes_compact"],
+                    help="lv_ensemble: instance-to-lane mapping (auto = time all three and keep the fastest)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="e2e: launch the solver eagerly instead of from CUDA graphs")
     ap.add_argument("--no-secondary", action="store_true", help="skip the single-instance and LML measurements")

@@ -112,17 +112,14 @@ typedef struct pdq_config {
   int32_t clip_dt;        /* RejectionLoop clip_dt (solvers_via_adaptive_steps.py:300-301) */
   int32_t correct_asymptotic_underconfidence; /* solver_mle (solvers.py:456-457) */
   int32_t kernel_variant;  /* isotropic mapping: 0 auto, 1 one thread per instance,
-                              2 / 3 eight lanes per instance with <= 128 / <= 85 registers (clip_dt only),
-                              4 warp-specialised: a covariance warp and a control warp per 32 instances
-                              (filter, TS0 without damping, error_residual_std, built-in fields);
+                              2 / 3 eight lanes per instance with <= 128 / <= 85 registers (clip_dt only);
                               dense: 2 eight lanes per instance, otherwise one thread per instance */
   double safety, factor_min, factor_max;           /* controller (defaults 0.95, 0.2, 10) */
   double exponent_integral, exponent_proportional; /* PI controller (0.3, 0.4) */
   double atol, rtol, eps, damp;                    /* solve(...) arguments */
   int64_t max_attempts;   /* bound on step attempts per instance (the reference has none) */
   int32_t instances_per_block; /* instances per CTA; 0: default.  Isotropic: 32 or 64 (one thread
-                                  each; default 64), 8, 16 or 32 (eight lanes each; default 32), 32
-                                  (warp-specialised: two warps per CTA);
+                                  each; default 64), 8, 16 or 32 (eight lanes each; default 32);
                                   dense: 8, 16 or 32 (one thread each; default 32), 1 to 4 (eight
                                   lanes each; default 4); block-diagonal: 0 */
   int32_t reserved0;      /* 0 */

@@ -23,7 +23,6 @@ __all__ = ["candidates", "tune", "tuned_config", "cache_key", "clear_cache"]
 # (kernel_variant, instances_per_block), see include/pdq.h
 _ISO_THREAD = [(1, 64), (1, 32)]
 _ISO_LANES = [(2, 32), (2, 16), (3, 32)]
-_ISO_PAIR = [(4, 32)]
 _DENSE_THREAD = [(1, 32), (1, 16)]
 _DENSE_LANES = [(2, 4), (2, 2)]
 
@@ -34,11 +33,10 @@ _lock = threading.Lock()
 def candidates(cfg):
     """The (kernel_variant, instances_per_block) pairs the ABI accepts for ``cfg``."""
     if cfg.ssm == _native.SSM["isotropic"]:
-        lean = (cfg.constraint == _native.CONSTRAINT["ts0"] and cfg.error == _native.ERROR["residual_std"]
-                and cfg.strategy == _native.STRATEGY["filter"] and cfg.field < _native.FIELD_USER_BASE)
-        lanes_ok = lean and cfg.clip_dt
-        pair_ok = lean and cfg.damp == 0.0
-        return _ISO_THREAD + (_ISO_LANES if lanes_ok else []) + (_ISO_PAIR if pair_ok else [])
+        lanes_ok = (cfg.clip_dt and cfg.constraint == _native.CONSTRAINT["ts0"]
+                    and cfg.error == _native.ERROR["residual_std"] and cfg.strategy == _native.STRATEGY["filter"]
+                    and cfg.field < _native.FIELD_USER_BASE)
+        return _ISO_THREAD + (_ISO_LANES if lanes_ok else [])
     if cfg.ssm == _native.SSM["dense"]:
         return _DENSE_THREAD + (_DENSE_LANES if cfg.error == _native.ERROR["residual_std"] else [])
     return [(0, 0)]

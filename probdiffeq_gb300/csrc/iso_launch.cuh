@@ -1,7 +1,6 @@
 // Template dispatch of the isotropic kernel over (precision, nu, interpolation).
 #pragma once
 
-#include "iso_pair.cuh"
 #include "iso_solver.cuh"
 #include "iso_warp.cuh"
 
@@ -91,46 +90,12 @@ cudaError_t launch_iso_precision(const IsoArgs& a, int nu, bool interp, cudaStre
   }
 }
 
-// Warp-specialised filter (iso_pair.cuh): 32 instances per CTA of two warps.
-template <typename T, int NU, class F, bool INTERP>
-cudaError_t launch_iso_pair_nu(const IsoArgs& a, cudaStream_t stream) {
-  cudaError_t e = ensure_stack<iso_pair_kernel<T, NU, F, INTERP>>();
-  if (e != cudaSuccess) return e;
-  const unsigned grid = unsigned((a.B + 31) / 32);
-  iso_pair_kernel<T, NU, F, INTERP><<<grid, 64, 0, stream>>>(a);
-  return cudaGetLastError();
-}
-
-template <typename T, class F>
-cudaError_t launch_iso_pair(const IsoArgs& a, int nu, bool interp, cudaStream_t stream) {
-#define PDQ_PAIR_NU(N) \
-  case N: return interp ? launch_iso_pair_nu<T, N, F, true>(a, stream) : launch_iso_pair_nu<T, N, F, false>(a, stream);
-  switch (nu) {
-    PDQ_PAIR_NU(1)
-    PDQ_PAIR_NU(2)
-    PDQ_PAIR_NU(3)
-    PDQ_PAIR_NU(4)
-    PDQ_PAIR_NU(5)
-    default: return cudaErrorInvalidValue;
-  }
-#undef PDQ_PAIR_NU
-}
-
 }  // namespace pdq
 
 // Per-(field, precision) entry points, each defined in its own translation
 // unit so the instantiations compile in parallel.
 #define PDQ_DECLARE_ISO_LAUNCH(NAME) \
   cudaError_t NAME(const pdq::IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block);
-// the warp-specialised filter of the same field and precision
-#define PDQ_DECLARE_ISO_PAIR_LAUNCH(NAME) \
-  cudaError_t NAME##_pair(const pdq::IsoArgs& a, int nu, bool interp, cudaStream_t stream);
-PDQ_DECLARE_ISO_PAIR_LAUNCH(pdq_launch_iso_lv_f32)
-PDQ_DECLARE_ISO_PAIR_LAUNCH(pdq_launch_iso_lv_f64)
-PDQ_DECLARE_ISO_PAIR_LAUNCH(pdq_launch_iso_vdp_f32)
-PDQ_DECLARE_ISO_PAIR_LAUNCH(pdq_launch_iso_vdp_f64)
-PDQ_DECLARE_ISO_PAIR_LAUNCH(pdq_launch_iso_fhn_f32)
-PDQ_DECLARE_ISO_PAIR_LAUNCH(pdq_launch_iso_fhn_f64)
 
 PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_lv_f32)
 PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_lv_f64)
@@ -149,9 +114,6 @@ PDQ_DECLARE_ISO_LAUNCH(pdq_launch_iso_fp_fhn_f64)
 #define PDQ_DEFINE_ISO_LAUNCH(NAME, T, F)                                                       \
   cudaError_t NAME(const pdq::IsoArgs& a, int nu, bool interp, cudaStream_t stream, int block) { \
     return pdq::launch_iso_precision<T, F>(a, nu, interp, stream, block);                       \
-  }                                                                                             \
-  cudaError_t NAME##_pair(const pdq::IsoArgs& a, int nu, bool interp, cudaStream_t stream) {     \
-    return pdq::launch_iso_pair<T, F>(a, nu, interp, stream);                                   \
   }
 
 #define PDQ_DEFINE_ISO_FP_LAUNCH(NAME, T, F)                                                    \

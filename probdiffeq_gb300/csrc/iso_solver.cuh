@@ -495,9 +495,8 @@ PDQ_D void joint_tail(T (&Z)[2 * n][n + 1], bool& ok) {
 // the first reflector, so the error estimate overlaps the rest.  Clears ok
 // when a sum of squares left the safe range (the caller then reruns the
 // attempt with iso_predict_chol and ts0_update).
-// The pieces of the joint predict-update (used in this order; a
-// warp-specialised kernel publishes the gain between the third and fourth):
-// the X rows of Z from L (independent of the noise scale) ...
+// The pieces of the joint predict-update, used in this order: the X rows of
+// Z from L (independent of the noise scale) ...
 template <typename T, int NU>
 PDQ_D void joint_x(const T (&L)[NU + 1][NU + 1], const T (&pinv)[NU + 1], T (&Z)[2 * (NU + 1)][NU + 2]) {
   constexpr int n = NU + 1;

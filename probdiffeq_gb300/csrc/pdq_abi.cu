@@ -224,26 +224,19 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.num_attempts = args->num_attempts;
     a.status = args->status;
     const bool interp = !c->clip_dt;
-    if (c->kernel_variant < 0 || c->kernel_variant > 4) return PDQ_ERROR_INVALID_VALUE;
+    if (c->kernel_variant < 0 || c->kernel_variant > 3) return PDQ_ERROR_INVALID_VALUE;
     // 0 (auto) and 1: one thread per instance; 2 / 3: the lane-cooperative
     // kernel (8 lanes per instance) with <= 128 / <= 85 registers per lane,
-    // for exact checkpoint landings only; 4: the warp-specialised filter (a
-    // covariance warp and a control warp per 32 instances), TS0 without
-    // damping and error_residual_std
-    const bool pair = c->kernel_variant == 4;
-    const bool warp = c->clip_dt && (c->kernel_variant == 2 || c->kernel_variant == 3);
-    if ((c->kernel_variant == 2 || c->kernel_variant == 3) && (!c->clip_dt || a.ts1 || a.state_error || fp))
-      return PDQ_ERROR_UNSUPPORTED;
-    if (pair && (a.ts1 || a.state_error || fp || c->damp != 0.0 || c->field >= PDQ_FIELD_USER_BASE))
-      return PDQ_ERROR_UNSUPPORTED;
+    // for exact checkpoint landings only
+    const bool warp = c->clip_dt && c->kernel_variant >= 2;
+    if (c->kernel_variant >= 2 && (!c->clip_dt || a.ts1 || a.state_error || fp)) return PDQ_ERROR_UNSUPPORTED;
     a.tan_params = args->u_mean_d_params;
     a.tan_y0 = args->u_mean_d_y0;
     a.tangents = (a.tan_params || a.tan_y0) ? 1 : 0;
     if (a.tangents && (a.ts1 || a.state_error || fp || c->kernel_variant >= 2 || c->field >= PDQ_FIELD_USER_BASE))
       return PDQ_ERROR_UNSUPPORTED;
     const int ipb = c->instances_per_block;
-    if (pair ? !(ipb == 0 || ipb == 32)
-             : (warp ? !(ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32) : !(ipb == 0 || ipb == 32 || ipb == 64)))
+    if (warp ? !(ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32) : !(ipb == 0 || ipb == 32 || ipb == 64))
       return PDQ_ERROR_INVALID_VALUE;
     a.instances_per_block = ipb;
     a.workspace = workspace;
@@ -266,25 +259,6 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
       if (warp) return PDQ_ERROR_UNSUPPORTED;
       err = pdq_launch_iso_user(a, c->field, f64, c->num_derivatives, interp, fp, stream, block);
       return err == cudaSuccess ? PDQ_SUCCESS : (err == cudaErrorInvalidSource ? PDQ_ERROR_COMPILE : PDQ_ERROR_CUDA);
-    }
-    if (pair) {
-      using PairLaunch = cudaError_t (*)(const pdq::IsoArgs&, int, bool, cudaStream_t);
-      PairLaunch launch_pair = nullptr;
-      switch (c->field) {
-        case PDQ_FIELD_LOTKA_VOLTERRA:
-          launch_pair = f64 ? pdq_launch_iso_lv_f64_pair : pdq_launch_iso_lv_f32_pair;
-          break;
-        case PDQ_FIELD_VAN_DER_POL:
-          launch_pair = f64 ? pdq_launch_iso_vdp_f64_pair : pdq_launch_iso_vdp_f32_pair;
-          break;
-        case PDQ_FIELD_FITZHUGH_NAGUMO:
-          launch_pair = f64 ? pdq_launch_iso_fhn_f64_pair : pdq_launch_iso_fhn_f32_pair;
-          break;
-        default:
-          return PDQ_ERROR_UNSUPPORTED;
-      }
-      err = launch_pair(a, c->num_derivatives, interp, stream);
-      return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
     }
     using IsoLaunch = cudaError_t (*)(const pdq::IsoArgs&, int, bool, cudaStream_t, int);
     IsoLaunch launch = nullptr;
