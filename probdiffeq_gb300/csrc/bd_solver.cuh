@@ -25,18 +25,10 @@
 //      and published in shared memory;  cluster barrier;
 //   3. every CTA sums the CL partials over DSMEM in rank order and takes the
 //      same accept/step decision.
-// The per-dimension state (mean n, lower Cholesky n(n+1)/2, and the low
-// parts of the mean's rows 0 and 1) lives in two scratch buffers in global
-// memory (L2-resident: 64 x 4096 x 16 floats is 17 MB per buffer),
-// coalesced across a warp's consecutive dimensions; the proposal is written
-// to the other buffer, so an accept is a parity flip.
-// Precision of the residual: the stencil's Laplacian amplifies the rounding
-// of u by 1/dx^2 (1.7e7 at d = 4096), so in float32 the residual u' - f(u)
-// that drives the error estimate has a noise floor far above its value at
-// rtol 1e-4, and the float32 solve took up to twice float64's steps.  The
-// float32 kernel therefore carries the mean's rows 0 and 1 as float pairs
-// (the extrapolation in increment form, as in the isotropic kernel) and
-// evaluates the stencil in float-pair arithmetic.
+// The per-dimension state (mean n, lower Cholesky n(n+1)/2) lives in two
+// scratch buffers in global memory (L2-resident: 64 x 4096 x 14 floats is
+// 15 MB per buffer), coalesced across a warp's consecutive dimensions; the
+// proposal is written to the other buffer, so an accept is a parity flip.
 // Time, step size and controller follow the isotropic kernel: Wide<T> time,
 // T controller, no float64 on the attempt path of the float32 kernel.
 //
@@ -131,19 +123,16 @@ PDQ_D void bd_cond_load(const T* base, int64_t stride, IsoBackward<T, NU, 1>& c)
   for (int i = 0; i < n; ++i) c.to[i] = base[(o++) * stride];
 }
 
-// Rows of a dimension's state: the mean (n), the lower Cholesky factor
-// (n(n+1)/2), the low parts of mean rows 0 and 1 (zero in float64).
 template <int NU>
 PDQ_HD constexpr int bd_state_rows() {
-  return (NU + 1) + (NU + 1) * (NU + 2) / 2 + 2;
+  return (NU + 1) + (NU + 1) * (NU + 2) / 2;
 }
 
 // Dynamic shared memory per CTA: staged means (n x dl), new terms and scales
-// (2 x dl), current scales (dl), the low parts of the staged rows 0 and 1
-// (2 x dl), in T.
+// (2 x dl), current scales (dl), in T.
 template <typename T, int NU>
 PDQ_HD size_t bd_smem_bytes(int dl) {
-  return size_t(NU + 1 + 5) * size_t(dl) * sizeof(T);
+  return size_t(NU + 1 + 3) * size_t(dl) * sizeof(T);
 }
 
 // Viscous Burgers with periodic central differences (the flux-form stencil
@@ -155,20 +144,10 @@ PDQ_D T burgers_f(T left, T mid, T right, T nu_visc, T inv_dx) {
   return -flux + nu_visc * lap;
 }
 
-// The same stencil in the wide type (float pairs for float32): the flux as
-// (r - l)(r + l), the scale factors 1/(4 dx) and 1/dx^2 as wide numbers.
-template <typename W>
-PDQ_D W burgers_f_wide(W left, W mid, W right, W nu_visc, W flux_scale, W lap_scale) {
-  const W flux = ((right - left) * (right + left)) * flux_scale;
-  const W lap = ((right + left) - (mid + mid)) * lap_scale;
-  return nu_visc * lap - flux;
-}
-
 template <typename T, int NU, bool FP = false>
 __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   constexpr int n = NU + 1;
   constexpr int NS = bd_state_rows<NU>();
-  constexpr int LO0 = NS - 2, LO1 = NS - 1;  // rows of the low parts of mean rows 0 and 1
   constexpr int CF = iso_cond_floats<NU, 1>();
   constexpr int OUT = 1;
   constexpr bool kNarrow = sizeof(T) == sizeof(float);
@@ -188,8 +167,6 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   T* newt = mps + n * dl;                   // [dl] whitened residual of the proposal (MLE)
   T* sig_new = newt + dl;                   // [dl] local scale of the proposal (dynamic)
   T* sig = sig_new + dl;                    // [dl] output scale of the current state
-  T* mps_lo0 = sig + dl;                    // [dl] low parts of the staged rows 0 and 1
-  T* mps_lo1 = mps_lo0 + dl;
   __shared__ W partial[2];                  // CTA partial sums (error norm), parity
   __shared__ W warp_sums[kBdThreads / 32];
 
@@ -203,9 +180,6 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
 
   const T nu_visc = T(a.params[inst]);
   const T inv_dx = T(d);
-  using WW = Wide<T>;
-  const WW nu_w = wide_from(a.params[inst], T(0));
-  const WW flux_scale = wide_from(0.25 * double(d), T(0)), lap_scale = wide_from(double(d) * double(d), T(0));
   const int S = a.S;
   const int S_out = a.terminal_only ? 1 : S;
   const double* save_at = a.save_at + inst * S;
@@ -238,21 +212,11 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
     __threadfence();
     cluster.sync();
   }
-  // to derivatives; Cholesky rows zero (exact initial coefficients); the
-  // wide rows: u0 and f(u0) from the float64 inputs
+  // to derivatives; Cholesky rows zero (exact initial coefficients)
   for (int jl = tid; jl < dl; jl += kBdThreads) {
     const int g = j0 + jl;
     for (int k = 0; k < n; ++k) st[k * d + g] = T(double(st[k * d + g]) * factorial(k));
     for (int r = n; r < NS; ++r) st[r * d + g] = T(0);
-    if constexpr (kNarrow) {
-      const int gl = (g - 1 + d) % d, gr = (g + 1) % d;
-      const double y = a.y0[inst * d + g], yl = a.y0[inst * d + gl], yr = a.y0[inst * d + gr];
-      const double idx = double(d);
-      const double f1 = -(yr * yr - yl * yl) * 0.25 * idx + double(a.params[inst]) * (yr - 2.0 * y + yl) * idx * idx;
-      st[LO0 * d + g] = T(y - double(T(y)));
-      st[1 * d + g] = T(f1);
-      st[LO1 * d + g] = T(f1 - double(T(f1)));
-    }
     mle_sum[g] = wide_from(0.0, T(0));
     sig[jl] = T(1);
     if constexpr (FP) {
@@ -296,8 +260,6 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       double* um = a.u_mean + (rec * d + g) * n;
       double* uc = a.u_chol + (rec * d + g) * n * n;
       for (int i = 0; i < n; ++i) um[i] = double(x[i * d + g]);
-      um[0] += double(x[LO0 * d + g]);
-      um[1] += double(x[LO1 * d + g]);
       for (int i = 0; i < n; ++i)
         for (int j = 0; j < n; ++j) uc[i * n + j] = (j <= i) ? double(x[(n + i * (i + 1) / 2 + j) * d + g]) : 0.0;
     }
@@ -355,20 +317,12 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
         T m[n];
 #pragma unroll
         for (int i = 0; i < n; ++i) m[i] = x[i * d + g];
-        // increment form mp_i = m_i + p_i sum_{k>i} A_ik pinv_k m_k, rows 0 and 1 wide
 #pragma unroll
         for (int i = 0; i < n; ++i) {
           T acc = T(0);
 #pragma unroll
-          for (int kk = i + 1; kk < n; ++kk) acc += T(iwp_a<NU>(i, kk)) * pinv[kk] * m[kk];
-          const T incr = p[i] * acc;
-          if (i < 2) {
-            const WW w = wide_pair(m[i], x[(i == 0 ? LO0 : LO1) * d + g]) + incr;
-            mps[i * dl + jl] = T(wide_hi(w));
-            (i == 0 ? mps_lo0 : mps_lo1)[jl] = T(wide_lo(w));
-          } else {
-            mps[i * dl + jl] = m[i] + incr;
-          }
+          for (int kk = i; kk < n; ++kk) acc += T(iwp_a<NU>(i, kk)) * pinv[kk] * m[kk];
+          mps[i * dl + jl] = p[i] * acc;
         }
       }
       cluster.sync();
@@ -376,8 +330,6 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       // ---- phase 2: stencil, calibration, predict, update, error partial ----
       const T* ex_left = cluster.map_shared_rank(mps, (rank - 1 + CL) % CL);
       const T* ex_right = cluster.map_shared_rank(mps, (rank + 1) % CL);
-      const T* ex_left_lo = cluster.map_shared_rank(mps_lo0, (rank - 1 + CL) % CL);
-      const T* ex_right_lo = cluster.map_shared_rank(mps_lo0, (rank + 1) % CL);
       W local = wide_from(0.0, T(0));
       T pinv_abs[n];
 #pragma unroll
@@ -387,16 +339,11 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
         const int g = j0 + jl;
         const T left = jl > 0 ? mps[jl - 1] : ex_left[dl - 1];
         const T right = jl < dl - 1 ? mps[jl + 1] : ex_right[0];
-        const T left_lo = jl > 0 ? mps_lo0[jl - 1] : ex_left_lo[dl - 1];
-        const T right_lo = jl < dl - 1 ? mps_lo0[jl + 1] : ex_right_lo[0];
         T mp[n];
 #pragma unroll
         for (int i = 0; i < n; ++i) mp[i] = mps[i * dl + jl];
-        const T mp_lo0 = mps_lo0[jl], mp_lo1 = mps_lo1[jl];
-        // the residual u' - f(u) at the extrapolated mean, stencil in the wide type
-        const WW fw = burgers_f_wide(wide_pair(left, left_lo), wide_pair(mp[0], mp_lo0), wide_pair(right, right_lo),
-                                     nu_w, flux_scale, lap_scale);
-        const T mobs = T(wide_hi(wide_pair(mp[OUT], mp_lo1) - fw));
+        const T f = burgers_f(left, mp[0], right, nu_visc, inv_dx);
+        const T mobs = mp[OUT] - f;
         // per-dimension residual_whitened_rms of fx.marginalise(apply_flat(m))
         const T sigma = dev_div(dev_abs(mobs), ell);
         const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma : T(1);
@@ -430,15 +377,7 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
         const T R_Y = ts0_update<T, NU, OUT>(Lp, damp, gain, Lnew, h0);
         T mnew[n];
 #pragma unroll
-        for (int i = 2; i < n; ++i) mnew[i] = mp[i] - gain[i] * mobs;
-        {
-          const WW w0 = wide_pair(mp[0], mp_lo0) + (-gain[0] * mobs);
-          const WW w1 = wide_pair(mp[1], mp_lo1) + (-gain[1] * mobs);
-          mnew[0] = T(wide_hi(w0));
-          mnew[1] = T(wide_hi(w1));
-          y[LO0 * d + g] = T(wide_lo(w0));
-          y[LO1 * d + g] = T(wide_lo(w1));
-        }
+        for (int i = 0; i < n; ++i) mnew[i] = mp[i] - gain[i] * mobs;
         // proposal -> the other buffer
 #pragma unroll
         for (int i = 0; i < n; ++i) y[i * d + g] = mnew[i];

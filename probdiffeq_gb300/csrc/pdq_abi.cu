@@ -132,7 +132,7 @@ pdq_status pdq_workspace_size(const pdq_config* c, int64_t num_instances, int32_
   if (c->ssm == PDQ_SSM_BLOCKDIAG) {
     const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
     const int nu = c->num_derivatives;
-    const size_t rows = size_t(nu + 1) + size_t(nu + 1) * (nu + 2) / 2 + 2;  // + low parts of mean rows 0, 1
+    const size_t rows = size_t(nu + 1) + size_t(nu + 1) * (nu + 2) / 2;
     *bytes = 2 * size_t(num_instances) * rows * size_t(c->ode_dim) * elem + size_t(num_instances) * c->ode_dim * 8;
     if (c->strategy == PDQ_STRATEGY_FIXEDPOINT) {
       // running conditionals (2 parity buffers) and one per checkpoint interval, per dimension
