@@ -11,7 +11,7 @@ template <typename T, int NU, class F>
 cudaError_t launch_lml_adj_fwd_nu(const LmlAdjArgs& aa, cudaStream_t stream) {
   cudaError_t e = ensure_stack<lml_plan_kernel<T, NU>>();
   if (e != cudaSuccess) return e;
-  lml_plan_kernel<T, NU><<<1, 32, 0, stream>>>(aa.base);
+  lml_plan_kernel<T, NU><<<1, kLmlPlanThreads, 0, stream>>>(aa.base);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = ensure_stack<lml_adj_fwd_kernel<T, NU, F>>();

@@ -10,7 +10,7 @@ cudaError_t launch_lml_nu(const LmlArgs& a, cudaStream_t stream) {
   // the shared covariance plan (skipped on the device when the workspace holds it already)
   cudaError_t e = ensure_stack<lml_plan_kernel<T, NU>>();
   if (e != cudaSuccess) return e;
-  lml_plan_kernel<T, NU><<<1, 32, 0, stream>>>(a);
+  lml_plan_kernel<T, NU><<<1, kLmlPlanThreads, 0, stream>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = ensure_stack<lml_kernel<T, NU, F>>();

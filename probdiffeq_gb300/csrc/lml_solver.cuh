@@ -243,197 +243,189 @@ PDQ_D void lml_marginalise(const LmlCond<T, P, NU, D>& c, const Dual<T, P> (&m)[
   }
 }
 
-// The covariance side of the forward pass, once for all samples (one thread).
+// Threads of the plan kernel's one block.
+constexpr int kLmlPlanThreads = 256;
+
+// The covariance side of the forward pass, once for all samples.  Thread 0
+// runs the recursion over the steps (it is sequential): the prior revert,
+// the merge into the running backward conditional and the update, in the
+// bulk type with the isotropic kernel's functions; for every step it leaves
+// the revert's A in the step's K slot.  Then the block forms K for all steps
+// in parallel, one observation interval per thread, in double: the running
+// conditional's A before the step is the product of the interval's
+// diag(Tv) A factors, recomputed by the interval's thread.
 template <typename T, int NU>
-__global__ void lml_plan_kernel(LmlArgs a) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+__global__ void __launch_bounds__(kLmlPlanThreads) lml_plan_kernel(LmlArgs a) {
+  if (blockIdx.x != 0) return;
   constexpr int n = NU + 1;
-  constexpr int OUT = 1;
-  using DT = Dual<T, 1>;
+  const int tid = threadIdx.x;
   double* key = reinterpret_cast<double*>(a.plan);
   const double want[7] = {1.2345678901234567e89, a.dt, a.damp, double(a.num_steps), double(a.save_every), double(NU),
                           double(sizeof(T))};
   const int num_obs = a.num_steps / a.save_every + 1;
   double* const std_copy = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(a.plan) +
                                                      lml_plan_std_offset(NU, a.num_steps, a.save_every, int(sizeof(T))));
-  bool same = key[7] == 1.0;
-  for (int i = 0; i < 7; ++i) same = same && __double_as_longlong(key[i]) == __double_as_longlong(want[i]);
-  for (int k = 0; same && k < num_obs; ++k) same = __double_as_longlong(std_copy[k]) == __double_as_longlong(a.std[k]);
-  if (same) return;
-  key[7] = 0.0;
+  __shared__ int s_same;
+  if (tid == 0) {
+    bool same = key[7] == 1.0;
+    for (int i = 0; i < 7; ++i) same = same && __double_as_longlong(key[i]) == __double_as_longlong(want[i]);
+    for (int k = 0; same && k < num_obs; ++k) same = __double_as_longlong(std_copy[k]) == __double_as_longlong(a.std[k]);
+    s_same = same ? 1 : 0;
+    if (!same) key[7] = 0.0;
+  }
+  __syncthreads();
+  if (s_same) return;
   T* const plan = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(a.plan) + kLmlPlanKeyBytes);
   T* const obs_tbl = plan + int64_t(a.num_steps) * lml_plan_step<NU>();
-
-  DT L[n][n];
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) L[i][j] = DT(T(0));
-  LmlCond<T, 1, NU, 1> bw;  // xi unused (means are per sample)
-  lml_cond_identity(bw);
   const T h = T(a.dt);
   T p[n], pinv[n];
   precon<T, NU>(h, p, pinv);
-  const T sq = dev_sqrt(dev_abs(h));
-  const T damp = T(a.damp);
-  for (int step = 1; step <= a.num_steps; ++step) {
-    T* tbl = plan + int64_t(step - 1) * lml_plan_step<NU>();
-    // revert (transition.revert(marginal))
-    DT M[2 * n][2 * n];
-    for (int r = 0; r < n; ++r)
-      for (int c = 0; c < n; ++c) {
-        M[r][c] = DT((r <= c) ? sq * T(a.q1[c][r]) : T(0));
-        M[r][n + c] = DT(T(0));
-        DT acc(T(0));
-        for (int k = c; k < n; ++k) acc = acc + T(iwp_a<NU>(c, k)) * (dev_abs(pinv[k]) * L[k][r]);
-        M[n + r][c] = acc;
-        M[n + r][n + c] = dev_abs(pinv[c]) * L[c][r];
-      }
-    qr_qconst<T, 1, 2 * n, 2 * n>(M);
-    DT Gt[n][n];
-    for (int col = 0; col < n; ++col)
-      for (int i = n - 1; i >= 0; --i) {
-        DT acc = M[i][n + col];
-        for (int k = i + 1; k < n; ++k) acc = acc - M[i][k] * Gt[k][col];
-        Gt[i][col] = acc / M[i][i];
-      }
-    LmlCond<T, 1, NU, 1> cn;
-    DT Lp[n][n];
+
+  if (tid == 0) {
+    T q1t[kMaxN][kMaxN];
+#pragma unroll
+    for (int i = 0; i < kMaxN; ++i)
+#pragma unroll
+      for (int j = 0; j < kMaxN; ++j) q1t[i][j] = T(a.q1[i][j]);
+    T L[n][n], m0[n][1];
+#pragma unroll
     for (int i = 0; i < n; ++i) {
-      for (int j = 0; j < n; ++j) {
-        cn.A[i][j] = Gt[j][i];
-        cn.X[i][j] = M[n + j][n + i];
-        Lp[i][j] = dual_abs_scale(p[i], M[j][i]);
-      }
-      cn.tl[i] = T(1) / p[i];
-      cn.to[i] = T(1) / pinv[i];
+      m0[i][0] = T(0);
+#pragma unroll
+      for (int j = 0; j < n; ++j) L[i][j] = T(0);
     }
-    // merge (ssm_impl_isotropic.py:91-105).  The offsets are linear in the
-    // mean m before the step: the revert's xi = (I - G^T A1) diag(p_inv) m and
-    // the merged xi += bw.A diag(Tv) xi_revert, so xi += K m with K formed here
-    T Tv[n];
-    for (int i = 0; i < n; ++i) Tv[i] = bw.tl[i] * cn.to[i];
-    T* const g_t = tbl;
-    T* const k_t = tbl + n;
-    {
+    IsoBackward<T, NU, 1> bw;  // xi unused (means are per sample)
+    iso_cond_identity(bw);
+    const T sq = dev_sqrt(dev_abs(h));
+    const T damp = T(a.damp);
+    for (int step = 1; step <= a.num_steps; ++step) {
+      T* const tbl = plan + int64_t(step - 1) * lml_plan_step<NU>();
+      // revert (transition.revert(marginal)), then merge (ssm_impl_isotropic.py:91-105)
+      IsoBackward<T, NU, 1> cn, merged;
+      T Lp[n][n];
+      iso_prior_revert<T, NU, 1>(q1t, m0, L, p, pinv, sq, Lp, cn);
+      iso_cond_merge(bw, cn, merged);
+      bw = merged;
+      // update (Givens, H = e_1): the gain and the corrected factor
+      T gain[n], Lnew[n][n];
+      ts0_update<T, NU, 1, false>(Lp, damp, gain, Lnew);
+#pragma unroll
+      for (int i = 0; i < n; ++i) {
+        tbl[i] = gain[i];
+#pragma unroll
+        for (int j = 0; j < n; ++j) {
+          tbl[n + i * n + j] = cn.A[i][j];  // replaced by K below
+          L[i][j] = Lnew[i][j];
+        }
+      }
+      // observation: the merged conditional goes to the table, reset
+      if (step % a.save_every == 0) {
+        T* o = obs_tbl + int64_t(step / a.save_every - 1) * lml_plan_obs<NU>();
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            o[i * n + j] = bw.A[i][j];
+            o[n * n + i * n + j] = bw.X[i][j];
+          }
+        for (int i = 0; i < n; ++i) {
+          o[2 * n * n + i] = bw.tl[i];
+          o[2 * n * n + n + i] = bw.to[i];
+        }
+        iso_cond_identity(bw);
+      }
+    }
+    // rv_at_t1: the terminal marginal through the (identity) conditional -- its factor
+    T rm[n][1], rL[n][n];
+    iso_cond_marginalise(bw, m0, L, rm, rL);
+    T* const term = obs_tbl + int64_t(num_obs - 1) * lml_plan_obs<NU>();
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) term[i * n + j] = rL[i][j];
+    // the backward pass's covariance side: marginalise through each stored
+    // conditional, then bayes_rule with to_derivative(0, std_k) (one Givens
+    // rotation: the update of coefficient 0 with noise std_k)
+    T* const bay = term + n * n;
+    for (int k = num_obs - 1; k >= 0; --k) {
+      if (k < num_obs - 1) {
+        IsoBackward<T, NU, 1> c;
+        const T* o = obs_tbl + int64_t(k) * lml_plan_obs<NU>();
+        for (int i = 0; i < n; ++i) {
+          for (int j = 0; j < n; ++j) {
+            c.A[i][j] = o[i * n + j];
+            c.X[i][j] = o[n * n + i * n + j];
+          }
+          c.xi[i][0] = T(0);
+          c.tl[i] = o[2 * n * n + i];
+          c.to[i] = o[2 * n * n + n + i];
+        }
+        T pm[n][1], pL[n][n];
+        iso_cond_marginalise(c, m0, rL, pm, pL);
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) rL[i][j] = pL[i][j];
+      }
+      T g[n], Lc[n][n];
+      const T ry = ts0_update<T, NU, 0, false>(rL, T(a.std[k]), g, Lc);
+      bay[k * (n + 1)] = ry;
+      std_copy[num_obs + k] = log(double(ry < T(0) ? -ry : ry));  // log|ry| in double
+      for (int i = 0; i < n; ++i) bay[k * (n + 1) + 1 + i] = g[i];
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) rL[i][j] = Lc[i][j];
+    }
+  }
+  __syncthreads();
+
+  // K per step, one observation interval per thread: the offsets are linear
+  // in the mean m before the step -- the revert's xi = (I - G^T A1) diag(p_inv) m,
+  // merged as xi += bw.A diag(Tv) xi_revert -- so xi += K m with
+  // K = bw.A diag(Tv) (I - G^T A1) diag(p_inv), bw.A the running
+  // conditional's A before the step (identity after an observation) and
+  // Tv = bw.tl * cn.to (bw.tl = 1 after an observation, else the previous
+  // step's to_latent 1 / p).
+  const int num_seg = (a.num_steps + a.save_every - 1) / a.save_every;
+  for (int q = tid; q < num_seg; q += blockDim.x) {
+    double bA[n][n];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) bA[i][j] = (i == j) ? 1.0 : 0.0;
+    const int s0 = q * a.save_every + 1;
+    const int s1 = min(a.num_steps, (q + 1) * a.save_every);
+    for (int step = s0; step <= s1; ++step) {
+      T* const k_t = plan + int64_t(step - 1) * lml_plan_step<NU>() + n;
+      double G[n][n];  // the revert's A (= G^T)
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) G[i][j] = double(k_t[i * n + j]);
+      double Tv[n];
+      for (int i = 0; i < n; ++i) {
+        const T tl = (step == s0) ? T(1) : T(1) / p[i];
+        Tv[i] = double(tl * (T(1) / pinv[i]));
+      }
       double C[n][n];  // (I - G^T A1) diag(p_inv)
       for (int k = 0; k < n; ++k)
         for (int j = 0; j < n; ++j) {
           double acc = (k == j) ? 1.0 : 0.0;
-          for (int l = 0; l <= j; ++l) acc -= double(cn.A[k][l].v) * double(iwp_a<NU>(l, j));
+          for (int l = 0; l <= j; ++l) acc -= G[k][l] * double(iwp_a<NU>(l, j));
           C[k][j] = acc * double(pinv[j]);
         }
+      double nA[n][n];
       for (int i = 0; i < n; ++i)
         for (int j = 0; j < n; ++j) {
-          double acc = 0.0;
-          for (int k = 0; k < n; ++k) acc += double(bw.A[i][k].v) * double(Tv[k]) * C[k][j];
-          k_t[i * n + j] = T(acc);
-        }
-    }
-    {
-      DT Mm[2 * n][n];
-      LmlCond<T, 1, NU, 1> out;
-      for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) {
-          DT g(T(0)), r1(T(0));
+          double acc = 0.0, accA = 0.0;
           for (int k = 0; k < n; ++k) {
-            g = g + bw.A[i][k] * (Tv[k] * cn.A[k][j]);
-            r1 = r1 + bw.A[i][k] * (dev_abs(Tv[k]) * cn.X[k][j]);
+            acc += bA[i][k] * Tv[k] * C[k][j];
+            accA += bA[i][k] * Tv[k] * G[k][j];
           }
-          out.A[i][j] = g;
-          Mm[j][i] = r1;
-          Mm[n + j][i] = bw.X[i][j];
+          k_t[i * n + j] = T(acc);
+          nA[i][j] = accA;
         }
-      qr_qconst<T, 1, 2 * n, n>(Mm);
-      for (int i = 0; i < n; ++i) {
-        for (int j = 0; j < n; ++j) out.X[i][j] = Mm[j][i];
-        out.tl[i] = cn.tl[i];
-        out.to[i] = bw.to[i];
-      }
-      for (int i = 0; i < n; ++i) {
-        for (int j = 0; j < n; ++j) {
-          bw.A[i][j] = out.A[i][j];
-          bw.X[i][j] = out.X[i][j];
-        }
-        bw.tl[i] = out.tl[i];
-        bw.to[i] = out.to[i];
-      }
-    }
-    // update (Givens, H = e_1): the gain and the corrected factor
-    DT Mu[n + 1][n + 1];
-    for (int c = 0; c <= n; ++c) Mu[0][c] = DT(c == 0 ? damp : T(0));
-    for (int r = 1; r <= n; ++r) {
-      Mu[r][0] = Lp[OUT][r - 1];
-      for (int c = 1; c <= n; ++c) Mu[r][c] = Lp[c - 1][r - 1];
-    }
-    for (int r = OUT + 1; r >= 1; --r) givens_qconst<T, 1, n + 1, n + 1>(Mu, r - 1, r, 0);
-    for (int c = 1; c <= OUT; ++c) givens_qconst<T, 1, n + 1, n + 1>(Mu, c, c + 1, c);
-    for (int i = 0; i < n; ++i) {
-      const DT g = Mu[0][i + 1] / Mu[0][0];
-      g_t[i] = g.v;
-      for (int j = 0; j < n; ++j) L[i][j] = Mu[j + 1][i + 1];
-    }
-    // observation: the merged conditional goes to the table, reset
-    if (step % a.save_every == 0) {
-      T* o = obs_tbl + int64_t(step / a.save_every - 1) * lml_plan_obs<NU>();
       for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) {
-          o[i * n + j] = bw.A[i][j].v;
-          o[n * n + i * n + j] = bw.X[i][j].v;
-        }
-      for (int i = 0; i < n; ++i) {
-        o[2 * n * n + i] = bw.tl[i];
-        o[2 * n * n + n + i] = bw.to[i];
-      }
-      lml_cond_identity(bw);
+        for (int j = 0; j < n; ++j) bA[i][j] = nA[i][j];
     }
   }
-  // rv_at_t1: the terminal marginal through the (identity) conditional -- its factor
-  DT m0[n][1], rm[n][1], rL[n][n];
-  for (int i = 0; i < n; ++i) m0[i][0] = DT(T(0));
-  lml_marginalise<T, 1, NU, 1>(bw, m0, L, rm, rL);
-  T* const term = obs_tbl + int64_t(num_obs - 1) * lml_plan_obs<NU>();
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) term[i * n + j] = rL[i][j].v;
-  // the backward pass's covariance side: marginalise through each stored
-  // conditional, then bayes_rule with to_derivative(0, std_k) (Givens)
-  T* const bay = term + n * n;
-  for (int k = num_obs - 1; k >= 0; --k) {
-    if (k < num_obs - 1) {
-      LmlCond<T, 1, NU, 1> c;
-      const T* o = obs_tbl + int64_t(k) * lml_plan_obs<NU>();
-      for (int i = 0; i < n; ++i) {
-        for (int j = 0; j < n; ++j) {
-          c.A[i][j] = DT(o[i * n + j]);
-          c.X[i][j] = DT(o[n * n + i * n + j]);
-        }
-        c.xi[i][0] = DT(T(0));
-        c.tl[i] = o[2 * n * n + i];
-        c.to[i] = o[2 * n * n + n + i];
-      }
-      DT pm[n][1], pL[n][n];
-      lml_marginalise<T, 1, NU, 1>(c, m0, rL, pm, pL);
-      for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) rL[i][j] = pL[i][j];
-    }
-    const T sk = T(a.std[k]);
-    DT Mo[n + 1][n + 1];
-    for (int c = 0; c <= n; ++c) Mo[0][c] = DT(c == 0 ? sk : T(0));
-    for (int r = 1; r <= n; ++r) {
-      Mo[r][0] = rL[0][r - 1];
-      for (int c = 1; c <= n; ++c) Mo[r][c] = rL[c - 1][r - 1];
-    }
-    givens_qconst<T, 1, n + 1, n + 1>(Mo, 0, 1, 0);
-    const DT ry = Mo[0][0];
-    bay[k * (n + 1)] = ry.v;
-    std_copy[num_obs + k] = log(double(ry.v < T(0) ? -ry.v : ry.v));  // log|ry| in double
-    for (int i = 0; i < n; ++i) bay[k * (n + 1) + 1 + i] = (Mo[0][i + 1] / ry).v;
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) rL[i][j] = Mo[j + 1][i + 1];
+  __syncthreads();
+  if (tid == 0) {
+    for (int k = 0; k < num_obs; ++k) std_copy[k] = a.std[k];
+    __threadfence();
+    for (int i = 0; i < 7; ++i) key[i] = want[i];
+    __threadfence();
+    key[7] = 1.0;
   }
-  for (int k = 0; k < num_obs; ++k) std_copy[k] = a.std[k];
-  __threadfence();
-  for (int i = 0; i < 7; ++i) key[i] = want[i];
-  __threadfence();
-  key[7] = 1.0;
 }
 
 template <typename T, int NU, class F>

@@ -72,10 +72,11 @@ static int run(FILE* in, long long B, int N, int se, int C, int avg) {
   aa.grad_y0 = gy0.data();
   aa.res = res;
 
-  blockDim = {uint32_t(kLmlThreads), 1, 1};
+  blockDim = {1, 1, 1};  // the plan kernel's block as one thread
   blockIdx = {0, 0, 0};
   threadIdx = {0, 0, 0};
   lml_plan_kernel<T, NU>(a);
+  blockDim = {uint32_t(kLmlThreads), 1, 1};
   const long long padded = (B + kLmlThreads - 1) / kLmlThreads * kLmlThreads;  // the launch's grid
   for (int pass = 0; pass < 2; ++pass)
     for (long long t = 0; t < padded; ++t) {

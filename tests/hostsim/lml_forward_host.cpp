@@ -64,10 +64,11 @@ static int run(FILE* in, long long B, int N, int se, int avg) {
   a.plan = plan;
   a.workspace = ws;
 
-  blockDim = {uint32_t(kLmlThreads), 1, 1};
+  blockDim = {1, 1, 1};  // the plan kernel's block as one thread
   blockIdx = {0, 0, 0};
   threadIdx = {0, 0, 0};
   lml_plan_kernel<double, NU>(a);
+  blockDim = {uint32_t(kLmlThreads), 1, 1};
   const long long threads = B * P;
   const long long padded = (threads + kLmlThreads - 1) / kLmlThreads * kLmlThreads;  // the launch's grid
   for (long long t = 0; t < padded; ++t) {
