@@ -353,6 +353,16 @@ def alloc_outputs(cfg, B, S, terminal_only, device, posterior=False, num_params=
             }
     elif cfg.ssm == SSM["blockdiag"]:
         mean_shape, chol_shape = (B, S_out, d, n), (B, S_out, d, n, n)
+        if posterior:
+            extra = {
+                "cond_A": torch.empty((B, S - 1, d, n, n), **f64),
+                "cond_noise_mean": torch.empty((B, S - 1, d, n), **f64),
+                "cond_noise_chol": torch.empty((B, S - 1, d, n, n), **f64),
+                "cond_to_latent": torch.empty((B, S - 1, d, n), **f64),
+                "cond_to_observed": torch.empty((B, S - 1, d, n), **f64),
+                "filter_mean": torch.empty((B, S, d, n), **f64),
+                "filter_chol": torch.empty((B, S, d, n, n), **f64),
+            }
     else:
         mean_shape, chol_shape = (B, S_out, n, d), (B, S_out, n, n)
         if posterior:

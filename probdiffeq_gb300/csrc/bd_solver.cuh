@@ -80,6 +80,16 @@ struct BdArgs {
   int32_t* status;
   void* workspace;       // 2 state buffers (B, ns, d) in T, then MLE sums (B, d), 8 bytes each;
                          // FP: then 2 conditional buffers (B, cf, d) and the checkpoints' (B, S - 1, cf, d) in T
+  // optional fixed-point outputs (nullptr: not written): the posterior's
+  // backward conditionals between consecutive checkpoints, per dimension,
+  // in the reference's block-diagonal layout, and the filtering marginals
+  double* cond_A;            // (B, S - 1, d, n, n)
+  double* cond_noise_mean;   // (B, S - 1, d, n)
+  double* cond_noise_chol;   // (B, S - 1, d, n, n), calibrated
+  double* cond_to_latent;    // (B, S - 1, d, n)
+  double* cond_to_observed;  // (B, S - 1, d, n)
+  double* filter_mean;       // (B, S, d, n)
+  double* filter_chol;       // (B, S, d, n, n), calibrated
 };
 
 // Conditional of one dimension in a strided buffer (element e of dimension g at e * d + g).
@@ -268,6 +278,21 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       a.num_steps[rec] = num_steps;
     }
   };
+  // FP: the filtering marginal at checkpoint s (the state, before the
+  // calibration, which the finalize step applies)
+  auto write_filter = [&](int s) {
+    if (!a.filter_mean) return;
+    const T* x = bufs[cur];
+    const int64_t rec = inst * S + s;
+    for (int jl = tid; jl < dl; jl += kBdThreads) {
+      const int g = j0 + jl;
+      double* fm = a.filter_mean + (rec * d + g) * n;
+      double* fc = a.filter_chol + (rec * d + g) * n * n;
+      for (int i = 0; i < n; ++i) fm[i] = double(x[i * d + g]);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) fc[i * n + j] = (j <= i) ? double(x[(n + i * (i + 1) / 2 + j) * d + g]) : 0.0;
+    }
+  };
   auto write_scale = [&](int s_out) {
     const int64_t rec = inst * S_out + s_out;
     for (int jl = tid; jl < dl; jl += kBdThreads) a.output_scale[rec * d + j0 + jl] = double(sig[jl]);
@@ -277,6 +302,7 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
     write_checkpoint(0, wide_value(t));
     for (int jl = tid; jl < dl; jl += kBdThreads) a.output_scale[(inst * S_out) * d + j0 + jl] = 1.0;
   }
+  if (FP) write_filter(0);
 
   for (int s = 1; s < S && status == PDQ_INSTANCE_OK; ++s) {
     const W t_next = wide_from(save_at[s], T(0));
@@ -452,6 +478,7 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       if (a.solver != PDQ_SOLVER_MLE) write_scale(s_out);
     }
     if constexpr (FP) {
+      write_filter(s);
       // close the checkpoint's conditional, reset (estimators_and_losses.py:534-547)
       IsoBackward<T, NU, 1> c, id;
       iso_cond_identity(id);
@@ -480,6 +507,32 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
 #pragma unroll 1
       for (int jl = tid; jl < dl; jl += kBdThreads) {
         const int g = j0 + jl;
+        // the posterior's conditionals (the reference's block-diagonal
+        // representation per dimension, ssm_impl_blockdiag.py:16-113: the
+        // revert and merge produce the same A, noise mean, noise factor,
+        // to_latent and to_observed per dimension as the isotropic pieces);
+        // the noise factor calibrated like the marginals
+        if (a.cond_A) {
+          double cal = 1.0;
+          if (a.solver == PDQ_SOLVER_MLE) {
+            cal = num_data > 0 ? sqrt(wide_value(mle_sum[g]) / num_data) : 0.0;
+            if (a.correct) cal /= sqrt(double(num_steps));
+          }
+          for (int s = 1; s < S; ++s) {
+            IsoBackward<T, NU, 1> c;
+            bd_cond_load<T, NU>(ckpt + int64_t(s - 1) * CF * d + g, d, c);
+            const int64_t cr = (inst * (S - 1) + (s - 1)) * d + g;
+            for (int i = 0; i < n; ++i) {
+              for (int j = 0; j < n; ++j) {
+                a.cond_A[cr * n * n + i * n + j] = double(c.A[i][j]);
+                a.cond_noise_chol[cr * n * n + i * n + j] = double(c.X[i][j]) * cal;
+              }
+              a.cond_noise_mean[cr * n + i] = double(c.xi[i][0]);
+              a.cond_to_latent[cr * n + i] = double(c.tl[i]);
+              a.cond_to_observed[cr * n + i] = double(c.to[i]);
+            }
+          }
+        }
         // the terminal state itself: the last checkpoint reset the running conditional
         T rm[n][1], rL[n][n];
 #pragma unroll
@@ -520,6 +573,16 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
         double* uc = a.u_chol + (rec * d + g) * n * n;
         for (int q = 0; q < n * n; ++q) uc[q] *= sc;
       }
+    }
+    if (FP && a.filter_chol) {
+      for (int s = 0; s < S; ++s)
+        for (int jl = tid; jl < dl; jl += kBdThreads) {
+          const int g = j0 + jl;
+          double sc = num_data > 0 ? sqrt(wide_value(mle_sum[g]) / num_data) : 0.0;
+          if (a.correct) sc /= sqrt(double(last));
+          double* fc = a.filter_chol + ((inst * S + s) * d + g) * n * n;
+          for (int q = 0; q < n * n; ++q) fc[q] *= sc;
+        }
     }
   }
   if (status != PDQ_INSTANCE_OK) {

@@ -288,9 +288,12 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
     if (c->strategy != PDQ_STRATEGY_FILTER && c->strategy != PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_INVALID_VALUE;
     if (!c->clip_dt) return PDQ_ERROR_UNSUPPORTED;  // checkpoints by exact landing only
-    if (args->cond_A || args->cond_noise_mean || args->cond_noise_chol || args->cond_to_latent ||
-        args->cond_to_observed || args->filter_mean || args->filter_chol)
-      return PDQ_ERROR_UNSUPPORTED;  // the posterior's conditionals stay in the workspace
+    const bool any_post = args->cond_A || args->cond_noise_mean || args->cond_noise_chol || args->cond_to_latent ||
+                          args->cond_to_observed || args->filter_mean || args->filter_chol;
+    const bool all_post = args->cond_A && args->cond_noise_mean && args->cond_noise_chol && args->cond_to_latent &&
+                          args->cond_to_observed && args->filter_mean && args->filter_chol;
+    if (any_post && c->strategy != PDQ_STRATEGY_FIXEDPOINT) return PDQ_ERROR_UNSUPPORTED;  // a smoother's posterior
+    if (any_post && !all_post) return PDQ_ERROR_INVALID_VALUE;
     if (c->num_derivatives < 2 || c->num_derivatives > 4) return PDQ_ERROR_UNSUPPORTED;
     const int d = c->ode_dim;
     if (d < 3) return PDQ_ERROR_INVALID_VALUE;
@@ -312,6 +315,15 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.ts1 = c->constraint == PDQ_CONSTRAINT_TS1 ? 1 : 0;
     a.state_error = c->error == PDQ_ERROR_STATE_STD ? 1 : 0;
     a.fixedpoint = c->strategy == PDQ_STRATEGY_FIXEDPOINT ? 1 : 0;
+    if (any_post) {
+      a.cond_A = args->cond_A;
+      a.cond_noise_mean = args->cond_noise_mean;
+      a.cond_noise_chol = args->cond_noise_chol;
+      a.cond_to_latent = args->cond_to_latent;
+      a.cond_to_observed = args->cond_to_observed;
+      a.filter_mean = args->filter_mean;
+      a.filter_chol = args->filter_chol;
+    }
     a.safety = c->safety;
     a.factor_min = c->factor_min;
     a.factor_max = c->factor_max;
