@@ -5,8 +5,8 @@
   with each factorisation's apply_flat / sample_flat) on the same
   conditionals and normal draws, for the isotropic, dense and block-diagonal
   factorisations (float64, 1e-10 of the largest sample entry: summation
-  order only).  Block-diagonal solutions run on the isotropic kernel as
-  B * d one-dimensional instances.
+  order only; 1e-9 block-diagonal).  Block-diagonal solutions run on the
+  isotropic kernel as B * d one-dimensional instances.
 * Samples reproduce the smoothed marginals: over 40000 samples the sample
   mean and std of every Taylor coefficient at every checkpoint match the
   solution's marginals (mean within 5 standard errors, std within 3 %).
@@ -94,7 +94,9 @@ def test_sampling_recursion_matches_the_oracle(ssm):
     torch.cuda.synchronize()
     ref = _oracle_samples(out, z, ssm)
     err = float((smp.cpu() - ref).abs().max() / ref.abs().max())
-    assert err < 1e-10, err  # summation order only
+    # summation order only; block-diagonal: the noise mean is scaled by
+    # to_observed before the isotropic kernel adds it (one more rounding)
+    assert err < (1e-9 if ssm == "blockdiag" else 1e-10), err
 
 
 @pytest.mark.parametrize("ssm", ["isotropic", "dense", "blockdiag"])
