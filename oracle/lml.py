@@ -14,11 +14,14 @@ import torch
 
 def lml_value_and_grads(theta, y0, data, dt, num_steps, save_every, std, average_pdfs=False, field="fitzhugh_nagumo",
                         num_derivatives=3):
-    """Returns (lml, d lml / d theta, d lml / d y0) as (float, ndarray, ndarray)."""
+    """Returns (lml, d lml / d theta, d lml / d y0) as (float, ndarray, ndarray).
+
+    ``field`` names a field of ``oracle.problems.FIELDS`` or is a callable
+    f(u, params) written with ``oracle.problems.stack``."""
     from oracle import linalg, problems, solvers, ssm
 
     linalg.set_qr_derivative("reference")
-    fn = problems.FIELDS[field]
+    fn = field if callable(field) else problems.FIELDS[field]
     th = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
     u0 = torch.tensor(y0, dtype=torch.float64, requires_grad=True)
     tc = problems.taylor_derivatives(fn, u0, th, num_derivatives)

@@ -40,6 +40,8 @@ EMBEDDED_HEADERS = [
     ("pdq_device.cuh", os.path.join(CSRC, "pdq_device.cuh")),
     ("iso_solver.cuh", os.path.join(CSRC, "iso_solver.cuh")),
     ("dense_solver.cuh", os.path.join(CSRC, "dense_solver.cuh")),
+    ("lml_solver.cuh", os.path.join(CSRC, "lml_solver.cuh")),
+    ("lml_adjoint.cuh", os.path.join(CSRC, "lml_adjoint.cuh")),
 ]
 
 

@@ -34,6 +34,7 @@
 #include "pdq_nvtx.h"
 #include "dense_solver.cuh"
 #include "iso_solver.cuh"
+#include "lml_adjoint.cuh"
 #include "nvrtc_fields.h"
 #include "pdq.h"
 #include "pdq_embedded_headers.inc"  // kPdqHeaderCount, kPdqHeaderNames, kPdqHeaderSources (generated)
@@ -70,6 +71,20 @@ std::string kernel_expression(bool f64, int nu, bool interp, bool fp, bool gen) 
 std::string dense_expression(bool f64, int nu, bool ts1, bool fp) {
   return std::string("pdq::dense_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
          ", pdq_user::Field, " + tf(ts1) + ", " + tf(fp) + ">";
+}
+
+// The LML kernels of a user field: the covariance plan (field-independent,
+// compiled into the same module) and the per-sample kernels.
+std::vector<std::string> lml_expressions(bool f64, int nu, bool adjoint) {
+  const std::string T = f64 ? "double" : "float", N = std::to_string(nu);
+  std::vector<std::string> e = {"pdq::lml_plan_kernel<" + T + ", " + N + ">"};
+  if (adjoint) {
+    e.push_back("pdq::lml_adj_fwd_kernel<" + T + ", " + N + ", pdq_user::Field>");
+    e.push_back("pdq::lml_adj_bwd_kernel<" + T + ", " + N + ", pdq_user::Field>");
+  } else {
+    e.push_back("pdq::lml_kernel<" + T + ", " + N + ", pdq_user::Field>");
+  }
+  return e;
 }
 
 void copy_log(const std::string& text, char* log, size_t log_bytes) {
@@ -193,6 +208,49 @@ cudaError_t user_kernel(UserField* f, const std::string& expression, const char*
   return cudaSuccess;
 }
 
+// The kernels for `expressions` (one module compiled with `header`), loaded on first use.
+cudaError_t user_kernels(UserField* f, const std::vector<std::string>& expressions, const char* header,
+                         std::vector<cudaKernel_t>* out) {
+  std::lock_guard<std::mutex> lock(f->mu);
+  out->clear();
+  bool all = true;
+  for (const auto& e : expressions) {
+    auto it = f->kernels.find(e);
+    if (it == f->kernels.end()) {
+      all = false;
+      break;
+    }
+    out->push_back(it->second);
+  }
+  if (all) return cudaSuccess;
+  out->clear();
+  std::string cubin, text;
+  std::vector<std::string> lowered;
+  if (compile(f->source, expressions, &cubin, &lowered, &text, header) != PDQ_SUCCESS) return cudaErrorInvalidSource;
+  cudaLibrary_t lib = nullptr;
+  cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) return e;
+  f->libraries.push_back(lib);
+  for (size_t i = 0; i < expressions.size(); ++i) {
+    cudaKernel_t k = nullptr;
+    e = cudaLibraryGetKernel(&k, lib, lowered[i].c_str());
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes attr;
+    e = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(k));
+    if (e != cudaSuccess) return e;
+    size_t cur = 0;
+    e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
+    if (e != cudaSuccess) return e;
+    if (attr.localSizeBytes + 1024 > cur) {
+      e = cudaDeviceSetLimit(cudaLimitStackSize, attr.localSizeBytes + 1024);
+      if (e != cudaSuccess) return e;
+    }
+    f->kernels.emplace(expressions[i], k);
+    out->push_back(k);
+  }
+  return cudaSuccess;
+}
+
 }  // namespace
 
 cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, int nu, bool interp, bool fp,
@@ -222,4 +280,38 @@ cudaError_t pdq_launch_dense_user(const pdq::DenseArgs& a, int32_t field, bool f
   const int block = a.instances_per_block > 0 ? a.instances_per_block : 32;  // one thread per instance
   const unsigned grid = unsigned((a.B + block - 1) / block);
   return cudaLaunchKernel(reinterpret_cast<const void*>(kernel), dim3(grid), dim3(unsigned(block)), params, 0, stream);
+}
+
+cudaError_t pdq_launch_lml_user(const pdq::LmlArgs& a, int32_t field, bool f64, int nu, cudaStream_t stream) {
+  UserField* f = lookup(field);
+  if (f == nullptr || nu < 2 || nu > 3) return cudaErrorInvalidValue;
+  std::vector<cudaKernel_t> k;
+  cudaError_t e = user_kernels(f, lml_expressions(f64, nu, false), "lml_solver.cuh", &k);
+  if (e != cudaSuccess) return e;
+  pdq::LmlArgs args = a;
+  void* params[] = {&args};
+  e = cudaLaunchKernel(reinterpret_cast<const void*>(k[0]), dim3(1), dim3(pdq::kLmlPlanThreads), params, 0, stream);
+  if (e != cudaSuccess) return e;
+  const int64_t threads = a.B * a.lanes_per_sample;
+  const unsigned grid = unsigned((threads + pdq::kLmlThreads - 1) / pdq::kLmlThreads);
+  return cudaLaunchKernel(reinterpret_cast<const void*>(k[1]), dim3(grid), dim3(pdq::kLmlThreads), params, 0, stream);
+}
+
+cudaError_t pdq_launch_lml_adj_user(const pdq::LmlAdjArgs& aa, int32_t field, bool f64, int nu, bool backward,
+                                    cudaStream_t stream) {
+  UserField* f = lookup(field);
+  if (f == nullptr || nu < 2 || nu > 3) return cudaErrorInvalidValue;
+  std::vector<cudaKernel_t> k;
+  cudaError_t e = user_kernels(f, lml_expressions(f64, nu, true), "lml_adjoint.cuh", &k);
+  if (e != cudaSuccess) return e;
+  pdq::LmlAdjArgs args = aa;
+  void* params[] = {&args};
+  const unsigned grid = unsigned((aa.base.B + pdq::kLmlThreads - 1) / pdq::kLmlThreads);
+  if (backward)
+    return cudaLaunchKernel(reinterpret_cast<const void*>(k[2]), dim3(grid), dim3(pdq::kLmlThreads), params, 0, stream);
+  pdq::LmlArgs base = aa.base;
+  void* plan_params[] = {&base};
+  e = cudaLaunchKernel(reinterpret_cast<const void*>(k[0]), dim3(1), dim3(pdq::kLmlPlanThreads), plan_params, 0, stream);
+  if (e != cudaSuccess) return e;
+  return cudaLaunchKernel(reinterpret_cast<const void*>(k[1]), dim3(grid), dim3(pdq::kLmlThreads), params, 0, stream);
 }

@@ -6,6 +6,7 @@
 
 #include "dense_solver.cuh"
 #include "iso_solver.cuh"
+#include "lml_adjoint.cuh"
 
 // State dimension / number of parameters of a registered user field (0 / -1 if unknown).
 int pdq_user_field_dim(int32_t field);
@@ -19,3 +20,10 @@ cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, 
 // The same for the dense kernel (one thread per instance).
 cudaError_t pdq_launch_dense_user(const pdq::DenseArgs& a, int32_t field, bool f64, int nu, bool ts1, bool fp,
                                   cudaStream_t stream);
+
+// The LML kernels for a registered user field: forward-mode gradient
+// (pdq_lml_fixed_grid), and the adjoint pair's value / adjoint pass
+// (pdq_lml_fwd / pdq_lml_bwd); the covariance plan kernel from the same module.
+cudaError_t pdq_launch_lml_user(const pdq::LmlArgs& a, int32_t field, bool f64, int nu, cudaStream_t stream);
+cudaError_t pdq_launch_lml_adj_user(const pdq::LmlAdjArgs& aa, int32_t field, bool f64, int nu, bool backward,
+                                    cudaStream_t stream);

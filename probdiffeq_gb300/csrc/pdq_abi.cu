@@ -465,14 +465,22 @@ static pdq_status lml_check(const pdq_config* c, int64_t B, int32_t num_steps, i
       c->solver != PDQ_SOLVER_PLAIN)
     return PDQ_ERROR_UNSUPPORTED;
   if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
-  if (c->field != PDQ_FIELD_FITZHUGH_NAGUMO && c->field != PDQ_FIELD_LOTKA_VOLTERRA) return PDQ_ERROR_UNSUPPORTED;
+  const bool user = c->field >= PDQ_FIELD_USER_BASE;
+  if (user) {  // a registered run-time field of the configuration's dimension
+    if (pdq_user_field_dim(c->field) != c->ode_dim || pdq_user_field_params(c->field) < 1) return PDQ_ERROR_INVALID_VALUE;
+  } else if (c->field != PDQ_FIELD_FITZHUGH_NAGUMO && c->field != PDQ_FIELD_LOTKA_VOLTERRA) {
+    return PDQ_ERROR_UNSUPPORTED;
+  }
   if (c->instances_per_block != 0) return PDQ_ERROR_INVALID_VALUE;
   if (c->field == PDQ_FIELD_LOTKA_VOLTERRA && c->precision != PDQ_PRECISION_F64) return PDQ_ERROR_UNSUPPORTED;
   if (B < 0 || num_steps < 1 || save_every < 1 || num_steps % save_every != 0) return PDQ_ERROR_INVALID_VALUE;
   return PDQ_SUCCESS;
 }
 
-static int lml_num_params(const pdq_config* c) { return c->field == PDQ_FIELD_FITZHUGH_NAGUMO ? 3 : 4; }
+static int lml_num_params(const pdq_config* c) {
+  if (c->field >= PDQ_FIELD_USER_BASE) return pdq_user_field_params(c->field);
+  return c->field == PDQ_FIELD_FITZHUGH_NAGUMO ? 3 : 4;
+}
 
 // Workspace: the shared covariance plan (key + tables, rounded to 256 bytes),
 // then per thread (P threads per sample, one tangent each) the backward
@@ -533,6 +541,10 @@ pdq_status pdq_lml_fixed_grid(const pdq_config* c, const pdq_lml_args* args, voi
   a.workspace = static_cast<unsigned char*>(workspace) + lml_plan_bytes(c, args->num_steps, args->save_every);
   cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
   cudaError_t err;
+  if (c->field >= PDQ_FIELD_USER_BASE) {
+    err = pdq_launch_lml_user(a, c->field, c->precision == PDQ_PRECISION_F64, c->num_derivatives, stream);
+    return err == cudaSuccess ? PDQ_SUCCESS : (err == cudaErrorInvalidSource ? PDQ_ERROR_COMPILE : PDQ_ERROR_CUDA);
+  }
   if (c->field == PDQ_FIELD_FITZHUGH_NAGUMO)
     err = c->precision == PDQ_PRECISION_F64 ? pdq_launch_lml_fhn_f64(a, c->num_derivatives, stream)
                                             : pdq_launch_lml_fhn_f32(a, c->num_derivatives, stream);
@@ -620,6 +632,10 @@ static pdq_status lml_adj_launch(const pdq_config* c, const pdq_lml_adjoint_args
   aa.res = static_cast<unsigned char*>(workspace) + lml_plan_bytes(c, l.num_steps, l.save_every);
   cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
   cudaError_t err;
+  if (c->field >= PDQ_FIELD_USER_BASE) {
+    err = pdq_launch_lml_adj_user(aa, c->field, c->precision == PDQ_PRECISION_F64, c->num_derivatives, backward, stream);
+    return err == cudaSuccess ? PDQ_SUCCESS : (err == cudaErrorInvalidSource ? PDQ_ERROR_COMPILE : PDQ_ERROR_CUDA);
+  }
   if (c->field == PDQ_FIELD_FITZHUGH_NAGUMO)
     err = c->precision == PDQ_PRECISION_F64 ? pdq_launch_lml_adj_fhn_f64(aa, c->num_derivatives, backward, stream)
                                             : pdq_launch_lml_adj_fhn_f32(aa, c->num_derivatives, backward, stream);

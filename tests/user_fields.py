@@ -65,3 +65,18 @@ def lorenz(u, p):
 
     s, r, b = p[0], p[1], p[2]
     return stack([s * (u[1] - u[0]), u[0] * (r - u[2]) - u[1], u[0] * u[1] - b * u[2]])
+
+
+# FitzHugh--Nagumo, as the built-in field (the LML configuration's problem)
+FITZHUGH_NAGUMO = """
+struct Field {
+  static constexpr int D = 2;
+  static constexpr int P = 3;
+  template <typename S, typename T>
+  PDQ_HD static void eval(const S* u, const T* p, S* out) {
+    const T a = p[0], b = p[1], c = p[2];
+    out[0] = c * (u[0] - u[0] * u[0] * u[0] * (T(1) / T(3)) + u[1]);
+    out[1] = -(T(1) / c) * (u[0] - a - b * u[1]);
+  }
+};
+"""
