@@ -14,8 +14,9 @@ device-resident inputs (CUDA events on the launching stream, an L2 flush
 between steps outside the events); ``e2e`` times the public API
 (``probdiffeq_gb300.ensemble.solve_ensemble``) from pinned host inputs to
 pinned host outputs, copies included.  The same line carries the float64
-batch, the single-instance latencies (the plain per-instance method) and the
-LML-gradient throughput under ``secondary``.
+batch, the single-instance latencies (the plain per-instance method), the
+LML-gradient throughput and the block-diagonal Burgers configuration (64
+instances, d = 4096, t in [0, 1], float32, one solve) under ``secondary``.
 
 Other workloads, one JSON line each (``--workload``):
   lv_single          one LV instance, dynamic calibration, float64 and float32
@@ -392,6 +393,151 @@ def lml_cpu_baseline(samples=2):
                       f"CPU restatement), one process, {threads} torch threads", "seconds": dt}
 
 
+def measured_peaks():
+    """The measured peaks of this GPU pool (HBM copy GB/s, bf16 TF/s), or {}."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def measured_l2_copy_gbs(torch, device, mib=16, reps=200):
+    """Copy bandwidth of an L2-resident buffer pair (2 x 16 MiB, read + write
+    bytes), CUDA events over ``reps`` back-to-back copies: the ceiling of a
+    kernel whose working set stays in L2."""
+    a = torch.ones(mib * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        b.copy_(a)
+    e1.record()
+    e1.synchronize()
+    return 2 * a.numel() * 4 * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+
+BURGERS_BYTES_PER_DIM = 2 * 14 * 4 + 4  # float32 state row read + written, one f value
+
+
+def oracle_burgers_attempt_seconds(d_small=64, t1=0.05):
+    """Seconds per attempt of the oracle's block-diagonal Burgers solve
+    (PyTorch float64, per-dimension loop) at d = d_small, measured over the
+    solve on [0, t1] after the Taylor-mode start."""
+    import time
+
+    import torch
+
+    from oracle import problems, solvers, ssm
+    from probdiffeq_gb300 import configs
+
+    threads = torch.get_num_threads()
+    torch.set_num_threads(1)  # d = 64 tensors: one thread is the fastest setting
+    try:
+        p = torch.tensor([0.01], dtype=torch.float64)
+        u0 = torch.tensor(configs.burgers_u0(1, d_small)[0])
+        tc = problems.taylor_derivatives(problems.burgers, u0, p, 3)
+        S = ssm.BdSSM()
+        c = S.constraint_ode_ts0(lambda u, t: problems.burgers(u[0], p))
+        t = time.perf_counter()
+        res = solvers.solve_adaptive_terminal_values(solvers.SolverDynamic(solvers.StrategyFilter(), c),
+                                                     solvers.ErrorResidualStd(c), S.prior_wiener_integrated(tc), 0.0,
+                                                     t1, 1e-4, 1e-4, dt0=0.1 * t1)
+        sec = (time.perf_counter() - t) / res.num_attempts
+    finally:
+        torch.set_num_threads(threads)
+    return sec, res.num_attempts, 1
+
+
+def burgers_blockdiag_secondary(torch, _native, ensemble, device, t1=1.0, cpu=True):
+    """The high-dimensional block-diagonal configuration: 64 viscous Burgers
+    instances (nu = 0.01), periodic grid of d = 4096, t in [0, t1], IWP nu = 3,
+    TS0 blockdiag filter, dynamic calibration, rtol = atol = 1e-4, float32.
+
+    One solve (seconds long) after a warm-up on a short horizon: the initial
+    values are copied from pinned host memory, the solver runs, the terminal
+    means are copied back to pinned host memory, all on one stream; CUDA
+    events bracket the solver launch (``value``) and the whole step (``e2e``).
+    The per-instance state (2 x 14 floats per dimension, 14.7 MB per buffer)
+    stays in L2, so the roofline is taken against the measured L2 copy
+    bandwidth and, for reference, the measured HBM copy bandwidth."""
+    from probdiffeq_gb300 import configs
+
+    B, d = 64, 4096
+    stream = torch.cuda.current_stream()
+    h_u0 = torch.tensor(configs.burgers_u0(B, d), dtype=torch.float64).pin_memory()
+    h_prm = torch.full((B, 1), 0.01, dtype=torch.float64).pin_memory()
+    d_u0 = torch.empty(h_u0.shape, dtype=torch.float64, device=device)
+    d_prm = torch.empty(h_prm.shape, dtype=torch.float64, device=device)
+    cfg = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=d, ssm="blockdiag", solver="dynamic",
+                               precision="float32", atol=1e-4, rtol=1e-4, clip_dt=True, max_attempts=1 << 26)
+    outs = _native.alloc_outputs(cfg, B, 2, True, device)
+    h_mean = torch.empty(tuple(outs["u_mean"].shape), dtype=outs["u_mean"].dtype).pin_memory()
+
+    def span(t_end):
+        sa = torch.tensor([0.0, t_end], dtype=torch.float64, device=device).expand(B, 2).contiguous()
+        return sa, torch.full((B,), 0.1 * t_end, dtype=torch.float64, device=device)
+
+    sa_w, dt0_w = span(1e-4)
+    sa, dt0 = span(t1)
+    d_u0.copy_(h_u0)
+    d_prm.copy_(h_prm)
+    _native.solve_adaptive(cfg, sa_w, d_prm, d_u0, dt0_w, True, outs, stream=stream)  # warm-up
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    d_u0.copy_(h_u0, non_blocking=True)
+    d_prm.copy_(h_prm, non_blocking=True)
+    ev[1].record(stream)
+    _native.solve_adaptive(cfg, sa, d_prm, d_u0, dt0, True, outs, stream=stream)
+    ev[2].record(stream)
+    h_mean.copy_(outs["u_mean"], non_blocking=True)
+    ev[3].record(stream)
+    ev[3].synchronize()
+    t_kernel = ev[1].elapsed_time(ev[2]) / 1e3
+    t_e2e = ev[0].elapsed_time(ev[3]) / 1e3
+    attempts = outs["num_attempts"].to(torch.float64)
+    status_ok = int((outs["status"] == 0).sum())
+    finite = bool(torch.isfinite(h_mean).all())
+    bytes_alg = float(attempts.sum()) * d * BURGERS_BYTES_PER_DIM
+    achieved = bytes_alg / t_kernel / 1e9
+    l2 = measured_l2_copy_gbs(torch, device)
+    hbm = measured_peaks().get("hbm_gbs")
+    out = {
+        "config": {"workload": "burgers_blockdiag", "instances": B, "d": d, "nu_visc": 0.01, "t_span": [0.0, t1],
+                   "num_derivatives": 3, "ssm": "blockdiag", "constraint": "ts0", "strategy": "filter",
+                   "solver": "dynamic", "rtol": 1e-4, "atol": 1e-4, "output": "terminal values (clip_dt)",
+                   "precision": "float32", "steps": 1, "warmup": "one solve on [0, 1e-4]",
+                   "l2": "state L2-resident by design; not flushed"},
+        "value": B / t_kernel, "unit": "solves/s", "ms_per_step": 1e3 * t_kernel,
+        "e2e": {"value": B / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h_u0.numel() * 8 + h_prm.numel() * 8,
+                "d2h_bytes_per_step": h_mean.numel() * h_mean.element_size()},
+        "stats": {"attempts_max": int(attempts.max()), "attempts_mean": float(attempts.mean()),
+                  "us_per_attempt_slowest": 1e6 * t_kernel / float(attempts.max()), "status_ok": status_ok,
+                  "terminal_means_finite": finite},
+        "roofline": {"bound": "l2", "achieved": achieved, "unit": "GB/s", "peak": l2, "frac": achieved / l2,
+                     "peak_source": "measured L2-resident copy (2 x 16 MiB, read + write bytes) on this GPU",
+                     "hbm_peak": hbm, "frac_of_hbm": (achieved / hbm) if hbm else None,
+                     "bytes_per_attempt_dimension": BURGERS_BYTES_PER_DIM,
+                     "note": "algorithmic bytes = sum over instances of attempts x d x (2 x 14 x 4 B + 4 B); "
+                             "averaged over the launch, in which instances finish at different times"},
+        "gpu_launches": 1,
+    }
+    if cpu:
+        sec, n_att, threads = oracle_burgers_attempt_seconds()
+        per_attempt = sec * d / 64
+        out["cpu_baseline"] = {
+            "value": 1.0 / (per_attempt * float(attempts.mean())), "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"oracle (PyTorch float64 CPU restatement, per-dimension loop) at d = 64 over t in [0, 0.05] "
+                      f"({n_att} attempts, {1e3 * sec:.1f} ms each), scaled x64 to d = 4096 and multiplied by this "
+                      f"run's mean attempts per instance; one process, {threads} torch threads",
+        }
+    return out
+
+
 # ---------------------------------------------------------------------------
 # the headline workload
 # ---------------------------------------------------------------------------
@@ -502,6 +648,9 @@ def run_lv_ensemble(args):
             }
             if not args.no_cpu_baseline:
                 secondary["lml_gradients_fhn"]["cpu_baseline"] = lml_cpu_baseline()
+            if args.burgers_t1 > 0 and world == 1:
+                secondary["burgers_blockdiag"] = burgers_blockdiag_secondary(
+                    torch, _native, ensemble, device, t1=args.burgers_t1, cpu=not args.no_cpu_baseline)
     finally:
         clk.__exit__(None, None, None)
 
@@ -768,7 +917,10 @@ def main():
                     help="lv_ensemble: instance-to-lane mapping (auto = time all three and keep the fastest)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="e2e: launch the solver eagerly instead of from CUDA graphs")
-    ap.add_argument("--no-secondary", action="store_true", help="skip the single-instance and LML measurements")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the single-instance, LML and block-diagonal Burgers measurements")
+    ap.add_argument("--burgers-t1", type=float, default=1.0,
+                    help="lv_ensemble: horizon of the block-diagonal Burgers secondary (0 skips it)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="ensemble size (16384 is the headline workload)")
     ap.add_argument("--mu-max", type=float, default=1000.0, help="vdp_dense: mu ~ log-uniform [1, mu_max]")

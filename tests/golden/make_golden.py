@@ -29,6 +29,13 @@ Fixtures:
   vdp_dense.json   van der Pol (mu = 1, 3), dense TS1, fixed-point smoother,
                    solver_dynamic, rtol = atol = 1e-5, 8 save points by
                    interpolation: smoothed means, Cholesky factors, steps
+  vdp_dense_mu30.json  the stiff dense configuration's solver at mu = 30:
+                   van der Pol, dense TS1, fixed-point smoother,
+                   solver_dynamic, rtol = atol = 1e-5, 100 save points
+                   linspace(0, 2 mu, 100) by interpolation: smoothed means,
+                   Cholesky factors, accepted steps and the attempt count
+                   (about 10 minutes of oracle time; not re-run by the CPU
+                   tests)
   fhn_lml.json     FitzHugh--Nagumo LML on 200 steps of 0.01 with 21
                    observations (data included), 2 parameter samples with
                    perturbed initial values: lml, d lml / d params,
@@ -172,7 +179,14 @@ def lv_sensitivities_fixture(params=None, y0=None):
     return out
 
 
-def vdp_dense_fixture(mus=None):
+def vdp_dense_mu30_fixture(mu=30.0, num_save=100):
+    """One instance of the stiff dense configuration at mu = 30 with its 100
+    save points (the oracle needs ~2e4 attempts)."""
+    out = vdp_dense_fixture([mu], num_save=num_save)
+    return out
+
+
+def vdp_dense_fixture(mus=None, num_save=8):
     """Dense TS1 van der Pol (first order), fixed-point smoother, dynamic
     calibration, error_residual_std, integral control, nu = 3,
     rtol = atol = 1e-5, save_at = linspace(0, 2 mu, 8) reached by
@@ -184,7 +198,7 @@ def vdp_dense_fixture(mus=None):
     out = {"mu": list(mus), "y0": [2.0, 0.0], "num_derivatives": 3, "rtol": 1e-5, "atol": 1e-5, "dt0": 0.1,
            "save_at": [], "records": []}
     for mu in mus:
-        save_at = np.linspace(0.0, 2.0 * mu, 8)
+        save_at = np.linspace(0.0, 2.0 * mu, num_save)
         p = torch.tensor([mu], dtype=torch.float64)
         tc = problems.taylor_derivatives(problems.van_der_pol, torch.tensor([2.0, 0.0], dtype=torch.float64), p, 3)
         D = ssm.DenseSSM()
@@ -198,6 +212,7 @@ def vdp_dense_fixture(mus=None):
             "u_mean": [u.mean.tolist() for u in res.u],
             "u_chol": [u.cholesky.tolist() for u in res.u],
             "num_steps": [int(s) for s in res.num_steps],
+            "num_attempts": int(res.num_attempts),
         })
     return out
 
@@ -230,15 +245,19 @@ def load(name):
         return json.load(f)
 
 
-def main():
+def main(names=None):
+    """Writes every fixture, or only those named on the command line."""
     torch.set_default_dtype(torch.float64)
     for name, fn in (("iwp.json", iwp_fixture), ("lv_filter.json", lv_filter_fixture),
                      ("lv_fixedpoint.json", lv_fixedpoint_fixture), ("lv_sensitivities.json", lv_sensitivities_fixture),
-                     ("vdp_dense.json", vdp_dense_fixture), ("fhn_lml.json", fhn_lml_fixture)):
+                     ("vdp_dense.json", vdp_dense_fixture), ("vdp_dense_mu30.json", vdp_dense_mu30_fixture),
+                     ("fhn_lml.json", fhn_lml_fixture)):
+        if names and name not in names:
+            continue
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(fn(), f, indent=1)
         print("wrote", name)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
