@@ -813,7 +813,7 @@ def run_vdp_dense(args):
             cfg = ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense", constraint="ts1",
                                        strategy="fixedpoint", solver="dynamic", precision=prec, atol=1e-5, rtol=1e-5,
                                        clip_dt=False, max_attempts=1 << 24,
-                                       kernel_variant={"lanes": 2}.get(args.variant, 1))
+                                       kernel_variant={"lanes": 2, "thread": 1}.get(args.variant, 3))
             outs = _native.alloc_outputs(cfg, B, 100, False, device, posterior=True)
             t = timed_region(torch, stream, lambda: _native.solve_adaptive(cfg, save_at, prm, y0, dt0, False, outs,
                                                                              stream=stream), args.steps, args.warmup)
@@ -826,7 +826,8 @@ def run_vdp_dense(args):
     cfg = {"workload": "van_der_pol_dense", "instances": B, "mu": f"log-uniform [1, {args.mu_max}]", "t_span": "[0, 2 mu]",
            "num_derivatives": 3, "ssm": "dense", "constraint": "ts1", "strategy": "fixedpoint", "solver": "dynamic",
            "save_at": 100, "rtol": 1e-5, "atol": 1e-5,
-           "mapping": "8 lanes per instance" if args.variant == "lanes" else "thread per instance"}
+           "mapping": {"lanes": "8 lanes per instance", "thread": "thread per instance"}.get(
+               args.variant, "structure-exploiting QRs, 4 lanes per instance")}
     print(json.dumps(base_line("ensemble IVP solves/s", res[first]["solves_per_s"], "solves/s", args,
                                res[first]["ms_per_step"], True, first, cfg, by_precision=res, gpu_launches=args.steps,
                                clocks=clk.summary())))

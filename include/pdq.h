@@ -113,7 +113,9 @@ typedef struct pdq_config {
   int32_t correct_asymptotic_underconfidence; /* solver_mle (solvers.py:456-457) */
   int32_t kernel_variant;  /* isotropic mapping: 0 auto, 1 one thread per instance,
                               2 / 3 eight lanes per instance with <= 128 / <= 85 registers (clip_dt only);
-                              dense: 2 eight lanes per instance, otherwise one thread per instance */
+                              dense: 0 auto (3, or 1 for error_state_std and run-time fields),
+                              1 one thread per instance, 2 eight lanes per instance,
+                              3 structure-exploiting QRs on four lanes per instance */
   double safety, factor_min, factor_max;           /* controller (defaults 0.95, 0.2, 10) */
   double exponent_integral, exponent_proportional; /* PI controller (0.3, 0.4) */
   double atol, rtol, eps, damp;                    /* solve(...) arguments */
@@ -121,7 +123,8 @@ typedef struct pdq_config {
   int32_t instances_per_block; /* instances per CTA; 0: default.  Isotropic: 32 or 64 (one thread
                                   each; default 64), 8, 16 or 32 (eight lanes each; default 32);
                                   dense: 8, 16 or 32 (one thread each; default 32), 1 to 4 (eight
-                                  lanes each; default 4); block-diagonal: 0 */
+                                  lanes each; default 4), 0 for variant 3 (eight instances per
+                                  32-thread CTA); block-diagonal: 0 */
   int32_t reserved0;      /* 0 */
 } pdq_config;
 

@@ -24,7 +24,7 @@ __all__ = ["candidates", "tune", "tuned_config", "cache_key", "clear_cache"]
 _ISO_THREAD = [(1, 64), (1, 32)]
 _ISO_LANES = [(2, 32), (2, 16), (3, 32)]
 _DENSE_THREAD = [(1, 32), (1, 16)]
-_DENSE_LANES = [(2, 4), (2, 2)]
+_DENSE_LANES = [(3, 0), (2, 4), (2, 2)]
 
 _cache = {}
 _lock = threading.Lock()
@@ -38,7 +38,8 @@ def candidates(cfg):
                     and cfg.field < _native.FIELD_USER_BASE)
         return _ISO_THREAD + (_ISO_LANES if lanes_ok else [])
     if cfg.ssm == _native.SSM["dense"]:
-        return _DENSE_THREAD + (_DENSE_LANES if cfg.error == _native.ERROR["residual_std"] else [])
+        lanes_ok = cfg.error == _native.ERROR["residual_std"] and cfg.field < _native.FIELD_USER_BASE
+        return _DENSE_THREAD + (_DENSE_LANES if lanes_ok else [])
     return [(0, 0)]
 
 

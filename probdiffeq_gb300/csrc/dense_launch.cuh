@@ -3,6 +3,7 @@
 
 #include "dense_coop.cuh"
 #include "dense_solver.cuh"
+#include "dense_struct.cuh"
 
 namespace pdq {
 
@@ -28,8 +29,32 @@ cudaError_t launch_dense_coop(const DenseArgs& a, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
+// Structure-exploiting kernel: four lanes per instance, eight instances per
+// warp-sized block, their states in dynamic shared memory.
+constexpr int kDenseStructLanes = 4;
+
+template <typename T, int NU, class F, bool TS1, bool FP>
+cudaError_t launch_dense_struct(const DenseArgs& a, cudaStream_t stream) {
+  constexpr int L = kDenseStructLanes, IPW = 32 / L;
+  const size_t smem = dense_struct_smem_bytes<NU, F::D>(sizeof(T), L);
+  static bool attr_set = false;
+  cudaError_t e = ensure_stack<dense_struct_kernel<T, NU, F, TS1, FP, L>>();
+  if (e != cudaSuccess) return e;
+  if (!attr_set) {
+    e = cudaFuncSetAttribute(dense_struct_kernel<T, NU, F, TS1, FP, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const unsigned grid = unsigned((a.B + IPW - 1) / IPW);
+  dense_struct_kernel<T, NU, F, TS1, FP, L><<<grid, 32, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+// block: 1 one thread per instance, 3 the structure-exploiting lanes, else the 8-lane cooperative kernel
 template <typename T, int NU, class F, bool TS1, bool FP>
 cudaError_t launch_dense_variant(const DenseArgs& a, cudaStream_t stream, int block) {
+  if (block == 3) return launch_dense_struct<T, NU, F, TS1, FP>(a, stream);
   if (block != 1) return launch_dense_coop<T, NU, F, TS1, FP>(a, stream);
   block = a.instances_per_block > 0 ? a.instances_per_block : 32;  // one thread per instance
   auto kernel = dense_adaptive_kernel<T, NU, F, TS1, FP>;

@@ -1,0 +1,895 @@
+// Dense-factorisation adaptive solver with the structure of the IWP prior and
+// of the ODE linearisation exploited: L lanes per IVP instance, the
+// instance's state in shared memory as a structure of arrays.
+//
+// Same algorithm, branches and references as dense_adaptive_kernel
+// (dense_solver.cuh): IWP transition / revert / merge / marginalise
+// (ssm_impl_dense.py:15-84, 347-363), TS1 / TS0 (ssm_impl_dense.py:237-334),
+// filter / fixed-point smoother (estimators_and_losses.py:347-591), solver /
+// solver_mle / solver_dynamic, error_residual_std, I / PI control and the
+// RejectionLoop with checkpoints (solvers_via_adaptive_steps.py:196-375).
+// What differs is how each QR is formed and who does the work:
+//
+// * predict / revert: the input [[s sqrt|h| Q^T, 0], [(A cl)^T, cl^T]]
+//   (Q = kron(Q1, I_d) lower triangular, cl = p^-1 L) has an upper-triangular
+//   top-left block, so reflector c touches row c and the N bottom rows only;
+//   the bottom-right block is then reduced by a dense N x N QR.
+// * merge and marginalise: [full N x N; upper-triangular N x N] -- reflector c
+//   acts on the contiguous rows c .. c + N.
+// * update: the linearisation J = [-J_f, I, 0, ...] (TS1) or [0, I, 0, ...]
+//   (TS0) reads only coefficients 0 and 1, so of the (d + N)^2 QR only the d
+//   observation rows and the first 2d rows of L^T take part (3d x (d + N),
+//   registers); the other rows of the factor carry over unchanged.  The
+//   observed covariance of the error estimate likewise reduces to a 3d x d QR.
+// * the L lanes of an instance deal the columns of every QR cyclically (a
+//   reflector is formed redundantly by all L lanes from shared memory, then
+//   each lane applies it to its own columns; no shuffles), and the rows of
+//   the matrix products; two __syncwarp per reflector order the shared-memory
+//   traffic.  Scalars (time, step, calibration, control, status) are computed
+//   identically in all lanes, so the control flow of a group is uniform.
+// * element e of instance slot s lives at smem[e * IPW + s] (IPW = 32 / L
+//   instances per warp): the lanes of a warp hit distinct banks.
+// * the three running normals (step_from, interp_from, proposal) and the
+//   three running conditionals (running, interp, merged) rotate through slots
+//   by index on acceptance instead of being copied.
+//
+// R factors may differ from a LAPACK QR in the signs of their rows; every
+// quantity formed from them (L L^T, R11^-1 R12, R22^T R22) is invariant.
+#pragma once
+
+#include "dense_solver.cuh"
+
+// The kernel's dynamic shared memory (a host run of the kernel body supplies a buffer instead).
+#ifndef PDQ_DENSE_STRUCT_SMEM
+#define PDQ_DENSE_STRUCT_SMEM extern __shared__ __align__(16) unsigned char dense_struct_smem[]
+#endif
+
+namespace pdq {
+
+template <int L>
+struct LaneGroup {
+  unsigned mask;
+  int lane;  // 0 .. L - 1
+  PDQ_D void sync() const {
+    if constexpr (L > 1) __syncwarp(mask);
+  }
+  // the first index >= j0 dealt to this lane (index j goes to lane j mod L)
+  PDQ_D int first(int j0) const { return j0 + ((lane - j0) & (L - 1)); }
+  PDQ_D bool owns(int j) const { return (j & (L - 1)) == lane; }
+};
+
+template <typename T, int IPW>
+struct Soa {
+  T* p;  // element 0 of this instance
+  PDQ_D T& operator[](int e) const { return p[e * IPW]; }
+};
+
+template <int NU, int D>
+struct DenseLayout {
+  static constexpr int n = NU + 1, N = n * D, NN = N * N;
+  static constexpr int kNormal = N + NN;        // m, L (row-major, lower)
+  static constexpr int kCond = 2 * NN + 3 * N;  // A, xi, X (row-major, lower), tl, to
+  static constexpr int kNormals = 4;            // step_from, interp_from, proposal, prediction (rotating)
+  static constexpr int kConds = 4;              // running, interp, merged, scratch (rotating)
+  static constexpr int m = 0, L = N;
+  static constexpr int A = 0, xi = NN, X = NN + N, tl = 2 * NN + N, to = 2 * NN + 2 * N;
+  static constexpr int normal0 = 0;
+  static constexpr int cond0 = kNormals * kNormal;
+  static constexpr int cnA = cond0 + kConds * kCond;  // this step's conditional: A (N x N), xi (N)
+  static constexpr int cnXi = cnA + NN;
+  static constexpr int W = cnXi + N;   // predict workspace, 2N x 2N, row stride 2N
+  static constexpr int WM = W + 4 * NN;  // merge / marginalise workspace, 2N x N, row stride N
+  static constexpr int size = WM + 2 * NN;
+  PDQ_HD static constexpr int normal(int k) { return normal0 + k * kNormal; }
+  PDQ_HD static constexpr int cond(int k) { return cond0 + k * kCond; }
+};
+
+// ||x|| with a rescaled sum of squares when the plain one leaves
+// [1e-30, 1e36] (float) / [1e-290, 1e300] (double), as householder_r.
+template <typename T, int K>
+PDQ_D void dstruct_norm(const T (&x)[K], T& nrm, T& nrm2) {
+  T s0 = T(0), s1 = T(0);
+#pragma unroll
+  for (int t = 0; t < K; t += 2) s0 += x[t] * x[t];
+#pragma unroll
+  for (int t = 1; t < K; t += 2) s1 += x[t] * x[t];
+  nrm2 = s0 + s1;
+  if (norm2_out_of_range(nrm2)) {
+    T sc = T(0);
+#pragma unroll
+    for (int t = 0; t < K; ++t) sc = fmax(sc, dev_abs(x[t]));
+    T acc = T(0);
+    if (sc > T(0)) {
+      const T inv = T(1) / sc;
+#pragma unroll
+      for (int t = 0; t < K; ++t) acc += (x[t] * inv) * (x[t] * inv);
+    }
+    nrm = sc * dev_sqrt(acc);
+    nrm2 = nrm > T(0) ? T(1) : T(0);
+  } else {
+    nrm = dev_sqrt(nrm2);
+  }
+}
+
+// Householder reflector of x (x[0] the diagonal), the convention of
+// householder_r: beta = -sign(x0) ||x||, v = [1, x[1:] / (x0 - beta)],
+// tau = (beta - x0) / beta.  Returns false for a zero column.
+template <typename T, int K>
+PDQ_D bool dstruct_reflector(T (&x)[K], T& beta, T& tau) {
+  T nrm, nrm2;
+  dstruct_norm(x, nrm, nrm2);
+  if (!(nrm2 > T(0))) return false;
+  const T alpha = x[0];
+  beta = alpha >= T(0) ? -nrm : nrm;
+  const T vinv = dev_rcp(alpha - beta);
+  tau = dev_div(beta - alpha, beta);
+#pragma unroll
+  for (int t = 1; t < K; ++t) x[t] *= vinv;
+  return true;
+}
+
+// QR of the 2N x N workspace WM = [full N x N; upper-triangular N x N]
+// (rows c .. c + N take part in reflector c); R in rows 0 .. N - 1.
+template <typename T, int N, int L, int IPW>
+PDQ_D void dstruct_qr_stacked(Soa<T, IPW> S, const LaneGroup<L>& g, int WM) {
+#pragma unroll 1
+  for (int c = 0; c < N; ++c) {
+    T x[N + 1];
+#pragma unroll
+    for (int t = 0; t <= N; ++t) x[t] = S[WM + (c + t) * N + c];
+    g.sync();  // every lane has read column c
+    T beta, tau;
+    if (dstruct_reflector(x, beta, tau)) {
+#pragma unroll 2
+      for (int j = g.first(c + 1); j < N; j += L) {
+        T w0 = S[WM + c * N + j], w1 = T(0);
+#pragma unroll
+        for (int t = 1; t <= N; t += 2) w0 += x[t] * S[WM + (c + t) * N + j];
+#pragma unroll
+        for (int t = 2; t <= N; t += 2) w1 += x[t] * S[WM + (c + t) * N + j];
+        const T w = tau * (w0 + w1);
+        S[WM + c * N + j] -= w;
+#pragma unroll
+        for (int t = 1; t <= N; ++t) S[WM + (c + t) * N + j] -= w * x[t];
+      }
+      if (g.owns(c)) S[WM + c * N + c] = beta;
+    }
+    g.sync();
+  }
+}
+
+// transition(h, scale).revert(rv) (REVERT: the predicted marginal into `pred`
+// and this step's backward conditional: A, xi into cnA / cnXi, its noise
+// factor left in W's bottom-right block as R22 (X = R22^T), to = 1 / p^-1,
+// tl = 1 / p) or .marginalise(rv) (the predicted marginal only)
+// (ssm_impl_dense.py:24-77 with :347-363).
+template <typename T, int NU, int D, bool REVERT, int L, int IPW>
+PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&q1)[kMaxN][kMaxN], int from, T h,
+                           T scale, int pred) {
+  using Lay = DenseLayout<NU, D>;
+  constexpr int n = NU + 1, N = Lay::N, C = REVERT ? 2 * N : N, WS = 2 * N;
+  constexpr int W = Lay::W;
+  T pc[n], pic[n];
+  precon<T, NU>(h, pc, pic);
+  const T sq = scale * dev_sqrt(dev_abs(h));
+  // mean (all lanes): mean_l = p^-1 m, mobs = A mean_l
+  T mean_l[N], mobs[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) mean_l[i] = pic[i / D] * S[from + Lay::m + i];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T acc = T(0);
+#pragma unroll
+    for (int kk = i / D; kk < n; ++kk) acc += T(iwp_a<NU>(i / D, kk)) * mean_l[kk * D + i % D];
+    mobs[i] = acc;
+  }
+  // fill, column-parallel
+#pragma unroll
+  for (int ci = 0; ci < n; ++ci)
+#pragma unroll
+    for (int cd = 0; cd < D; ++cd) {
+      const int c = ci * D + cd;
+      if (g.owns(c)) {
+#pragma unroll
+        for (int r = 0; r < N; ++r)
+          S[W + r * WS + c] = (r % D == cd && r / D <= ci) ? sq * T(q1[ci][r / D]) : T(0);
+#pragma unroll
+        for (int r = 0; r < N; ++r) {
+          // (A cl)[c][r] = sum_k A1[ci][k / D] p^-1_k L[k][r] over k = kk d + cd, kk >= ci, k >= r
+          T acc = T(0);
+#pragma unroll
+          for (int kk = ci; kk < n; ++kk) {
+            const int k = kk * D + cd;
+            if (k >= r) acc += T(iwp_a<NU>(ci, kk)) * pic[kk] * S[from + Lay::L + k * N + r];
+          }
+          S[W + (N + r) * WS + c] = acc;
+        }
+      }
+      if constexpr (REVERT) {
+        if (g.owns(N + c)) {
+#pragma unroll
+          for (int r = 0; r < N; ++r) S[W + r * WS + N + c] = T(0);
+#pragma unroll
+          for (int r = 0; r < N; ++r) S[W + (N + r) * WS + N + c] = r <= c ? pic[ci] * S[from + Lay::L + c * N + r] : T(0);
+        }
+      }
+    }
+  g.sync();
+  // reflectors 0 .. N - 1: row c and the N bottom rows
+#pragma unroll 1
+  for (int c = 0; c < N; ++c) {
+    T x[N + 1];
+    x[0] = S[W + c * WS + c];
+#pragma unroll
+    for (int r = 0; r < N; ++r) x[1 + r] = S[W + (N + r) * WS + c];
+    g.sync();
+    T beta, tau;
+    if (dstruct_reflector(x, beta, tau)) {
+#pragma unroll 2
+      for (int j = g.first(c + 1); j < C; j += L) {
+        T w0 = S[W + c * WS + j], w1 = T(0);
+#pragma unroll
+        for (int r = 0; r < N; r += 2) w0 += x[1 + r] * S[W + (N + r) * WS + j];
+#pragma unroll
+        for (int r = 1; r < N; r += 2) w1 += x[1 + r] * S[W + (N + r) * WS + j];
+        const T w = tau * (w0 + w1);
+        S[W + c * WS + j] -= w;
+#pragma unroll
+        for (int r = 0; r < N; ++r) S[W + (N + r) * WS + j] -= w * x[1 + r];
+      }
+      if (g.owns(c)) S[W + c * WS + c] = beta;
+    }
+    g.sync();
+  }
+  if constexpr (REVERT) {
+    // the bottom-right N x N block, dense: column N + cc over rows N + cc .. 2N - 1
+#pragma unroll 1
+    for (int cc = 0; cc < N - 1; ++cc) {
+      const int c = N + cc;
+      T x[N];
+#pragma unroll
+      for (int t = 0; t < N; ++t) x[t] = (t < N - cc) ? S[W + (c + t) * WS + c] : T(0);
+      g.sync();
+      T beta, tau;
+      if (dstruct_reflector(x, beta, tau)) {
+#pragma unroll 2
+        for (int j = g.first(c + 1); j < 2 * N; j += L) {
+          T w0 = S[W + c * WS + j], w1 = T(0);
+#pragma unroll
+          for (int t = 1; t < N; t += 2)
+            if (t < N - cc) w0 += x[t] * S[W + (c + t) * WS + j];
+#pragma unroll
+          for (int t = 2; t < N; t += 2)
+            if (t < N - cc) w1 += x[t] * S[W + (c + t) * WS + j];
+          const T w = tau * (w0 + w1);
+          S[W + c * WS + j] -= w;
+#pragma unroll
+          for (int t = 1; t < N; ++t)
+            if (t < N - cc) S[W + (c + t) * WS + j] -= w * x[t];
+        }
+        if (g.owns(c)) S[W + c * WS + c] = beta;
+      }
+      g.sync();
+    }
+  }
+  // the predicted marginal: m = p mobs, L = |p| R11^T
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (g.owns(i)) {
+      S[pred + Lay::m + i] = pc[i / D] * mobs[i];
+#pragma unroll
+      for (int j = 0; j < N; ++j) S[pred + Lay::L + i * N + j] = (j <= i) ? dev_abs(pc[i / D]) * S[W + j * WS + i] : T(0);
+    }
+  if constexpr (REVERT) {
+    // G^T = R11^-1 R12 column by column; cond.A[jj][i] = G^T[i][jj], cond.xi = mean_l - G mobs
+#pragma unroll
+    for (int jj = 0; jj < N; ++jj)
+      if (g.owns(jj)) {
+        T gc[N];
+#pragma unroll
+        for (int i = N - 1; i >= 0; --i) {
+          T acc = S[W + i * WS + N + jj];
+#pragma unroll
+          for (int k = i + 1; k < N; ++k) acc -= S[W + i * WS + k] * gc[k];
+          gc[i] = dev_div(acc, S[W + i * WS + i]);
+        }
+        T xi = mean_l[jj];
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+          S[Lay::cnA + jj * N + k] = gc[k];
+          xi -= gc[k] * mobs[k];
+        }
+        S[Lay::cnXi + jj] = xi;
+      }
+  }
+  g.sync();
+}
+
+// outer.merge(inner) (ssm_impl_dense.py:35-49) with the inner conditional
+// the one dstruct_predict<REVERT> left (A, xi in cnA / cnXi, X = R22^T in W,
+// tl = 1 / p, to = 1 / p^-1 for step h); result into the conditional `out`.
+template <typename T, int NU, int D, int L, int IPW>
+PDQ_D void dstruct_merge(Soa<T, IPW> S, const LaneGroup<L>& g, int o, T h, int out) {
+  using Lay = DenseLayout<NU, D>;
+  constexpr int n = NU + 1, N = Lay::N, WS = 2 * N;
+  constexpr int W = Lay::W, WM = Lay::WM;
+  T pc[n], pic[n];
+  precon<T, NU>(h, pc, pic);
+  T Tv[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) Tv[k] = S[o + Lay::tl + k] * dev_rcp(pic[k / D]);
+  // out.A = o.A T in.A and R1 = (o.A |T| in.X)^T by columns j of in.A / in.X
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+    if (g.owns(j)) {
+      T u[N], u2[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        u[k] = Tv[k] * S[Lay::cnA + k * N + j];
+        u2[k] = k >= j ? dev_abs(Tv[k]) * S[W + (N + j) * WS + N + k] : T(0);
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        T ga = T(0), r1 = T(0);
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+          const T oa = S[o + Lay::A + i * N + k];
+          ga += oa * u[k];
+          if (k >= j) r1 += oa * u2[k];
+        }
+        S[out + Lay::A + i * N + j] = ga;
+        S[WM + j * N + i] = r1;
+      }
+      // R2 row j = (o.X^T) row j
+#pragma unroll
+      for (int i = 0; i < N; ++i) S[WM + (N + j) * N + i] = i >= j ? S[o + Lay::X + i * N + j] : T(0);
+      // out.xi[j] = o.xi[j] + (o.A T in.xi)[j]
+      T x = S[o + Lay::xi + j];
+#pragma unroll
+      for (int k = 0; k < N; ++k) x += S[o + Lay::A + j * N + k] * Tv[k] * S[Lay::cnXi + k];
+      S[out + Lay::xi + j] = x;
+      S[out + Lay::tl + j] = dev_rcp(pc[j / D]);
+      S[out + Lay::to + j] = S[o + Lay::to + j];
+    }
+  g.sync();
+  dstruct_qr_stacked<T, N, L, IPW>(S, g, WM);
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (g.owns(i)) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) S[out + Lay::X + i * N + j] = (j <= i) ? S[WM + j * N + i] : T(0);
+    }
+  g.sync();
+}
+
+// cond.marginalise(rv) (ssm_impl_dense.py:24-33): the conditional `c`
+// applied to the normal `rv`, result into the normal `out`.
+template <typename T, int NU, int D, int L, int IPW>
+PDQ_D void dstruct_cond_marginalise(Soa<T, IPW> S, const LaneGroup<L>& g, int c, int rv, int out) {
+  using Lay = DenseLayout<NU, D>;
+  constexpr int N = Lay::N, WM = Lay::WM;
+  // rows r of (A (tl L))^T and of X^T, by rows
+#pragma unroll
+  for (int r = 0; r < N; ++r)
+    if (g.owns(r)) {
+      T u[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k) u[k] = k >= r ? S[c + Lay::tl + k] * S[rv + Lay::L + k * N + r] : T(0);
+#pragma unroll
+      for (int col = 0; col < N; ++col) {
+        T acc = T(0);
+#pragma unroll
+        for (int k = r; k < N; ++k) acc += S[c + Lay::A + col * N + k] * u[k];
+        S[WM + r * N + col] = acc;
+        S[WM + (N + r) * N + col] = col >= r ? S[c + Lay::X + col * N + r] : T(0);
+      }
+    }
+  // the mean (all lanes read rv before anyone writes out; rv != out)
+  T mo[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc += S[c + Lay::A + i * N + k] * S[c + Lay::tl + k] * S[rv + Lay::m + k];
+    mo[i] = S[c + Lay::to + i] * (acc + S[c + Lay::xi + i]);
+  }
+  g.sync();
+  dstruct_qr_stacked<T, N, L, IPW>(S, g, WM);
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (g.owns(i)) {
+      S[out + Lay::m + i] = mo[i];
+      const T to = dev_abs(S[c + Lay::to + i]);
+#pragma unroll
+      for (int j = 0; j < N; ++j) S[out + Lay::L + i * N + j] = (j <= i) ? to * S[WM + j * N + i] : T(0);
+    }
+  g.sync();
+}
+
+template <typename T, int N, int L, int IPW>
+PDQ_D void dstruct_cond_identity(Soa<T, IPW> S, const LaneGroup<L>& g, int c) {
+  constexpr int NN = N * N;  // the DenseLayout offsets: A 0, xi NN, X NN + N, tl 2 NN + N, to 2 NN + 2 N
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (g.owns(i)) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        S[c + i * N + j] = (i == j) ? T(1) : T(0);  // A
+        S[c + NN + N + i * N + j] = T(0);           // X
+      }
+      S[c + NN + i] = T(0);               // xi
+      S[c + 2 * NN + N + i] = T(1);       // tl
+      S[c + 2 * NN + 2 * N + i] = T(1);   // to
+    }
+  g.sync();
+}
+
+template <typename T, int K, int L, int IPW>
+PDQ_D void dstruct_copy(Soa<T, IPW> S, const LaneGroup<L>& g, int dst, int src) {
+#pragma unroll 4
+  for (int e = g.lane; e < K; e += L) S[dst + e] = S[src + e];
+  g.sync();
+}
+
+// store_cond / load_cond (dense_solver.cuh) from / to shared memory: one
+// lane writes the workspace record (rare: once per checkpoint).
+template <typename T, int N, int L, int IPW>
+PDQ_D void dstruct_store_cond(Soa<T, IPW> S, const LaneGroup<L>& g, int c, T* base) {
+  constexpr int NN = N * N;
+  if (g.lane == 0) {
+    int o = 0;
+    for (int e = 0; e < NN + N; ++e) base[o++] = S[c + e];  // A, xi
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j <= i; ++j) base[o++] = S[c + NN + N + i * N + j];
+    for (int e = 0; e < 2 * N; ++e) base[o++] = S[c + 2 * NN + N + e];  // tl, to
+  }
+  g.sync();
+}
+
+template <typename T, int N, int L, int IPW>
+PDQ_D void dstruct_load_cond(Soa<T, IPW> S, const LaneGroup<L>& g, int c, const T* base) {
+  constexpr int NN = N * N;
+  if (g.lane == 0) {
+    int o = 0;
+    for (int e = 0; e < NN + N; ++e) S[c + e] = base[o++];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) S[c + NN + N + i * N + j] = (j <= i) ? base[o++] : T(0);
+    for (int e = 0; e < 2 * N; ++e) S[c + 2 * NN + N + e] = base[o++];
+  }
+  g.sync();
+}
+
+template <typename T, int N, int L, int IPW>
+PDQ_D void dstruct_write_normal(Soa<T, IPW> S, const LaneGroup<L>& g, int x, double* mean, double* chol) {
+  for (int e = g.lane; e < N; e += L) mean[e] = double(S[x + e]);
+  for (int e = g.lane; e < N * N; e += L) chol[e] = double(S[x + N + e]);
+}
+
+template <typename T, int NU, class F, bool TS1, bool FP, int L>
+__global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
+  constexpr int D = F::D, P = F::P, n = NU + 1;
+  using Lay = DenseLayout<NU, D>;
+  constexpr int N = Lay::N, IPW = 32 / L;
+  PDQ_DENSE_STRUCT_SMEM;
+  const int slot = int(threadIdx.x) / L;
+  const LaneGroup<L> g{((1u << L) - 1u) << (slot * L), int(threadIdx.x) % L};
+  const int64_t b = int64_t(blockIdx.x) * IPW + slot;
+  if (b >= a.B) return;  // the whole group leaves together
+  const Soa<T, IPW> S{reinterpret_cast<T*>(dense_struct_smem) + slot};
+  const int Sn = a.S;
+  const int S_out = a.terminal_only ? 1 : Sn;
+  const double* save_at = a.save_at + b * Sn;
+  T* ws = FP ? reinterpret_cast<T*>(a.workspace) + b * int64_t(Sn - 1) * cond_floats<N>() : nullptr;
+
+  double pd[P];
+  T pt[P];
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    pd[k] = a.params[b * P + k];
+    pt[k] = T(pd[k]);
+  }
+  // slots (offsets into the instance's shared-memory record)
+  int ix = Lay::normal(0), ii = Lay::normal(1), inew = Lay::normal(2), ipred = Lay::normal(3);
+  int ibw = Lay::cond(0), ibwi = Lay::cond(1), img = Lay::cond(2), itmp = Lay::cond(3);
+  {
+    double y0[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) y0[j] = a.y0[b * D + j];
+    double tc[n][D];
+    taylor_init<F, NU>(y0, pd, tc);
+    if (g.lane == 0) {
+#pragma unroll
+      for (int i = 0; i < n; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) S[ix + Lay::m + i * D + j] = T(tc[i][j]);
+      for (int e = 0; e < N * N; ++e) S[ix + Lay::L + e] = T(0);
+    }
+    g.sync();
+  }
+  dstruct_copy<T, Lay::kNormal, L, IPW>(S, g, ii, ix);
+  if constexpr (FP) {
+    dstruct_cond_identity<T, N, L, IPW>(S, g, ibw);
+    dstruct_cond_identity<T, N, L, IPW>(S, g, ibwi);
+  }
+
+  double t = save_at[0], ti = t, dt = a.dt0[b], pi_prev = 1.0, mle_sumsq = 0.0;
+  int num_data = 0, num_steps = 0, attempts = 0, status = PDQ_INSTANCE_OK;
+  T sigma_sf = T(1);
+  const T damp = T(a.damp);
+
+  if (!a.terminal_only) {
+    dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.u_mean + (b * S_out) * N, a.u_chol + (b * S_out) * N * N);
+    if (g.lane == 0) {
+      a.output_scale[b * S_out] = 1.0;
+      a.t_out[b * S_out] = t;
+      a.num_steps[b * S_out] = 0;
+    }
+  }
+  if (a.filter_mean) dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.filter_mean + (b * Sn) * N, a.filter_chol + (b * Sn) * N * N);
+
+  // one attempt per iteration (the retry loop flattened into the checkpoint loop)
+  int s = 1;
+  double t_next = save_at[1];
+  while (s < Sn) {
+    if (t + a.eps < t_next) {
+      bool accepted = false;
+      {
+        const double dt_use = a.clip_dt ? fmin(dt, t_next - t) : dt;
+        if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
+          status = PDQ_INSTANCE_DT_UNDERFLOW;
+          break;
+        }
+        if (attempts >= a.max_attempts) {
+          status = PDQ_INSTANCE_MAX_STEPS;
+          break;
+        }
+        ++attempts;
+        const T h = T(dt_use);
+        T pc[n], pic[n];
+        precon<T, NU>(h, pc, pic);
+        // u = transition(h, 1).apply_flat(mean): mean mp, chol |p| sqrt|h| Q
+        T mp[2 * D];  // coefficients 0 and 1 are all the linearisation reads
+#pragma unroll
+        for (int i = 0; i < 2 * D; ++i) {
+          T acc = T(0);
+#pragma unroll
+          for (int kk = i / D; kk < n; ++kk) acc += T(iwp_a<NU>(i / D, kk)) * pic[kk] * S[ix + Lay::m + kk * D + i % D];
+          mp[i] = pc[i / D] * acc;
+        }
+        // linearisation at mp: J (d x 2d; zero beyond), b; residual r = J mp + b
+        T J[D][2 * D], bl[D];
+        {
+          T f[D];
+          if constexpr (TS1) {
+            T Jf[D][D];
+            eval_with_jacobian<F>(&mp[0], pt, f, Jf);
+#pragma unroll
+            for (int aa = 0; aa < D; ++aa) {
+#pragma unroll
+              for (int k = 0; k < D; ++k) {
+                J[aa][k] = -Jf[aa][k];
+                J[aa][D + k] = (k == aa) ? T(1) : T(0);
+              }
+              T jx = T(0);
+#pragma unroll
+              for (int k = 0; k < D; ++k) jx += Jf[aa][k] * mp[k];
+              bl[aa] = -f[aa] + jx;
+            }
+          } else {
+            F::eval(&mp[0], pt, f);
+#pragma unroll
+            for (int aa = 0; aa < D; ++aa) {
+#pragma unroll
+              for (int k = 0; k < 2 * D; ++k) J[aa][k] = (k == D + aa) ? T(1) : T(0);
+              bl[aa] = -f[aa];
+            }
+          }
+        }
+        T r[D];
+#pragma unroll
+        for (int aa = 0; aa < D; ++aa) {
+          T acc = bl[aa];
+#pragma unroll
+          for (int k = 0; k < 2 * D; ++k) acc += J[aa][k] * mp[k];
+          r[aa] = acc;
+        }
+        // observed = fx.marginalise(u): R of [(J Lu)^T (rows < 2d; zero beyond); damp I]
+        const T sqh = dev_sqrt(dev_abs(h));
+        T Mo[3 * D][D];
+#pragma unroll
+        for (int rr = 0; rr < 2 * D; ++rr)
+#pragma unroll
+          for (int aa = 0; aa < D; ++aa) {
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < 2 * D; ++k)
+              if (k % D == rr % D && rr / D <= k / D) acc += J[aa][k] * dev_abs(pc[k / D]) * sqh * T(a.q1[k / D][rr / D]);
+            Mo[rr][aa] = acc;
+          }
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) Mo[2 * D + i][j] = (i == j) ? damp : T(0);
+        householder_r<T, 3 * D, D>(Mo);
+        T w[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          T acc = r[i];
+#pragma unroll
+          for (int k = 0; k < i; ++k) acc -= Mo[k][i] * w[k];
+          w[i] = dev_div(acc, Mo[i][i]);
+        }
+        T ww = T(0);
+#pragma unroll
+        for (int i = 0; i < D; ++i) ww += w[i] * w[i];
+        const T sigma_loc = dev_sqrt(ww * T(1.0 / D));
+        const T s_pred = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
+
+        // prediction (and this step's backward conditional, merged into the running one)
+        dstruct_predict<T, NU, D, FP, L, IPW>(S, g, a.q1, ix, h, s_pred, ipred);
+        if constexpr (FP) dstruct_merge<T, NU, D, L, IPW>(S, g, ibw, h, img);
+
+        // update: fx.revert(pred), the 3d rows of [[damp I, 0], [(J Lp)^T, Lp^T]] that take part
+        T Wu[3 * D][D + N];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = 0; j < D + N; ++j) Wu[i][j] = (i == j) ? damp : T(0);
+#pragma unroll
+        for (int rr = 0; rr < 2 * D; ++rr) {
+#pragma unroll
+          for (int aa = 0; aa < D; ++aa) {
+            T acc = T(0);
+#pragma unroll
+            for (int k = rr; k < 2 * D; ++k) acc += J[aa][k] * S[ipred + Lay::L + k * N + rr];
+            Wu[D + rr][aa] = acc;
+          }
+#pragma unroll
+          for (int c = 0; c < N; ++c) Wu[D + rr][D + c] = c >= rr ? S[ipred + Lay::L + c * N + rr] : T(0);
+        }
+        householder_r<T, 3 * D, D + N>(Wu);
+        // G^T = R_Y^-1 R12 (d x N); the proposal's mean mp - G ro, ro = r (the linearisation point is mp)
+        T Gt[D][N];
+#pragma unroll
+        for (int col = 0; col < N; ++col)
+#pragma unroll
+          for (int i = D - 1; i >= 0; --i) {
+            T acc = Wu[i][D + col];
+#pragma unroll
+            for (int k = i + 1; k < D; ++k) acc -= Wu[i][k] * Gt[k][col];
+            Gt[i][col] = dev_div(acc, Wu[i][i]);
+          }
+        // the proposal's mean and factor: rows 0 .. 2d - 1 of L^T from Wu, the others from Lp
+        T m0new[D];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          T acc = S[ipred + Lay::m + i];
+#pragma unroll
+          for (int aa = 0; aa < D; ++aa) acc -= Gt[aa][i] * r[aa];
+          if (i < D) m0new[i] = acc;
+          if (g.owns(i)) {
+            S[inew + Lay::m + i] = acc;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+              T v;
+              if (j > i) v = T(0);
+              else if (j < 2 * D) v = Wu[D + j][D + i];
+              else v = S[ipred + Lay::L + i * N + j];
+              S[inew + Lay::L + i * N + j] = v;
+            }
+          }
+        }
+        g.sync();
+        // error_residual_std: sigma * row norms of the observed factor * dt
+        double sumsq = 0.0;
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          T rn = T(0);
+#pragma unroll
+          for (int k = 0; k <= j; ++k) rn += Mo[k][j] * Mo[k][j];
+          const T err_abs = dev_abs(sigma_loc) * dev_sqrt(rn) * h;
+          const T ref = fmax(dev_abs(S[ix + Lay::m + j]), dev_abs(m0new[j]));
+          const T ratio = dev_div(err_abs, T(a.atol) + T(a.rtol) * ref);
+          sumsq += double(ratio) * double(ratio);
+        }
+        const double norm2 = sumsq * (1.0 / D);
+        if (!(norm2 == norm2) || isinf(norm2)) {
+          status = PDQ_INSTANCE_NONFINITE;
+          break;
+        }
+        const T ep = dev_fpow(T(norm2), T(-0.5 / n));
+        double factor;
+        if (a.control == PDQ_CONTROL_INTEGRAL) {
+          factor = a.safety * double(ep);
+        } else {
+          factor = a.safety * double(dev_fpow(ep, T(a.exp_i))) * double(dev_fpow(dev_div(ep, T(pi_prev)), T(a.exp_p)));
+          if (norm2 <= 1.0) pi_prev = double(ep);
+        }
+        factor = fmax(a.factor_min, fmin(factor, a.factor_max));
+        dt = factor * dt_use;
+        accepted = norm2 <= 1.0;
+        if (accepted) {
+          ti = t;
+          t = t + dt_use;
+          ++num_steps;
+          {  // interp_from <- step_from <- proposal
+            const int o = ii;
+            ii = ix;
+            ix = inew;
+            inew = o;
+          }
+          if constexpr (FP) {  // interp conditional <- running <- merged
+            const int o = ibwi;
+            ibwi = ibw;
+            ibw = img;
+            img = o;
+          }
+          if (a.solver == PDQ_SOLVER_MLE) {
+            T wv[D];
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+              T acc = r[i];
+#pragma unroll
+              for (int k = 0; k < i; ++k) acc -= Wu[k][i] * wv[k];
+              wv[i] = dev_div(acc, Wu[i][i]);
+            }
+            T q = T(0);
+#pragma unroll
+            for (int i = 0; i < D; ++i) q += wv[i] * wv[i];
+            mle_sumsq += double(q) * (1.0 / D);
+            ++num_data;
+          }
+          sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
+        }
+      }
+      if (!accepted) continue;  // retry in the next iteration
+    }
+    const bool record = (!a.terminal_only) || (s == Sn - 1);
+    const int s_out = a.terminal_only ? 0 : s;
+    const int64_t rec = b * S_out + s_out;
+    if (t + a.eps < t_next) {
+      // interp_skip
+    } else if (t > t_next + a.eps) {
+      // interp_beyond_t1 (solvers.py:205-269)
+      const T h0 = T(t_next - ti), h1 = T(t - t_next);
+      if constexpr (FP) {
+        // estimators_and_losses.py:549-591
+        dstruct_predict<T, NU, D, true, L, IPW>(S, g, a.q1, ii, h0, sigma_sf, ipred);  // extrapolated_t, c0
+        dstruct_merge<T, NU, D, L, IPW>(S, g, ibwi, h0, itmp);                         // its conditional
+        dstruct_store_cond<T, N, L, IPW>(S, g, itmp, ws + int64_t(s - 1) * cond_floats<N>());
+        {  // keep extrapolated_t in the proposal slot
+          const int o = inew;
+          inew = ipred;
+          ipred = o;
+        }
+        dstruct_predict<T, NU, D, true, L, IPW>(S, g, a.q1, inew, h1, sigma_sf, ipred);  // c1
+        dstruct_cond_identity<T, N, L, IPW>(S, g, ibwi);
+        dstruct_merge<T, NU, D, L, IPW>(S, g, ibwi, h1, ibw);  // extrapolated_t1.conditional -> step_from's
+        {  // interp_from = extrapolated_t
+          const int o = ii;
+          ii = inew;
+          inew = o;
+        }
+        // the interp conditional stays the identity
+      } else {
+        dstruct_predict<T, NU, D, false, L, IPW>(S, g, a.q1, ii, h0, sigma_sf, ipred);
+        const int o = ii;
+        ii = ipred;
+        ipred = o;
+      }
+      ti = t_next;
+      if (record) {
+        dstruct_write_normal<T, N, L, IPW>(S, g, ii, a.u_mean + rec * N, a.u_chol + rec * N * N);
+        if (g.lane == 0) {
+          a.output_scale[rec] = double(sigma_sf);
+          a.t_out[rec] = t_next;
+          a.num_steps[rec] = num_steps;
+        }
+      }
+      if (a.filter_mean)
+        dstruct_write_normal<T, N, L, IPW>(S, g, ii, a.filter_mean + (b * Sn + s) * N, a.filter_chol + (b * Sn + s) * N * N);
+    } else {
+      // interp_at_t1 (solvers.py:271-315)
+      if constexpr (FP) {
+        dstruct_store_cond<T, N, L, IPW>(S, g, ibw, ws + int64_t(s - 1) * cond_floats<N>());
+        dstruct_cond_identity<T, N, L, IPW>(S, g, ibw);
+        dstruct_cond_identity<T, N, L, IPW>(S, g, ibwi);
+      }
+      dstruct_copy<T, Lay::kNormal, L, IPW>(S, g, ii, ix);
+      ti = t;
+      if (record) {
+        dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.u_mean + rec * N, a.u_chol + rec * N * N);
+        if (g.lane == 0) {
+          a.output_scale[rec] = double(sigma_sf);
+          a.t_out[rec] = t;
+          a.num_steps[rec] = num_steps;
+        }
+      }
+      if (a.filter_mean)
+        dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.filter_mean + (b * Sn + s) * N, a.filter_chol + (b * Sn + s) * N * N);
+    }
+    if (!(t + a.eps < t_next)) {  // checkpoint s done
+      ++s;
+      if (s < Sn) t_next = save_at[s];
+    }
+  }
+
+  // ---- finalize (solvers.py:439-480, 601-633, 735-767) ----
+  double scale = 1.0;
+  if (status == PDQ_INSTANCE_OK && a.solver == PDQ_SOLVER_MLE) {
+    scale = num_data > 0 ? sqrt(mle_sumsq / num_data) : 0.0;
+    if (a.correct) scale /= sqrt(double(a.num_steps[b * S_out + (S_out - 1)]));
+  }
+  if (status == PDQ_INSTANCE_OK && FP) {
+    // Smoother.finalize: rv_at_t1 = posterior1.conditional.marginalise(marginal),
+    // then the reverse scan of marginalise over the checkpoint conditionals
+    int irv = inew, iprev = ipred;
+    dstruct_cond_marginalise<T, NU, D, L, IPW>(S, g, ibw, ix, irv);
+    for (int s2 = Sn - 1; s2 >= 1; --s2) {
+      if (!a.terminal_only || s2 == Sn - 1) {
+        const int64_t rec = b * S_out + (a.terminal_only ? 0 : s2);
+        dstruct_write_normal<T, N, L, IPW>(S, g, irv, a.u_mean + rec * N, a.u_chol + rec * N * N);
+      }
+      if (a.terminal_only) break;
+      dstruct_load_cond<T, N, L, IPW>(S, g, itmp, ws + int64_t(s2 - 1) * cond_floats<N>());
+      if (a.cond_A) {
+        const int64_t cr = b * (Sn - 1) + (s2 - 1);
+        constexpr int NN = N * N;
+        for (int e = g.lane; e < NN; e += L) {
+          a.cond_A[cr * NN + e] = double(S[itmp + Lay::A + e]);
+          a.cond_noise_chol[cr * NN + e] = double(S[itmp + Lay::X + e]) * scale;
+        }
+        for (int e = g.lane; e < N; e += L) {
+          a.cond_noise_mean[cr * N + e] = double(S[itmp + Lay::xi + e]);
+          a.cond_to_latent[cr * N + e] = double(S[itmp + Lay::tl + e]);
+          a.cond_to_observed[cr * N + e] = double(S[itmp + Lay::to + e]);
+        }
+      }
+      dstruct_cond_marginalise<T, NU, D, L, IPW>(S, g, itmp, irv, iprev);
+      {
+        const int o = irv;
+        irv = iprev;
+        iprev = o;
+      }
+      if (s2 == 1) {
+        const int64_t rec = b * S_out;
+        dstruct_write_normal<T, N, L, IPW>(S, g, irv, a.u_mean + rec * N, a.u_chol + rec * N * N);
+      }
+    }
+  }
+  __syncwarp(g.mask);  // the group's output writes are ordered before the rescaling below
+  if (status == PDQ_INSTANCE_OK) {
+    if (a.solver == PDQ_SOLVER_MLE) {
+      for (int s2 = 0; s2 < S_out; ++s2) {
+        const int64_t rec = b * S_out + s2;
+        for (int k = g.lane; k < N * N; k += L) a.u_chol[rec * N * N + k] *= scale;
+        if (g.lane == 0) a.output_scale[rec] = scale;
+      }
+      if (a.filter_chol)
+        for (int k = g.lane; k < Sn * N * N; k += L) a.filter_chol[b * Sn * N * N + k] *= scale;
+    }
+  } else {
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    for (int s2 = 0; s2 < S_out; ++s2) {
+      const int64_t rec = b * S_out + s2;
+      for (int k = g.lane; k < N; k += L) a.u_mean[rec * N + k] = nan;
+      for (int k = g.lane; k < N * N; k += L) a.u_chol[rec * N * N + k] = nan;
+      if (g.lane == 0) {
+        a.output_scale[rec] = nan;
+        a.t_out[rec] = nan;
+        a.num_steps[rec] = num_steps;
+      }
+    }
+  }
+  if (g.lane == 0) {
+    a.num_attempts[b] = attempts;
+    a.status[b] = status;
+  }
+}
+
+template <int NU, int D>
+constexpr size_t dense_struct_smem_bytes(size_t elem, int L) {
+  return size_t(32 / L) * size_t(DenseLayout<NU, D>::size) * elem;
+}
+
+}  // namespace pdq

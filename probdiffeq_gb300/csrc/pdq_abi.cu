@@ -364,13 +364,20 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
   }
   if (c->ssm == PDQ_SSM_DENSE) {
-    // error_state_std: the thread-per-instance mapping
-    if (c->error == PDQ_ERROR_STATE_STD && c->kernel_variant == 2) return PDQ_ERROR_UNSUPPORTED;
+    // kernel_variant 1: one thread per instance; 2: eight lanes per instance; 3: the structure-exploiting
+    // kernel (four lanes per instance); 0: 3 unless error_state_std or a run-time field asks for 1
+    // (error_state_std: the thread-per-instance mapping only)
+    const bool state_std = c->error == PDQ_ERROR_STATE_STD;
+    const bool user_field = c->field >= PDQ_FIELD_USER_BASE;
+    if (state_std && (c->kernel_variant == 2 || c->kernel_variant == 3)) return PDQ_ERROR_UNSUPPORTED;
+    if (user_field && (c->kernel_variant == 2 || c->kernel_variant == 3)) return PDQ_ERROR_UNSUPPORTED;
+    const int variant = c->kernel_variant != 0 ? c->kernel_variant : ((state_std || user_field) ? 1 : 3);
     if (args->u_mean_d_params || args->u_mean_d_y0) return PDQ_ERROR_UNSUPPORTED;
     {
       const int ipb = c->instances_per_block;
-      if (c->kernel_variant == 2 ? !(ipb >= 0 && ipb <= 4) : !(ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32))
-        return PDQ_ERROR_INVALID_VALUE;
+      const bool ok = variant == 2 ? (ipb >= 0 && ipb <= 4)
+                                   : (variant == 3 ? ipb == 0 : (ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32));
+      if (!ok) return PDQ_ERROR_INVALID_VALUE;
     }
     if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
@@ -429,11 +436,9 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.workspace = workspace;
     const bool ts1 = c->constraint == PDQ_CONSTRAINT_TS1;
     const bool f64 = c->precision == PDQ_PRECISION_F64;
-    // kernel_variant 2: eight lanes per instance (shared-memory state); otherwise one thread per instance
-    const int block = c->kernel_variant == 2 ? 0 : 1;
+    const int block = variant == 2 ? 0 : variant;  // the launchers' mapping code
     cudaError_t err;
-    if (c->field >= PDQ_FIELD_USER_BASE) {
-      if (c->kernel_variant == 2) return PDQ_ERROR_UNSUPPORTED;  // run-time fields: one thread per instance
+    if (user_field) {  // run-time fields: one thread per instance
       err = pdq_launch_dense_user(a, c->field, f64, c->num_derivatives, ts1, fp, stream);
       return err == cudaSuccess ? PDQ_SUCCESS : (err == cudaErrorInvalidSource ? PDQ_ERROR_COMPILE : PDQ_ERROR_CUDA);
     }

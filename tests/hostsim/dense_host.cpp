@@ -2,7 +2,10 @@
 // per instance, TS1 with the Jacobian on dual numbers) on the CPU, every
 // instance as its own "thread", on buffers of exactly the sizes the library
 // uses (the fixed-point smoother's scratch of backward conditionals
-// included), so AddressSanitizer flags any access outside them.
+// included), so AddressSanitizer flags any access outside them.  With
+// PDQ_HOST_DENSE_KERNEL=struct in the environment it runs the
+// structure-exploiting kernel (dense_struct_kernel) with one lane per
+// instance instead, its shared memory a buffer of the launch's size.
 //
 // Input file (whitespace-separated): field (0 Lotka-Volterra, 1 van der Pol)
 // nu (2 or 3) strategy (0 filter, 1 fixed-point smoother) B S solver control
@@ -12,9 +15,14 @@
 // "t num_steps u_mean[N] u_chol[N N]", N = (nu + 1) 2.
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
+static std::vector<unsigned char> g_smem;  // the structure-exploiting kernel's shared memory
+#define PDQ_DENSE_STRUCT_SMEM unsigned char* dense_struct_smem = g_smem.data()
+
 #include "dense_solver.cuh"
+#include "dense_struct.cuh"
 
 thread_local pdq_host_uint3 threadIdx, blockIdx, blockDim;
 
@@ -77,10 +85,16 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   const int block = 32;
   blockDim = {uint32_t(block), 1, 1};
   const long long padded = (B + block - 1) / block * block;  // the launch's grid
+  const char* kern = getenv("PDQ_HOST_DENSE_KERNEL");
+  const bool structured = kern != nullptr && strcmp(kern, "struct") == 0;
+  if (structured) g_smem.assign(dense_struct_smem_bytes<NU, D>(sizeof(double), 1), 0);
   for (long long g = 0; g < padded; ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
-    dense_adaptive_kernel<double, NU, F, true, FP>(a);
+    if (structured)
+      dense_struct_kernel<double, NU, F, true, FP, 1>(a);
+    else
+      dense_adaptive_kernel<double, NU, F, true, FP>(a);
   }
   for (long long b = 0; b < B; ++b) {
     printf("%d %d\n", status[b], attempts[b]);

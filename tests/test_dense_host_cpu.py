@@ -1,10 +1,12 @@
-"""The dense kernel's float64 body run on the CPU against the golden fixture.
+"""The dense kernels' float64 bodies run on the CPU against the golden fixture.
 
 ``tests/hostsim/dense_host.cpp`` compiles ``dense_adaptive_kernel`` (one
 thread per instance; van der Pol, TS1 with the Jacobian on dual numbers, the
 fixed-point smoother with its scratch of backward conditionals and the
-backward pass) with the host compiler under AddressSanitizer and UBSan, and
-runs it on the inputs of ``tests/golden/vdp_dense.json`` (the oracle's
+backward pass) and ``dense_struct_kernel`` (the structure-exploiting QRs;
+one lane per instance, its shared memory a host buffer) with the host
+compiler under AddressSanitizer and UBSan, and runs them on the inputs of
+``tests/golden/vdp_dense.json`` (the oracle's
 smoothed marginals at 8 save points reached by interpolation, mu = 1 and
 3).  Tolerances of the GPU parity tests (float64): the solution within 1e-8,
 every Taylor row and L L^T within 1e-5, accepted steps within +-1.
@@ -32,7 +34,16 @@ def rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
-def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path):
+KERNELS = ["thread", "struct"]
+
+
+@pytest.fixture(params=KERNELS)
+def kernel(request, monkeypatch):
+    monkeypatch.setenv("PDQ_HOST_DENSE_KERNEL", request.param)
+    return request.param
+
+
+def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path, kernel):
     gold = make_golden.load("vdp_dense.json")
     mus = gold["mu"]
     B, S, d, N = len(mus), len(gold["save_at"][0]), 2, 8
@@ -73,7 +84,7 @@ def _run_lv(harness, tmp_path, strategy, solver, save_at, tol):
 
 @pytest.mark.parametrize("solver", [0, 1, 2])
 @pytest.mark.parametrize("strategy", ["filter", "smoother"])
-def test_host_dense_kernel_behaviour_close_to_t1(harness, tmp_path, strategy, solver):
+def test_host_dense_kernel_behaviour_close_to_t1(harness, tmp_path, strategy, solver, kernel):
     """The reference's test_dense_output/test_behaviour_close_to_t1.py:58-94
     on the dense kernel: Lotka--Volterra, TS1, nu = 2, tol 1e-1, 30 save
     points up to the second-to-last point of the oracle's save-every-step
@@ -103,3 +114,30 @@ def test_host_dense_kernel_behaviour_close_to_t1(harness, tmp_path, strategy, so
         mb, Lb = b[:N], b[N:].reshape(N, N)
         assert np.allclose(ma, mb, atol=tol, rtol=10 * tol)
         assert np.allclose(La @ La.T, Lb @ Lb.T, atol=tol, rtol=10 * tol)
+
+
+def test_host_dense_mu30_100_save_points_matches_fixture(harness, tmp_path, kernel):
+    """The stiff configuration's solver at mu = 30 with 100 save points
+    (``tests/golden/vdp_dense_mu30.json``: the oracle's 1.9e4 accepted steps
+    in 3.2e4 attempts): the same attempt count, accepted steps within +-1 at
+    every save point, the solution within 1e-8, rows and L L^T within 1e-5."""
+    gold = make_golden.load("vdp_dense_mu30.json")
+    rec = gold["records"][0]
+    S, d, N = len(gold["save_at"][0]), 2, 8
+    head = [1, 3, 1, 1, S, 2, 0, 0]
+    body = np.concatenate([[gold["atol"], gold["rtol"]], np.ravel(gold["save_at"]), gold["mu"], gold["y0"],
+                           [gold["dt0"]], q1_iwp(3).ravel()])
+    path = tmp_path / "input_mu30.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lines = hostsim.run_harness(harness, path)
+    status, attempts = (int(x) for x in lines[0].split())
+    assert status == 0 and attempts == rec["num_attempts"]
+    steps_o = [0] + rec["num_steps"]
+    for s in range(S):
+        vals = [float(x) for x in lines[1 + s].split()]
+        gm, gc = np.array(vals[2:2 + N]), np.array(vals[2 + N:]).reshape(N, N)
+        om, oc = np.array(rec["u_mean"][s]), np.array(rec["u_chol"][s])
+        assert rel(gm[:d], om[:d]) <= 1e-8, s
+        assert max(rel(gm[i * d:(i + 1) * d], om[i * d:(i + 1) * d]) for i in range(N // d)) <= 1e-5, s
+        assert rel(gc @ gc.T, oc @ oc.T) <= 1e-5, s
+        assert abs(int(vals[1]) - steps_o[s]) <= 1, s
