@@ -94,7 +94,9 @@ enum {
   PDQ_INSTANCE_OK = 0,
   PDQ_INSTANCE_MAX_STEPS = 1,   /* attempt bound reached before the last checkpoint */
   PDQ_INSTANCE_DT_UNDERFLOW = 2,/* step size collapsed below 1e-14 * max(1, |t|) */
-  PDQ_INSTANCE_NONFINITE = 3    /* NaN or Inf in the error norm or the state */
+  PDQ_INSTANCE_NONFINITE = 3,   /* NaN or Inf in the error norm or the state */
+  PDQ_INSTANCE_RECORD_FULL = 4  /* pdq_terminal_fwd: more accepted steps than the record holds
+                                   (the solve itself finished; rerun with a larger capacity) */
 };
 
 typedef struct pdq_config {
@@ -276,6 +278,51 @@ pdq_status pdq_lml_fwd(const pdq_config* config, const pdq_lml_adjoint_args* arg
                        size_t workspace_bytes, void* stream);
 pdq_status pdq_lml_bwd(const pdq_config* config, const pdq_lml_adjoint_args* args, void* workspace,
                        size_t workspace_bytes, void* stream);
+#endif
+
+/* Reverse-mode (adjoint) gradient of adaptive terminal values, split into
+ * the forward and backward halves of a custom VJP: the counterpart of
+ * jax.vjp / jax.grad through solve_adaptive_terminal_values with its
+ * stop-gradient on the step size (probdiffeq/_ivpsolve/
+ * solvers_via_adaptive_steps.py:16-43, 294-301).
+ * pdq_terminal_fwd solves exactly as pdq_solve_adaptive (same args, same
+ * outputs) and records in `record`, per instance, the size of every accepted
+ * step and the state before every checkpoint_every-th one, for at most
+ * `capacity` accepted steps; an instance that takes more finishes its solve
+ * and reports PDQ_INSTANCE_RECORD_FULL (rerun with capacity >= its
+ * num_steps).  pdq_terminal_bwd then reads the record (same config, same
+ * capacity and checkpoint_every, record untouched in between), recomputes
+ * each segment of checkpoint_every steps from its state and differentiates
+ * the mean recursion in reverse, writing
+ *   grad_params (B, P) = sum over (i, j) of cotangent[b, i, j] d u_mean[b, i, j] / d params
+ *   grad_y0     (B, d) = the same for d / d y0
+ * for the terminal mean u_mean (B, 1, n, d) (its Taylor coefficients at t1).
+ * Instances whose forward status is not PDQ_INSTANCE_OK get NaN gradients.
+ * config: ssm isotropic, constraint TS0, strategy filter, error
+ * residual_std, clip_dt, damp 0, solver plain or mle (whose prediction runs
+ * at unit scale, so the gains do not depend on the parameters), built-in
+ * field; args: terminal_only, two save points; kernel_variant 0 or 1.  The
+ * record must be 16-byte aligned. */
+typedef struct pdq_terminal_adjoint_args {
+  int64_t num_instances;     /* B, as in the forward call */
+  int32_t capacity;          /* accepted steps the record holds per instance, >= 1 */
+  int32_t checkpoint_every;  /* accepted steps between stored states, 1 <= C <= capacity */
+  const double* params;      /* (B, P), as in the forward call */
+  const double* y0;          /* (B, d), as in the forward call */
+  const int32_t* num_steps;  /* (B,) the forward call's num_steps (accepted steps to t1) */
+  const int32_t* status;     /* (B,) the forward call's status */
+  const double* cotangent;   /* (B, n, d) d loss / d u_mean at t1 */
+  double* grad_params;       /* (B, P) output, or NULL */
+  double* grad_y0;           /* (B, d) output, or NULL */
+} pdq_terminal_adjoint_args;
+
+#if !defined(__CUDACC_RTC__)
+pdq_status pdq_terminal_record_size(const pdq_config* config, int64_t num_instances, int32_t capacity,
+                                    int32_t checkpoint_every, size_t* bytes);
+pdq_status pdq_terminal_fwd(const pdq_config* config, const pdq_adaptive_args* args, int32_t capacity,
+                            int32_t checkpoint_every, void* record, size_t record_bytes, void* stream);
+pdq_status pdq_terminal_bwd(const pdq_config* config, const pdq_terminal_adjoint_args* args, void* record,
+                            size_t record_bytes, void* stream);
 #endif
 
 /* Size of the scratch array inside the library used by pdq_lml_fixed_grid_static. */

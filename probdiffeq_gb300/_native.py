@@ -5,6 +5,7 @@ loudly when the library is missing: there is no CPU fallback.
 """
 
 import ctypes
+import math
 import os
 
 import torch
@@ -156,6 +157,21 @@ class PdqLmlAdjointArgs(ctypes.Structure):
         ("grad_y0", ctypes.c_void_p),
     ]
 
+class PdqTerminalAdjointArgs(ctypes.Structure):
+    _fields_ = [
+        ("num_instances", ctypes.c_int64),
+        ("capacity", ctypes.c_int32),
+        ("checkpoint_every", ctypes.c_int32),
+        ("params", ctypes.c_void_p),
+        ("y0", ctypes.c_void_p),
+        ("num_steps", ctypes.c_void_p),
+        ("status", ctypes.c_void_p),
+        ("cotangent", ctypes.c_void_p),
+        ("grad_params", ctypes.c_void_p),
+        ("grad_y0", ctypes.c_void_p),
+    ]
+
+
 # Every symbol include/pdq.h declares, with its ctypes signature.
 SIGNATURES = {
     "pdq_abi_version": (ctypes.c_uint32, []),
@@ -198,6 +214,20 @@ SIGNATURES = {
     "pdq_lml_fixed_grid_static": (
         ctypes.c_int,
         [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqLmlArgs), ctypes.c_void_p],
+    ),
+    "pdq_terminal_record_size": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "pdq_terminal_fwd": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqAdaptiveArgs), ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+         ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "pdq_terminal_bwd": (
+        ctypes.c_int,
+        [ctypes.POINTER(PdqConfig), ctypes.POINTER(PdqTerminalAdjointArgs), ctypes.c_void_p, ctypes.c_size_t,
+         ctypes.c_void_p],
     ),
     "pdq_sample_markov": (ctypes.c_int, [ctypes.POINTER(PdqSampleArgs), ctypes.c_void_p]),
     "pdq_offgrid_marginals": (ctypes.c_int, [ctypes.POINTER(PdqOffgridArgs), ctypes.c_void_p]),
@@ -320,6 +350,71 @@ def solve_adaptive(cfg, save_at, params, y0, dt0, terminal_only, outputs, stream
 
 OPTIONAL_OUTPUTS = ("cond_A", "cond_noise_mean", "cond_noise_chol", "cond_to_latent", "cond_to_observed", "filter_mean", "filter_chol")
 SENSITIVITY_OUTPUTS = ("u_mean_d_params", "u_mean_d_y0")
+
+
+INSTANCE_RECORD_FULL = 4
+TERMINAL_CAPACITY = 2048  # first guess of accepted steps per instance for terminal_fwd
+
+
+def terminal_record_size(cfg, B, capacity, checkpoint_every):
+    nbytes = ctypes.c_size_t(0)
+    check(load().pdq_terminal_record_size(ctypes.byref(cfg), int(B), int(capacity), int(checkpoint_every),
+                                          ctypes.byref(nbytes)), "pdq_terminal_record_size")
+    return int(nbytes.value)
+
+
+def terminal_fwd(cfg, save_at, params, y0, dt0, *, capacity=None, checkpoint_every=None, stream=None):
+    """Terminal values (``pdq_terminal_fwd``) with the record the adjoint
+    pass reads.  Device tensors as ``solve_adaptive`` (save_at (B, 2)).
+    ``capacity`` None: a first guess, and when an instance took more accepted
+    steps (PDQ_INSTANCE_RECORD_FULL; one host synchronisation) a rerun with
+    exactly the largest count; ``checkpoint_every`` None: round(sqrt(capacity)).
+    Returns the outputs of ``alloc_outputs`` plus the record ("_record",
+    "_capacity", "_checkpoint_every")."""
+    B = y0.shape[0]
+    outputs = alloc_outputs(cfg, B, 2, True, y0.device)
+    cap = int(capacity) if capacity is not None else TERMINAL_CAPACITY
+    lib = load()
+    while True:
+        ckpt = min(cap, int(checkpoint_every) if checkpoint_every else max(1, round(math.sqrt(cap))))
+        nbytes = terminal_record_size(cfg, B, cap, ckpt)
+        rec = torch.empty(nbytes, dtype=torch.uint8, device=y0.device)
+        args = PdqAdaptiveArgs()
+        args.num_instances = B
+        args.num_save_at = 2
+        args.terminal_only = 1
+        args.save_at, args.params, args.y0, args.dt0 = _ptr(save_at), _ptr(params), _ptr(y0), _ptr(dt0)
+        for k in ("u_mean", "u_chol", "output_scale", "t", "num_steps", "num_attempts", "status"):
+            setattr(args, k, _ptr(outputs[k]))
+        check(lib.pdq_terminal_fwd(ctypes.byref(cfg), ctypes.byref(args), cap, ckpt, _ptr(rec), ctypes.c_size_t(nbytes),
+                                   _stream_handle(stream)), "pdq_terminal_fwd")
+        if capacity is None and bool((outputs["status"] == INSTANCE_RECORD_FULL).any()):
+            cap = int(outputs["num_steps"].max())
+            continue
+        break
+    outputs.update(_record=rec, _capacity=cap, _checkpoint_every=ckpt)
+    return outputs
+
+
+def terminal_bwd(cfg, fwd, params, y0, cotangent, *, params_grad=True, y0_grad=True, stream=None):
+    """The adjoint pass (``pdq_terminal_bwd``) for a cotangent (B, n, d) of
+    the terminal mean of ``terminal_fwd``'s outputs ``fwd`` (same cfg,
+    params and y0); returns (grad_params (B, P) or None, grad_y0 (B, d) or None)."""
+    B = y0.shape[0]
+    f64 = dict(dtype=torch.float64, device=y0.device)
+    cot = cotangent.detach().to(dtype=torch.float64).contiguous()
+    gp = torch.empty((B, params.shape[1]), **f64) if params_grad else None
+    gy = torch.empty((B, y0.shape[1]), **f64) if y0_grad else None
+    t = PdqTerminalAdjointArgs()
+    t.num_instances = B
+    t.capacity, t.checkpoint_every = fwd["_capacity"], fwd["_checkpoint_every"]
+    t.params, t.y0 = _ptr(params), _ptr(y0)
+    t.num_steps, t.status = _ptr(fwd["num_steps"]), _ptr(fwd["status"])
+    t.cotangent, t.grad_params, t.grad_y0 = _ptr(cot), _ptr(gp), _ptr(gy)
+    rec = fwd["_record"]
+    check(load().pdq_terminal_bwd(ctypes.byref(cfg), ctypes.byref(t), _ptr(rec), ctypes.c_size_t(rec.numel()),
+                                  _stream_handle(stream)), "pdq_terminal_bwd")
+    return gp, gy
 
 
 def workspace_size(cfg, B, S):

@@ -110,19 +110,53 @@ class _TerminalValues(torch.autograd.Function):
         return g_params, g_y0, None, None, None, None, None
 
 
+class _TerminalValuesAdjoint(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, params, y0, cfg, t0, t1, dt0, stream, capacity, checkpoint_every):
+        p, y = params.detach().contiguous(), y0.detach().contiguous()
+        B = y.shape[0]
+        save_at = torch.tensor([float(t0), float(t1)], dtype=torch.float64, device=y.device).expand(B, 2).contiguous()
+        dt = torch.as_tensor(dt0, dtype=torch.float64, device=y.device).expand(B).contiguous()
+        out = _native.terminal_fwd(cfg, save_at, p, y, dt, capacity=capacity, checkpoint_every=checkpoint_every,
+                                   stream=stream)
+        ctx.cfg, ctx.fwd, ctx.inputs, ctx.stream = cfg, out, (p, y), stream
+        ctx.mark_non_differentiable(out["status"])
+        return out["u_mean"][:, 0], out["status"]
+
+    @staticmethod
+    def backward(ctx, g_mean, g_status):
+        p, y = ctx.inputs
+        gp, gy = _native.terminal_bwd(ctx.cfg, ctx.fwd, p, y, g_mean, params_grad=ctx.needs_input_grad[0],
+                                      y0_grad=ctx.needs_input_grad[1], stream=ctx.stream)
+        return gp, gy, None, None, None, None, None, None, None
+
+
 def terminal_values(params, y0, *, t0, t1, field="lotka_volterra", num_derivatives=4, solver="mle", atol=1e-6,
-                    rtol=1e-6, dt0=0.1, precision="float64", stream=None):
+                    rtol=1e-6, dt0=0.1, precision="float64", stream=None, mode="forward", capacity=None,
+                    checkpoint_every=None):
     """Differentiable terminal values of an isotropic TS0 filter solve.
 
     params (B, P) and y0 (B, d) float64 CUDA tensors (``requires_grad`` for
     gradients).  Returns (u_mean (B, n, d) -- the Taylor coefficients at t1 --,
-    status (B,) int32).  The backward pass contracts the cotangent with the
-    forward-mode sensitivities the same launch computed (P + d threads per
-    instance), the counterpart of ``jax.grad`` through
+    status (B,) int32): the counterpart of ``jax.grad`` through
     ``solve_adaptive_terminal_values`` with its stop-gradient on the step size
     (probdiffeq/_ivpsolve/solvers_via_adaptive_steps.py:16-43, 294-301).
+
+    mode "forward": the backward pass contracts the cotangent with the
+    forward-mode sensitivities the same launch computed (P + d threads per
+    instance).  mode "adjoint": the forward pass records the accepted steps
+    (``pdq_terminal_fwd``; ``capacity`` accepted steps per instance, None for
+    a guess and one rerun if it was too small; the state every
+    ``checkpoint_every`` steps, None for sqrt(capacity)), the backward pass
+    differentiates them in reverse (``pdq_terminal_bwd``) at a cost
+    independent of P + d.  The adjoint takes solver "none" or "mle".
     """
     cfg = ensemble.make_config(field=field, num_derivatives=num_derivatives, ode_dim=y0.shape[-1], ssm="isotropic",
                                constraint="ts0", strategy="filter", solver=solver, precision=precision, atol=atol,
                                rtol=rtol, clip_dt=True)
+    if mode == "adjoint":
+        return _TerminalValuesAdjoint.apply(params, y0, cfg, float(t0), float(t1), dt0, stream, capacity,
+                                            checkpoint_every)
+    if mode != "forward":
+        raise ValueError(f"unknown gradient mode {mode!r} (expected 'forward' or 'adjoint')")
     return _TerminalValues.apply(params, y0, cfg, float(t0), float(t1), dt0, stream)

@@ -121,5 +121,50 @@ def build(force=False, verbose=False):
     return LIB
 
 
+JAX_FFI_SRC = os.path.join(PKG, "jax_ffi", "ffi_pdq.cc")
+JAX_FFI_LIB = os.path.join(PKG, "libpdq_jax_ffi.so")
+
+
+def jax_ffi_include_dir():
+    """The directory holding jaxlib's xla/ffi/api/ffi.h, or None when jaxlib is not installed."""
+    try:
+        import jax.ffi
+
+        cands = [jax.ffi.include_dir()]
+    except Exception:  # no jax, or a jax without ffi.include_dir
+        cands = []
+    try:
+        import jaxlib
+
+        cands.append(os.path.join(os.path.dirname(jaxlib.__file__), "include"))
+    except Exception:
+        pass
+    for d in cands:
+        if os.path.exists(os.path.join(d, "xla", "ffi", "api", "ffi.h")):
+            return d
+    return None
+
+
+def build_jax_ffi(force=False):
+    """Compile the XLA FFI handlers (jax_ffi/ffi_pdq.cc) against jaxlib's
+    headers into libpdq_jax_ffi.so, linked to libpdq_gb300.so; returns its
+    path, or None (nothing built) when jaxlib's headers are not found."""
+    inc = jax_ffi_include_dir()
+    if inc is None:
+        return None
+    lib = build()
+    if not force and os.path.exists(JAX_FFI_LIB) and os.path.getmtime(JAX_FFI_LIB) >= max(
+            os.path.getmtime(JAX_FFI_SRC), os.path.getmtime(lib)):
+        return JAX_FFI_LIB
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc_path())), "include")
+    cmd = [shutil.which("g++") or "g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-I" + inc, "-I" + INCLUDE,
+           "-I" + cuda_inc, JAX_FFI_SRC, "-o", JAX_FFI_LIB, "-L" + PKG, "-lpdq_gb300", "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"jax ffi build failed:\n{res.stdout}\n{res.stderr}")
+    return JAX_FFI_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_jax_ffi(force="--force" in sys.argv) or "jax ffi handlers: jaxlib headers not found, not built")

@@ -70,6 +70,11 @@ struct IsoArgs {
   // (B, S_out, n, d, P) and d u_mean / d y0 (B, S_out, n, d, d)
   double* tan_params;
   double* tan_y0;       // (B, S, n, n), calibrated
+  // record of the accepted steps for the terminal-value adjoint (REC only;
+  // layout in tv_adjoint.cuh): step sizes, and the state before every
+  // rec_ckpt-th accepted step, for at most rec_capacity accepted steps
+  void* record;
+  int32_t rec_capacity, rec_ckpt;
 };
 
 // A constant in the kernel's precision: the float copy for float, else the double.
@@ -1035,13 +1040,20 @@ PDQ_D void write_tangent(const IsoArgs& a, int64_t rec, int k, const T (&dm)[NU 
 // reference stops gradients through dt), and with H = e_1 the covariance
 // recursion does not depend on the parameters, so the tangent of an update
 // is dm' = dmp - gain (dmp_1 - df), dmp = p A p^-1 dm, df = J_f dmp_0 + df/dtheta.
-template <typename T, int NU, class F, bool INTERP, bool FP = false, bool GEN = true, bool TAN = false>
+// REC (lean TS0 filter, exact landings): records each accepted step's size
+// and the state before every rec_ckpt-th accepted step for the
+// terminal-value adjoint (tv_adjoint.cuh); an instance with more accepted
+// steps than rec_capacity finishes its solve and reports
+// PDQ_INSTANCE_RECORD_FULL.
+template <typename T, int NU, class F, bool INTERP, bool FP = false, bool GEN = true, bool TAN = false, bool REC = false>
 __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   constexpr int n = NU + 1;
   constexpr int D = F::D;
   constexpr int P = F::P;
   constexpr int OUT = 1;  // ODE u' = f(u): observe coefficient 1 (problems.py:283-295)
   static_assert(!(TAN && (FP || GEN)), "sensitivities: TS0 filter only");
+  static_assert(!(REC && (FP || GEN || TAN || INTERP)), "record: the lean TS0 filter with exact landings only");
+  bool rec_full = false;
   const int64_t gtid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t b = TAN ? gtid / (P + D) : gtid;
   const int kdir = TAN ? int(gtid % (P + D)) : 0;
@@ -1369,6 +1381,27 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
       dt = dt_new;
       pi_prev = pi_new;
       if (accepted) {
+        if constexpr (REC) {
+          // element e of instance b at record[e * B + b]: the step size, then
+          // every rec_ckpt steps the state the step starts from
+          if (num_steps < a.rec_capacity) {
+            T* rec = reinterpret_cast<T*>(a.record);
+            rec[int64_t(num_steps) * a.B + b] = h;
+            if (num_steps % a.rec_ckpt == 0) {
+              int64_t e = int64_t(a.rec_capacity) + int64_t(num_steps / a.rec_ckpt) * (n * D + n * n);
+#pragma unroll
+              for (int i = 0; i < n; ++i)
+#pragma unroll
+                for (int j = 0; j < D; ++j) rec[(e++) * a.B + b] = m[i][j];
+#pragma unroll
+              for (int i = 0; i < n; ++i)
+#pragma unroll
+                for (int j = 0; j < n; ++j) rec[(e++) * a.B + b] = L[i][j];
+            }
+          } else {
+            rec_full = true;
+          }
+        }
         if constexpr (INTERP) {
           ti = t;
 #pragma unroll
@@ -1614,7 +1647,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
     }
   }
   a.num_attempts[b] = attempts;
-  a.status[b] = status;
+  a.status[b] = (REC && rec_full && status == PDQ_INSTANCE_OK) ? int(PDQ_INSTANCE_RECORD_FULL) : status;
 }
 
 }  // namespace pdq

@@ -11,6 +11,7 @@
 #include "lml_launch.cuh"
 #include "iso_launch.cuh"
 #include "nvrtc_fields.h"
+#include "tv_launch.cuh"
 #include "pdq.h"
 
 namespace {
@@ -72,6 +73,88 @@ pdq_status validate_common(const pdq_config* c) {
   if (!(ipb == 0 || (ipb >= 1 && ipb <= 4) || ipb == 8 || ipb == 16 || ipb == 32 || ipb == 64))
     return PDQ_ERROR_INVALID_VALUE;
   return PDQ_SUCCESS;
+}
+
+// The isotropic kernels' arguments from the configuration and the solve's
+// buffers (the mapping, the posterior outputs and the record stay zero).
+void iso_args_fill(const pdq_config* c, const pdq_adaptive_args* args, pdq::IsoArgs& a) {
+  memset(&a, 0, sizeof(a));
+  a.B = args->num_instances;
+  a.S = args->num_save_at;
+  a.terminal_only = args->terminal_only ? 1 : 0;
+  a.solver = c->solver;
+  a.control = c->control;
+  a.clip_dt = c->clip_dt ? 1 : 0;
+  a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
+  a.ts1 = c->constraint == PDQ_CONSTRAINT_TS1 ? 1 : 0;
+  a.state_error = c->error == PDQ_ERROR_STATE_STD ? 1 : 0;
+  a.safety = c->safety;
+  a.factor_min = c->factor_min;
+  a.factor_max = c->factor_max;
+  a.exp_i = c->exponent_integral;
+  a.exp_p = c->exponent_proportional;
+  a.atol = c->atol;
+  a.rtol = c->rtol;
+  a.eps = c->eps;
+  a.damp = c->damp;
+  a.max_attempts = c->max_attempts;
+  iwp_q1(c->num_derivatives, a.q1);
+  for (int i = 0; i < pdq::kMaxN; ++i)
+    for (int j = 0; j < pdq::kMaxN; ++j) a.q1f[i][j] = float(a.q1[i][j]);
+  a.safety_f = float(a.safety);
+  a.factor_min_f = float(a.factor_min);
+  a.factor_max_f = float(a.factor_max);
+  a.exp_i_f = float(a.exp_i);
+  a.exp_p_f = float(a.exp_p);
+  a.atol_f = float(a.atol);
+  a.rtol_f = float(a.rtol);
+  a.eps_f = float(a.eps);
+  a.damp_f = float(a.damp);
+  a.save_at = args->save_at;
+  a.params = args->params;
+  a.y0 = args->y0;
+  a.dt0 = args->dt0;
+  a.u_mean = args->u_mean;
+  a.u_chol = args->u_chol;
+  a.output_scale = args->output_scale;
+  a.t_out = args->t;
+  a.num_steps = args->num_steps;
+  a.num_attempts = args->num_attempts;
+  a.status = args->status;
+}
+
+// The terminal-value adjoint's configuration rules (include/pdq.h).
+pdq_status terminal_check(const pdq_config* c) {
+  const pdq_status st = validate_common(c);
+  if (st != PDQ_SUCCESS) return st;
+  if (c->ssm != PDQ_SSM_ISOTROPIC || c->constraint != PDQ_CONSTRAINT_TS0 || c->strategy != PDQ_STRATEGY_FILTER ||
+      c->error != PDQ_ERROR_RESIDUAL_STD || !c->clip_dt || c->damp != 0.0 ||
+      (c->solver != PDQ_SOLVER_PLAIN && c->solver != PDQ_SOLVER_MLE) || c->field >= PDQ_FIELD_USER_BASE ||
+      c->kernel_variant > 1)
+    return PDQ_ERROR_UNSUPPORTED;
+  if (!(c->instances_per_block == 0 || c->instances_per_block == 64)) return PDQ_ERROR_INVALID_VALUE;
+  return PDQ_SUCCESS;
+}
+
+using TvLaunch = cudaError_t (*)(const pdq::IsoArgs&, const pdq::TvAdjArgs*, int, cudaStream_t);
+
+TvLaunch tv_launcher(const pdq_config* c) {
+  const bool f64 = c->precision == PDQ_PRECISION_F64;
+  switch (c->field) {
+    case PDQ_FIELD_LOTKA_VOLTERRA: return f64 ? pdq_launch_tv_lv_f64 : pdq_launch_tv_lv_f32;
+    case PDQ_FIELD_VAN_DER_POL: return f64 ? pdq_launch_tv_vdp_f64 : pdq_launch_tv_vdp_f32;
+    case PDQ_FIELD_FITZHUGH_NAGUMO: return f64 ? pdq_launch_tv_fhn_f64 : pdq_launch_tv_fhn_f32;
+    default: return nullptr;
+  }
+}
+
+// Bytes of the record and, after it at a 256-byte boundary, the adjoint pass's scratch.
+void terminal_sizes(const pdq_config* c, int64_t B, int32_t capacity, int32_t ckpt, size_t* rec_bytes,
+                    size_t* total) {
+  const size_t elem = c->precision == PDQ_PRECISION_F64 ? 8 : 4;
+  const size_t rec = size_t(B) * size_t(pdq::tv_record_elems(c->num_derivatives, c->ode_dim, capacity, ckpt)) * elem;
+  *rec_bytes = (rec + 255) / 256 * 256;
+  *total = *rec_bytes + size_t(B) * size_t(pdq::tv_scratch_elems(c->num_derivatives, c->ode_dim, ckpt)) * elem;
 }
 
 }  // namespace
@@ -180,49 +263,7 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
       if (workspace == nullptr || workspace_bytes < need) return PDQ_ERROR_WORKSPACE;
     }
     pdq::IsoArgs a;
-    memset(&a, 0, sizeof(a));
-    a.B = args->num_instances;
-    a.S = args->num_save_at;
-    a.terminal_only = args->terminal_only ? 1 : 0;
-    a.solver = c->solver;
-    a.control = c->control;
-    a.clip_dt = c->clip_dt ? 1 : 0;
-    a.correct = c->correct_asymptotic_underconfidence ? 1 : 0;
-    a.ts1 = c->constraint == PDQ_CONSTRAINT_TS1 ? 1 : 0;
-    a.state_error = c->error == PDQ_ERROR_STATE_STD ? 1 : 0;
-    a.safety = c->safety;
-    a.factor_min = c->factor_min;
-    a.factor_max = c->factor_max;
-    a.exp_i = c->exponent_integral;
-    a.exp_p = c->exponent_proportional;
-    a.atol = c->atol;
-    a.rtol = c->rtol;
-    a.eps = c->eps;
-    a.damp = c->damp;
-    a.max_attempts = c->max_attempts;
-    iwp_q1(c->num_derivatives, a.q1);
-    for (int i = 0; i < pdq::kMaxN; ++i)
-      for (int j = 0; j < pdq::kMaxN; ++j) a.q1f[i][j] = float(a.q1[i][j]);
-    a.safety_f = float(a.safety);
-    a.factor_min_f = float(a.factor_min);
-    a.factor_max_f = float(a.factor_max);
-    a.exp_i_f = float(a.exp_i);
-    a.exp_p_f = float(a.exp_p);
-    a.atol_f = float(a.atol);
-    a.rtol_f = float(a.rtol);
-    a.eps_f = float(a.eps);
-    a.damp_f = float(a.damp);
-    a.save_at = args->save_at;
-    a.params = args->params;
-    a.y0 = args->y0;
-    a.dt0 = args->dt0;
-    a.u_mean = args->u_mean;
-    a.u_chol = args->u_chol;
-    a.output_scale = args->output_scale;
-    a.t_out = args->t;
-    a.num_steps = args->num_steps;
-    a.num_attempts = args->num_attempts;
-    a.status = args->status;
+    iso_args_fill(c, args, a);
     const bool interp = !c->clip_dt;
     if (c->kernel_variant < 0 || c->kernel_variant > 3) return PDQ_ERROR_INVALID_VALUE;
     // 0 (auto) and 1: one thread per instance; 2 / 3: the lane-cooperative
@@ -662,6 +703,83 @@ pdq_status pdq_lml_bwd(const pdq_config* c, const pdq_lml_adjoint_args* args, vo
 }
 
 }  // extern "C"
+
+extern "C" pdq_status pdq_terminal_record_size(const pdq_config* c, int64_t B, int32_t capacity,
+                                               int32_t checkpoint_every, size_t* bytes) {
+  if (bytes == nullptr) return PDQ_ERROR_INVALID_VALUE;
+  const pdq_status st = terminal_check(c);
+  if (st != PDQ_SUCCESS) return st;
+  if (B < 0 || capacity < 1 || checkpoint_every < 1 || checkpoint_every > capacity) return PDQ_ERROR_INVALID_VALUE;
+  size_t rec = 0;
+  terminal_sizes(c, B, capacity, checkpoint_every, &rec, bytes);
+  return PDQ_SUCCESS;
+}
+
+extern "C" pdq_status pdq_terminal_fwd(const pdq_config* c, const pdq_adaptive_args* args, int32_t capacity,
+                                       int32_t checkpoint_every, void* record, size_t record_bytes, void* stream_ptr) {
+  pdq::NvtxRange nvtx_range("pdq_terminal_fwd");
+  const pdq_status st = terminal_check(c);
+  if (st != PDQ_SUCCESS) return st;
+  if (args == nullptr || args->num_instances < 0 || args->num_save_at != 2 || !args->terminal_only)
+    return PDQ_ERROR_INVALID_VALUE;
+  if (capacity < 1 || checkpoint_every < 1 || checkpoint_every > capacity) return PDQ_ERROR_INVALID_VALUE;
+  if (args->u_mean_d_params || args->u_mean_d_y0 || args->cond_A || args->filter_mean) return PDQ_ERROR_UNSUPPORTED;
+  if (args->num_instances == 0) return PDQ_SUCCESS;
+  if (!args->save_at || !args->params || !args->y0 || !args->dt0 || !args->u_mean || !args->u_chol ||
+      !args->output_scale || !args->t || !args->num_steps || !args->num_attempts || !args->status)
+    return PDQ_ERROR_INVALID_VALUE;
+  size_t rec = 0, need = 0;
+  terminal_sizes(c, args->num_instances, capacity, checkpoint_every, &rec, &need);
+  if (record == nullptr || record_bytes < need || (reinterpret_cast<uintptr_t>(record) & 15) != 0)
+    return PDQ_ERROR_WORKSPACE;
+  pdq::IsoArgs a;
+  iso_args_fill(c, args, a);
+  a.record = record;
+  a.rec_capacity = capacity;
+  a.rec_ckpt = checkpoint_every;
+  const TvLaunch launch = tv_launcher(c);
+  if (launch == nullptr) return PDQ_ERROR_UNSUPPORTED;
+  const cudaError_t err = launch(a, nullptr, c->num_derivatives, static_cast<cudaStream_t>(stream_ptr));
+  return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+}
+
+extern "C" pdq_status pdq_terminal_bwd(const pdq_config* c, const pdq_terminal_adjoint_args* t, void* record,
+                                       size_t record_bytes, void* stream_ptr) {
+  pdq::NvtxRange nvtx_range("pdq_terminal_bwd");
+  const pdq_status st = terminal_check(c);
+  if (st != PDQ_SUCCESS) return st;
+  if (t == nullptr || t->num_instances < 0) return PDQ_ERROR_INVALID_VALUE;
+  if (t->capacity < 1 || t->checkpoint_every < 1 || t->checkpoint_every > t->capacity) return PDQ_ERROR_INVALID_VALUE;
+  if (t->num_instances == 0) return PDQ_SUCCESS;
+  if (!t->params || !t->y0 || !t->num_steps || !t->status || !t->cotangent) return PDQ_ERROR_INVALID_VALUE;
+  size_t rec = 0, need = 0;
+  terminal_sizes(c, t->num_instances, t->capacity, t->checkpoint_every, &rec, &need);
+  if (record == nullptr || record_bytes < need || (reinterpret_cast<uintptr_t>(record) & 15) != 0)
+    return PDQ_ERROR_WORKSPACE;
+  pdq_adaptive_args args;
+  memset(&args, 0, sizeof(args));
+  args.num_instances = t->num_instances;
+  args.num_save_at = 2;
+  args.terminal_only = 1;
+  args.params = t->params;
+  args.y0 = t->y0;
+  pdq::IsoArgs a;
+  iso_args_fill(c, &args, a);
+  pdq::TvAdjArgs ta;
+  ta.capacity = t->capacity;
+  ta.ckpt = t->checkpoint_every;
+  ta.num_steps = t->num_steps;
+  ta.status = t->status;
+  ta.cotangent = t->cotangent;
+  ta.grad_params = t->grad_params;
+  ta.grad_y0 = t->grad_y0;
+  ta.record = record;
+  ta.scratch = static_cast<unsigned char*>(record) + rec;
+  const TvLaunch launch = tv_launcher(c);
+  if (launch == nullptr) return PDQ_ERROR_UNSUPPORTED;
+  const cudaError_t err = launch(a, &ta, c->num_derivatives, static_cast<cudaStream_t>(stream_ptr));
+  return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+}
 
 extern "C" pdq_status pdq_offgrid_marginals(const pdq_offgrid_args* args, void* stream) {
   pdq::NvtxRange nvtx_range("pdq_offgrid_marginals");

@@ -1,0 +1,4 @@
+// Terminal-value adjoint (record pass and adjoint pass) for the LotkaVolterra field in float bulk precision.
+#include "tv_launch.cuh"
+
+PDQ_DEFINE_TV_LAUNCH(pdq_launch_tv_lv_f32, float, pdq::LotkaVolterra)

@@ -9,20 +9,25 @@
 // conditionals and the backward pass), mode 2 the filter with forward-mode
 // sensitivities (P + d threads per instance), modes 3 and 4 the general
 // filter instantiation with error_state_std, with TS0 (3) or TS1 (4, the
-// Jacobian trace along d).
+// Jacobian trace along d), mode 5 the terminal-value adjoint: the record
+// pass (the lean filter with REC) and then the adjoint pass
+// (iso_tv_bwd_kernel) for a cotangent of the terminal mean.
 //
 // Input file (whitespace-separated): precision (0 float32, 1 float64) mode nu
 // B S solver control clip_dt terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
-// dt0 (B), Q1 ((nu + 1) x (nu + 1), row-major).  solver / control take the
-// PDQ_SOLVER_* / PDQ_CONTROL_* codes.
+// dt0 (B), Q1 ((nu + 1) x (nu + 1), row-major); mode 5 then the cotangent
+// (B x (nu + 1) x 2), the record's capacity and checkpoint_every.  solver /
+// control take the PDQ_SOLVER_* / PDQ_CONTROL_* codes.
 // Output: per instance a line "status attempts", then per output record a
 // line "t num_steps output_scale u_mean[n d] u_chol[n n]" (mode 2: followed
-// by d u_mean / d params [n d 4] and d u_mean / d y0 [n d 2]).
+// by d u_mean / d params [n d 4] and d u_mean / d y0 [n d 2]; mode 5:
+// followed by the gradients d <cotangent, u_mean> / d params [4] and / d y0 [2]).
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
 
 #include "iso_solver.cuh"
+#include "tv_adjoint.cuh"
 
 thread_local pdq_host_uint3 threadIdx, blockIdx, blockDim;
 
@@ -49,6 +54,13 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   std::vector<int32_t> steps(B * S_out), attempts(B), status(B);
   std::vector<double> tan_p(MODE == 2 ? B * S_out * n * D * P : 0), tan_y(MODE == 2 ? B * S_out * n * D * D : 0);
   std::vector<T> ws(MODE == 1 ? B * (S - 1) * iso_cond_floats<NU, D>() : 0);
+  std::vector<double> cot(MODE == 5 ? B * n * D : 0), grad_p(MODE == 5 ? B * P : 0), grad_y(MODE == 5 ? B * D : 0);
+  std::vector<T> rec;
+  int cap = 0, ckpt = 0;
+  if constexpr (MODE == 5) {
+    if (!read_all(in, cot) || fscanf(in, "%d %d", &cap, &ckpt) != 2 || cap < 1 || ckpt < 1 || ckpt > cap) return 2;
+    rec.assign(B * (tv_record_elems(NU, D, cap, ckpt) + tv_scratch_elems(NU, D, ckpt)), T(0));
+  }
 
   IsoArgs a;
   memset(&a, 0, sizeof(a));
@@ -106,6 +118,11 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
     a.tan_y0 = tan_y.data();
     a.tangents = 1;
   }
+  if (MODE == 5) {
+    a.record = rec.data();
+    a.rec_capacity = cap;
+    a.rec_ckpt = ckpt;
+  }
 
   const int block = 64;
   blockDim = {uint32_t(block), 1, 1};
@@ -118,6 +135,24 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
     if constexpr (MODE == 1) iso_adaptive_kernel<T, NU, F, INTERP, true, true>(a);
     if constexpr (MODE == 2) iso_adaptive_kernel<T, NU, F, INTERP, false, false, true>(a);
     if constexpr (MODE == 3 || MODE == 4) iso_adaptive_kernel<T, NU, F, INTERP, false, true>(a);
+    if constexpr (MODE == 5 && !INTERP) iso_adaptive_kernel<T, NU, F, false, false, false, false, true>(a);
+  }
+  if constexpr (MODE == 5) {
+    TvAdjArgs ta;
+    ta.capacity = cap;
+    ta.ckpt = ckpt;
+    ta.num_steps = steps.data();
+    ta.status = status.data();
+    ta.cotangent = cot.data();
+    ta.grad_params = grad_p.data();
+    ta.grad_y0 = grad_y.data();
+    ta.record = rec.data();
+    ta.scratch = rec.data() + B * tv_record_elems(NU, D, cap, ckpt);
+    for (long long g = 0; g < padded; ++g) {
+      blockIdx = {uint32_t(g / block), 0, 0};
+      threadIdx = {uint32_t(g % block), 0, 0};
+      iso_tv_bwd_kernel<T, NU, F>(a, ta);
+    }
   }
   for (long long b = 0; b < B; ++b) {
     printf("%d %d\n", status[b], attempts[b]);
@@ -129,6 +164,10 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
       if (MODE == 2) {
         for (int e = 0; e < n * D * P; ++e) printf(" %.17g", tan_p[r * n * D * P + e]);
         for (int e = 0; e < n * D * D; ++e) printf(" %.17g", tan_y[r * n * D * D + e]);
+      }
+      if (MODE == 5) {
+        for (int e = 0; e < P; ++e) printf(" %.17g", grad_p[b * P + e]);
+        for (int e = 0; e < D; ++e) printf(" %.17g", grad_y[b * D + e]);
       }
       printf("\n");
     }
@@ -148,7 +187,7 @@ int main(int argc, char** argv) {
   if (B < 1 || S < 2) return 2;
   int rc = 2;
   const bool interp = !clip_dt;
-  const int args_ok = (mode >= 0 && mode <= 4) && (nu == 3 || nu == 4);
+  const int args_ok = (mode >= 0 && mode <= 5) && (nu == 3 || nu == 4) && (mode != 5 || (clip_dt && terminal_only && S == 2));
   if (!args_ok) return 2;
 #define PDQ_HOST_RUN(NU_, MODE_)                                                                        \
   rc = prec ? (interp ? run<double, NU_, true, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)    \
@@ -161,6 +200,9 @@ int main(int argc, char** argv) {
   if (nu == 3 && mode == 2) PDQ_HOST_RUN(3, 2);
   if (nu == 3 && mode == 3) PDQ_HOST_RUN(3, 3);
   if (nu == 3 && mode == 4) PDQ_HOST_RUN(3, 4);
+  if (nu == 4 && mode == 2) PDQ_HOST_RUN(4, 2);
+  if (nu == 4 && mode == 5) PDQ_HOST_RUN(4, 5);
+  if (nu == 3 && mode == 5) PDQ_HOST_RUN(3, 5);
 #undef PDQ_HOST_RUN
   fclose(in);
   return rc;
