@@ -473,8 +473,10 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
   PDQ_DENSE_STRUCT_SMEM;
   const int slot = int(threadIdx.x) / L;
   const LaneGroup<L> g{((1u << L) - 1u) << (slot * L), int(threadIdx.x) % L};
-  const int64_t b = int64_t(blockIdx.x) * IPW + slot;
-  if (b >= a.B) return;  // the whole group leaves together
+  // a slot past the batch shadows the last instance (reads only) so that
+  // every lane of the warp takes part in the warp-uniform attempt loop
+  const bool valid = int64_t(blockIdx.x) * IPW + slot < a.B;
+  const int64_t b = valid ? int64_t(blockIdx.x) * IPW + slot : a.B - 1;
   const Soa<T, IPW> S{reinterpret_cast<T*>(dense_struct_smem) + slot};
   const int Sn = a.S;
   const int S_out = a.terminal_only ? 1 : Sn;
@@ -517,7 +519,7 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
   T sigma_sf = T(1);
   const T damp = T(a.damp);
 
-  if (!a.terminal_only) {
+  if (valid && !a.terminal_only) {
     dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.u_mean + (b * S_out) * N, a.u_chol + (b * S_out) * N * N);
     if (g.lane == 0) {
       a.output_scale[b * S_out] = 1.0;
@@ -525,26 +527,40 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
       a.num_steps[b * S_out] = 0;
     }
   }
-  if (a.filter_mean) dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.filter_mean + (b * Sn) * N, a.filter_chol + (b * Sn) * N * N);
+  if (valid && a.filter_mean)
+    dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.filter_mean + (b * Sn) * N, a.filter_chol + (b * Sn) * N * N);
 
-  // one attempt per iteration (the retry loop flattened into the checkpoint loop)
+  // One attempt per iteration (the retry loop flattened into the checkpoint
+  // loop), warp-uniform: every group of the warp runs the attempt's
+  // arithmetic in every iteration while any group still solves, so the
+  // groups stay converged through the QRs (a group that is not stepping --
+  // done, failed, or at a checkpoint -- computes on a dummy step into its
+  // scratch slots and discards the result; only the rare checkpoint branches
+  // diverge).  Per instance the sequence of attempts and checkpoint branches
+  // is the nested loop's (solvers_via_adaptive_steps.py:196-375).
   int s = 1;
   double t_next = save_at[1];
-  while (s < Sn) {
-    if (t + a.eps < t_next) {
-      bool accepted = false;
-      {
-        const double dt_use = a.clip_dt ? fmin(dt, t_next - t) : dt;
-        if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
-          status = PDQ_INSTANCE_DT_UNDERFLOW;
-          break;
-        }
-        if (attempts >= a.max_attempts) {
-          status = PDQ_INSTANCE_MAX_STEPS;
-          break;
-        }
+  bool active = valid;
+  while (__any_sync(0xffffffffu, active)) {
+    bool stepping = active && t + a.eps < t_next;
+    bool accepted = false;
+    double dt_use = dt;
+    if (stepping) {
+      dt_use = a.clip_dt ? fmin(dt, t_next - t) : dt;
+      if (!(fabs(dt_use) > 1e-14 * fmax(1.0, fabs(t)))) {
+        status = PDQ_INSTANCE_DT_UNDERFLOW;
+        active = stepping = false;
+      } else if (attempts >= a.max_attempts) {
+        status = PDQ_INSTANCE_MAX_STEPS;
+        active = stepping = false;
+      } else {
         ++attempts;
-        const T h = T(dt_use);
+      }
+    }
+    {
+      {
+        // a group that is not stepping computes on a finite dummy step
+        const T h = stepping ? T(dt_use) : T(1);
         T pc[n], pic[n];
         precon<T, NU>(h, pc, pic);
         // u = transition(h, 1).apply_flat(mean): mean mp, chol |p| sqrt|h| Q
@@ -693,9 +709,9 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
           sumsq += double(ratio) * double(ratio);
         }
         const double norm2 = sumsq * (1.0 / D);
-        if (!(norm2 == norm2) || isinf(norm2)) {
+        if (stepping && (!(norm2 == norm2) || isinf(norm2))) {
           status = PDQ_INSTANCE_NONFINITE;
-          break;
+          active = stepping = false;
         }
         const T ep = dev_fpow(T(norm2), T(-0.5 / n));
         double factor;
@@ -703,11 +719,11 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
           factor = a.safety * double(ep);
         } else {
           factor = a.safety * double(dev_fpow(ep, T(a.exp_i))) * double(dev_fpow(dev_div(ep, T(pi_prev)), T(a.exp_p)));
-          if (norm2 <= 1.0) pi_prev = double(ep);
+          if (stepping && norm2 <= 1.0) pi_prev = double(ep);
         }
         factor = fmax(a.factor_min, fmin(factor, a.factor_max));
-        dt = factor * dt_use;
-        accepted = norm2 <= 1.0;
+        if (stepping) dt = factor * dt_use;
+        accepted = stepping && norm2 <= 1.0;
         if (accepted) {
           ti = t;
           t = t + dt_use;
@@ -742,14 +758,14 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
           sigma_sf = (a.solver == PDQ_SOLVER_DYNAMIC) ? sigma_loc : T(1);
         }
       }
-      if (!accepted) continue;  // retry in the next iteration
     }
+    // a rejected attempt retries in the next iteration; the checkpoint
+    // branches below run when the step reached or passed t_next
+    if (!active || t + a.eps < t_next) continue;
     const bool record = (!a.terminal_only) || (s == Sn - 1);
     const int s_out = a.terminal_only ? 0 : s;
     const int64_t rec = b * S_out + s_out;
-    if (t + a.eps < t_next) {
-      // interp_skip
-    } else if (t > t_next + a.eps) {
+    if (t > t_next + a.eps) {
       // interp_beyond_t1 (solvers.py:205-269)
       const T h0 = T(t_next - ti), h1 = T(t - t_next);
       if constexpr (FP) {
@@ -808,12 +824,16 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
       if (a.filter_mean)
         dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.filter_mean + (b * Sn + s) * N, a.filter_chol + (b * Sn + s) * N * N);
     }
-    if (!(t + a.eps < t_next)) {  // checkpoint s done
-      ++s;
-      if (s < Sn) t_next = save_at[s];
+    // checkpoint s done
+    ++s;
+    if (s < Sn) {
+      t_next = save_at[s];
+    } else {
+      active = false;
     }
   }
 
+  if (!valid) return;
   // ---- finalize (solvers.py:439-480, 601-633, 735-767) ----
   double scale = 1.0;
   if (status == PDQ_INSTANCE_OK && a.solver == PDQ_SOLVER_MLE) {

@@ -41,6 +41,7 @@ inline T __shfl_xor_sync(unsigned, T v, int, int = 32) {
   return v;
 }
 inline void __syncwarp(unsigned = 0xffffffffu) {}
+inline bool __any_sync(unsigned, bool p) { return p; }  // one lane: its own predicate
 inline void __syncthreads() {}
 inline void __threadfence() {}
 inline double __longlong_as_double(long long v) {

@@ -222,8 +222,14 @@ def test_vdp_mu30_100_save_points_matches_fixture(precision):
     (the oracle's 1.9e4 accepted steps, 3.2e4 attempts; the oracle output is
     the committed fixture ``tests/golden/vdp_dense_mu30.json``), the default
     (structure-exploiting) kernel.  Float64: the live-oracle tolerances at
-    every save point; float32: the solution within 1e-3 and accepted steps
+    every save point.  Float32: matched accuracy -- its error against the
+    exact solution (scipy Radau, rtol = atol = 1e-12) within 2x the float64
+    oracle's own error against it, in the median and at the maximum over the
+    save points (the solver's error at rtol 1e-5 reaches several percent at
+    the relaxation oscillations' fast transitions), and accepted steps
     within 2 %."""
+    import scipy.integrate
+
     from tests.golden import make_golden
 
     gold = make_golden.load("vdp_dense_mu30.json")
@@ -233,6 +239,16 @@ def test_vdp_mu30_100_save_points_matches_fixture(precision):
     out = gpu_dense("van_der_pol", [[mu]], [gold["y0"]], save_at, precision)
     assert int(out["status"][0]) == 0
     steps_o = [0] + list(rec["num_steps"])
+    if precision == "float32":
+        truth = scipy.integrate.solve_ivp(
+            lambda t, u: [u[1], mu * ((1 - u[0] ** 2) * u[1] - u[0])], (0.0, save_at[-1]), gold["y0"],
+            method="Radau", rtol=1e-12, atol=1e-12, t_eval=save_at,
+            jac=lambda t, u: [[0.0, 1.0], [mu * (-2 * u[0] * u[1] - 1), mu * (1 - u[0] ** 2)]]).y.T
+        scale = np.abs(truth).max(axis=1)
+        e32 = np.abs(out["u_mean"][0, :, :2].numpy() - truth).max(axis=1) / scale
+        e64 = np.abs(np.array([m[:2] for m in rec["u_mean"]]) - truth).max(axis=1) / scale
+        assert np.median(e32) <= 2 * np.median(e64), (np.median(e32), np.median(e64))
+        assert e32.max() <= 2 * e64.max(), (e32.max(), e64.max())
     for s in range(len(save_at)):
         om = torch.tensor(rec["u_mean"][s], dtype=torch.float64)
         oc = torch.tensor(rec["u_chol"][s], dtype=torch.float64)
@@ -243,7 +259,6 @@ def test_vdp_mu30_100_save_points_matches_fixture(precision):
             assert rel(gc @ gc.T, oc @ oc.T) <= 1e-5, s
             allowed = 1
         else:
-            assert rel(gm[:2], om[:2]) <= 1e-3, s
             assert torch.isfinite(gc).all()
             allowed = max(1, math.ceil(0.02 * steps_o[s]))
         assert abs(int(out["num_steps"][0, s]) - steps_o[s]) <= allowed, (s, int(out["num_steps"][0, s]), steps_o[s])
