@@ -438,6 +438,24 @@ pdq_status pdq_register_field(const char* name, const char* source, int32_t dim,
                               int32_t* field_id, char* log, size_t log_bytes);
 #endif
 
+/* Register a stencil field for the block-diagonal kernel (any d, periodic
+ * grid), compiled at run time like pdq_register_field.  `source` defines
+ *   struct Stencil {
+ *     static constexpr int P = <number of parameters>;
+ *     template <typename S, typename T>
+ *     PDQ_HD static S eval(const S& left, const S& mid, const S& right, const T* p, T inv_dx);
+ *   };
+ * component j of f from u_{j-1}, u_j, u_{j+1} (indices mod d), the
+ * parameters and inv_dx = d, generic over the scalar S (the bulk type, and
+ * float64 Taylor jets for the Taylor-mode start); the built-in Burgers field
+ * is such a stencil.  The id goes into pdq_config.field with ssm
+ * PDQ_SSM_BLOCKDIAG (TS0; num_params must match P); other factorisations
+ * reject it. */
+#if !defined(__CUDACC_RTC__)
+pdq_status pdq_register_stencil(const char* name, const char* source, int32_t num_params, int32_t* field_id,
+                                char* log, size_t log_bytes);
+#endif
+
 #ifdef __cplusplus
 }
 #endif

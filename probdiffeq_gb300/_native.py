@@ -236,6 +236,11 @@ SIGNATURES = {
         [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
          ctypes.c_char_p, ctypes.c_size_t],
     ),
+    "pdq_register_stencil": (
+        ctypes.c_int,
+        [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.c_char_p,
+         ctypes.c_size_t],
+    ),
     "pdq_probe_fp32_fma": (
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
@@ -296,6 +301,23 @@ def register_field(name, source, dim, num_params):
                                 ctypes.sizeof(log))
     if st != 0:
         raise NativeError(st, "pdq_register_field:\n" + log.value.decode(errors="replace"))
+    FIELD[name] = fid.value
+    return fid.value
+
+
+def register_stencil(name, source, num_params):
+    """Compile a stencil field for the block-diagonal kernel (CUDA C++ source
+    of ``struct Stencil``, any d on a periodic grid) with NVRTC
+    (``pdq_register_stencil``); returns its field id and makes ``name`` usable
+    as the field of a block-diagonal configuration (TS0).  Raises NativeError
+    with the compiler log on failure."""
+    lib = load()
+    fid = ctypes.c_int32(-1)
+    log = ctypes.create_string_buffer(1 << 16)
+    st = lib.pdq_register_stencil(name.encode(), source.encode(), int(num_params), ctypes.byref(fid), log,
+                                  ctypes.sizeof(log))
+    if st != 0:
+        raise NativeError(st, "pdq_register_stencil:\n" + log.value.decode(errors="replace"))
     FIELD[name] = fid.value
     return fid.value
 

@@ -42,6 +42,7 @@ EMBEDDED_HEADERS = [
     ("dense_solver.cuh", os.path.join(CSRC, "dense_solver.cuh")),
     ("lml_solver.cuh", os.path.join(CSRC, "lml_solver.cuh")),
     ("lml_adjoint.cuh", os.path.join(CSRC, "lml_adjoint.cuh")),
+    ("bd_solver.cuh", os.path.join(CSRC, "bd_solver.cuh")),
 ]
 
 

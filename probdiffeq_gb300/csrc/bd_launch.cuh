@@ -13,14 +13,13 @@ inline int bd_cluster_size(int d) {
   return cl;
 }
 
-template <typename T, int NU, bool FP>
-cudaError_t launch_bd_kernel(BdArgs a, cudaStream_t stream) {
-  cudaError_t e = ensure_stack<bd_adaptive_kernel<T, NU, FP>>();
-  if (e != cudaSuccess) return e;
+// One cluster of a.cluster CTAs per instance with `smem` bytes of dynamic
+// shared memory per CTA; `kernel` is a bd_adaptive_kernel instantiation
+// (built in, or compiled at run time for a user stencil).
+inline cudaError_t launch_bd_cluster(const void* kernel, BdArgs a, size_t smem, cudaStream_t stream) {
   const int CL = a.cluster;
-  const size_t smem = bd_smem_bytes<T, NU>(a.d / CL);
   if (smem > 48 * 1024) {
-    e = cudaFuncSetAttribute(bd_adaptive_kernel<T, NU, FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
   }
   cudaLaunchConfig_t cfg = {};
@@ -35,9 +34,18 @@ cudaError_t launch_bd_kernel(BdArgs a, cudaStream_t stream) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  e = cudaLaunchKernelEx(&cfg, bd_adaptive_kernel<T, NU, FP>, a);
+  void* args[] = {&a};
+  cudaError_t e = cudaLaunchKernelExC(&cfg, kernel, args);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
+}
+
+template <typename T, int NU, bool FP>
+cudaError_t launch_bd_kernel(BdArgs a, cudaStream_t stream) {
+  cudaError_t e = ensure_stack<bd_adaptive_kernel<T, NU, FP>>();
+  if (e != cudaSuccess) return e;
+  return launch_bd_cluster(reinterpret_cast<const void*>(bd_adaptive_kernel<T, NU, FP>), a,
+                           bd_smem_bytes<T, NU>(a.d / a.cluster), stream);
 }
 
 template <typename T, int NU>

@@ -43,13 +43,27 @@
 // stored conditionals (Smoother.finalize, MarkovSequence.evaluate_marginals).
 #pragma once
 
-#include <cooperative_groups.h>
-
 #include "iso_solver.cuh"
 
 namespace pdq {
 
-namespace cg = cooperative_groups;
+// Thread-block-cluster operations (those of cooperative_groups'
+// cluster_group, on the device intrinsics, so that the kernel also compiles
+// under NVRTC, which has no toolkit headers): the block's rank in its
+// cluster, the cluster barrier (arrive with release, wait with acquire
+// semantics), and the address of the same shared-memory variable in
+// another block of the cluster.
+struct Cluster {
+  PDQ_D unsigned block_rank() const { return __clusterRelativeBlockRank(); }
+  PDQ_D void sync() const {
+    __cluster_barrier_arrive();
+    __cluster_barrier_wait();
+  }
+  template <typename T>
+  PDQ_D T* map_shared_rank(T* p, int rank) const {
+    return static_cast<T*>(__cluster_map_shared_rank(const_cast<void*>(static_cast<const void*>(p)), unsigned(rank)));
+  }
+};
 
 constexpr int kBdThreads = 256;
 constexpr int kBdMaxDimsPerThread = 8;
@@ -145,16 +159,48 @@ PDQ_HD size_t bd_smem_bytes(int dl) {
   return size_t(NU + 1 + 3) * size_t(dl) * sizeof(T);
 }
 
+// Stencil fields of the block-diagonal kernel: component j of f depends on
+// u_{j-1}, u_j, u_{j+1} (periodic in j), the parameters p and the grid's
+// inverse spacing inv_dx = d; written once, generic over the scalar type S
+// (the bulk type for the attempts, float64 jets for the Taylor-mode start):
+//   struct Stencil {
+//     static constexpr int P = ...;  // number of parameters
+//     template <typename S, typename T>
+//     PDQ_HD static S eval(const S& left, const S& mid, const S& right, const T* p, T inv_dx);
+//   };
+// TS1 needs the Jacobian's diagonal d f_j / d u_j; the kernel takes it from
+// a stencil that declares it the same for every j (kConstantDiagonal,
+// diag(p, inv_dx)), as the Burgers stencil's is.
+//
 // Viscous Burgers with periodic central differences (the flux-form stencil
 // of benchmarks/A5_work-precision-burgers-pde.py:124-134, periodic wrap).
-template <typename T>
-PDQ_D T burgers_f(T left, T mid, T right, T nu_visc, T inv_dx) {
-  const T flux = (right * right - left * left) * (T(0.25) * inv_dx);
-  const T lap = (right - T(2) * mid + left) * (inv_dx * inv_dx);
-  return -flux + nu_visc * lap;
-}
+struct BurgersStencil {
+  static constexpr int P = 1;  // viscosity
+  static constexpr bool kConstantDiagonal = true;
+  template <typename S, typename T>
+  PDQ_HD static S eval(const S& left, const S& mid, const S& right, const T* p, T inv_dx) {
+    const S flux = (right * right - left * left) * (T(0.25) * inv_dx);
+    const S lap = (right - T(2) * mid + left) * (inv_dx * inv_dx);
+    return -flux + p[0] * lap;
+  }
+  // the central-difference flux term does not involve u_j
+  template <typename T>
+  PDQ_HD static T diag(const T* p, T inv_dx) {
+    return -(T(2) * p[0] * inv_dx * inv_dx);
+  }
+};
 
-template <typename T, int NU, bool FP = false>
+// Whether a stencil declares a constant Jacobian diagonal (TS1 available).
+template <class ST, class = void>
+struct StencilConstantDiagonal {
+  static constexpr bool value = false;
+};
+template <class ST>
+struct StencilConstantDiagonal<ST, decltype(void(ST::kConstantDiagonal))> {
+  static constexpr bool value = ST::kConstantDiagonal;
+};
+
+template <typename T, int NU, bool FP = false, class ST = BurgersStencil>
 __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   constexpr int n = NU + 1;
   constexpr int NS = bd_state_rows<NU>();
@@ -162,7 +208,7 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   constexpr int OUT = 1;
   constexpr bool kNarrow = sizeof(T) == sizeof(float);
   using W = Wide<T>;
-  cg::cluster_group cluster = cg::this_cluster();
+  const Cluster cluster;
   const int CL = a.cluster;
   const int rank = int(cluster.block_rank());
   const int64_t inst = blockIdx.x / CL;
@@ -188,7 +234,14 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   T* const cbufs[2] = {cond0 + inst * CF * int64_t(d), cond0 + (a.B + inst) * CF * int64_t(d)};
   T* const ckpt = cond0 + 2 * a.B * CF * int64_t(d) + inst * int64_t(a.S - 1) * CF * int64_t(d);
 
-  const T nu_visc = T(a.params[inst]);
+  constexpr int P = ST::P;
+  double pd[P > 0 ? P : 1];
+  T pt[P > 0 ? P : 1];
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    pd[k] = a.params[inst * P + k];
+    pt[k] = T(pd[k]);
+  }
   const T inv_dx = T(d);
   const int S = a.S;
   const int S_out = a.terminal_only ? 1 : S;
@@ -208,16 +261,15 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
     for (int jl = tid; jl < dl; jl += kBdThreads) {
       const int g = j0 + jl;
       const int gl = (g - 1 + d) % d, gr = (g + 1) % d;
-      // [f(u)]_k with quadratic flux: (u^2)_k = sum_l a_l a_{k-l}
-      double sq_l = 0.0, sq_r = 0.0;
+      // coefficient k of f from coefficients 0 .. k of the neighbours (the stencil on jets)
+      Jet<double, NU + 1> jl_, jm, jr;
       for (int l = 0; l <= k; ++l) {
-        sq_l += double(st[l * d + gl]) * double(st[(k - l) * d + gl]);
-        sq_r += double(st[l * d + gr]) * double(st[(k - l) * d + gr]);
+        jl_.c[l] = double(st[l * d + gl]);
+        jm.c[l] = double(st[l * d + g]);
+        jr.c[l] = double(st[l * d + gr]);
       }
-      const double ul = st[k * d + gl], um = st[k * d + g], ur = st[k * d + gr];
-      const double idx = double(d);
-      const double fk = -(sq_r - sq_l) * 0.25 * idx + double(a.params[inst]) * (ur - 2.0 * um + ul) * idx * idx;
-      st[(k + 1) * d + g] = T(fk / (k + 1));
+      const Jet<double, NU + 1> fj = ST::eval(jl_, jm, jr, static_cast<const double*>(pd), double(d));
+      st[(k + 1) * d + g] = T(fj.c[k] / (k + 1));
     }
     __threadfence();
     cluster.sync();
@@ -327,7 +379,10 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       // Jacobian's diagonal is d f_j / d u_j = -2 nu / dx^2 for every j (the
       // central-difference flux term does not involve u_j), so H_j = [h0, 1, 0, ...]
       // with one h0 for all dimensions
-      const T h0 = a.ts1 ? T(2) * nu_visc * inv_dx * inv_dx : T(0);
+      T h0 = T(0);
+      if constexpr (StencilConstantDiagonal<ST>::value) {
+        if (a.ts1) h0 = -ST::diag(static_cast<const T*>(pt), inv_dx);
+      }
       const T ell = a.ts1 ? observed_std_ts1<T, NU>(p[OUT], h, h0, q00, q10, q11, damp)
                           : observed_std(p[OUT], h, q1_out_norm, damp);
       // error_state_std: the conditioned unit-scale std of u is the same for
@@ -368,7 +423,7 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
         T mp[n];
 #pragma unroll
         for (int i = 0; i < n; ++i) mp[i] = mps[i * dl + jl];
-        const T f = burgers_f(left, mp[0], right, nu_visc, inv_dx);
+        const T f = ST::eval(left, mp[0], right, static_cast<const T*>(pt), inv_dx);
         const T mobs = mp[OUT] - f;
         // per-dimension residual_whitened_rms of fx.marginalise(apply_flat(m))
         const T sigma = dev_div(dev_abs(mobs), ell);

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "pdq_nvtx.h"
+#include "bd_launch.cuh"
 #include "dense_solver.cuh"
 #include "iso_solver.cuh"
 #include "lml_adjoint.cuh"
@@ -44,6 +45,7 @@ namespace {
 struct UserField {
   std::string name, source;
   int dim = 0, params = 0;
+  bool stencil = false;  // a block-diagonal stencil (struct Stencil) rather than a field (struct Field)
   std::mutex mu;
   // (kernel expression) -> loaded kernel
   std::map<std::string, cudaKernel_t> kernels;
@@ -71,6 +73,11 @@ std::string kernel_expression(bool f64, int nu, bool interp, bool fp, bool gen) 
 std::string dense_expression(bool f64, int nu, bool ts1, bool fp) {
   return std::string("pdq::dense_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
          ", pdq_user::Field, " + tf(ts1) + ", " + tf(fp) + ">";
+}
+
+std::string bd_expression(bool f64, int nu, bool fp) {
+  return std::string("pdq::bd_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) + ", " +
+         tf(fp) + ", pdq_user::Stencil>";
 }
 
 // The LML kernels of a user field: the covariance plan (field-independent,
@@ -164,9 +171,36 @@ extern "C" pdq_status pdq_register_field(const char* name, const char* source, i
   return PDQ_SUCCESS;
 }
 
+extern "C" pdq_status pdq_register_stencil(const char* name, const char* source, int32_t num_params,
+                                           int32_t* field_id, char* log, size_t log_bytes) {
+  pdq::NvtxRange nvtx_range("pdq_register_stencil");
+  if (field_id == nullptr || !nonempty(name) || !nonempty(source) || num_params < 0 || num_params > 64)
+    return PDQ_ERROR_INVALID_VALUE;
+  std::string cubin, text;
+  std::vector<std::string> lowered;
+  const pdq_status st = compile(source, {bd_expression(false, 3, false)}, &cubin, &lowered, &text, "bd_solver.cuh");
+  copy_log(text, log, log_bytes);
+  if (st != PDQ_SUCCESS) return st;
+  auto f = std::make_unique<UserField>();
+  f->name = name;
+  f->source = source;
+  f->dim = -1;  // any d
+  f->params = num_params;
+  f->stencil = true;
+  std::lock_guard<std::mutex> lock(g_registry_mu);
+  *field_id = PDQ_FIELD_USER_BASE + int32_t(g_fields.size());
+  g_fields.push_back(std::move(f));
+  return PDQ_SUCCESS;
+}
+
 int pdq_user_field_dim(int32_t field) {
   UserField* f = lookup(field);
   return f ? f->dim : 0;
+}
+
+bool pdq_user_field_is_stencil(int32_t field) {
+  UserField* f = lookup(field);
+  return f != nullptr && f->stencil;
 }
 
 int pdq_user_field_params(int32_t field) {
@@ -314,4 +348,15 @@ cudaError_t pdq_launch_lml_adj_user(const pdq::LmlAdjArgs& aa, int32_t field, bo
   e = cudaLaunchKernel(reinterpret_cast<const void*>(k[0]), dim3(1), dim3(pdq::kLmlPlanThreads), plan_params, 0, stream);
   if (e != cudaSuccess) return e;
   return cudaLaunchKernel(reinterpret_cast<const void*>(k[1]), dim3(grid), dim3(pdq::kLmlThreads), params, 0, stream);
+}
+
+cudaError_t pdq_launch_bd_user(const pdq::BdArgs& a, int32_t field, bool f64, int nu, cudaStream_t stream) {
+  UserField* f = lookup(field);
+  if (f == nullptr || !f->stencil || nu < 2 || nu > 4) return cudaErrorInvalidValue;
+  cudaKernel_t kernel = nullptr;
+  cudaError_t e = user_kernel(f, bd_expression(f64, nu, a.fixedpoint != 0), "bd_solver.cuh", &kernel);
+  if (e != cudaSuccess) return e;
+  // bd_smem_bytes<T, NU>: staged means (n rows), new terms, scales and current scales (3 rows) of dl dimensions
+  const size_t smem = size_t(nu + 1 + 3) * size_t(a.d / a.cluster) * (f64 ? sizeof(double) : sizeof(float));
+  return pdq::launch_bd_cluster(reinterpret_cast<const void*>(kernel), a, smem, stream);
 }

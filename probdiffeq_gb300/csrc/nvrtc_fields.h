@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include "bd_solver.cuh"
 #include "dense_solver.cuh"
 #include "iso_solver.cuh"
 #include "lml_adjoint.cuh"
@@ -11,6 +12,8 @@
 // State dimension / number of parameters of a registered user field (0 / -1 if unknown).
 int pdq_user_field_dim(int32_t field);
 int pdq_user_field_params(int32_t field);
+// Whether a registered id is a block-diagonal stencil (pdq_register_stencil).
+bool pdq_user_field_is_stencil(int32_t field);
 
 // Launch the isotropic kernel instantiated for a registered user field;
 // compiles and loads the variant on first use.
@@ -27,3 +30,7 @@ cudaError_t pdq_launch_dense_user(const pdq::DenseArgs& a, int32_t field, bool f
 cudaError_t pdq_launch_lml_user(const pdq::LmlArgs& a, int32_t field, bool f64, int nu, cudaStream_t stream);
 cudaError_t pdq_launch_lml_adj_user(const pdq::LmlAdjArgs& aa, int32_t field, bool f64, int nu, bool backward,
                                     cudaStream_t stream);
+
+// The block-diagonal cluster kernel instantiated for a registered user
+// stencil (struct Stencil); compiles and loads the variant on first use.
+cudaError_t pdq_launch_bd_user(const pdq::BdArgs& a, int32_t field, bool f64, int nu, cudaStream_t stream);

@@ -68,6 +68,9 @@ pdq_status validate_common(const pdq_config* c) {
   if (!(c->factor_min > 0) || !(c->factor_max >= c->factor_min) || !(c->safety > 0)) return PDQ_ERROR_INVALID_VALUE;
   if (c->max_attempts < 1) return PDQ_ERROR_INVALID_VALUE;
   if (c->reserved0 != 0) return PDQ_ERROR_INVALID_VALUE;
+  // a registered stencil serves the block-diagonal kernel only
+  if (c->field >= PDQ_FIELD_USER_BASE && pdq_user_field_is_stencil(c->field) && c->ssm != PDQ_SSM_BLOCKDIAG)
+    return PDQ_ERROR_UNSUPPORTED;
   // launch shapes any mapping accepts (each mapping checks its own subset)
   const int ipb = c->instances_per_block;
   if (!(ipb == 0 || (ipb >= 1 && ipb <= 4) || ipb == 8 || ipb == 16 || ipb == 32 || ipb == 64))
@@ -323,7 +326,10 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
   }
   if (c->ssm == PDQ_SSM_BLOCKDIAG) {
-    if (c->field != PDQ_FIELD_BURGERS) return PDQ_ERROR_UNSUPPORTED;
+    // the Burgers stencil, or a registered one (pdq_register_stencil; TS0 only)
+    const bool user_stencil = c->field >= PDQ_FIELD_USER_BASE && pdq_user_field_is_stencil(c->field);
+    if (c->field != PDQ_FIELD_BURGERS && !user_stencil) return PDQ_ERROR_UNSUPPORTED;
+    if (user_stencil && c->constraint != PDQ_CONSTRAINT_TS0) return PDQ_ERROR_UNSUPPORTED;
     if (c->instances_per_block != 0) return PDQ_ERROR_INVALID_VALUE;  // one cluster per instance
     if (args->u_mean_d_params || args->u_mean_d_y0) return PDQ_ERROR_UNSUPPORTED;
     if (c->constraint != PDQ_CONSTRAINT_TS0 && c->constraint != PDQ_CONSTRAINT_TS1) return PDQ_ERROR_INVALID_VALUE;
@@ -399,6 +405,11 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     a.num_attempts = args->num_attempts;
     a.status = args->status;
     a.workspace = workspace;
+    if (user_stencil) {
+      const cudaError_t err =
+          pdq_launch_bd_user(a, c->field, c->precision == PDQ_PRECISION_F64, c->num_derivatives, stream);
+      return err == cudaSuccess ? PDQ_SUCCESS : (err == cudaErrorInvalidSource ? PDQ_ERROR_COMPILE : PDQ_ERROR_CUDA);
+    }
     const cudaError_t err = c->precision == PDQ_PRECISION_F64
                                 ? pdq_launch_bd_burgers_f64(a, c->num_derivatives, stream)
                                 : pdq_launch_bd_burgers_f32(a, c->num_derivatives, stream);

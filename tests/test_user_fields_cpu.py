@@ -41,3 +41,16 @@ def test_api_registration_makes_the_name_usable():
         probdiffeq.ode("cpu_test_api_brusselator", [1.0, 3.0, 4.0])
     with pytest.raises(ValueError):
         probdiffeq.register_field("lotka_volterra", user_fields.LOTKA_VOLTERRA, dim=2, num_params=4)
+
+
+def test_registering_a_stencil_compiles_the_block_diagonal_kernel():
+    """A block-diagonal stencil (struct Stencil) compiles with the cluster
+    kernel; a configuration of another factorisation rejects its id."""
+    from probdiffeq_gb300 import ensemble
+
+    fid = _native.register_stencil("cpu_test_allen_cahn", user_fields.ALLEN_CAHN_STENCIL, 1)
+    assert fid >= 1000
+    cfg = ensemble.make_config(field="cpu_test_allen_cahn", num_derivatives=3, ode_dim=64, ssm="blockdiag")
+    assert cfg.field == fid
+    with pytest.raises(_native.NativeError):  # a Field source is not a stencil
+        _native.register_stencil("cpu_test_stencil_broken", user_fields.BRUSSELATOR, 2)

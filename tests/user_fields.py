@@ -80,3 +80,40 @@ struct Field {
   }
 };
 """
+
+
+# Block-diagonal stencils (struct Stencil): the viscous Burgers stencil of the
+# built-in field, and Allen--Cahn, u_t = eps^2 u_xx + u - u^3 (periodic
+# central differences), with the oracle's definition below
+BURGERS_STENCIL = """
+struct Stencil {
+  static constexpr int P = 1;
+  template <typename S, typename T>
+  PDQ_HD static S eval(const S& left, const S& mid, const S& right, const T* p, T inv_dx) {
+    const S flux = (right * right - left * left) * (T(0.25) * inv_dx);
+    const S lap = (right - T(2) * mid + left) * (inv_dx * inv_dx);
+    return -flux + p[0] * lap;
+  }
+};
+"""
+
+ALLEN_CAHN_STENCIL = """
+struct Stencil {
+  static constexpr int P = 1;
+  template <typename S, typename T>
+  PDQ_HD static S eval(const S& left, const S& mid, const S& right, const T* p, T inv_dx) {
+    const S lap = (right - T(2) * mid + left) * (inv_dx * inv_dx);
+    return p[0] * lap + mid - mid * mid * mid;
+  }
+};
+"""
+
+
+def allen_cahn(u, p):
+    from oracle.problems import Series, roll
+
+    d = u.c.shape[-1] if isinstance(u, Series) else u.shape[-1]
+    inv_dx = float(d)
+    left, right = roll(u, 1), roll(u, -1)
+    lap = (right - 2.0 * u + left) * (inv_dx * inv_dx)
+    return lap * p[0] + u - u * u * u
