@@ -79,7 +79,9 @@ struct DenseLayout {
   static constexpr int cnXi = cnA + NN;
   static constexpr int W = cnXi + N;   // predict workspace, 2N x 2N, row stride 2N
   static constexpr int WM = W + 4 * NN;  // merge / marginalise workspace, 2N x N, row stride N
-  static constexpr int size = WM + 2 * NN;
+  // this step's constants for the lanes' column loops: p (n), p^-1 (n), A1 (n x n), s sqrt|h| Q1 (n x n)
+  static constexpr int PT = WM + 2 * NN;
+  static constexpr int size = PT + 2 * n + 2 * n * n;
   PDQ_HD static constexpr int normal(int k) { return normal0 + k * kNormal; }
   PDQ_HD static constexpr int cond(int k) { return cond0 + k * kCond; }
 };
@@ -183,37 +185,51 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
     for (int kk = i / D; kk < n; ++kk) acc += T(iwp_a<NU>(i / D, kk)) * mean_l[kk * D + i % D];
     mobs[i] = acc;
   }
-  // fill, column-parallel
+  // the preconditioner and A1 for the lanes' column loops (runtime indices read shared memory)
+  if (g.lane == 0) {
 #pragma unroll
-  for (int ci = 0; ci < n; ++ci)
+    for (int i = 0; i < n; ++i) {
+      S[Lay::PT + i] = pc[i];
+      S[Lay::PT + n + i] = pic[i];
 #pragma unroll
-    for (int cd = 0; cd < D; ++cd) {
-      const int c = ci * D + cd;
-      if (g.owns(c)) {
-#pragma unroll
-        for (int r = 0; r < N; ++r)
-          S[W + r * WS + c] = (r % D == cd && r / D <= ci) ? sq * T(q1[ci][r / D]) : T(0);
-#pragma unroll
-        for (int r = 0; r < N; ++r) {
-          // (A cl)[c][r] = sum_k A1[ci][k / D] p^-1_k L[k][r] over k = kk d + cd, kk >= ci, k >= r
-          T acc = T(0);
-#pragma unroll
-          for (int kk = ci; kk < n; ++kk) {
-            const int k = kk * D + cd;
-            if (k >= r) acc += T(iwp_a<NU>(ci, kk)) * pic[kk] * S[from + Lay::L + k * N + r];
-          }
-          S[W + (N + r) * WS + c] = acc;
-        }
-      }
-      if constexpr (REVERT) {
-        if (g.owns(N + c)) {
-#pragma unroll
-          for (int r = 0; r < N; ++r) S[W + r * WS + N + c] = T(0);
-#pragma unroll
-          for (int r = 0; r < N; ++r) S[W + (N + r) * WS + N + c] = r <= c ? pic[ci] * S[from + Lay::L + c * N + r] : T(0);
-        }
+      for (int k = 0; k < n; ++k) {
+        S[Lay::PT + 2 * n + i * n + k] = T(iwp_a<NU>(i, k));
+        S[Lay::PT + 2 * n + n * n + i * n + k] = sq * T(q1[i][k]);
       }
     }
+  }
+  g.sync();
+  // fill, column-parallel
+#pragma unroll 1
+  for (int c = g.lane; c < C; c += L) {
+    if (c < N) {
+      const int ci = c / D, cd = c - ci * D;
+#pragma unroll
+      for (int r = 0; r < N; ++r)
+        S[W + r * WS + c] = (r % D == cd && r / D <= ci) ? S[Lay::PT + 2 * n + n * n + ci * n + r / D] : T(0);
+      // (A cl)[c][r] = sum_k A1[ci][k / D] p^-1_k L[k][r] over k = kk d + cd, kk >= ci, k >= r
+      T coef[n];
+#pragma unroll
+      for (int kk = 0; kk < n; ++kk) coef[kk] = S[Lay::PT + 2 * n + ci * n + kk] * pic[kk];
+#pragma unroll
+      for (int r = 0; r < N; ++r) {
+        T acc = T(0);
+#pragma unroll
+        for (int kk = 0; kk < n; ++kk) {
+          const int k = kk * D + cd;
+          if (kk >= ci && k >= r) acc += coef[kk] * S[from + Lay::L + k * N + r];
+        }
+        S[W + (N + r) * WS + c] = acc;
+      }
+    } else {
+      const int cc = c - N;
+      const T pk = S[Lay::PT + n + cc / D];
+#pragma unroll
+      for (int r = 0; r < N; ++r) S[W + r * WS + c] = T(0);
+#pragma unroll
+      for (int r = 0; r < N; ++r) S[W + (N + r) * WS + c] = r <= cc ? pk * S[from + Lay::L + cc * N + r] : T(0);
+    }
+  }
   g.sync();
   // reflectors 0 .. N - 1: row c and the N bottom rows
 #pragma unroll 1
@@ -275,32 +291,33 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
   // the predicted marginal: m = p mobs, L = |p| R11^T
 #pragma unroll
   for (int i = 0; i < N; ++i)
-    if (g.owns(i)) {
-      S[pred + Lay::m + i] = pc[i / D] * mobs[i];
+    if (g.owns(i)) S[pred + Lay::m + i] = pc[i / D] * mobs[i];
+#pragma unroll 1
+  for (int i = g.lane; i < N; i += L) {
+    const T pa = dev_abs(S[Lay::PT + i / D]);
 #pragma unroll
-      for (int j = 0; j < N; ++j) S[pred + Lay::L + i * N + j] = (j <= i) ? dev_abs(pc[i / D]) * S[W + j * WS + i] : T(0);
-    }
+    for (int j = 0; j < N; ++j) S[pred + Lay::L + i * N + j] = (j <= i) ? pa * S[W + j * WS + i] : T(0);
+  }
   if constexpr (REVERT) {
     // G^T = R11^-1 R12 column by column; cond.A[jj][i] = G^T[i][jj], cond.xi = mean_l - G mobs
+#pragma unroll 1
+    for (int jj = g.lane; jj < N; jj += L) {
+      T gc[N];
 #pragma unroll
-    for (int jj = 0; jj < N; ++jj)
-      if (g.owns(jj)) {
-        T gc[N];
+      for (int i = N - 1; i >= 0; --i) {
+        T acc = S[W + i * WS + N + jj];
 #pragma unroll
-        for (int i = N - 1; i >= 0; --i) {
-          T acc = S[W + i * WS + N + jj];
-#pragma unroll
-          for (int k = i + 1; k < N; ++k) acc -= S[W + i * WS + k] * gc[k];
-          gc[i] = dev_div(acc, S[W + i * WS + i]);
-        }
-        T xi = mean_l[jj];
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-          S[Lay::cnA + jj * N + k] = gc[k];
-          xi -= gc[k] * mobs[k];
-        }
-        S[Lay::cnXi + jj] = xi;
+        for (int k = i + 1; k < N; ++k) acc -= S[W + i * WS + k] * gc[k];
+        gc[i] = dev_div(acc, S[W + i * WS + i]);
       }
+      T xi = S[Lay::PT + n + jj / D] * S[from + Lay::m + jj];  // mean_l[jj]
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        S[Lay::cnA + jj * N + k] = gc[k];
+        xi -= gc[k] * mobs[k];
+      }
+      S[Lay::cnXi + jj] = xi;
+    }
   }
   g.sync();
 }
@@ -319,9 +336,9 @@ PDQ_D void dstruct_merge(Soa<T, IPW> S, const LaneGroup<L>& g, int o, T h, int o
 #pragma unroll
   for (int k = 0; k < N; ++k) Tv[k] = S[o + Lay::tl + k] * dev_rcp(pic[k / D]);
   // out.A = o.A T in.A and R1 = (o.A |T| in.X)^T by columns j of in.A / in.X
-#pragma unroll
-  for (int j = 0; j < N; ++j)
-    if (g.owns(j)) {
+#pragma unroll 1
+  for (int j = g.lane; j < N; j += L) {
+    {
       T u[N], u2[N];
 #pragma unroll
       for (int k = 0; k < N; ++k) {
@@ -348,17 +365,17 @@ PDQ_D void dstruct_merge(Soa<T, IPW> S, const LaneGroup<L>& g, int o, T h, int o
 #pragma unroll
       for (int k = 0; k < N; ++k) x += S[o + Lay::A + j * N + k] * Tv[k] * S[Lay::cnXi + k];
       S[out + Lay::xi + j] = x;
-      S[out + Lay::tl + j] = dev_rcp(pc[j / D]);
+      S[out + Lay::tl + j] = dev_rcp(S[Lay::PT + j / D]);
       S[out + Lay::to + j] = S[o + Lay::to + j];
     }
+  }
   g.sync();
   dstruct_qr_stacked<T, N, L, IPW>(S, g, WM);
+#pragma unroll 1
+  for (int i = g.lane; i < N; i += L) {
 #pragma unroll
-  for (int i = 0; i < N; ++i)
-    if (g.owns(i)) {
-#pragma unroll
-      for (int j = 0; j < N; ++j) S[out + Lay::X + i * N + j] = (j <= i) ? S[WM + j * N + i] : T(0);
-    }
+    for (int j = 0; j < N; ++j) S[out + Lay::X + i * N + j] = (j <= i) ? S[WM + j * N + i] : T(0);
+  }
   g.sync();
 }
 
@@ -369,9 +386,9 @@ PDQ_D void dstruct_cond_marginalise(Soa<T, IPW> S, const LaneGroup<L>& g, int c,
   using Lay = DenseLayout<NU, D>;
   constexpr int N = Lay::N, WM = Lay::WM;
   // rows r of (A (tl L))^T and of X^T, by rows
-#pragma unroll
-  for (int r = 0; r < N; ++r)
-    if (g.owns(r)) {
+#pragma unroll 1
+  for (int r = g.lane; r < N; r += L) {
+    {
       T u[N];
 #pragma unroll
       for (int k = 0; k < N; ++k) u[k] = k >= r ? S[c + Lay::tl + k] * S[rv + Lay::L + k * N + r] : T(0);
@@ -384,6 +401,7 @@ PDQ_D void dstruct_cond_marginalise(Soa<T, IPW> S, const LaneGroup<L>& g, int c,
         S[WM + (N + r) * N + col] = col >= r ? S[c + Lay::X + col * N + r] : T(0);
       }
     }
+  }
   // the mean (all lanes read rv before anyone writes out; rv != out)
   T mo[N];
 #pragma unroll
@@ -397,12 +415,13 @@ PDQ_D void dstruct_cond_marginalise(Soa<T, IPW> S, const LaneGroup<L>& g, int c,
   dstruct_qr_stacked<T, N, L, IPW>(S, g, WM);
 #pragma unroll
   for (int i = 0; i < N; ++i)
-    if (g.owns(i)) {
-      S[out + Lay::m + i] = mo[i];
-      const T to = dev_abs(S[c + Lay::to + i]);
+    if (g.owns(i)) S[out + Lay::m + i] = mo[i];
+#pragma unroll 1
+  for (int i = g.lane; i < N; i += L) {
+    const T to = dev_abs(S[c + Lay::to + i]);
 #pragma unroll
-      for (int j = 0; j < N; ++j) S[out + Lay::L + i * N + j] = (j <= i) ? to * S[WM + j * N + i] : T(0);
-    }
+    for (int j = 0; j < N; ++j) S[out + Lay::L + i * N + j] = (j <= i) ? to * S[WM + j * N + i] : T(0);
+  }
   g.sync();
 }
 
