@@ -64,23 +64,29 @@ struct Soa {
   PDQ_D T& operator[](int e) const { return p[e * IPW]; }
 };
 
+// Matrices are row-major with padded row strides (N + 1, 2N + 1): the lanes
+// of a group that own different rows of a matrix then hit different banks
+// (with a stride that is a multiple of 32 / IPW they would share one).
 template <int NU, int D>
 struct DenseLayout {
   static constexpr int n = NU + 1, N = n * D, NN = N * N;
-  static constexpr int kNormal = N + NN;        // m, L (row-major, lower)
-  static constexpr int kCond = 2 * NN + 3 * N;  // A, xi, X (row-major, lower), tl, to
+  static constexpr int LD = N + 1;                // row stride of the N x N matrices
+  static constexpr int WS = 2 * N + 1;            // row stride of the predict workspace
+  static constexpr int WMS = N + 1;               // row stride of the merge workspace
+  static constexpr int kNormal = N + N * LD;      // m, L (lower)
+  static constexpr int kCond = 2 * N * LD + 3 * N;  // A, xi, X (lower), tl, to
   static constexpr int kNormals = 4;            // step_from, interp_from, proposal, prediction (rotating)
   static constexpr int kConds = 4;              // running, interp, merged, scratch (rotating)
   static constexpr int m = 0, L = N;
-  static constexpr int A = 0, xi = NN, X = NN + N, tl = 2 * NN + N, to = 2 * NN + 2 * N;
+  static constexpr int A = 0, xi = N * LD, X = N * LD + N, tl = 2 * N * LD + N, to = 2 * N * LD + 2 * N;
   static constexpr int normal0 = 0;
   static constexpr int cond0 = kNormals * kNormal;
   static constexpr int cnA = cond0 + kConds * kCond;  // this step's conditional: A (N x N), xi (N)
-  static constexpr int cnXi = cnA + NN;
-  static constexpr int W = cnXi + N;   // predict workspace, 2N x 2N, row stride 2N
-  static constexpr int WM = W + 4 * NN;  // merge / marginalise workspace, 2N x N, row stride N
+  static constexpr int cnXi = cnA + N * LD;
+  static constexpr int W = cnXi + N;        // predict workspace, 2N x 2N
+  static constexpr int WM = W + 2 * N * WS;  // merge / marginalise workspace, 2N x N
   // this step's constants for the lanes' column loops: p (n), p^-1 (n), A1 (n x n), s sqrt|h| Q1 (n x n)
-  static constexpr int PT = WM + 2 * NN;
+  static constexpr int PT = WM + 2 * N * WMS;
   static constexpr int size = PT + 2 * n + 2 * n * n;
   PDQ_HD static constexpr int normal(int k) { return normal0 + k * kNormal; }
   PDQ_HD static constexpr int cond(int k) { return cond0 + k * kCond; }
@@ -132,29 +138,29 @@ PDQ_D bool dstruct_reflector(T (&x)[K], T& beta, T& tau) {
 
 // QR of the 2N x N workspace WM = [full N x N; upper-triangular N x N]
 // (rows c .. c + N take part in reflector c); R in rows 0 .. N - 1.
-template <typename T, int N, int L, int IPW>
+template <typename T, int N, int L, int IPW, int LDM = N + 1>
 PDQ_D void dstruct_qr_stacked(Soa<T, IPW> S, const LaneGroup<L>& g, int WM) {
 #pragma unroll 1
   for (int c = 0; c < N; ++c) {
     T x[N + 1];
 #pragma unroll
-    for (int t = 0; t <= N; ++t) x[t] = S[WM + (c + t) * N + c];
+    for (int t = 0; t <= N; ++t) x[t] = S[WM + (c + t) * LDM + c];
     g.sync();  // every lane has read column c
     T beta, tau;
     if (dstruct_reflector(x, beta, tau)) {
 #pragma unroll 2
       for (int j = g.first(c + 1); j < N; j += L) {
-        T w0 = S[WM + c * N + j], w1 = T(0);
+        T w0 = S[WM + c * LDM + j], w1 = T(0);
 #pragma unroll
-        for (int t = 1; t <= N; t += 2) w0 += x[t] * S[WM + (c + t) * N + j];
+        for (int t = 1; t <= N; t += 2) w0 += x[t] * S[WM + (c + t) * LDM + j];
 #pragma unroll
-        for (int t = 2; t <= N; t += 2) w1 += x[t] * S[WM + (c + t) * N + j];
+        for (int t = 2; t <= N; t += 2) w1 += x[t] * S[WM + (c + t) * LDM + j];
         const T w = tau * (w0 + w1);
-        S[WM + c * N + j] -= w;
+        S[WM + c * LDM + j] -= w;
 #pragma unroll
-        for (int t = 1; t <= N; ++t) S[WM + (c + t) * N + j] -= w * x[t];
+        for (int t = 1; t <= N; ++t) S[WM + (c + t) * LDM + j] -= w * x[t];
       }
-      if (g.owns(c)) S[WM + c * N + c] = beta;
+      if (g.owns(c)) S[WM + c * LDM + c] = beta;
     }
     g.sync();
   }
@@ -169,7 +175,7 @@ template <typename T, int NU, int D, bool REVERT, int L, int IPW>
 PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&q1)[kMaxN][kMaxN], int from, T h,
                            T scale, int pred) {
   using Lay = DenseLayout<NU, D>;
-  constexpr int n = NU + 1, N = Lay::N, C = REVERT ? 2 * N : N, WS = 2 * N;
+  constexpr int n = NU + 1, N = Lay::N, C = REVERT ? 2 * N : N, WS = Lay::WS, LD = Lay::LD;
   constexpr int W = Lay::W;
   T pc[n], pic[n];
   precon<T, NU>(h, pc, pic);
@@ -217,7 +223,7 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
 #pragma unroll
         for (int kk = 0; kk < n; ++kk) {
           const int k = kk * D + cd;
-          if (kk >= ci && k >= r) acc += coef[kk] * S[from + Lay::L + k * N + r];
+          if (kk >= ci && k >= r) acc += coef[kk] * S[from + Lay::L + k * LD + r];
         }
         S[W + (N + r) * WS + c] = acc;
       }
@@ -227,7 +233,7 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
 #pragma unroll
       for (int r = 0; r < N; ++r) S[W + r * WS + c] = T(0);
 #pragma unroll
-      for (int r = 0; r < N; ++r) S[W + (N + r) * WS + c] = r <= cc ? pk * S[from + Lay::L + cc * N + r] : T(0);
+      for (int r = 0; r < N; ++r) S[W + (N + r) * WS + c] = r <= cc ? pk * S[from + Lay::L + cc * LD + r] : T(0);
     }
   }
   g.sync();
@@ -296,7 +302,7 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
   for (int i = g.lane; i < N; i += L) {
     const T pa = dev_abs(S[Lay::PT + i / D]);
 #pragma unroll
-    for (int j = 0; j < N; ++j) S[pred + Lay::L + i * N + j] = (j <= i) ? pa * S[W + j * WS + i] : T(0);
+    for (int j = 0; j < N; ++j) S[pred + Lay::L + i * LD + j] = (j <= i) ? pa * S[W + j * WS + i] : T(0);
   }
   if constexpr (REVERT) {
     // G^T = R11^-1 R12 column by column; cond.A[jj][i] = G^T[i][jj], cond.xi = mean_l - G mobs
@@ -313,7 +319,7 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
       T xi = S[Lay::PT + n + jj / D] * S[from + Lay::m + jj];  // mean_l[jj]
 #pragma unroll
       for (int k = 0; k < N; ++k) {
-        S[Lay::cnA + jj * N + k] = gc[k];
+        S[Lay::cnA + jj * LD + k] = gc[k];
         xi -= gc[k] * mobs[k];
       }
       S[Lay::cnXi + jj] = xi;
@@ -328,7 +334,7 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
 template <typename T, int NU, int D, int L, int IPW>
 PDQ_D void dstruct_merge(Soa<T, IPW> S, const LaneGroup<L>& g, int o, T h, int out) {
   using Lay = DenseLayout<NU, D>;
-  constexpr int n = NU + 1, N = Lay::N, WS = 2 * N;
+  constexpr int n = NU + 1, N = Lay::N, WS = Lay::WS, LD = Lay::LD, WMS = Lay::WMS;
   constexpr int W = Lay::W, WM = Lay::WM;
   T pc[n], pic[n];
   precon<T, NU>(h, pc, pic);
@@ -342,7 +348,7 @@ PDQ_D void dstruct_merge(Soa<T, IPW> S, const LaneGroup<L>& g, int o, T h, int o
       T u[N], u2[N];
 #pragma unroll
       for (int k = 0; k < N; ++k) {
-        u[k] = Tv[k] * S[Lay::cnA + k * N + j];
+        u[k] = Tv[k] * S[Lay::cnA + k * LD + j];
         u2[k] = k >= j ? dev_abs(Tv[k]) * S[W + (N + j) * WS + N + k] : T(0);
       }
 #pragma unroll
@@ -350,31 +356,31 @@ PDQ_D void dstruct_merge(Soa<T, IPW> S, const LaneGroup<L>& g, int o, T h, int o
         T ga = T(0), r1 = T(0);
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-          const T oa = S[o + Lay::A + i * N + k];
+          const T oa = S[o + Lay::A + i * LD + k];
           ga += oa * u[k];
           if (k >= j) r1 += oa * u2[k];
         }
-        S[out + Lay::A + i * N + j] = ga;
-        S[WM + j * N + i] = r1;
+        S[out + Lay::A + i * LD + j] = ga;
+        S[WM + j * WMS + i] = r1;
       }
       // R2 row j = (o.X^T) row j
 #pragma unroll
-      for (int i = 0; i < N; ++i) S[WM + (N + j) * N + i] = i >= j ? S[o + Lay::X + i * N + j] : T(0);
+      for (int i = 0; i < N; ++i) S[WM + (N + j) * WMS + i] = i >= j ? S[o + Lay::X + i * LD + j] : T(0);
       // out.xi[j] = o.xi[j] + (o.A T in.xi)[j]
       T x = S[o + Lay::xi + j];
 #pragma unroll
-      for (int k = 0; k < N; ++k) x += S[o + Lay::A + j * N + k] * Tv[k] * S[Lay::cnXi + k];
+      for (int k = 0; k < N; ++k) x += S[o + Lay::A + j * LD + k] * Tv[k] * S[Lay::cnXi + k];
       S[out + Lay::xi + j] = x;
       S[out + Lay::tl + j] = dev_rcp(S[Lay::PT + j / D]);
       S[out + Lay::to + j] = S[o + Lay::to + j];
     }
   }
   g.sync();
-  dstruct_qr_stacked<T, N, L, IPW>(S, g, WM);
+  dstruct_qr_stacked<T, N, L, IPW, WMS>(S, g, WM);
 #pragma unroll 1
   for (int i = g.lane; i < N; i += L) {
 #pragma unroll
-    for (int j = 0; j < N; ++j) S[out + Lay::X + i * N + j] = (j <= i) ? S[WM + j * N + i] : T(0);
+    for (int j = 0; j < N; ++j) S[out + Lay::X + i * LD + j] = (j <= i) ? S[WM + j * WMS + i] : T(0);
   }
   g.sync();
 }
@@ -384,21 +390,21 @@ PDQ_D void dstruct_merge(Soa<T, IPW> S, const LaneGroup<L>& g, int o, T h, int o
 template <typename T, int NU, int D, int L, int IPW>
 PDQ_D void dstruct_cond_marginalise(Soa<T, IPW> S, const LaneGroup<L>& g, int c, int rv, int out) {
   using Lay = DenseLayout<NU, D>;
-  constexpr int N = Lay::N, WM = Lay::WM;
+  constexpr int N = Lay::N, WM = Lay::WM, LD = Lay::LD, WMS = Lay::WMS;
   // rows r of (A (tl L))^T and of X^T, by rows
 #pragma unroll 1
   for (int r = g.lane; r < N; r += L) {
     {
       T u[N];
 #pragma unroll
-      for (int k = 0; k < N; ++k) u[k] = k >= r ? S[c + Lay::tl + k] * S[rv + Lay::L + k * N + r] : T(0);
+      for (int k = 0; k < N; ++k) u[k] = k >= r ? S[c + Lay::tl + k] * S[rv + Lay::L + k * LD + r] : T(0);
 #pragma unroll
       for (int col = 0; col < N; ++col) {
         T acc = T(0);
 #pragma unroll
-        for (int k = r; k < N; ++k) acc += S[c + Lay::A + col * N + k] * u[k];
-        S[WM + r * N + col] = acc;
-        S[WM + (N + r) * N + col] = col >= r ? S[c + Lay::X + col * N + r] : T(0);
+        for (int k = r; k < N; ++k) acc += S[c + Lay::A + col * LD + k] * u[k];
+        S[WM + r * WMS + col] = acc;
+        S[WM + (N + r) * WMS + col] = col >= r ? S[c + Lay::X + col * LD + r] : T(0);
       }
     }
   }
@@ -408,11 +414,11 @@ PDQ_D void dstruct_cond_marginalise(Soa<T, IPW> S, const LaneGroup<L>& g, int c,
   for (int i = 0; i < N; ++i) {
     T acc = T(0);
 #pragma unroll
-    for (int k = 0; k < N; ++k) acc += S[c + Lay::A + i * N + k] * S[c + Lay::tl + k] * S[rv + Lay::m + k];
+    for (int k = 0; k < N; ++k) acc += S[c + Lay::A + i * LD + k] * S[c + Lay::tl + k] * S[rv + Lay::m + k];
     mo[i] = S[c + Lay::to + i] * (acc + S[c + Lay::xi + i]);
   }
   g.sync();
-  dstruct_qr_stacked<T, N, L, IPW>(S, g, WM);
+  dstruct_qr_stacked<T, N, L, IPW, WMS>(S, g, WM);
 #pragma unroll
   for (int i = 0; i < N; ++i)
     if (g.owns(i)) S[out + Lay::m + i] = mo[i];
@@ -420,26 +426,26 @@ PDQ_D void dstruct_cond_marginalise(Soa<T, IPW> S, const LaneGroup<L>& g, int c,
   for (int i = g.lane; i < N; i += L) {
     const T to = dev_abs(S[c + Lay::to + i]);
 #pragma unroll
-    for (int j = 0; j < N; ++j) S[out + Lay::L + i * N + j] = (j <= i) ? to * S[WM + j * N + i] : T(0);
+    for (int j = 0; j < N; ++j) S[out + Lay::L + i * LD + j] = (j <= i) ? to * S[WM + j * WMS + i] : T(0);
   }
   g.sync();
 }
 
-template <typename T, int N, int L, int IPW>
+template <typename T, int NU, int D, int L, int IPW>
 PDQ_D void dstruct_cond_identity(Soa<T, IPW> S, const LaneGroup<L>& g, int c) {
-  constexpr int NN = N * N;  // the DenseLayout offsets: A 0, xi NN, X NN + N, tl 2 NN + N, to 2 NN + 2 N
+  using Lay = DenseLayout<NU, D>;
+  constexpr int N = Lay::N, LD = Lay::LD;
+#pragma unroll 1
+  for (int i = g.lane; i < N; i += L) {
 #pragma unroll
-  for (int i = 0; i < N; ++i)
-    if (g.owns(i)) {
-#pragma unroll
-      for (int j = 0; j < N; ++j) {
-        S[c + i * N + j] = (i == j) ? T(1) : T(0);  // A
-        S[c + NN + N + i * N + j] = T(0);           // X
-      }
-      S[c + NN + i] = T(0);               // xi
-      S[c + 2 * NN + N + i] = T(1);       // tl
-      S[c + 2 * NN + 2 * N + i] = T(1);   // to
+    for (int j = 0; j < N; ++j) {
+      S[c + Lay::A + i * LD + j] = (i == j) ? T(1) : T(0);
+      S[c + Lay::X + i * LD + j] = T(0);
     }
+    S[c + Lay::xi + i] = T(0);
+    S[c + Lay::tl + i] = T(1);
+    S[c + Lay::to + i] = T(1);
+  }
   g.sync();
 }
 
@@ -450,38 +456,50 @@ PDQ_D void dstruct_copy(Soa<T, IPW> S, const LaneGroup<L>& g, int dst, int src) 
   g.sync();
 }
 
-// store_cond / load_cond (dense_solver.cuh) from / to shared memory: one
-// lane writes the workspace record (rare: once per checkpoint).
-template <typename T, int N, int L, int IPW>
+// store_cond / load_cond (dense_solver.cuh: A, xi, the packed lower X, tl,
+// to) from / to shared memory: one lane writes the workspace record (rare:
+// once per checkpoint).
+template <typename T, int NU, int D, int L, int IPW>
 PDQ_D void dstruct_store_cond(Soa<T, IPW> S, const LaneGroup<L>& g, int c, T* base) {
-  constexpr int NN = N * N;
+  using Lay = DenseLayout<NU, D>;
+  constexpr int N = Lay::N, LD = Lay::LD;
   if (g.lane == 0) {
     int o = 0;
-    for (int e = 0; e < NN + N; ++e) base[o++] = S[c + e];  // A, xi
     for (int i = 0; i < N; ++i)
-      for (int j = 0; j <= i; ++j) base[o++] = S[c + NN + N + i * N + j];
-    for (int e = 0; e < 2 * N; ++e) base[o++] = S[c + 2 * NN + N + e];  // tl, to
+      for (int j = 0; j < N; ++j) base[o++] = S[c + Lay::A + i * LD + j];
+    for (int i = 0; i < N; ++i) base[o++] = S[c + Lay::xi + i];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j <= i; ++j) base[o++] = S[c + Lay::X + i * LD + j];
+    for (int i = 0; i < N; ++i) base[o++] = S[c + Lay::tl + i];
+    for (int i = 0; i < N; ++i) base[o++] = S[c + Lay::to + i];
   }
   g.sync();
 }
 
-template <typename T, int N, int L, int IPW>
+template <typename T, int NU, int D, int L, int IPW>
 PDQ_D void dstruct_load_cond(Soa<T, IPW> S, const LaneGroup<L>& g, int c, const T* base) {
-  constexpr int NN = N * N;
+  using Lay = DenseLayout<NU, D>;
+  constexpr int N = Lay::N, LD = Lay::LD;
   if (g.lane == 0) {
     int o = 0;
-    for (int e = 0; e < NN + N; ++e) S[c + e] = base[o++];
     for (int i = 0; i < N; ++i)
-      for (int j = 0; j < N; ++j) S[c + NN + N + i * N + j] = (j <= i) ? base[o++] : T(0);
-    for (int e = 0; e < 2 * N; ++e) S[c + 2 * NN + N + e] = base[o++];
+      for (int j = 0; j < N; ++j) S[c + Lay::A + i * LD + j] = base[o++];
+    for (int i = 0; i < N; ++i) S[c + Lay::xi + i] = base[o++];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) S[c + Lay::X + i * LD + j] = (j <= i) ? base[o++] : T(0);
+    for (int i = 0; i < N; ++i) S[c + Lay::tl + i] = base[o++];
+    for (int i = 0; i < N; ++i) S[c + Lay::to + i] = base[o++];
   }
   g.sync();
 }
 
-template <typename T, int N, int L, int IPW>
+// A normal (mean, Cholesky factor) from shared memory to the float64 outputs (row stride N).
+template <typename T, int NU, int D, int L, int IPW>
 PDQ_D void dstruct_write_normal(Soa<T, IPW> S, const LaneGroup<L>& g, int x, double* mean, double* chol) {
-  for (int e = g.lane; e < N; e += L) mean[e] = double(S[x + e]);
-  for (int e = g.lane; e < N * N; e += L) chol[e] = double(S[x + N + e]);
+  using Lay = DenseLayout<NU, D>;
+  constexpr int N = Lay::N, LD = Lay::LD;
+  for (int e = g.lane; e < N; e += L) mean[e] = double(S[x + Lay::m + e]);
+  for (int e = g.lane; e < N * N; e += L) chol[e] = double(S[x + Lay::L + (e / N) * LD + e % N]);
 }
 
 template <typename T, int NU, class F, bool TS1, bool FP, int L>
@@ -523,14 +541,14 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
       for (int i = 0; i < n; ++i)
 #pragma unroll
         for (int j = 0; j < D; ++j) S[ix + Lay::m + i * D + j] = T(tc[i][j]);
-      for (int e = 0; e < N * N; ++e) S[ix + Lay::L + e] = T(0);
+      for (int e = 0; e < N * Lay::LD; ++e) S[ix + Lay::L + e] = T(0);
     }
     g.sync();
   }
   dstruct_copy<T, Lay::kNormal, L, IPW>(S, g, ii, ix);
   if constexpr (FP) {
-    dstruct_cond_identity<T, N, L, IPW>(S, g, ibw);
-    dstruct_cond_identity<T, N, L, IPW>(S, g, ibwi);
+    dstruct_cond_identity<T, NU, D, L, IPW>(S, g, ibw);
+    dstruct_cond_identity<T, NU, D, L, IPW>(S, g, ibwi);
   }
 
   double t = save_at[0], ti = t, dt = a.dt0[b], pi_prev = 1.0, mle_sumsq = 0.0;
@@ -539,7 +557,7 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
   const T damp = T(a.damp);
 
   if (valid && !a.terminal_only) {
-    dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.u_mean + (b * S_out) * N, a.u_chol + (b * S_out) * N * N);
+    dstruct_write_normal<T, NU, D, L, IPW>(S, g, ix, a.u_mean + (b * S_out) * N, a.u_chol + (b * S_out) * N * N);
     if (g.lane == 0) {
       a.output_scale[b * S_out] = 1.0;
       a.t_out[b * S_out] = t;
@@ -547,7 +565,7 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
     }
   }
   if (valid && a.filter_mean)
-    dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.filter_mean + (b * Sn) * N, a.filter_chol + (b * Sn) * N * N);
+    dstruct_write_normal<T, NU, D, L, IPW>(S, g, ix, a.filter_mean + (b * Sn) * N, a.filter_chol + (b * Sn) * N * N);
 
   // One attempt per iteration (the retry loop flattened into the checkpoint
   // loop), warp-uniform: every group of the warp runs the attempt's
@@ -676,11 +694,11 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
           for (int aa = 0; aa < D; ++aa) {
             T acc = T(0);
 #pragma unroll
-            for (int k = rr; k < 2 * D; ++k) acc += J[aa][k] * S[ipred + Lay::L + k * N + rr];
+            for (int k = rr; k < 2 * D; ++k) acc += J[aa][k] * S[ipred + Lay::L + k * Lay::LD + rr];
             Wu[D + rr][aa] = acc;
           }
 #pragma unroll
-          for (int c = 0; c < N; ++c) Wu[D + rr][D + c] = c >= rr ? S[ipred + Lay::L + c * N + rr] : T(0);
+          for (int c = 0; c < N; ++c) Wu[D + rr][D + c] = c >= rr ? S[ipred + Lay::L + c * Lay::LD + rr] : T(0);
         }
         householder_r<T, 3 * D, D + N>(Wu);
         // G^T = R_Y^-1 R12 (d x N); the proposal's mean mp - G ro, ro = r (the linearisation point is mp)
@@ -709,8 +727,8 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
               T v;
               if (j > i) v = T(0);
               else if (j < 2 * D) v = Wu[D + j][D + i];
-              else v = S[ipred + Lay::L + i * N + j];
-              S[inew + Lay::L + i * N + j] = v;
+              else v = S[ipred + Lay::L + i * Lay::LD + j];
+              S[inew + Lay::L + i * Lay::LD + j] = v;
             }
           }
         }
@@ -791,14 +809,14 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
         // estimators_and_losses.py:549-591
         dstruct_predict<T, NU, D, true, L, IPW>(S, g, a.q1, ii, h0, sigma_sf, ipred);  // extrapolated_t, c0
         dstruct_merge<T, NU, D, L, IPW>(S, g, ibwi, h0, itmp);                         // its conditional
-        dstruct_store_cond<T, N, L, IPW>(S, g, itmp, ws + int64_t(s - 1) * cond_floats<N>());
+        dstruct_store_cond<T, NU, D, L, IPW>(S, g, itmp, ws + int64_t(s - 1) * cond_floats<N>());
         {  // keep extrapolated_t in the proposal slot
           const int o = inew;
           inew = ipred;
           ipred = o;
         }
         dstruct_predict<T, NU, D, true, L, IPW>(S, g, a.q1, inew, h1, sigma_sf, ipred);  // c1
-        dstruct_cond_identity<T, N, L, IPW>(S, g, ibwi);
+        dstruct_cond_identity<T, NU, D, L, IPW>(S, g, ibwi);
         dstruct_merge<T, NU, D, L, IPW>(S, g, ibwi, h1, ibw);  // extrapolated_t1.conditional -> step_from's
         {  // interp_from = extrapolated_t
           const int o = ii;
@@ -814,7 +832,7 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
       }
       ti = t_next;
       if (record) {
-        dstruct_write_normal<T, N, L, IPW>(S, g, ii, a.u_mean + rec * N, a.u_chol + rec * N * N);
+        dstruct_write_normal<T, NU, D, L, IPW>(S, g, ii, a.u_mean + rec * N, a.u_chol + rec * N * N);
         if (g.lane == 0) {
           a.output_scale[rec] = double(sigma_sf);
           a.t_out[rec] = t_next;
@@ -822,18 +840,18 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
         }
       }
       if (a.filter_mean)
-        dstruct_write_normal<T, N, L, IPW>(S, g, ii, a.filter_mean + (b * Sn + s) * N, a.filter_chol + (b * Sn + s) * N * N);
+        dstruct_write_normal<T, NU, D, L, IPW>(S, g, ii, a.filter_mean + (b * Sn + s) * N, a.filter_chol + (b * Sn + s) * N * N);
     } else {
       // interp_at_t1 (solvers.py:271-315)
       if constexpr (FP) {
-        dstruct_store_cond<T, N, L, IPW>(S, g, ibw, ws + int64_t(s - 1) * cond_floats<N>());
-        dstruct_cond_identity<T, N, L, IPW>(S, g, ibw);
-        dstruct_cond_identity<T, N, L, IPW>(S, g, ibwi);
+        dstruct_store_cond<T, NU, D, L, IPW>(S, g, ibw, ws + int64_t(s - 1) * cond_floats<N>());
+        dstruct_cond_identity<T, NU, D, L, IPW>(S, g, ibw);
+        dstruct_cond_identity<T, NU, D, L, IPW>(S, g, ibwi);
       }
       dstruct_copy<T, Lay::kNormal, L, IPW>(S, g, ii, ix);
       ti = t;
       if (record) {
-        dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.u_mean + rec * N, a.u_chol + rec * N * N);
+        dstruct_write_normal<T, NU, D, L, IPW>(S, g, ix, a.u_mean + rec * N, a.u_chol + rec * N * N);
         if (g.lane == 0) {
           a.output_scale[rec] = double(sigma_sf);
           a.t_out[rec] = t;
@@ -841,7 +859,7 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
         }
       }
       if (a.filter_mean)
-        dstruct_write_normal<T, N, L, IPW>(S, g, ix, a.filter_mean + (b * Sn + s) * N, a.filter_chol + (b * Sn + s) * N * N);
+        dstruct_write_normal<T, NU, D, L, IPW>(S, g, ix, a.filter_mean + (b * Sn + s) * N, a.filter_chol + (b * Sn + s) * N * N);
     }
     // checkpoint s done
     ++s;
@@ -867,16 +885,16 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
     for (int s2 = Sn - 1; s2 >= 1; --s2) {
       if (!a.terminal_only || s2 == Sn - 1) {
         const int64_t rec = b * S_out + (a.terminal_only ? 0 : s2);
-        dstruct_write_normal<T, N, L, IPW>(S, g, irv, a.u_mean + rec * N, a.u_chol + rec * N * N);
+        dstruct_write_normal<T, NU, D, L, IPW>(S, g, irv, a.u_mean + rec * N, a.u_chol + rec * N * N);
       }
       if (a.terminal_only) break;
-      dstruct_load_cond<T, N, L, IPW>(S, g, itmp, ws + int64_t(s2 - 1) * cond_floats<N>());
+      dstruct_load_cond<T, NU, D, L, IPW>(S, g, itmp, ws + int64_t(s2 - 1) * cond_floats<N>());
       if (a.cond_A) {
         const int64_t cr = b * (Sn - 1) + (s2 - 1);
         constexpr int NN = N * N;
         for (int e = g.lane; e < NN; e += L) {
-          a.cond_A[cr * NN + e] = double(S[itmp + Lay::A + e]);
-          a.cond_noise_chol[cr * NN + e] = double(S[itmp + Lay::X + e]) * scale;
+          a.cond_A[cr * NN + e] = double(S[itmp + Lay::A + (e / N) * Lay::LD + e % N]);
+          a.cond_noise_chol[cr * NN + e] = double(S[itmp + Lay::X + (e / N) * Lay::LD + e % N]) * scale;
         }
         for (int e = g.lane; e < N; e += L) {
           a.cond_noise_mean[cr * N + e] = double(S[itmp + Lay::xi + e]);
@@ -892,7 +910,7 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
       }
       if (s2 == 1) {
         const int64_t rec = b * S_out;
-        dstruct_write_normal<T, N, L, IPW>(S, g, irv, a.u_mean + rec * N, a.u_chol + rec * N * N);
+        dstruct_write_normal<T, NU, D, L, IPW>(S, g, irv, a.u_mean + rec * N, a.u_chol + rec * N * N);
       }
     }
   }
