@@ -15,8 +15,11 @@ between steps outside the events); ``e2e`` times the public API
 (``probdiffeq_gb300.ensemble.solve_ensemble``) from pinned host inputs to
 pinned host outputs, copies included.  The same line carries the float64
 batch, the single-instance latencies (the plain per-instance method), the
-LML-gradient throughput and the block-diagonal Burgers configuration (64
-instances, d = 4096, t in [0, 1], float32, one solve) under ``secondary``.
+LML-gradient throughput, the block-diagonal Burgers configuration (64
+instances, d = 4096, t in [0, 1], float32, one solve) and the stiff dense
+van der Pol configuration (4096 instances, mu <= 1000, 100 save points,
+float32, one solve; float64 against float32 on mu <= 10) under
+``secondary``.
 
 Other workloads, one JSON line each (``--workload``):
   lv_single          one LV instance, dynamic calibration, float64 and float32
@@ -544,6 +547,150 @@ def burgers_blockdiag_secondary(torch, _native, ensemble, device, t1=1.0, cpu=Tr
     return out
 
 
+# FLOP per attempt of the structured dense kernel (N = 8, d = 2, TS1, fixed-point
+# smoother): predict fill 320, revert QR phase 1 3456 and phase 2 742, G and the
+# conditional's offset 640, merge products 1792 and QR 1152, the update on the 3d
+# rows the linearisation reads 658, observed QR, field and Jacobian, error ~360
+VDP_FLOPS_PER_ATTEMPT = 9120
+
+
+def oracle_vdp_attempt_seconds(mu=3.0):
+    """Seconds per attempt of the oracle's dense TS1 fixed-point solve of van
+    der Pol (PyTorch float64, one thread) at ``mu`` with 100 save points."""
+    import time
+
+    import numpy as np
+    import torch
+
+    from oracle import problems, solvers, ssm
+
+    threads = torch.get_num_threads()
+    torch.set_num_threads(1)
+    try:
+        p = torch.tensor([mu], dtype=torch.float64)
+        tc = problems.taylor_derivatives(problems.van_der_pol, torch.tensor([2.0, 0.0], dtype=torch.float64), p, 3)
+        S = ssm.DenseSSM()
+        c = S.constraint_ode_ts1(lambda u, t: problems.van_der_pol(u[0], p),
+                                 lambda u, t: problems.jacobian(problems.van_der_pol, u, p), 2)
+        t = time.perf_counter()
+        res = solvers.solve_adaptive_save_at(solvers.SolverDynamic(solvers.StrategyFixedPoint(), c),
+                                             solvers.ErrorResidualStd(c), S.prior_wiener_integrated(tc),
+                                             np.linspace(0.0, 2.0 * mu, 100), 1e-5, 1e-5)
+        sec = (time.perf_counter() - t) / res.num_attempts
+    finally:
+        torch.set_num_threads(threads)
+    return sec, res.num_attempts
+
+
+def vdp_dense_secondary(torch, _native, ensemble, device, mu_max=1000.0, cpu=True):
+    """The stiff dense configuration: 4096 van der Pol instances, mu ~
+    log-uniform [1, mu_max], y0 = (2, 0), t in [0, 2 mu] with 100 save points,
+    IWP nu = 3, dense TS1, fixed-point smoother, dynamic calibration,
+    rtol = atol = 1e-5; float32, the structure-exploiting kernel.
+
+    One solve (about a minute at mu_max = 1000: the slowest instance takes
+    3.1 M attempts) after a warm-up on mu <= 2: inputs copied from pinned host
+    memory, the solver, the 100 smoothed marginals and the posterior's
+    backward conditionals copied back to pinned host memory, CUDA events
+    around the solver (``value``) and the whole step (``e2e``).  The float64
+    batch and a float32 one for the ratio run on mu <= 10 (a float64 solve to
+    mu = 1000 takes about ten minutes: GB300's FP64 pipe)."""
+    from probdiffeq_gb300 import configs
+
+    B, S = 4096, 100
+    stream = torch.cuda.current_stream()
+
+    def cfg_of(precision):
+        return ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense", constraint="ts1",
+                                    strategy="fixedpoint", solver="dynamic", precision=precision, atol=1e-5,
+                                    rtol=1e-5, clip_dt=False, max_attempts=1 << 24)
+
+    def inputs(mu_hi):
+        mu, save_at, y0 = configs.vdp_dense(B, mu_hi)
+        return (mu[:, None].contiguous().pin_memory(), save_at.pin_memory(), y0.pin_memory(),
+                torch.full((B,), 0.1, dtype=torch.float64).pin_memory())
+
+    def solve(cfg, host, outs):
+        dev = [x.to(device, non_blocking=True) for x in host]
+        _native.solve_adaptive(cfg, dev[1], dev[0], dev[2], dev[3], False, outs, stream=stream)
+        return dev
+
+    cfg32 = cfg_of("float32")
+    outs = _native.alloc_outputs(cfg32, B, S, False, device, posterior=True)
+    solve(cfg32, inputs(2.0), outs)  # warm-up (module load, first touch)
+    torch.cuda.synchronize()
+    host = inputs(mu_max)
+    h_out = {k: torch.empty(tuple(v.shape), dtype=v.dtype).pin_memory() for k, v in outs.items()
+             if isinstance(v, torch.Tensor) and not k.startswith("_")}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    dev = [x.to(device, non_blocking=True) for x in host]
+    ev[1].record(stream)
+    _native.solve_adaptive(cfg32, dev[1], dev[0], dev[2], dev[3], False, outs, stream=stream)
+    ev[2].record(stream)
+    for k, v in h_out.items():
+        v.copy_(outs[k], non_blocking=True)
+    ev[3].record(stream)
+    ev[3].synchronize()
+    t_kernel = ev[1].elapsed_time(ev[2]) / 1e3
+    t_e2e = ev[0].elapsed_time(ev[3]) / 1e3
+    attempts = outs["num_attempts"].to(torch.float64)
+    steps = outs["num_steps"][:, -1].to(torch.float64)
+    status_ok = int((outs["status"] == 0).sum())
+    flops = float(attempts.sum()) * VDP_FLOPS_PER_ATTEMPT
+    achieved = flops / t_kernel / 1e12
+    peak, sms = measured_fp32_peak(torch, _native, device)
+    out = {
+        "config": {"workload": "van_der_pol_dense", "instances": B, "mu": f"log-uniform [1, {mu_max}]",
+                   "t_span": "[0, 2 mu]", "save_at": S, "num_derivatives": 3, "ssm": "dense", "constraint": "ts1",
+                   "strategy": "fixedpoint", "solver": "dynamic", "rtol": 1e-5, "atol": 1e-5, "precision": "float32",
+                   "kernel": "structure-exploiting QRs, 4 lanes per instance", "steps": 1,
+                   "warmup": "one solve with mu <= 2"},
+        "value": B / t_kernel, "unit": "solves/s", "ms_per_step": 1e3 * t_kernel,
+        "e2e": {"value": B / t_e2e, "unit": "solves/s",
+                "h2d_bytes_per_step": sum(x.numel() * x.element_size() for x in host),
+                "d2h_bytes_per_step": sum(v.numel() * v.element_size() for v in h_out.values())},
+        "stats": {"attempts_max": int(attempts.max()), "attempts_mean": float(attempts.mean()),
+                  "accepted_steps_max": int(steps.max()), "accepted_steps_mean": float(steps.mean()),
+                  "us_per_attempt_slowest": 1e6 * t_kernel / float(attempts.max()), "status_ok": status_ok},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "flops_per_attempt": VDP_FLOPS_PER_ATTEMPT,
+                     "peak_source": f"measured FP32 FMA probe on this GPU ({sms} SMs)",
+                     "note": "latency-bound: the batch time is the slowest instance's 3.1 M attempts, each a "
+                             "chain of dependent reflectors on four lanes; most SMs are idle for most of it"},
+        "gpu_launches": 1,
+    }
+    # float64 and float32 on mu <= 10 (the float64 batch to mu = 1000 does not fit the run's time)
+    small = inputs(10.0)
+    res = {}
+    for precision in ("float32", "float64"):
+        c = cfg_of(precision)
+        o = _native.alloc_outputs(c, B, S, False, device, posterior=True)
+        solve(c, small, o)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        d = [x.to(device) for x in small]
+        torch.cuda.synchronize()
+        e0.record(stream)
+        _native.solve_adaptive(c, d[1], d[0], d[2], d[3], False, o, stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        res[precision] = {"solves_per_s": B / t, "ms_per_step": 1e3 * t, "attempts_max": int(o["num_attempts"].max()),
+                          "status_ok": int((o["status"] == 0).sum())}
+    res["fp32_speedup"] = res["float32"]["solves_per_s"] / res["float64"]["solves_per_s"]
+    out["mu_le_10"] = res
+    if cpu:
+        sec, n_att = oracle_vdp_attempt_seconds()
+        out["cpu_baseline"] = {
+            "value": 1.0 / (sec * float(attempts.mean())), "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"oracle (PyTorch float64 CPU restatement) at mu = 3 with 100 save points ({n_att} attempts, "
+                      f"{1e3 * sec:.1f} ms each), multiplied by this run's mean attempts per instance; one process, "
+                      "one torch thread",
+        }
+    return out
+
+
 # ---------------------------------------------------------------------------
 # the headline workload
 # ---------------------------------------------------------------------------
@@ -657,6 +804,9 @@ def run_lv_ensemble(args):
             if args.burgers_t1 > 0 and world == 1:
                 secondary["burgers_blockdiag"] = burgers_blockdiag_secondary(
                     torch, _native, ensemble, device, t1=args.burgers_t1, cpu=not args.no_cpu_baseline)
+            if args.vdp_mu_max > 0 and world == 1:
+                secondary["vdp_dense"] = vdp_dense_secondary(torch, _native, ensemble, device, mu_max=args.vdp_mu_max,
+                                                             cpu=not args.no_cpu_baseline)
     finally:
         clk.__exit__(None, None, None)
 
@@ -928,6 +1078,8 @@ def main():
                     help="skip the single-instance, LML and block-diagonal Burgers measurements")
     ap.add_argument("--burgers-t1", type=float, default=1.0,
                     help="lv_ensemble: horizon of the block-diagonal Burgers secondary (0 skips it)")
+    ap.add_argument("--vdp-mu-max", type=float, default=1000.0,
+                    help="lv_ensemble: mu range of the stiff dense van der Pol secondary (0 skips it)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="ensemble size (16384 is the headline workload)")
     ap.add_argument("--mu-max", type=float, default=1000.0, help="vdp_dense: mu ~ log-uniform [1, mu_max]")
