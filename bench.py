@@ -288,6 +288,26 @@ def single_instance(torch, _native, ensemble, device, reps=3):
     return out
 
 
+def single_instance_cpu_baseline(reps=20):
+    """The plain single-instance method on the CPU (the configuration's own
+    statement: one LV instance, float64 on the CPU): the float64 C port of the
+    reference algorithm (dynamic calibration, terminal values on [0, 50]), one
+    thread, the mean over ``reps`` solves."""
+    import time
+
+    from oracle.port import port
+
+    params, y0 = [[0.5, 0.05, 0.5, 0.05]], [[20.0, 20.0]]
+    port.solve_iso_terminal("lotka_volterra", params, y0, 4, "dynamic", threads=1)  # load, warm
+    t = time.perf_counter()
+    for _ in range(reps):
+        out = port.solve_iso_terminal("lotka_volterra", params, y0, 4, "dynamic", threads=1)
+    sec = (time.perf_counter() - t) / reps
+    return {"value": 1e3 * sec, "unit": "ms per solve", "cores": 1, "kind": "port",
+            "sample": f"{reps} solves of the one instance, float64 C port of the reference algorithm, one thread "
+                      f"({int(out['num_attempts'][0])} attempts)"}
+
+
 LML_FLOPS_PER_GRADIENT = None  # set in lml_gradients from the workload sizes
 
 
@@ -801,6 +821,7 @@ def run_lv_ensemble(args):
             }
             if not args.no_cpu_baseline:
                 secondary["lml_gradients_fhn"]["cpu_baseline"] = lml_cpu_baseline()
+                secondary["single_instance_lv_dynamic"]["cpu_baseline"] = single_instance_cpu_baseline()
             if args.burgers_t1 > 0 and world == 1:
                 secondary["burgers_blockdiag"] = burgers_blockdiag_secondary(
                     torch, _native, ensemble, device, t1=args.burgers_t1, cpu=not args.no_cpu_baseline)
@@ -923,9 +944,10 @@ def run_lv_single(args):
         r = single_instance(torch, _native, ensemble, device, reps=args.steps)
     cfg = {"workload": "lotka_volterra_single", "instances": 1, "params": [0.5, 0.05, 0.5, 0.05], "y0": [20.0, 20.0],
            "t_span": [0.0, 50.0], "num_derivatives": 4, "solver": "dynamic", "rtol": 1e-6, "atol": 1e-6}
+    cpu = None if args.no_cpu_baseline else single_instance_cpu_baseline()
     print(json.dumps(base_line("single-instance solve latency (float64)", r["float64"]["ms_per_solve"], "ms", args,
                                r["float64"]["ms_per_solve"], False, "f64", cfg, float32=r["float32"],
-                               gpu_launches=args.steps, clocks=clk.summary())))
+                               cpu_baseline=cpu, gpu_launches=args.steps, clocks=clk.summary())))
 
 
 def run_fhn_lml(args):
