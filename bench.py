@@ -448,7 +448,11 @@ def measured_l2_copy_gbs(torch, device, sizes_mib=(16, 24, 32), reps=200):
     return best
 
 
-BURGERS_BYTES_PER_DIM = 2 * 14 * 4 + 4  # float32 state row read + written, one f value
+# Algorithmic bytes per attempt and dimension of the block-diagonal solver, the
+# configuration's work model: read and write m (n) and L (n^2) in float32, one f
+# value (n = 4: 164 B; the kernel stores L packed, 2 x 14 floats + f = 116 B)
+BURGERS_BYTES_PER_DIM = 2 * (4 + 16) * 4 + 4
+BURGERS_STORED_BYTES_PER_DIM = 2 * 14 * 4 + 4
 
 
 def oracle_burgers_attempt_seconds(d_small=64, t1=0.05):
@@ -532,8 +536,13 @@ def burgers_blockdiag_secondary(torch, _native, ensemble, device, t1=1.0, cpu=Tr
     finite = bool(torch.isfinite(h_mean).all())
     bytes_alg = float(attempts.sum()) * d * BURGERS_BYTES_PER_DIM
     achieved = bytes_alg / t_kernel / 1e9
+    stored = float(attempts.sum()) * d * BURGERS_STORED_BYTES_PER_DIM / t_kernel / 1e9
     l2 = measured_l2_copy_gbs(torch, device)
-    hbm = measured_peaks().get("hbm_gbs")
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    hbm_src = "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy)"
+    if not hbm:
+        hbm, hbm_src = 6800.0, "fallback 6.8 TB/s (no measured peak file)"
     out = {
         "config": {"workload": "burgers_blockdiag", "instances": B, "d": d, "nu_visc": 0.01, "t_span": [0.0, t1],
                    "num_derivatives": 3, "ssm": "blockdiag", "constraint": "ts0", "strategy": "filter",
@@ -546,13 +555,15 @@ def burgers_blockdiag_secondary(torch, _native, ensemble, device, t1=1.0, cpu=Tr
         "stats": {"attempts_max": int(attempts.max()), "attempts_mean": float(attempts.mean()),
                   "us_per_attempt_slowest": 1e6 * t_kernel / float(attempts.max()), "status_ok": status_ok,
                   "terminal_means_finite": finite},
-        "roofline": {"bound": "l2", "achieved": achieved, "unit": "GB/s", "peak": l2, "frac": achieved / l2,
-                     "peak_source": "measured L2-resident copy (best of 2 x 16 / 24 / 32 MiB, read + write bytes) "
-                                    "on this GPU",
-                     "hbm_peak": hbm, "frac_of_hbm": (achieved / hbm) if hbm else None,
+        "roofline": {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "peak": hbm, "frac": achieved / hbm,
+                     "peak_source": hbm_src,
                      "bytes_per_attempt_dimension": BURGERS_BYTES_PER_DIM,
-                     "note": "algorithmic bytes = sum over instances of attempts x d x (2 x 14 x 4 B + 4 B); "
-                             "averaged over the launch, in which instances finish at different times"},
+                     "l2_peak": l2, "frac_of_l2": achieved / l2,
+                     "l2_peak_source": "measured L2-resident copy (best of 2 x 16 / 24 / 32 MiB, read + write bytes)",
+                     "stored_bytes_gbs": stored,
+                     "note": "algorithmic bytes = sum over instances of attempts x d x (2 (n + n^2) 4 B + 4 B), "
+                             "averaged over the launch, in which instances finish at different times; the state "
+                             "(2 x 14.7 MB) stays L2-resident, DRAM sees only inputs and outputs"},
         "gpu_launches": 1,
     }
     if cpu:
@@ -567,11 +578,15 @@ def burgers_blockdiag_secondary(torch, _native, ensemble, device, t1=1.0, cpu=Tr
     return out
 
 
-# FLOP per attempt of the structured dense kernel (N = 8, d = 2, TS1, fixed-point
-# smoother): predict fill 320, revert QR phase 1 3456 and phase 2 742, G and the
-# conditional's offset 640, merge products 1792 and QR 1152, the update on the 3d
-# rows the linearisation reads 658, observed QR, field and Jacobian, error ~360
-VDP_FLOPS_PER_ATTEMPT = 9120
+def dense_flops_per_attempt(N=8, d=2):
+    """Algorithmic FLOP per attempt of the dense TS1 fixed-point solver, the
+    convention of the configuration's work model (matmuls dense 2mnk,
+    Householder R-only QR of m x n 2mn^2 - (2/3)n^3): predict 2N^3 + (10/3)N^3,
+    update (revert) (4/3)(N+d)^3, merge 2N^3 + (10/3)N^3, TS1 2dN."""
+    return 2 * N**3 + 10 / 3 * N**3 + 4 / 3 * (N + d) ** 3 + 2 * N**3 + 10 / 3 * N**3 + 2 * d * N
+
+
+VDP_FLOPS_PER_ATTEMPT = dense_flops_per_attempt()
 
 
 def oracle_vdp_attempt_seconds(mu=3.0):
