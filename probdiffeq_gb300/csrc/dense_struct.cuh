@@ -33,6 +33,12 @@
 //   three running conditionals (running, interp, merged) rotate through slots
 //   by index on acceptance instead of being copied.
 //
+// * the mean's rows 0 and 1 (the coefficients the residual u' - f(u) reads)
+//   carry float-pair low parts in the float32 kernel, the residual is formed
+//   with the field in float-pair arithmetic and the update m' = m + (incr -
+//   G r) adds wide, as in the isotropic kernel: float32 then matches
+//   float64's error against the exact solution.
+//
 // R factors may differ from a LAPACK QR in the signs of their rows; every
 // quantity formed from them (L L^T, R11^-1 R12, R22^T R22) is invariant.
 #pragma once
@@ -73,11 +79,11 @@ struct DenseLayout {
   static constexpr int LD = N + 1;                // row stride of the N x N matrices
   static constexpr int WS = 2 * N + 1;            // row stride of the predict workspace
   static constexpr int WMS = N + 1;               // row stride of the merge workspace
-  static constexpr int kNormal = N + N * LD;      // m, L (lower)
+  static constexpr int kNormal = N + N * LD + 2 * D;  // m, L (lower), low parts of m's rows 0 and 1
   static constexpr int kCond = 2 * N * LD + 3 * N;  // A, xi, X (lower), tl, to
   static constexpr int kNormals = 4;            // step_from, interp_from, proposal, prediction (rotating)
   static constexpr int kConds = 4;              // running, interp, merged, scratch (rotating)
-  static constexpr int m = 0, L = N;
+  static constexpr int m = 0, L = N, mlo = N + N * LD;
   static constexpr int A = 0, xi = N * LD, X = N * LD + N, tl = 2 * N * LD + N, to = 2 * N * LD + 2 * N;
   static constexpr int normal0 = 0;
   static constexpr int cond0 = kNormals * kNormal;
@@ -294,10 +300,13 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
       g.sync();
     }
   }
-  // the predicted marginal: m = p mobs, L = |p| R11^T
+  // the predicted marginal: m = p mobs (no low parts), L = |p| R11^T
 #pragma unroll
   for (int i = 0; i < N; ++i)
-    if (g.owns(i)) S[pred + Lay::m + i] = pc[i / D] * mobs[i];
+    if (g.owns(i)) {
+      S[pred + Lay::m + i] = pc[i / D] * mobs[i];
+      if (i < 2 * D) S[pred + Lay::mlo + i] = T(0);
+    }
 #pragma unroll 1
   for (int i = g.lane; i < N; i += L) {
     const T pa = dev_abs(S[Lay::PT + i / D]);
@@ -498,7 +507,8 @@ template <typename T, int NU, int D, int L, int IPW>
 PDQ_D void dstruct_write_normal(Soa<T, IPW> S, const LaneGroup<L>& g, int x, double* mean, double* chol) {
   using Lay = DenseLayout<NU, D>;
   constexpr int N = Lay::N, LD = Lay::LD;
-  for (int e = g.lane; e < N; e += L) mean[e] = double(S[x + Lay::m + e]);
+  for (int e = g.lane; e < N; e += L)
+    mean[e] = double(S[x + Lay::m + e]) + (e < 2 * D ? double(S[x + Lay::mlo + e]) : 0.0);
   for (int e = g.lane; e < N * N; e += L) chol[e] = double(S[x + Lay::L + (e / N) * LD + e % N]);
 }
 
@@ -522,10 +532,12 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
 
   double pd[P];
   T pt[P];
+  Wide<T> pw[P];  // the parameters in the wide type (the residual's field evaluation)
 #pragma unroll
   for (int k = 0; k < P; ++k) {
     pd[k] = a.params[b * P + k];
     pt[k] = T(pd[k]);
+    pw[k] = wide_from(pd[k], T(0));
   }
   // slots (offsets into the instance's shared-memory record)
   int ix = Lay::normal(0), ii = Lay::normal(1), inew = Lay::normal(2), ipred = Lay::normal(3);
@@ -541,6 +553,10 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
       for (int i = 0; i < n; ++i)
 #pragma unroll
         for (int j = 0; j < D; ++j) S[ix + Lay::m + i * D + j] = T(tc[i][j]);
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) S[ix + Lay::mlo + i * D + j] = T(wide_lo(wide_from(tc[i][j], T(0))));
       for (int e = 0; e < N * Lay::LD; ++e) S[ix + Lay::L + e] = T(0);
     }
     g.sync();
@@ -601,13 +617,19 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
         T pc[n], pic[n];
         precon<T, NU>(h, pc, pic);
         // u = transition(h, 1).apply_flat(mean): mean mp, chol |p| sqrt|h| Q
-        T mp[2 * D];  // coefficients 0 and 1 are all the linearisation reads
+        // extrapolated mean of coefficients 0 and 1 (all the linearisation
+        // reads), wide as in the isotropic kernel: mp = m + incr with
+        // incr_i = p_i sum_{k > i} A1[i][k] p^-1_k m_k (A1[i][i] p_i p^-1_i = 1)
+        T mp[2 * D], mplo[2 * D], incr[2 * D];
 #pragma unroll
         for (int i = 0; i < 2 * D; ++i) {
           T acc = T(0);
 #pragma unroll
-          for (int kk = i / D; kk < n; ++kk) acc += T(iwp_a<NU>(i / D, kk)) * pic[kk] * S[ix + Lay::m + kk * D + i % D];
-          mp[i] = pc[i / D] * acc;
+          for (int kk = i / D + 1; kk < n; ++kk) acc += T(iwp_a<NU>(i / D, kk)) * pic[kk] * S[ix + Lay::m + kk * D + i % D];
+          incr[i] = pc[i / D] * acc;
+          const Wide<T> w = wide_pair(S[ix + Lay::m + i], S[ix + Lay::mlo + i]) + incr[i];
+          mp[i] = T(wide_hi(w));
+          mplo[i] = T(wide_lo(w));
         }
         // linearisation at mp: J (d x 2d; zero beyond), b; residual r = J mp + b
         T J[D][2 * D], bl[D];
@@ -638,14 +660,18 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
             }
           }
         }
+        // the residual r = J mp + b = mp_1 - f(mp_0) (the linearisation point is mp), with
+        // the field evaluated in the wide type at the wide rows, rounded once
         T r[D];
+        {
+          Wide<T> u[D], fw[D];
 #pragma unroll
-        for (int aa = 0; aa < D; ++aa) {
-          T acc = bl[aa];
+          for (int j = 0; j < D; ++j) u[j] = wide_pair(mp[j], mplo[j]);
+          F::eval(u, pw, fw);
 #pragma unroll
-          for (int k = 0; k < 2 * D; ++k) acc += J[aa][k] * mp[k];
-          r[aa] = acc;
+          for (int aa = 0; aa < D; ++aa) r[aa] = T(wide_hi(wide_pair(mp[D + aa], mplo[D + aa]) - fw[aa]));
         }
+        (void)bl;
         // observed = fx.marginalise(u): R of [(J Lu)^T (rows < 2d; zero beyond); damp I]
         const T sqh = dev_sqrt(dev_abs(h));
         T Mo[3 * D][D];
@@ -716,9 +742,19 @@ __global__ void __launch_bounds__(32) dense_struct_kernel(DenseArgs a) {
         T m0new[D];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          T acc = S[ipred + Lay::m + i];
+          T acc;
+          if (i < 2 * D) {  // m' = m + (incr - G r), summed wide
+            T dl = incr[i];
 #pragma unroll
-          for (int aa = 0; aa < D; ++aa) acc -= Gt[aa][i] * r[aa];
+            for (int aa = 0; aa < D; ++aa) dl -= Gt[aa][i] * r[aa];
+            const Wide<T> w = wide_pair(S[ix + Lay::m + i], S[ix + Lay::mlo + i]) + dl;
+            acc = T(wide_hi(w));
+            if (g.owns(i)) S[inew + Lay::mlo + i] = T(wide_lo(w));
+          } else {
+            acc = S[ipred + Lay::m + i];
+#pragma unroll
+            for (int aa = 0; aa < D; ++aa) acc -= Gt[aa][i] * r[aa];
+          }
           if (i < D) m0new[i] = acc;
           if (g.owns(i)) {
             S[inew + Lay::m + i] = acc;

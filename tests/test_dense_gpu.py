@@ -222,15 +222,13 @@ def test_vdp_mu30_100_save_points_matches_fixture(precision):
     (the oracle's 1.9e4 accepted steps, 3.2e4 attempts; the oracle output is
     the committed fixture ``tests/golden/vdp_dense_mu30.json``), the default
     (structure-exploiting) kernel.  Float64: the live-oracle tolerances at
-    every save point.  Float32: its error against the exact solution (scipy
-    Radau, rtol = atol = 1e-12) within 3x the float64 oracle's own error
-    against it in the median over the save points, and within 4x at the
-    maximum (the solver's error at rtol 1e-5 reaches several percent at the
-    relaxation oscillations' fast transitions, where a small shift in time
-    is a large difference in u; float32 measured 2.3x in the median and
-    3.1x at the maximum: the dense kernel carries its means in float32
-    without the isotropic kernel's float-pair rows), and accepted steps
-    within 2 %."""
+    every save point.  Float32: matched accuracy -- its error against the
+    exact solution (scipy Radau, rtol = atol = 1e-12) within 2x the float64
+    oracle's own error against it, in the median and at the maximum over the
+    save points (the solver's error at rtol 1e-5 reaches several percent at
+    the relaxation oscillations' fast transitions; the kernel carries the
+    mean's rows 0 and 1 and the residual in float pairs, without which
+    float32 measured 2.3x / 3.1x), and accepted steps within 2 %."""
     import scipy.integrate
 
     from tests.golden import make_golden
@@ -250,8 +248,8 @@ def test_vdp_mu30_100_save_points_matches_fixture(precision):
         scale = np.abs(truth).max(axis=1)
         e32 = np.abs(out["u_mean"][0, :, :2].numpy() - truth).max(axis=1) / scale
         e64 = np.abs(np.array([m[:2] for m in rec["u_mean"]]) - truth).max(axis=1) / scale
-        assert np.median(e32) <= 3 * np.median(e64), (np.median(e32), np.median(e64))
-        assert e32.max() <= 4 * e64.max(), (e32.max(), e64.max())
+        assert np.median(e32) <= 2 * np.median(e64), (np.median(e32), np.median(e64))
+        assert e32.max() <= 2 * e64.max(), (e32.max(), e64.max())
     for s in range(len(save_at)):
         om = torch.tensor(rec["u_mean"][s], dtype=torch.float64)
         oc = torch.tensor(rec["u_chol"][s], dtype=torch.float64)
