@@ -691,8 +691,9 @@ def vdp_dense_secondary(torch, _native, ensemble, device, mu_max=1000.0, cpu=Tru
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "flops_per_attempt": VDP_FLOPS_PER_ATTEMPT,
                      "peak_source": f"measured FP32 FMA probe on this GPU ({sms} SMs)",
-                     "note": "latency-bound: the batch time is the slowest instance's 3.1 M attempts, each a "
-                             "chain of dependent reflectors on four lanes; most SMs are idle for most of it"},
+                     "note": f"latency-bound: the batch time is the slowest instance's {attempts.max() / 1e6:.2f} M "
+                             "attempts, each a chain of dependent reflectors on four lanes; most SMs are idle for "
+                             "most of it"},
         "gpu_launches": 1,
     }
     # float64 and float32 on mu <= 10 (the float64 batch to mu = 1000 does not fit the run's time)
@@ -770,7 +771,8 @@ def run_lv_ensemble(args):
     def device_step(c):
         _native.solve_adaptive(c, d_save, d_params, d_y0, d_dt0, True, outs, stream=stream)
 
-    names = {1: "thread per instance", 2: "8 lanes per instance, <=128 regs", 3: "8 lanes per instance, <=85 regs"}
+    names = {1: "thread per instance", 2: "8 lanes per instance, <=128 regs", 3: "8 lanes per instance, <=85 regs",
+             4: "a covariance warp and a mean warp per 32 instances"}
 
     def label(cand):
         return f"{names[cand[0]]}, {cand[1] or 'default'} instances per CTA"
@@ -782,7 +784,7 @@ def run_lv_ensemble(args):
         def tune(precision):
             return autotune.tune(config(precision), d_save, d_params, d_y0, d_dt0, True, stream=stream)
 
-        fixed = {"thread": 1, "lanes": 2, "lanes_compact": 3}.get(args.variant)
+        fixed = {"thread": 1, "lanes": 2, "lanes_compact": 3, "split": 4}.get(args.variant)
         if fixed is None:
             best32, tune32 = tune("float32")
             best64, tune64 = tune("float64")
@@ -1107,8 +1109,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lv_ensemble",
                     choices=["lv_ensemble", "lv_single", "fhn_lml", "vdp_dense", "burgers_blockdiag"])
-    ap.add_argument("--variant", default="auto", choices=["auto", "thread", "lanes", "lanes_compact"],
-                    help="lv_ensemble: instance-to-lane mapping (auto = time all three and keep the fastest)")
+    ap.add_argument("--variant", default="auto", choices=["auto", "thread", "lanes", "lanes_compact", "split"],
+                    help="lv_ensemble: instance-to-lane mapping (auto = time the autotuner's candidates and keep "
+                         "the fastest)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="e2e: launch the solver eagerly instead of from CUDA graphs")
     ap.add_argument("--no-secondary", action="store_true",

@@ -114,7 +114,9 @@ typedef struct pdq_config {
   int32_t clip_dt;        /* RejectionLoop clip_dt (solvers_via_adaptive_steps.py:300-301) */
   int32_t correct_asymptotic_underconfidence; /* solver_mle (solvers.py:456-457) */
   int32_t kernel_variant;  /* isotropic mapping: 0 auto, 1 one thread per instance,
-                              2 / 3 eight lanes per instance with <= 128 / <= 85 registers (clip_dt only);
+                              2 / 3 eight lanes per instance with <= 128 / <= 85 registers (clip_dt only),
+                              4 a covariance warp and a mean warp per 32 instances (the filter with
+                              TS0, no damping, error_residual_std, clip_dt, solver none or mle);
                               dense: 0 auto (3, or 1 for error_state_std and run-time fields),
                               1 one thread per instance, 2 eight lanes per instance,
                               3 structure-exploiting QRs on four lanes per instance */

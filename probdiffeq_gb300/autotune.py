@@ -23,6 +23,7 @@ __all__ = ["candidates", "tune", "tuned_config", "cache_key", "clear_cache"]
 # (kernel_variant, instances_per_block), see include/pdq.h
 _ISO_THREAD = [(1, 64), (1, 32)]
 _ISO_LANES = [(2, 32), (2, 16), (3, 32)]
+_ISO_SPLIT = [(4, 0)]
 _DENSE_THREAD = [(1, 32), (1, 16)]
 _DENSE_LANES = [(3, 0), (2, 4), (2, 2)]
 
@@ -36,7 +37,8 @@ def candidates(cfg):
         lanes_ok = (cfg.clip_dt and cfg.constraint == _native.CONSTRAINT["ts0"]
                     and cfg.error == _native.ERROR["residual_std"] and cfg.strategy == _native.STRATEGY["filter"]
                     and cfg.field < _native.FIELD_USER_BASE)
-        return _ISO_THREAD + (_ISO_LANES if lanes_ok else [])
+        split_ok = (lanes_ok and cfg.damp == 0.0 and cfg.solver != _native.SOLVER["dynamic"])
+        return _ISO_THREAD + (_ISO_LANES if lanes_ok else []) + (_ISO_SPLIT if split_ok else [])
     if cfg.ssm == _native.SSM["dense"]:
         lanes_ok = cfg.error == _native.ERROR["residual_std"] and cfg.field < _native.FIELD_USER_BASE
         return _DENSE_THREAD + (_DENSE_LANES if lanes_ok else [])

@@ -165,7 +165,7 @@ PDQ_D void iso_mean_increment(const T (&m)[NU + 1][D], const T (&p)[NU + 1], con
       T acc = T(0);
 #pragma unroll
       for (int k = i + 1; k < n; ++k) acc += T(iwp_a<NU>(i, k)) * x[k][j];
-      incr[i][j] = p[i] * acc;
+      incr[i][j] = mul_nc(p[i], acc);  // rounded here, whatever consumes it
     }
 }
 
@@ -712,6 +712,46 @@ PDQ_D T state_std0(const A& a, const T (&p)[NU + 1], T h, T damp, T h0) {
   return dev_abs(Lc[0][0]);
 }
 
+// Error norm, acceptance and step-size controller of one attempt, from the
+// absolute error err_abs (error_residual_std or error_state_std): the
+// per-dimension ratios err_abs / (atol + rtol max(|m_0j|, |mnew_0j|)) summed
+// wide (solvers.py:925-996, the RMS norm), accepted iff the error power
+// norm^(-1/n) >= 1, i.e. iff the sum is <= D, and the I or PI controller's
+// next step (controllers.py:24-84).
+template <typename T, int NU, int D>
+PDQ_D void iso_accept_and_control(const IsoArgs& a, T err_abs, const T (&m)[NU + 1][D], const T (&mnew)[NU + 1][D],
+                                  T dt_use, T pi_prev, bool& accepted, bool& nonfinite, T& pi_new, T& dt_new) {
+  constexpr int n = NU + 1;
+  const T atol = cst<T>(a.atol, a.atol_f), rtol = cst<T>(a.rtol, a.rtol_f);
+  const T safety = cst<T>(a.safety, a.safety_f);
+  const T factor_min = cst<T>(a.factor_min, a.factor_min_f), factor_max = cst<T>(a.factor_max, a.factor_max_f);
+  Wide<T> sumsq = wide_from(0.0, T(0));
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    const T ref = fmax(dev_abs(m[0][j]), dev_abs(mnew[0][j]));
+    const T ratio = dev_div(err_abs, atol + rtol * ref);
+    sumsq = wide_add_sq(sumsq, ratio);
+  }
+  // error_norm^2 = sumsq / D; accepted iff error_power = error_norm^(-1/n)
+  // >= 1, i.e. iff sumsq <= D (decided on the wide sum)
+  const T norm2 = T(wide_hi(sumsq)) * T(1.0 / D);
+  nonfinite = !(norm2 == norm2) || isinf(norm2);
+  const T ep = dev_fpow(norm2, T(-0.5 / n));
+  accepted = wide_le(sumsq, T(D));
+  T factor;
+  pi_new = pi_prev;
+  if (a.control == PDQ_CONTROL_INTEGRAL) {
+    factor = safety * ep;
+  } else {
+    const T gi = dev_fpow(ep, cst<T>(a.exp_i, a.exp_i_f));
+    const T gp = dev_fpow(dev_div(ep, pi_prev), cst<T>(a.exp_p, a.exp_p_f));
+    factor = safety * gi * gp;
+    if (accepted) pi_new = ep;
+  }
+  factor = fmax(factor_min, fmin(factor, factor_max));
+  dt_new = factor * dt_use;
+}
+
 template <typename T, int NU, int D>
 PDQ_D void write_record(const IsoArgs& a, int64_t b, int s_out, int S_out, const T (&m)[NU + 1][D],
                         const T (&lo)[2][D], const T (&L)[NU + 1][NU + 1], double scale, double t, int steps) {
@@ -1151,9 +1191,6 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   T sigma_sf = T(1);  // output scale of step_from (dynamic solver)
   const T damp = cst<T>(a.damp, a.damp_f);
   const T eps = cst<T>(a.eps, a.eps_f);
-  const T atol = cst<T>(a.atol, a.atol_f), rtol = cst<T>(a.rtol, a.rtol_f);
-  const T safety = cst<T>(a.safety, a.safety_f);
-  const T factor_min = cst<T>(a.factor_min, a.factor_min_f), factor_max = cst<T>(a.factor_max, a.factor_max_f);
 
   // ||Q1 row OUT||^2 enters the observed std of the linearised residual
   T q1_out2 = T(0);
@@ -1295,7 +1332,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
 #pragma unroll
           for (int i = 0; i < n; ++i)
 #pragma unroll
-            for (int j = 0; j < D; ++j) dlt[i][j] = incr[i][j] - gain[i] * mobs[j];
+            for (int j = 0; j < D; ++j) dlt[i][j] = fma_nc(-gain[i], mobs[j], incr[i][j]);
           iso_mean_add<T, NU, D>(m, mlo, dlt, mnew, mnewlo);
         }
         if constexpr (TAN) {
@@ -1331,33 +1368,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
         } else {
           err_abs = rms_mobs * h;
         }
-        W sumsq = wide_from(0.0, T(0));
-#pragma unroll
-        for (int j = 0; j < D; ++j) {
-          const T ref = fmax(dev_abs(m[0][j]), dev_abs(mnew[0][j]));
-          const T ratio = dev_div(err_abs, atol + rtol * ref);
-          sumsq = wide_add_sq(sumsq, ratio);
-        }
-        // error_norm^2 = sumsq / D; accepted iff error_power = error_norm^(-1/n)
-        // >= 1, i.e. iff sumsq <= D (decided on the wide sum)
-        const T norm2 = T(wide_hi(sumsq)) * T(1.0 / D);
-        nonfinite = !(norm2 == norm2) || isinf(norm2);
-        const T ep = dev_fpow(norm2, T(-0.5 / n));
-        accepted = wide_le(sumsq, T(D));
-
-        // ---- controller (controllers.py:24-84) ----
-        T factor;
-        pi_new = pi_prev;
-        if (a.control == PDQ_CONTROL_INTEGRAL) {
-          factor = safety * ep;
-        } else {
-          const T gi = dev_fpow(ep, cst<T>(a.exp_i, a.exp_i_f));
-          const T gp = dev_fpow(dev_div(ep, pi_prev), cst<T>(a.exp_p, a.exp_p_f));
-          factor = safety * gi * gp;
-          if (accepted) pi_new = ep;
-        }
-        factor = fmax(factor_min, fmin(factor, factor_max));
-        dt_new = factor * dt_use;
+        iso_accept_and_control<T, NU, D>(a, err_abs, m, mnew, dt_use, pi_prev, accepted, nonfinite, pi_new, dt_new);
       };
       if constexpr (FP) {
         attempt(BoolTag<true>{});

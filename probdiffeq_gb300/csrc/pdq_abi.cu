@@ -10,6 +10,7 @@
 #include "lml_adj_launch.cuh"
 #include "lml_launch.cuh"
 #include "iso_launch.cuh"
+#include "iso_split_launch.cuh"
 #include "nvrtc_fields.h"
 #include "tv_launch.cuh"
 #include "pdq.h"
@@ -268,7 +269,27 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     pdq::IsoArgs a;
     iso_args_fill(c, args, a);
     const bool interp = !c->clip_dt;
-    if (c->kernel_variant < 0 || c->kernel_variant > 3) return PDQ_ERROR_INVALID_VALUE;
+    if (c->kernel_variant < 0 || c->kernel_variant > 4) return PDQ_ERROR_INVALID_VALUE;
+    if (c->kernel_variant == 4) {
+      // a covariance warp and a mean warp per 32 instances: the lean filter
+      // (TS0 without damping, error_residual_std, exact landings), solver none or mle
+      if (!c->clip_dt || a.ts1 || a.state_error || fp || a.damp != 0.0 || c->solver == PDQ_SOLVER_DYNAMIC ||
+          args->u_mean_d_params || args->u_mean_d_y0 || c->field >= PDQ_FIELD_USER_BASE)
+        return PDQ_ERROR_UNSUPPORTED;
+      if (c->instances_per_block != 0) return PDQ_ERROR_INVALID_VALUE;
+      using SplitLaunch = cudaError_t (*)(const pdq::IsoArgs&, int, cudaStream_t);
+      const bool f64 = c->precision == PDQ_PRECISION_F64;
+      SplitLaunch launch = nullptr;
+      switch (c->field) {
+        case PDQ_FIELD_LOTKA_VOLTERRA: launch = f64 ? pdq_launch_iso_split_lv_f64 : pdq_launch_iso_split_lv_f32; break;
+        case PDQ_FIELD_VAN_DER_POL: launch = f64 ? pdq_launch_iso_split_vdp_f64 : pdq_launch_iso_split_vdp_f32; break;
+        case PDQ_FIELD_FITZHUGH_NAGUMO:
+          launch = f64 ? pdq_launch_iso_split_fhn_f64 : pdq_launch_iso_split_fhn_f32;
+          break;
+        default: return PDQ_ERROR_UNSUPPORTED;
+      }
+      return launch(a, c->num_derivatives, stream) == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
+    }
     // 0 (auto) and 1: one thread per instance; 2 / 3: the lane-cooperative
     // kernel (8 lanes per instance) with <= 128 / <= 85 registers per lane,
     // for exact checkpoint landings only

@@ -120,6 +120,28 @@ PDQ_D double fast_sqrt(double x) { return sqrt(x); }
 PDQ_D double fast_rsqrt(double x) { return rsqrt(x); }
 PDQ_D double fast_rcp(double x) { return 1.0 / x; }
 
+// Named CTA barriers for a producer / consumer pair of warps: the producer
+// arrives (and goes on), the consumer waits until `count` threads (both
+// warps) have arrived.  Shared-memory writes before the arrive are visible
+// to the consumer after its wait.  The warp reconverges first, since the
+// aligned barrier wants every lane of the warp at the same instruction.
+PDQ_D void named_arrive(int id, int count) {
+#if defined(__CUDA_ARCH__)
+  __syncwarp();
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+#elif defined(PDQ_HOST_SIM)
+  pdq_host_named_arrive(id);  // host runs of the kernel bodies (tests)
+#endif
+}
+PDQ_D void named_sync(int id, int count) {
+#if defined(__CUDA_ARCH__)
+  __syncwarp();
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+#elif defined(PDQ_HOST_SIM)
+  pdq_host_named_sync(id);  // host runs of the kernel bodies (tests)
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // Wide scalars for time and accumulators
 // ---------------------------------------------------------------------------
@@ -165,6 +187,21 @@ PDQ_HD float mul_rn(float a, float b) {
   return a * b;
 #endif
 }
+// A product rounded on its own and a product-sum rounded once, both fixed by
+// the source rather than by the compiler's choice of which product to fuse
+// into which sum: kernels that share an update (the one-thread isotropic
+// kernel and its split twin) then round it alike.
+PDQ_HD float mul_nc(float a, float b) { return mul_rn(a, b); }
+PDQ_HD double mul_nc(double a, double b) {
+#if defined(__CUDA_ARCH__)
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+PDQ_HD float fma_nc(float a, float b, float c) { return fmaf(a, b, c); }
+PDQ_HD double fma_nc(double a, double b, double c) { return fma(a, b, c); }
+
 // a / b to a few ulp (single-instruction reciprocal and a product)
 PDQ_HD float div_approx(float a, float b) {
 #if defined(__CUDA_ARCH__)

@@ -54,7 +54,7 @@ def make_config(
     cfg.safety, cfg.factor_min, cfg.factor_max = float(safety), float(factor_min), float(factor_max)
     cfg.exponent_integral, cfg.exponent_proportional = float(exponent_integral), float(exponent_proportional)
     cfg.max_attempts = int(max_attempts)
-    cfg.kernel_variant = {"auto": 0, "thread": 1, "lanes": 2, "lanes_compact": 3}.get(kernel_variant, kernel_variant)
+    cfg.kernel_variant = {"auto": 0, "thread": 1, "lanes": 2, "lanes_compact": 3, "split": 4}.get(kernel_variant, kernel_variant)
     cfg.instances_per_block = int(instances_per_block)
     return cfg
 

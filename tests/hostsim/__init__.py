@@ -17,7 +17,7 @@ def compile_harness(source, exe):
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("no host C++ compiler")
-    cmd = [cxx, "-std=c++17", "-O1", "-g", "-ffp-contract=off", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+    cmd = [cxx, "-std=c++17", "-O1", "-g", "-pthread", "-ffp-contract=off", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
            "-I" + HERE, "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "probdiffeq_gb300", "csrc"),
            os.path.join(HERE, source), "-o", str(exe)]
     res = subprocess.run(cmd, capture_output=True, text=True)

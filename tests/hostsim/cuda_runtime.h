@@ -3,13 +3,52 @@
 // on the CPU, one "thread" at a time, under AddressSanitizer.  Test
 // infrastructure only: the qualifiers become no-ops, the read-only-cache
 // load is a plain load, warp primitives act on a single lane, and the CUDA
-// runtime calls used by the launch helpers are inert.  Only kernels that
-// need no cooperation between threads can run this way.
+// runtime calls used by the launch helpers are inert.  Kernels whose warps
+// cooperate run with a warp width of one lane, each warp as a host thread
+// (named barriers and __syncthreads below).
 #pragma once
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
+
+#define PDQ_HOST_SIM 1
+
+// Named barriers of a kernel whose warps run as host threads: a phase
+// completes when `expected` threads have arrived; `sync` waits for the phase
+// it arrived in, `arrive` does not wait.
+struct PdqHostBarrier {
+  std::mutex mu;
+  std::condition_variable cv;
+  int expected = 2, count = 0;
+  long phase = 0;
+  void arrive() {
+    std::lock_guard<std::mutex> lk(mu);
+    if (++count == expected) {
+      count = 0;
+      ++phase;
+      cv.notify_all();
+    }
+  }
+  void sync() {
+    std::unique_lock<std::mutex> lk(mu);
+    const long ph = phase;
+    if (++count == expected) {
+      count = 0;
+      ++phase;
+      cv.notify_all();
+      return;
+    }
+    cv.wait(lk, [&] { return phase != ph; });
+  }
+};
+// the named barriers (indexed by id; 0 is __syncthreads') of the block the
+// calling thread runs in, when its threads run concurrently (else null)
+inline thread_local PdqHostBarrier* pdq_host_barriers = nullptr;
+inline void pdq_host_named_arrive(int id) { pdq_host_barriers[id].arrive(); }
+inline void pdq_host_named_sync(int id) { pdq_host_barriers[id].sync(); }
 
 #define __host__
 #define __device__
@@ -42,7 +81,9 @@ inline T __shfl_xor_sync(unsigned, T v, int, int = 32) {
 }
 inline void __syncwarp(unsigned = 0xffffffffu) {}
 inline bool __any_sync(unsigned, bool p) { return p; }  // one lane: its own predicate
-inline void __syncthreads() {}
+inline void __syncthreads() {
+  if (pdq_host_barriers) pdq_host_barriers[0].sync();
+}
 inline void __threadfence() {}
 inline double __longlong_as_double(long long v) {
   double d;

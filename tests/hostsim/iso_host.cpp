@@ -11,7 +11,9 @@
 // filter instantiation with error_state_std, with TS0 (3) or TS1 (4, the
 // Jacobian trace along d), mode 5 the terminal-value adjoint: the record
 // pass (the lean filter with REC) and then the adjoint pass
-// (iso_tv_bwd_kernel) for a cotangent of the terminal mean.
+// (iso_tv_bwd_kernel) for a cotangent of the terminal mean; mode 6 the
+// split filter (iso_split_kernel: a covariance warp and a mean warp per
+// instance, run as two host threads), exact landings only.
 //
 // Input file (whitespace-separated): precision (0 float32, 1 float64) mode nu
 // B S solver control clip_dt terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
@@ -24,9 +26,11 @@
 // followed by the gradients d <cotangent, u_mean> / d params [4] and / d y0 [2]).
 #include <cstdio>
 #include <cstdlib>
+#include <thread>
 #include <vector>
 
 #include "iso_solver.cuh"
+#include "iso_split.cuh"
 #include "tv_adjoint.cuh"
 
 thread_local pdq_host_uint3 threadIdx, blockIdx, blockDim;
@@ -124,10 +128,28 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
     a.rec_ckpt = ckpt;
   }
 
+  if constexpr (MODE == 6 && !INTERP) {
+    // the split kernel with one-lane warps: per instance a block of two
+    // threads (the covariance and the mean warp) with their own barriers
+    for (long long b = 0; b < B; ++b) {
+      PdqHostBarrier bars[3];
+      auto warp = [&](unsigned tid) {
+        blockDim = {2, 1, 1};
+        blockIdx = {uint32_t(b), 0, 0};
+        threadIdx = {tid, 0, 0};
+        pdq_host_barriers = bars;
+        iso_split_kernel<T, NU, F, 1>(a);
+        pdq_host_barriers = nullptr;
+      };
+      std::thread cov(warp, 0u), mean(warp, 1u);
+      cov.join();
+      mean.join();
+    }
+  }
   const int block = 64;
   blockDim = {uint32_t(block), 1, 1};
   const long long threads = MODE == 2 ? B * (P + D) : B;
-  const long long padded = (threads + block - 1) / block * block;  // the launch's grid
+  const long long padded = MODE == 6 ? 0 : (threads + block - 1) / block * block;  // the launch's grid
   for (long long g = 0; g < padded; ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
@@ -187,7 +209,8 @@ int main(int argc, char** argv) {
   if (B < 1 || S < 2) return 2;
   int rc = 2;
   const bool interp = !clip_dt;
-  const int args_ok = (mode >= 0 && mode <= 5) && (nu == 3 || nu == 4) && (mode != 5 || (clip_dt && terminal_only && S == 2));
+  const int args_ok = (mode >= 0 && mode <= 6) && (nu == 3 || nu == 4 || (nu == 5 && (mode == 0 || mode == 6))) &&
+                      (mode != 5 || (clip_dt && terminal_only && S == 2)) && (mode != 6 || clip_dt);
   if (!args_ok) return 2;
 #define PDQ_HOST_RUN(NU_, MODE_)                                                                        \
   rc = prec ? (interp ? run<double, NU_, true, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)    \
@@ -203,6 +226,10 @@ int main(int argc, char** argv) {
   if (nu == 4 && mode == 2) PDQ_HOST_RUN(4, 2);
   if (nu == 4 && mode == 5) PDQ_HOST_RUN(4, 5);
   if (nu == 3 && mode == 5) PDQ_HOST_RUN(3, 5);
+  if (nu == 4 && mode == 6) PDQ_HOST_RUN(4, 6);
+  if (nu == 5 && mode == 0) PDQ_HOST_RUN(5, 0);
+  if (nu == 5 && mode == 6) PDQ_HOST_RUN(5, 6);
+  if (nu == 3 && mode == 6) PDQ_HOST_RUN(3, 6);
 #undef PDQ_HOST_RUN
   fclose(in);
   return rc;

@@ -250,3 +250,33 @@ def test_host_headline_kernel_on_the_benchmark_distribution(harness, tmp_path, p
             assert abs(vals[2] - ref["output_scale"][b]) <= 1e-6 * abs(ref["output_scale"][b])
         else:
             assert err <= 1e-3 and abs(steps - rsteps) <= max(1, int(0.1 * rsteps)), (b, err, steps, rsteps)
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+@pytest.mark.parametrize("solver,terminal", [("mle", True), ("none", True), ("mle", False)])
+def test_host_split_kernel_equals_the_one_thread_kernel(harness, tmp_path, precision, solver, terminal):
+    """The split filter (iso_split_kernel: a covariance warp and a mean warp
+    per instance, here two host threads meeting at the named barriers) runs
+    the one-thread kernel's arithmetic, so its records are bit for bit the
+    lean instantiation's: 16 of the benchmark's Lotka--Volterra instances,
+    nu = 4, rtol = atol = 1e-6, exact landings, terminal values or 6 save
+    points, float64 and float32 bulk."""
+    import bench
+
+    params, y0 = (x.numpy() for x in bench.lv_inputs(16, seed=3))
+    nu, B = 4, 16
+    save_at = [0.0, 50.0] if terminal else [0.0, 1.0, 1.0 + 1e-3, 7.5, 20.0, 30.0]
+    codes = {"none": 0, "mle": 1}
+
+    def run(mode):
+        head = [precision, mode, nu, B, len(save_at), codes[solver], 0, 1, int(terminal)]
+        body = np.concatenate([[1e-6, 1e-6], np.tile(save_at, B), params.ravel(), y0.ravel(), np.full(B, 0.1),
+                               q1_iwp(nu).ravel()])
+        path = tmp_path / f"input{mode}.txt"
+        path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+        return hostsim.run_harness(harness, path)
+
+    one, split = run(0), run(6)
+    assert len(one) == B * (1 + (1 if terminal else len(save_at)))
+    assert split == one
+    assert all(line.split()[0] == "0" for line in one[::1 + (1 if terminal else len(save_at))])
