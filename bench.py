@@ -635,10 +635,12 @@ def vdp_dense_secondary(torch, _native, ensemble, device, mu_max=1000.0, cpu=Tru
     B, S = 4096, 100
     stream = torch.cuda.current_stream()
 
+    # sixteen lanes per instance: the batch time is the stiffest instances' attempts run back to
+    # back on an otherwise idle GPU, where the most lanes per attempt give the shortest chain
     def cfg_of(precision):
         return ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense", constraint="ts1",
                                     strategy="fixedpoint", solver="dynamic", precision=precision, atol=1e-5,
-                                    rtol=1e-5, clip_dt=False, max_attempts=1 << 24)
+                                    rtol=1e-5, clip_dt=False, max_attempts=1 << 24, kernel_variant=5)
 
     def inputs(mu_hi):
         mu, save_at, y0 = configs.vdp_dense(B, mu_hi)
@@ -679,7 +681,7 @@ def vdp_dense_secondary(torch, _native, ensemble, device, mu_max=1000.0, cpu=Tru
         "config": {"workload": "van_der_pol_dense", "instances": B, "mu": f"log-uniform [1, {mu_max}]",
                    "t_span": "[0, 2 mu]", "save_at": S, "num_derivatives": 3, "ssm": "dense", "constraint": "ts1",
                    "strategy": "fixedpoint", "solver": "dynamic", "rtol": 1e-5, "atol": 1e-5, "precision": "float32",
-                   "kernel": "structure-exploiting QRs, 4 lanes per instance", "steps": 1,
+                   "kernel": "structure-exploiting QRs, 16 lanes per instance", "steps": 1,
                    "warmup": "one solve with mu <= 2"},
         "value": B / t_kernel, "unit": "solves/s", "ms_per_step": 1e3 * t_kernel,
         "e2e": {"value": B / t_e2e, "unit": "solves/s",
@@ -692,8 +694,8 @@ def vdp_dense_secondary(torch, _native, ensemble, device, mu_max=1000.0, cpu=Tru
                      "flops_per_attempt": VDP_FLOPS_PER_ATTEMPT,
                      "peak_source": f"measured FP32 FMA probe on this GPU ({sms} SMs)",
                      "note": f"latency-bound: the batch time is the slowest instance's {attempts.max() / 1e6:.2f} M "
-                             "attempts, each a chain of dependent reflectors on four lanes; most SMs are idle for "
-                             "most of it"},
+                             "attempts, each a chain of dependent reflectors on sixteen lanes; most SMs are idle "
+                             "for most of it"},
         "gpu_launches": 1,
     }
     # float64 and float32 on mu <= 10 (the float64 batch to mu = 1000 does not fit the run's time)
@@ -1008,7 +1010,8 @@ def run_vdp_dense(args):
             cfg = ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense", constraint="ts1",
                                        strategy="fixedpoint", solver="dynamic", precision=prec, atol=1e-5, rtol=1e-5,
                                        clip_dt=False, max_attempts=1 << 24,
-                                       kernel_variant={"lanes": 2, "thread": 1}.get(args.variant, 3))
+                                       kernel_variant={"lanes": 2, "thread": 1, "struct": 3, "struct8": 4}.get(
+                                           args.variant, 5))
             outs = _native.alloc_outputs(cfg, B, 100, False, device, posterior=True)
             t = timed_region(torch, stream, lambda: _native.solve_adaptive(cfg, save_at, prm, y0, dt0, False, outs,
                                                                              stream=stream), args.steps, args.warmup)
@@ -1021,8 +1024,10 @@ def run_vdp_dense(args):
     cfg = {"workload": "van_der_pol_dense", "instances": B, "mu": f"log-uniform [1, {args.mu_max}]", "t_span": "[0, 2 mu]",
            "num_derivatives": 3, "ssm": "dense", "constraint": "ts1", "strategy": "fixedpoint", "solver": "dynamic",
            "save_at": 100, "rtol": 1e-5, "atol": 1e-5,
-           "mapping": {"lanes": "8 lanes per instance", "thread": "thread per instance"}.get(
-               args.variant, "structure-exploiting QRs, 4 lanes per instance")}
+           "mapping": {"lanes": "8 lanes per instance", "thread": "thread per instance",
+                       "struct": "structure-exploiting QRs, 4 lanes per instance",
+                       "struct8": "structure-exploiting QRs, 8 lanes per instance"}.get(
+               args.variant, "structure-exploiting QRs, 16 lanes per instance")}
     print(json.dumps(base_line("ensemble IVP solves/s", res[first]["solves_per_s"], "solves/s", args,
                                res[first]["ms_per_step"], True, first, cfg, by_precision=res, gpu_launches=args.steps,
                                clocks=clk.summary())))
@@ -1109,7 +1114,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lv_ensemble",
                     choices=["lv_ensemble", "lv_single", "fhn_lml", "vdp_dense", "burgers_blockdiag"])
-    ap.add_argument("--variant", default="auto", choices=["auto", "thread", "lanes", "lanes_compact", "split"],
+    ap.add_argument("--variant", default="auto", choices=["auto", "thread", "lanes", "lanes_compact", "split", "struct",
+                                                              "struct8", "struct16"],
                     help="lv_ensemble: instance-to-lane mapping (auto = time the autotuner's candidates and keep "
                          "the fastest)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

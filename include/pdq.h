@@ -117,9 +117,10 @@ typedef struct pdq_config {
                               2 / 3 eight lanes per instance with <= 128 / <= 85 registers (clip_dt only),
                               4 a covariance warp and a mean warp per 32 instances (the filter with
                               TS0, no damping, error_residual_std, clip_dt, solver none or mle);
-                              dense: 0 auto (3, or 1 for error_state_std and run-time fields),
+                              dense: 0 auto (4, or 1 for error_state_std and run-time fields),
                               1 one thread per instance, 2 eight lanes per instance,
-                              3 structure-exploiting QRs on four lanes per instance */
+                              3 / 4 / 5 structure-exploiting QRs on four / eight / sixteen lanes
+                              per instance */
   double safety, factor_min, factor_max;           /* controller (defaults 0.95, 0.2, 10) */
   double exponent_integral, exponent_proportional; /* PI controller (0.3, 0.4) */
   double atol, rtol, eps, damp;                    /* solve(...) arguments */

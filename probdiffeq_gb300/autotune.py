@@ -25,7 +25,7 @@ _ISO_THREAD = [(1, 64), (1, 32)]
 _ISO_LANES = [(2, 32), (2, 16), (3, 32)]
 _ISO_SPLIT = [(4, 0)]
 _DENSE_THREAD = [(1, 32), (1, 16)]
-_DENSE_LANES = [(3, 0), (2, 4), (2, 2)]
+_DENSE_LANES = [(3, 0), (4, 0), (5, 0), (2, 4), (2, 2)]
 
 _cache = {}
 _lock = threading.Lock()

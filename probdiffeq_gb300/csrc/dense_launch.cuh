@@ -29,13 +29,15 @@ cudaError_t launch_dense_coop(const DenseArgs& a, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-// Structure-exploiting kernel: four lanes per instance, eight instances per
-// warp-sized block, their states in dynamic shared memory.
+// Structure-exploiting kernel: L lanes per instance (four; eight or sixteen
+// in their own translation units), 32 / L instances per warp-sized block,
+// their states in dynamic shared memory.
 constexpr int kDenseStructLanes = 4;
 
-template <typename T, int NU, class F, bool TS1, bool FP>
+template <typename T, int NU, class F, bool TS1, bool FP, int L = kDenseStructLanes>
 cudaError_t launch_dense_struct(const DenseArgs& a, cudaStream_t stream) {
-  constexpr int L = kDenseStructLanes, IPW = 32 / L;
+  static_assert(L == 4 || L == 8 || L == 16, "lane groups of four, eight or sixteen");
+  constexpr int IPW = 32 / L;
   const size_t smem = dense_struct_smem_bytes<NU, F::D>(sizeof(T), L);
   static bool attr_set = false;
   cudaError_t e = ensure_stack<dense_struct_kernel<T, NU, F, TS1, FP, L>>();
@@ -82,6 +84,25 @@ cudaError_t launch_dense_precision(const DenseArgs& a, int nu, bool ts1, bool fp
   }
 }
 
+// The structure-exploiting kernel with L lanes per instance, dispatched over
+// (nu, TS0/TS1, filter/fixed-point).
+template <typename T, class F, int L>
+cudaError_t launch_dense_struct_precision(const DenseArgs& a, int nu, bool ts1, bool fp, cudaStream_t stream) {
+  switch (nu) {
+    case 2:
+      return ts1 ? (fp ? launch_dense_struct<T, 2, F, true, true, L>(a, stream)
+                       : launch_dense_struct<T, 2, F, true, false, L>(a, stream))
+                 : (fp ? launch_dense_struct<T, 2, F, false, true, L>(a, stream)
+                       : launch_dense_struct<T, 2, F, false, false, L>(a, stream));
+    case 3:
+      return ts1 ? (fp ? launch_dense_struct<T, 3, F, true, true, L>(a, stream)
+                       : launch_dense_struct<T, 3, F, true, false, L>(a, stream))
+                 : (fp ? launch_dense_struct<T, 3, F, false, true, L>(a, stream)
+                       : launch_dense_struct<T, 3, F, false, false, L>(a, stream));
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 }  // namespace pdq
 
 #define PDQ_DECLARE_DENSE_LAUNCH(NAME) \
@@ -97,4 +118,22 @@ PDQ_DECLARE_DENSE_LAUNCH(pdq_launch_dense_fhn_f64)
 #define PDQ_DEFINE_DENSE_LAUNCH(NAME, T, F)                                                                 \
   cudaError_t NAME(const pdq::DenseArgs& a, int nu, bool ts1, bool fp, cudaStream_t stream, int block) { \
     return pdq::launch_dense_precision<T, F>(a, nu, ts1, fp, stream, block);                              \
+  }
+
+// the structure-exploiting kernel with eight or sixteen lanes per instance
+#define PDQ_DECLARE_DENSE_LANES_LAUNCH(NAME) \
+  cudaError_t NAME(const pdq::DenseArgs& a, int nu, bool ts1, bool fp, int lanes, cudaStream_t stream);
+
+PDQ_DECLARE_DENSE_LANES_LAUNCH(pdq_launch_dense_lanes_lv_f32)
+PDQ_DECLARE_DENSE_LANES_LAUNCH(pdq_launch_dense_lanes_lv_f64)
+PDQ_DECLARE_DENSE_LANES_LAUNCH(pdq_launch_dense_lanes_vdp_f32)
+PDQ_DECLARE_DENSE_LANES_LAUNCH(pdq_launch_dense_lanes_vdp_f64)
+PDQ_DECLARE_DENSE_LANES_LAUNCH(pdq_launch_dense_lanes_fhn_f32)
+PDQ_DECLARE_DENSE_LANES_LAUNCH(pdq_launch_dense_lanes_fhn_f64)
+
+#define PDQ_DEFINE_DENSE_LANES_LAUNCH(NAME, T, F)                                                         \
+  cudaError_t NAME(const pdq::DenseArgs& a, int nu, bool ts1, bool fp, int lanes, cudaStream_t stream) { \
+    if (lanes == 8) return pdq::launch_dense_struct_precision<T, F, 8>(a, nu, ts1, fp, stream);           \
+    if (lanes == 16) return pdq::launch_dense_struct_precision<T, F, 16>(a, nu, ts1, fp, stream);         \
+    return cudaErrorInvalidValue;                                                                          \
   }

@@ -1226,10 +1226,15 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
   int s = 1;
   W t_next = wide_from(save_at[1], T(0));
   bool safe_next = false;  // the next attempt takes the range-checked predict and update
+  // before(t, t_next) and t_next - t, carried across iterations: an attempt
+  // forms them for its candidate time alongside its arithmetic, so an
+  // accepted step does not recompute them at the head of the next one
+  bool bef = before(t, t_next);
+  T rem = wide_diff(t_next, t);
   while (s < S) {
-    if (before(t, t_next)) {
+    if (bef) {
       // ---- one attempt of the rejection loop (solvers_via_adaptive_steps.py:249-328) ----
-      const T remaining = wide_diff(t_next, t);
+      const T remaining = rem;
       const bool clipped = a.clip_dt && !(dt < remaining);
       const T dt_use = clipped ? remaining : dt;
       if (!(dev_abs(dt_use) > T(1e-14) * fmax(T(1), dev_abs(T(wide_hi(t)))))) {
@@ -1242,6 +1247,17 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
       }
       ++attempts;
       const T h = dt_use;
+      // the time after this attempt if it is accepted: a step clipped to the
+      // checkpoint lands on it exactly in float pairs; float64 adds as the
+      // reference does
+      W t_acc;
+      if constexpr (kNarrow) {
+        t_acc = clipped ? t_next : wide_add(t, dt_use);
+      } else {
+        t_acc = t + dt_use;
+      }
+      const bool bef_acc = before(t_acc, t_next);
+      const T rem_acc = wide_diff(t_next, t_acc);
       // The attempt's arithmetic, a generic lambda instantiated twice: with
       // the branch-free predict and update (SAFE false), and with the
       // range-checked ones (SAFE true), which rerun an attempt whose sums of
@@ -1445,13 +1461,9 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           iso_cond_merge(bw, cnew, merged);
           bw = merged;
         }
-        // a step clipped to the checkpoint lands on it exactly in float
-        // pairs; float64 adds as the reference does
-        if constexpr (kNarrow) {
-          t = clipped ? t_next : wide_add(t, dt_use);
-        } else {
-          t = t + dt_use;
-        }
+        t = t_acc;
+        bef = bef_acc;
+        rem = rem_acc;
         ++num_steps;
 #pragma unroll
         for (int i = 0; i < n; ++i) {
@@ -1477,7 +1489,7 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
     // ---- checkpoint branch (solvers_via_adaptive_steps.py:242-247) ----
     const int s_out = a.terminal_only ? 0 : s;
     const bool record = (!a.terminal_only) || (s == S - 1);
-    if (before(t, t_next)) {
+    if (bef) {
       // interp_skip: keep stepping towards the checkpoint
     } else if (INTERP && before(t_next, t)) {
       if constexpr (INTERP) {
@@ -1580,9 +1592,13 @@ __global__ void __launch_bounds__(64) iso_adaptive_kernel(IsoArgs a) {
           for (int j = 0; j < D; ++j) milo[i][j] = mlo[i][j];
       }
     }
-    if (!before(t, t_next)) {  // checkpoint s done
+    if (!bef) {  // checkpoint s done
       ++s;
-      if (s < S) t_next = wide_from(save_at[s], T(0));
+      if (s < S) {
+        t_next = wide_from(save_at[s], T(0));
+        bef = before(t, t_next);
+        rem = wide_diff(t_next, t);
+      }
     }
   }
 

@@ -437,19 +437,19 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     return err == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
   }
   if (c->ssm == PDQ_SSM_DENSE) {
-    // kernel_variant 1: one thread per instance; 2: eight lanes per instance; 3: the structure-exploiting
-    // kernel (four lanes per instance); 0: 3 unless error_state_std or a run-time field asks for 1
-    // (error_state_std: the thread-per-instance mapping only)
+    // kernel_variant 1: one thread per instance; 2: eight lanes per instance; 3 / 4 / 5: the
+    // structure-exploiting kernel with four / eight / sixteen lanes per instance; 0: 4 unless
+    // error_state_std or a run-time field asks for 1 (error_state_std: the thread-per-instance mapping only)
     const bool state_std = c->error == PDQ_ERROR_STATE_STD;
     const bool user_field = c->field >= PDQ_FIELD_USER_BASE;
-    if (state_std && (c->kernel_variant == 2 || c->kernel_variant == 3)) return PDQ_ERROR_UNSUPPORTED;
-    if (user_field && (c->kernel_variant == 2 || c->kernel_variant == 3)) return PDQ_ERROR_UNSUPPORTED;
-    const int variant = c->kernel_variant != 0 ? c->kernel_variant : ((state_std || user_field) ? 1 : 3);
+    if (c->kernel_variant < 0 || c->kernel_variant > 5) return PDQ_ERROR_INVALID_VALUE;
+    if ((state_std || user_field) && c->kernel_variant >= 2) return PDQ_ERROR_UNSUPPORTED;
+    const int variant = c->kernel_variant != 0 ? c->kernel_variant : ((state_std || user_field) ? 1 : 4);
     if (args->u_mean_d_params || args->u_mean_d_y0) return PDQ_ERROR_UNSUPPORTED;
     {
       const int ipb = c->instances_per_block;
       const bool ok = variant == 2 ? (ipb >= 0 && ipb <= 4)
-                                   : (variant == 3 ? ipb == 0 : (ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32));
+                                   : (variant >= 3 ? ipb == 0 : (ipb == 0 || ipb == 8 || ipb == 16 || ipb == 32));
       if (!ok) return PDQ_ERROR_INVALID_VALUE;
     }
     if (c->num_derivatives < 2 || c->num_derivatives > 3) return PDQ_ERROR_UNSUPPORTED;
@@ -514,6 +514,24 @@ pdq_status pdq_solve_adaptive(const pdq_config* c, const pdq_adaptive_args* args
     if (user_field) {  // run-time fields: one thread per instance
       err = pdq_launch_dense_user(a, c->field, f64, c->num_derivatives, ts1, fp, stream);
       return err == cudaSuccess ? PDQ_SUCCESS : (err == cudaErrorInvalidSource ? PDQ_ERROR_COMPILE : PDQ_ERROR_CUDA);
+    }
+    if (variant >= 4) {  // eight / sixteen lanes per instance (own translation units)
+      using DenseLanes = cudaError_t (*)(const pdq::DenseArgs&, int, bool, bool, int, cudaStream_t);
+      DenseLanes launch = nullptr;
+      switch (c->field) {
+        case PDQ_FIELD_LOTKA_VOLTERRA:
+          launch = f64 ? pdq_launch_dense_lanes_lv_f64 : pdq_launch_dense_lanes_lv_f32;
+          break;
+        case PDQ_FIELD_VAN_DER_POL:
+          launch = f64 ? pdq_launch_dense_lanes_vdp_f64 : pdq_launch_dense_lanes_vdp_f32;
+          break;
+        case PDQ_FIELD_FITZHUGH_NAGUMO:
+          launch = f64 ? pdq_launch_dense_lanes_fhn_f64 : pdq_launch_dense_lanes_fhn_f32;
+          break;
+        default: return PDQ_ERROR_UNSUPPORTED;
+      }
+      const int lanes = variant == 4 ? 8 : 16;
+      return launch(a, c->num_derivatives, ts1, fp, lanes, stream) == cudaSuccess ? PDQ_SUCCESS : PDQ_ERROR_CUDA;
     }
     switch (c->field) {
       case PDQ_FIELD_LOTKA_VOLTERRA:

@@ -34,7 +34,7 @@ def test_candidates_follow_the_abi_rules():
     bd = ensemble.make_config(field="burgers", num_derivatives=3, ode_dim=64, ssm="blockdiag")
     assert autotune.candidates(bd) == [(0, 0)]
     for v, ipb in autotune.candidates(iso) + autotune.candidates(dense):
-        assert ipb in (2, 4, 8, 16, 32, 64) or (v, ipb) in ((3, 0), (4, 0))
+        assert ipb in (2, 4, 8, 16, 32, 64) or (v, ipb) in ((3, 0), (4, 0), (5, 0))
 
 
 def test_cache_key_ignores_the_mapping_and_buckets_batch_sizes():

@@ -99,10 +99,10 @@ def f32_tol(o64, o32):
 TOL64 = dict(u=1e-8, rows=1e-5, cov=1e-5)
 
 
-VARIANTS = {"thread": 1, "lanes": 2, "struct": 3}
+VARIANTS = {"thread": 1, "lanes": 2, "struct": 3, "struct8": 4, "struct16": 5}
 
 
-@pytest.mark.parametrize("variant", ["thread", "lanes", "struct"])
+@pytest.mark.parametrize("variant", ["thread", "lanes", "struct", "struct8", "struct16"])
 @pytest.mark.parametrize("precision", ["float64", "float32"])
 @pytest.mark.parametrize("mu", [1.0, 3.0])
 def test_vdp_fixedpoint_ts1_save_at(mu, precision, variant):
@@ -134,7 +134,7 @@ def test_vdp_fixedpoint_ts1_save_at(mu, precision, variant):
             assert rel(out["filter_mean"][0, s], f.mean) < 1e-6
 
 
-@pytest.mark.parametrize("variant", ["thread", "lanes", "struct"])
+@pytest.mark.parametrize("variant", ["thread", "lanes", "struct", "struct8", "struct16"])
 def test_vdp_filter_ts0_and_mle(variant):
     """Dense TS0 with the filter and MLE calibration, float64."""
     save_at = np.linspace(0.0, 2.0, 5)
@@ -164,7 +164,7 @@ def test_vdp_error_state_std(solver, strategy):
     # the lane mappings do not implement it
     from probdiffeq_gb300 import _native
 
-    for variant in (2, 3):
+    for variant in (2, 3, 4, 5):
         with pytest.raises(_native.NativeError):
             gpu_dense("van_der_pol", [[mu]], [[2.0, 0.0]], save_at, "float64", error="state_std", variant=variant)
 
@@ -190,7 +190,7 @@ def test_dense_equals_isotropic_on_lotka_volterra():
     assert rel(Ld @ Ld.T, Ci) < 1e-7
 
 
-@pytest.mark.parametrize("variant", ["thread", "lanes", "struct"])
+@pytest.mark.parametrize("variant", ["thread", "lanes", "struct", "struct8", "struct16"])
 def test_dense_batch_and_workspace_errors(variant):
     """Several instances in one launch (five: a partly filled block for the
     lane mappings); too small a workspace is rejected before launch."""
