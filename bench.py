@@ -808,6 +808,10 @@ def run_lv_ensemble(args):
         t_dev64 = timed_region(torch, stream, lambda: device_step(cfg64), k64, 1, flush, world, dist)
         mean64 = outs["u_mean"][:, 0].clone()
         attempts64 = outs["num_attempts"].to(torch.float64).sum().item()
+        # the plain float64 kernel (one thread per instance), when the autotuner chose another mapping
+        cfg64_thread = config("float64", 1, 0)
+        t_dev64_thread = (t_dev64 if best64[0] == 1 else
+                          timed_region(torch, stream, lambda: device_step(cfg64_thread), k64, 1, flush, world, dist))
         # terminal u: float32 vs float64 relative to each instance's largest component
         rel = ((mean32[:, 0] - mean64[:, 0]).abs().amax(dim=1) / mean64[:, 0].abs().amax(dim=1)).cpu()
         rel_f32_f64 = {"median": rel.median().item(), "max": rel.max().item()}
@@ -912,6 +916,9 @@ def run_lv_ensemble(args):
             "ms_per_step": 1e3 * t_dev64 / k64,
             "attempts_per_step": attempts64,
             "fp32_speedup": value / (world * B * k64 / t_dev64),
+            "mapping": label(best64),
+            "thread_per_instance": {"ms_per_step": 1e3 * t_dev64_thread / k64,
+                                    "fp32_speedup": value / (world * B * k64 / t_dev64_thread)},
             "rel_terminal_diff_f32_vs_f64": rel_f32_f64,
         },
         "stats": {

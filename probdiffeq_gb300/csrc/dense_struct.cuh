@@ -154,7 +154,7 @@ PDQ_D void dstruct_qr_stacked(Soa<T, IPW> S, const LaneGroup<L>& g, int WM) {
     g.sync();  // every lane has read column c
     T beta, tau;
     if (dstruct_reflector(x, beta, tau)) {
-#pragma unroll 2
+#pragma unroll(L >= 8 ? 1 : 2)
       for (int j = g.first(c + 1); j < N; j += L) {
         T w0 = S[WM + c * LDM + j], w1 = T(0);
 #pragma unroll
@@ -253,7 +253,7 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
     g.sync();
     T beta, tau;
     if (dstruct_reflector(x, beta, tau)) {
-#pragma unroll 2
+#pragma unroll(L >= 8 ? 1 : 2)
       for (int j = g.first(c + 1); j < C; j += L) {
         T w0 = S[W + c * WS + j], w1 = T(0);
 #pragma unroll
@@ -280,7 +280,7 @@ PDQ_D void dstruct_predict(Soa<T, IPW> S, const LaneGroup<L>& g, const double (&
       g.sync();
       T beta, tau;
       if (dstruct_reflector(x, beta, tau)) {
-#pragma unroll 2
+#pragma unroll(L >= 8 ? 1 : 2)
         for (int j = g.first(c + 1); j < 2 * N; j += L) {
           T w0 = S[W + c * WS + j], w1 = T(0);
 #pragma unroll

@@ -1,6 +1,7 @@
 // Template dispatch of the isotropic kernel over (precision, nu, interpolation).
 #pragma once
 
+#include "iso_lean.cuh"
 #include "iso_solver.cuh"
 #include "iso_warp.cuh"
 
@@ -49,14 +50,27 @@ cudaError_t launch_iso_tangents(const IsoArgs& a, cudaStream_t stream, int block
   return cudaGetLastError();
 }
 
+// The branch-light lean kernel (iso_lean.cuh): the filter with undamped TS0,
+// error_residual_std and exact landings.
+template <typename T, int NU, class F>
+cudaError_t launch_iso_lean(const IsoArgs& a, cudaStream_t stream, int block) {
+  cudaError_t e = ensure_stack<iso_lean_kernel<T, NU, F>>();
+  if (e != cudaSuccess) return e;
+  const unsigned grid = unsigned((a.B + block - 1) / block);
+  iso_lean_kernel<T, NU, F><<<grid, block, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
 // The fixed-point smoother, TS1, error_state_std and a damped update take
 // the general instantiation; the filter with undamped TS0 and
-// error_residual_std the lean one (whose update is the single-QR array form).
+// error_residual_std the lean one (whose update is the single-QR array form),
+// with exact landings the branch-light kernel.
 template <typename T, int NU, class F, bool FP>
 cudaError_t launch_iso_nu(const IsoArgs& a, bool interp, cudaStream_t stream, int block) {
   if constexpr (!FP) {
     if (a.tangents) return interp ? launch_iso_tangents<T, NU, F, true>(a, stream, block)
                                   : launch_iso_tangents<T, NU, F, false>(a, stream, block);
+    if (!interp && !a.ts1 && !a.state_error && a.damp == 0.0) return launch_iso_lean<T, NU, F>(a, stream, block);
   }
   if (FP || a.ts1 || a.state_error || a.damp != 0.0)
     return interp ? launch_iso_kernel<T, NU, F, true, FP, true>(a, stream, block)

@@ -13,7 +13,8 @@
 // pass (the lean filter with REC) and then the adjoint pass
 // (iso_tv_bwd_kernel) for a cotangent of the terminal mean; mode 6 the
 // split filter (iso_split_kernel: a covariance warp and a mean warp per
-// instance, run as two host threads), exact landings only.
+// instance, run as two host threads), mode 7 the branch-light lean filter
+// (iso_lean_kernel); modes 6 and 7 with exact landings only.
 //
 // Input file (whitespace-separated): precision (0 float32, 1 float64) mode nu
 // B S solver control clip_dt terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
@@ -29,6 +30,7 @@
 #include <thread>
 #include <vector>
 
+#include "iso_lean.cuh"
 #include "iso_solver.cuh"
 #include "iso_split.cuh"
 #include "tv_adjoint.cuh"
@@ -158,6 +160,7 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
     if constexpr (MODE == 2) iso_adaptive_kernel<T, NU, F, INTERP, false, false, true>(a);
     if constexpr (MODE == 3 || MODE == 4) iso_adaptive_kernel<T, NU, F, INTERP, false, true>(a);
     if constexpr (MODE == 5 && !INTERP) iso_adaptive_kernel<T, NU, F, false, false, false, false, true>(a);
+    if constexpr (MODE == 7 && !INTERP) iso_lean_kernel<T, NU, F>(a);
   }
   if constexpr (MODE == 5) {
     TvAdjArgs ta;
@@ -209,8 +212,8 @@ int main(int argc, char** argv) {
   if (B < 1 || S < 2) return 2;
   int rc = 2;
   const bool interp = !clip_dt;
-  const int args_ok = (mode >= 0 && mode <= 6) && (nu == 3 || nu == 4 || (nu == 5 && (mode == 0 || mode == 6))) &&
-                      (mode != 5 || (clip_dt && terminal_only && S == 2)) && (mode != 6 || clip_dt);
+  const int args_ok = (mode >= 0 && mode <= 7) && (nu == 3 || nu == 4 || (nu == 5 && (mode == 0 || mode >= 6))) &&
+                      (mode != 5 || (clip_dt && terminal_only && S == 2)) && (mode < 6 || clip_dt);
   if (!args_ok) return 2;
 #define PDQ_HOST_RUN(NU_, MODE_)                                                                        \
   rc = prec ? (interp ? run<double, NU_, true, MODE_>(in, B, S, solver, control, clip_dt, terminal_only)    \
@@ -229,6 +232,9 @@ int main(int argc, char** argv) {
   if (nu == 4 && mode == 6) PDQ_HOST_RUN(4, 6);
   if (nu == 5 && mode == 0) PDQ_HOST_RUN(5, 0);
   if (nu == 5 && mode == 6) PDQ_HOST_RUN(5, 6);
+  if (nu == 4 && mode == 7) PDQ_HOST_RUN(4, 7);
+  if (nu == 3 && mode == 7) PDQ_HOST_RUN(3, 7);
+  if (nu == 5 && mode == 7) PDQ_HOST_RUN(5, 7);
   if (nu == 3 && mode == 6) PDQ_HOST_RUN(3, 6);
 #undef PDQ_HOST_RUN
   fclose(in);

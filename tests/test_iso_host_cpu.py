@@ -254,13 +254,14 @@ def test_host_headline_kernel_on_the_benchmark_distribution(harness, tmp_path, p
 
 @pytest.mark.parametrize("precision", [1, 0])
 @pytest.mark.parametrize("solver,terminal", [("mle", True), ("none", True), ("mle", False)])
-def test_host_split_kernel_equals_the_one_thread_kernel(harness, tmp_path, precision, solver, terminal):
-    """The split filter (iso_split_kernel: a covariance warp and a mean warp
-    per instance, here two host threads meeting at the named barriers) runs
-    the one-thread kernel's arithmetic, so its records are bit for bit the
-    lean instantiation's: 16 of the benchmark's Lotka--Volterra instances,
-    nu = 4, rtol = atol = 1e-6, exact landings, terminal values or 6 save
-    points, float64 and float32 bulk."""
+def test_host_lean_and_split_kernels_equal_the_one_thread_kernel(harness, tmp_path, precision, solver, terminal):
+    """The branch-light lean kernel (iso_lean_kernel) and the split filter
+    (iso_split_kernel: a covariance warp and a mean warp per instance, here
+    two host threads meeting at the named barriers) run the arithmetic of
+    iso_adaptive_kernel's lean instantiation, so their records are its own bit
+    for bit: 16 of the benchmark's Lotka--Volterra instances, nu = 4,
+    rtol = atol = 1e-6, exact landings, terminal values or 6 save points,
+    float64 and float32 bulk."""
     import bench
 
     params, y0 = (x.numpy() for x in bench.lv_inputs(16, seed=3))
@@ -276,7 +277,8 @@ def test_host_split_kernel_equals_the_one_thread_kernel(harness, tmp_path, preci
         path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
         return hostsim.run_harness(harness, path)
 
-    one, split = run(0), run(6)
+    one, split, lean = run(0), run(6), run(7)
     assert len(one) == B * (1 + (1 if terminal else len(save_at)))
     assert split == one
+    assert lean == one
     assert all(line.split()[0] == "0" for line in one[::1 + (1 if terminal else len(save_at))])
