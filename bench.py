@@ -66,7 +66,7 @@ WORKLOAD = {
     "output": "terminal values (clip_dt)",
     "l2": "flushed between timed steps (256 MiB write)",
 }
-PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "iso_adaptive_kernel_lv16384.md")
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "iso_lean_kernel_lv16384.md")
 
 
 def lv_inputs(B, seed):
