@@ -388,11 +388,11 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       // error_state_std: the conditioned unit-scale std of u is the same for
       // every dimension (one H, one unit-scale factor), so it is formed once
       const T std0 = a.state_error ? state_std0<T, NU, OUT>(a, p, h, damp, h0) : T(0);
-      const T* x = bufs[cur];
-      T* y = bufs[cur ^ 1];
+      const T* __restrict__ x = bufs[cur];  // the two state buffers never alias
+      T* __restrict__ y = bufs[cur ^ 1];
 
       // ---- phase 1: extrapolated means staged in shared memory ----
-#pragma unroll 1
+#pragma unroll(FP ? 1 : 2)
       for (int jl = tid; jl < dl; jl += kBdThreads) {
         const int g = j0 + jl;
         T m[n];
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
       T pinv_abs[n];
 #pragma unroll
       for (int i = 0; i < n; ++i) pinv_abs[i] = dev_abs(pinv[i]);
-#pragma unroll 1
+#pragma unroll(FP ? 1 : 2)
       for (int jl = tid; jl < dl; jl += kBdThreads) {
         const int g = j0 + jl;
         const T left = jl > 0 ? mps[jl - 1] : ex_left[dl - 1];
