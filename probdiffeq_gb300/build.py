@@ -39,6 +39,7 @@ EMBEDDED_HEADERS = [
     ("pdq.h", os.path.join(INCLUDE, "pdq.h")),
     ("pdq_device.cuh", os.path.join(CSRC, "pdq_device.cuh")),
     ("iso_solver.cuh", os.path.join(CSRC, "iso_solver.cuh")),
+    ("iso_lean.cuh", os.path.join(CSRC, "iso_lean.cuh")),
     ("dense_solver.cuh", os.path.join(CSRC, "dense_solver.cuh")),
     ("lml_solver.cuh", os.path.join(CSRC, "lml_solver.cuh")),
     ("lml_adjoint.cuh", os.path.join(CSRC, "lml_adjoint.cuh")),

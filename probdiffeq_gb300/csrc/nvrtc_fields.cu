@@ -64,8 +64,13 @@ UserField* lookup(int32_t field) {
 
 const char* tf(bool b) { return b ? "true" : "false"; }
 
-// gen: the instantiation with TS1 / error_state_std / damping (as the built-in fields' dispatch)
+// gen: the instantiation with TS1 / error_state_std / damping; the filter
+// without them and with exact landings takes the branch-light lean kernel
+// (as the built-in fields' dispatch)
 std::string kernel_expression(bool f64, int nu, bool interp, bool fp, bool gen) {
+  if (!interp && !fp && !gen)
+    return std::string("pdq::iso_lean_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
+           ", pdq_user::Field>";
   return std::string("pdq::iso_adaptive_kernel<") + (f64 ? "double" : "float") + ", " + std::to_string(nu) +
          ", pdq_user::Field, " + tf(interp) + ", " + tf(fp) + ", " + tf(gen) + ">";
 }
@@ -157,7 +162,8 @@ extern "C" pdq_status pdq_register_field(const char* name, const char* source, i
   // validate by compiling one variant (no device needed)
   std::string cubin, text;
   std::vector<std::string> lowered;
-  const pdq_status st = compile(source, {kernel_expression(false, 2, false, false, false)}, &cubin, &lowered, &text);
+  const pdq_status st =
+      compile(source, {kernel_expression(false, 2, false, false, false)}, &cubin, &lowered, &text, "iso_lean.cuh");
   copy_log(text, log, log_bytes);
   if (st != PDQ_SUCCESS) return st;
   auto f = std::make_unique<UserField>();
@@ -294,7 +300,7 @@ cudaError_t pdq_launch_iso_user(const pdq::IsoArgs& a, int32_t field, bool f64, 
   // (the lean instantiation's single-QR update needs TS0 without damping)
   const bool gen = fp || a.ts1 || a.state_error || a.damp != 0.0;
   cudaKernel_t kernel = nullptr;
-  cudaError_t e = user_kernel(f, kernel_expression(f64, nu, interp, fp, gen), "iso_solver.cuh", &kernel);
+  cudaError_t e = user_kernel(f, kernel_expression(f64, nu, interp, fp, gen), "iso_lean.cuh", &kernel);
   if (e != cudaSuccess) return e;
   pdq::IsoArgs args = a;
   void* params[] = {&args};
