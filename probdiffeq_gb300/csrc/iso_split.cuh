@@ -39,7 +39,7 @@ namespace pdq {
 constexpr int kSplitBarX = 1;
 constexpr int kSplitBarY = 2;
 
-// flags of an attempt round, per instance
+// flags of one exchange between the warps, per instance
 constexpr int kSplitAttempt = 1;   // attempt with step size h
 constexpr int kSplitSafe = 2;      // with the range-checked predict and update
 constexpr int kSplitCommit = 4;    // the previous attempt was accepted: L = candidate
@@ -49,7 +49,7 @@ struct SplitShared {
   T h[W];
   int flags[W];
   int rec_lo[W], rec_cnt[W];  // records [rec_lo, rec_lo + rec_cnt) take the (committed) L
-  int go;                     // some instance attempts in this round
+  int go;                     // some instance attempts in this exchange
   T gain[NU + 1][W];
   T ry[W];
   int ok[W];
