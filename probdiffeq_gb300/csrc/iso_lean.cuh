@@ -215,6 +215,9 @@ __global__ void __launch_bounds__(64) iso_lean_kernel(IsoArgs a) {
     mle_sumsq = (commit && mle) ? sumsq_new : mle_sumsq;
     num_data += (commit && mle) ? 1 : 0;
     sigma_sf = commit ? (dynamic ? sigma_loc : T(1)) : sigma_sf;
+    // Termination: every iteration either counts an attempt (bounded by
+    // max_attempts, checked above) or, after a fast attempt that left the
+    // safe range, reruns it with the range-checked path, which always counts.
     if (!valid) {
       if (stop) {
         status = underflow ? PDQ_INSTANCE_DT_UNDERFLOW : PDQ_INSTANCE_MAX_STEPS;
