@@ -13,6 +13,26 @@ from . import _native
 DEFAULT_MAX_ATTEMPTS = 1 << 20
 
 
+# Instance-to-thread mappings by name (include/pdq.h kernel_variant): the
+# isotropic kernels (one thread, eight lanes with two register budgets, a
+# covariance warp and a mean warp per 32 instances) and the dense ones (one
+# thread, eight cooperative lanes, the structure-exploiting kernel on four,
+# eight or sixteen lanes).
+_VARIANTS = {
+    "isotropic": {"auto": 0, "thread": 1, "lanes": 2, "lanes_compact": 3, "split": 4},
+    "dense": {"auto": 0, "thread": 1, "lanes": 2, "struct": 3, "struct8": 4, "struct16": 5},
+}
+
+
+def _kernel_variant(ssm, kernel_variant):
+    if isinstance(kernel_variant, str):
+        names = _VARIANTS.get(ssm, {"auto": 0})
+        if kernel_variant not in names:
+            raise ValueError(f"kernel_variant {kernel_variant!r} for ssm {ssm!r}: one of {sorted(names)}")
+        return names[kernel_variant]
+    return int(kernel_variant)
+
+
 def make_config(
     *,
     field,
@@ -54,7 +74,7 @@ def make_config(
     cfg.safety, cfg.factor_min, cfg.factor_max = float(safety), float(factor_min), float(factor_max)
     cfg.exponent_integral, cfg.exponent_proportional = float(exponent_integral), float(exponent_proportional)
     cfg.max_attempts = int(max_attempts)
-    cfg.kernel_variant = {"auto": 0, "thread": 1, "lanes": 2, "lanes_compact": 3, "split": 4}.get(kernel_variant, kernel_variant)
+    cfg.kernel_variant = _kernel_variant(ssm, kernel_variant)
     cfg.instances_per_block = int(instances_per_block)
     return cfg
 

@@ -46,3 +46,21 @@ def test_cache_key_ignores_the_mapping_and_buckets_batch_sizes():
     c = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2, precision="float64")
     assert autotune.cache_key(a, 100, 2, True, "cpu") != autotune.cache_key(c, 100, 2, True, "cpu")
     assert autotune.cache_key(a, 100, 2, True, "cpu") != autotune.cache_key(a, 100, 3, True, "cpu")
+
+
+def test_kernel_variant_names_follow_the_state_space_model():
+    """Names of the mappings (include/pdq.h kernel_variant) per factorisation:
+    "split" is the isotropic covariance / mean warp pair, "struct8" the dense
+    structure-exploiting kernel on eight lanes; a name of the other
+    factorisation is rejected before any call."""
+    iso = ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2, kernel_variant="split")
+    assert iso.kernel_variant == 4
+    dense = ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense",
+                                 kernel_variant="struct16")
+    assert dense.kernel_variant == 5
+    assert ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense",
+                                kernel_variant=4).kernel_variant == 4
+    with pytest.raises(ValueError):
+        ensemble.make_config(field="van_der_pol", num_derivatives=3, ode_dim=2, ssm="dense", kernel_variant="split")
+    with pytest.raises(ValueError):
+        ensemble.make_config(field="lotka_volterra", num_derivatives=4, ode_dim=2, kernel_variant="struct8")
