@@ -50,6 +50,39 @@ inline thread_local PdqHostBarrier* pdq_host_barriers = nullptr;
 inline void pdq_host_named_arrive(int id) { pdq_host_barriers[id].arrive(); }
 inline void pdq_host_named_sync(int id) { pdq_host_barriers[id].sync(); }
 
+// A warp whose 32 lanes run as host threads: __syncwarp(mask) waits for the
+// lanes of mask, __any_sync(mask, p) also ORs their predicates.  One barrier
+// per mask value; the lanes of a mask meet its barriers in the same order.
+struct PdqHostWarp {
+  struct Bar {
+    int count = 0;
+    long gen = 0;
+    bool acc = false, result = false;
+  };
+  std::mutex mu;
+  std::condition_variable cv;
+  Bar bars[33];  // by the mask's lowest lane and width: masks are contiguous lane groups here
+  static int key(unsigned mask) { return mask == 0xffffffffu ? 32 : __builtin_ctz(mask); }
+  bool meet(unsigned mask, bool p) {
+    std::unique_lock<std::mutex> lk(mu);
+    Bar& b = bars[key(mask)];
+    const long gen = b.gen;
+    b.acc = b.acc || p;
+    if (++b.count == __builtin_popcount(mask)) {
+      b.result = b.acc;
+      b.acc = false;
+      b.count = 0;
+      ++b.gen;
+      cv.notify_all();
+      return b.result;
+    }
+    cv.wait(lk, [&] { return b.gen != gen; });
+    return b.result;
+  }
+};
+// the warp the calling thread runs in, when its lanes run concurrently (else null)
+inline thread_local PdqHostWarp* pdq_host_warp = nullptr;
+
 #define __host__
 #define __device__
 #define __global__
@@ -79,8 +112,12 @@ template <typename T>
 inline T __shfl_xor_sync(unsigned, T v, int, int = 32) {
   return v;
 }
-inline void __syncwarp(unsigned = 0xffffffffu) {}
-inline bool __any_sync(unsigned, bool p) { return p; }  // one lane: its own predicate
+inline void __syncwarp(unsigned mask = 0xffffffffu) {
+  if (pdq_host_warp) pdq_host_warp->meet(mask, false);
+}
+inline bool __any_sync(unsigned mask, bool p) {  // one lane: its own predicate
+  return pdq_host_warp ? pdq_host_warp->meet(mask, p) : p;
+}
 inline void __syncthreads() {
   if (pdq_host_barriers) pdq_host_barriers[0].sync();
 }

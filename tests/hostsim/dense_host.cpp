@@ -5,7 +5,9 @@
 // included), so AddressSanitizer flags any access outside them.  With
 // PDQ_HOST_DENSE_KERNEL=struct in the environment it runs the
 // structure-exploiting kernel (dense_struct_kernel) with one lane per
-// instance instead, its shared memory a buffer of the launch's size.
+// instance instead, its shared memory a buffer of the launch's size; with
+// PDQ_HOST_DENSE_LANES=4, 8 or 16 as well, with that many lanes per instance,
+// each 32-lane block's lanes as host threads (warp barriers emulated).
 //
 // Input file (whitespace-separated): field (0 Lotka-Volterra, 1 van der Pol)
 // nu (2 or 3) strategy (0 filter, 1 fixed-point smoother) B S solver control
@@ -16,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 static std::vector<unsigned char> g_smem;  // the structure-exploiting kernel's shared memory
@@ -87,8 +90,35 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   const long long padded = (B + block - 1) / block * block;  // the launch's grid
   const char* kern = getenv("PDQ_HOST_DENSE_KERNEL");
   const bool structured = kern != nullptr && strcmp(kern, "struct") == 0;
-  if (structured) g_smem.assign(dense_struct_smem_bytes<NU, D>(sizeof(double), 1), 0);
-  for (long long g = 0; g < padded; ++g) {
+  const char* lanes_env = getenv("PDQ_HOST_DENSE_LANES");
+  const int lanes = lanes_env ? atoi(lanes_env) : 1;
+  if (structured && lanes > 1) {
+    // the structure-exploiting kernel as launched: 32 / L instances per
+    // 32-thread block, its 32 lanes as host threads meeting at the warp's
+    // barriers, the blocks one after another
+    if (lanes != 4 && lanes != 8 && lanes != 16) return 2;
+    const int ipw = 32 / lanes;
+    const long long grid = (B + ipw - 1) / ipw;
+    g_smem.assign(dense_struct_smem_bytes<NU, D>(sizeof(double), lanes), 0);
+    for (long long blk = 0; blk < grid; ++blk) {
+      PdqHostWarp warp;
+      std::vector<std::thread> threads;
+      for (unsigned tid = 0; tid < 32; ++tid)
+        threads.emplace_back([&, tid] {
+          blockDim = {32, 1, 1};
+          blockIdx = {uint32_t(blk), 0, 0};
+          threadIdx = {tid, 0, 0};
+          pdq_host_warp = &warp;
+          if (lanes == 4) dense_struct_kernel<double, NU, F, true, FP, 4>(a);
+          if (lanes == 8) dense_struct_kernel<double, NU, F, true, FP, 8>(a);
+          if (lanes == 16) dense_struct_kernel<double, NU, F, true, FP, 16>(a);
+          pdq_host_warp = nullptr;
+        });
+      for (auto& th : threads) th.join();
+    }
+  }
+  if (structured && lanes == 1) g_smem.assign(dense_struct_smem_bytes<NU, D>(sizeof(double), 1), 0);
+  for (long long g = 0; g < (structured && lanes > 1 ? 0 : padded); ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
     if (structured)

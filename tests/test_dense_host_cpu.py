@@ -4,7 +4,8 @@
 thread per instance; van der Pol, TS1 with the Jacobian on dual numbers, the
 fixed-point smoother with its scratch of backward conditionals and the
 backward pass) and ``dense_struct_kernel`` (the structure-exploiting QRs;
-one lane per instance, its shared memory a host buffer) with the host
+one lane per instance, its shared memory a host buffer; and with four,
+eight and sixteen lanes, each block's 32 lanes as host threads) with the host
 compiler under AddressSanitizer and UBSan, and runs them on the inputs of
 ``tests/golden/vdp_dense.json`` (the oracle's
 smoothed marginals at 8 save points reached by interpolation, mu = 1 and
@@ -141,3 +142,30 @@ def test_host_dense_mu30_100_save_points_matches_fixture(harness, tmp_path, kern
         assert max(rel(gm[i * d:(i + 1) * d], om[i * d:(i + 1) * d]) for i in range(N // d)) <= 1e-5, s
         assert rel(gc @ gc.T, oc @ oc.T) <= 1e-5, s
         assert abs(int(vals[1]) - steps_o[s]) <= 1, s
+
+
+def test_host_struct_kernel_lane_counts_agree(harness, tmp_path, monkeypatch):
+    """The structure-exploiting kernel as launched with four, eight and
+    sixteen lanes per instance (32 / L instances per block, the 32 lanes as
+    host threads meeting at the warp's barriers, the slots of absent
+    instances running the warp-uniform loop's dummy steps) gives the records
+    of the one-lane run bit for bit: the lanes change which lane computes a
+    column or row, not the order of any sum.  Van der Pol mu = 1 and 3, TS1,
+    the fixed-point smoother, 8 save points by interpolation."""
+    gold = make_golden.load("vdp_dense.json")
+    mus = gold["mu"]
+    B, S = len(mus), len(gold["save_at"][0])
+    head = [1, 3, 1, B, S, 2, 0, 0]
+    body = np.concatenate([[gold["atol"], gold["rtol"]], np.ravel(gold["save_at"]), mus,
+                           np.tile(gold["y0"], B), np.full(B, gold["dt0"]), q1_iwp(3).ravel()])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    monkeypatch.setenv("PDQ_HOST_DENSE_KERNEL", "struct")
+    outs = {}
+    for lanes in (1, 4, 8, 16):
+        monkeypatch.setenv("PDQ_HOST_DENSE_LANES", str(lanes))
+        outs[lanes] = hostsim.run_harness(harness, path)
+    assert len(outs[1]) == B * (1 + S)
+    assert all(int(outs[1][b * (1 + S)].split()[0]) == 0 for b in range(B))
+    for lanes in (4, 8, 16):
+        assert outs[lanes] == outs[1], lanes
