@@ -61,12 +61,19 @@ struct PdqHostWarp {
   };
   std::mutex mu;
   std::condition_variable cv;
-  Bar bars[33];  // by the mask's lowest lane and width: masks are contiguous lane groups here
+  Bar bars[33];  // by the mask's lowest lane: masks are contiguous lane groups here
+  // values published for a shuffle, by barrier generation parity (a lane is
+  // at most one generation ahead of the slowest lane of its mask)
+  unsigned char slots[2][32][8];
   static int key(unsigned mask) { return mask == 0xffffffffu ? 32 : __builtin_ctz(mask); }
-  bool meet(unsigned mask, bool p) {
+  // every lane of mask arrives; returns the OR of their predicates and, for a
+  // shuffle, copies lane src's published value into out
+  bool meet(unsigned mask, bool p, int lane = -1, const void* in = nullptr, int src = -1, void* out = nullptr,
+            size_t bytes = 0) {
     std::unique_lock<std::mutex> lk(mu);
     Bar& b = bars[key(mask)];
     const long gen = b.gen;
+    if (in) std::memcpy(slots[gen & 1][lane], in, bytes);
     b.acc = b.acc || p;
     if (++b.count == __builtin_popcount(mask)) {
       b.result = b.acc;
@@ -74,9 +81,10 @@ struct PdqHostWarp {
       b.count = 0;
       ++b.gen;
       cv.notify_all();
-      return b.result;
+    } else {
+      cv.wait(lk, [&] { return b.gen != gen; });
     }
-    cv.wait(lk, [&] { return b.gen != gen; });
+    if (out) std::memcpy(out, slots[gen & 1][src], bytes);
     return b.result;
   }
 };
@@ -108,9 +116,30 @@ template <typename T>
 inline T __ldg(const T* p) {
   return *p;
 }
+// Shuffles: with the warp's lanes as host threads the value of the source
+// lane (within width-wide segments); a lane alone gets its own value.
 template <typename T>
-inline T __shfl_xor_sync(unsigned, T v, int, int = 32) {
-  return v;
+inline T __shfl_sync(unsigned mask, T v, int src, int width = 32);
+template <typename T>
+inline T __shfl_xor_sync(unsigned mask, T v, int lane_mask, int width = 32);
+template <typename T>
+inline T __shfl_sync(unsigned mask, T v, int src, int width) {
+  static_assert(sizeof(T) <= 8, "one word per lane");
+  if (!pdq_host_warp) return v;
+  const int lane = int(threadIdx.x & 31u);
+  T r;
+  pdq_host_warp->meet(mask, false, lane, &v, (lane & ~(width - 1)) + (src % width), &r, sizeof(T));
+  return r;
+}
+template <typename T>
+inline T __shfl_xor_sync(unsigned mask, T v, int lane_mask, int width) {
+  static_assert(sizeof(T) <= 8, "one word per lane");
+  if (!pdq_host_warp) return v;
+  const int lane = int(threadIdx.x & 31u);
+  (void)width;
+  T r;
+  pdq_host_warp->meet(mask, false, lane, &v, lane ^ lane_mask, &r, sizeof(T));
+  return r;
 }
 inline void __syncwarp(unsigned mask = 0xffffffffu) {
   if (pdq_host_warp) pdq_host_warp->meet(mask, false);

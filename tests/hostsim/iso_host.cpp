@@ -14,7 +14,9 @@
 // (iso_tv_bwd_kernel) for a cotangent of the terminal mean; mode 6 the
 // split filter (iso_split_kernel: a covariance warp and a mean warp per
 // instance, run as two host threads), mode 7 the branch-light lean filter
-// (iso_lean_kernel); modes 6 and 7 with exact landings only.
+// (iso_lean_kernel), mode 8 the eight-lane kernel (iso_warp_kernel, each
+// warp's lanes as host threads with emulated shuffles); modes 6 to 8 with
+// exact landings only.
 //
 // Input file (whitespace-separated): precision (0 float32, 1 float64) mode nu
 // B S solver control clip_dt terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
@@ -33,6 +35,7 @@
 #include "iso_lean.cuh"
 #include "iso_solver.cuh"
 #include "iso_split.cuh"
+#include "iso_warp.cuh"
 #include "tv_adjoint.cuh"
 
 thread_local pdq_host_uint3 threadIdx, blockIdx, blockDim;
@@ -148,10 +151,29 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
       mean.join();
     }
   }
+  if constexpr (MODE == 8 && !INTERP) {
+    // the eight-lane kernel: each warp's 32 lanes (four instances) as host
+    // threads exchanging the reflectors and rotations by emulated shuffles
+    const long long warps = (B * 8 + 31) / 32;
+    for (long long w = 0; w < warps; ++w) {
+      PdqHostWarp warp;
+      std::vector<std::thread> lanes;
+      for (unsigned tid = 0; tid < 32; ++tid)
+        lanes.emplace_back([&, tid] {
+          blockDim = {256, 1, 1};
+          blockIdx = {uint32_t(w / 8), 0, 0};
+          threadIdx = {uint32_t((w % 8) * 32 + tid), 0, 0};
+          pdq_host_warp = &warp;
+          iso_warp_kernel<T, NU, F, 8, 2>(a);
+          pdq_host_warp = nullptr;
+        });
+      for (auto& th : lanes) th.join();
+    }
+  }
   const int block = 64;
   blockDim = {uint32_t(block), 1, 1};
   const long long threads = MODE == 2 ? B * (P + D) : B;
-  const long long padded = MODE == 6 ? 0 : (threads + block - 1) / block * block;  // the launch's grid
+  const long long padded = (MODE == 6 || MODE == 8) ? 0 : (threads + block - 1) / block * block;  // the launch's grid
   for (long long g = 0; g < padded; ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
@@ -212,7 +234,7 @@ int main(int argc, char** argv) {
   if (B < 1 || S < 2) return 2;
   int rc = 2;
   const bool interp = !clip_dt;
-  const int args_ok = (mode >= 0 && mode <= 7) && (nu == 3 || nu == 4 || (nu == 5 && (mode == 0 || mode >= 6))) &&
+  const int args_ok = (mode >= 0 && mode <= 8) && (nu == 3 || nu == 4 || (nu == 5 && (mode == 0 || mode >= 6))) &&
                       (mode != 5 || (clip_dt && terminal_only && S == 2)) && (mode < 6 || clip_dt);
   if (!args_ok) return 2;
 #define PDQ_HOST_RUN(NU_, MODE_)                                                                        \
@@ -235,6 +257,8 @@ int main(int argc, char** argv) {
   if (nu == 4 && mode == 7) PDQ_HOST_RUN(4, 7);
   if (nu == 3 && mode == 7) PDQ_HOST_RUN(3, 7);
   if (nu == 5 && mode == 7) PDQ_HOST_RUN(5, 7);
+  if (nu == 4 && mode == 8) PDQ_HOST_RUN(4, 8);
+  if (nu == 3 && mode == 8) PDQ_HOST_RUN(3, 8);
   if (nu == 3 && mode == 6) PDQ_HOST_RUN(3, 6);
 #undef PDQ_HOST_RUN
   fclose(in);

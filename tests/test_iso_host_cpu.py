@@ -311,3 +311,48 @@ def test_host_lean_and_split_kernels_equal_the_one_thread_kernel_with_failures(h
     assert statuses.count(0) >= B // 2
     if nu == 5:
         assert any(s != 0 for s in statuses)
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_host_eight_lane_kernel_matches_golden_records(harness, tmp_path, precision):
+    """The eight-lane kernel (iso_warp_kernel: a group of eight lanes per
+    instance exchanging reflectors and rotations by shuffles; here each
+    warp's 32 lanes run as host threads with emulated shuffles) on the
+    golden MLE terminal-value run: float64 within the GPU parity tests'
+    tolerances of the oracle's records (solution 1e-9, rows and L L^T 1e-6,
+    accepted steps +-1, output scale 1e-6); float32 bulk within 1e-4 of the
+    solution and +-10 % of the steps."""
+    gold = make_golden.load("lv_filter.json")
+    r = gold["mle_terminal"]
+    assert r["clip_dt"]
+    nu, n, d = gold["num_derivatives"], gold["num_derivatives"] + 1, 2
+    params, y0 = np.array(gold["params"]), np.array(gold["y0"])
+    B, S = params.shape[0], len(r["save_at"])
+    head = [precision, 8, nu, B, S, SOLVER["mle"], 0, 1, 1]
+    body = np.concatenate([[r["atol"], r["rtol"]], np.tile(r["save_at"], B), params.ravel(), y0.ravel(),
+                           np.full(B, gold["dt0"]), q1_iwp(nu).ravel()])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lines = hostsim.run_harness(harness, path)
+    assert len(lines) == 2 * B
+    for b, rec in enumerate(r["records"]):
+        status, attempts = (int(x) for x in lines[2 * b].split())
+        assert status == 0 and attempts > 0
+        vals = [float(x) for x in lines[2 * b + 1].split()]
+        steps, scale = int(vals[1]), vals[2]
+        gm = np.array(vals[3:3 + n * d]).reshape(n, d)
+        gc = np.array(vals[3 + n * d:]).reshape(n, n)
+        om, oc = np.array(rec["u_mean"][S - 1]), np.array(rec["u_chol"][S - 1])
+        steps_o = rec["num_steps"][S - 2]
+        err = float(np.abs(gm[0] - om[0]).max() / np.abs(om[0]).max())
+        if precision == 1:
+            assert err <= 1e-9, (b, err)
+            for i in range(n):
+                assert float(np.abs(gm[i] - om[i]).max() / max(np.abs(om[i]).max(), 1e-300)) <= 1e-6, (b, i)
+            cg, co = gc @ gc.T, oc @ oc.T
+            assert float(np.abs(cg - co).max() / max(np.abs(co).max(), 1e-300)) <= 1e-6, b
+            assert abs(steps - steps_o) <= 1, (b, steps, steps_o)
+            so = rec["output_scale"][-1]
+            assert abs(scale - so) <= 1e-6 * abs(so), (scale, so)
+        else:
+            assert err <= 1e-4 and abs(steps - steps_o) <= max(1, int(0.1 * steps_o)), (b, err, steps, steps_o)
