@@ -21,6 +21,11 @@
 // memory and a fully unrolled code far beyond the instruction cache.
 #pragma once
 
+// The kernel's dynamic shared memory (a host run of the kernel body supplies a buffer instead).
+#ifndef PDQ_DENSE_COOP_SMEM
+#define PDQ_DENSE_COOP_SMEM extern __shared__ __align__(16) unsigned char coop_smem_raw[]
+#endif
+
 #include "dense_solver.cuh"
 
 namespace pdq {
@@ -391,7 +396,7 @@ template <typename T, int NU, class F, bool TS1, bool FP>
 __global__ void __launch_bounds__(128) dense_coop_kernel(DenseArgs a) {
   constexpr int D = F::D, P = F::P, n = NU + 1, N = n * D;
   using State = CoopState<T, N, D>;
-  extern __shared__ __align__(16) unsigned char coop_smem_raw[];
+  PDQ_DENSE_COOP_SMEM;
   // one instance per warp, on lanes 0-7: instances take different branches
   // (accept / reject, checkpoints), and groups sharing a warp would serialise
   const int group_in_block = threadIdx.x / 32;
@@ -622,6 +627,7 @@ __global__ void __launch_bounds__(128) dense_coop_kernel(DenseArgs a) {
 #pragma unroll
               for (int i = 0; i < D; ++i) q += wv[i] * wv[i];
             }
+            g.sync();  // every lane has read R_Y from M, which the merge below overwrites
             if constexpr (FP) coop_merge(st.bw, st.cn, st.mg, st.M, g);
             ti = t;
             coop_normal_copy(st.xi, st.x, g);

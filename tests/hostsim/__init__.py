@@ -12,15 +12,19 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 
 
-def compile_harness(source, exe):
-    """Compile ``tests/hostsim/<source>`` to ``exe``; skips the test without g++."""
+def compile_harness(source, exe, sanitize="address,undefined"):
+    """Compile ``tests/hostsim/<source>`` to ``exe`` (AddressSanitizer and
+    UBSan, or ``sanitize="thread"`` for ThreadSanitizer); skips the test
+    without g++."""
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("no host C++ compiler")
-    cmd = [cxx, "-std=c++17", "-O1", "-g", "-pthread", "-ffp-contract=off", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+    cmd = [cxx, "-std=c++17", "-O1", "-g", "-pthread", "-ffp-contract=off", "-fsanitize=" + sanitize, "-fno-sanitize-recover=all",
            "-I" + HERE, "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "probdiffeq_gb300", "csrc"),
            os.path.join(HERE, source), "-o", str(exe)]
     res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0 and "sanitize" in res.stderr and sanitize == "thread":
+        pytest.skip("no ThreadSanitizer runtime")
     if res.returncode != 0 and "sanitize" in res.stderr:
         cmd = [c for c in cmd if "sanitize" not in c]  # a toolchain without the sanitizer runtimes
         res = subprocess.run(cmd, capture_output=True, text=True)

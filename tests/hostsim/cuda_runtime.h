@@ -95,6 +95,7 @@ inline thread_local PdqHostWarp* pdq_host_warp = nullptr;
 #define __device__
 #define __global__
 #define __forceinline__ inline
+#define __noinline__ __attribute__((noinline))
 #define __shared__ static
 #define __align__(n) __attribute__((aligned(n)))
 #define __launch_bounds__(...)

@@ -7,7 +7,9 @@
 // structure-exploiting kernel (dense_struct_kernel) with one lane per
 // instance instead, its shared memory a buffer of the launch's size; with
 // PDQ_HOST_DENSE_LANES=4, 8 or 16 as well, with that many lanes per instance,
-// each 32-lane block's lanes as host threads (warp barriers emulated).
+// each 32-lane block's lanes as host threads (warp barriers emulated); with
+// PDQ_HOST_DENSE_KERNEL=coop the lane-cooperative kernel (dense_coop_kernel,
+// eight lanes per instance as host threads, shuffles emulated).
 //
 // Input file (whitespace-separated): field (0 Lotka-Volterra, 1 van der Pol)
 // nu (2 or 3) strategy (0 filter, 1 fixed-point smoother) B S solver control
@@ -21,9 +23,11 @@
 #include <thread>
 #include <vector>
 
-static std::vector<unsigned char> g_smem;  // the structure-exploiting kernel's shared memory
+static std::vector<unsigned char> g_smem;  // the structure-exploiting and lane-cooperative kernels' shared memory
 #define PDQ_DENSE_STRUCT_SMEM unsigned char* dense_struct_smem = g_smem.data()
+#define PDQ_DENSE_COOP_SMEM unsigned char* coop_smem_raw = g_smem.data()
 
+#include "dense_coop.cuh"
 #include "dense_solver.cuh"
 #include "dense_struct.cuh"
 
@@ -117,8 +121,28 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
       for (auto& th : threads) th.join();
     }
   }
+  const bool coop = kern != nullptr && strcmp(kern, "coop") == 0;
+  if (coop) {
+    // the lane-cooperative kernel, one instance per 32-thread block: its
+    // eight lanes as host threads exchanging sums by emulated shuffles
+    g_smem.assign(sizeof(CoopState<double, N, D>), 0);
+    for (long long b = 0; b < B; ++b) {
+      PdqHostWarp warp;
+      std::vector<std::thread> threads;
+      for (unsigned tid = 0; tid < unsigned(kCoopLanes); ++tid)
+        threads.emplace_back([&, tid] {
+          blockDim = {32, 1, 1};
+          blockIdx = {uint32_t(b), 0, 0};
+          threadIdx = {tid, 0, 0};
+          pdq_host_warp = &warp;
+          dense_coop_kernel<double, NU, F, true, FP>(a);
+          pdq_host_warp = nullptr;
+        });
+      for (auto& th : threads) th.join();
+    }
+  }
   if (structured && lanes == 1) g_smem.assign(dense_struct_smem_bytes<NU, D>(sizeof(double), 1), 0);
-  for (long long g = 0; g < (structured && lanes > 1 ? 0 : padded); ++g) {
+  for (long long g = 0; g < ((structured && lanes > 1) || coop ? 0 : padded); ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
     if (structured)

@@ -5,7 +5,9 @@ thread per instance; van der Pol, TS1 with the Jacobian on dual numbers, the
 fixed-point smoother with its scratch of backward conditionals and the
 backward pass) and ``dense_struct_kernel`` (the structure-exploiting QRs;
 one lane per instance, its shared memory a host buffer; and with four,
-eight and sixteen lanes, each block's 32 lanes as host threads) with the host
+eight and sixteen lanes, each block's 32 lanes as host threads) and
+``dense_coop_kernel`` (eight lanes per instance as host threads, shuffles
+emulated) with the host
 compiler under AddressSanitizer and UBSan, and runs them on the inputs of
 ``tests/golden/vdp_dense.json`` (the oracle's
 smoothed marginals at 8 save points reached by interpolation, mu = 1 and
@@ -44,7 +46,15 @@ def kernel(request, monkeypatch):
     return request.param
 
 
-def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path, kernel):
+# the lane-cooperative kernel too (its eight lanes as host threads with
+# emulated shuffles: slower on the host, so on the short runs only)
+@pytest.fixture(params=KERNELS + ["coop"])
+def kernel_all(request, monkeypatch):
+    monkeypatch.setenv("PDQ_HOST_DENSE_KERNEL", request.param)
+    return request.param
+
+
+def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path, kernel_all):
     gold = make_golden.load("vdp_dense.json")
     mus = gold["mu"]
     B, S, d, N = len(mus), len(gold["save_at"][0]), 2, 8
@@ -85,7 +95,7 @@ def _run_lv(harness, tmp_path, strategy, solver, save_at, tol):
 
 @pytest.mark.parametrize("solver", [0, 1, 2])
 @pytest.mark.parametrize("strategy", ["filter", "smoother"])
-def test_host_dense_kernel_behaviour_close_to_t1(harness, tmp_path, strategy, solver, kernel):
+def test_host_dense_kernel_behaviour_close_to_t1(harness, tmp_path, strategy, solver, kernel_all):
     """The reference's test_dense_output/test_behaviour_close_to_t1.py:58-94
     on the dense kernel: Lotka--Volterra, TS1, nu = 2, tol 1e-1, 30 save
     points up to the second-to-last point of the oracle's save-every-step

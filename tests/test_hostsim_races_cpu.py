@@ -1,0 +1,84 @@
+"""The warp-cooperative kernels under ThreadSanitizer.
+
+The host harnesses run each warp's lanes as host threads, with
+``__syncwarp``, ``__any_sync``, the shuffles and the named barriers emulated
+by mutex-guarded barriers (``tests/hostsim/cuda_runtime.h``), so a lane that
+reads shared memory another lane writes without a barrier between them is a
+data race ThreadSanitizer reports (and the harness exits non-zero).  Covered:
+the dense lane-cooperative kernel (fixed-point smoother with MLE
+calibration: the update's R_Y is read from the shared workspace that the
+merge then overwrites), the structure-exploiting dense kernel on four, eight
+and sixteen lanes, and the isotropic split (covariance / mean warp) and
+eight-lane kernels.
+"""
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests import hostsim
+
+
+def q1_iwp(nu):
+    n = nu + 1
+    H = np.array([[1.0 / (2 * nu + 1 - i - j) for j in range(n)] for i in range(n)])
+    return np.linalg.cholesky(H)
+
+
+@pytest.fixture(scope="module")
+def dense_tsan(tmp_path_factory):
+    return hostsim.compile_harness("dense_host.cpp", tmp_path_factory.mktemp("tsan") / "dense_host_tsan",
+                                   sanitize="thread")
+
+
+@pytest.fixture(scope="module")
+def iso_tsan(tmp_path_factory):
+    return hostsim.compile_harness("iso_host.cpp", tmp_path_factory.mktemp("tsan") / "iso_host_tsan",
+                                   sanitize="thread")
+
+
+@pytest.mark.parametrize("kernel,lanes", [("coop", 1), ("struct", 4), ("struct", 8), ("struct", 16)])
+@pytest.mark.parametrize("solver", [1, 2])
+def test_dense_cooperative_kernels_have_no_races(dense_tsan, tmp_path, monkeypatch, kernel, lanes, solver):
+    """Lotka--Volterra, nu = 2, TS1, the fixed-point smoother, 12 save points."""
+    ts = np.linspace(0.0, 1.9, 12)
+    head = [0, 2, 1, 1, len(ts), solver, 0, 0]
+    body = np.concatenate([[0.1, 0.1], ts, [0.5, 0.05, 0.5, 0.05], [20.0, 20.0], [0.1], q1_iwp(2).ravel()])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    monkeypatch.setenv("PDQ_HOST_DENSE_KERNEL", kernel)
+    monkeypatch.setenv("PDQ_HOST_DENSE_LANES", str(lanes))
+    lines = hostsim.run_harness(dense_tsan, path)  # a reported race exits non-zero
+    assert int(lines[0].split()[0]) == 0
+    assert all(np.isfinite([float(x) for x in line.split()]).all() for line in lines[1:])
+
+
+@pytest.mark.parametrize("mode", [6, 8])
+@pytest.mark.parametrize("precision", [1, 0])
+def test_isotropic_cooperative_kernels_have_no_races(iso_tsan, tmp_path, mode, precision):
+    """The split kernel (mode 6) and the eight-lane kernel (mode 8): eight of
+    the benchmark's Lotka--Volterra instances, nu = 4, MLE, exact landings on
+    5 save points."""
+    import bench
+
+    params, y0 = (x.numpy() for x in bench.lv_inputs(8, seed=3))
+    B, save_at = 8, [0.0, 1.0, 1.0 + 1e-3, 7.5, 20.0]
+    head = [precision, mode, 4, B, len(save_at), 1, 0, 1, 0]
+    body = np.concatenate([[1e-6, 1e-6], np.tile(save_at, B), params.ravel(), y0.ravel(), np.full(B, 0.1),
+                           q1_iwp(4).ravel()])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lines = hostsim.run_harness(iso_tsan, path)
+    assert all(int(lines[b * (1 + len(save_at))].split()[0]) == 0 for b in range(B))
+
+
+def test_thread_sanitizer_is_active(dense_tsan, tmp_path):
+    """The harness really is a ThreadSanitizer build (else the tests above
+    prove nothing): the sanitizer's runtime answers TSAN_OPTIONS=help=1."""
+    empty = tmp_path / "empty.txt"
+    empty.write_text("")
+    res = subprocess.run([dense_tsan, str(empty)], capture_output=True, text=True, timeout=60,
+                         env=dict(os.environ, TSAN_OPTIONS="help=1"))
+    assert "ThreadSanitizer" in res.stderr or "tsan" in res.stderr.lower()
