@@ -47,14 +47,14 @@ def kernel(request, monkeypatch):
 
 
 # the lane-cooperative kernel too (its eight lanes as host threads with
-# emulated shuffles: slower on the host, so on the short runs only)
+# emulated shuffles: slower on the host, so on the short Lotka--Volterra runs)
 @pytest.fixture(params=KERNELS + ["coop"])
 def kernel_all(request, monkeypatch):
     monkeypatch.setenv("PDQ_HOST_DENSE_KERNEL", request.param)
     return request.param
 
 
-def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path, kernel_all):
+def test_host_dense_fixed_point_kernel_matches_golden_records(harness, tmp_path, kernel):
     gold = make_golden.load("vdp_dense.json")
     mus = gold["mu"]
     B, S, d, N = len(mus), len(gold["save_at"][0]), 2, 8
@@ -160,13 +160,13 @@ def test_host_struct_kernel_lane_counts_agree(harness, tmp_path, monkeypatch):
     host threads meeting at the warp's barriers, the slots of absent
     instances running the warp-uniform loop's dummy steps) gives the records
     of the one-lane run bit for bit: the lanes change which lane computes a
-    column or row, not the order of any sum.  Van der Pol mu = 1 and 3, TS1,
-    the fixed-point smoother, 8 save points by interpolation."""
+    column or row, not the order of any sum.  Van der Pol mu = 1, TS1, the
+    fixed-point smoother, 8 save points by interpolation."""
     gold = make_golden.load("vdp_dense.json")
-    mus = gold["mu"]
+    mus = gold["mu"][:1]  # mu = 1 (the stiffer mu = 3 instance only lengthens the host run)
     B, S = len(mus), len(gold["save_at"][0])
     head = [1, 3, 1, B, S, 2, 0, 0]
-    body = np.concatenate([[gold["atol"], gold["rtol"]], np.ravel(gold["save_at"]), mus,
+    body = np.concatenate([[gold["atol"], gold["rtol"]], np.ravel(gold["save_at"][:B]), mus,
                            np.tile(gold["y0"], B), np.full(B, gold["dt0"]), q1_iwp(3).ravel()])
     path = tmp_path / "input.txt"
     path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
