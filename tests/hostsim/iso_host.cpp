@@ -15,8 +15,9 @@
 // split filter (iso_split_kernel: a covariance warp and a mean warp per
 // instance, run as two host threads), mode 7 the branch-light lean filter
 // (iso_lean_kernel), mode 8 the eight-lane kernel (iso_warp_kernel, each
-// warp's lanes as host threads with emulated shuffles); modes 6 to 8 with
-// exact landings only.
+// warp's lanes as host threads with emulated shuffles), mode 9 the split
+// kernel as launched (two 32-lane warps per 32 instances, 64 host threads
+// per block); modes 6 to 9 with exact landings only.
 //
 // Input file (whitespace-separated): precision (0 float32, 1 float64) mode nu
 // B S solver control clip_dt terminal_only, then atol rtol, save_at (B x S), params (B x 4), y0 (B x 2),
@@ -151,6 +152,31 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
       mean.join();
     }
   }
+  if constexpr (MODE == 9 && !INTERP) {
+    // the split kernel as launched: 32 instances per block of two 32-lane
+    // warps, all 64 lanes as host threads (the warps' __any_sync emulated
+    // per warp, the named barriers and __syncthreads per block), the last
+    // block ragged when B is not a multiple of 32
+    const long long grid = (B + 31) / 32;
+    for (long long blk = 0; blk < grid; ++blk) {
+      PdqHostBarrier bars[3];
+      for (auto& br : bars) br.expected = 64;
+      PdqHostWarp warps[2];
+      std::vector<std::thread> lanes;
+      for (unsigned tid = 0; tid < 64; ++tid)
+        lanes.emplace_back([&, tid] {
+          blockDim = {64, 1, 1};
+          blockIdx = {uint32_t(blk), 0, 0};
+          threadIdx = {tid, 0, 0};
+          pdq_host_barriers = bars;
+          pdq_host_warp = &warps[tid / 32];
+          iso_split_kernel<T, NU, F, 32>(a);
+          pdq_host_warp = nullptr;
+          pdq_host_barriers = nullptr;
+        });
+      for (auto& th : lanes) th.join();
+    }
+  }
   if constexpr (MODE == 8 && !INTERP) {
     // the eight-lane kernel: each warp's 32 lanes (four instances) as host
     // threads exchanging the reflectors and rotations by emulated shuffles
@@ -173,7 +199,7 @@ static int run(FILE* in, long long B, int S, int solver, int control, int clip_d
   const int block = 64;
   blockDim = {uint32_t(block), 1, 1};
   const long long threads = MODE == 2 ? B * (P + D) : B;
-  const long long padded = (MODE == 6 || MODE == 8) ? 0 : (threads + block - 1) / block * block;  // the launch's grid
+  const long long padded = (MODE == 6 || MODE >= 8) ? 0 : (threads + block - 1) / block * block;  // the launch's grid
   for (long long g = 0; g < padded; ++g) {
     blockIdx = {uint32_t(g / block), 0, 0};
     threadIdx = {uint32_t(g % block), 0, 0};
@@ -234,7 +260,7 @@ int main(int argc, char** argv) {
   if (B < 1 || S < 2) return 2;
   int rc = 2;
   const bool interp = !clip_dt;
-  const int args_ok = (mode >= 0 && mode <= 8) && (nu == 3 || nu == 4 || (nu == 5 && (mode == 0 || mode >= 6))) &&
+  const int args_ok = (mode >= 0 && mode <= 9) && (nu == 3 || nu == 4 || (nu == 5 && (mode == 0 || mode >= 6))) &&
                       (mode != 5 || (clip_dt && terminal_only && S == 2)) && (mode < 6 || clip_dt);
   if (!args_ok) return 2;
 #define PDQ_HOST_RUN(NU_, MODE_)                                                                        \
@@ -259,6 +285,7 @@ int main(int argc, char** argv) {
   if (nu == 5 && mode == 7) PDQ_HOST_RUN(5, 7);
   if (nu == 4 && mode == 8) PDQ_HOST_RUN(4, 8);
   if (nu == 3 && mode == 8) PDQ_HOST_RUN(3, 8);
+  if (nu == 4 && mode == 9) PDQ_HOST_RUN(4, 9);
   if (nu == 3 && mode == 6) PDQ_HOST_RUN(3, 6);
 #undef PDQ_HOST_RUN
   fclose(in);

@@ -55,10 +55,11 @@ def test_dense_cooperative_kernels_have_no_races(dense_tsan, tmp_path, monkeypat
     assert all(np.isfinite([float(x) for x in line.split()]).all() for line in lines[1:])
 
 
-@pytest.mark.parametrize("mode", [6, 8])
+@pytest.mark.parametrize("mode", [6, 8, 9])
 @pytest.mark.parametrize("precision", [1, 0])
 def test_isotropic_cooperative_kernels_have_no_races(iso_tsan, tmp_path, mode, precision):
-    """The split kernel (mode 6) and the eight-lane kernel (mode 8): four of
+    """The split kernel (mode 6: one-lane warps; mode 9: as launched, two
+    32-lane warps as 64 host threads) and the eight-lane kernel (mode 8): four of
     the benchmark's Lotka--Volterra instances, nu = 4, MLE, exact landings on
     4 save points."""
     import bench

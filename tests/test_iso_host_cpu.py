@@ -256,8 +256,9 @@ def test_host_headline_kernel_on_the_benchmark_distribution(harness, tmp_path, p
 @pytest.mark.parametrize("solver,terminal", [("mle", True), ("none", True), ("mle", False)])
 def test_host_lean_and_split_kernels_equal_the_one_thread_kernel(harness, tmp_path, precision, solver, terminal):
     """The branch-light lean kernel (iso_lean_kernel) and the split filter
-    (iso_split_kernel: a covariance warp and a mean warp per instance, here
-    two host threads meeting at the named barriers) run the arithmetic of
+    (iso_split_kernel: a covariance warp and a mean warp, here with one lane
+    per warp as two host threads meeting at the named barriers, and as
+    launched with 32-lane warps as 64 host threads) run the arithmetic of
     iso_adaptive_kernel's lean instantiation, so their records are its own bit
     for bit: 16 of the benchmark's Lotka--Volterra instances, nu = 4,
     rtol = atol = 1e-6, exact landings, terminal values or 6 save points,
@@ -277,10 +278,11 @@ def test_host_lean_and_split_kernels_equal_the_one_thread_kernel(harness, tmp_pa
         path.write_text(" ".join(str(v) for v in head) + " " + " ".join(repr(float(v)) for v in body))
         return hostsim.run_harness(harness, path)
 
-    one, split, lean = run(0), run(6), run(7)
+    one, split, lean, split32 = run(0), run(6), run(7), run(9)
     assert len(one) == B * (1 + (1 if terminal else len(save_at)))
     assert split == one
     assert lean == one
+    assert split32 == one  # as launched: two 32-lane warps, 16 of the 32 instance slots empty
     assert all(line.split()[0] == "0" for line in one[::1 + (1 if terminal else len(save_at))])
 
 
