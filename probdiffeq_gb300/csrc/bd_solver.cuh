@@ -53,6 +53,15 @@ namespace pdq {
 // cluster, the cluster barrier (arrive with release, wait with acquire
 // semantics), and the address of the same shared-memory variable in
 // another block of the cluster.
+// The kernel's shared memory: the dynamic part and the fixed arrays (a host
+// run of the kernel body supplies per-block buffers instead).
+#ifndef PDQ_BD_SMEM
+#define PDQ_BD_SMEM extern __shared__ unsigned char smem_raw[]
+#endif
+#ifndef PDQ_BD_SHARED
+#define PDQ_BD_SHARED(type, name, count) __shared__ type name[count]
+#endif
+
 struct Cluster {
   PDQ_D unsigned block_rank() const { return __clusterRelativeBlockRank(); }
   PDQ_D void sync() const {
@@ -218,13 +227,13 @@ __global__ void __launch_bounds__(kBdThreads, 2) bd_adaptive_kernel(BdArgs a) {
   const int j0 = rank * dl;
   const int tid = threadIdx.x;
 
-  extern __shared__ unsigned char smem_raw[];
+  PDQ_BD_SMEM;
   T* mps = reinterpret_cast<T*>(smem_raw);  // [n][dl] extrapolated means of this CTA's dimensions
   T* newt = mps + n * dl;                   // [dl] whitened residual of the proposal (MLE)
   T* sig_new = newt + dl;                   // [dl] local scale of the proposal (dynamic)
   T* sig = sig_new + dl;                    // [dl] output scale of the current state
-  __shared__ W partial[2];                  // CTA partial sums (error norm), parity
-  __shared__ W warp_sums[kBdThreads / 32];
+  PDQ_BD_SHARED(W, partial, 2);                  // CTA partial sums (error norm), parity
+  PDQ_BD_SHARED(W, warp_sums, kBdThreads / 32);
 
   T* const buf0 = reinterpret_cast<T*>(a.workspace);
   T* const bufs[2] = {buf0 + inst * NS * int64_t(d), buf0 + (a.B + inst) * NS * int64_t(d)};

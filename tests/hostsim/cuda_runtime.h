@@ -11,8 +11,12 @@
 #include <cmath>
 #include <condition_variable>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
 
 #define PDQ_HOST_SIM 1
 
@@ -91,6 +95,50 @@ struct PdqHostWarp {
 // the warp the calling thread runs in, when its lanes run concurrently (else null)
 inline thread_local PdqHostWarp* pdq_host_warp = nullptr;
 
+// A thread-block cluster whose blocks' threads run as host threads: block r
+// of the cluster has its shared memory at base + r * region (the dynamic
+// part first, then the fixed arrays at offsets common to all blocks), and a
+// cluster barrier with separate arrive and wait.
+struct PdqHostCluster {
+  int dim = 1;
+  unsigned char* base = nullptr;
+  size_t region = 0, dynamic_bytes = 0;
+  int expected = 1, count = 0;
+  long phase = 0;
+  std::mutex mu;
+  std::condition_variable cv;
+  size_t next_fixed = 0;
+  std::vector<std::pair<std::string, size_t>> fixed;  // name -> offset past the dynamic part
+  long arrive() {
+    std::lock_guard<std::mutex> lk(mu);
+    const long ph = phase;
+    if (++count == expected) {
+      count = 0;
+      ++phase;
+      cv.notify_all();
+    }
+    return ph;
+  }
+  void wait(long ph) {
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [&] { return phase != ph; });
+  }
+  // the offset of a fixed shared array (the same in every block)
+  size_t fixed_offset(const char* name, size_t bytes) {
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto& f : fixed)
+      if (f.first == name) return f.second;
+    const size_t off = dynamic_bytes + next_fixed;
+    next_fixed += (bytes + 15) / 16 * 16;
+    if (off + bytes > region) std::abort();  // the harness sized the region too small
+    fixed.emplace_back(name, off);
+    return off;
+  }
+};
+// the cluster the calling thread's block belongs to (else null)
+inline thread_local PdqHostCluster* pdq_host_cluster = nullptr;
+inline thread_local long pdq_host_cluster_phase = 0;
+
 #define __host__
 #define __device__
 #define __global__
@@ -147,6 +195,25 @@ inline void __syncwarp(unsigned mask = 0xffffffffu) {
 }
 inline bool __any_sync(unsigned mask, bool p) {  // one lane: its own predicate
   return pdq_host_warp ? pdq_host_warp->meet(mask, p) : p;
+}
+inline unsigned __clusterRelativeBlockRank() {
+  return pdq_host_cluster ? unsigned(blockIdx.x % unsigned(pdq_host_cluster->dim)) : 0u;
+}
+inline void __cluster_barrier_arrive() {
+  if (pdq_host_cluster) pdq_host_cluster_phase = pdq_host_cluster->arrive();
+}
+inline void __cluster_barrier_wait() {
+  if (pdq_host_cluster) pdq_host_cluster->wait(pdq_host_cluster_phase);
+}
+inline void* __cluster_map_shared_rank(void* p, unsigned rank) {
+  PdqHostCluster* c = pdq_host_cluster;
+  if (!c) return p;
+  const size_t off = size_t(static_cast<unsigned char*>(p) - c->base) % c->region;
+  return c->base + size_t(rank) * c->region + off;
+}
+// this block's shared memory
+inline unsigned char* pdq_host_block_smem() {
+  return pdq_host_cluster->base + size_t(__clusterRelativeBlockRank()) * pdq_host_cluster->region;
 }
 inline void __syncthreads() {
   if (pdq_host_barriers) pdq_host_barriers[0].sync();
