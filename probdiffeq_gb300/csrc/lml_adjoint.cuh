@@ -93,9 +93,14 @@ PDQ_D void lml_stage_chunk(T* stage, const T* plan, int chunk, int num_steps, in
   for (int e = lane; e < count; e += 32) stage[e] = src[e];
   __syncwarp();
 #else
-  // host runs of the kernel bodies execute one lane at a time: it stages the whole chunk
-  (void)lane;
-  for (int e = 0; e < count; ++e) stage[e] = src[e];
+  if (PDQ_HOST_LANES_CONCURRENT) {  // host runs with the warp's lanes as threads
+    __syncwarp();
+    for (int e = lane; e < count; e += 32) stage[e] = src[e];
+    __syncwarp();
+  } else {
+    // host runs of the kernel bodies execute one lane at a time: it stages the whole chunk
+    for (int e = 0; e < count; ++e) stage[e] = src[e];
+  }
 #endif
 }
 

@@ -499,8 +499,14 @@ __global__ void __launch_bounds__(kLmlThreads) lml_kernel(LmlArgs a) {
       for (int e = lane; e < count; e += 32) stage[e] = src[e];
       __syncwarp();
 #else
-      // host runs of the kernel body execute one lane at a time: it stages the whole chunk
-      for (int e = 0; e < count; ++e) stage[e] = src[e];
+      if (PDQ_HOST_LANES_CONCURRENT) {  // host runs with the warp's lanes as threads
+        __syncwarp();
+        for (int e = lane; e < count; e += 32) stage[e] = src[e];
+        __syncwarp();
+      } else {
+        // host runs of the kernel body execute one lane at a time: it stages the whole chunk
+        for (int e = 0; e < count; ++e) stage[e] = src[e];
+      }
 #endif
     }
     if (!valid || status != PDQ_INSTANCE_OK) continue;

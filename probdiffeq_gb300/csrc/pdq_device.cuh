@@ -120,6 +120,14 @@ PDQ_D double fast_sqrt(double x) { return sqrt(x); }
 PDQ_D double fast_rsqrt(double x) { return rsqrt(x); }
 PDQ_D double fast_rcp(double x) { return 1.0 / x; }
 
+// Host runs of the kernel bodies (tests) either run a warp's lanes one at a
+// time or as concurrent threads; device code never reads this.
+#if defined(PDQ_HOST_SIM)
+#define PDQ_HOST_LANES_CONCURRENT (pdq_host_warp != nullptr)
+#else
+#define PDQ_HOST_LANES_CONCURRENT false
+#endif
+
 // Named CTA barriers for a producer / consumer pair of warps: the producer
 // arrives (and goes on), the consumer waits until `count` threads (both
 // warps) have arrived.  Shared-memory writes before the arrive are visible

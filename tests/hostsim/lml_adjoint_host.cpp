@@ -13,6 +13,7 @@
 // Output: one line per sample: status lml grad[P] grad_y0[2].
 #include <cstdio>
 #include <cstdlib>
+#include <thread>
 #include <vector>
 
 #include "lml_adjoint.cuh"
@@ -78,7 +79,28 @@ static int run(FILE* in, long long B, int N, int se, int C, int avg) {
   lml_plan_kernel<T, NU>(a);
   blockDim = {uint32_t(kLmlThreads), 1, 1};
   const long long padded = (B + kLmlThreads - 1) / kLmlThreads * kLmlThreads;  // the launch's grid
-  for (int pass = 0; pass < 2; ++pass)
+  const bool warps = getenv("PDQ_HOST_LML_WARPS") != nullptr;  // each block's 32 lanes as threads
+  for (int pass = 0; pass < 2; ++pass) {
+    if (warps) {
+      for (long long blk = 0; blk < padded / kLmlThreads; ++blk) {
+        PdqHostWarp warp;
+        std::vector<std::thread> lanes;
+        for (unsigned tid = 0; tid < unsigned(kLmlThreads); ++tid)
+          lanes.emplace_back([&, tid] {
+            blockDim = {uint32_t(kLmlThreads), 1, 1};
+            blockIdx = {uint32_t(blk), 0, 0};
+            threadIdx = {tid, 0, 0};
+            pdq_host_warp = &warp;
+            if (pass == 0)
+              lml_adj_fwd_kernel<T, NU, F>(aa);
+            else
+              lml_adj_bwd_kernel<T, NU, F>(aa);
+            pdq_host_warp = nullptr;
+          });
+        for (auto& th : lanes) th.join();
+      }
+      continue;
+    }
     for (long long t = 0; t < padded; ++t) {
       blockIdx = {uint32_t(t / kLmlThreads), 0, 0};
       threadIdx = {uint32_t(t % kLmlThreads), 0, 0};
@@ -87,6 +109,7 @@ static int run(FILE* in, long long B, int N, int se, int C, int avg) {
       else
         lml_adj_bwd_kernel<T, NU, F>(aa);
     }
+  }
   for (long long b = 0; b < B; ++b) {
     printf("%d %.17g", status[b], lml[b]);
     for (int q = 0; q < P; ++q) printf(" %.17g", grad[b * P + q]);

@@ -11,6 +11,7 @@
 // Output: one line per sample: status lml grad[P].
 #include <cstdio>
 #include <cstdlib>
+#include <thread>
 #include <vector>
 
 #include "lml_solver.cuh"
@@ -71,10 +72,27 @@ static int run(FILE* in, long long B, int N, int se, int avg) {
   blockDim = {uint32_t(kLmlThreads), 1, 1};
   const long long threads = B * P;
   const long long padded = (threads + kLmlThreads - 1) / kLmlThreads * kLmlThreads;  // the launch's grid
-  for (long long t = 0; t < padded; ++t) {
-    blockIdx = {uint32_t(t / kLmlThreads), 0, 0};
-    threadIdx = {uint32_t(t % kLmlThreads), 0, 0};
-    lml_kernel<double, NU, F>(a);
+  if (getenv("PDQ_HOST_LML_WARPS") != nullptr) {  // each block's 32 lanes as threads
+    for (long long blk = 0; blk < padded / kLmlThreads; ++blk) {
+      PdqHostWarp warp;
+      std::vector<std::thread> lanes;
+      for (unsigned tid = 0; tid < unsigned(kLmlThreads); ++tid)
+        lanes.emplace_back([&, tid] {
+          blockDim = {uint32_t(kLmlThreads), 1, 1};
+          blockIdx = {uint32_t(blk), 0, 0};
+          threadIdx = {tid, 0, 0};
+          pdq_host_warp = &warp;
+          lml_kernel<double, NU, F>(a);
+          pdq_host_warp = nullptr;
+        });
+      for (auto& th : lanes) th.join();
+    }
+  } else {
+    for (long long t = 0; t < padded; ++t) {
+      blockIdx = {uint32_t(t / kLmlThreads), 0, 0};
+      threadIdx = {uint32_t(t % kLmlThreads), 0, 0};
+      lml_kernel<double, NU, F>(a);
+    }
   }
   for (long long b = 0; b < B; ++b) {
     printf("%d %.17g", status[b], lml[b]);

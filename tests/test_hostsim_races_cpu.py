@@ -8,8 +8,8 @@ data race ThreadSanitizer reports (and the harness exits non-zero).  Covered:
 the dense lane-cooperative kernel (fixed-point smoother with MLE
 calibration: the update's R_Y is read from the shared workspace that the
 merge then overwrites), the structure-exploiting dense kernel on four, eight
-and sixteen lanes, and the isotropic split (covariance / mean warp) and
-eight-lane kernels.
+and sixteen lanes, the isotropic split (covariance / mean warp) and
+eight-lane kernels, and the LML kernels' warp-staged step tables.
 """
 
 import os
@@ -83,3 +83,29 @@ def test_thread_sanitizer_is_active(dense_tsan, tmp_path):
     res = subprocess.run([dense_tsan, str(empty)], capture_output=True, text=True, timeout=60,
                          env=dict(os.environ, TSAN_OPTIONS="help=1"))
     assert "ThreadSanitizer" in res.stderr or "tsan" in res.stderr.lower()
+
+
+@pytest.fixture(scope="module")
+def lml_tsan(tmp_path_factory):
+    return hostsim.compile_harness("lml_adjoint_host.cpp", tmp_path_factory.mktemp("tsan") / "lml_adjoint_tsan",
+                                   sanitize="thread")
+
+
+def test_lml_adjoint_kernels_have_no_races(lml_tsan, tmp_path, monkeypatch):
+    """The LML value and adjoint passes with each block's 32 lanes as
+    threads: the warp stages every chunk of step tables into shared memory
+    between two barriers while the lanes read the previous chunk."""
+    from tests import lml_problem
+
+    dt, save_every = 0.01, 10
+    num_steps, data = lml_problem.observations(t1=1.0, dt=dt, save_every=save_every)
+    thetas = lml_problem.theta_samples(3, seed=1)
+    y0s = np.tile(lml_problem.U0, (3, 1))
+    head = [1, 0, 3, 3, num_steps, save_every, 10, 0]
+    body = np.concatenate([np.ravel(thetas), np.ravel(y0s), np.ravel(data), np.full(data.shape[0], lml_problem.STD),
+                           [1.0, 1.0, 1.0], [dt], np.ravel(q1_iwp(3))])
+    path = tmp_path / "input.txt"
+    path.write_text(" ".join(str(int(v)) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    monkeypatch.setenv("PDQ_HOST_LML_WARPS", "1")
+    lines = hostsim.run_harness(lml_tsan, path)
+    assert len(lines) == 3 and all(line.split()[0] == "0" for line in lines)

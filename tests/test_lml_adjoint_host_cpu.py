@@ -139,3 +139,30 @@ def test_host_float32_adjoint_against_oracle(harness, tmp_path):
         assert abs(out[b, 1] - v) <= 1e-3 * abs(v), (out[b, 1], v)
         assert np.abs(out[b, 2:5] - g).max() <= 5e-2 * np.linalg.norm(g), (out[b, 2:5], g)
         assert np.abs(out[b, 5:7] - gy).max() <= 5e-2 * np.linalg.norm(gy), (out[b, 5:7], gy)
+
+
+def test_host_lml_kernels_with_concurrent_lanes(harness, forward_harness, tmp_path, monkeypatch):
+    """Each block's 32 lanes as host threads, so the step tables are staged
+    into shared memory by the whole warp between its barriers (as on the
+    device) instead of by each lane alone: the records equal the one-lane
+    runs bit for bit (the adjoint pair, and the forward-mode kernel with its
+    P tangent lanes per sample)."""
+    dt, save_every = 0.01, 10
+    num_steps, data = lml_problem.observations(t1=2.0, dt=dt, save_every=save_every)
+    thetas = lml_problem.theta_samples(5, seed=2)
+    y0s = np.tile(lml_problem.U0, (5, 1))
+    cot = [1.0, -0.5, 2.0, 0.25, -1.0]
+    monkeypatch.delenv("PDQ_HOST_LML_WARPS", raising=False)
+    one = run(harness, tmp_path, thetas, y0s, data, dt, num_steps, save_every, 14, False, cot)
+    monkeypatch.setenv("PDQ_HOST_LML_WARPS", "1")
+    lanes = run(harness, tmp_path, thetas, y0s, data, dt, num_steps, save_every, 14, False, cot)
+    assert np.array_equal(one, lanes)
+
+    head = [0, 3, 5, num_steps, save_every, 0]
+    body = np.concatenate([thetas.ravel(), y0s.ravel(), np.ravel(data), np.full(data.shape[0], lml_problem.STD), [dt],
+                           np.ravel(q1_iwp(3))])
+    path = tmp_path / "forward.txt"
+    path.write_text(" ".join(str(int(v)) for v in head) + " " + " ".join(repr(float(v)) for v in body))
+    lanes_fwd = hostsim.run_harness(forward_harness, path)
+    monkeypatch.delenv("PDQ_HOST_LML_WARPS")
+    assert hostsim.run_harness(forward_harness, path) == lanes_fwd
